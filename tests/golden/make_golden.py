@@ -1,0 +1,138 @@
+"""Generate the golden fixtures from the compiled reference.
+
+Run from the repository root after ``python oracle/build_ref.py``:
+
+    python tests/golden/make_golden.py
+
+Every array in ``tests/golden/*.npz`` is produced by the reference's own C++
+code (``oracle/_ref/libodref.so``) on small seeded meshes from
+``opendeformer_gb300.meshgen``; the tests compare the oracle restatement and
+the GPU path against them.  Cases:
+
+* ``pattern_*``: pattern arrays and element->value map, including a case with
+  partial-axis constraints (DOF blocks straddling nodes, a degenerate last row
+  block and scalar tail columns since the DOF count is not a multiple of 3);
+* ``elements_<material>``: per-element 78 stiffness + 12 force values,
+  assembled values, f_int and mass at a seeded displacement field;
+* ``be_<material>``: displacements after backward-Euler steps (Jacobi CG);
+* ``nm_<material>``: displacements after Newmark steps (restated integrator on
+  reference components, Jacobi CG);
+* ``kat_math``: polar decomposition, Givens QR and symmetric eigensolve on
+  random and near-singular matrices.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from opendeformer_gb300 import meshgen  # noqa: E402
+from oracle import reforacle as R  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+MATS = {"corotational": (1000.0, 1e5, 0.45, 0.1),
+        "neohookean": (1000.0, 98640.0, 0.4506, 0.1),
+        "stvk": (1000.0, 1e5, 0.40, 0.1)}
+
+
+def small_mesh():
+    return meshgen.tet_grid(4, 2, 2, h=0.05, jitter=0.1, seed=11, tets_per_cube=6)
+
+
+def partial_constraints(g):
+    """x=0 face fully fixed plus single-axis constraints on three more nodes."""
+    cd = list(meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0)))
+    top = g.face_nodes(2, 1)
+    cd += [3 * int(top[3]) + 1, 3 * int(top[6]) + 2, 3 * int(top[7]) + 0, 3 * int(top[7]) + 2]
+    return np.array(sorted(set(cd)), np.int32)
+
+
+def save(name, **arrays):
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **arrays)
+
+
+def main():
+    g = small_mesh()
+    cases = {"full": meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0)),
+             "partial": partial_constraints(g)}
+    for cname, cd in cases.items():
+        s = R.RefScene(g.X, g.tets, g.facets, cd, "corotational", *MATS["corotational"])
+        pcol, rows, oris, emap = s.pattern()
+        save(f"pattern_{cname}", X=g.X, tets=g.tets, facets=g.facets, cdofs=cd, dofs=s.dofs,
+             sizes=s.sizes, pcol=pcol, rows=rows, oris=oris, emap=emap)
+
+    rng = np.random.default_rng(123)
+    u = rng.normal(scale=0.002, size=(g.n_nodes, 3))
+    for mat, (rho, E, nu, thr) in MATS.items():
+        for cname, cd in cases.items():
+            s = R.RefScene(g.X, g.tets, g.facets, cd, mat, rho, E, nu, thr)
+            s.set_displacements(u)
+            K, f = s.element_values()
+            vals, fint = s.assemble()
+            mass = s.mass()
+            x = rng.normal(size=s.dofs)
+            y = s.spmdv(vals, x)
+            A = vals * (1.0 / 3600.0) + mass
+            b = rng.normal(size=s.dofs)
+            xs, its = s.cg(A, b, tol=1e-10, maxit=2000, precond="jacobi")
+            fext = s.loads(body=[0.0, 0.0, -9800.0],
+                           tractions=[([0.0, -500.0, 0.0], g.face_facets(0, 1))])
+            save(f"elements_{mat}_{cname}", u=u, K78=K, f12=f, values=vals, fint=fint,
+                 mass=mass, spmv_x=x, spmv_y=y, cg_b=b, cg_x=xs, cg_iters=its, fext=fext,
+                 material=np.array([rho, E, nu, thr]))
+
+    for mat, (rho, E, nu, thr) in MATS.items():
+        cd = cases["full"]
+        s = R.RefScene(g.X, g.tets, g.facets, cd, mat, rho, E, nu, thr)
+        s.be_setup(1.0 / 60.0, 0.01, 0.001, tol=1e-10, maxit=2000, precond="jacobi")
+        fext = s.loads(body=[0.0, 0.0, -9800.0])
+        s.be_apply_loads()
+        iters = s.be_step(20)
+        save(f"be_{mat}", fext=fext, u=s.displacements(), v=s.be_velocity(), steps=20, iters=iters,
+             params=np.array([1.0 / 60.0, 0.01, 0.001, 1e-10]))
+        s = R.RefScene(g.X, g.tets, g.facets, cd, mat, rho, E, nu, thr)
+        s.nm_setup(1.0 / 60.0, 0.01, 0.001, beta=0.25, gamma=0.5, newton=2, tol=1e-10, maxit=2000,
+                   precond="jacobi")
+        fext = s.loads(body=[0.0, 0.0, -9800.0])
+        s.nm_apply_loads()
+        iters = s.nm_step(10)
+        d, v, a = s.nm_state()
+        save(f"nm_{mat}", fext=fext, u=s.displacements(), d=d, v=v, a=a, steps=10, iters=iters,
+             params=np.array([1.0 / 60.0, 0.01, 0.001, 0.25, 0.5, 2, 1e-10]))
+
+    # math known-answer vectors
+    rng = np.random.default_rng(7)
+    Fs = []
+    for k in range(400):
+        F = rng.normal(size=(3, 3)) * 10 ** rng.uniform(-2, 1)
+        if k % 4 == 1:
+            F = np.eye(3) + 1e-9 * rng.normal(size=(3, 3))
+        if k % 4 == 2:
+            F[:, 2] = 0.5 * F[:, 0] + 0.25 * F[:, 1] + 1e-12 * rng.normal(size=3)
+        if k % 8 == 3:
+            F = -F  # reflected
+        Fs.append(F)
+    Fs = np.array(Fs)
+    polR = np.array([R.polar(F)[0] for F in Fs])
+    polS = np.array([R.polar(F)[1] for F in Fs])
+    qrQ = np.array([R.qr(F)[0] for F in Fs])
+    qrR = np.array([R.qr(F)[1] for F in Fs])
+    tri = []
+    for F in Fs:
+        S = F @ F.T
+        tri.append([S[0, 0], S[0, 1], S[0, 2], S[1, 1], S[1, 2], S[2, 2]])
+    tri = np.array(tri)
+    ev = np.array([R.eigsym(t)[0] for t in tri])
+    evec = np.array([R.eigsym(t)[1] for t in tri])
+    save("kat_math", F=Fs, polar_R=polR, polar_S=polS, qr_Q=qrQ, qr_R=qrR, tri=tri, eig_vals=ev,
+         eig_vecs=evec)
+    print("golden fixtures written to", OUT)
+
+
+if __name__ == "__main__":
+    main()
