@@ -1,0 +1,219 @@
+/*
+ * od_gb300.h -- C ABI of the GB300-native implicit FEM time step.
+ *
+ * Plain C types only (no CUDA or torch types).  Host pointers in, device-
+ * resident state inside.  Every call returns an od_status; od_last_error()
+ * gives a message for the calling thread.  One context per host thread;
+ * scenes are not shared across threads without external locking (the
+ * reference is single-threaded and not re-entrant either).
+ *
+ * Reference interfaces replaced (paths inside OpenDeformer/):
+ *   FullOrderNonlinearMaterial<SpMatrix>   material/fullOrderNonlinear.h:36-44
+ *   MechMaterial::generateMassMatrix       core/mechMaterial.h:31-32
+ *   BlockedSymSparseMatrix + SpMDV         core/sparseMatrix.h:183-274, core/numerMethod.h:134-262
+ *   LinearSolver / CGSolver                core/linearSolver.h:12-20, solver/cgSolver.h:16-17
+ *   Preconditioner (+ Jacobi, IC)          core/preconditioner.h:12-22
+ *   Forcer                                 core/forcer.h:13-22
+ *   Intergrator / NonlinearImplicitBackwardEuler
+ *                                          core/intergrator.h:13-35,
+ *                                          intergrator/nonlinearImplicitBackwardEuler.h:48-128
+ *   Simulator::runTimeSteps / getVertexPositions  core/simulator.h:21-22
+ */
+#ifndef OD_GB300_H
+#define OD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OD_ABI_VERSION 1
+
+typedef enum od_status {
+  OD_OK = 0,
+  OD_ERR_INVALID_ARG = 1,
+  OD_ERR_OUT_OF_MEMORY = 2,
+  OD_ERR_NOT_CONVERGED = 3, /* PCG hit max_iter (the reference exits silently) */
+  OD_ERR_NAN = 4,           /* non-finite residual or state */
+  OD_ERR_DEVICE_TIMEOUT = 5,/* a bounded device wait ran out */
+  OD_ERR_CUDA = 6,
+  OD_ERR_UNSUPPORTED = 7,
+  OD_ERR_INTERNAL = 8
+} od_status;
+
+typedef enum od_material_kind {
+  OD_MATERIAL_COROTATIONAL = 0, /* material/corotationalHyperelastic.h:11-21 */
+  OD_MATERIAL_NEOHOOKEAN = 1,   /* material/invertibleNeoHookean.h */
+  OD_MATERIAL_STVK = 2          /* material/invertibleStVK.h */
+} od_material_kind;
+
+typedef enum od_precond_kind {
+  OD_PRECOND_NONE = 0,         /* Preconditioner (identity), core/preconditioner.h:14-16 */
+  OD_PRECOND_JACOBI = 1,       /* solver/jacobiPreconditioner.cpp:12-26 */
+  OD_PRECOND_BLOCK_JACOBI = 2, /* 3x3 diagonal blocks (no reference counterpart) */
+  OD_PRECOND_IC0 = 3           /* shifted IC(0), level-scheduled (no reference counterpart;
+                                  the reference's fill-in IC is inCholeskyPreconditioner.cpp) */
+} od_precond_kind;
+
+typedef enum od_precision {
+  OD_PRECISION_FP64 = 0,  /* plain FP64 everywhere */
+  OD_PRECISION_MIXED = 1  /* FP32 matrix/SpMV/preconditioner apply; FP64 dots, residual
+                             replacement and outer iterative refinement */
+} od_precision;
+
+typedef enum od_integrator_kind {
+  OD_INTEGRATOR_BACKWARD_EULER = 0, /* nonlinearImplicitBackwardEuler.h:82-116 */
+  OD_INTEGRATOR_NEWMARK = 1         /* full-order Newmark + Newton (formulas of
+                                       intergrator/linearNewmark.cpp:27-30,57-79) */
+} od_integrator_kind;
+
+typedef struct od_material {
+  int kind;          /* od_material_kind */
+  double density;    /* rho, kg/m^3 */
+  double youngs;     /* E, Pa */
+  double poisson;    /* nu */
+  double threshold;  /* corotational compressing threshold / invertible inversion threshold */
+} od_material;
+
+typedef struct od_solver_params {
+  double tol;         /* stop when ||r||^2 <= tol^2 ||b||^2 (cgSolver.cpp:42-46) */
+  int max_iter;
+  int precond;        /* od_precond_kind */
+  int precision;      /* od_precision */
+  int replace_every;  /* mixed: true-residual recompute period (0 = 25) */
+  double inner_tol;   /* mixed: inner FP32 solve tolerance (0 = 1e-4) */
+  int max_refine;     /* mixed: max outer refinement sweeps (0 = 20) */
+} od_solver_params;
+
+typedef struct od_solve_stats {
+  int iterations;       /* total inner iterations */
+  int refinements;      /* mixed: outer sweeps */
+  double rel_residual;  /* ||b - A x|| / ||b|| at exit (FP64) */
+  double ic_shift;      /* IC(0) diagonal shift used */
+  int status;           /* od_status of the solve */
+} od_solve_stats;
+
+typedef struct od_integrator_params {
+  int kind;              /* od_integrator_kind */
+  double dt;             /* time step h */
+  double alpha_m;        /* Rayleigh mass damping */
+  double beta_k;         /* Rayleigh stiffness damping */
+  double nm_beta;        /* Newmark beta (0.25) */
+  double nm_gamma;       /* Newmark gamma (0.5) */
+  int newton_iters;      /* Newmark Newton iterations per step (>= 1) */
+  od_solver_params solver;
+} od_integrator_params;
+
+typedef struct od_step_stats {
+  int steps;
+  int pcg_iterations;    /* summed over solves */
+  int solves;
+  double max_rel_residual;
+  int status;
+} od_step_stats;
+
+typedef struct od_scene_info {
+  int n_nodes, n_tets, n_facets;
+  int dofs;                  /* compacted DOF count (NodeIndexer::getMatrixOrder) */
+  int num_block_columns;     /* reference numBlockColumn */
+  int num_remained_columns;  /* reference numRemainedColumn */
+  int num_row_indices;       /* reference blockPcol[last] */
+  int num_values;            /* reference blockColumnOris[last] */
+  int num_full_blocks;       /* device full-BSR block count (both triangles) */
+  int num_colors;            /* element colours used by the atomic-free scatter */
+  long long device_bytes;    /* device memory held by the scene */
+} od_scene_info;
+
+typedef struct od_ctx od_ctx;
+typedef struct od_scene od_scene;
+
+const char* od_status_string(od_status s);
+const char* od_last_error(void);
+int od_abi_version(void);
+
+/* Context: one CUDA device and stream.  Replaces nothing in the reference
+ * (it has no device); owns the stream every call of its scenes runs on. */
+od_status od_ctx_create(int device, od_ctx** out);
+od_status od_ctx_destroy(od_ctx* ctx);
+od_status od_ctx_synchronize(od_ctx* ctx);
+
+/* Scene = TetMesh + Constrainer/NodeIndexer + material + pattern + caches.
+ * Replaces TetMesh(numN, numE, numS) + setVertex/setElement/setFacet
+ * (mesh/tetmesh.h:12, core/mesh.cpp:7-40), NodeIndexer(constrainer)
+ * (core/nodeIndexer.cpp:8-10), material ctor + getPrecomputes +
+ * getMatrixStructure + getMatrixIndicesPerElement + generateMassMatrix
+ * (material/fullOrderNonlinear.h:36-110, core/mechMaterial.cpp:69-98).
+ *   X: n_nodes*3 rest positions; tets: n_tets*4; facets: n_facets*3;
+ *   cdofs: sorted constrained DOFs 3*node+axis (Constrainer output). */
+od_status od_scene_create(od_ctx* ctx, int n_nodes, const double* X, int n_tets, const int* tets,
+                          int n_facets, const int* facets, int n_cdofs, const int* cdofs,
+                          const od_material* material, od_scene** out);
+od_status od_scene_destroy(od_scene* scene);
+od_status od_scene_get_info(od_scene* scene, od_scene_info* info);
+
+/* Pattern export, bit-identical to BlockedSymSparseMatrix's blockPcol /
+ * blockRows / blockColumnOris (core/sparseMatrix.h:186-274) and to the
+ * element->value map of getMatrixIndicesPerElement (fullOrderNonlinear.h:73-110,
+ * 78 ints per tet, -1 for constrained).  Any output may be NULL. */
+od_status od_scene_pattern(od_scene* scene, int* block_pcol, int* block_rows,
+                           int* block_column_oris, int* elem_map);
+
+/* Mesh displacement (Mesh::getVertexDisplacement, core/mesh.h:38-39), n_nodes*3.
+ * Constrained DOFs keep what is written here (prescribed displacements). */
+od_status od_scene_set_displacements(od_scene* scene, const double* u);
+od_status od_scene_get_displacements(od_scene* scene, double* u);
+/* Simulator::getVertexPositions (core/simulator.cpp:24-33): X + u as float. */
+od_status od_scene_get_positions(od_scene* scene, float* xyz);
+
+/* FullOrderNonlinearMaterial::generateMatrixAndVirtualWorks
+ * (corotationalHyperelastic.cpp:43-102, invertibleHyperelastic.cpp:34-114):
+ * tangent values in the reference value layout and internal forces (dofs),
+ * at the current mesh displacement.  Outputs may be NULL (device only). */
+od_status od_scene_evaluate(od_scene* scene, double* values, double* f_int);
+/* Per-element 78 packed stiffness values and 12 nodal forces (element order). */
+od_status od_scene_element_values(od_scene* scene, double* k78, double* f12);
+/* MechMaterial::generateMassMatrix values (mechMaterial.cpp:69-98). */
+od_status od_scene_mass(od_scene* scene, double* values);
+
+/* SpMDV (numerMethod.h:134-262): y += A x, A given by reference-layout values. */
+od_status od_scene_spmdv(od_scene* scene, const double* values, const double* x, double* y);
+/* CGSolver::solveLinearSystem (cgSolver.cpp:13-57) on A (reference-layout
+ * values); x is the warm start and the result. */
+od_status od_scene_pcg(od_scene* scene, const double* values, const double* b, double* x,
+                       const od_solver_params* params, od_solve_stats* stats);
+
+/* Forcer + Intergrator::setExternalVirtualWork (core/forcer.cpp:8-96,
+ * nonlinearImplicitBackwardEuler.h:118-120): body force density (N/m^3, may be
+ * NULL) then n_groups uniform tractions (Pa) over facet lists, evaluated on
+ * the device at the current displacement (deformed facet areas).  Loads stay
+ * frozen until the next call. */
+od_status od_scene_set_loads(od_scene* scene, const double* body, int n_groups,
+                             const double* tractions, const int* group_sizes,
+                             const int* facet_ids);
+od_status od_scene_set_external_forces(od_scene* scene, const double* f_ext);
+od_status od_scene_get_external_forces(od_scene* scene, double* f_ext);
+
+/* Integrator (NonlinearImplicitBackwardEuler ctor, nonlinearImplicitBackwardEuler.h:48-73,
+ * or the full-order Newmark).  Resets the state to rest. */
+od_status od_integrator_setup(od_scene* scene, const od_integrator_params* params);
+/* Simulator::runTimeSteps (simulator.cpp:35-38): n steps, each followed by the
+ * mesh displacement update (updateMeshVerticesDisplacements,
+ * nonlinearImplicitBackwardEuler.h:103-116). */
+od_status od_step(od_scene* scene, int n_steps, od_step_stats* stats);
+/* State vectors over the compacted DOFs (any may be NULL).  Backward Euler
+ * has v only (d and a are reported as zero). */
+od_status od_get_state(od_scene* scene, double* d, double* v, double* a);
+od_status od_set_state(od_scene* scene, const double* d, const double* v, const double* a);
+
+/* Checkpoint / resume: mesh displacement + integrator vectors as a host blob.
+ * Call with buf == NULL to query the size. */
+od_status od_scene_save(od_scene* scene, void* buf, size_t* size);
+od_status od_scene_load(od_scene* scene, const void* buf, size_t size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OD_GB300_H */

@@ -1,0 +1,431 @@
+"""Python host side of the GB300 implicit FEM step, over the C ABI.
+
+Mirrors the reference's plugin seams so that code written against the
+reference reads the same:
+
+* materials: ``CorotationalHyperelasticMaterial(rho, youngs, poisson,
+  threshold)`` (material/corotationalHyperelastic.h:13),
+  ``InvertibleNeoHookeanMaterial`` / ``InvertibleStVKMaterial(rho, youngs,
+  poisson, inversionThreshold)`` (material/invertibleNeoHookean.h,
+  material/invertibleStVK.h);
+* preconditioners / solver: ``JacobiPreconditioner()``,
+  ``BlockJacobiPreconditioner()``, ``IC0Preconditioner()`` and
+  ``CGSolver(tol, maxIter, preconditioner)`` (solver/cgSolver.h:16-17);
+* integrators: ``NonlinearImplicitBackwardEuler(massDamp, stiffDamp, ts,
+  solver)`` (intergrator/nonlinearImplicitBackwardEuler.h:48-73) and
+  ``NewmarkIntegrator(beta, gamma, massDamp, stiffDamp, ts, solver,
+  newton_iters)``;
+* ``Simulator(scene, integrator)`` with ``runTimeSteps`` /
+  ``getVertexPositions`` (core/simulator.h:12-28).
+
+Everything computes on the GPU through ``libodgpu.so``; there is no CPU
+fallback: if the library is missing, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libodgpu.so")
+
+OD_OK = 0
+STATUS = {0: "OD_OK", 1: "OD_ERR_INVALID_ARG", 2: "OD_ERR_OUT_OF_MEMORY", 3: "OD_ERR_NOT_CONVERGED",
+          4: "OD_ERR_NAN", 5: "OD_ERR_DEVICE_TIMEOUT", 6: "OD_ERR_CUDA", 7: "OD_ERR_UNSUPPORTED",
+          8: "OD_ERR_INTERNAL"}
+
+MATERIAL_KIND = {"corotational": 0, "neohookean": 1, "stvk": 2}
+PRECOND_KIND = {"none": 0, "jacobi": 1, "block_jacobi": 2, "ic0": 3}
+PRECISION = {"fp64": 0, "mixed": 1}
+
+
+class ODError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class od_material(C.Structure):
+    _fields_ = [("kind", C.c_int), ("density", C.c_double), ("youngs", C.c_double),
+                ("poisson", C.c_double), ("threshold", C.c_double)]
+
+
+class od_solver_params(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("precond", C.c_int), ("precision", C.c_int),
+                ("replace_every", C.c_int), ("inner_tol", C.c_double), ("max_refine", C.c_int)]
+
+
+class od_solve_stats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("refinements", C.c_int), ("rel_residual", C.c_double),
+                ("ic_shift", C.c_double), ("status", C.c_int)]
+
+
+class od_integrator_params(C.Structure):
+    _fields_ = [("kind", C.c_int), ("dt", C.c_double), ("alpha_m", C.c_double), ("beta_k", C.c_double),
+                ("nm_beta", C.c_double), ("nm_gamma", C.c_double), ("newton_iters", C.c_int),
+                ("solver", od_solver_params)]
+
+
+class od_step_stats(C.Structure):
+    _fields_ = [("steps", C.c_int), ("pcg_iterations", C.c_int), ("solves", C.c_int),
+                ("max_rel_residual", C.c_double), ("status", C.c_int)]
+
+
+class od_scene_info(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("n_tets", C.c_int), ("n_facets", C.c_int), ("dofs", C.c_int),
+                ("num_block_columns", C.c_int), ("num_remained_columns", C.c_int),
+                ("num_row_indices", C.c_int), ("num_values", C.c_int), ("num_full_blocks", C.c_int),
+                ("num_colors", C.c_int), ("device_bytes", C.c_longlong)]
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+_lib = None
+
+# name -> (restype, argtypes); every entry point of include/od_gb300.h
+SIGNATURES = {
+    "od_status_string": (C.c_char_p, [C.c_int]),
+    "od_last_error": (C.c_char_p, []),
+    "od_abi_version": (C.c_int, []),
+    "od_ctx_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),
+    "od_ctx_destroy": (C.c_int, [_vp]),
+    "od_ctx_synchronize": (C.c_int, [_vp]),
+    "od_scene_create": (C.c_int, [_vp, C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip,
+                                  C.POINTER(od_material), C.POINTER(_vp)]),
+    "od_scene_destroy": (C.c_int, [_vp]),
+    "od_scene_get_info": (C.c_int, [_vp, C.POINTER(od_scene_info)]),
+    "od_scene_pattern": (C.c_int, [_vp, _ip, _ip, _ip, _ip]),
+    "od_scene_set_displacements": (C.c_int, [_vp, _dp]),
+    "od_scene_get_displacements": (C.c_int, [_vp, _dp]),
+    "od_scene_get_positions": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "od_scene_evaluate": (C.c_int, [_vp, _dp, _dp]),
+    "od_scene_element_values": (C.c_int, [_vp, _dp, _dp]),
+    "od_scene_mass": (C.c_int, [_vp, _dp]),
+    "od_scene_spmdv": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "od_scene_pcg": (C.c_int, [_vp, _dp, _dp, _dp, C.POINTER(od_solver_params), C.POINTER(od_solve_stats)]),
+    "od_scene_set_loads": (C.c_int, [_vp, _dp, C.c_int, _dp, _ip, _ip]),
+    "od_scene_set_external_forces": (C.c_int, [_vp, _dp]),
+    "od_scene_get_external_forces": (C.c_int, [_vp, _dp]),
+    "od_integrator_setup": (C.c_int, [_vp, C.POINTER(od_integrator_params)]),
+    "od_step": (C.c_int, [_vp, C.c_int, C.POINTER(od_step_stats)]),
+    "od_get_state": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "od_set_state": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "od_scene_save": (C.c_int, [_vp, _vp, C.POINTER(C.c_size_t)]),
+    "od_scene_load": (C.c_int, [_vp, _vp, C.c_size_t]),
+}
+
+
+def load_library(path: str | None = None):
+    """Load libodgpu.so (raises if it was not built: there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"GB300 library not built: {path} (run opendeformer_gb300/build.py)")
+    L = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(status, what=""):
+    if status != OD_OK:
+        msg = load_library().od_last_error().decode(errors="replace")
+        raise ODError(status, f"{what}: {msg}")
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+# ----------------------------------------------------------------- values
+@dataclasses.dataclass
+class Material:
+    kind: str
+    density: float
+    youngs: float
+    poisson: float
+    threshold: float
+
+    def to_c(self):
+        return od_material(MATERIAL_KIND[self.kind], self.density, self.youngs, self.poisson, self.threshold)
+
+
+def CorotationalHyperelasticMaterial(rho, youngs, poisson, compressingThreshold):
+    return Material("corotational", rho, youngs, poisson, compressingThreshold)
+
+
+def InvertibleNeoHookeanMaterial(rho, youngs, poisson, inversionThreshold):
+    return Material("neohookean", rho, youngs, poisson, inversionThreshold)
+
+
+def InvertibleStVKMaterial(rho, youngs, poisson, inversionThreshold):
+    return Material("stvk", rho, youngs, poisson, inversionThreshold)
+
+
+@dataclasses.dataclass
+class Preconditioner:
+    kind: str = "none"
+
+
+def JacobiPreconditioner():
+    return Preconditioner("jacobi")
+
+
+def BlockJacobiPreconditioner():
+    return Preconditioner("block_jacobi")
+
+
+def IC0Preconditioner():
+    return Preconditioner("ic0")
+
+
+@dataclasses.dataclass
+class CGSolver:
+    tol: float = 1e-8
+    maxIter: int = 1000
+    preconditioner: Preconditioner = dataclasses.field(default_factory=Preconditioner)
+    precision: str = "fp64"
+    replace_every: int = 0
+    inner_tol: float = 0.0
+    max_refine: int = 0
+
+    def to_c(self):
+        return od_solver_params(self.tol, self.maxIter, PRECOND_KIND[self.preconditioner.kind],
+                                PRECISION[self.precision], self.replace_every, self.inner_tol,
+                                self.max_refine)
+
+
+@dataclasses.dataclass
+class NonlinearImplicitBackwardEuler:
+    massDamp: float
+    stiffDamp: float
+    ts: float
+    solver: CGSolver
+
+    def to_c(self):
+        return od_integrator_params(0, self.ts, self.massDamp, self.stiffDamp, 0.25, 0.5, 1, self.solver.to_c())
+
+
+@dataclasses.dataclass
+class NewmarkIntegrator:
+    beta: float
+    gamma: float
+    massDamp: float
+    stiffDamp: float
+    ts: float
+    solver: CGSolver
+    newton_iters: int = 1
+
+    def to_c(self):
+        return od_integrator_params(1, self.ts, self.massDamp, self.stiffDamp, self.beta, self.gamma,
+                                    self.newton_iters, self.solver.to_c())
+
+
+# ----------------------------------------------------------------- handles
+class Context:
+    """One CUDA device and stream (od_ctx)."""
+
+    def __init__(self, device: int = 0):
+        L = load_library()
+        h = _vp()
+        _check(L.od_ctx_create(device, C.byref(h)), "od_ctx_create")
+        self.h = h
+
+    def synchronize(self):
+        _check(load_library().od_ctx_synchronize(self.h), "od_ctx_synchronize")
+
+    def close(self):
+        if getattr(self, "h", None):
+            load_library().od_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Scene:
+    """Mesh + constraints + material on the device (od_scene)."""
+
+    def __init__(self, ctx: Context, X, tets, facets, cdofs, material: Material):
+        L = load_library()
+        self.ctx = ctx
+        self.X = np.ascontiguousarray(X, dtype=np.float64).reshape(-1, 3)
+        self.tets = np.ascontiguousarray(tets, dtype=np.int32).reshape(-1, 4)
+        self.facets = np.ascontiguousarray(facets, dtype=np.int32).reshape(-1, 3)
+        self.cdofs = np.ascontiguousarray(np.unique(np.asarray(cdofs, dtype=np.int64)), dtype=np.int32)
+        self.material = material
+        h = _vp()
+        m = material.to_c()
+        _check(L.od_scene_create(ctx.h, self.X.shape[0], _d(self.X), self.tets.shape[0], _i(self.tets),
+                                 self.facets.shape[0], _i(self.facets), self.cdofs.size, _i(self.cdofs),
+                                 C.byref(m), C.byref(h)), "od_scene_create")
+        self.h = h
+        self.info = od_scene_info()
+        _check(L.od_scene_get_info(self.h, C.byref(self.info)), "od_scene_get_info")
+        self.dofs = self.info.dofs
+        self.n_nodes = self.info.n_nodes
+        self.n_tets = self.info.n_tets
+
+    def close(self):
+        if getattr(self, "h", None):
+            load_library().od_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def n_values(self) -> int:
+        return self.info.num_values
+
+    def pattern(self):
+        i = self.info
+        nc = i.num_block_columns + i.num_remained_columns
+        pcol = np.zeros(nc + 1, np.int32)
+        rows = np.zeros(i.num_row_indices, np.int32)
+        oris = np.zeros(nc + 1, np.int32)
+        emap = np.zeros((self.n_tets, 78), np.int32)
+        _check(load_library().od_scene_pattern(self.h, _i(pcol), _i(rows), _i(oris), _i(emap)), "pattern")
+        return pcol, rows, oris, emap
+
+    def set_displacements(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1, 3)
+        _check(load_library().od_scene_set_displacements(self.h, _d(u)), "set_displacements")
+
+    def displacements(self):
+        u = np.zeros((self.n_nodes, 3))
+        _check(load_library().od_scene_get_displacements(self.h, _d(u)), "get_displacements")
+        return u
+
+    def getVertexPositions(self):
+        xyz = np.zeros((self.n_nodes, 3), np.float32)
+        _check(load_library().od_scene_get_positions(self.h, xyz.ctypes.data_as(C.POINTER(C.c_float))),
+               "get_positions")
+        return xyz
+
+    def evaluate(self):
+        """generateMatrixAndVirtualWorks: (tangent values, internal forces)."""
+        v = np.zeros(self.n_values)
+        f = np.zeros(self.dofs)
+        _check(load_library().od_scene_evaluate(self.h, _d(v), _d(f)), "evaluate")
+        return v, f
+
+    def element_values(self):
+        K = np.zeros((self.n_tets, 78))
+        f = np.zeros((self.n_tets, 12))
+        _check(load_library().od_scene_element_values(self.h, _d(K), _d(f)), "element_values")
+        return K, f
+
+    def mass(self):
+        v = np.zeros(self.n_values)
+        _check(load_library().od_scene_mass(self.h, _d(v)), "mass")
+        return v
+
+    def spmdv(self, values, x, y=None):
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(self.dofs) if y is None else np.array(y, dtype=np.float64)
+        _check(load_library().od_scene_spmdv(self.h, _d(values), _d(x), _d(y)), "spmdv")
+        return y
+
+    def pcg(self, values, b, x0=None, solver: CGSolver | None = None):
+        solver = solver or CGSolver()
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(self.dofs) if x0 is None else np.array(x0, dtype=np.float64)
+        p = solver.to_c()
+        st = od_solve_stats()
+        _check(load_library().od_scene_pcg(self.h, _d(values), _d(b), _d(x), C.byref(p), C.byref(st)), "pcg")
+        return x, st
+
+    def set_loads(self, body=None, tractions=()):
+        """Forcer: body force density (N/m^3) then (traction Pa, facet ids) groups."""
+        ng = len(tractions)
+        tv = np.zeros((max(ng, 1), 3))
+        sizes = np.zeros(max(ng, 1), np.int32)
+        ids = [np.zeros(0, np.int32)]
+        for k, (t, fac) in enumerate(tractions):
+            tv[k] = t
+            fac = np.asarray(fac, dtype=np.int32)
+            sizes[k] = fac.size
+            ids.append(fac)
+        ids = np.ascontiguousarray(np.concatenate(ids), dtype=np.int32)
+        if ids.size == 0:
+            ids = np.zeros(1, np.int32)
+        b = None if body is None else np.ascontiguousarray(body, dtype=np.float64)
+        _check(load_library().od_scene_set_loads(self.h, None if b is None else _d(b), ng, _d(tv), _i(sizes),
+                                                 _i(ids)), "set_loads")
+
+    def set_external_forces(self, f):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        _check(load_library().od_scene_set_external_forces(self.h, _d(f)), "set_external_forces")
+
+    def external_forces(self):
+        f = np.zeros(self.dofs)
+        _check(load_library().od_scene_get_external_forces(self.h, _d(f)), "get_external_forces")
+        return f
+
+    def setup_integrator(self, integrator):
+        p = integrator.to_c()
+        _check(load_library().od_integrator_setup(self.h, C.byref(p)), "integrator_setup")
+
+    def step(self, n: int = 1):
+        st = od_step_stats()
+        _check(load_library().od_step(self.h, n, C.byref(st)), "step")
+        return st
+
+    def state(self):
+        d, v, a = np.zeros(self.dofs), np.zeros(self.dofs), np.zeros(self.dofs)
+        _check(load_library().od_get_state(self.h, _d(d), _d(v), _d(a)), "get_state")
+        return d, v, a
+
+    def set_state(self, d=None, v=None, a=None):
+        args = [None if x is None else _d(np.ascontiguousarray(x, dtype=np.float64)) for x in (d, v, a)]
+        keep = [np.ascontiguousarray(x, dtype=np.float64) if x is not None else None for x in (d, v, a)]
+        args = [None if k is None else _d(k) for k in keep]
+        _check(load_library().od_set_state(self.h, *args), "set_state")
+
+    def save(self) -> bytes:
+        L = load_library()
+        n = C.c_size_t(0)
+        _check(L.od_scene_save(self.h, None, C.byref(n)), "save")
+        buf = (C.c_char * n.value)()
+        _check(L.od_scene_save(self.h, C.cast(buf, _vp), C.byref(n)), "save")
+        return bytes(buf)
+
+    def load(self, blob: bytes):
+        buf = C.create_string_buffer(blob, len(blob))
+        _check(load_library().od_scene_load(self.h, C.cast(buf, _vp), len(blob)), "load")
+
+
+class Simulator:
+    """Simulator(mesh, indexer, integrator) (core/simulator.h:15-16)."""
+
+    def __init__(self, scene: Scene, integrator):
+        self.scene = scene
+        scene.setup_integrator(integrator)
+
+    def runTimeSteps(self, stepCount: int):
+        return self.scene.step(stepCount)
+
+    def getVertexPositions(self):
+        return self.scene.getVertexPositions()

@@ -1,0 +1,548 @@
+// Per-tetrahedron kernels: precomputes, mass, loads and the material
+// kernels (corotational linear, invertible Neo-Hookean / StVK) producing the
+// 78 packed stiffness values and 12 nodal forces of every element, scattered
+// without atomics: elements are coloured so that one launch (one colour)
+// never touches a matrix value or force entry twice.
+//
+// One thread per element; element data is structure-of-arrays in colour
+// order (pre[k * ne + e], emap[k * ne + e]) so every per-element load and the
+// map loads are coalesced.
+#include "od_internal.h"
+#include "od_math.cuh"
+
+namespace od {
+
+// packed position of (i, i) in the 78-entry upper triangle of the 12x12
+// element matrix (tetelement.cpp:284)
+__constant__ int c_diag12[12] = {0, 12, 23, 33, 42, 50, 57, 63, 68, 72, 75, 77};
+
+__device__ __forceinline__ V3t<double> ld3(const double* p, int n) {
+  return {p[3 * n], p[3 * n + 1], p[3 * n + 2]};
+}
+
+__device__ __forceinline__ double tet_vol(V3t<double> a, V3t<double> b, V3t<double> c, V3t<double> d) {
+  V3t<double> ab = v_sub(b, a), ac = v_sub(c, a), ad = v_sub(d, a);
+  return fabs(v_dot(ab, v_cross(ac, ad))) / 6.0;
+}
+
+// ------------------------------------------------------------ precomputes
+// getCorotationalTetElementPrecomputes (tetelement.cpp:501-544) and
+// InvertibleHyperelasticTetElement::getPrecomputes (tetelement.cpp:253-266),
+// written in element (colour) order.
+__global__ void precompute_kernel(int ne, int kind, const int4* __restrict__ tets,
+                                  const double* __restrict__ X, double D0, double D1, double D2,
+                                  double* __restrict__ pre) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  int4 t = tets[e];
+  V3t<double> p0 = ld3(X, t.x), p1 = ld3(X, t.y), p2 = ld3(X, t.z), p3 = ld3(X, t.w);
+  // shape-function gradients scaled by 6V (tetelement.cpp:18-48)
+  V3t<double> da = v_sub(p0, p3), db = v_sub(p1, p3), dc = v_sub(p2, p3), ca = v_sub(p0, p2), cb = v_sub(p1, p2);
+  V3t<double> g[4];
+  if (v_dot(da, v_cross(db, dc)) > 0.0) {
+    g[0] = v_cross(db, dc); g[1] = v_cross(dc, da); g[2] = v_cross(da, db); g[3] = v_cross(cb, ca);
+  } else {
+    g[0] = v_cross(dc, db); g[1] = v_cross(da, dc); g[2] = v_cross(db, da); g[3] = v_cross(ca, cb);
+  }
+  double vol = tet_vol(p0, p1, p2, p3);
+  V3t<double> ab = v_sub(p1, p0), ac = v_sub(p2, p0), ad = v_sub(p3, p0);
+  double Dm[9] = {ab.x, ac.x, ad.x, ab.y, ac.y, ad.y, ab.z, ac.z, ad.z}, Di[9];
+  double inv = 1.0 / det3(Dm);
+  Di[0] = (Dm[4] * Dm[8] - Dm[5] * Dm[7]) * inv;
+  Di[1] = (Dm[2] * Dm[7] - Dm[1] * Dm[8]) * inv;
+  Di[2] = (Dm[1] * Dm[5] - Dm[2] * Dm[4]) * inv;
+  Di[3] = (Dm[5] * Dm[6] - Dm[3] * Dm[8]) * inv;
+  Di[4] = (Dm[0] * Dm[8] - Dm[2] * Dm[6]) * inv;
+  Di[5] = (Dm[2] * Dm[3] - Dm[0] * Dm[5]) * inv;
+  Di[6] = (Dm[3] * Dm[7] - Dm[4] * Dm[6]) * inv;
+  Di[7] = (Dm[1] * Dm[6] - Dm[0] * Dm[7]) * inv;
+  Di[8] = (Dm[0] * Dm[4] - Dm[1] * Dm[3]) * inv;
+  if (kind == OD_MATERIAL_COROTATIONAL) {
+    const double f = 1.0 / (36.0 * vol);
+    int k = 0;
+    for (int a = 0; a < 4; a++) {
+      const double Ba[3] = {g[a].x, g[a].y, g[a].z};
+      for (int b = a; b < 4; b++) {
+        const double Bb[3] = {g[b].x, g[b].y, g[b].z};
+        pre[(size_t)(k + 0) * ne + e] = (D0 * Ba[0] * Bb[0] + D2 * (Ba[1] * Bb[1] + Ba[2] * Bb[2])) * f;
+        pre[(size_t)(k + 1) * ne + e] = (D1 * Ba[0] * Bb[1] + D2 * Ba[1] * Bb[0]) * f;
+        pre[(size_t)(k + 2) * ne + e] = (D1 * Ba[0] * Bb[2] + D2 * Ba[2] * Bb[0]) * f;
+        pre[(size_t)(k + 3) * ne + e] = (D1 * Ba[1] * Bb[0] + D2 * Ba[0] * Bb[1]) * f;
+        pre[(size_t)(k + 4) * ne + e] = (D0 * Ba[1] * Bb[1] + D2 * (Ba[0] * Bb[0] + Ba[2] * Bb[2])) * f;
+        pre[(size_t)(k + 5) * ne + e] = (D1 * Ba[1] * Bb[2] + D2 * Ba[2] * Bb[1]) * f;
+        pre[(size_t)(k + 6) * ne + e] = (D1 * Ba[2] * Bb[0] + D2 * Ba[0] * Bb[2]) * f;
+        pre[(size_t)(k + 7) * ne + e] = (D1 * Ba[2] * Bb[1] + D2 * Ba[1] * Bb[2]) * f;
+        pre[(size_t)(k + 8) * ne + e] = (D0 * Ba[2] * Bb[2] + D2 * (Ba[0] * Bb[0] + Ba[1] * Bb[1])) * f;
+        k += 9;
+      }
+    }
+    for (int i = 0; i < 9; i++) pre[(size_t)(90 + i) * ne + e] = Di[i];
+    pre[(size_t)99 * ne + e] = vol;
+  } else {
+    for (int a = 0; a < 4; a++) {
+      pre[(size_t)(3 * a) * ne + e] = g[a].x;
+      pre[(size_t)(3 * a + 1) * ne + e] = g[a].y;
+      pre[(size_t)(3 * a + 2) * ne + e] = g[a].z;
+    }
+    for (int i = 0; i < 9; i++) pre[(size_t)(12 + i) * ne + e] = Di[i];
+    pre[(size_t)21 * ne + e] = vol;
+  }
+}
+
+// ------------------------------------------------------------ mass / loads
+__device__ __forceinline__ int local12(int a, int b) { return a * 12 - ((a - 1) * a) / 2 + b - a; }
+
+// consistent mass, rho V / 10 on the diagonal and rho V / 20 off it, same
+// axis only (tetelement.cpp:51-66, mechMaterial.cpp:69-98); one colour
+__global__ void mass_kernel(int e0, int e1, int ne, int vslot, double rho, const double* __restrict__ pre,
+                            const int* __restrict__ emap, double* __restrict__ M) {
+  int e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= e1) return;
+  double vol = pre[(size_t)vslot * ne + e];
+  double od = vol * 0.05, dg = vol * 0.1;
+  for (int a = 0; a < 4; a++)
+    for (int b = a; b < 4; b++) {
+      double entry = rho * (a == b ? dg : od);
+      for (int ax = 0; ax < 3; ax++) {
+        int idx = emap[(size_t)local12(3 * a + ax, 3 * b + ax) * ne + e];
+        if (idx >= 0) M[idx] += entry;
+      }
+    }
+}
+
+// V/4 per incident element, summed per node (body-force weights); one colour
+__global__ void node_vol_kernel(int e0, int e1, int ne, int vslot, const int4* __restrict__ tets,
+                                const double* __restrict__ pre, double* __restrict__ nv) {
+  int e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= e1) return;
+  int4 t = tets[e];
+  double q = pre[(size_t)vslot * ne + e] / 4.0;
+  nv[t.x] += q; nv[t.y] += q; nv[t.z] += q; nv[t.w] += q;
+}
+
+// body force density times the node's volume share (Forcer::addBodyForce,
+// core/forcer.cpp:8-33 with TetElement::getBodyVirtualWorks, tetelement.cpp:68-77)
+__global__ void body_force_kernel(int n, const int* __restrict__ free_pos, const double* __restrict__ nv,
+                                  double bx, double by, double bz, double* __restrict__ fext) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int p = free_pos[i];
+  int ax = p % 3;
+  double b = ax == 0 ? bx : (ax == 1 ? by : bz);
+  fext[i] = nv[p / 3] * b;
+}
+
+// uniform traction over deformed facets, area / 3 per vertex
+// (TetFacet::getSurfVirtualWorks, tetelement.cpp:79-89); one facet colour
+__global__ void traction_kernel(int f0, int f1, const int* __restrict__ fids, const double* __restrict__ tvec,
+                                const int* __restrict__ facets, const double* __restrict__ X,
+                                const double* __restrict__ u, const int* __restrict__ node_dof,
+                                double* __restrict__ fext) {
+  int k = f0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= f1) return;
+  int f = fids[k];
+  int n[3] = {facets[3 * f], facets[3 * f + 1], facets[3 * f + 2]};
+  V3t<double> p[3];
+  for (int i = 0; i < 3; i++) {
+    p[i] = {X[3 * n[i]] + u[3 * n[i]], X[3 * n[i] + 1] + u[3 * n[i] + 1], X[3 * n[i] + 2] + u[3 * n[i] + 2]};
+  }
+  V3t<double> cr = v_cross(v_sub(p[1], p[0]), v_sub(p[2], p[0]));
+  double area = sqrt(v_len2(cr)) * 0.5;
+  double fac = area / 3.0;
+  for (int i = 0; i < 3; i++)
+    for (int ax = 0; ax < 3; ax++) {
+      double w = fac * tvec[3 * k + ax];
+      int g = node_dof[3 * n[i] + ax];
+      if (w != 0.0 && g >= 0) fext[g] += w;
+    }
+}
+
+// -------------------------------------------------- corotational element
+// F = [x1-x0, x2-x0, x3-x0] Dm^-1; R = polar(F), or the proper QR factor when
+// the deformed volume is below threshold * rest volume
+// (tetelement.cpp:546-573); K_ab = R K0_ab R^T packed into 78 values and
+// f_a = sum_b (R K0_ab R^T x_b - R K0_ab X_b) (tetelement.cpp:583-651).
+// MODE 0 scatters into K / fint through the element map (one colour per
+// launch); MODE 1 stores per-element values in original element order.
+template <int MODE>
+__global__ void __launch_bounds__(128) corot_kernel(int e0, int e1, int ne, const int4* __restrict__ tets,
+                                                    const double* __restrict__ X, const double* __restrict__ u,
+                                                    const double* __restrict__ pre, double thr,
+                                                    const int* __restrict__ emap, const int* __restrict__ gdof,
+                                                    double* __restrict__ K, double* __restrict__ fint,
+                                                    double* __restrict__ out78, double* __restrict__ out12,
+                                                    const int* __restrict__ perm) {
+  int e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= e1) return;
+  int4 t = tets[e];
+  const int nd[4] = {t.x, t.y, t.z, t.w};
+  V3t<double> o[4], c[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    o[i] = ld3(X, nd[i]);
+    V3t<double> du = ld3(u, nd[i]);
+    c[i] = {o[i].x + du.x, o[i].y + du.y, o[i].z + du.z};
+  }
+  double Di[9], F[9];
+#pragma unroll
+  for (int i = 0; i < 9; i++) { Di[i] = pre[(size_t)(90 + i) * ne + e]; F[i] = 0.0; }
+#pragma unroll
+  for (int i = 1; i < 4; i++) {
+    double ax[3] = {c[i].x - c[0].x, c[i].y - c[0].y, c[i].z - c[0].z};
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) F[j * 3 + k] += ax[j] * Di[(i - 1) * 3 + k];
+  }
+  const double v0 = pre[(size_t)99 * ne + e];
+  const double v1 = tet_vol(c[0], c[1], c[2], c[3]);
+  double R[9];
+  if (v1 >= thr * v0) polar3<double>(F, R);
+  else qr3<double>(F, R);
+
+  double f[12];
+#pragma unroll
+  for (int i = 0; i < 12; i++) f[i] = 0.0;
+  const size_t obase = MODE == 1 ? (size_t)perm[e] * 78 : 0;
+  auto put = [&](int k, double val) {
+    if (MODE == 0) {
+      int idx = emap[(size_t)k * ne + e];
+      if (idx >= 0) K[idx] += val;
+    } else {
+      out78[obase + k] = val;
+    }
+  };
+  int blk = 0;
+#pragma unroll 1
+  for (int a = 0; a < 4; a++) {
+    double K0[9], QK[9], QKQT[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) K0[i] = pre[(size_t)(9 * blk + i) * ne + e];
+    blk++;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) QK[i * 3 + j] = R[i * 3] * K0[j] + R[i * 3 + 1] * K0[3 + j] + R[i * 3 + 2] * K0[6 + j];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) QKQT[i * 3 + j] = QK[i * 3] * R[j * 3] + QK[i * 3 + 1] * R[j * 3 + 1] + QK[i * 3 + 2] * R[j * 3 + 2];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3 - i; j++) put(c_diag12[a * 3 + i] + j, QKQT[i * 3 + i + j]);
+    const double ca[3] = {c[a].x, c[a].y, c[a].z}, oa[3] = {o[a].x, o[a].y, o[a].z};
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) f[a * 3 + i] += QKQT[i * 3 + j] * ca[j] - QK[i * 3 + j] * oa[j];
+#pragma unroll 1
+    for (int b = a + 1; b < 4; b++) {
+      double QKT[9];
+#pragma unroll
+      for (int i = 0; i < 9; i++) K0[i] = pre[(size_t)(9 * blk + i) * ne + e];
+      blk++;
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          QK[i * 3 + j] = R[i * 3] * K0[j] + R[i * 3 + 1] * K0[3 + j] + R[i * 3 + 2] * K0[6 + j];
+          QKT[i * 3 + j] = R[i * 3] * K0[j * 3] + R[i * 3 + 1] * K0[j * 3 + 1] + R[i * 3 + 2] * K0[j * 3 + 2];
+        }
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) QKQT[i * 3 + j] = QK[i * 3] * R[j * 3] + QK[i * 3 + 1] * R[j * 3 + 1] + QK[i * 3 + 2] * R[j * 3 + 2];
+      const double cb[3] = {c[b].x, c[b].y, c[b].z}, ob[3] = {o[b].x, o[b].y, o[b].z};
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          put(c_diag12[a * 3 + i] + (b - a) * 3 - i + j, QKQT[i * 3 + j]);
+          f[a * 3 + i] += QKQT[i * 3 + j] * cb[j] - QK[i * 3 + j] * ob[j];
+          f[b * 3 + i] += QKQT[j * 3 + i] * ca[j] - QKT[i * 3 + j] * oa[j];
+        }
+    }
+  }
+  if (MODE == 0) {
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      int g = gdof[(size_t)k * ne + e];
+      if (g >= 0) fint[g] += f[k];
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 12; k++) out12[(size_t)perm[e] * 12 + k] = f[k];
+  }
+}
+
+// ------------------------------------------- invertible hyperelastic element
+// Invertible SVD of F, energy derivatives in the invariants I1 = sum s^2,
+// I2 = sum s^4, I3 = prod s^2 (invertibleHyperelastic.h:22-30): Neo-Hookean
+// (invertibleNeoHookean.cpp:11-20) or StVK (invertibleStVK.cpp:11-20);
+// P = U diag(2 g1 s + 4 g2 s^3 + 2 g3 I3 / s) V^T (invertibleHyperelastic.cpp:
+// 247-265); dP/dF in the singular-value frame projected to PSD
+// (tetelement.cpp:357-499) -- only its 21 structural non-zeros are formed;
+// K_ab = U [sum_kl dP_ikjl (V^T dN_a)_k (V^T dN_b)_l] U^T / (36 V)
+// (tetelement.cpp:282-342); f_a = P dN_a / 6, f_3 = -(f_0 + f_1 + f_2)
+// (tetelement.cpp:344-355).
+template <int MODE>
+__global__ void __launch_bounds__(128) invhyper_kernel(int e0, int e1, int ne, int stvk, const int4* __restrict__ tets,
+                                                       const double* __restrict__ X, const double* __restrict__ u,
+                                                       const double* __restrict__ pre, double thr, double lambda,
+                                                       double mu, const int* __restrict__ emap,
+                                                       const int* __restrict__ gdof, double* __restrict__ K,
+                                                       double* __restrict__ fint, double* __restrict__ out78,
+                                                       double* __restrict__ out12, const int* __restrict__ perm) {
+  int e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= e1) return;
+  int4 t = tets[e];
+  const int nd[4] = {t.x, t.y, t.z, t.w};
+  V3t<double> c[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    V3t<double> x = ld3(X, nd[i]), du = ld3(u, nd[i]);
+    c[i] = {x.x + du.x, x.y + du.y, x.z + du.z};
+  }
+  double F[9];
+#pragma unroll
+  for (int i = 0; i < 9; i++) F[i] = 0.0;
+#pragma unroll
+  for (int i = 1; i < 4; i++) {
+    double ax[3] = {c[i].x - c[0].x, c[i].y - c[0].y, c[i].z - c[0].z};
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) F[j * 3 + k] += ax[j] * pre[(size_t)(12 + (i - 1) * 3 + k) * ne + e];
+  }
+  double sig[3], U[9], VT[9];
+  invertible_svd<double>(F, thr, sig, U, VT);
+  const double s02 = sig[0] * sig[0], s12 = sig[1] * sig[1], s22 = sig[2] * sig[2];
+  const double I1 = s02 + s12 + s22, I3 = s02 * s12 * s22;
+  double g0, g1, g2, h0 = 0.0, h5 = 0.0;
+  if (!stvk) {
+    g0 = 0.5 * mu;
+    g1 = 0.0;
+    g2 = (-0.5 * mu + 0.25 * lambda * log(I3)) / I3;
+    h5 = (0.5 * mu + 0.25 * lambda * (1.0 - log(I3))) / (I3 * I3);
+  } else {
+    g0 = 0.25 * lambda * (I1 - 3.0) - 0.5 * mu;
+    g1 = 0.25 * mu;
+    g2 = 0.0;
+    h0 = 0.25 * lambda;
+  }
+  // dP/dF non-zeros (tetelement.cpp:357-437)
+  const double sc01 = sig[0] * sig[1], sc02 = sig[0] * sig[2], sc12 = sig[1] * sig[2];
+  double a01 = 2.0 * g0 + 4.0 * (s02 + s12) * g1;
+  double a02 = 2.0 * g0 + 4.0 * (s02 + s22) * g1;
+  double a12 = 2.0 * g0 + 4.0 * (s12 + s22) * g1;
+  const double a00 = 2.0 * g0 + 8.0 * s02 * g1, a11 = 2.0 * g0 + 8.0 * s12 * g1, a22 = 2.0 * g0 + 8.0 * s22 * g1;
+  const double d00 = I3 * g2 / s02, d01 = I3 * g2 / sc01, d02 = I3 * g2 / sc02;
+  const double d11 = I3 * g2 / s12, d12 = I3 * g2 / sc12, d22 = I3 * g2 / s22;
+  const double b00 = 4.0 * s02 * g1 - 2.0 * d00, b11 = 4.0 * s12 * g1 - 2.0 * d11, b22 = 4.0 * s22 * g1 - 2.0 * d22;
+  double b01 = 4.0 * sc01 * g1 - 2.0 * d01, b02 = 4.0 * sc02 * g1 - 2.0 * d02, b12 = 4.0 * sc12 * g1 - 2.0 * d12;
+  // Hessian in the invariants is diag-like: only H00 (StVK) or H22 (NH) set
+  double w[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    w[i][0] = 2.0 * sig[i];
+    w[i][1] = 4.0 * sig[i] * (i == 0 ? s02 : (i == 1 ? s12 : s22));
+    w[i][2] = 2.0 * I3 / sig[i];
+  }
+  // w_i . (H w_j) with H = diag(h0, 0, h5) in the invariants (the only
+  // non-zero Hessian entries of both energies)
+  auto qf = [&](int i, int j) { return w[i][0] * (h0 * w[j][0]) + w[i][2] * (h5 * w[j][2]); };
+  double T[6] = {a00 + b00 + (qf(0, 0) + 4.0 * d00), qf(1, 0) + 4.0 * d01, qf(2, 0) + 4.0 * d02,
+                 a11 + b11 + (qf(1, 1) + 4.0 * d11), qf(2, 1) + 4.0 * d12, a22 + b22 + (qf(2, 2) + 4.0 * d22)};
+  psd3<double>(T);
+  psd2<double>(a01, b01);
+  psd2<double>(a02, b02);
+  psd2<double>(a12, b12);
+  const double Tm[3][3] = {{T[0], T[1], T[2]}, {T[1], T[3], T[4]}, {T[2], T[4], T[5]}};
+  const double Al[3][3] = {{0.0, a01, a02}, {a01, 0.0, a12}, {a02, a12, 0.0}};
+  const double Be[3][3] = {{0.0, b01, b02}, {b01, 0.0, b12}, {b02, b12, 0.0}};
+
+  // P = U diag(de) V^T
+  double de[3], P[9];
+#pragma unroll
+  for (int i = 0; i < 3; i++) de[i] = 2.0 * g0 * sig[i] + 4.0 * g1 * sig[i] * sig[i] * sig[i] + 2.0 * g2 * I3 / sig[i];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      P[i * 3 + j] = U[i * 3] * (VT[j] * de[0]) + U[i * 3 + 1] * (VT[3 + j] * de[1]) + U[i * 3 + 2] * (VT[6 + j] * de[2]);
+
+  // a_n = V^T dN_n
+  double an[4][3];
+#pragma unroll
+  for (int nn = 0; nn < 4; nn++) {
+    double d0 = pre[(size_t)(3 * nn) * ne + e], d1 = pre[(size_t)(3 * nn + 1) * ne + e], d2 = pre[(size_t)(3 * nn + 2) * ne + e];
+#pragma unroll
+    for (int i = 0; i < 3; i++) an[nn][i] = VT[3 * i] * d0 + VT[3 * i + 1] * d1 + VT[3 * i + 2] * d2;
+  }
+  const double fac = 1.0 / (36.0 * pre[(size_t)21 * ne + e]);
+  const size_t obase = MODE == 1 ? (size_t)perm[e] * 78 : 0;
+  auto put = [&](int k, double val) {
+    if (MODE == 0) {
+      int idx = emap[(size_t)k * ne + e];
+      if (idx >= 0) K[idx] += val;
+    } else {
+      out78[obase + k] = val;
+    }
+  };
+#pragma unroll 1
+  for (int a = 0; a < 4; a++) {
+#pragma unroll 1
+    for (int b = a; b < 4; b++) {
+      double sm[9];
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          double en = 0.0;
+          if (i == j) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) en += (k == i ? Tm[i][i] : Al[i][k]) * an[a][k] * an[b][k];
+          } else if (i < j) {
+            en += Tm[i][j] * an[a][i] * an[b][j];
+            en += Be[i][j] * an[a][j] * an[b][i];
+          } else {
+            en += Be[i][j] * an[a][j] * an[b][i];
+            en += Tm[i][j] * an[a][i] * an[b][j];
+          }
+          sm[i * 3 + j] = en;
+        }
+      double tmp[9], out[9];
+      mul3(U, sm, tmp);
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) out[i * 3 + j] = tmp[i * 3] * U[j * 3] + tmp[i * 3 + 1] * U[j * 3 + 1] + tmp[i * 3 + 2] * U[j * 3 + 2];
+      if (a == b) {
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3 - i; j++) put(c_diag12[a * 3 + i] + j, out[i * 3 + i + j] * fac);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++) put(c_diag12[a * 3 + i] + (b - a) * 3 - i + j, out[i * 3 + j] * fac);
+      }
+    }
+  }
+  double f[12];
+  const double sixth = 1.0 / 6.0;
+#pragma unroll
+  for (int nn = 0; nn < 3; nn++) {
+    double d0 = pre[(size_t)(3 * nn) * ne + e], d1 = pre[(size_t)(3 * nn + 1) * ne + e], d2 = pre[(size_t)(3 * nn + 2) * ne + e];
+#pragma unroll
+    for (int i = 0; i < 3; i++) f[3 * nn + i] = (P[3 * i] * d0 + P[3 * i + 1] * d1 + P[3 * i + 2] * d2) * sixth;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) f[9 + i] = -(f[i] + f[3 + i] + f[6 + i]);
+  if (MODE == 0) {
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      int g = gdof[(size_t)k * ne + e];
+      if (g >= 0) fint[g] += f[k];
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 12; k++) out12[(size_t)perm[e] * 12 + k] = f[k];
+  }
+}
+
+// ---------------------------------------------------------------- launches
+static inline int nblk(int n, int t) { return (n + t - 1) / t; }
+
+od_status launch_precompute(Scene* s) {
+  const int T = 128;
+  if (s->n_tets == 0) return OD_OK;
+  precompute_kernel<<<nblk(s->n_tets, T), T, 0, s->ctx->stream>>>(s->n_tets, s->mat.kind, s->tets, s->X, s->D[0],
+                                                                   s->D[1], s->D[2], s->pre);
+  OD_CUDA(cudaGetLastError());
+  return OD_OK;
+}
+
+static int vol_slot(const Scene* s) { return s->mat.kind == OD_MATERIAL_COROTATIONAL ? 99 : 21; }
+
+od_status launch_mass(Scene* s) {
+  const int T = 128;
+  OD_CUDA(cudaMemsetAsync(s->M, 0, sizeof(double) * (size_t)s->nvals, s->ctx->stream));
+  OD_CUDA(cudaMemsetAsync(s->node_vol4, 0, sizeof(double) * (size_t)s->n_nodes, s->ctx->stream));
+  for (size_t c = 0; c + 1 < s->color_off.size(); c++) {
+    int e0 = s->color_off[c], e1 = s->color_off[c + 1];
+    if (e1 <= e0) continue;
+    mass_kernel<<<nblk(e1 - e0, T), T, 0, s->ctx->stream>>>(e0, e1, s->n_tets, vol_slot(s), s->mat.density, s->pre,
+                                                             s->emap, s->M);
+    node_vol_kernel<<<nblk(e1 - e0, T), T, 0, s->ctx->stream>>>(e0, e1, s->n_tets, vol_slot(s), s->tets, s->pre,
+                                                                 s->node_vol4);
+  }
+  OD_CUDA(cudaGetLastError());
+  return OD_OK;
+}
+
+od_status launch_eval(Scene* s, bool zero_first) {
+  const int T = 128;
+  cudaStream_t st = s->ctx->stream;
+  if (zero_first) {
+    OD_CUDA(cudaMemsetAsync(s->K, 0, sizeof(double) * (size_t)s->nvals, st));
+    OD_CUDA(cudaMemsetAsync(s->fint, 0, sizeof(double) * (size_t)s->pcg.n_pad, st));
+  }
+  for (size_t c = 0; c + 1 < s->color_off.size(); c++) {
+    int e0 = s->color_off[c], e1 = s->color_off[c + 1];
+    if (e1 <= e0) continue;
+    if (s->mat.kind == OD_MATERIAL_COROTATIONAL)
+      corot_kernel<0><<<nblk(e1 - e0, T), T, 0, st>>>(e0, e1, s->n_tets, s->tets, s->X, s->u, s->pre,
+                                                       s->mat.threshold, s->emap, s->gdof, s->K, s->fint, nullptr,
+                                                       nullptr, nullptr);
+    else
+      invhyper_kernel<0><<<nblk(e1 - e0, T), T, 0, st>>>(e0, e1, s->n_tets, s->mat.kind == OD_MATERIAL_STVK,
+                                                          s->tets, s->X, s->u, s->pre, s->mat.threshold, s->lambda,
+                                                          s->mu, s->emap, s->gdof, s->K, s->fint, nullptr, nullptr,
+                                                          nullptr);
+  }
+  OD_CUDA(cudaGetLastError());
+  return OD_OK;
+}
+
+od_status launch_element_values(Scene* s, double* d_k78, double* d_f12) {
+  const int T = 128;
+  cudaStream_t st = s->ctx->stream;
+  if (s->n_tets == 0) return OD_OK;
+  if (s->mat.kind == OD_MATERIAL_COROTATIONAL)
+    corot_kernel<1><<<nblk(s->n_tets, T), T, 0, st>>>(0, s->n_tets, s->n_tets, s->tets, s->X, s->u, s->pre,
+                                                       s->mat.threshold, s->emap, s->gdof, nullptr, nullptr, d_k78,
+                                                       d_f12, s->perm);
+  else
+    invhyper_kernel<1><<<nblk(s->n_tets, T), T, 0, st>>>(0, s->n_tets, s->n_tets, s->mat.kind == OD_MATERIAL_STVK,
+                                                          s->tets, s->X, s->u, s->pre, s->mat.threshold, s->lambda,
+                                                          s->mu, s->emap, s->gdof, nullptr, nullptr, d_k78, d_f12,
+                                                          s->perm);
+  OD_CUDA(cudaGetLastError());
+  return OD_OK;
+}
+
+// body part then traction colours; s->trac_* hold the colour-ordered facets
+od_status launch_loads(Scene* s, const double* body, int n_facets_total) {
+  const int T = 128;
+  cudaStream_t st = s->ctx->stream;
+  double b[3] = {0, 0, 0};
+  if (body) { b[0] = body[0]; b[1] = body[1]; b[2] = body[2]; }
+  OD_CUDA(cudaMemsetAsync(s->fext, 0, sizeof(double) * (size_t)s->pcg.n_pad, st));
+  if (s->dofs > 0)
+    body_force_kernel<<<nblk(s->dofs, T), T, 0, st>>>(s->dofs, s->free_pos, s->node_vol4, b[0], b[1], b[2], s->fext);
+  if (n_facets_total > 0) {
+    for (size_t c = 0; c + 1 < s->trac_color_off.size(); c++) {
+      int f0 = s->trac_color_off[c], f1 = s->trac_color_off[c + 1];
+      if (f1 <= f0) continue;
+      traction_kernel<<<nblk(f1 - f0, T), T, 0, st>>>(f0, f1, s->trac_facets, s->trac_vec, s->facets_dev, s->X,
+                                                       s->u, s->node_dof, s->fext);
+    }
+  }
+  OD_CUDA(cudaGetLastError());
+  return OD_OK;
+}
+
+}  // namespace od

@@ -1,0 +1,194 @@
+// Internal data model of the GB300 implicit FEM step (not part of the ABI).
+//
+// HBM layout of one scene (all arrays device-resident, element arrays in
+// colour order so every colour is a contiguous range):
+//   X, u            n_nodes*3 double   rest positions / mesh displacement
+//   tets            n_tets int4        node ids
+//   pre             SoA [k][n_tets]    corotational: 90 K0 + 9 Dm^-1 + V;
+//                                      invertible:   12 dN + 9 Dm^-1 + V
+//   emap            SoA [78][n_tets]   reference element->value map
+//   gdof            SoA [12][n_tets]   compacted DOF of each element DOF or -1
+//   K, M, D         n_values double    tangent / mass / external damping in the
+//                                      reference lower block-CSC value layout
+//   full BSR        row_ptr[nb+1], col[nnzb] over padded 3-DOF blocks (both
+//                   triangles); desc[nnzb] says where each block's 9 values
+//                   live in the lower layout; A[nnzb*9] in FP64 or FP32
+//   vectors         n_pad = 3*nb doubles (padding DOFs carry an identity row)
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/od_gb300.h"
+
+namespace od {
+
+// Where a full-BSR block takes its values from in the lower layout.
+enum BlockKind : int32_t {
+  BK_LOWER = 0,      // stored block (br, bc) br > bc, column-major: a[r][c] = v[off + c*3 + r]
+  BK_UPPER = 1,      // transpose of a stored block: a[r][c] = v[off + r*3 + c]
+  BK_DIAG = 2,       // packed symmetric diagonal block (6 values)
+  BK_GENERAL = 3     // irregular: per-entry table at gen[off*9 .. +9] (-1 zero, -2 identity)
+};
+
+struct FullBsr {
+  int nb = 0;                 // block rows (= ceil(dofs / 3))
+  int nnzb = 0;               // stored blocks (both triangles)
+  int* row_ptr = nullptr;     // nb + 1
+  int* col = nullptr;         // nnzb
+  int* desc_off = nullptr;    // nnzb
+  int* desc_kind = nullptr;   // nnzb
+  int* gen = nullptr;         // 9 per general block
+  int n_general = 0;
+  int* diag_pos = nullptr;    // nb: index of the diagonal block in each row
+};
+
+struct SolveScalars {           // device-resident PCG scalars (one cache line set)
+  double rz, rz_new, pq, rr, bb, eps, alpha, beta;
+  double rr0;
+  int iter, max_iter, done, status;
+  unsigned int count1, count2;  // last-block-done counters
+};
+
+struct Pcg {
+  int n_pad = 0;
+  int precision = OD_PRECISION_FP64;
+  double* x = nullptr;
+  double* r = nullptr;
+  double* z = nullptr;
+  double* p = nullptr;
+  double* q = nullptr;
+  double* b = nullptr;
+  double* partial = nullptr;    // 2 per CTA
+  SolveScalars* sc = nullptr;
+  SolveScalars* sc_host = nullptr;  // pinned mirror
+  int grid = 0;
+  // preconditioner
+  double* pinv = nullptr;       // Jacobi: n_pad; block-Jacobi: 9*nb
+  // IC(0) (scalar CSR of the padded lower pattern)
+  int ic_n = 0, ic_nnz = 0;
+  int* ic_rp = nullptr;
+  int* ic_ci = nullptr;
+  int* ic_src = nullptr;        // source entry in the full BSR A (block*9 + r*3 + c)
+  double* ic_val = nullptr;
+  int* ic_diag = nullptr;       // position of the diagonal in each row
+  int n_levels_f = 0, n_levels_b = 0;
+  int* lvl_rows_f = nullptr;    // rows sorted by forward level
+  int* lvl_rows_b = nullptr;
+  std::vector<int> lvl_ptr_f, lvl_ptr_b;  // host level offsets
+  int* ic_bad = nullptr;        // breakdown flag
+  // upper (transposed) CSR for the backward sweep: for row i, entries L_ji j > i
+  int* icT_rp = nullptr;
+  int* icT_ci = nullptr;
+  int* icT_pos = nullptr;       // index into ic_val
+  double ic_shift = 0.0;
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+};
+
+struct Scene {
+  Ctx* ctx = nullptr;
+  int n_nodes = 0, n_tets = 0, n_facets = 0, dofs = 0;
+  od_material mat{};
+  double lambda = 0, mu = 0, D[3] = {0, 0, 0};
+  // host copies
+  std::vector<double> hX;
+  std::vector<int> htets, hfacets, hcd, hfree_pos, hnode_dof;
+  std::vector<int> hpcol, hrows, horis, hemap;
+  int nbc = 0, nrem = 0, nvals = 0;
+  std::vector<int> color_off;      // element colour ranges (colour order)
+  std::vector<int> elem_perm;      // colour-order position -> original element
+  // device
+  double* X = nullptr;
+  double* u = nullptr;
+  int4* tets = nullptr;
+  double* pre = nullptr;
+  int n_pre = 0;
+  int* emap = nullptr;
+  int* gdof = nullptr;
+  int* perm = nullptr;
+  int* free_pos = nullptr;         // compacted DOF -> 3*node + axis
+  int* node_dof = nullptr;         // 3*node + axis -> compacted DOF or -1
+  int* facets_dev = nullptr;       // n_facets * 3
+  double* node_vol4 = nullptr;     // sum over incident tets of V/4
+  double* K = nullptr;
+  double* M = nullptr;
+  double* Dm = nullptr;            // external damping (zero unless set)
+  double* fint = nullptr;
+  double* fext = nullptr;
+  double* work_vals = nullptr;     // host-supplied values (SpMDV / PCG drop-in)
+  FullBsr bsr;
+  void* A = nullptr;               // full BSR values (double or float)
+  double* A64 = nullptr;           // FP64 full values (mixed path keeps both)
+  float* A32 = nullptr;
+  Pcg pcg;
+  // integrator
+  od_integrator_params ip{};
+  bool has_integrator = false;
+  double *v = nullptr, *d = nullptr, *a = nullptr, *dp = nullptr, *vp = nullptr, *dv = nullptr,
+         *rhs = nullptr, *tmp = nullptr, *tmp2 = nullptr;
+  double time = 0.0;
+  long long device_bytes = 0;
+  // traction loads (per call)
+  int* trac_facets = nullptr;      // colour-ordered facet ids
+  double* trac_vec = nullptr;      // per facet traction (3)
+  int trac_cap = 0;
+  std::vector<int> trac_color_off;
+};
+
+// ---- error handling ----
+void set_error(const std::string& msg);
+od_status cuda_fail(cudaError_t e, const char* what);
+#define OD_CUDA(call)                                        \
+  do {                                                       \
+    cudaError_t _e = (call);                                 \
+    if (_e != cudaSuccess) return ::od::cuda_fail(_e, #call); \
+  } while (0)
+
+// ---- host algorithms (od_host.cpp) ----
+int global_index(const std::vector<int>& cd, int node, int axis);
+void build_pattern(const std::vector<int>& gidx, int n_tets, int dofs, std::vector<int>& pcol,
+                   std::vector<int>& rows, std::vector<int>& oris, int& nbc, int& nrem, int& nvals);
+void build_emap(const std::vector<int>& gidx, int n_tets, int dofs, int nbc,
+                const std::vector<int>& pcol, const std::vector<int>& rows,
+                const std::vector<int>& oris, std::vector<int>& emap);
+int color_elements(const std::vector<int>& nodes, int per_elem, int n_elem, int n_nodes,
+                   std::vector<int>& perm, std::vector<int>& color_off);
+struct HostBsr {
+  int nb = 0;
+  std::vector<int> row_ptr, col, desc_off, desc_kind, gen, diag_pos;
+};
+void build_full_bsr(int dofs, int nbc, int nrem, const std::vector<int>& pcol,
+                    const std::vector<int>& rows, const std::vector<int>& oris, HostBsr& out);
+void build_ic_levels(const std::vector<int>& rp, const std::vector<int>& ci, int n,
+                     std::vector<int>& rows_by_level, std::vector<int>& lvl_ptr, bool forward);
+
+// ---- kernels (od_elements.cu) ----
+od_status launch_precompute(Scene* s);
+od_status launch_mass(Scene* s);
+od_status launch_eval(Scene* s, bool zero_first);       // K, fint at current u
+od_status launch_element_values(Scene* s, double* d_k78, double* d_f12);
+od_status launch_loads(Scene* s, const double* body, int n_facets_total);
+
+// ---- kernels (od_sparse.cu) ----
+od_status pcg_alloc(Scene* s);
+void pcg_free(Scene* s);
+// A64 = c1 V1 + c2 V2 + c3 V3 expanded to the full BSR (V2, V3 may be NULL)
+od_status launch_expand(Scene* s, const double* v1, double c1, const double* v2, double c2, const double* v3,
+                        double c3);
+// y (+)= c1 V1 x1 + c2 V2 x2 + c3 V3 x3, V* in the lower layout (V2, V3 may be NULL)
+od_status launch_spmv_lower(Scene* s, const double* v1, double c1, const double* x1, const double* v2, double c2,
+                            const double* x2, const double* v3, double c3, const double* x3, double* y,
+                            bool accumulate);
+od_status launch_spmv_full(Scene* s, const double* x, double* y);
+// PCG on A64; b and x are device vectors of length n_pad
+od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm, od_solve_stats* st);
+
+}  // namespace od

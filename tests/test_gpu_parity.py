@@ -1,0 +1,191 @@
+"""GPU parity through the C ABI against the reference's golden vectors and
+the oracle restatement.
+
+Tolerances (from the project's parity contract):
+* sparsity pattern and element->value map: bit-exact;
+* per-element stiffness / forces and assembled values: 1e-12 relative to the
+  largest magnitude (summation order and FMA contraction differ);
+* displacements after N steps: 1e-8 relative (plain FP64 path).
+"""
+import numpy as np
+import pytest
+
+from opendeformer_gb300 import api, meshgen
+from tests.gpu_util import ctx, material, rel_err
+
+pytestmark = pytest.mark.gpu
+
+MATS = ["corotational", "neohookean", "stvk"]
+
+
+def gpu_scene(golden, mat, case):
+    p = golden(f"pattern_{case}")
+    e = golden(f"elements_{mat}_{case}")
+    s = api.Scene(ctx(), p["X"], p["tets"], p["facets"], p["cdofs"], material(mat, *e["material"]))
+    return s, p, e
+
+
+@pytest.mark.parametrize("case", ["full", "partial"])
+def test_pattern_bit_exact(golden, case):
+    s, p, _ = gpu_scene(golden, "corotational", case)
+    assert s.dofs == int(p["dofs"])
+    pcol, rows, oris, emap = s.pattern()
+    assert np.array_equal(pcol, p["pcol"])
+    assert np.array_equal(rows, p["rows"])
+    assert np.array_equal(oris, p["oris"])
+    assert np.array_equal(emap, p["emap"])
+
+
+@pytest.mark.parametrize("mat", MATS)
+@pytest.mark.parametrize("case", ["full", "partial"])
+def test_elements_assembly_mass_loads(golden, mat, case):
+    s, p, e = gpu_scene(golden, mat, case)
+    s.set_displacements(e["u"])
+    K, f = s.element_values()
+    assert rel_err(K, e["K78"]) <= 1e-12
+    assert rel_err(f, e["f12"]) <= 1e-12
+    vals, fint = s.evaluate()
+    assert rel_err(vals, e["values"]) <= 1e-12
+    assert rel_err(fint, e["fint"]) <= 1e-12
+    assert rel_err(s.mass(), e["mass"]) <= 1e-13
+    y = s.spmdv(e["values"], e["spmv_x"])
+    assert rel_err(y, e["spmv_y"]) <= 1e-12
+    g = meshgen.tet_grid(4, 2, 2, h=0.05, jitter=0.1, seed=11, tets_per_cube=6)
+    s.set_loads(body=[0, 0, -9800.0], tractions=[([0, -500.0, 0], g.face_facets(0, 1))])
+    assert rel_err(s.external_forces(), e["fext"]) <= 1e-12
+
+
+@pytest.mark.parametrize("mat", MATS)
+@pytest.mark.parametrize("case", ["full", "partial"])
+def test_jacobi_pcg_matches_reference(golden, mat, case):
+    s, p, e = gpu_scene(golden, mat, case)
+    A = e["values"] * (1.0 / 3600.0) + e["mass"]
+    x, st = s.pcg(A, e["cg_b"], solver=api.CGSolver(1e-10, 2000, api.JacobiPreconditioner()))
+    assert st.status == 0
+    assert abs(st.iterations - int(e["cg_iters"])) <= 2
+    assert rel_err(x, e["cg_x"]) <= 1e-8
+
+
+@pytest.mark.parametrize("precond", ["none", "jacobi", "block_jacobi", "ic0"])
+def test_preconditioners_converge(golden, precond):
+    s, p, e = gpu_scene(golden, "neohookean", "partial")
+    A = e["values"] * (1.0 / 3600.0) + e["mass"]
+    x, st = s.pcg(A, e["cg_b"], solver=api.CGSolver(1e-11, 5000, api.Preconditioner(precond)))
+    assert st.status == 0
+    assert st.rel_residual <= 1e-10
+    assert rel_err(x, e["cg_x"]) <= 1e-7
+
+
+@pytest.mark.parametrize("precond", ["block_jacobi", "ic0"])
+def test_preconditioner_iterations_match_oracle(golden, precond):
+    from oracle import restated as O
+    p = golden("pattern_partial")
+    e = golden("elements_stvk_partial")
+    s, _, _ = gpu_scene(golden, "stvk", "partial")
+    A = e["values"] * (1.0 / 3600.0) + e["mass"]
+    o = O.OracleScene(p["X"], p["tets"], p["facets"], p["cdofs"], "stvk", *e["material"])
+    xo, ito = o.pcg(A, e["cg_b"], tol=1e-10, maxit=2000, precond=precond)
+    x, st = s.pcg(A, e["cg_b"], solver=api.CGSolver(1e-10, 2000, api.Preconditioner(precond)))
+    assert abs(st.iterations - ito) <= 2
+    assert rel_err(x, xo) <= 1e-8
+
+
+@pytest.mark.parametrize("mat", MATS)
+def test_backward_euler_matches_reference(golden, mat):
+    p = golden("pattern_full")
+    e = golden(f"elements_{mat}_full")
+    be = golden(f"be_{mat}")
+    s = api.Scene(ctx(), p["X"], p["tets"], p["facets"], p["cdofs"], material(mat, *e["material"]))
+    dt, am, bk, tol = be["params"]
+    s.setup_integrator(api.NonlinearImplicitBackwardEuler(am, bk, dt, api.CGSolver(tol, 2000, api.JacobiPreconditioner())))
+    s.set_external_forces(be["fext"])
+    st = s.step(int(be["steps"]))
+    assert st.steps == int(be["steps"]) and st.status == 0
+    assert rel_err(s.displacements(), be["u"]) <= 1e-8
+    _, v, _ = s.state()
+    assert rel_err(v, be["v"]) <= 1e-8
+
+
+@pytest.mark.parametrize("mat", MATS)
+def test_newmark_matches_reference_restatement(golden, mat):
+    p = golden("pattern_full")
+    e = golden(f"elements_{mat}_full")
+    nm = golden(f"nm_{mat}")
+    s = api.Scene(ctx(), p["X"], p["tets"], p["facets"], p["cdofs"], material(mat, *e["material"]))
+    dt, am, bk, beta, gamma, newton, tol = nm["params"]
+    s.setup_integrator(api.NewmarkIntegrator(beta, gamma, am, bk, dt, api.CGSolver(tol, 2000, api.JacobiPreconditioner()),
+                                             int(newton)))
+    s.set_external_forces(nm["fext"])
+    s.step(int(nm["steps"]))
+    d, v, a = s.state()
+    assert rel_err(d, nm["d"]) <= 1e-8
+    assert rel_err(s.displacements(), nm["u"]) <= 1e-8
+
+
+def test_cantilever_3000_backward_euler_vs_oracle():
+    from oracle import restated as O
+    g = meshgen.cantilever_3000()
+    cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+    s = api.Scene(ctx(), g.X, g.tets, g.facets, cd, api.CorotationalHyperelasticMaterial(1000, 1e5, 0.45, 0.1))
+    o = O.OracleScene(g.X, g.tets, g.facets, cd, "corotational", 1000, 1e5, 0.45, 0.1)
+    o.integrator_setup(1 / 60, 0.01, 0.001, tol=1e-8, maxit=1000, precond="jacobi")
+    o.set_fext(o.loads(body=[0, 0, -9800.0]))
+    s.setup_integrator(api.NonlinearImplicitBackwardEuler(0.01, 0.001, 1 / 60, api.CGSolver(1e-8, 1000, api.JacobiPreconditioner())))
+    s.set_loads(body=[0, 0, -9800.0])
+    its_o = o.be_step(100)
+    st = s.step(100)
+    assert abs(st.pcg_iterations - its_o) <= 0.01 * its_o
+    assert rel_err(s.displacements(), o.displacements()) <= 1e-8
+
+
+@pytest.mark.parametrize("precond", ["jacobi", "block_jacobi", "ic0"])
+def test_cantilever_3000_newmark_vs_oracle(precond):
+    """Newmark on the soft cantilever stays within 1e-8 of the oracle for the
+    first 15 steps (afterwards the large-rotation trajectory is chaotic: two
+    CPU implementations of the same algorithm also separate)."""
+    from oracle import restated as O
+    g = meshgen.cantilever_3000()
+    cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+    s = api.Scene(ctx(), g.X, g.tets, g.facets, cd, api.CorotationalHyperelasticMaterial(1000, 1e5, 0.45, 0.1))
+    o = O.OracleScene(g.X, g.tets, g.facets, cd, "corotational", 1000, 1e5, 0.45, 0.1)
+    o.integrator_setup(1 / 60, 0.01, 0.001, newton=1, tol=1e-8, maxit=1000, precond=precond)
+    o.set_fext(o.loads(body=[0, 0, -9800.0]))
+    s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, 0.01, 0.001, 1 / 60,
+                                             api.CGSolver(1e-8, 1000, api.Preconditioner(precond)), 1))
+    s.set_loads(body=[0, 0, -9800.0])
+    o.nm_step(15)
+    s.step(15)
+    assert rel_err(s.displacements(), o.displacements()) <= 1e-8
+
+
+def test_checkpoint_resume_is_bitwise():
+    g = meshgen.tet_grid(6, 3, 3, h=0.05, jitter=0.1, seed=3)
+    cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+    mat = api.InvertibleNeoHookeanMaterial(1000, 98640.0, 0.4506, 0.1)
+    integ = api.NewmarkIntegrator(0.25, 0.5, 0.01, 0.001, 1 / 120, api.CGSolver(1e-8, 1000, api.BlockJacobiPreconditioner()), 2)
+    a = api.Scene(ctx(), g.X, g.tets, g.facets, cd, mat)
+    a.setup_integrator(integ)
+    a.set_loads(body=[0, 0, -9800.0])
+    a.step(6)
+    blob = a.save()
+    a.step(4)
+    b = api.Scene(ctx(), g.X, g.tets, g.facets, cd, mat)
+    b.setup_integrator(integ)
+    b.load(blob)
+    b.step(4)
+    assert np.array_equal(a.displacements(), b.displacements())
+    assert all(np.array_equal(x, y) for x, y in zip(a.state(), b.state()))
+
+
+def test_invalid_arguments_are_rejected():
+    g = meshgen.tet_grid(2, 1, 1)
+    bad = g.tets.copy()
+    bad[0, 0] = 10_000
+    with pytest.raises(api.ODError) as ei:
+        api.Scene(ctx(), g.X, bad, g.facets, [], api.CorotationalHyperelasticMaterial(1000, 1e5, 0.3, 0.1))
+    assert ei.value.status == 1
+    s = api.Scene(ctx(), g.X, g.tets, g.facets, [], api.CorotationalHyperelasticMaterial(1000, 1e5, 0.3, 0.1))
+    with pytest.raises(api.ODError):
+        s.step(1)  # no integrator yet
+    with pytest.raises(api.ODError):
+        s.setup_integrator(api.NonlinearImplicitBackwardEuler(0.01, 0.001, -1.0, api.CGSolver()))
