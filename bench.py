@@ -1,0 +1,401 @@
+"""Benchmark of the implicit FEM time step on GB300.
+
+Default workload (the configuration the headline metric is quoted on): a
+64x16x16-cube grid of 0.05 m cubes split into 6 tets each (98,304 tets,
+18,785 nodes), seeded jitter 0.15 h, invertible Neo-Hookean (mu = 3.4e4 Pa,
+lambda = 3.1e5 Pa, rho = 1000), x = 0 face fixed, the opposite face loaded by
+a 500 Pa traction along -y scaled by sin(2 pi 2 t), implicit Newmark
+(beta 1/4, gamma 1/2, dt 1/120 s, Rayleigh 0.01 / 0.001) with 3 Newton
+iterations per step, block-Jacobi PCG at relative tolerance 1e-8.  A "step"
+is one Newmark step.  Synthetic seeded mesh (the reference ships no data).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line.  --impl reference times the reference's own CPU code
+(oracle/_ref, compiled from the reference sources) on the same workload;
+the reference has no block-Jacobi, so it runs its Jacobi PCG.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from opendeformer_gb300 import meshgen  # noqa: E402
+
+NH_MU, NH_LAMBDA = 3.4e4, 3.1e5
+NH_E = NH_MU * (3 * NH_LAMBDA + 2 * NH_MU) / (NH_LAMBDA + NH_MU)
+NH_NU = NH_LAMBDA / (2 * (NH_LAMBDA + NH_MU))
+
+WORKLOADS = {
+    "beam98k_nh_newmark": dict(mesh=lambda: meshgen.beam_98k(), material=("neohookean", 1000.0, NH_E, NH_NU, 0.1),
+                               dt=1 / 120, newton=3, alpha_m=0.01, beta_k=0.001, traction=500.0,
+                               freq=2.0, body=None, tol=1e-8),
+    "cantilever3000_corot_newmark": dict(mesh=lambda: meshgen.cantilever_3000(),
+                                         material=("corotational", 1000.0, 1e5, 0.45, 0.1), dt=1 / 60, newton=1,
+                                         alpha_m=0.01, beta_k=0.001, traction=0.0, freq=0.0,
+                                         body=(0.0, 0.0, -9800.0), tol=1e-8),
+}
+L2_FLUSH_BYTES = 256 << 20
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, val in zip(names, parts[5:9]):
+                    if val.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def traction_groups(g, amp):
+    return [([0.0, -amp, 0.0], g.face_facets(0, 1))] if amp else []
+
+
+def spmv_bytes(info):
+    """Algorithmic bytes of one full-BSR FP64 SpMV launch (values + column
+    indices + row pointers + x read once + y written once)."""
+    nb = (info.dofs + 2) // 3
+    return info.num_full_blocks * (9 * 8 + 4) + (nb + 1) * 4 + 2 * 3 * nb * 8
+
+
+def pcg_iteration_bytes(info, precond):
+    """Algorithmic bytes of one PCG iteration: the SpMV, the x/r/z update with
+    the preconditioner apply, and the direction update (each array once)."""
+    n = 3 * ((info.dofs + 2) // 3)
+    pre = {"block_jacobi": 3 * n * 8, "jacobi": n * 8}.get(precond, 0)
+    return spmv_bytes(info) + (16 + 8 + 8 + 16 + 8) * n + pre + (16 + 8) * n
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profiles(workload, kernel):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == workload and parts[1] == kernel:
+                return float(parts[2])
+    return None
+
+
+def cpu_reference_sample(wl, max_seconds=15.0, max_steps=8):
+    """The reference's CPU Newmark (reference material, SpMDV, CGSolver with its
+    Jacobi preconditioner) on the same workload; a bounded sample."""
+    from oracle import build_ref, reforacle
+    if not reforacle.available():
+        build_ref.build()
+    g = wl["mesh"]()
+    cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+    kind, rho, E, nu, thr = wl["material"]
+    s = reforacle.RefScene(g.X, g.tets, g.facets, cd, kind, rho, E, nu, thr)
+    s.nm_setup(wl["dt"], wl["alpha_m"], wl["beta_k"], newton=wl["newton"], tol=wl["tol"], maxit=5000,
+               precond="jacobi")
+    steps, t_used = 0, 0.0
+    t = 0.0
+    while steps < max_steps and t_used < max_seconds:
+        t += wl["dt"]
+        scale = math.sin(2 * math.pi * wl["freq"] * t) if wl["freq"] else 1.0
+        t0 = time.perf_counter()
+        s.loads(body=wl["body"], tractions=[(np.array(tr) * scale, fac) for tr, fac in
+                                            traction_groups(g, wl["traction"])])
+        s.nm_apply_loads()
+        s.nm_step(1)
+        t_used += time.perf_counter() - t0
+        steps += 1
+    return steps, t_used
+
+
+def run_reference(args, wl):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    from oracle import build_ref, reforacle
+    if not reforacle.available():
+        if build_ref.build() is None:
+            print(json.dumps({"impl": "reference", "unavailable": "reference sources not present to build oracle/_ref"}))
+            return 0
+    g = wl["mesh"]()
+    cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+    kind, rho, E, nu, thr = wl["material"]
+    s = reforacle.RefScene(g.X, g.tets, g.facets, cd, kind, rho, E, nu, thr)
+    s.nm_setup(wl["dt"], wl["alpha_m"], wl["beta_k"], newton=wl["newton"], tol=wl["tol"], maxit=5000,
+               precond="jacobi")
+    t = 0.0
+    groups = traction_groups(g, wl["traction"])
+
+    def one():
+        nonlocal t
+        t += wl["dt"]
+        scale = math.sin(2 * math.pi * wl["freq"] * t) if wl["freq"] else 1.0
+        s.loads(body=wl["body"], tractions=[(np.array(tr) * scale, fac) for tr, fac in groups])
+        s.nm_apply_loads()
+        return s.nm_step(1)
+
+    for _ in range(args.warmup):
+        one()
+    t0 = time.perf_counter()
+    iters = 0
+    for _ in range(args.steps):
+        iters += one()
+    el = time.perf_counter() - t0
+    v = args.steps / el
+    line = {"metric": "newmark_steps_per_s", "value": v, "unit": "steps/s", "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * el / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": args.workload, "n_tets": g.n_tets, "precond": "jacobi (reference)",
+                       "pcg_iterations_per_step": iters / args.steps},
+            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "reference",
+                             "sample": f"{args.steps} Newmark steps after {args.warmup} warm-up, single thread "
+                                       "(the reference has no threading)"},
+            "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args, wl):
+    import torch
+    from opendeformer_gb300 import api
+
+    rank, world, local_rank = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist = dist_mod
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local_rank)
+    g = wl["mesh"]()
+    cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+    kind, rho, E, nu, thr = wl["material"]
+    ctx = api.Context(local_rank)
+    scene = api.Scene(ctx, g.X, g.tets, g.facets, cd, api.Material(kind, rho, E, nu, thr))
+    solver = api.CGSolver(wl["tol"], 5000, api.Preconditioner(args.precond), precision=args.precision)
+    integ = api.NewmarkIntegrator(0.25, 0.5, wl["alpha_m"], wl["beta_k"], wl["dt"], solver, wl["newton"])
+    scene.setup_integrator(integ)
+    groups = traction_groups(g, wl["traction"])
+    scene.set_loads(body=wl["body"], tractions=groups)
+    if wl["freq"]:
+        scene.set_traction_schedule(wl["freq"])
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        st = scene.step(1)
+        if st.status not in (0, 3):
+            raise RuntimeError(f"step failed with status {st.status}")
+    flush.zero_()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    ctx.reset_counters()
+    ctx.set_profiling(True)
+    dev_ms, iters, solves, worst = 0.0, 0, 0, 0.0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = scene.step(1)
+        dev_ms += st.device_ms
+        iters += st.pcg_iterations
+        solves += st.solves
+        worst = max(worst, st.max_rel_residual)
+        flush.zero_()          # L2 flush between timed steps (outside the step's events)
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ctx.set_profiling(False)
+    counters = ctx.counters()
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    total_ms = dev_ms
+    if dist:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * args.steps / (total_ms / 1000.0)
+
+    # end to end through the public API with host buffers: per step the
+    # traction arrays go host->device (pinned), the displacement field comes back
+    e2e = None
+    if not args.no_e2e:
+        fac = groups[0][1] if groups else np.zeros(0, np.int32)
+        ids_h = torch.from_numpy(np.ascontiguousarray(fac, dtype=np.int32)).pin_memory()
+        u_h = torch.empty((g.n_nodes, 3), dtype=torch.float64).pin_memory()
+        scene.set_traction_schedule(0.0)
+        h2d = ids_h.numel() * 4 + 3 * 8 + 4 + (24 if wl["body"] else 0)
+        d2h = u_h.numel() * 8
+        tt = scene_time = (args.warmup + args.steps) * wl["dt"]
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for _ in range(args.steps):
+            tt += wl["dt"]
+            scale = math.sin(2 * math.pi * wl["freq"] * tt) if wl["freq"] else 1.0
+            ids = ids_h.numpy()
+            tr = [([0.0, -wl["traction"] * scale, 0.0], ids)] if groups else []
+            scene.set_loads(body=wl["body"], tractions=tr)
+            scene.step(1)
+            api._check(api.load_library().od_scene_get_displacements(
+                scene.h, u_h.numpy().ctypes.data_as(api._dp)), "get_displacements")
+        e2e_wall = time.perf_counter() - t1
+        del scene_time
+        e2e_v = args.steps / e2e_wall
+        if dist:
+            t = torch.tensor([e2e_wall], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_v = world * args.steps / float(t.item())
+        e2e = {"value": e2e_v, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    info = scene.info
+    peak, peak_kind = peaks()
+    if counters.pcg_launches:
+        # persistent PCG solve kernel: one launch per linear solve
+        per_iter = pcg_iteration_bytes(info, args.precond)
+        init = spmv_bytes(info) + 6 * 8 * info.dofs
+        avg_iters = counters.pcg_iterations / counters.pcg_launches
+        nbytes = init + avg_iters * per_iter
+        avg_ms = counters.pcg_ms / counters.pcg_launches
+        kname = "pcg_persistent_kernel<double> (whole FP64 PCG solve, one cooperative launch)"
+        kms, kl = counters.pcg_ms, counters.pcg_launches
+        tkey = "pcg_persistent_kernel"
+    else:
+        nbytes = spmv_bytes(info)
+        avg_ms = counters.spmv_ms / max(1, counters.spmv_launches)
+        kname = "pcg_spmv_kernel<double> (full-BSR FP64 SpMV + p.q)"
+        kms, kl = counters.spmv_ms, counters.spmv_launches
+        tkey = "pcg_spmv_kernel"
+    achieved = nbytes / (avg_ms * 1e-3) / 1e9 if kl else None
+    traffic = traffic_from_profiles(args.workload, tkey)
+    roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "peak_source": peak_kind, "algorithmic_bytes_per_launch": nbytes,
+                "avg_launch_ms": avg_ms, "launches": kl,
+                "share_of_step_time": kms / total_ms if total_ms else None,
+                "note": "FP64 on GB300 runs at about one operation per SM per cycle: the FP64 solve is bound "
+                        "by the FP64 pipe, not HBM, and the 98k-tet system (18.6 MB) stays L2-resident"}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            n, secs = cpu_reference_sample(wl)
+            cpu = {"value": n / secs, "unit": "steps/s", "cores": 1, "kind": "reference",
+                   "sample": f"{n} Newmark steps of the same workload, reference CPU code (Jacobi PCG), "
+                             f"single thread, {secs:.1f} s"}
+        except Exception as exc:
+            cpu = {"value": None, "unit": "steps/s", "cores": 1, "kind": "reference", "sample": f"failed: {exc}"}
+    if rank == 0:
+        line = {"metric": "newmark_steps_per_s", "value": value, "unit": "steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32/f64",
+                "data": "synthetic",
+                "config": {"workload": args.workload, "n_tets": g.n_tets, "n_nodes": g.n_nodes,
+                           "dofs": info.dofs, "precond": args.precond, "precision": args.precision,
+                           "newton_iters": wl["newton"], "dt": wl["dt"], "tol": wl["tol"],
+                           "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                           "l2": "flushed between timed steps (256 MiB write, outside the step events)",
+                           "pcg_iterations_per_step": iters / args.steps,
+                           "solves_per_step": solves / args.steps, "max_rel_residual": worst,
+                           "wall_s_timed_region": wall},
+                "e2e": e2e, "gpu_launches": counters.kernel_launches, "clocks": clocks, "roofline": roofline,
+                "cpu_baseline": cpu}
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="beam98k_nh_newmark")
+    ap.add_argument("--precond", choices=["block_jacobi", "ic0", "jacobi", "none"], default="block_jacobi")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, wl)
+    return run_gpu(args, wl)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

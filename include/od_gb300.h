@@ -112,7 +112,19 @@ typedef struct od_step_stats {
   int solves;
   double max_rel_residual;
   int status;
+  double device_ms;      /* CUDA-event time on the context stream, first launch to last */
 } od_step_stats;
+
+/* Launch and timing counters of a context (no reference counterpart). */
+typedef struct od_counters {
+  long long kernel_launches;  /* every kernel this library launched */
+  long long host_syncs;       /* stream synchronisations inside library calls */
+  long long spmv_launches;    /* PCG SpMV launches timed while profiling is on */
+  double spmv_ms;             /* their summed CUDA-event durations */
+  long long pcg_launches;     /* persistent (one-launch) PCG solves timed while profiling */
+  long long pcg_iterations;   /* their iterations */
+  double pcg_ms;              /* their summed CUDA-event durations */
+} od_counters;
 
 typedef struct od_scene_info {
   int n_nodes, n_tets, n_facets;
@@ -138,6 +150,11 @@ int od_abi_version(void);
 od_status od_ctx_create(int device, od_ctx** out);
 od_status od_ctx_destroy(od_ctx* ctx);
 od_status od_ctx_synchronize(od_ctx* ctx);
+/* Counters (no reference counterpart).  With profiling on, every PCG SpMV
+ * launch is bracketed by CUDA events on the context stream. */
+od_status od_ctx_set_profiling(od_ctx* ctx, int enable);
+od_status od_ctx_get_counters(od_ctx* ctx, od_counters* out);
+od_status od_ctx_reset_counters(od_ctx* ctx);
 
 /* Scene = TetMesh + Constrainer/NodeIndexer + material + pattern + caches.
  * Replaces TetMesh(numN, numE, numS) + setVertex/setElement/setFacet
@@ -192,6 +209,17 @@ od_status od_scene_pcg(od_scene* scene, const double* values, const double* b, d
 od_status od_scene_set_loads(od_scene* scene, const double* body, int n_groups,
                              const double* tractions, const int* group_sizes,
                              const int* facet_ids);
+/* Re-evaluates the loads of the last od_scene_set_loads at the current
+ * displacement with every traction scaled by traction_scale, on the device
+ * (the per-step Forcer rebuild of a time-varying traction, without host
+ * copies). */
+od_status od_scene_update_loads(od_scene* scene, double traction_scale);
+/* Time-varying traction: when frequency_hz > 0 every od_step step first
+ * re-evaluates the loads (as od_scene_update_loads) with the tractions scaled
+ * by sin(2 pi frequency_hz t + phase), t the end time of that step -- the
+ * per-step Forcer rebuild of a periodic surface load.  frequency_hz = 0 turns
+ * it off (loads stay frozen). */
+od_status od_scene_set_traction_schedule(od_scene* scene, double frequency_hz, double phase);
 od_status od_scene_set_external_forces(od_scene* scene, const double* f_ext);
 od_status od_scene_get_external_forces(od_scene* scene, double* f_ext);
 

@@ -23,9 +23,11 @@ fallback: if the library is missing, loading raises.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import dataclasses
 import os
+import weakref
 
 import numpy as np
 
@@ -71,7 +73,13 @@ class od_integrator_params(C.Structure):
 
 class od_step_stats(C.Structure):
     _fields_ = [("steps", C.c_int), ("pcg_iterations", C.c_int), ("solves", C.c_int),
-                ("max_rel_residual", C.c_double), ("status", C.c_int)]
+                ("max_rel_residual", C.c_double), ("status", C.c_int), ("device_ms", C.c_double)]
+
+
+class od_counters(C.Structure):
+    _fields_ = [("kernel_launches", C.c_longlong), ("host_syncs", C.c_longlong),
+                ("spmv_launches", C.c_longlong), ("spmv_ms", C.c_double),
+                ("pcg_launches", C.c_longlong), ("pcg_iterations", C.c_longlong), ("pcg_ms", C.c_double)]
 
 
 class od_scene_info(C.Structure):
@@ -86,6 +94,28 @@ _ip = C.POINTER(C.c_int)
 _vp = C.c_void_p
 _lib = None
 
+# Live handles, released in a safe order (scenes before contexts) when the
+# interpreter exits, before the CUDA runtime itself is torn down.
+_live_scenes: "weakref.WeakSet" = weakref.WeakSet()
+_live_ctxs: "weakref.WeakSet" = weakref.WeakSet()
+_shutting_down = False
+
+
+@atexit.register
+def _release_all():
+    global _shutting_down
+    for sc in list(_live_scenes):
+        try:
+            sc.close()
+        except Exception:
+            pass
+    for cx in list(_live_ctxs):
+        try:
+            cx.close()
+        except Exception:
+            pass
+    _shutting_down = True
+
 # name -> (restype, argtypes); every entry point of include/od_gb300.h
 SIGNATURES = {
     "od_status_string": (C.c_char_p, [C.c_int]),
@@ -94,6 +124,9 @@ SIGNATURES = {
     "od_ctx_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),
     "od_ctx_destroy": (C.c_int, [_vp]),
     "od_ctx_synchronize": (C.c_int, [_vp]),
+    "od_ctx_set_profiling": (C.c_int, [_vp, C.c_int]),
+    "od_ctx_get_counters": (C.c_int, [_vp, C.POINTER(od_counters)]),
+    "od_ctx_reset_counters": (C.c_int, [_vp]),
     "od_scene_create": (C.c_int, [_vp, C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip,
                                   C.POINTER(od_material), C.POINTER(_vp)]),
     "od_scene_destroy": (C.c_int, [_vp]),
@@ -108,6 +141,8 @@ SIGNATURES = {
     "od_scene_spmdv": (C.c_int, [_vp, _dp, _dp, _dp]),
     "od_scene_pcg": (C.c_int, [_vp, _dp, _dp, _dp, C.POINTER(od_solver_params), C.POINTER(od_solve_stats)]),
     "od_scene_set_loads": (C.c_int, [_vp, _dp, C.c_int, _dp, _ip, _ip]),
+    "od_scene_update_loads": (C.c_int, [_vp, C.c_double]),
+    "od_scene_set_traction_schedule": (C.c_int, [_vp, C.c_double, C.c_double]),
     "od_scene_set_external_forces": (C.c_int, [_vp, _dp]),
     "od_scene_get_external_forces": (C.c_int, [_vp, _dp]),
     "od_integrator_setup": (C.c_int, [_vp, C.POINTER(od_integrator_params)]),
@@ -243,14 +278,26 @@ class Context:
         h = _vp()
         _check(L.od_ctx_create(device, C.byref(h)), "od_ctx_create")
         self.h = h
+        _live_ctxs.add(self)
 
     def synchronize(self):
         _check(load_library().od_ctx_synchronize(self.h), "od_ctx_synchronize")
 
+    def set_profiling(self, enable: bool):
+        _check(load_library().od_ctx_set_profiling(self.h, 1 if enable else 0), "od_ctx_set_profiling")
+
+    def counters(self):
+        c = od_counters()
+        _check(load_library().od_ctx_get_counters(self.h, C.byref(c)), "od_ctx_get_counters")
+        return c
+
+    def reset_counters(self):
+        _check(load_library().od_ctx_reset_counters(self.h), "od_ctx_reset_counters")
+
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and not _shutting_down:
             load_library().od_ctx_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -276,6 +323,7 @@ class Scene:
                                  self.facets.shape[0], _i(self.facets), self.cdofs.size, _i(self.cdofs),
                                  C.byref(m), C.byref(h)), "od_scene_create")
         self.h = h
+        _live_scenes.add(self)
         self.info = od_scene_info()
         _check(L.od_scene_get_info(self.h, C.byref(self.info)), "od_scene_get_info")
         self.dofs = self.info.dofs
@@ -283,9 +331,9 @@ class Scene:
         self.n_tets = self.info.n_tets
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and not _shutting_down:
             load_library().od_scene_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -375,6 +423,15 @@ class Scene:
         _check(load_library().od_scene_set_loads(self.h, None if b is None else _d(b), ng, _d(tv), _i(sizes),
                                                  _i(ids)), "set_loads")
 
+    def update_loads(self, traction_scale: float):
+        """Re-evaluate the stored loads on the device with scaled tractions."""
+        _check(load_library().od_scene_update_loads(self.h, float(traction_scale)), "update_loads")
+
+    def set_traction_schedule(self, frequency_hz: float, phase: float = 0.0):
+        """Scale tractions by sin(2 pi f t + phase) at the start of every step."""
+        _check(load_library().od_scene_set_traction_schedule(self.h, float(frequency_hz), float(phase)),
+               "set_traction_schedule")
+
     def set_external_forces(self, f):
         f = np.ascontiguousarray(f, dtype=np.float64)
         _check(load_library().od_scene_set_external_forces(self.h, _d(f)), "set_external_forces")
@@ -399,7 +456,6 @@ class Scene:
         return d, v, a
 
     def set_state(self, d=None, v=None, a=None):
-        args = [None if x is None else _d(np.ascontiguousarray(x, dtype=np.float64)) for x in (d, v, a)]
         keep = [np.ascontiguousarray(x, dtype=np.float64) if x is not None else None for x in (d, v, a)]
         args = [None if k is None else _d(k) for k in keep]
         _check(load_library().od_set_state(self.h, *args), "set_state")

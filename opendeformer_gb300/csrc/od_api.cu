@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <stdexcept>
@@ -24,6 +25,12 @@ od_status cuda_fail(cudaError_t e, const char* what) {
 }
 
 static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+
+od_status sync_stream(Scene* s) {
+  s->ctx->host_syncs++;
+  OD_CUDA(cudaStreamSynchronize(s->ctx->stream));
+  return OD_OK;
+}
 
 // ------------------------------------------------------ integrator kernels
 // u[free_pos[i]] = v[i] (mode 0) or += h v[i] (mode 1)
@@ -110,11 +117,6 @@ struct od_scene {
     }                                        \
   } while (0)
 
-#define OD_TRY(expr)                 \
-  do {                               \
-    od_status _st = (expr);          \
-    if (_st != OD_OK) return _st;    \
-  } while (0)
 
 template <class T>
 static od_status dalloc(Scene* s, T** p, size_t n) {
@@ -172,7 +174,39 @@ od_status od_ctx_destroy(od_ctx* ctx) {
   cudaSetDevice(ctx->c.device);
   cudaStreamSynchronize(ctx->c.stream);
   cudaStreamDestroy(ctx->c.stream);
+  for (auto& e : ctx->c.ev_pool) cudaEventDestroy(e);
   delete ctx;
+  return OD_OK;
+}
+
+od_status od_ctx_set_profiling(od_ctx* ctx, int enable) {
+  OD_CHECK_ARG(ctx, "od_ctx_set_profiling: ctx is NULL");
+  OD_CUDA(cudaSetDevice(ctx->c.device));
+  if (enable && ctx->c.ev_pool.empty()) {
+    ctx->c.ev_pool.resize(2 * 64);
+    for (auto& e : ctx->c.ev_pool) OD_CUDA(cudaEventCreate(&e));
+  }
+  ctx->c.profiling = enable ? 1 : 0;
+  return OD_OK;
+}
+
+od_status od_ctx_get_counters(od_ctx* ctx, od_counters* out) {
+  OD_CHECK_ARG(ctx && out, "od_ctx_get_counters: NULL argument");
+  out->kernel_launches = ctx->c.launches;
+  out->host_syncs = ctx->c.host_syncs;
+  out->spmv_launches = ctx->c.spmv_launches;
+  out->spmv_ms = ctx->c.spmv_ms;
+  out->pcg_launches = ctx->c.pcg_kernel_launches;
+  out->pcg_iterations = ctx->c.pcg_kernel_iters;
+  out->pcg_ms = ctx->c.pcg_kernel_ms;
+  return OD_OK;
+}
+
+od_status od_ctx_reset_counters(od_ctx* ctx) {
+  OD_CHECK_ARG(ctx, "od_ctx_reset_counters: ctx is NULL");
+  ctx->c.launches = ctx->c.host_syncs = ctx->c.spmv_launches = 0;
+  ctx->c.pcg_kernel_launches = ctx->c.pcg_kernel_iters = 0;
+  ctx->c.spmv_ms = ctx->c.pcg_kernel_ms = 0.0;
   return OD_OK;
 }
 
@@ -192,9 +226,11 @@ static void scene_free(Scene* s) {
                   (void*)s->A64, (void*)s->A32, (void*)s->v, (void*)s->d, (void*)s->a, (void*)s->dp, (void*)s->vp,
                   (void*)s->dv, (void*)s->rhs, (void*)s->tmp, (void*)s->trac_facets, (void*)s->trac_vec,
                   (void*)s->bsr.row_ptr, (void*)s->bsr.col, (void*)s->bsr.desc_off, (void*)s->bsr.desc_kind,
-                  (void*)s->bsr.gen, (void*)s->bsr.diag_pos, (void*)s->tmp2})
+                  (void*)s->bsr.gen, (void*)s->bsr.diag_pos, (void*)s->tmp2, (void*)s->stage_k,
+                  (void*)s->stage_f})
     if (p) cudaFree(p);
   pcg_free(s);
+  if (s->ev_step[0]) { cudaEventDestroy(s->ev_step[0]); cudaEventDestroy(s->ev_step[1]); }
 }
 
 static od_status scene_build(Scene* s, int n_nodes, const double* X, int n_tets, const int* tets, int n_facets,
@@ -258,6 +294,8 @@ static od_status scene_build(Scene* s, int n_nodes, const double* X, int n_tets,
   OD_TRY(dalloc(s, &s->M, (size_t)s->nvals));
   OD_TRY(dalloc(s, &s->Dm, (size_t)s->nvals));
   OD_TRY(dalloc(s, &s->work_vals, (size_t)s->nvals));
+  OD_TRY(dalloc(s, &s->stage_k, 78 * (size_t)ne));
+  OD_TRY(dalloc(s, &s->stage_f, 12 * (size_t)ne));
   OD_CUDA(cudaMemset(s->K, 0, sizeof(double) * std::max(1, s->nvals)));
   OD_CUDA(cudaMemset(s->Dm, 0, sizeof(double) * std::max(1, s->nvals)));
   s->bsr.nb = hb.nb;
@@ -271,6 +309,8 @@ static od_status scene_build(Scene* s, int n_nodes, const double* X, int n_tets,
   OD_TRY(dupload(s, &s->bsr.diag_pos, hb.diag_pos.data(), hb.diag_pos.size()));
   OD_TRY(dalloc(s, &s->A64, 9 * (size_t)s->bsr.nnzb));
   OD_TRY(pcg_alloc(s));
+  // OD_GB300_PCG_PERSISTENT=0 selects the multi-kernel PCG for every preconditioner
+  if (const char* e = std::getenv("OD_GB300_PCG_PERSISTENT")) s->pcg.disable_persistent = (e[0] == '0');
   const size_t np = (size_t)std::max(1, s->pcg.n_pad);
   for (double** v : {&s->fint, &s->fext, &s->v, &s->d, &s->a, &s->dp, &s->vp, &s->dv, &s->rhs, &s->tmp, &s->tmp2}) {
     OD_TRY(dalloc(s, v, np));
@@ -278,7 +318,7 @@ static od_status scene_build(Scene* s, int n_nodes, const double* X, int n_tets,
   }
   OD_TRY(launch_precompute(s));
   OD_TRY(launch_mass(s));
-  OD_CUDA(cudaStreamSynchronize(s->ctx->stream));
+  OD_TRY(sync_stream(s));
   return OD_OK;
 }
 
@@ -372,7 +412,7 @@ od_status od_scene_set_displacements(od_scene* scene, const double* u) {
   Scene* s = &scene->s;
   OD_CUDA(cudaSetDevice(s->ctx->device));
   OD_CUDA(cudaMemcpyAsync(s->u, u, sizeof(double) * 3 * (size_t)s->n_nodes, cudaMemcpyHostToDevice, s->ctx->stream));
-  OD_CUDA(cudaStreamSynchronize(s->ctx->stream));
+  OD_TRY(sync_stream(s));
   return OD_OK;
 }
 
@@ -381,7 +421,7 @@ od_status od_scene_get_displacements(od_scene* scene, double* u) {
   Scene* s = &scene->s;
   OD_CUDA(cudaSetDevice(s->ctx->device));
   OD_CUDA(cudaMemcpyAsync(u, s->u, sizeof(double) * 3 * (size_t)s->n_nodes, cudaMemcpyDeviceToHost, s->ctx->stream));
-  OD_CUDA(cudaStreamSynchronize(s->ctx->stream));
+  OD_TRY(sync_stream(s));
   return OD_OK;
 }
 
@@ -401,7 +441,7 @@ od_status od_scene_evaluate(od_scene* scene, double* values, double* f_int) {
   OD_TRY(launch_eval(s, true));
   if (values) OD_CUDA(cudaMemcpyAsync(values, s->K, sizeof(double) * s->nvals, cudaMemcpyDeviceToHost, s->ctx->stream));
   if (f_int) OD_CUDA(cudaMemcpyAsync(f_int, s->fint, sizeof(double) * s->dofs, cudaMemcpyDeviceToHost, s->ctx->stream));
-  OD_CUDA(cudaStreamSynchronize(s->ctx->stream));
+  OD_TRY(sync_stream(s));
   return OD_OK;
 }
 
@@ -430,7 +470,7 @@ od_status od_scene_mass(od_scene* scene, double* values) {
   Scene* s = &scene->s;
   OD_CUDA(cudaSetDevice(s->ctx->device));
   OD_CUDA(cudaMemcpyAsync(values, s->M, sizeof(double) * s->nvals, cudaMemcpyDeviceToHost, s->ctx->stream));
-  OD_CUDA(cudaStreamSynchronize(s->ctx->stream));
+  OD_TRY(sync_stream(s));
   return OD_OK;
 }
 
@@ -444,7 +484,7 @@ od_status od_scene_spmdv(od_scene* scene, const double* values, const double* x,
   OD_CUDA(cudaMemcpyAsync(s->tmp2, y, sizeof(double) * s->dofs, cudaMemcpyHostToDevice, st));
   OD_TRY(launch_spmv_lower(s, s->work_vals, 1.0, s->tmp, nullptr, 0.0, nullptr, nullptr, 0.0, nullptr, s->tmp2, true));
   OD_CUDA(cudaMemcpyAsync(y, s->tmp2, sizeof(double) * s->dofs, cudaMemcpyDeviceToHost, st));
-  OD_CUDA(cudaStreamSynchronize(st));
+  OD_TRY(sync_stream(s));
   return OD_OK;
 }
 
@@ -470,7 +510,7 @@ od_status od_scene_pcg(od_scene* scene, const double* values, const double* b, d
   od_solve_stats ls{};
   OD_TRY(pcg_solve(s, s->rhs, s->dv, params, &ls));
   OD_CUDA(cudaMemcpyAsync(x, s->dv, sizeof(double) * s->dofs, cudaMemcpyDeviceToHost, st));
-  OD_CUDA(cudaStreamSynchronize(st));
+  OD_TRY(sync_stream(s));
   if (stats) *stats = ls;
   return (od_status)ls.status == OD_ERR_NAN ? OD_ERR_NAN : OD_OK;
 }
@@ -517,8 +557,27 @@ od_status od_scene_set_loads(od_scene* scene, const double* body, int n_groups, 
     OD_CUDA(cudaMemcpyAsync(s->trac_facets, fo.data(), sizeof(int) * nf, cudaMemcpyHostToDevice, s->ctx->stream));
     OD_CUDA(cudaMemcpyAsync(s->trac_vec, to.data(), sizeof(double) * 3 * nf, cudaMemcpyHostToDevice, s->ctx->stream));
   }
-  OD_TRY(launch_loads(s, body, nf));
-  OD_CUDA(cudaStreamSynchronize(s->ctx->stream));
+  s->n_trac = nf;
+  s->has_body = body != nullptr;
+  if (body) for (int i = 0; i < 3; i++) s->load_body[i] = body[i];
+  OD_TRY(launch_loads(s, body, nf, 1.0));
+  OD_TRY(sync_stream(s));
+  return OD_OK;
+}
+
+od_status od_scene_update_loads(od_scene* scene, double traction_scale) {
+  OD_CHECK_ARG(scene, "od_scene_update_loads: scene is NULL");
+  Scene* s = &scene->s;
+  OD_CUDA(cudaSetDevice(s->ctx->device));
+  OD_TRY(launch_loads(s, s->has_body ? s->load_body : nullptr, s->n_trac, traction_scale));
+  return OD_OK;
+}
+
+od_status od_scene_set_traction_schedule(od_scene* scene, double frequency_hz, double phase) {
+  OD_CHECK_ARG(scene, "od_scene_set_traction_schedule: scene is NULL");
+  OD_CHECK_ARG(frequency_hz >= 0.0, "od_scene_set_traction_schedule: negative frequency");
+  scene->s.sched_freq = frequency_hz;
+  scene->s.sched_phase = phase;
   return OD_OK;
 }
 
@@ -527,7 +586,7 @@ od_status od_scene_set_external_forces(od_scene* scene, const double* f_ext) {
   Scene* s = &scene->s;
   OD_CUDA(cudaSetDevice(s->ctx->device));
   OD_CUDA(cudaMemcpyAsync(s->fext, f_ext, sizeof(double) * s->dofs, cudaMemcpyHostToDevice, s->ctx->stream));
-  OD_CUDA(cudaStreamSynchronize(s->ctx->stream));
+  OD_TRY(sync_stream(s));
   return OD_OK;
 }
 
@@ -536,7 +595,7 @@ od_status od_scene_get_external_forces(od_scene* scene, double* f_ext) {
   Scene* s = &scene->s;
   OD_CUDA(cudaSetDevice(s->ctx->device));
   OD_CUDA(cudaMemcpyAsync(f_ext, s->fext, sizeof(double) * s->dofs, cudaMemcpyDeviceToHost, s->ctx->stream));
-  OD_CUDA(cudaStreamSynchronize(s->ctx->stream));
+  OD_TRY(sync_stream(s));
   return OD_OK;
 }
 
@@ -555,7 +614,7 @@ od_status od_integrator_setup(od_scene* scene, const od_integrator_params* p) {
   s->time = 0.0;
   const size_t np = sizeof(double) * (size_t)std::max(1, s->pcg.n_pad);
   for (double* v : {s->v, s->d, s->a, s->dp, s->vp, s->dv}) OD_CUDA(cudaMemsetAsync(v, 0, np, s->ctx->stream));
-  OD_CUDA(cudaStreamSynchronize(s->ctx->stream));
+  OD_TRY(sync_stream(s));
   return OD_OK;
 }
 
@@ -569,12 +628,15 @@ static od_status be_step(Scene* s, od_step_stats* acc) {
   OD_TRY(launch_eval(s, true));
   // A0 v with A0 = (h + beta_K) K + alpha_M M + D
   OD_TRY(launch_spmv_lower(s, s->K, h + p.beta_k, s->v, s->M, p.alpha_m, s->v, s->Dm, 1.0, s->v, s->tmp, false));
+  OD_KL(s);
   be_rhs_kernel<<<nblk(n, T), T, 0, st>>>(n, h, s->fext, s->fint, s->tmp, s->rhs);
   // A = h A0 + M
   OD_TRY(launch_expand(s, s->K, h * (h + p.beta_k), s->M, h * p.alpha_m + 1.0, s->Dm, h));
   od_solve_stats ss{};
   OD_TRY(pcg_solve(s, s->rhs, s->dv, &p.solver, &ss));
+  OD_KL(s);
   add_kernel<<<nblk(n, T), T, 0, st>>>(n, s->dv, s->v);
+  OD_KL(s);
   write_mesh_kernel<<<nblk(n, T), T, 0, st>>>(n, s->free_pos, s->v, h, 1, s->u);
   OD_CUDA(cudaGetLastError());
   acc->pcg_iterations += ss.iterations;
@@ -592,20 +654,24 @@ static od_status nm_step(Scene* s, od_step_stats* acc) {
   const int n = s->dofs, T = 256;
   cudaStream_t st = s->ctx->stream;
   const double h = p.dt, bh2 = p.nm_beta * h * h, gh = p.nm_gamma * h;
+  OD_KL(s);
   nm_predict_kernel<<<nblk(n, T), T, 0, st>>>(n, h, (0.5 - p.nm_beta) * h * h, (1.0 - p.nm_gamma) * h, s->d, s->v,
                                               s->a, s->dp, s->vp);
   for (int it = 0; it < p.newton_iters; it++) {
+    OD_KL(s);
     nm_stage_kernel<<<nblk(n, T), T, 0, st>>>(n, s->free_pos, bh2, gh, p.alpha_m, s->dp, s->vp, s->a, s->u, s->tmp,
                                               s->tmp2);
     OD_TRY(launch_eval(s, true));
     // y = M (alpha_M v_k + a_k) + beta_K K v_k (+ D v_k)
     OD_TRY(launch_spmv_lower(s, s->M, 1.0, s->tmp, s->K, p.beta_k, s->tmp2, s->Dm, 1.0, s->tmp2, s->rhs, false));
+    OD_KL(s);
     nm_residual_kernel<<<nblk(n, T), T, 0, st>>>(n, s->fext, s->fint, s->rhs, s->rhs);
     // A = (1 + gamma h alpha_M) M + (gamma h beta_K + beta h^2) K + gamma h D
     OD_TRY(launch_expand(s, s->K, gh * p.beta_k + bh2, s->M, 1.0 + gh * p.alpha_m, s->Dm, gh));
     OD_CUDA(cudaMemsetAsync(s->dv, 0, sizeof(double) * (size_t)s->pcg.n_pad, st));
     od_solve_stats ss{};
     OD_TRY(pcg_solve(s, s->rhs, s->dv, &p.solver, &ss));
+    OD_KL(s);
     add_kernel<<<nblk(n, T), T, 0, st>>>(n, s->dv, s->a);
     acc->pcg_iterations += ss.iterations;
     acc->solves += 1;
@@ -613,6 +679,7 @@ static od_status nm_step(Scene* s, od_step_stats* acc) {
     if (ss.status == OD_ERR_NAN) return OD_ERR_NAN;
     if (ss.status != OD_OK && acc->status == OD_OK) acc->status = ss.status;
   }
+  OD_KL(s);
   nm_correct_kernel<<<nblk(n, T), T, 0, st>>>(n, s->free_pos, bh2, gh, s->dp, s->vp, s->a, s->d, s->v, s->u);
   OD_CUDA(cudaGetLastError());
   return OD_OK;
@@ -626,12 +693,27 @@ od_status od_step(od_scene* scene, int n_steps, od_step_stats* stats) {
   OD_CUDA(cudaSetDevice(s->ctx->device));
   od_step_stats acc{};
   od_status st = OD_OK;
+  if (!s->ev_step[0]) {
+    OD_CUDA(cudaEventCreate(&s->ev_step[0]));
+    OD_CUDA(cudaEventCreate(&s->ev_step[1]));
+  }
+  OD_CUDA(cudaEventRecord(s->ev_step[0], s->ctx->stream));
   for (int k = 0; k < n_steps && st == OD_OK; k++) {
+    if (s->sched_freq > 0.0) {
+      const double t = s->time + s->ip.dt;
+      st = launch_loads(s, s->has_body ? s->load_body : nullptr, s->n_trac,
+                        std::sin(2.0 * 3.14159265358979323846 * s->sched_freq * t + s->sched_phase));
+      if (st != OD_OK) break;
+    }
     st = s->ip.kind == OD_INTEGRATOR_NEWMARK ? nm_step(s, &acc) : be_step(s, &acc);
     if (st == OD_OK) { acc.steps++; s->time += s->ip.dt; }
   }
+  cudaEventRecord(s->ev_step[1], s->ctx->stream);
+  s->ctx->host_syncs++;
   cudaError_t e = cudaStreamSynchronize(s->ctx->stream);
   if (e != cudaSuccess && st == OD_OK) st = cuda_fail(e, "od_step");
+  float ms = 0.f;
+  if (st == OD_OK && cudaEventElapsedTime(&ms, s->ev_step[0], s->ev_step[1]) == cudaSuccess) acc.device_ms = ms;
   if (st != OD_OK && acc.status == OD_OK) acc.status = st;
   if (stats) *stats = acc;
   return st;
@@ -646,7 +728,7 @@ od_status od_get_state(od_scene* scene, double* d, double* v, double* a) {
   if (d) OD_CUDA(cudaMemcpyAsync(d, s->d, nb, cudaMemcpyDeviceToHost, st));
   if (v) OD_CUDA(cudaMemcpyAsync(v, s->v, nb, cudaMemcpyDeviceToHost, st));
   if (a) OD_CUDA(cudaMemcpyAsync(a, s->a, nb, cudaMemcpyDeviceToHost, st));
-  OD_CUDA(cudaStreamSynchronize(st));
+  OD_TRY(sync_stream(s));
   return OD_OK;
 }
 
@@ -659,7 +741,7 @@ od_status od_set_state(od_scene* scene, const double* d, const double* v, const 
   if (d) OD_CUDA(cudaMemcpyAsync(s->d, d, nb, cudaMemcpyHostToDevice, st));
   if (v) OD_CUDA(cudaMemcpyAsync(s->v, v, nb, cudaMemcpyHostToDevice, st));
   if (a) OD_CUDA(cudaMemcpyAsync(s->a, a, nb, cudaMemcpyHostToDevice, st));
-  OD_CUDA(cudaStreamSynchronize(st));
+  OD_TRY(sync_stream(s));
   return OD_OK;
 }
 
@@ -685,7 +767,7 @@ od_status od_scene_save(od_scene* scene, void* buf, size_t* size) {
     OD_CUDA(cudaMemcpyAsync(p, v, sizeof(double) * s->dofs, cudaMemcpyDeviceToHost, st));
     p += s->dofs;
   }
-  OD_CUDA(cudaStreamSynchronize(st));
+  OD_TRY(sync_stream(s));
   *size = need;
   return OD_OK;
 }
@@ -709,7 +791,7 @@ od_status od_scene_load(od_scene* scene, const void* buf, size_t size) {
     OD_CUDA(cudaMemcpyAsync(v, p, sizeof(double) * s->dofs, cudaMemcpyHostToDevice, st));
     p += s->dofs;
   }
-  OD_CUDA(cudaStreamSynchronize(st));
+  OD_TRY(sync_stream(s));
   return OD_OK;
 }
 

@@ -135,7 +135,7 @@ __global__ void body_force_kernel(int n, const int* __restrict__ free_pos, const
 // uniform traction over deformed facets, area / 3 per vertex
 // (TetFacet::getSurfVirtualWorks, tetelement.cpp:79-89); one facet colour
 __global__ void traction_kernel(int f0, int f1, const int* __restrict__ fids, const double* __restrict__ tvec,
-                                const int* __restrict__ facets, const double* __restrict__ X,
+                                double scale, const int* __restrict__ facets, const double* __restrict__ X,
                                 const double* __restrict__ u, const int* __restrict__ node_dof,
                                 double* __restrict__ fext) {
   int k = f0 + blockIdx.x * blockDim.x + threadIdx.x;
@@ -151,7 +151,7 @@ __global__ void traction_kernel(int f0, int f1, const int* __restrict__ fids, co
   double fac = area / 3.0;
   for (int i = 0; i < 3; i++)
     for (int ax = 0; ax < 3; ax++) {
-      double w = fac * tvec[3 * k + ax];
+      double w = fac * (scale * tvec[3 * k + ax]);
       int g = node_dof[3 * n[i] + ax];
       if (w != 0.0 && g >= 0) fext[g] += w;
     }
@@ -163,7 +163,9 @@ __global__ void traction_kernel(int f0, int f1, const int* __restrict__ fids, co
 // (tetelement.cpp:546-573); K_ab = R K0_ab R^T packed into 78 values and
 // f_a = sum_b (R K0_ab R^T x_b - R K0_ab X_b) (tetelement.cpp:583-651).
 // MODE 0 scatters into K / fint through the element map (one colour per
-// launch); MODE 1 stores per-element values in original element order.
+// launch); MODE 1 stores per-element values in original element order;
+// MODE 2 stores them in the colour-ordered staging arrays (all elements in
+// one launch, scattered afterwards colour by colour).
 template <int MODE>
 __global__ void __launch_bounds__(128) corot_kernel(int e0, int e1, int ne, const int4* __restrict__ tets,
                                                     const double* __restrict__ X, const double* __restrict__ u,
@@ -208,8 +210,10 @@ __global__ void __launch_bounds__(128) corot_kernel(int e0, int e1, int ne, cons
     if (MODE == 0) {
       int idx = emap[(size_t)k * ne + e];
       if (idx >= 0) K[idx] += val;
-    } else {
+    } else if (MODE == 1) {
       out78[obase + k] = val;
+    } else {
+      out78[(size_t)k * ne + e] = val;
     }
   };
   int blk = 0;
@@ -270,9 +274,12 @@ __global__ void __launch_bounds__(128) corot_kernel(int e0, int e1, int ne, cons
       int g = gdof[(size_t)k * ne + e];
       if (g >= 0) fint[g] += f[k];
     }
-  } else {
+  } else if (MODE == 1) {
 #pragma unroll
     for (int k = 0; k < 12; k++) out12[(size_t)perm[e] * 12 + k] = f[k];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 12; k++) out12[(size_t)k * ne + e] = f[k];
   }
 }
 
@@ -386,8 +393,10 @@ __global__ void __launch_bounds__(128) invhyper_kernel(int e0, int e1, int ne, i
     if (MODE == 0) {
       int idx = emap[(size_t)k * ne + e];
       if (idx >= 0) K[idx] += val;
-    } else {
+    } else if (MODE == 1) {
       out78[obase + k] = val;
+    } else {
+      out78[(size_t)k * ne + e] = val;
     }
   };
 #pragma unroll 1
@@ -447,18 +456,43 @@ __global__ void __launch_bounds__(128) invhyper_kernel(int e0, int e1, int ne, i
       int g = gdof[(size_t)k * ne + e];
       if (g >= 0) fint[g] += f[k];
     }
-  } else {
+  } else if (MODE == 1) {
 #pragma unroll
     for (int k = 0; k < 12; k++) out12[(size_t)perm[e] * 12 + k] = f[k];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 12; k++) out12[(size_t)k * ne + e] = f[k];
+  }
+}
+
+// atomic-free scatter of staged element values, one colour per launch
+// (corotationalHyperelastic.cpp:100-120): no two elements of a colour share
+// a matrix value or a force entry.  One thread per (element, entry): entries
+// 0..77 are stiffness values, 78..89 forces; for a fixed entry consecutive
+// threads read consecutive staged values and map entries.
+__global__ void scatter_kernel(int e0, int cnt, int ne, const double* __restrict__ k78, const double* __restrict__ f12,
+                               const int* __restrict__ emap, const int* __restrict__ gdof, double* __restrict__ K,
+                               double* __restrict__ fint) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 90LL * cnt) return;
+  const int k = (int)(t / cnt);
+  const int e = e0 + (int)(t - (long long)k * cnt);
+  if (k < 78) {
+    const int idx = emap[(size_t)k * ne + e];
+    if (idx >= 0) K[idx] += k78[(size_t)k * ne + e];
+  } else {
+    const int g = gdof[(size_t)(k - 78) * ne + e];
+    if (g >= 0) fint[g] += f12[(size_t)(k - 78) * ne + e];
   }
 }
 
 // ---------------------------------------------------------------- launches
-static inline int nblk(int n, int t) { return (n + t - 1) / t; }
+static inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
 od_status launch_precompute(Scene* s) {
   const int T = 128;
   if (s->n_tets == 0) return OD_OK;
+  OD_KL(s);
   precompute_kernel<<<nblk(s->n_tets, T), T, 0, s->ctx->stream>>>(s->n_tets, s->mat.kind, s->tets, s->X, s->D[0],
                                                                    s->D[1], s->D[2], s->pre);
   OD_CUDA(cudaGetLastError());
@@ -474,8 +508,10 @@ od_status launch_mass(Scene* s) {
   for (size_t c = 0; c + 1 < s->color_off.size(); c++) {
     int e0 = s->color_off[c], e1 = s->color_off[c + 1];
     if (e1 <= e0) continue;
+    OD_KL(s);
     mass_kernel<<<nblk(e1 - e0, T), T, 0, s->ctx->stream>>>(e0, e1, s->n_tets, vol_slot(s), s->mat.density, s->pre,
                                                              s->emap, s->M);
+    OD_KL(s);
     node_vol_kernel<<<nblk(e1 - e0, T), T, 0, s->ctx->stream>>>(e0, e1, s->n_tets, vol_slot(s), s->tets, s->pre,
                                                                  s->node_vol4);
   }
@@ -490,18 +526,25 @@ od_status launch_eval(Scene* s, bool zero_first) {
     OD_CUDA(cudaMemsetAsync(s->K, 0, sizeof(double) * (size_t)s->nvals, st));
     OD_CUDA(cudaMemsetAsync(s->fint, 0, sizeof(double) * (size_t)s->pcg.n_pad, st));
   }
+  if (s->n_tets == 0) return OD_OK;
+  // 1) every element at full occupancy into the colour-ordered staging arrays
+  OD_KL(s);
+  if (s->mat.kind == OD_MATERIAL_COROTATIONAL)
+    corot_kernel<2><<<nblk(s->n_tets, T), T, 0, st>>>(0, s->n_tets, s->n_tets, s->tets, s->X, s->u, s->pre,
+                                                       s->mat.threshold, s->emap, s->gdof, nullptr, nullptr, s->stage_k,
+                                                       s->stage_f, nullptr);
+  else
+    invhyper_kernel<2><<<nblk(s->n_tets, T), T, 0, st>>>(0, s->n_tets, s->n_tets, s->mat.kind == OD_MATERIAL_STVK,
+                                                          s->tets, s->X, s->u, s->pre, s->mat.threshold, s->lambda,
+                                                          s->mu, s->emap, s->gdof, nullptr, nullptr, s->stage_k,
+                                                          s->stage_f, nullptr);
+  // 2) atomic-free scatter, one colour per launch
   for (size_t c = 0; c + 1 < s->color_off.size(); c++) {
     int e0 = s->color_off[c], e1 = s->color_off[c + 1];
     if (e1 <= e0) continue;
-    if (s->mat.kind == OD_MATERIAL_COROTATIONAL)
-      corot_kernel<0><<<nblk(e1 - e0, T), T, 0, st>>>(e0, e1, s->n_tets, s->tets, s->X, s->u, s->pre,
-                                                       s->mat.threshold, s->emap, s->gdof, s->K, s->fint, nullptr,
-                                                       nullptr, nullptr);
-    else
-      invhyper_kernel<0><<<nblk(e1 - e0, T), T, 0, st>>>(e0, e1, s->n_tets, s->mat.kind == OD_MATERIAL_STVK,
-                                                          s->tets, s->X, s->u, s->pre, s->mat.threshold, s->lambda,
-                                                          s->mu, s->emap, s->gdof, s->K, s->fint, nullptr, nullptr,
-                                                          nullptr);
+    OD_KL(s);
+    scatter_kernel<<<nblk(90LL * (e1 - e0), 256), 256, 0, st>>>(e0, e1 - e0, s->n_tets, s->stage_k, s->stage_f,
+                                                                 s->emap, s->gdof, s->K, s->fint);
   }
   OD_CUDA(cudaGetLastError());
   return OD_OK;
@@ -511,6 +554,7 @@ od_status launch_element_values(Scene* s, double* d_k78, double* d_f12) {
   const int T = 128;
   cudaStream_t st = s->ctx->stream;
   if (s->n_tets == 0) return OD_OK;
+  OD_KL(s);
   if (s->mat.kind == OD_MATERIAL_COROTATIONAL)
     corot_kernel<1><<<nblk(s->n_tets, T), T, 0, st>>>(0, s->n_tets, s->n_tets, s->tets, s->X, s->u, s->pre,
                                                        s->mat.threshold, s->emap, s->gdof, nullptr, nullptr, d_k78,
@@ -525,20 +569,23 @@ od_status launch_element_values(Scene* s, double* d_k78, double* d_f12) {
 }
 
 // body part then traction colours; s->trac_* hold the colour-ordered facets
-od_status launch_loads(Scene* s, const double* body, int n_facets_total) {
+od_status launch_loads(Scene* s, const double* body, int n_facets_total, double traction_scale) {
   const int T = 128;
   cudaStream_t st = s->ctx->stream;
   double b[3] = {0, 0, 0};
   if (body) { b[0] = body[0]; b[1] = body[1]; b[2] = body[2]; }
   OD_CUDA(cudaMemsetAsync(s->fext, 0, sizeof(double) * (size_t)s->pcg.n_pad, st));
-  if (s->dofs > 0)
+  if (s->dofs > 0) {
+    OD_KL(s);
     body_force_kernel<<<nblk(s->dofs, T), T, 0, st>>>(s->dofs, s->free_pos, s->node_vol4, b[0], b[1], b[2], s->fext);
+  }
   if (n_facets_total > 0) {
     for (size_t c = 0; c + 1 < s->trac_color_off.size(); c++) {
       int f0 = s->trac_color_off[c], f1 = s->trac_color_off[c + 1];
       if (f1 <= f0) continue;
-      traction_kernel<<<nblk(f1 - f0, T), T, 0, st>>>(f0, f1, s->trac_facets, s->trac_vec, s->facets_dev, s->X,
-                                                       s->u, s->node_dof, s->fext);
+      OD_KL(s);
+      traction_kernel<<<nblk(f1 - f0, T), T, 0, st>>>(f0, f1, s->trac_facets, s->trac_vec, traction_scale,
+                                                       s->facets_dev, s->X, s->u, s->node_dof, s->fext);
     }
   }
   OD_CUDA(cudaGetLastError());

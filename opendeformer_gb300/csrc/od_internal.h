@@ -46,11 +46,10 @@ struct FullBsr {
   int* diag_pos = nullptr;    // nb: index of the diagonal block in each row
 };
 
-struct SolveScalars {           // device-resident PCG scalars (one cache line set)
-  double rz, rz_new, pq, rr, bb, eps, alpha, beta;
-  double rr0;
+struct SolveScalars {           // device-resident PCG scalars
+  double rz[2];                 // r.z by iteration parity
+  double rr, bb, eps, rr0, tr_num, tr_den, alpha, beta;
   int iter, max_iter, done, status;
-  unsigned int count1, count2;  // last-block-done counters
 };
 
 struct Pcg {
@@ -62,7 +61,7 @@ struct Pcg {
   double* p = nullptr;
   double* q = nullptr;
   double* b = nullptr;
-  double* partial = nullptr;    // 2 per CTA
+  double* partial = nullptr;    // 4 arrays of per-CTA partials
   SolveScalars* sc = nullptr;
   SolveScalars* sc_host = nullptr;  // pinned mirror
   int grid = 0;
@@ -85,13 +84,30 @@ struct Pcg {
   int* icT_ci = nullptr;
   int* icT_pos = nullptr;       // index into ic_val
   double ic_shift = 0.0;
+  // persistent (cooperative) solve
+  void* gbar = nullptr;         // grid barrier state
+  int* timeout_host = nullptr;  // pinned
+  int coop_grid = 0;            // co-resident CTAs, 0 if cooperative launch is unavailable
+  int disable_persistent = 0;
 };
 
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   int num_sms = 0;
+  // counters
+  long long launches = 0;
+  long long host_syncs = 0;
+  long long spmv_launches = 0;
+  double spmv_ms = 0.0;
+  long long pcg_kernel_launches = 0;  // persistent solves timed while profiling
+  long long pcg_kernel_iters = 0;
+  double pcg_kernel_ms = 0.0;
+  int profiling = 0;
+  std::vector<cudaEvent_t> ev_pool;   // event pairs for SpMV timing
 };
+
+#define OD_KL(scene) ((scene)->ctx->launches++)
 
 struct Scene {
   Ctx* ctx = nullptr;
@@ -121,9 +137,12 @@ struct Scene {
   double* K = nullptr;
   double* M = nullptr;
   double* Dm = nullptr;            // external damping (zero unless set)
+  bool has_damping = false;        // Dm holds non-zero values
   double* fint = nullptr;
   double* fext = nullptr;
   double* work_vals = nullptr;     // host-supplied values (SpMDV / PCG drop-in)
+  double* stage_k = nullptr;       // SoA [78][n_tets] element stiffness (colour order)
+  double* stage_f = nullptr;       // SoA [12][n_tets] element forces
   FullBsr bsr;
   void* A = nullptr;               // full BSR values (double or float)
   double* A64 = nullptr;           // FP64 full values (mixed path keeps both)
@@ -141,11 +160,21 @@ struct Scene {
   double* trac_vec = nullptr;      // per facet traction (3)
   int trac_cap = 0;
   std::vector<int> trac_color_off;
+  int n_trac = 0;                  // facet entries of the last od_scene_set_loads
+  double load_body[3] = {0, 0, 0};
+  bool has_body = false;
+  cudaEvent_t ev_step[2] = {nullptr, nullptr};
+  double sched_freq = 0.0, sched_phase = 0.0;   // traction schedule
 };
 
 // ---- error handling ----
 void set_error(const std::string& msg);
 od_status cuda_fail(cudaError_t e, const char* what);
+#define OD_TRY(expr)              \
+  do {                            \
+    od_status _st = (expr);       \
+    if (_st != OD_OK) return _st; \
+  } while (0)
 #define OD_CUDA(call)                                        \
   do {                                                       \
     cudaError_t _e = (call);                                 \
@@ -175,7 +204,8 @@ od_status launch_precompute(Scene* s);
 od_status launch_mass(Scene* s);
 od_status launch_eval(Scene* s, bool zero_first);       // K, fint at current u
 od_status launch_element_values(Scene* s, double* d_k78, double* d_f12);
-od_status launch_loads(Scene* s, const double* body, int n_facets_total);
+od_status launch_loads(Scene* s, const double* body, int n_facets_total, double traction_scale);
+od_status sync_stream(Scene* s);
 
 // ---- kernels (od_sparse.cu) ----
 od_status pcg_alloc(Scene* s);

@@ -560,6 +560,14 @@ __device__ void invertible_svd(const FT* F, FT thr, FT* sig, FT* U, FT* VT) {
 // PSD projection of a packed symmetric 3x3 (tetelement.cpp:439-465)
 template <class FT>
 __device__ void psd3(FT* m) {
+  // Positive leading minors (Sylvester) prove every eigenvalue positive, in
+  // which case the projection leaves the matrix unchanged: skip the eigensolve.
+  {
+    const FT m01 = m[0] * m[3] - m[1] * m[1];
+    const FT dt = m[0] * (m[3] * m[5] - m[4] * m[4]) - m[1] * (m[1] * m[5] - m[4] * m[2]) +
+                  m[2] * (m[1] * m[4] - m[3] * m[2]);
+    if (m[0] > FT(0) && m01 > FT(0) && dt > FT(0)) return;
+  }
   FT QT[9], ev[3];
   eig_sym3(m, ev, QT);
   bool neg = false;

@@ -53,28 +53,6 @@ __device__ __forceinline__ double block_sum(double v) {
   return t;  // valid in thread 0
 }
 
-// true in every thread of the last CTA to arrive; partials written before
-// the call are then visible to it
-__device__ __forceinline__ bool last_block(unsigned int* counter) {
-  __shared__ bool is_last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned int t = atomicAdd(counter, 1u);
-    is_last = (t == gridDim.x - 1);
-  }
-  __syncthreads();
-  return is_last;
-}
-
-// sum of partial[j*stride + slot] over j < n, in index order per thread, then
-// the fixed tree
-__device__ __forceinline__ double reduce_partials(const double* partial, int n, int stride, int slot) {
-  double acc = 0.0;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) acc += __ldcg(partial + (size_t)j * stride + slot);
-  return block_sum(acc);
-}
-
 // ------------------------------------------------------------- expansion
 // A_full = c1 V1 + c2 V2 + c3 V3 for every full-BSR entry, V* in the
 // reference lower layout (BlockedSymSparseMatrix Scale/Add,
@@ -100,87 +78,71 @@ __global__ void expand_kernel(long long total, const int* __restrict__ kind, con
 }
 
 // y (+)= c1 V1 x1 + c2 V2 x2 + c3 V3 x3 with V* read from the lower layout
-// through the full-BSR descriptors (SpMDV semantics, numerMethod.h:134-262)
+// through the full-BSR descriptors (SpMDV semantics, numerMethod.h:134-262).
+// Three lanes per block row as in the full-BSR product; absent sources
+// (NULL) cost nothing.
+template <int NSRC>
 __global__ void spmv_lower_kernel(int nb, const int* __restrict__ rp, const int* __restrict__ col,
                                   const int* __restrict__ kind, const int* __restrict__ off,
                                   const int* __restrict__ gen, const double* __restrict__ v1, double c1,
                                   const double* __restrict__ x1, const double* __restrict__ v2, double c2,
                                   const double* __restrict__ x2, const double* __restrict__ v3, double c3,
                                   const double* __restrict__ x3, double* __restrict__ y, int accumulate) {
-  const int lane = threadIdx.x & (kRowLanes - 1);
-  const int row = blockIdx.x * (blockDim.x / kRowLanes) + threadIdx.x / kRowLanes;
-  double y0 = 0.0, y1 = 0.0, y2 = 0.0;
-  if (row < nb) {
-    for (int k = rp[row] + lane; k < rp[row + 1]; k += kRowLanes) {
-      const int cb = col[k], kd = kind[k], of = off[k];
+  const int lane = threadIdx.x & 31;
+  if (lane >= 30) return;
+  const int row = (blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5)) * 10 + lane / 3;
+  const int r = lane % 3;
+  if (row >= nb) return;
+  double acc = 0.0;
+  for (int k = rp[row]; k < rp[row + 1]; k++) {
+    const int cb = 3 * col[k], kd = kind[k], of = off[k];
 #pragma unroll
-      for (int r = 0; r < 3; r++) {
-        double acc = 0.0;
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          int src = lower_src(kd, of, r, c, gen);
-          double a1 = 0.0, a2 = 0.0, a3 = 0.0;
-          if (src >= 0) {
-            a1 = c1 * v1[src];
-            if (v2) a2 = c2 * v2[src];
-            if (v3) a3 = c3 * v3[src];
-          } else if (src == -2) {
-            a1 = c1;
-          }
-          acc += a1 * x1[3 * cb + c];
-          if (v2) acc += a2 * x2[3 * cb + c];
-          if (v3) acc += a3 * x3[3 * cb + c];
-        }
-        if (r == 0) y0 += acc; else if (r == 1) y1 += acc; else y2 += acc;
+    for (int c = 0; c < 3; c++) {
+      const int src = lower_src(kd, of, r, c, gen);
+      if (src >= 0) {
+        acc = fma(c1 * v1[src], x1[cb + c], acc);
+        if (NSRC >= 2) acc = fma(c2 * v2[src], x2[cb + c], acc);
+        if (NSRC >= 3) acc = fma(c3 * v3[src], x3[cb + c], acc);
+      } else if (src == -2) {
+        acc = fma(c1, x1[cb + c], acc);
       }
     }
   }
-#pragma unroll
-  for (int o = kRowLanes / 2; o > 0; o >>= 1) {
-    y0 += __shfl_down_sync(0xffffffffu, y0, o, kRowLanes);
-    y1 += __shfl_down_sync(0xffffffffu, y1, o, kRowLanes);
-    y2 += __shfl_down_sync(0xffffffffu, y2, o, kRowLanes);
-  }
-  if (lane == 0 && row < nb) {
-    if (accumulate) { y[3 * row] += y0; y[3 * row + 1] += y1; y[3 * row + 2] += y2; }
-    else { y[3 * row] = y0; y[3 * row + 1] = y1; y[3 * row + 2] = y2; }
-  }
+  if (accumulate) y[3 * row + r] += acc;
+  else y[3 * row + r] = acc;
 }
 
-// row-block product of the full BSR with a 16-lane group per block row
-template <class TA>
-__device__ __forceinline__ void bsr_row(int row, int nb, const int* __restrict__ rp, const int* __restrict__ col,
-                                        const TA* __restrict__ A, const double* __restrict__ x, double& y0,
-                                        double& y1, double& y2) {
-  const int lane = threadIdx.x & (kRowLanes - 1);
-  y0 = y1 = y2 = 0.0;
-  if (row < nb) {
-    for (int k = rp[row] + lane; k < rp[row + 1]; k += kRowLanes) {
-      const TA* a = A + (size_t)k * 9;
-      const int c = col[k];
-      const double x0 = x[3 * c], x1 = x[3 * c + 1], x2 = x[3 * c + 2];
-      y0 += (double)a[0] * x0 + (double)a[1] * x1 + (double)a[2] * x2;
-      y1 += (double)a[3] * x0 + (double)a[4] * x1 + (double)a[5] * x2;
-      y2 += (double)a[6] * x0 + (double)a[7] * x1 + (double)a[8] * x2;
-    }
+// Row-block products of the full BSR.  Three lanes per block row, lane r
+// owning row r of the block row: it walks the row's blocks and does three
+// FMAs per block with the block's row r (three contiguous values) -- exactly
+// one FMA per stored value and no cross-lane reduction, which matters on a
+// part whose FP64 rate is low.  Ten block rows per warp (lanes 30, 31 idle).
+constexpr int kRowsPerWarp = 10;
+constexpr int kWarpRows = (kThreads / 32) * kRowsPerWarp;  // block rows per 256-thread CTA
+
+template <class TA, class TX>
+__device__ __forceinline__ double bsr_subrow(int row, int r, const int* __restrict__ rp, const int* __restrict__ col,
+                                             const TA* __restrict__ A, const TX* __restrict__ x) {
+  double y = 0.0;
+  const int kb = rp[row], ke = rp[row + 1];
+  for (int k = kb; k < ke; k++) {
+    const TA* a = A + (size_t)k * 9 + 3 * r;
+    const int c = 3 * col[k];
+    y = fma((double)a[0], (double)x[c], y);
+    y = fma((double)a[1], (double)x[c + 1], y);
+    y = fma((double)a[2], (double)x[c + 2], y);
   }
-#pragma unroll
-  for (int o = kRowLanes / 2; o > 0; o >>= 1) {
-    y0 += __shfl_down_sync(0xffffffffu, y0, o, kRowLanes);
-    y1 += __shfl_down_sync(0xffffffffu, y1, o, kRowLanes);
-    y2 += __shfl_down_sync(0xffffffffu, y2, o, kRowLanes);
-  }
+  return y;
 }
 
 template <class TA>
 __global__ void spmv_full_kernel(int nb, const int* __restrict__ rp, const int* __restrict__ col,
                                  const TA* __restrict__ A, const double* __restrict__ x, double* __restrict__ y) {
-  const int row = blockIdx.x * (blockDim.x / kRowLanes) + threadIdx.x / kRowLanes;
-  double y0, y1, y2;
-  bsr_row<TA>(row, nb, rp, col, A, x, y0, y1, y2);
-  if ((threadIdx.x & (kRowLanes - 1)) == 0 && row < nb) {
-    y[3 * row] = y0; y[3 * row + 1] = y1; y[3 * row + 2] = y2;
-  }
+  const int lane = threadIdx.x & 31;
+  if (lane >= 3 * kRowsPerWarp) return;
+  const int row = (blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5)) * kRowsPerWarp + lane / 3;
+  const int r = lane % 3;
+  if (row < nb) y[3 * row + r] = bsr_subrow<TA, double>(row, r, rp, col, A, x);
 }
 
 // ------------------------------------------------------- preconditioners
@@ -232,133 +194,491 @@ __device__ __forceinline__ void apply_local_precond(int kind, int i, const doubl
 }
 
 // ------------------------------------------------------------ PCG kernels
-// init: r = b - A x0; z = M^-1 r; p = z; rz = r.z; eps = tol^2 b.b; rr = r.r
-// (cgSolver.cpp:20-30).  For IC(0) (local == 0) z and p are formed later.
+// Scalars flow through per-CTA partials: a producer kernel writes one
+// partial per CTA, and every CTA of the consumer kernel sums all of them in
+// the same fixed order (so every CTA sees the identical value, without
+// atomics).  The grids are capped at two CTAs per SM with grid-stride loops,
+// which keeps the partial count small.  r.z is kept in two parity slots: the
+// kernel that reads slot s of iteration k only ever writes slot 1 - s.
+constexpr int kUpdThreads = 192;  // multiple of 3 (whole 3x3 blocks) and of 32
+
+// sum of part[0..m) by every thread of the CTA (fixed order), broadcast
+__device__ __forceinline__ double sum_partials(const double* __restrict__ part, int m) {
+  __shared__ double bc;
+  double acc = 0.0;
+  for (int j = threadIdx.x; j < m; j += blockDim.x) acc += __ldcg(part + j);
+  double t = block_sum(acc);
+  if (threadIdx.x == 0) bc = t;
+  __syncthreads();
+  double v = bc;
+  __syncthreads();
+  return v;
+}
+
+// r = b - A x0; z = M^-1 r; p = z (local preconditioners); partials of r.z,
+// b.b and r.r (cgSolver.cpp:20-30)
 template <class TA>
 __global__ void pcg_init_kernel(int nb, const int* __restrict__ rp, const int* __restrict__ col,
                                 const TA* __restrict__ A, const double* __restrict__ b, const double* __restrict__ x,
-                                double* __restrict__ r, double* __restrict__ z, double* __restrict__ p, int pkind,
-                                const double* __restrict__ pinv, double tol, int max_iter, double* __restrict__ partial,
-                                SolveScalars* sc) {
-  const int row = blockIdx.x * (blockDim.x / kRowLanes) + threadIdx.x / kRowLanes;
-  double q0, q1, q2;
-  bsr_row<TA>(row, nb, rp, col, A, x, q0, q1, q2);
+                                double* __restrict__ r_out, double* __restrict__ z, double* __restrict__ p, int pkind,
+                                const double* __restrict__ pinv, double* __restrict__ part_rz,
+                                double* __restrict__ part_bb, double* __restrict__ part_rr) {
   double rz = 0.0, bb = 0.0, rr = 0.0;
-  if ((threadIdx.x & (kRowLanes - 1)) == 0 && row < nb) {
-    double rv[3], zv[3];
-    const double bv[3] = {b[3 * row], b[3 * row + 1], b[3 * row + 2]};
-    rv[0] = bv[0] - q0; rv[1] = bv[1] - q1; rv[2] = bv[2] - q2;
-    apply_local_precond(pkind, row, pinv, rv, zv);
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      r[3 * row + d] = rv[d];
-      if (pkind != OD_PRECOND_IC0) { z[3 * row + d] = zv[d]; p[3 * row + d] = zv[d]; }
-      rz += rv[d] * zv[d];
-      bb += bv[d] * bv[d];
-      rr += rv[d] * rv[d];
+  const int lane = threadIdx.x & 31;
+  const int warp_global = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+  __shared__ double rsh[kThreads];
+  for (int wb = warp_global * kRowsPerWarp; wb < nb; wb += gridDim.x * kWarpRows) {
+    const int row = wb + lane / 3, r = lane % 3;
+    const bool valid = lane < 3 * kRowsPerWarp && row < nb;
+    double rv = 0.0, bv = 0.0;
+    if (valid) {
+      const double qv = bsr_subrow<TA, double>(row, r, rp, col, A, x);
+      bv = b[3 * row + r];
+      rv = bv - qv;
+      r_out[3 * row + r] = rv;
     }
+    __syncwarp();
+    rsh[threadIdx.x] = rv;
+    __syncwarp();
+    if (valid) {
+      double zv = rv;
+      if (pkind == OD_PRECOND_JACOBI) zv = pinv[3 * row + r] * rv;
+      else if (pkind == OD_PRECOND_BLOCK_JACOBI) {
+        const double* m = pinv + 9 * (size_t)row + 3 * r;
+        const int lb = threadIdx.x - r;
+        zv = m[0] * rsh[lb] + m[1] * rsh[lb + 1] + m[2] * rsh[lb + 2];
+      }
+      if (pkind != OD_PRECOND_IC0) { z[3 * row + r] = zv; p[3 * row + r] = zv; rz += rv * zv; }
+      bb += bv * bv;
+      rr += rv * rv;
+    }
+    __syncwarp();
   }
   double s0 = block_sum(rz), s1 = block_sum(bb), s2 = block_sum(rr);
+  if (threadIdx.x == 0) { part_rz[blockIdx.x] = s0; part_bb[blockIdx.x] = s1; part_rr[blockIdx.x] = s2; }
+}
+
+// single CTA: rz, b.b, r.r, eps = tol^2 b.b, iteration 0, stop flag
+__global__ void pcg_init_finish(const double* __restrict__ part_rz, int g_rz, const double* __restrict__ part_bb,
+                                const double* __restrict__ part_rr, int g, double tol, int max_iter,
+                                SolveScalars* sc) {
+  const double rz = sum_partials(part_rz, g_rz);
+  const double bb = sum_partials(part_bb, g);
+  const double rr = sum_partials(part_rr, g);
   if (threadIdx.x == 0) {
-    partial[3 * blockIdx.x] = s0; partial[3 * blockIdx.x + 1] = s1; partial[3 * blockIdx.x + 2] = s2;
-  }
-  if (last_block(&sc->count1)) {
-    double t0 = reduce_partials(partial, gridDim.x, 3, 0);
-    double t1 = reduce_partials(partial, gridDim.x, 3, 1);
-    double t2 = reduce_partials(partial, gridDim.x, 3, 2);
-    if (threadIdx.x == 0) {
-      sc->rz = t0; sc->bb = t1; sc->rr = t2; sc->rr0 = t2;
-      sc->eps = t1 * tol * tol;
-      sc->iter = 0;
-      sc->max_iter = max_iter;
-      sc->status = isfinite(t2) ? OD_OK : OD_ERR_NAN;
-      sc->done = !(0 < max_iter && t2 > sc->eps) || !isfinite(t2);
-      sc->count1 = 0;
-    }
+    sc->rz[0] = rz; sc->rz[1] = rz;
+    sc->bb = bb; sc->rr = rr; sc->rr0 = rr;
+    sc->eps = bb * tol * tol;
+    sc->iter = 0;
+    sc->max_iter = max_iter;
+    sc->status = isfinite(rr) ? OD_OK : OD_ERR_NAN;
+    sc->done = !(0 < max_iter && rr > sc->eps) || !isfinite(rr);
   }
 }
 
-// K1: q = A p and alpha = rz / (p.q)
+// K1: q = A p; partials of p.q
 template <class TA>
 __global__ void pcg_spmv_kernel(int nb, const int* __restrict__ rp, const int* __restrict__ col,
                                 const TA* __restrict__ A, const double* __restrict__ p, double* __restrict__ q,
-                                double* __restrict__ partial, SolveScalars* sc) {
-  if (*(volatile int*)&sc->done) return;
-  const int row = blockIdx.x * (blockDim.x / kRowLanes) + threadIdx.x / kRowLanes;
-  double y0, y1, y2;
-  bsr_row<TA>(row, nb, rp, col, A, p, y0, y1, y2);
+                                double* __restrict__ part_pq, const SolveScalars* sc) {
+  if (*(volatile const int*)&sc->done) return;
   double pq = 0.0;
-  if ((threadIdx.x & (kRowLanes - 1)) == 0 && row < nb) {
-    q[3 * row] = y0; q[3 * row + 1] = y1; q[3 * row + 2] = y2;
-    pq = p[3 * row] * y0 + p[3 * row + 1] * y1 + p[3 * row + 2] * y2;
-  }
-  double s = block_sum(pq);
-  if (threadIdx.x == 0) partial[blockIdx.x] = s;
-  if (last_block(&sc->count1)) {
-    double t = reduce_partials(partial, gridDim.x, 1, 0);
-    if (threadIdx.x == 0) {
-      double alpha = sc->rz / t;
-      sc->pq = t;
-      sc->alpha = alpha;
-      if (!isfinite(alpha)) { sc->status = OD_ERR_NAN; sc->done = 1; }
-      sc->count1 = 0;
+  const int lane = threadIdx.x & 31;
+  const int warp_global = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+  for (int wb = warp_global * kRowsPerWarp; wb < nb; wb += gridDim.x * kWarpRows) {
+    const int row = wb + lane / 3, r = lane % 3;
+    if (lane < 3 * kRowsPerWarp && row < nb) {
+      const double y = bsr_subrow<TA, double>(row, r, rp, col, A, p);
+      q[3 * row + r] = y;
+      pq = fma(p[3 * row + r], y, pq);
     }
   }
+  double t = block_sum(pq);
+  if (threadIdx.x == 0) part_pq[blockIdx.x] = t;
 }
 
-// K2: x += alpha p; r -= alpha q; z = M^-1 r (local preconditioners);
-// beta = (r.z)_new / (r.z); stop test of cgSolver.cpp:32
-__global__ void pcg_update_kernel(int nb, double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
-                                  const double* __restrict__ p, const double* __restrict__ q, int pkind,
-                                  const double* __restrict__ pinv, double* __restrict__ partial, SolveScalars* sc,
-                                  int finish) {
+// K2: alpha = rz / p.q; x += alpha p; r -= alpha q; z = M^-1 r (local
+// preconditioners); partials of r.z and r.r.  One thread per DOF; a CTA step
+// covers whole 3x3 blocks so block-Jacobi reads its block's residual from
+// shared memory.
+__global__ void __launch_bounds__(kUpdThreads) pcg_update_kernel(int n, double* __restrict__ x, double* __restrict__ r,
+                                                                 double* __restrict__ z, const double* __restrict__ p,
+                                                                 const double* __restrict__ q, int pkind,
+                                                                 const double* __restrict__ pinv,
+                                                                 const double* __restrict__ part_pq, int g_pq,
+                                                                 double* __restrict__ part_rz,
+                                                                 double* __restrict__ part_rr, SolveScalars* sc,
+                                                                 int slot) {
   if (*(volatile int*)&sc->done) return;
-  const double alpha = sc->alpha;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ double rs[kUpdThreads];
+  const double pq = sum_partials(part_pq, g_pq);
+  const double alpha = sc->rz[slot] / pq;
+  if (blockIdx.x == 0 && threadIdx.x == 0) sc->alpha = alpha;
   double rz = 0.0, rr = 0.0;
-  if (i < nb) {
-    double rv[3], zv[3];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      x[3 * i + d] += alpha * p[3 * i + d];
-      rv[d] = r[3 * i + d] - alpha * q[3 * i + d];
-      r[3 * i + d] = rv[d];
+  for (int base = blockIdx.x * kUpdThreads; base < n; base += gridDim.x * kUpdThreads) {
+    const int i = base + threadIdx.x;
+    const bool valid = i < n;
+    double rv = 0.0;
+    if (valid) {
+      x[i] += alpha * p[i];
+      rv = r[i] - alpha * q[i];
+      r[i] = rv;
     }
-    if (pkind != OD_PRECOND_IC0) {
-      apply_local_precond(pkind, i, pinv, rv, zv);
-#pragma unroll
-      for (int d = 0; d < 3; d++) { z[3 * i + d] = zv[d]; rz += rv[d] * zv[d]; }
+    __syncthreads();
+    rs[threadIdx.x] = rv;
+    __syncthreads();
+    rr += rv * rv;
+    if (valid && pkind != OD_PRECOND_IC0) {
+      double zv;
+      if (pkind == OD_PRECOND_JACOBI) {
+        zv = pinv[i] * rv;
+      } else if (pkind == OD_PRECOND_BLOCK_JACOBI) {
+        const int d = i % 3, lb = threadIdx.x - d;
+        const double* m = pinv + 3 * (size_t)i;  // row d of block i / 3
+        zv = m[0] * rs[lb] + m[1] * rs[lb + 1] + m[2] * rs[lb + 2];
+      } else {
+        zv = rv;
+      }
+      z[i] = zv;
+      rz += rv * zv;
     }
-#pragma unroll
-    for (int d = 0; d < 3; d++) rr += rv[d] * rv[d];
   }
   double s0 = block_sum(rz), s1 = block_sum(rr);
-  if (threadIdx.x == 0) { partial[2 * blockIdx.x] = s0; partial[2 * blockIdx.x + 1] = s1; }
-  if (last_block(&sc->count2)) {
-    double t0 = reduce_partials(partial, gridDim.x, 2, 0);
-    double t1 = reduce_partials(partial, gridDim.x, 2, 1);
-    if (threadIdx.x == 0) {
-      sc->rr = t1;
-      if (finish) {
-        double beta = t0 / sc->rz;
-        sc->beta = beta;
-        sc->rz = t0;
-        sc->iter += 1;
-        if (!isfinite(t1) || !isfinite(beta)) { sc->status = OD_ERR_NAN; sc->done = 1; }
-        else sc->done = !(sc->iter < sc->max_iter && t1 > sc->eps);
-      }
-      sc->count2 = 0;
-    }
+  if (threadIdx.x == 0) { part_rz[blockIdx.x] = s0; part_rr[blockIdx.x] = s1; }
+}
+
+// partials of r.z (IC(0): after the triangular solves)
+__global__ void pcg_rz_kernel(int n, const double* __restrict__ r, const double* __restrict__ z,
+                              double* __restrict__ part_rz, const SolveScalars* sc) {
+  if (sc && *(volatile const int*)&sc->done) return;
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) acc += r[i] * z[i];
+  double t = block_sum(acc);
+  if (threadIdx.x == 0) part_rz[blockIdx.x] = t;
+}
+
+// K3: beta = (r.z)_new / (r.z); p = z + beta p; CTA 0 records the new r.z
+// in the other slot, r.r, the iteration count and the stop test
+// (cgSolver.cpp:32-54)
+__global__ void pcg_direction_kernel(int n, const double* __restrict__ z, double* __restrict__ p,
+                                     const double* __restrict__ part_rz, int g_rz, const double* __restrict__ part_rr,
+                                     int g_rr, SolveScalars* sc, int slot) {
+  if (*(volatile int*)&sc->done) return;
+  const double rz_new = sum_partials(part_rz, g_rz);
+  const double rr = sum_partials(part_rr, g_rr);
+  const double beta = rz_new / sc->rz[slot];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = beta * p[i] + z[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sc->rz[1 - slot] = rz_new;
+    sc->rr = rr;
+    sc->beta = beta;
+    const int it = sc->iter + 1;
+    sc->iter = it;
+    if (!isfinite(rr) || !isfinite(beta)) { sc->status = OD_ERR_NAN; sc->done = 1; }
+    else sc->done = !(it < sc->max_iter && rr > sc->eps);
   }
 }
 
-// K3: p = z + beta p
-__global__ void pcg_direction_kernel(int n, const double* __restrict__ z, double* __restrict__ p, SolveScalars* sc,
-                                     int check_done) {
-  if (check_done && *(volatile int*)&sc->done) return;
-  const double beta = sc->beta;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) p[i] = beta * p[i] + z[i];
+// ||b - q||^2 and ||b||^2 (true residual, q = A x); single CTA
+__global__ void residual_norm_kernel(int n, const double* __restrict__ b, const double* __restrict__ q,
+                                     SolveScalars* sc) {
+  double d2 = 0.0, bb = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double d = b[i] - q[i];
+    d2 += d * d;
+    bb += b[i] * b[i];
+  }
+  double t0 = block_sum(d2), t1 = block_sum(bb);
+  if (threadIdx.x == 0) { sc->tr_num = t0; sc->tr_den = t1; }
+}
+
+// ------------------------------------------------------ persistent PCG
+// The whole Jacobi / block-Jacobi / unpreconditioned solve in one
+// cooperative launch: every CTA is resident (cudaLaunchCooperativeKernel
+// refuses grids that are not), the phases of an iteration are separated by a
+// grid barrier, and every CTA forms the scalars itself from the per-CTA
+// partials in a fixed order, so all CTAs take identical loop decisions.
+//
+// The barrier is a sense (generation) barrier in global memory.  Its waits
+// are bounded: after kSpinLimit polls the waiting CTA records a timeout and
+// every CTA leaves the solve at the next barrier, so the kernel always
+// returns and the host reports OD_ERR_DEVICE_TIMEOUT.
+struct GridBarrier {
+  unsigned int arrive;
+  unsigned int gen;
+  int timeout;
+  int pad;
+};
+constexpr unsigned long long kSpinLimit = 1ull << 22;  // polls (about 1-2 s of L2 round trips) before a timeout
+constexpr int kPThreads = 768;                          // 24 warps; multiple of 3
+
+// arrival of one thread per CTA (acquire/release atomics: measured 1.9 us
+// per barrier over 152 CTAs on GB300, against 2.3 us with full fences);
+// returns 0 after a timeout
+__device__ __forceinline__ int barrier_arrive_wait(GridBarrier* gb) {
+  unsigned int g, a;
+  asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(g) : "l"(&gb->gen) : "memory");
+  asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;" : "=r"(a) : "l"(&gb->arrive) : "memory");
+  int ok = 1;
+  if (a == gridDim.x - 1) {
+    gb->arrive = 0;
+    asm volatile("red.release.gpu.add.u32 [%0], 1;" ::"l"(&gb->gen) : "memory");
+  } else {
+    unsigned long long spins = 0;
+    unsigned int cur;
+    do {
+      asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(cur) : "l"(&gb->gen) : "memory");
+      if (++spins > kSpinLimit) { atomicExch(&gb->timeout, 1); ok = 0; break; }
+    } while (cur == g);
+  }
+  return ok && !*(volatile int*)&gb->timeout;
+}
+
+__device__ __forceinline__ bool grid_barrier(GridBarrier* gb) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) ok_s = barrier_arrive_wait(gb);
+  __syncthreads();
+  return ok_s != 0;
+}
+
+// sum of part[0..m) by every CTA in the same order, broadcast to the CTA
+__device__ __forceinline__ double cta_sum(const double* __restrict__ part, int m) {
+  return sum_partials(part, m);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;  // lane 0
+}
+
+// Grid-wide sums of NV per-thread values with one grid barrier and two
+// CTA barriers: warps reduce by shuffles, warp 0 forms the CTA partials,
+// lane 0 of warp 0 takes part in the grid barrier, then warp 0 sums all CTA
+// partials in a fixed order and broadcasts through shared memory.  Every
+// CTA obtains bitwise the same sums.  Returns false after a barrier timeout.
+template <int NV>
+__device__ __forceinline__ bool grid_sums(double (&v)[NV], double* __restrict__ part, GridBarrier* gb) {
+  __shared__ double ws[NV][32];
+  __shared__ double res[NV];
+  __shared__ int ok_s;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int G = gridDim.x;
+#pragma unroll
+  for (int j = 0; j < NV; j++) {
+    double t = warp_sum(v[j]);
+    if (lane == 0) ws[j][w] = t;
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+      double t = warp_sum(lane < nw ? ws[j][lane] : 0.0);
+      if (lane == 0) part[(size_t)j * G + blockIdx.x] = t;
+    }
+    int ok = 1;
+    if (lane == 0) ok = barrier_arrive_wait(gb);
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+      double acc = 0.0;
+      for (int c = lane; c < G; c += 32) acc += __ldcg(part + (size_t)j * G + c);
+      acc = warp_sum(acc);
+      if (lane == 0) res[j] = acc;
+    }
+    if (lane == 0) ok_s = ok;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < NV; j++) v[j] = res[j];
+  return ok_s != 0;
+}
+
+// Work decomposition of the persistent solve: "groups" of 10 block rows
+// (30 DOFs, lanes 0..29 of a warp; lane l owns DOF 30 g + l, i.e. row l % 3
+// of block row 10 g + l / 3).  Group g goes to warp g / G of CTA g % G, so
+// every CTA -- every SM, whose FP64 pipe is the limit -- gets an equal share.
+// With GPW > 0 a warp owns at most GPW groups and keeps x, r, z, p and q of
+// its DOFs in registers across the grid barriers; only p goes back to memory
+// (the SpMV gathers it).  With GPW == 0 the vectors stream from memory.
+// Loop over the groups a warp owns.  With GPW > 0 the outer loop is fully
+// unrolled (k is a compile-time index into the register arrays) and the
+// inner one runs at most once; with GPW == 0 the inner loop strides over all
+// groups and the vectors live in memory.
+#define OD_GROUP_LOOP(k, g)                                                   \
+  _Pragma("unroll") for (int k = 0; k < (GPW > 0 ? NR : 1); k++)              \
+    for (int g = g0 + k * gstride; g < ngroups; g += (GPW > 0 ? ngroups : gstride))
+
+template <class TA, int GPW>
+__global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
+    int nb, const int* __restrict__ rp, const int* __restrict__ col, const TA* __restrict__ A,
+    const double* __restrict__ b, double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
+    double* __restrict__ p, double* __restrict__ q, int pkind, const double* __restrict__ pinv,
+    double* __restrict__ part, double tol, int max_iter, SolveScalars* sc, GridBarrier* gb) {
+  constexpr int NR = GPW > 0 ? GPW : 1;
+  const int G = gridDim.x;
+  double* part_1 = part;          // one-value reductions (p.q, residual)
+  double* part_2 = part + G;      // two/three-value reductions (G entries per value)
+  const int lane = threadIdx.x & 31;
+  const int wpc = kPThreads / 32;
+  const int w = threadIdx.x >> 5;
+  const int ngroups = (nb + kRowsPerWarp - 1) / kRowsPerWarp;
+  const int gstride = G * wpc;
+  const int g0 = w * G + blockIdx.x;
+  const int rsub = lane % 3;
+  const int lbase = lane - rsub;
+
+  double xr[NR], rv[NR], zv[NR], pv[NR], qv[NR];
+
+  // z = M^-1 r inside the warp (block-Jacobi through shuffles of the 3 lanes
+  // of a block row; every lane takes part in the shuffles)
+  auto apply_precond = [&](int row, bool valid, double rl) {
+    double r0 = __shfl_sync(0xffffffffu, rl, lbase < 32 ? lbase : 0);
+    double r1 = __shfl_sync(0xffffffffu, rl, lbase + 1 < 32 ? lbase + 1 : 0);
+    double r2 = __shfl_sync(0xffffffffu, rl, lbase + 2 < 32 ? lbase + 2 : 0);
+    if (!valid) return 0.0;
+    if (pkind == OD_PRECOND_JACOBI) return pinv[3 * row + rsub] * rl;
+    if (pkind == OD_PRECOND_BLOCK_JACOBI) {
+      const double* m = pinv + 9 * (size_t)row + 3 * rsub;
+      return m[0] * r0 + m[1] * r1 + m[2] * r2;
+    }
+    return rl;
+  };
+
+  // ---- init: r = b - A x; z = M^-1 r; p = z (cgSolver.cpp:20-30)
+  double rz = 0.0, bb = 0.0, rr = 0.0;
+  {
+    OD_GROUP_LOOP(k, g) {
+      const int row = g * kRowsPerWarp + lane / 3;
+      const bool valid = lane < 30 && row < nb;
+      const int i = 3 * row + rsub;
+      double bv = 0.0, xl = 0.0, rl = 0.0;
+      if (valid) {
+        bv = b[i];
+        xl = x[i];
+        rl = bv - bsr_subrow<TA, double>(row, rsub, rp, col, A, x);
+      }
+      const double zl = apply_precond(row, valid, rl);
+      if (valid) {
+        rz = fma(rl, zl, rz);
+        bb = fma(bv, bv, bb);
+        rr = fma(rl, rl, rr);
+        if (GPW > 0) { xr[k] = xl; rv[k] = rl; zv[k] = zl; pv[k] = zl; }
+        else { r[i] = rl; z[i] = zl; }
+        p[i] = zl;
+      }
+    }
+  }
+  {
+    double v3[3] = {rz, bb, rr};
+    if (!grid_sums<3>(v3, part_2, gb)) return;
+    rz = v3[0]; bb = v3[1]; rr = v3[2];
+  }
+  const double eps = bb * tol * tol;
+  int it = 0;
+  int status = isfinite(rr) ? OD_OK : OD_ERR_NAN;
+
+  while (status == OD_OK && it < max_iter && rr > eps) {
+    // ---- q = A p; p.q
+    double pq = 0.0;
+    {
+      OD_GROUP_LOOP(k, g) {
+        const int row = g * kRowsPerWarp + lane / 3;
+        if (lane < 30 && row < nb) {
+          const int i = 3 * row + rsub;
+          const double y = bsr_subrow<TA, double>(row, rsub, rp, col, A, p);
+          const double pl = GPW > 0 ? pv[k] : p[i];
+          if (GPW > 0) qv[k] = y; else q[i] = y;
+          pq = fma(pl, y, pq);
+        }
+      }
+    }
+    double v1[1] = {pq};
+    if (!grid_sums<1>(v1, part_1, gb)) return;
+    const double alpha = rz / v1[0];
+    // ---- x += alpha p; r -= alpha q; z = M^-1 r; r.z, r.r
+    double rzn = 0.0, rrn = 0.0;
+    {
+      OD_GROUP_LOOP(k, g) {
+        const int row = g * kRowsPerWarp + lane / 3;
+        const bool valid = lane < 30 && row < nb;
+        const int i = 3 * row + rsub;
+        double rl = 0.0;
+        if (valid) {
+          if (GPW > 0) {
+            xr[k] = fma(alpha, pv[k], xr[k]);
+            rl = fma(-alpha, qv[k], rv[k]);
+            rv[k] = rl;
+          } else {
+            x[i] = fma(alpha, p[i], x[i]);
+            rl = fma(-alpha, q[i], r[i]);
+            r[i] = rl;
+          }
+        }
+        const double zl = apply_precond(row, valid, rl);
+        if (valid) {
+          if (GPW > 0) zv[k] = zl; else z[i] = zl;
+          rzn = fma(rl, zl, rzn);
+          rrn = fma(rl, rl, rrn);
+        }
+      }
+    }
+    double v2[2] = {rzn, rrn};
+    if (!grid_sums<2>(v2, part_2, gb)) return;
+    const double rz_new = v2[0];
+    rr = v2[1];
+    const double beta = rz_new / rz;
+    rz = rz_new;
+    it++;
+    if (!isfinite(rr) || !isfinite(beta)) status = OD_ERR_NAN;
+    // ---- p = z + beta p
+    {
+      OD_GROUP_LOOP(k, g) {
+        const int row = g * kRowsPerWarp + lane / 3;
+        if (lane < 30 && row < nb) {
+          const int i = 3 * row + rsub;
+          if (GPW > 0) { pv[k] = fma(beta, pv[k], zv[k]); p[i] = pv[k]; }
+          else p[i] = fma(beta, p[i], z[i]);
+        }
+      }
+    }
+    if (!grid_barrier(gb)) return;
+  }
+  // ---- write back x, then the true residual ||b - A x||^2
+  if (GPW > 0) {
+    OD_GROUP_LOOP(k, g) {
+      const int row = g * kRowsPerWarp + lane / 3;
+      if (lane < 30 && row < nb) x[3 * row + rsub] = xr[k];
+    }
+  }
+  if (!grid_barrier(gb)) return;
+  double d2 = 0.0;
+  OD_GROUP_LOOP(k, g) {
+    (void)k;
+    const int row = g * kRowsPerWarp + lane / 3;
+    if (lane < 30 && row < nb) {
+      const double dv = b[3 * row + rsub] - bsr_subrow<TA, double>(row, rsub, rp, col, A, x);
+      d2 = fma(dv, dv, d2);
+    }
+  }
+  double vr[1] = {d2};
+  if (!grid_sums<1>(vr, part_1, gb)) return;
+  if (blockIdx.x == 0) {
+    const double tr = vr[0];
+    if (threadIdx.x == 0) {
+      sc->rz[0] = rz;
+      sc->rr = rr;
+      sc->bb = bb;
+      sc->eps = eps;
+      sc->iter = it;
+      sc->max_iter = max_iter;
+      sc->status = status;
+      sc->tr_num = tr;
+      sc->tr_den = bb;
+      sc->done = 1;
+    }
+  }
 }
 
 // ----------------------------------------------------------------- IC(0)
@@ -426,33 +746,6 @@ __global__ void ic0_backward_level(int l0, int l1, const int* __restrict__ rows,
   z[i] = s / L[rp[i + 1] - 1];
 }
 
-// r.z partial and finish for IC(0) (K2 split: the update kernel ran with
-// finish = 0 and formed r.r)
-__global__ void pcg_rz_finish_kernel(int n, const double* __restrict__ r, const double* __restrict__ z,
-                                     double* __restrict__ partial, SolveScalars* sc, int init) {
-  if (!init && *(volatile int*)&sc->done) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double rz = i < n ? r[i] * z[i] : 0.0;
-  double s = block_sum(rz);
-  if (threadIdx.x == 0) partial[blockIdx.x] = s;
-  if (last_block(&sc->count2)) {
-    double t0 = reduce_partials(partial, gridDim.x, 1, 0);
-    if (threadIdx.x == 0) {
-      if (init) {
-        sc->rz = t0;
-      } else {
-        double beta = t0 / sc->rz;
-        sc->beta = beta;
-        sc->rz = t0;
-        sc->iter += 1;
-        if (!isfinite(sc->rr) || !isfinite(beta)) { sc->status = OD_ERR_NAN; sc->done = 1; }
-        else sc->done = !(sc->iter < sc->max_iter && sc->rr > sc->eps);
-      }
-      sc->count2 = 0;
-    }
-  }
-}
-
 __global__ void copy_kernel(int n, const double* __restrict__ a, double* __restrict__ b) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) b[i] = a[i];
@@ -465,6 +758,8 @@ od_status launch_expand(Scene* s, const double* v1, double c1, const double* v2,
                         double c3) {
   const long long total = 9LL * s->bsr.nnzb;
   if (total == 0) return OD_OK;
+  if (v3 && !s->has_damping) v3 = nullptr;
+  OD_KL(s);
   expand_kernel<double><<<nblk(total, kThreads), kThreads, 0, s->ctx->stream>>>(
       total, s->bsr.desc_kind, s->bsr.desc_off, s->bsr.gen, v1, c1, v2, c2, v3, c3, s->A64);
   OD_CUDA(cudaGetLastError());
@@ -476,10 +771,23 @@ od_status launch_spmv_lower(Scene* s, const double* v1, double c1, const double*
                             bool accumulate) {
   const int nb = s->bsr.nb;
   if (nb == 0) return OD_OK;
-  const int rows_per_cta = kThreads / kRowLanes;
-  spmv_lower_kernel<<<nblk(nb, rows_per_cta), kThreads, 0, s->ctx->stream>>>(
-      nb, s->bsr.row_ptr, s->bsr.col, s->bsr.desc_kind, s->bsr.desc_off, s->bsr.gen, v1, c1, x1, v2, c2, x2, v3, c3,
-      x3, y, accumulate ? 1 : 0);
+  // drop a second / third source that is absent or known to be zero
+  if (v3 && !s->has_damping) v3 = nullptr;
+  if (v2 && v2 == s->Dm && !s->has_damping) { v2 = v3; c2 = c3; x2 = x3; v3 = nullptr; }
+  const int g = nblk(nb, (kThreads / 32) * 10);
+  OD_KL(s);
+  if (v3)
+    spmv_lower_kernel<3><<<g, kThreads, 0, s->ctx->stream>>>(nb, s->bsr.row_ptr, s->bsr.col, s->bsr.desc_kind,
+                                                              s->bsr.desc_off, s->bsr.gen, v1, c1, x1, v2, c2, x2, v3,
+                                                              c3, x3, y, accumulate ? 1 : 0);
+  else if (v2)
+    spmv_lower_kernel<2><<<g, kThreads, 0, s->ctx->stream>>>(nb, s->bsr.row_ptr, s->bsr.col, s->bsr.desc_kind,
+                                                              s->bsr.desc_off, s->bsr.gen, v1, c1, x1, v2, c2, x2,
+                                                              nullptr, 0.0, nullptr, y, accumulate ? 1 : 0);
+  else
+    spmv_lower_kernel<1><<<g, kThreads, 0, s->ctx->stream>>>(nb, s->bsr.row_ptr, s->bsr.col, s->bsr.desc_kind,
+                                                              s->bsr.desc_off, s->bsr.gen, v1, c1, x1, nullptr, 0.0,
+                                                              nullptr, nullptr, 0.0, nullptr, y, accumulate ? 1 : 0);
   OD_CUDA(cudaGetLastError());
   return OD_OK;
 }
@@ -487,8 +795,8 @@ od_status launch_spmv_lower(Scene* s, const double* v1, double c1, const double*
 od_status launch_spmv_full(Scene* s, const double* x, double* y) {
   const int nb = s->bsr.nb;
   if (nb == 0) return OD_OK;
-  const int rows_per_cta = kThreads / kRowLanes;
-  spmv_full_kernel<double><<<nblk(nb, rows_per_cta), kThreads, 0, s->ctx->stream>>>(nb, s->bsr.row_ptr, s->bsr.col,
+  OD_KL(s);
+  spmv_full_kernel<double><<<nblk(nb, kWarpRows), kThreads, 0, s->ctx->stream>>>(nb, s->bsr.row_ptr, s->bsr.col,
                                                                                     s->A64, x, y);
   OD_CUDA(cudaGetLastError());
   return OD_OK;
@@ -582,13 +890,14 @@ static od_status ic0_factor(Scene* s) {
     OD_CUDA(cudaMemsetAsync(P.ic_bad, 0, sizeof(int), strm));
     for (int l = 0; l < P.n_levels_f; l++) {
       int l0 = P.lvl_ptr_f[l], l1 = P.lvl_ptr_f[l + 1];
+      OD_KL(s);
       ic0_factor_level<double><<<nblk(l1 - l0, 128), 128, 0, strm>>>(l0, l1, P.lvl_rows_f, P.ic_rp, P.ic_ci, P.ic_src,
                                                                       s->A64, P.ic_val, shift, P.ic_bad);
     }
     OD_CUDA(cudaGetLastError());
     int bad = 0;
     OD_CUDA(cudaMemcpyAsync(&bad, P.ic_bad, sizeof(int), cudaMemcpyDeviceToHost, strm));
-    OD_CUDA(cudaStreamSynchronize(strm));
+    OD_TRY(sync_stream(s));
     if (!bad) break;
     shift = shift == 0.0 ? 1e-3 : 2.0 * shift;
   }
@@ -601,11 +910,13 @@ static void ic0_apply(Scene* s, const double* r, double* z, const SolveScalars* 
   cudaStream_t strm = s->ctx->stream;
   for (int l = 0; l < P.n_levels_f; l++) {
     int l0 = P.lvl_ptr_f[l], l1 = P.lvl_ptr_f[l + 1];
+    OD_KL(s);
     ic0_forward_level<<<nblk(l1 - l0, 128), 128, 0, strm>>>(l0, l1, P.lvl_rows_f, P.ic_rp, P.ic_ci, P.ic_val, r,
                                                             P.q /*y*/, sc);
   }
   for (int l = 0; l < P.n_levels_b; l++) {
     int l0 = P.lvl_ptr_b[l], l1 = P.lvl_ptr_b[l + 1];
+    OD_KL(s);
     ic0_backward_level<<<nblk(l1 - l0, 128), 128, 0, strm>>>(l0, l1, P.lvl_rows_b, P.icT_rp, P.icT_ci, P.icT_pos,
                                                              P.ic_rp, P.ic_val, P.q, z, sc);
   }
@@ -615,19 +926,33 @@ od_status pcg_alloc(Scene* s) {
   Pcg& P = s->pcg;
   const int n = 3 * s->bsr.nb;
   P.n_pad = n;
-  const int rows_per_cta = kThreads / kRowLanes;
-  P.grid = std::max(nblk(s->bsr.nb, rows_per_cta), nblk(n, kThreads));
+  P.grid = std::max(1, 2 * std::max(1, s->ctx->num_sms));  // partial capacity per array
   size_t nv = std::max(1, n);
   for (double** v : {&P.x, &P.r, &P.z, &P.p, &P.q, &P.b}) {
     OD_CUDA(cudaMalloc(v, sizeof(double) * nv));
     OD_CUDA(cudaMemset(*v, 0, sizeof(double) * nv));
   }
-  OD_CUDA(cudaMalloc(&P.partial, sizeof(double) * 3 * (size_t)std::max(1, P.grid)));
+  OD_CUDA(cudaMalloc(&P.partial, sizeof(double) * 4 * (size_t)P.grid));
   OD_CUDA(cudaMalloc(&P.sc, sizeof(SolveScalars)));
   OD_CUDA(cudaMemset(P.sc, 0, sizeof(SolveScalars)));
   OD_CUDA(cudaMallocHost(&P.sc_host, sizeof(SolveScalars)));
   OD_CUDA(cudaMalloc(&P.pinv, sizeof(double) * 9 * (size_t)std::max(1, s->bsr.nb)));
-  s->device_bytes += (long long)sizeof(double) * (6 * nv + 9 * (size_t)s->bsr.nb + 3 * (size_t)P.grid);
+  OD_CUDA(cudaMalloc(&P.gbar, sizeof(GridBarrier)));
+  OD_CUDA(cudaMemset(P.gbar, 0, sizeof(GridBarrier)));
+  OD_CUDA(cudaMallocHost(&P.timeout_host, sizeof(int)));
+  // co-resident CTAs for the cooperative solve: one 768-thread CTA per SM
+  // (fewest arrivals per grid barrier; the round-robin group mapping keeps
+  // every SM's FP64 pipe equally loaded)
+  int coop = 0, bps = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, s->ctx->device);
+  if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pcg_persistent_kernel<double, 4>, kPThreads, 0) ==
+                  cudaSuccess && bps > 0) {
+    P.coop_grid = std::min(bps, 1) * std::max(1, s->ctx->num_sms);
+    P.grid = std::max(P.grid, P.coop_grid);
+  }
+  OD_CUDA(cudaFree(P.partial));
+  OD_CUDA(cudaMalloc(&P.partial, sizeof(double) * 4 * (size_t)P.grid));
+  s->device_bytes += (long long)sizeof(double) * (6 * nv + 9 * (size_t)s->bsr.nb + 4 * (size_t)P.grid);
   return OD_OK;
 }
 
@@ -637,8 +962,51 @@ void pcg_free(Scene* s) {
   for (int* v : {P.ic_rp, P.ic_ci, P.ic_src, P.lvl_rows_f, P.lvl_rows_b, P.icT_rp, P.icT_ci, P.icT_pos, P.ic_bad})
     cudaFree(v);
   cudaFree(P.sc);
+  cudaFree(P.gbar);
   if (P.sc_host) cudaFreeHost(P.sc_host);
+  if (P.timeout_host) cudaFreeHost(P.timeout_host);
   P = Pcg();
+}
+
+// true residual ||b - A x|| / ||b|| on the device, then the statistics
+static od_status pcg_finish(Scene* s, const double* d_b, double* d_x, double shift, od_solve_stats* st,
+                            bool persistent, bool timed_persistent) {
+  Pcg& P = s->pcg;
+  cudaStream_t strm = s->ctx->stream;
+  const int nb = s->bsr.nb, n = P.n_pad;
+  if (!persistent) {
+    OD_KL(s);
+    spmv_full_kernel<double><<<nblk(nb, kWarpRows), kThreads, 0, strm>>>(nb, s->bsr.row_ptr, s->bsr.col, s->A64,
+                                                                         d_x, P.q);
+    OD_KL(s);
+    residual_norm_kernel<<<1, 1024, 0, strm>>>(n, d_b, P.q, P.sc);
+    OD_CUDA(cudaGetLastError());
+  }
+  OD_CUDA(cudaMemcpyAsync(P.sc_host, P.sc, sizeof(SolveScalars), cudaMemcpyDeviceToHost, strm));
+  int timeout = 0;
+  if (P.gbar) OD_CUDA(cudaMemcpyAsync(P.timeout_host, &((GridBarrier*)P.gbar)->timeout, sizeof(int),
+                                      cudaMemcpyDeviceToHost, strm));
+  OD_TRY(sync_stream(s));
+  if (P.gbar) timeout = *P.timeout_host;
+  const SolveScalars& h = *P.sc_host;
+  if (timed_persistent) {
+    float ms = 0.f;
+    OD_CUDA(cudaEventElapsedTime(&ms, s->ctx->ev_pool[0], s->ctx->ev_pool[1]));
+    s->ctx->pcg_kernel_ms += ms;
+    s->ctx->pcg_kernel_launches++;
+    s->ctx->pcg_kernel_iters += h.iter;
+  }
+  od_status status = (od_status)h.status;
+  if (timeout) { status = OD_ERR_DEVICE_TIMEOUT; set_error("PCG grid barrier timed out"); }
+  if (status == OD_OK && h.iter >= h.max_iter && h.rr > h.eps) status = OD_ERR_NOT_CONVERGED;
+  if (st) {
+    st->iterations = h.iter;
+    st->refinements = 0;
+    st->rel_residual = h.tr_den > 0.0 ? std::sqrt(h.tr_num / h.tr_den) : std::sqrt(h.tr_num);
+    st->ic_shift = shift;
+    st->status = status;
+  }
+  return status == OD_ERR_DEVICE_TIMEOUT ? OD_ERR_DEVICE_TIMEOUT : OD_OK;
 }
 
 // Solve A64 x = b (device vectors of length n_pad; padding entries zero).
@@ -650,70 +1018,113 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
   const int nb = s->bsr.nb, n = P.n_pad;
   const int pk = prm->precond;
   if (pk < 0 || pk > OD_PRECOND_IC0) { set_error("unknown preconditioner"); return OD_ERR_INVALID_ARG; }
-  const int rows_per_cta = kThreads / kRowLanes;
-  const int g_rows = nblk(nb, rows_per_cta), g_blk = nblk(nb, kThreads), g_vec = nblk(n, kThreads);
   if (nb == 0) {
-    if (st) { *st = od_solve_stats{}; }
+    if (st) *st = od_solve_stats{};
     return OD_OK;
   }
+  const int G = P.grid;
+  const int g_rows = std::min(G, nblk(nb, kWarpRows));
+  const int g_upd = std::min(G, nblk(n, kUpdThreads));
+  const int g_vec = std::min(G, nblk(n, kThreads));
+  double* part_a = P.partial;           // p.q / init r.z
+  double* part_b = P.partial + G;       // r.r
+  double* part_c = P.partial + 2 * G;   // r.z
+  double* part_d = P.partial + 3 * G;   // init b.b
   double shift = 0.0;
   if (pk == OD_PRECOND_JACOBI || pk == OD_PRECOND_BLOCK_JACOBI) {
-    precond_setup_kernel<double><<<g_blk, kThreads, 0, strm>>>(nb, pk, s->bsr.diag_pos, s->A64, P.pinv);
+    OD_KL(s);
+    precond_setup_kernel<double><<<nblk(nb, kThreads), kThreads, 0, strm>>>(nb, pk, s->bsr.diag_pos, s->A64, P.pinv);
   } else if (pk == OD_PRECOND_IC0) {
     od_status e = ic0_factor(s);
     if (e != OD_OK) return e;
     shift = P.ic_shift;
   }
+  if (pk != OD_PRECOND_IC0 && P.coop_grid > 0 && !P.disable_persistent) {
+    // one cooperative launch for the whole solve
+    OD_CUDA(cudaMemsetAsync(P.gbar, 0, sizeof(GridBarrier), strm));
+    const int G2 = P.coop_grid;
+    const int ngroups = (nb + kRowsPerWarp - 1) / kRowsPerWarp;
+    const int warps = G2 * (kPThreads / 32);
+    const int need = (ngroups + warps - 1) / warps;   // groups per warp
+    const double tol = prm->tol;
+    const int maxit = prm->max_iter;
+    GridBarrier* gbp = (GridBarrier*)P.gbar;
+    const int* rpp = s->bsr.row_ptr;
+    const int* colp = s->bsr.col;
+    const double* Ap = s->A64;
+    double* xp = d_x;
+    int pkv = pk;
+    void* args[] = {(void*)&nb, (void*)&rpp, (void*)&colp, (void*)&Ap, (void*)&d_b, (void*)&xp, (void*)&P.r,
+                    (void*)&P.z, (void*)&P.p, (void*)&P.q, (void*)&pkv, (void*)&P.pinv, (void*)&P.partial,
+                    (void*)&tol, (void*)&maxit, (void*)&P.sc, (void*)&gbp};
+    void* fn = need <= 1 ? (void*)pcg_persistent_kernel<double, 1>
+             : need <= 2 ? (void*)pcg_persistent_kernel<double, 2>
+             : need <= 4 ? (void*)pcg_persistent_kernel<double, 4>
+                         : (void*)pcg_persistent_kernel<double, 0>;
+    const bool prof = s->ctx->profiling && s->ctx->ev_pool.size() >= 2;
+    if (prof) OD_CUDA(cudaEventRecord(s->ctx->ev_pool[0], strm));
+    OD_KL(s);
+    OD_CUDA(cudaLaunchCooperativeKernel(fn, dim3(G2), dim3(kPThreads), args, 0, strm));
+    if (prof) OD_CUDA(cudaEventRecord(s->ctx->ev_pool[1], strm));
+    return pcg_finish(s, d_b, d_x, shift, st, true, prof);
+  }
+  OD_KL(s);
   pcg_init_kernel<double><<<g_rows, kThreads, 0, strm>>>(nb, s->bsr.row_ptr, s->bsr.col, s->A64, d_b, d_x, P.r, P.z,
-                                                          P.p, pk, P.pinv, prm->tol, prm->max_iter, P.partial, P.sc);
+                                                          P.p, pk, P.pinv, part_c, part_d, part_b);
+  int g_rz0 = g_rows;
   if (pk == OD_PRECOND_IC0) {
     ic0_apply(s, P.r, P.z, nullptr);
-    pcg_rz_finish_kernel<<<g_vec, kThreads, 0, strm>>>(n, P.r, P.z, P.partial, P.sc, 1);
-    copy_kernel<<<g_vec, kThreads, 0, strm>>>(n, P.z, P.p);
+    OD_KL(s);
+    pcg_rz_kernel<<<g_vec, kThreads, 0, strm>>>(n, P.r, P.z, part_c, nullptr);
+    g_rz0 = g_vec;
+    OD_KL(s);
+    copy_kernel<<<nblk(n, kThreads), kThreads, 0, strm>>>(n, P.z, P.p);
   }
+  OD_KL(s);
+  pcg_init_finish<<<1, kThreads, 0, strm>>>(part_c, g_rz0, part_d, part_b, g_rows, prm->tol, prm->max_iter, P.sc);
   OD_CUDA(cudaGetLastError());
   // iterations are queued in chunks; every kernel returns at once after the
   // stop flag is set, and the host reads the flag between chunks
   const int chunk = 16;
+  int ev_used = 0, spmv_seen = 0;
+  long long launched = 0;
   for (;;) {
-    for (int k = 0; k < chunk; k++) {
+    for (int k = 0; k < chunk; k++, launched++) {
+      const int slot = (int)(launched & 1);
+      const bool prof = s->ctx->profiling && ev_used + 2 <= (int)s->ctx->ev_pool.size();
+      if (prof) OD_CUDA(cudaEventRecord(s->ctx->ev_pool[ev_used], strm));
+      OD_KL(s);
       pcg_spmv_kernel<double><<<g_rows, kThreads, 0, strm>>>(nb, s->bsr.row_ptr, s->bsr.col, s->A64, P.p, P.q,
-                                                              P.partial, P.sc);
+                                                              part_a, P.sc);
+      if (prof) { OD_CUDA(cudaEventRecord(s->ctx->ev_pool[ev_used + 1], strm)); ev_used += 2; }
+      OD_KL(s);
+      pcg_update_kernel<<<g_upd, kUpdThreads, 0, strm>>>(n, d_x, P.r, P.z, P.p, P.q, pk, P.pinv, part_a, g_rows,
+                                                         part_c, part_b, P.sc, slot);
+      int g_rz = g_upd;
       if (pk == OD_PRECOND_IC0) {
-        pcg_update_kernel<<<g_blk, kThreads, 0, strm>>>(nb, d_x, P.r, P.z, P.p, P.q, pk, P.pinv, P.partial, P.sc, 0);
         ic0_apply(s, P.r, P.z, P.sc);
-        pcg_rz_finish_kernel<<<g_vec, kThreads, 0, strm>>>(n, P.r, P.z, P.partial, P.sc, 0);
-        pcg_direction_kernel<<<g_vec, kThreads, 0, strm>>>(n, P.z, P.p, P.sc, 0);
-      } else {
-        pcg_update_kernel<<<g_blk, kThreads, 0, strm>>>(nb, d_x, P.r, P.z, P.p, P.q, pk, P.pinv, P.partial, P.sc, 1);
-        pcg_direction_kernel<<<g_vec, kThreads, 0, strm>>>(n, P.z, P.p, P.sc, 0);
+        OD_KL(s);
+        pcg_rz_kernel<<<g_vec, kThreads, 0, strm>>>(n, P.r, P.z, part_c, P.sc);
+        g_rz = g_vec;
       }
+      OD_KL(s);
+      pcg_direction_kernel<<<g_vec, kThreads, 0, strm>>>(n, P.z, P.p, part_c, g_rz, part_b, g_upd, P.sc, slot);
     }
     OD_CUDA(cudaGetLastError());
     OD_CUDA(cudaMemcpyAsync(P.sc_host, P.sc, sizeof(SolveScalars), cudaMemcpyDeviceToHost, strm));
-    OD_CUDA(cudaStreamSynchronize(strm));
+    OD_TRY(sync_stream(s));
+    // SpMV launches that did work (the ones after the stop flag returned at
+    // once and are not counted)
+    for (int k = 0; k + 1 < ev_used; k += 2) {
+      float ms = 0.f;
+      OD_CUDA(cudaEventElapsedTime(&ms, s->ctx->ev_pool[k], s->ctx->ev_pool[k + 1]));
+      if (k / 2 < P.sc_host->iter - spmv_seen) { s->ctx->spmv_ms += ms; s->ctx->spmv_launches++; }
+    }
+    spmv_seen = P.sc_host->iter;
+    ev_used = 0;
     if (P.sc_host->done) break;
   }
-  const SolveScalars& h = *P.sc_host;
-  // true residual ||b - A x|| / ||b||
-  spmv_full_kernel<double><<<g_rows, kThreads, 0, strm>>>(nb, s->bsr.row_ptr, s->bsr.col, s->A64, d_x, P.q);
-  OD_CUDA(cudaGetLastError());
-  std::vector<double> hb(n), hq(n);
-  OD_CUDA(cudaMemcpyAsync(hb.data(), d_b, sizeof(double) * n, cudaMemcpyDeviceToHost, strm));
-  OD_CUDA(cudaMemcpyAsync(hq.data(), P.q, sizeof(double) * n, cudaMemcpyDeviceToHost, strm));
-  OD_CUDA(cudaStreamSynchronize(strm));
-  double num = 0.0, den = 0.0;
-  for (int i = 0; i < n; i++) { double d = hb[i] - hq[i]; num += d * d; den += hb[i] * hb[i]; }
-  od_status status = (od_status)h.status;
-  if (status == OD_OK && h.iter >= h.max_iter && h.rr > h.eps) status = OD_ERR_NOT_CONVERGED;
-  if (st) {
-    st->iterations = h.iter;
-    st->refinements = 0;
-    st->rel_residual = den > 0.0 ? std::sqrt(num / den) : std::sqrt(num);
-    st->ic_shift = shift;
-    st->status = status;
-  }
-  return OD_OK;
+  return pcg_finish(s, d_b, d_x, shift, st, false, false);
 }
 
 }  // namespace od

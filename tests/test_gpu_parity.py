@@ -189,3 +189,22 @@ def test_invalid_arguments_are_rejected():
         s.step(1)  # no integrator yet
     with pytest.raises(api.ODError):
         s.setup_integrator(api.NonlinearImplicitBackwardEuler(0.01, 0.001, -1.0, api.CGSolver()))
+
+
+@pytest.mark.parametrize("precond", ["none", "jacobi", "block_jacobi"])
+def test_persistent_and_multikernel_pcg_agree(golden, precond, monkeypatch):
+    """The one-launch cooperative PCG and the multi-kernel PCG are the same
+    algorithm with different reduction orders: iteration counts within 3% and
+    solutions within 1e-8 on this badly conditioned matrix."""
+    p = golden("pattern_full")
+    e = golden("elements_neohookean_full")
+    A = e["values"] * (1.0 / 3600.0) + e["mass"]
+    out = {}
+    for flag in ("1", "0"):
+        monkeypatch.setenv("OD_GB300_PCG_PERSISTENT", flag)
+        s = api.Scene(ctx(), p["X"], p["tets"], p["facets"], p["cdofs"], material("neohookean", *e["material"]))
+        out[flag] = s.pcg(A, e["cg_b"], solver=api.CGSolver(1e-10, 3000, api.Preconditioner(precond)))
+    (x1, s1), (x0, s0) = out["1"], out["0"]
+    assert s1.status == 0 and s0.status == 0
+    assert abs(s1.iterations - s0.iterations) <= max(2, 0.03 * s0.iterations)
+    assert rel_err(x1, x0) <= 1e-8
