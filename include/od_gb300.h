@@ -235,6 +235,26 @@ od_status od_step(od_scene* scene, int n_steps, od_step_stats* stats);
 od_status od_get_state(od_scene* scene, double* d, double* v, double* a);
 od_status od_set_state(od_scene* scene, const double* d, const double* v, const double* a);
 
+/* Allocation-free PCG.  No counterpart in the reference.  For callers that
+ * cannot allocate device memory -- a host application whose own allocator
+ * owns the GPU's memory, or a plugin running inside another program's
+ * capture or real-time loop -- this solves A x = b with the none, Jacobi or
+ * block-Jacobi preconditioner (FP64) for a full block-CSR matrix the caller
+ * already holds on the device: nb block rows, row pointers d_row_ptr[nb+1],
+ * block columns d_col[], 9 row-major values per 3x3 block in d_values[];
+ * d_b and d_x have 3*nb entries, d_x is the warm start and the result.
+ * Every work vector lives in one fixed device array inside the library
+ * (OD_NOALLOC_MAX_BLOCK_ROWS block rows at most, about 5.5 MB, held by every
+ * GPU that loads the library until exit); the call allocates nothing.
+ * Larger systems are rejected with OD_ERR_INVALID_ARG.  The array is shared:
+ * calls that overlap on the GPU race, so callers serialise them.  The first
+ * call on a device looks up the array's device address; make it before any
+ * stream capture.  stream is a cudaStream_t (NULL: the default stream). */
+#define OD_NOALLOC_MAX_BLOCK_ROWS 32768
+od_status od_bsr_pcg_noalloc(int nb, const int* d_row_ptr, const int* d_col, const double* d_values,
+                             const double* d_b, double* d_x, const od_solver_params* params,
+                             void* stream, od_solve_stats* stats);
+
 /* Checkpoint / resume: mesh displacement + integrator vectors as a host blob.
  * Call with buf == NULL to query the size. */
 od_status od_scene_save(od_scene* scene, void* buf, size_t* size);

@@ -149,6 +149,8 @@ SIGNATURES = {
     "od_step": (C.c_int, [_vp, C.c_int, C.POINTER(od_step_stats)]),
     "od_get_state": (C.c_int, [_vp, _dp, _dp, _dp]),
     "od_set_state": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "od_bsr_pcg_noalloc": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, C.POINTER(od_solver_params), _vp,
+                                     C.POINTER(od_solve_stats)]),
     "od_scene_save": (C.c_int, [_vp, _vp, C.POINTER(C.c_size_t)]),
     "od_scene_load": (C.c_int, [_vp, _vp, C.c_size_t]),
 }
