@@ -89,6 +89,9 @@ struct Pcg {
   int* timeout_host = nullptr;  // pinned
   int coop_grid = 0;            // co-resident CTAs, 0 if cooperative launch is unavailable
   int disable_persistent = 0;
+  // mixed precision (lazily allocated)
+  float* v32 = nullptr;         // d, r, z, p, q (n each) + block-Jacobi (9 per block row)
+  double* r64 = nullptr;        // outer FP64 residual
 };
 
 struct Ctx {

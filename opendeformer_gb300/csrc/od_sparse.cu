@@ -681,6 +681,219 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
   }
 }
 
+// --------------------------------------------------- mixed precision
+// Inner solve of the iterative refinement: PCG on the FP32 copy of A with
+// FP32 vectors, FP32 SpMV with FP32 accumulation and an FP32 block-Jacobi /
+// Jacobi apply.  Dot products are accumulated per thread in compensated FP32
+// (error-free TwoProduct by FMA and TwoSum, i.e. twice-FP32 accuracy on the
+// FP32 units) and reduced across threads and CTAs in FP64.
+
+struct Comp { float s, c; };
+__device__ __forceinline__ void comp_add_prod(Comp& a, float x, float y) {
+  const float p = x * y;
+  const float e = fmaf(x, y, -p);       // x*y = p + e exactly
+  const float s = a.s + p;
+  const float z = s - a.s;
+  const float t = (a.s - (s - z)) + (p - z);  // a.s + p = s + t exactly
+  a.s = s;
+  a.c += t + e;
+}
+__device__ __forceinline__ double comp_value(const Comp& a) { return (double)a.s + (double)a.c; }
+
+__device__ __forceinline__ float bsr_subrow32(int row, int r, const int* __restrict__ rp, const int* __restrict__ col,
+                                              const float* __restrict__ A, const float* __restrict__ x) {
+  float y = 0.f;
+  const int kb = rp[row], ke = rp[row + 1];
+  for (int k = kb; k < ke; k++) {
+    const float* a = A + (size_t)k * 9 + 3 * r;
+    const int c = 3 * col[k];
+    y = fmaf(a[0], x[c], y);
+    y = fmaf(a[1], x[c + 1], y);
+    y = fmaf(a[2], x[c + 2], y);
+  }
+  return y;
+}
+
+// FP32 Jacobi / block-Jacobi from the FP64 diagonal blocks
+__global__ void precond_setup32_kernel(int nb, int kind, const int* __restrict__ diag_pos, const double* __restrict__ A,
+                                       float* __restrict__ pinv) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  const double* a = A + (size_t)diag_pos[i] * 9;
+  if (kind == OD_PRECOND_JACOBI) {
+    for (int d = 0; d < 3; d++) pinv[3 * i + d] = (float)(a[4 * d] > 0.0 ? 1.0 / a[4 * d] : 1.0);
+  } else {
+    double m[9];
+    for (int k = 0; k < 9; k++) m[k] = a[k];
+    const double det = m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+                       m[2] * (m[3] * m[7] - m[4] * m[6]);
+    const double inv = 1.0 / det;
+    float* o = pinv + 9 * (size_t)i;
+    o[0] = (float)((m[4] * m[8] - m[5] * m[7]) * inv);
+    o[1] = (float)((m[2] * m[7] - m[1] * m[8]) * inv);
+    o[2] = (float)((m[1] * m[5] - m[2] * m[4]) * inv);
+    o[3] = (float)((m[5] * m[6] - m[3] * m[8]) * inv);
+    o[4] = (float)((m[0] * m[8] - m[2] * m[6]) * inv);
+    o[5] = (float)((m[2] * m[3] - m[0] * m[5]) * inv);
+    o[6] = (float)((m[3] * m[7] - m[4] * m[6]) * inv);
+    o[7] = (float)((m[1] * m[6] - m[0] * m[7]) * inv);
+    o[8] = (float)((m[0] * m[4] - m[1] * m[3]) * inv);
+  }
+}
+
+// r64 = b - A64 x64 (FP64) and partials of r.r, b.b
+__global__ void refine_residual_kernel(int nb, const int* __restrict__ rp, const int* __restrict__ col,
+                                       const double* __restrict__ A, const double* __restrict__ b,
+                                       const double* __restrict__ x, double* __restrict__ r, double* __restrict__ part) {
+  const int lane = threadIdx.x & 31;
+  const int warp_global = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+  double rr = 0.0, bb = 0.0;
+  for (int wb = warp_global * kRowsPerWarp; wb < nb; wb += gridDim.x * kWarpRows) {
+    const int row = wb + lane / 3, rs = lane % 3;
+    if (lane < 30 && row < nb) {
+      const int i = 3 * row + rs;
+      const double rv = b[i] - bsr_subrow<double, double>(row, rs, rp, col, A, x);
+      r[i] = rv;
+      rr = fma(rv, rv, rr);
+      bb = fma(b[i], b[i], bb);
+    }
+  }
+  double t0 = block_sum(rr), t1 = block_sum(bb);
+  if (threadIdx.x == 0) { part[2 * blockIdx.x] = t0; part[2 * blockIdx.x + 1] = t1; }
+}
+
+__global__ void refine_norm_finish(const double* __restrict__ part, int g, SolveScalars* sc) {
+  double a = 0.0, b = 0.0;
+  for (int j = threadIdx.x; j < g; j += blockDim.x) { a += part[2 * j]; b += part[2 * j + 1]; }
+  double t0 = block_sum(a), t1 = block_sum(b);
+  if (threadIdx.x == 0) { sc->tr_num = t0; sc->tr_den = t1; }
+}
+
+// x64 += d32
+__global__ void refine_update_kernel(int n, const float* __restrict__ d, double* __restrict__ x) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] += (double)d[i];
+}
+
+// Inner FP32 PCG, one cooperative launch: solves A32 d = r64 from d = 0 until
+// ||r_inner|| <= inner_tol ||r64|| or max_iter (vectors stream from memory).
+__global__ void __launch_bounds__(kPThreads, 1) pcg32_inner_kernel(
+    int nb, const int* __restrict__ rp, const int* __restrict__ col, const float* __restrict__ A,
+    const double* __restrict__ rhs, float* __restrict__ d, float* __restrict__ r, float* __restrict__ z,
+    float* __restrict__ p, float* __restrict__ q, int pkind, const float* __restrict__ pinv,
+    double* __restrict__ part, double inner_tol, int max_iter, SolveScalars* sc, GridBarrier* gb) {
+  const int G = gridDim.x;
+  double* part_1 = part;
+  double* part_2 = part + G;
+  const int lane = threadIdx.x & 31;
+  const int wpc = kPThreads / 32;
+  const int w = threadIdx.x >> 5;
+  const int ngroups = (nb + kRowsPerWarp - 1) / kRowsPerWarp;
+  const int gstride = G * wpc;
+  const int g0 = w * G + blockIdx.x;
+  const int rsub = lane % 3;
+  const int lbase = lane - rsub;
+
+  auto apply_precond = [&](int row, bool valid, float rl) {
+    float r0 = __shfl_sync(0xffffffffu, rl, lbase < 32 ? lbase : 0);
+    float r1 = __shfl_sync(0xffffffffu, rl, lbase + 1 < 32 ? lbase + 1 : 0);
+    float r2 = __shfl_sync(0xffffffffu, rl, lbase + 2 < 32 ? lbase + 2 : 0);
+    if (!valid) return 0.f;
+    if (pkind == OD_PRECOND_JACOBI) return pinv[3 * row + rsub] * rl;
+    if (pkind == OD_PRECOND_BLOCK_JACOBI) {
+      const float* m = pinv + 9 * (size_t)row + 3 * rsub;
+      return fmaf(m[0], r0, fmaf(m[1], r1, m[2] * r2));
+    }
+    return rl;
+  };
+
+  // init: d = 0, r = rhs, z = M^-1 r, p = z
+  Comp crz{0.f, 0.f}, crr{0.f, 0.f};
+  for (int g = g0; g < ngroups; g += gstride) {
+    const int row = g * kRowsPerWarp + lane / 3;
+    const bool valid = lane < 30 && row < nb;
+    const int i = 3 * row + rsub;
+    float rl = 0.f;
+    if (valid) {
+      rl = (float)rhs[i];
+      r[i] = rl;
+      d[i] = 0.f;
+    }
+    const float zl = apply_precond(row, valid, rl);
+    if (valid) {
+      z[i] = zl;
+      p[i] = zl;
+      comp_add_prod(crz, rl, zl);
+      comp_add_prod(crr, rl, rl);
+    }
+  }
+  double rz, rr;
+  {
+    double v2[2] = {comp_value(crz), comp_value(crr)};
+    if (!grid_sums<2>(v2, part_2, gb)) return;
+    rz = v2[0];
+    rr = v2[1];
+  }
+  const double eps = rr * inner_tol * inner_tol;
+  int it = 0;
+  int status = isfinite(rr) ? OD_OK : OD_ERR_NAN;
+  while (status == OD_OK && it < max_iter && rr > eps) {
+    Comp cpq{0.f, 0.f};
+    for (int g = g0; g < ngroups; g += gstride) {
+      const int row = g * kRowsPerWarp + lane / 3;
+      if (lane < 30 && row < nb) {
+        const int i = 3 * row + rsub;
+        const float y = bsr_subrow32(row, rsub, rp, col, A, p);
+        q[i] = y;
+        comp_add_prod(cpq, p[i], y);
+      }
+    }
+    double v1[1] = {comp_value(cpq)};
+    if (!grid_sums<1>(v1, part_1, gb)) return;
+    const float alpha = (float)(rz / v1[0]);
+    Comp cz{0.f, 0.f}, cr{0.f, 0.f};
+    for (int g = g0; g < ngroups; g += gstride) {
+      const int row = g * kRowsPerWarp + lane / 3;
+      const bool valid = lane < 30 && row < nb;
+      const int i = 3 * row + rsub;
+      float rl = 0.f;
+      if (valid) {
+        d[i] = fmaf(alpha, p[i], d[i]);
+        rl = fmaf(-alpha, q[i], r[i]);
+        r[i] = rl;
+      }
+      const float zl = apply_precond(row, valid, rl);
+      if (valid) {
+        z[i] = zl;
+        comp_add_prod(cz, rl, zl);
+        comp_add_prod(cr, rl, rl);
+      }
+    }
+    double v2[2] = {comp_value(cz), comp_value(cr)};
+    if (!grid_sums<2>(v2, part_2, gb)) return;
+    const double beta = v2[0] / rz;
+    rz = v2[0];
+    rr = v2[1];
+    it++;
+    if (!isfinite(rr) || !isfinite(beta)) status = OD_ERR_NAN;
+    const float bf = (float)beta;
+    for (int g = g0; g < ngroups; g += gstride) {
+      const int row = g * kRowsPerWarp + lane / 3;
+      if (lane < 30 && row < nb) {
+        const int i = 3 * row + rsub;
+        p[i] = fmaf(bf, p[i], z[i]);
+      }
+    }
+    if (!grid_barrier(gb)) return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sc->iter = it;
+    sc->rr = rr;
+    sc->status = status;
+    sc->done = 1;
+  }
+}
+
 // ----------------------------------------------------------------- IC(0)
 // Shifted IC(0) of the padded scalar lower pattern (a row-oriented,
 // level-scheduled factorisation; no reference counterpart).  Rows of one
@@ -764,6 +977,12 @@ od_status launch_expand(Scene* s, const double* v1, double c1, const double* v2,
       total, s->bsr.desc_kind, s->bsr.desc_off, s->bsr.gen, v1, c1, v2, c2, v3, c3, s->A64);
   OD_CUDA(cudaGetLastError());
   return OD_OK;
+}
+
+// FP32 copy of A64 for the inner mixed-precision solve
+__global__ void to_fp32_kernel(long long n, const double* __restrict__ a, float* __restrict__ b) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
 }
 
 od_status launch_spmv_lower(Scene* s, const double* v1, double c1, const double* x1, const double* v2, double c2,
@@ -963,6 +1182,8 @@ void pcg_free(Scene* s) {
     cudaFree(v);
   cudaFree(P.sc);
   cudaFree(P.gbar);
+  cudaFree(P.v32);
+  cudaFree(P.r64);
   if (P.sc_host) cudaFreeHost(P.sc_host);
   if (P.timeout_host) cudaFreeHost(P.timeout_host);
   P = Pcg();
@@ -1009,6 +1230,110 @@ static od_status pcg_finish(Scene* s, const double* d_b, double* d_x, double shi
   return status == OD_ERR_DEVICE_TIMEOUT ? OD_ERR_DEVICE_TIMEOUT : OD_OK;
 }
 
+// Mixed-precision solve: FP64 iterative refinement around the FP32 inner
+// PCG.  Every outer sweep recomputes the true residual b - A x in FP64 (the
+// residual replacement), solves A32 d = r to inner_tol relative with the FP32
+// PCG, and adds d to x in FP64; it stops when ||b - A x|| <= tol ||b||.
+static od_status pcg_solve_mixed(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm,
+                                 od_solve_stats* st) {
+  Pcg& P = s->pcg;
+  cudaStream_t strm = s->ctx->stream;
+  const int nb = s->bsr.nb, n = P.n_pad;
+  const int pk = prm->precond;
+  if (pk == OD_PRECOND_IC0) { set_error("mixed precision supports the none, Jacobi and block-Jacobi preconditioners"); return OD_ERR_UNSUPPORTED; }
+  if (P.coop_grid <= 0) { set_error("mixed precision needs cooperative launch"); return OD_ERR_UNSUPPORTED; }
+  // lazily allocated FP32 storage
+  if (!s->A32) {
+    OD_CUDA(cudaMalloc(&s->A32, sizeof(float) * 9 * (size_t)s->bsr.nnzb));
+    OD_CUDA(cudaMalloc(&P.v32, sizeof(float) * (5 * (size_t)n + 9 * (size_t)nb)));
+    OD_CUDA(cudaMalloc(&P.r64, sizeof(double) * (size_t)n));
+    s->device_bytes += (long long)sizeof(float) * (9 * (size_t)s->bsr.nnzb + 5 * (size_t)n + 9 * (size_t)nb) +
+                       (long long)sizeof(double) * n;
+  }
+  float* d32 = P.v32;
+  float* r32 = d32 + n;
+  float* z32 = r32 + n;
+  float* p32 = z32 + n;
+  float* q32 = p32 + n;
+  float* pinv32 = q32 + n;
+  const long long nv = 9LL * s->bsr.nnzb;
+  OD_KL(s);
+  to_fp32_kernel<<<nblk(nv, kThreads), kThreads, 0, strm>>>(nv, s->A64, s->A32);
+  if (pk != OD_PRECOND_NONE) {
+    OD_KL(s);
+    precond_setup32_kernel<<<nblk(nb, kThreads), kThreads, 0, strm>>>(nb, pk, s->bsr.diag_pos, s->A64, pinv32);
+  }
+  const double inner_tol = prm->inner_tol > 0.0 ? prm->inner_tol : 1e-4;
+  const int max_refine = prm->max_refine > 0 ? prm->max_refine : 20;
+  const int g_res = std::min(P.grid / 2, nblk(nb, kWarpRows));
+  auto residual = [&]() -> od_status {
+    OD_KL(s);
+    refine_residual_kernel<<<g_res, kThreads, 0, strm>>>(nb, s->bsr.row_ptr, s->bsr.col, s->A64, d_b, d_x, P.r64,
+                                                         P.partial);
+    OD_KL(s);
+    refine_norm_finish<<<1, kThreads, 0, strm>>>(P.partial, g_res, P.sc);
+    OD_CUDA(cudaGetLastError());
+    OD_CUDA(cudaMemcpyAsync(P.sc_host, P.sc, sizeof(SolveScalars), cudaMemcpyDeviceToHost, strm));
+    OD_TRY(sync_stream(s));
+    return OD_OK;
+  };
+  OD_TRY(residual());
+  const double bb = P.sc_host->tr_den;
+  double rr = P.sc_host->tr_num;
+  const double eps = bb * prm->tol * prm->tol;
+  int total_it = 0, sweeps = 0;
+  od_status status = std::isfinite(rr) ? OD_OK : OD_ERR_NAN;
+  const int G2 = P.coop_grid;
+  const bool prof = s->ctx->profiling && s->ctx->ev_pool.size() >= 2;
+  while (status == OD_OK && rr > eps && sweeps < max_refine && total_it < prm->max_iter) {
+    OD_CUDA(cudaMemsetAsync(P.gbar, 0, sizeof(GridBarrier), strm));
+    int maxit = prm->max_iter - total_it;
+    GridBarrier* gbp = (GridBarrier*)P.gbar;
+    const int* rpp = s->bsr.row_ptr;
+    const int* colp = s->bsr.col;
+    const float* Ap = s->A32;
+    const double* rhs = P.r64;
+    int pkv = pk;
+    double itol = inner_tol;
+    int nbv = nb;
+    void* args[] = {(void*)&nbv, (void*)&rpp, (void*)&colp, (void*)&Ap, (void*)&rhs, (void*)&d32, (void*)&r32,
+                    (void*)&z32, (void*)&p32, (void*)&q32, (void*)&pkv, (void*)&pinv32, (void*)&P.partial,
+                    (void*)&itol, (void*)&maxit, (void*)&P.sc, (void*)&gbp};
+    if (prof) OD_CUDA(cudaEventRecord(s->ctx->ev_pool[0], strm));
+    OD_KL(s);
+    OD_CUDA(cudaLaunchCooperativeKernel((void*)pcg32_inner_kernel, dim3(G2), dim3(kPThreads), args, 0, strm));
+    if (prof) OD_CUDA(cudaEventRecord(s->ctx->ev_pool[1], strm));
+    OD_KL(s);
+    refine_update_kernel<<<nblk(n, kThreads), kThreads, 0, strm>>>(n, d32, d_x);
+    OD_CUDA(cudaMemcpyAsync(P.timeout_host, &((GridBarrier*)P.gbar)->timeout, sizeof(int), cudaMemcpyDeviceToHost,
+                            strm));
+    OD_TRY(residual());  // also brings back the inner statistics
+    if (*P.timeout_host) { set_error("PCG grid barrier timed out"); status = OD_ERR_DEVICE_TIMEOUT; break; }
+    const int inner_it = P.sc_host->iter;
+    if (prof) {
+      float ms = 0.f;
+      OD_CUDA(cudaEventElapsedTime(&ms, s->ctx->ev_pool[0], s->ctx->ev_pool[1]));
+      s->ctx->pcg_kernel_ms += ms;
+      s->ctx->pcg_kernel_launches++;
+      s->ctx->pcg_kernel_iters += inner_it;
+    }
+    total_it += inner_it;
+    sweeps++;
+    rr = P.sc_host->tr_num;
+    if (!std::isfinite(rr)) status = OD_ERR_NAN;
+    if (inner_it == 0) break;  // no progress possible
+  }
+  if (status == OD_OK && rr > eps) status = OD_ERR_NOT_CONVERGED;
+  if (st) {
+    st->iterations = total_it;
+    st->refinements = sweeps;
+    st->rel_residual = bb > 0.0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+    st->ic_shift = 0.0;
+    st->status = status;
+  }
+  return status == OD_ERR_DEVICE_TIMEOUT ? OD_ERR_DEVICE_TIMEOUT : OD_OK;
+}
+
 // Solve A64 x = b (device vectors of length n_pad; padding entries zero).
 // The preconditioner is rebuilt from A64 first, as CGSolver does on every
 // solve (cgSolver.cpp:23).
@@ -1022,6 +1347,7 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
     if (st) *st = od_solve_stats{};
     return OD_OK;
   }
+  if (prm->precision == OD_PRECISION_MIXED) return pcg_solve_mixed(s, d_b, d_x, prm, st);
   const int G = P.grid;
   const int g_rows = std::min(G, nblk(nb, kWarpRows));
   const int g_upd = std::min(G, nblk(n, kUpdThreads));

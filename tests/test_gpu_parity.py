@@ -208,3 +208,36 @@ def test_persistent_and_multikernel_pcg_agree(golden, precond, monkeypatch):
     assert s1.status == 0 and s0.status == 0
     assert abs(s1.iterations - s0.iterations) <= max(2, 0.03 * s0.iterations)
     assert rel_err(x1, x0) <= 1e-8
+
+
+@pytest.mark.parametrize("precond", ["none", "jacobi", "block_jacobi"])
+def test_mixed_precision_solve_reaches_fp64_tolerance(golden, precond):
+    """FP32 inner PCG + FP64 refinement reaches the same true-residual
+    tolerance as the FP64 solve and the same solution."""
+    p = golden("pattern_full")
+    e = golden("elements_stvk_full")
+    A = e["values"] * (1.0 / 3600.0) + e["mass"]
+    s = api.Scene(ctx(), p["X"], p["tets"], p["facets"], p["cdofs"], material("stvk", *e["material"]))
+    x64, s64 = s.pcg(A, e["cg_b"], solver=api.CGSolver(1e-10, 3000, api.Preconditioner(precond)))
+    xm, sm = s.pcg(A, e["cg_b"], solver=api.CGSolver(1e-10, 3000, api.Preconditioner(precond), precision="mixed"))
+    assert sm.status == 0 and sm.refinements >= 1
+    assert sm.rel_residual <= 1e-10
+    assert rel_err(xm, x64) <= 1e-8
+
+
+def test_mixed_precision_newmark_within_1e6_of_fp64():
+    g = meshgen.tet_grid(12, 4, 4, h=0.05, jitter=0.15, seed=2)
+    cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+    mat = api.InvertibleNeoHookeanMaterial(1000.0, 98640.0, 0.4506, 0.1)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        s = api.Scene(ctx(), g.X, g.tets, g.facets, cd, mat)
+        s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, 0.01, 0.001, 1 / 120,
+                                                 api.CGSolver(1e-10, 3000, api.BlockJacobiPreconditioner(),
+                                                              precision=prec), 3))
+        s.set_loads(tractions=[([0.0, -500.0, 0.0], g.face_facets(0, 1))])
+        s.set_traction_schedule(2.0)
+        st = s.step(20)
+        assert st.status == 0
+        out[prec] = s.displacements()
+    assert rel_err(out["mixed"], out["fp64"]) <= 1e-6
