@@ -223,7 +223,7 @@ static void scene_free(Scene* s) {
   for (void* p : {(void*)s->X, (void*)s->u, (void*)s->tets, (void*)s->pre, (void*)s->emap, (void*)s->gdof,
                   (void*)s->perm, (void*)s->free_pos, (void*)s->node_dof, (void*)s->facets_dev, (void*)s->node_vol4,
                   (void*)s->K, (void*)s->M, (void*)s->Dm, (void*)s->fint, (void*)s->fext, (void*)s->work_vals,
-                  (void*)s->A64, (void*)s->A32, (void*)s->v, (void*)s->d, (void*)s->a, (void*)s->dp, (void*)s->vp,
+                  (void*)s->A64, (void*)s->v, (void*)s->d, (void*)s->a, (void*)s->dp, (void*)s->vp,
                   (void*)s->dv, (void*)s->rhs, (void*)s->tmp, (void*)s->trac_facets, (void*)s->trac_vec,
                   (void*)s->bsr.row_ptr, (void*)s->bsr.col, (void*)s->bsr.desc_off, (void*)s->bsr.desc_kind,
                   (void*)s->bsr.gen, (void*)s->bsr.diag_pos, (void*)s->tmp2, (void*)s->stage_k,
@@ -307,6 +307,8 @@ static od_status scene_build(Scene* s, int n_nodes, const double* X, int n_tets,
   OD_TRY(dupload(s, &s->bsr.desc_kind, hb.desc_kind.data(), hb.desc_kind.size()));
   OD_TRY(dupload(s, &s->bsr.gen, hb.gen.data(), hb.gen.size()));
   OD_TRY(dupload(s, &s->bsr.diag_pos, hb.diag_pos.data(), hb.diag_pos.size()));
+  s->hbsr_rp = std::move(hb.row_ptr);   // kept for the mixed-precision slice layout
+  s->hbsr_col = std::move(hb.col);
   OD_TRY(dalloc(s, &s->A64, 9 * (size_t)s->bsr.nnzb));
   OD_TRY(pcg_alloc(s));
   // OD_GB300_PCG_PERSISTENT=0 selects the multi-kernel PCG for every preconditioner

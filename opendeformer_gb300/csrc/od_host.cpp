@@ -317,4 +317,58 @@ void build_ic_levels(const std::vector<int>& rp, const std::vector<int>& ci, int
   for (int i = 0; i < n; i++) rows_by_level[pos[lvl[i]]++] = i;
 }
 
+// Slice structure of the FP32 inner-solve matrix (SELL-C-sigma with C =
+// kSliceRows, sigma = kSliceWindow): block rows are ordered by block count,
+// longest first, within each window (stable, so equal rows keep mesh order),
+// cut into slices, and every slice is padded to its longest row rounded up
+// to an even step count (so every slice starts on a 16-byte boundary of the
+// value and column arrays, as bulk copies require).  Padding slots point at
+// the slot's own slice row and take the value zero.
+void build_sliced(const std::vector<int>& row_ptr, const std::vector<int>& col, int nb, HostSliced& out) {
+  const int S = kSliceRows;
+  const int ns = (nb + S - 1) / S;
+  out.ns = ns;
+  std::vector<int> order(nb);
+  for (int i = 0; i < nb; i++) order[i] = i;
+  auto len = [&](int r) { return row_ptr[r + 1] - row_ptr[r]; };
+  for (int w0 = 0; w0 < nb; w0 += kSliceWindow) {
+    const int w1 = std::min(nb, w0 + kSliceWindow);
+    std::stable_sort(order.begin() + w0, order.begin() + w1, [&](int a, int b) { return len(a) > len(b); });
+  }
+  std::vector<int> inv(nb);
+  out.perm.assign((size_t)ns * S, -1);
+  for (int i = 0; i < nb; i++) {
+    out.perm[i] = order[i];
+    inv[order[i]] = i;
+  }
+  out.off.assign(ns + 1, 0);
+  for (int sl = 0; sl < ns; sl++) {
+    int m = 0;
+    for (int t = 0; t < S; t++) {
+      const int r = out.perm[(size_t)sl * S + t];
+      if (r >= 0) m = std::max(m, len(r));
+    }
+    out.off[sl + 1] = out.off[sl] + m + (m & 1);
+  }
+  const size_t steps = (size_t)out.off[ns];
+  out.col.assign(steps * S, 0);
+  out.src.assign(steps * S, -1);
+  for (int sl = 0; sl < ns; sl++) {
+    for (int t = 0; t < S; t++) {
+      const int rs = sl * S + t;
+      const int r = out.perm[rs];
+      const int k0 = out.off[sl], k1 = out.off[sl + 1];
+      int m = 0;
+      if (r >= 0) {
+        m = len(r);
+        for (int j = 0; j < m; j++) {
+          out.col[(size_t)(k0 + j) * S + t] = inv[col[row_ptr[r] + j]];
+          out.src[(size_t)(k0 + j) * S + t] = row_ptr[r] + j;
+        }
+      }
+      for (int k = k0 + m; k < k1; k++) out.col[(size_t)k * S + t] = rs;
+    }
+  }
+}
+
 }  // namespace od

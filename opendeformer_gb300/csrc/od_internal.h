@@ -89,10 +89,28 @@ struct Pcg {
   int* timeout_host = nullptr;  // pinned
   int coop_grid = 0;            // co-resident CTAs, 0 if cooperative launch is unavailable
   int disable_persistent = 0;
-  // mixed precision (lazily allocated)
-  float* v32 = nullptr;         // d, r, z, p, q (n each) + block-Jacobi (9 per block row)
+  // mixed precision (lazily allocated).  The FP32 matrix is stored in slices
+  // of kSliceRows block rows (rows sorted by block count, longest first,
+  // within windows of kSliceWindow rows); the k-th blocks of a slice's rows
+  // sit together, values [step][j][lane] with lane = 3*row_in_slice + r, so a
+  // warp reads each step as three contiguous 120-byte runs.  Inner vectors
+  // are in slice order: element 30*slice + lane.
+  int sl_ns = 0;                // slices
+  long long sl_steps = 0;       // sum over slices of the (even) padded length
+  std::vector<int> sl_off_host; // sl_off on the host
+  int sl_cta_grid = 0;          // grid size sl_cta was cut for
+  int* sl_cta = nullptr;        // sl_cta_grid+1: first slice of each CTA
+  int* sl_perm = nullptr;       // sl_ns*kSliceRows: slice row -> block row, -1 padding
+  int* sl_off = nullptr;        // sl_ns+1: first step of each slice
+  int* sl_col = nullptr;        // sl_steps*kSliceRows: block column as a slice row
+  int* sl_src = nullptr;        // sl_steps*kSliceRows: full-BSR block, -1 padding
+  float* sl_val = nullptr;      // sl_steps*90
+  float* v32 = nullptr;         // p (float4 per slice row), d, r, z, q (30 per slice), preconditioner (90 per slice)
   double* r64 = nullptr;        // outer FP64 residual
 };
+
+constexpr int kSliceRows = 10;      // block rows per slice (3 lanes each, 30 of a warp's 32)
+constexpr int kSliceWindow = 320;   // rows sorted by length inside windows of this many rows
 
 struct Ctx {
   int device = 0;
@@ -121,6 +139,7 @@ struct Scene {
   std::vector<double> hX;
   std::vector<int> htets, hfacets, hcd, hfree_pos, hnode_dof;
   std::vector<int> hpcol, hrows, horis, hemap;
+  std::vector<int> hbsr_rp, hbsr_col;   // full BSR row pointers / block columns
   int nbc = 0, nrem = 0, nvals = 0;
   std::vector<int> color_off;      // element colour ranges (colour order)
   std::vector<int> elem_perm;      // colour-order position -> original element
@@ -148,8 +167,7 @@ struct Scene {
   double* stage_f = nullptr;       // SoA [12][n_tets] element forces
   FullBsr bsr;
   void* A = nullptr;               // full BSR values (double or float)
-  double* A64 = nullptr;           // FP64 full values (mixed path keeps both)
-  float* A32 = nullptr;
+  double* A64 = nullptr;           // FP64 full values
   Pcg pcg;
   // integrator
   od_integrator_params ip{};
@@ -199,6 +217,11 @@ struct HostBsr {
 };
 void build_full_bsr(int dofs, int nbc, int nrem, const std::vector<int>& pcol,
                     const std::vector<int>& rows, const std::vector<int>& oris, HostBsr& out);
+struct HostSliced {
+  int ns = 0;
+  std::vector<int> perm, off, col, src;
+};
+void build_sliced(const std::vector<int>& row_ptr, const std::vector<int>& col, int nb, HostSliced& out);
 void build_ic_levels(const std::vector<int>& rp, const std::vector<int>& ci, int n,
                      std::vector<int>& rows_by_level, std::vector<int>& lvl_ptr, bool forward);
 

@@ -20,7 +20,6 @@
 
 namespace od {
 
-constexpr int kRowLanes = 16;     // lanes per block row in the SpMV kernels
 constexpr int kThreads = 256;
 
 __constant__ int c_di3[3] = {0, 3, 5};
@@ -700,45 +699,58 @@ __device__ __forceinline__ void comp_add_prod(Comp& a, float x, float y) {
 }
 __device__ __forceinline__ double comp_value(const Comp& a) { return (double)a.s + (double)a.c; }
 
-__device__ __forceinline__ float bsr_subrow32(int row, int r, const int* __restrict__ rp, const int* __restrict__ col,
-                                              const float* __restrict__ A, const float* __restrict__ x) {
-  float y = 0.f;
-  const int kb = rp[row], ke = rp[row + 1];
-  for (int k = kb; k < ke; k++) {
-    const float* a = A + (size_t)k * 9 + 3 * r;
-    const int c = 3 * col[k];
-    y = fmaf(a[0], x[c], y);
-    y = fmaf(a[1], x[c + 1], y);
-    y = fmaf(a[2], x[c + 2], y);
-  }
-  return y;
+// ---- sliced FP32 matrix (the layout is described with Pcg::sl_val)
+
+// sl_val from the FP64 full-BSR values: value v = [step][j][lane]
+__global__ void sliced_fill_kernel(long long nval, const int* __restrict__ src, const double* __restrict__ A64,
+                                   float* __restrict__ val) {
+  const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (v >= nval) return;
+  const long long step = v / 90;
+  const int rem = (int)(v - step * 90);
+  const int j = rem / 30, lane = rem - 30 * j;
+  const int blk = src[step * kSliceRows + lane / 3];
+  val[v] = blk >= 0 ? (float)A64[(size_t)blk * 9 + 3 * (lane % 3) + j] : 0.f;
 }
 
-// FP32 Jacobi / block-Jacobi from the FP64 diagonal blocks
-__global__ void precond_setup32_kernel(int nb, int kind, const int* __restrict__ diag_pos, const double* __restrict__ A,
-                                       float* __restrict__ pinv) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nb) return;
-  const double* a = A + (size_t)diag_pos[i] * 9;
+// FP32 Jacobi (30 per slice) or block-Jacobi (90 per slice, [j][lane]) from
+// the FP64 diagonal blocks, in slice order; padding rows get zeros
+__global__ void sliced_precond_kernel(int nrs, int kind, const int* __restrict__ perm,
+                                      const int* __restrict__ diag_pos, const double* __restrict__ A,
+                                      float* __restrict__ pinv) {
+  const int rs = blockIdx.x * blockDim.x + threadIdx.x;
+  if (rs >= nrs) return;
+  const int sl = rs / kSliceRows, t = rs - sl * kSliceRows;
+  const int row = perm[rs];
   if (kind == OD_PRECOND_JACOBI) {
-    for (int d = 0; d < 3; d++) pinv[3 * i + d] = (float)(a[4 * d] > 0.0 ? 1.0 / a[4 * d] : 1.0);
-  } else {
-    double m[9];
-    for (int k = 0; k < 9; k++) m[k] = a[k];
+    for (int d = 0; d < 3; d++) {
+      float v = 0.f;
+      if (row >= 0) {
+        const double a = A[(size_t)diag_pos[row] * 9 + 4 * d];
+        v = (float)(a > 0.0 ? 1.0 / a : 1.0);
+      }
+      pinv[(size_t)30 * sl + 3 * t + d] = v;
+    }
+    return;
+  }
+  double o[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (row >= 0) {
+    const double* m = A + (size_t)diag_pos[row] * 9;
     const double det = m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
                        m[2] * (m[3] * m[7] - m[4] * m[6]);
     const double inv = 1.0 / det;
-    float* o = pinv + 9 * (size_t)i;
-    o[0] = (float)((m[4] * m[8] - m[5] * m[7]) * inv);
-    o[1] = (float)((m[2] * m[7] - m[1] * m[8]) * inv);
-    o[2] = (float)((m[1] * m[5] - m[2] * m[4]) * inv);
-    o[3] = (float)((m[5] * m[6] - m[3] * m[8]) * inv);
-    o[4] = (float)((m[0] * m[8] - m[2] * m[6]) * inv);
-    o[5] = (float)((m[2] * m[3] - m[0] * m[5]) * inv);
-    o[6] = (float)((m[3] * m[7] - m[4] * m[6]) * inv);
-    o[7] = (float)((m[1] * m[6] - m[0] * m[7]) * inv);
-    o[8] = (float)((m[0] * m[4] - m[1] * m[3]) * inv);
+    o[0] = (m[4] * m[8] - m[5] * m[7]) * inv;
+    o[1] = (m[2] * m[7] - m[1] * m[8]) * inv;
+    o[2] = (m[1] * m[5] - m[2] * m[4]) * inv;
+    o[3] = (m[5] * m[6] - m[3] * m[8]) * inv;
+    o[4] = (m[0] * m[8] - m[2] * m[6]) * inv;
+    o[5] = (m[2] * m[3] - m[0] * m[5]) * inv;
+    o[6] = (m[3] * m[7] - m[4] * m[6]) * inv;
+    o[7] = (m[1] * m[6] - m[0] * m[7]) * inv;
+    o[8] = (m[0] * m[4] - m[1] * m[3]) * inv;
   }
+  for (int r = 0; r < 3; r++)
+    for (int j = 0; j < 3; j++) pinv[(size_t)90 * sl + 30 * j + 3 * t + r] = (float)o[3 * r + j];
 }
 
 // r64 = b - A64 x64 (FP64) and partials of r.r, b.b
@@ -769,124 +781,386 @@ __global__ void refine_norm_finish(const double* __restrict__ part, int g, Solve
   if (threadIdx.x == 0) { sc->tr_num = t0; sc->tr_den = t1; }
 }
 
-// x64 += d32
-__global__ void refine_update_kernel(int n, const float* __restrict__ d, double* __restrict__ x) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) x[i] += (double)d[i];
+// x64[perm] += scale * d (slice order back to block rows)
+__global__ void sliced_update_kernel(int nrs, const int* __restrict__ perm, const float* __restrict__ d, double scale,
+                                     double* __restrict__ x) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= 3 * nrs) return;
+  const int rs = tid / 3, c = tid - 3 * rs;
+  const int row = perm[rs];
+  if (row < 0) return;
+  const int sl = rs / kSliceRows, t = rs - sl * kSliceRows;
+  x[3 * (size_t)row + c] += scale * (double)d[(size_t)30 * sl + 3 * t + c];
 }
 
-// Inner FP32 PCG, one cooperative launch: solves A32 d = r64 from d = 0 until
-// ||r_inner|| <= inner_tol ||r64|| or max_iter (vectors stream from memory).
-__global__ void __launch_bounds__(kPThreads, 1) pcg32_inner_kernel(
-    int nb, const int* __restrict__ rp, const int* __restrict__ col, const float* __restrict__ A,
-    const double* __restrict__ rhs, float* __restrict__ d, float* __restrict__ r, float* __restrict__ z,
-    float* __restrict__ p, float* __restrict__ q, int pkind, const float* __restrict__ pinv,
-    double* __restrict__ part, double inner_tol, int max_iter, SolveScalars* sc, GridBarrier* gb) {
+// ---- bulk-copy ring of the inner FP32 PCG
+// Every CTA owns a contiguous range of slices; consumer warp w of the CTA
+// takes slices first + w, first + w + kRingWarps, ...  Producer lane w (of the
+// CTA's last warp) streams warp w's slices, cut into pieces of at most
+// kRingSteps steps, from global memory into a private two-stage ring in
+// shared memory with cp.async.bulk (evict-first in L2, so the vectors stay
+// resident), signalling a "full" mbarrier per stage; the consumer warp
+// releases a stage through its "empty" mbarrier.  The matrix does not change
+// during a solve, so the producer keeps cycling through the same pieces: the
+// next iteration's stream overlaps the vector phases and grid barriers.
+constexpr int kRingWarps = 12;                       // consumer warps per CTA
+constexpr int kRingThreads = 32 * (kRingWarps + 1);  // + the producer warp
+constexpr int kRingConsumers = 32 * kRingWarps;
+constexpr int kRingSteps = 20;                       // steps per piece (even)
+constexpr int kRingStageBytes = kRingSteps * 400;    // 90 floats + 10 ints per step
+constexpr int kRingSmem = kRingWarps * 2 * kRingStageBytes + kRingWarps * 2 * 2 * 8;
+constexpr unsigned long long kMbarSpinLimit = 1ull << 24;
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait; false after kMbarSpinLimit polls
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  for (unsigned long long i = 0; i < kMbarSpinLimit; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar,
+                                         unsigned long long policy) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(policy)
+      : "memory");
+}
+template <int NT>
+__device__ __forceinline__ void named_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory");
+}
+
+// grid_sums / grid_barrier over the first NT threads of every CTA (the
+// consumer warps), with a named CTA barrier; same order of summation as
+// grid_sums, so every CTA obtains bitwise the same sums
+template <int NV, int NT>
+__device__ __forceinline__ bool grid_sums_named(double (&v)[NV], double* __restrict__ part, GridBarrier* gb) {
+  __shared__ double ws[NV][32];
+  __shared__ double res[NV];
+  __shared__ int ok_s;
+  constexpr int nw = NT / 32;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int G = gridDim.x;
+#pragma unroll
+  for (int j = 0; j < NV; j++) {
+    double t = warp_sum(v[j]);
+    if (lane == 0) ws[j][w] = t;
+  }
+  named_sync<NT>();
+  if (w == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+      double t = warp_sum(lane < nw ? ws[j][lane] : 0.0);
+      if (lane == 0) part[(size_t)j * G + blockIdx.x] = t;
+    }
+    int ok = 1;
+    if (lane == 0) ok = barrier_arrive_wait(gb);
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+      double acc = 0.0;
+      for (int c = lane; c < G; c += 32) acc += __ldcg(part + (size_t)j * G + c);
+      acc = warp_sum(acc);
+      if (lane == 0) res[j] = acc;
+    }
+    if (lane == 0) ok_s = ok;
+  }
+  named_sync<NT>();
+#pragma unroll
+  for (int j = 0; j < NV; j++) v[j] = res[j];
+  return ok_s != 0;
+}
+
+template <int NT>
+__device__ __forceinline__ bool grid_barrier_named(GridBarrier* gb) {
+  __shared__ int okb_s;
+  named_sync<NT>();
+  if (threadIdx.x == 0) okb_s = barrier_arrive_wait(gb);
+  named_sync<NT>();
+  return okb_s != 0;
+}
+
+// Inner FP32 PCG on the sliced matrix, one cooperative launch of
+// kRingThreads per CTA: solves A32 d = rhs_scale * rhs from d = 0 until
+// ||r_inner|| <= inner_tol ||r_0|| or max_iter.  Lane l < 30 of a consumer
+// warp owns slice element 30*slice + l, i.e. component l%3 of slice row l/3
+// (lanes 30, 31 shadow lane 29 and store nothing).  Dot products accumulate
+// in compensated FP32 per lane and are summed in FP64 across the grid.
+__global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
+    const int* __restrict__ cta_first, const int* __restrict__ perm, const int* __restrict__ off,
+    const int* __restrict__ col, const float* __restrict__ val, const double* __restrict__ rhs, double rhs_scale,
+    float* __restrict__ d, float* __restrict__ r, float* __restrict__ z, float4* __restrict__ p4,
+    float* __restrict__ q, int pkind, const float* __restrict__ pinv, double* __restrict__ part, double inner_tol,
+    int max_iter, SolveScalars* sc, GridBarrier* gb) {
+  extern __shared__ __align__(128) unsigned char ring_smem[];
+  unsigned long long* full = reinterpret_cast<unsigned long long*>(ring_smem + kRingWarps * 2 * kRingStageBytes);
+  unsigned long long* empty = full + 2 * kRingWarps;
+  __shared__ volatile int stop_s;
+  const int G = gridDim.x;
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const int sfirst = cta_first[blockIdx.x], send = cta_first[blockIdx.x + 1];
+  if (threadIdx.x == 0) stop_s = 0;
+  if (threadIdx.x < 2 * kRingWarps) {
+    mbar_init(full + threadIdx.x, 1);
+    mbar_init(empty + threadIdx.x, 1);
+  }
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+
+  if (w == kRingWarps) {
+    // ---------------- producer: lane pw feeds consumer warp pw
+    const int pw = lane;
+    if (pw >= kRingWarps) return;
+    unsigned long long policy;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(policy));
+    unsigned pc = 0;            // pieces issued
+    bool ok = true;
+    if (sfirst + pw < send) {
+      while (ok) {
+        for (int sl = sfirst + pw; sl < send && ok; sl += kRingWarps) {
+          const int k1 = off[sl + 1];
+          for (int k = off[sl]; k < k1; k += kRingSteps) {
+            const int n = min(kRingSteps, k1 - k);
+            const int j = pc & 1;
+            const unsigned par = ((pc >> 1) & 1) ^ 1;
+            bool got = false;
+            for (unsigned long long i = 0; i < kMbarSpinLimit; i++) {
+              if (mbar_try_wait(empty + 2 * pw + j, par)) { got = true; break; }
+              if (stop_s) break;
+            }
+            if (!got) { ok = false; break; }
+            unsigned char* st = ring_smem + (size_t)(2 * pw + j) * kRingStageBytes;
+            mbar_expect_tx(full + 2 * pw + j, (unsigned)n * 400u);
+            bulk_g2s(st, val + (size_t)k * 90, (unsigned)n * 360u, full + 2 * pw + j, policy);
+            bulk_g2s(st + kRingSteps * 360, col + (size_t)k * kSliceRows, (unsigned)n * 40u, full + 2 * pw + j,
+                     policy);
+            pc++;
+          }
+        }
+      }
+      // drain: the last arming of each stage must complete before the CTA exits
+      for (unsigned t = 0; t < 2 && t < pc; t++) {
+        const unsigned last = pc - 1 - t;
+        mbar_wait(full + 2 * pw + (last & 1), (last >> 1) & 1);
+      }
+    }
+    return;
+  }
+
+  // ---------------- consumers
   double* part_1 = part;
   double* part_2 = part + G;
-  const int lane = threadIdx.x & 31;
-  const int wpc = kPThreads / 32;
-  const int w = threadIdx.x >> 5;
-  const int ngroups = (nb + kRowsPerWarp - 1) / kRowsPerWarp;
-  const int gstride = G * wpc;
-  const int g0 = w * G + blockIdx.x;
-  const int rsub = lane % 3;
-  const int lbase = lane - rsub;
+  const bool act = lane < 30;
+  const int ln = act ? lane : 29;
+  const int t = ln / 3, rsub = ln - 3 * t, lbase = 3 * t;
+  float* pf = reinterpret_cast<float*>(p4);
+  unsigned pc = 0;  // pieces consumed
 
-  auto apply_precond = [&](int row, bool valid, float rl) {
-    float r0 = __shfl_sync(0xffffffffu, rl, lbase < 32 ? lbase : 0);
-    float r1 = __shfl_sync(0xffffffffu, rl, lbase + 1 < 32 ? lbase + 1 : 0);
-    float r2 = __shfl_sync(0xffffffffu, rl, lbase + 2 < 32 ? lbase + 2 : 0);
-    if (!valid) return 0.f;
-    if (pkind == OD_PRECOND_JACOBI) return pinv[3 * row + rsub] * rl;
+  auto precond = [&](int sl, float rl) -> float {
+    const float r0 = __shfl_sync(0xffffffffu, rl, lbase);
+    const float r1 = __shfl_sync(0xffffffffu, rl, lbase + 1);
+    const float r2 = __shfl_sync(0xffffffffu, rl, lbase + 2);
+    if (pkind == OD_PRECOND_JACOBI) return pinv[(size_t)30 * sl + ln] * rl;
     if (pkind == OD_PRECOND_BLOCK_JACOBI) {
-      const float* m = pinv + 9 * (size_t)row + 3 * rsub;
-      return fmaf(m[0], r0, fmaf(m[1], r1, m[2] * r2));
+      const float* m = pinv + (size_t)90 * sl + ln;
+      return fmaf(m[0], r0, fmaf(m[30], r1, m[60] * r2));
     }
     return rl;
   };
 
+  int it = 0;
+  double rr = 0.0;
+  int status = OD_OK;
+  bool alive = true;
   // init: d = 0, r = rhs, z = M^-1 r, p = z
   Comp crz{0.f, 0.f}, crr{0.f, 0.f};
-  for (int g = g0; g < ngroups; g += gstride) {
-    const int row = g * kRowsPerWarp + lane / 3;
-    const bool valid = lane < 30 && row < nb;
-    const int i = 3 * row + rsub;
-    float rl = 0.f;
-    if (valid) {
-      rl = (float)rhs[i];
+  for (int sl = sfirst + w; sl < send; sl += kRingWarps) {
+    const int rs = sl * kSliceRows + t;
+    const int row = perm[rs];
+    const float rl = row >= 0 ? (float)(rhs[3 * (size_t)row + rsub] * rhs_scale) : 0.f;
+    const float zl = precond(sl, rl);
+    if (act) {
+      const size_t i = (size_t)30 * sl + lane;
       r[i] = rl;
       d[i] = 0.f;
-    }
-    const float zl = apply_precond(row, valid, rl);
-    if (valid) {
       z[i] = zl;
-      p[i] = zl;
+      pf[4 * (size_t)rs + rsub] = zl;
       comp_add_prod(crz, rl, zl);
       comp_add_prod(crr, rl, rl);
     }
   }
-  double rz, rr;
+  double rz;
   {
     double v2[2] = {comp_value(crz), comp_value(crr)};
-    if (!grid_sums<2>(v2, part_2, gb)) return;
+    alive = grid_sums_named<2, kRingConsumers>(v2, part_2, gb);
     rz = v2[0];
     rr = v2[1];
   }
   const double eps = rr * inner_tol * inner_tol;
-  int it = 0;
-  int status = isfinite(rr) ? OD_OK : OD_ERR_NAN;
-  while (status == OD_OK && it < max_iter && rr > eps) {
+  if (!isfinite(rr)) status = OD_ERR_NAN;
+  while (alive && status == OD_OK && it < max_iter && rr > eps) {
+    // q = A p (pieces from the ring), p.q
     Comp cpq{0.f, 0.f};
-    for (int g = g0; g < ngroups; g += gstride) {
-      const int row = g * kRowsPerWarp + lane / 3;
-      if (lane < 30 && row < nb) {
-        const int i = 3 * row + rsub;
-        const float y = bsr_subrow32(row, rsub, rp, col, A, p);
-        q[i] = y;
-        comp_add_prod(cpq, p[i], y);
+    for (int sl = sfirst + w; sl < send && alive; sl += kRingWarps) {
+      const int k1 = off[sl + 1];
+      float y0 = 0.f, y1 = 0.f, y2 = 0.f;  // partial rows 0, 1, 2 of block row t
+      for (int k = off[sl]; k < k1; k += kRingSteps) {
+        const int n = min(kRingSteps, k1 - k);
+        const int j = pc & 1;
+        if (!__all_sync(0xffffffffu, mbar_wait(full + 2 * w + j, (pc >> 1) & 1))) {
+          atomicExch(&gb->timeout, 1);
+          alive = false;
+          break;
+        }
+        const unsigned char* stg = ring_smem + (size_t)(2 * w + j) * kRingStageBytes;
+        const float* sv = reinterpret_cast<const float*>(stg);
+        const int* scol = reinterpret_cast<const int*>(stg + kRingSteps * 360);
+        // lane (t, rsub) takes steps rsub, rsub + 3, ... of the piece for all
+        // three rows of block row t: every gather is issued before any use
+        constexpr int kPer = (kRingSteps + 2) / 3;
+        float4 x[kPer];
+#pragma unroll
+        for (int u = 0; u < kPer; u++) {
+          const int st = rsub + 3 * u;
+          x[u] = st < n ? p4[scol[st * kSliceRows + t]] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < kPer; u++) {
+          const int st = rsub + 3 * u;
+          if (st < n) {
+            const float* a = sv + st * 90 + lbase;  // a[30 j + r] = A[r][j]
+            y0 = fmaf(a[0], x[u].x, y0);
+            y0 = fmaf(a[30], x[u].y, y0);
+            y0 = fmaf(a[60], x[u].z, y0);
+            y1 = fmaf(a[1], x[u].x, y1);
+            y1 = fmaf(a[31], x[u].y, y1);
+            y1 = fmaf(a[61], x[u].z, y1);
+            y2 = fmaf(a[2], x[u].x, y2);
+            y2 = fmaf(a[32], x[u].y, y2);
+            y2 = fmaf(a[62], x[u].z, y2);
+          }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(empty + 2 * w + j);
+        pc++;
+      }
+      // row rsub of block row t: own partial + the two neighbours' (fixed order)
+      const int l1 = lbase + (rsub == 2 ? 0 : rsub + 1), l2 = lbase + (rsub == 0 ? 2 : rsub - 1);
+      const float a0 = __shfl_sync(0xffffffffu, y0, l1), b0 = __shfl_sync(0xffffffffu, y0, l2);
+      const float a1 = __shfl_sync(0xffffffffu, y1, l1), b1 = __shfl_sync(0xffffffffu, y1, l2);
+      const float a2 = __shfl_sync(0xffffffffu, y2, l1), b2 = __shfl_sync(0xffffffffu, y2, l2);
+      const float own = rsub == 0 ? y0 : (rsub == 1 ? y1 : y2);
+      const float na = rsub == 0 ? a0 : (rsub == 1 ? a1 : a2);
+      const float nb = rsub == 0 ? b0 : (rsub == 1 ? b1 : b2);
+      const float y = (own + na) + nb;
+      if (act) {
+        q[(size_t)30 * sl + lane] = y;
+        comp_add_prod(cpq, pf[4 * (size_t)(sl * kSliceRows + t) + rsub], y);
       }
     }
     double v1[1] = {comp_value(cpq)};
-    if (!grid_sums<1>(v1, part_1, gb)) return;
+    if (!grid_sums_named<1, kRingConsumers>(v1, part_1, gb)) alive = false;
+    if (!alive) break;
     const float alpha = (float)(rz / v1[0]);
+    // d += alpha p, r -= alpha q, z = M^-1 r, r.z, r.r: kUB slices per
+    // batch, all loads of a batch issued before any use
+    constexpr int kUB = 4;
     Comp cz{0.f, 0.f}, cr{0.f, 0.f};
-    for (int g = g0; g < ngroups; g += gstride) {
-      const int row = g * kRowsPerWarp + lane / 3;
-      const bool valid = lane < 30 && row < nb;
-      const int i = 3 * row + rsub;
-      float rl = 0.f;
-      if (valid) {
-        d[i] = fmaf(alpha, p[i], d[i]);
-        rl = fmaf(-alpha, q[i], r[i]);
-        r[i] = rl;
+    for (int sl0 = sfirst + w; sl0 < send; sl0 += kUB * kRingWarps) {
+      float dv[kUB], pv[kUB], qv[kUB], rv[kUB], m0[kUB], m1[kUB], m2[kUB];
+#pragma unroll
+      for (int u = 0; u < kUB; u++) {
+        const int sl = sl0 + u * kRingWarps;
+        if (sl < send) {
+          const size_t i = (size_t)30 * sl + ln;
+          dv[u] = d[i];
+          pv[u] = pf[4 * (size_t)(sl * kSliceRows + t) + rsub];
+          qv[u] = q[i];
+          rv[u] = r[i];
+          if (pkind == OD_PRECOND_BLOCK_JACOBI) {
+            const float* m = pinv + (size_t)90 * sl + ln;
+            m0[u] = m[0];
+            m1[u] = m[30];
+            m2[u] = m[60];
+          } else if (pkind == OD_PRECOND_JACOBI) {
+            m0[u] = pinv[(size_t)30 * sl + ln];
+          }
+        }
       }
-      const float zl = apply_precond(row, valid, rl);
-      if (valid) {
-        z[i] = zl;
-        comp_add_prod(cz, rl, zl);
-        comp_add_prod(cr, rl, rl);
+#pragma unroll
+      for (int u = 0; u < kUB; u++) {
+        const int sl = sl0 + u * kRingWarps;
+        if (sl < send) {  // warp-uniform
+          const size_t i = (size_t)30 * sl + ln;
+          const float rl = act ? fmaf(-alpha, qv[u], rv[u]) : 0.f;
+          const float r0 = __shfl_sync(0xffffffffu, rl, lbase);
+          const float r1 = __shfl_sync(0xffffffffu, rl, lbase + 1);
+          const float r2 = __shfl_sync(0xffffffffu, rl, lbase + 2);
+          float zl = rl;
+          if (pkind == OD_PRECOND_BLOCK_JACOBI) zl = fmaf(m0[u], r0, fmaf(m1[u], r1, m2[u] * r2));
+          else if (pkind == OD_PRECOND_JACOBI) zl = m0[u] * rl;
+          if (act) {
+            d[i] = fmaf(alpha, pv[u], dv[u]);
+            r[i] = rl;
+            z[i] = zl;
+            comp_add_prod(cz, rl, zl);
+            comp_add_prod(cr, rl, rl);
+          }
+        }
       }
     }
     double v2[2] = {comp_value(cz), comp_value(cr)};
-    if (!grid_sums<2>(v2, part_2, gb)) return;
+    if (!grid_sums_named<2, kRingConsumers>(v2, part_2, gb)) { alive = false; break; }
     const double beta = v2[0] / rz;
     rz = v2[0];
     rr = v2[1];
     it++;
     if (!isfinite(rr) || !isfinite(beta)) status = OD_ERR_NAN;
     const float bf = (float)beta;
-    for (int g = g0; g < ngroups; g += gstride) {
-      const int row = g * kRowsPerWarp + lane / 3;
-      if (lane < 30 && row < nb) {
-        const int i = 3 * row + rsub;
-        p[i] = fmaf(bf, p[i], z[i]);
+    // p = z + beta p, kUD slices per batch
+    constexpr int kUD = 8;
+    for (int sl0 = sfirst + w; sl0 < send; sl0 += kUD * kRingWarps) {
+      float zv[kUD], pv[kUD];
+#pragma unroll
+      for (int u = 0; u < kUD; u++) {
+        const int sl = sl0 + u * kRingWarps;
+        if (sl < send) {
+          zv[u] = z[(size_t)30 * sl + ln];
+          pv[u] = pf[4 * (size_t)(sl * kSliceRows + t) + rsub];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kUD; u++) {
+        const int sl = sl0 + u * kRingWarps;
+        if (sl < send && act) pf[4 * (size_t)(sl * kSliceRows + t) + rsub] = fmaf(bf, pv[u], zv[u]);
       }
     }
-    if (!grid_barrier(gb)) return;
+    if (!grid_barrier_named<kRingConsumers>(gb)) { alive = false; break; }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  named_sync<kRingConsumers>();
+  if (threadIdx.x == 0) stop_s = 1;
+  if (alive && blockIdx.x == 0 && threadIdx.x == 0) {
     sc->iter = it;
     sc->rr = rr;
     sc->status = status;
@@ -977,12 +1251,6 @@ od_status launch_expand(Scene* s, const double* v1, double c1, const double* v2,
       total, s->bsr.desc_kind, s->bsr.desc_off, s->bsr.gen, v1, c1, v2, c2, v3, c3, s->A64);
   OD_CUDA(cudaGetLastError());
   return OD_OK;
-}
-
-// FP32 copy of A64 for the inner mixed-precision solve
-__global__ void to_fp32_kernel(long long n, const double* __restrict__ a, float* __restrict__ b) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] = (float)a[i];
 }
 
 od_status launch_spmv_lower(Scene* s, const double* v1, double c1, const double* x1, const double* v2, double c2,
@@ -1184,6 +1452,8 @@ void pcg_free(Scene* s) {
   cudaFree(P.gbar);
   cudaFree(P.v32);
   cudaFree(P.r64);
+  cudaFree(P.sl_val);
+  for (int* v : {P.sl_perm, P.sl_off, P.sl_col, P.sl_src, P.sl_cta}) cudaFree(v);
   if (P.sc_host) cudaFreeHost(P.sc_host);
   if (P.timeout_host) cudaFreeHost(P.timeout_host);
   P = Pcg();
@@ -1230,38 +1500,100 @@ static od_status pcg_finish(Scene* s, const double* d_b, double* d_x, double shi
   return status == OD_ERR_DEVICE_TIMEOUT ? OD_ERR_DEVICE_TIMEOUT : OD_OK;
 }
 
+// Slice structure and FP32 storage of the mixed-precision inner solve,
+// built on first use (the pattern never changes for a scene).
+static od_status sliced_alloc(Scene* s) {
+  Pcg& P = s->pcg;
+  if (P.sl_val) return OD_OK;
+  HostSliced hs;
+  build_sliced(s->hbsr_rp, s->hbsr_col, s->bsr.nb, hs);
+  P.sl_ns = hs.ns;
+  P.sl_steps = hs.off[hs.ns];
+  P.sl_off_host = hs.off;
+  auto up = [&](int** dst, const std::vector<int>& v) -> od_status {
+    OD_CUDA(cudaMalloc(dst, sizeof(int) * std::max<size_t>(1, v.size())));
+    OD_CUDA(cudaMemcpy(*dst, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice));
+    s->device_bytes += (long long)sizeof(int) * v.size();
+    return OD_OK;
+  };
+  OD_TRY(up(&P.sl_perm, hs.perm));
+  OD_TRY(up(&P.sl_off, hs.off));
+  OD_TRY(up(&P.sl_col, hs.col));
+  OD_TRY(up(&P.sl_src, hs.src));
+  const size_t ns = (size_t)hs.ns;
+  const size_t nval = (size_t)std::max<long long>(1, P.sl_steps) * 90;
+  const size_t nvec = 40 * ns + 4 * 30 * ns + 90 * ns;
+  OD_CUDA(cudaMalloc(&P.sl_val, sizeof(float) * nval));
+  OD_CUDA(cudaMalloc(&P.v32, sizeof(float) * nvec));
+  OD_CUDA(cudaMemset(P.v32, 0, sizeof(float) * nvec));
+  OD_CUDA(cudaMalloc(&P.r64, sizeof(double) * (size_t)P.n_pad));
+  s->device_bytes += (long long)(sizeof(float) * (nval + nvec) + sizeof(double) * (size_t)P.n_pad);
+  return OD_OK;
+}
+
+// co-resident CTAs of the ring kernel (one per SM), 0 if it cannot launch
+static int ring_kernel_ctas(const Ctx* ctx) {
+  if (cudaFuncSetAttribute(pcg32_ring_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kRingSmem) != cudaSuccess)
+    return 0;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg32_ring_kernel, kRingThreads, kRingSmem) !=
+      cudaSuccess)
+    return 0;
+  return std::min(per_sm, 1) * ctx->num_sms;
+}
+
+// contiguous slice ranges per CTA with about equal step counts
+static od_status ring_partition(Scene* s, int G) {
+  Pcg& P = s->pcg;
+  if (P.sl_cta && P.sl_cta_grid == G) return OD_OK;
+  const std::vector<int>& off = P.sl_off_host;
+  const int ns = P.sl_ns;
+  std::vector<int> first(G + 1, ns);
+  first[0] = 0;
+  int sl = 0;
+  for (int b = 1; b < G; b++) {
+    const long long target = (long long)off[ns] * b / G;
+    while (sl < ns && off[sl] < target) sl++;
+    first[b] = sl;
+  }
+  if (P.sl_cta) cudaFree(P.sl_cta);
+  P.sl_cta = nullptr;
+  OD_CUDA(cudaMalloc(&P.sl_cta, sizeof(int) * (G + 1)));
+  OD_CUDA(cudaMemcpy(P.sl_cta, first.data(), sizeof(int) * (G + 1), cudaMemcpyHostToDevice));
+  P.sl_cta_grid = G;
+  return OD_OK;
+}
+
 // Mixed-precision solve: FP64 iterative refinement around the FP32 inner
 // PCG.  Every outer sweep recomputes the true residual b - A x in FP64 (the
-// residual replacement), solves A32 d = r to inner_tol relative with the FP32
-// PCG, and adds d to x in FP64; it stops when ||b - A x|| <= tol ||b||.
+// residual replacement), solves A32 d = r / ||r|| to inner_tol relative with
+// the FP32 sliced PCG, and adds ||r|| d to x in FP64; it stops when
+// ||b - A x|| <= tol ||b||.
 static od_status pcg_solve_mixed(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm,
                                  od_solve_stats* st) {
   Pcg& P = s->pcg;
   cudaStream_t strm = s->ctx->stream;
-  const int nb = s->bsr.nb, n = P.n_pad;
+  const int nb = s->bsr.nb;
   const int pk = prm->precond;
   if (pk == OD_PRECOND_IC0) { set_error("mixed precision supports the none, Jacobi and block-Jacobi preconditioners"); return OD_ERR_UNSUPPORTED; }
-  if (P.coop_grid <= 0) { set_error("mixed precision needs cooperative launch"); return OD_ERR_UNSUPPORTED; }
-  // lazily allocated FP32 storage
-  if (!s->A32) {
-    OD_CUDA(cudaMalloc(&s->A32, sizeof(float) * 9 * (size_t)s->bsr.nnzb));
-    OD_CUDA(cudaMalloc(&P.v32, sizeof(float) * (5 * (size_t)n + 9 * (size_t)nb)));
-    OD_CUDA(cudaMalloc(&P.r64, sizeof(double) * (size_t)n));
-    s->device_bytes += (long long)sizeof(float) * (9 * (size_t)s->bsr.nnzb + 5 * (size_t)n + 9 * (size_t)nb) +
-                       (long long)sizeof(double) * n;
-  }
-  float* d32 = P.v32;
-  float* r32 = d32 + n;
-  float* z32 = r32 + n;
-  float* p32 = z32 + n;
-  float* q32 = p32 + n;
-  float* pinv32 = q32 + n;
-  const long long nv = 9LL * s->bsr.nnzb;
+  const int G2 = P.coop_grid > 0 ? ring_kernel_ctas(s->ctx) : 0;
+  if (G2 <= 0) { set_error("mixed precision needs cooperative launch"); return OD_ERR_UNSUPPORTED; }
+  OD_TRY(sliced_alloc(s));
+  OD_TRY(ring_partition(s, G2));
+  const int ns = P.sl_ns, nrs = ns * kSliceRows;
+  float4* p4 = reinterpret_cast<float4*>(P.v32);
+  float* d32 = P.v32 + 40 * (size_t)ns;
+  float* r32 = d32 + 30 * (size_t)ns;
+  float* z32 = r32 + 30 * (size_t)ns;
+  float* q32 = z32 + 30 * (size_t)ns;
+  float* pinv32 = q32 + 30 * (size_t)ns;
+  const long long nval = 90LL * P.sl_steps;
   OD_KL(s);
-  to_fp32_kernel<<<nblk(nv, kThreads), kThreads, 0, strm>>>(nv, s->A64, s->A32);
+  sliced_fill_kernel<<<nblk(nval, kThreads), kThreads, 0, strm>>>(nval, P.sl_src, s->A64, P.sl_val);
   if (pk != OD_PRECOND_NONE) {
     OD_KL(s);
-    precond_setup32_kernel<<<nblk(nb, kThreads), kThreads, 0, strm>>>(nb, pk, s->bsr.diag_pos, s->A64, pinv32);
+    sliced_precond_kernel<<<nblk(nrs, kThreads), kThreads, 0, strm>>>(nrs, pk, P.sl_perm, s->bsr.diag_pos, s->A64,
+                                                                      pinv32);
   }
   const double inner_tol = prm->inner_tol > 0.0 ? prm->inner_tol : 1e-4;
   const int max_refine = prm->max_refine > 0 ? prm->max_refine : 20;
@@ -1283,28 +1615,30 @@ static od_status pcg_solve_mixed(Scene* s, const double* d_b, double* d_x, const
   const double eps = bb * prm->tol * prm->tol;
   int total_it = 0, sweeps = 0;
   od_status status = std::isfinite(rr) ? OD_OK : OD_ERR_NAN;
-  const int G2 = P.coop_grid;
   const bool prof = s->ctx->profiling && s->ctx->ev_pool.size() >= 2;
   while (status == OD_OK && rr > eps && sweeps < max_refine && total_it < prm->max_iter) {
     OD_CUDA(cudaMemsetAsync(P.gbar, 0, sizeof(GridBarrier), strm));
+    const double rnorm = std::sqrt(rr);
+    double rhs_scale = rnorm > 0.0 ? 1.0 / rnorm : 1.0;
     int maxit = prm->max_iter - total_it;
     GridBarrier* gbp = (GridBarrier*)P.gbar;
-    const int* rpp = s->bsr.row_ptr;
-    const int* colp = s->bsr.col;
-    const float* Ap = s->A32;
     const double* rhs = P.r64;
     int pkv = pk;
-    double itol = inner_tol;
-    int nbv = nb;
-    void* args[] = {(void*)&nbv, (void*)&rpp, (void*)&colp, (void*)&Ap, (void*)&rhs, (void*)&d32, (void*)&r32,
-                    (void*)&z32, (void*)&p32, (void*)&q32, (void*)&pkv, (void*)&pinv32, (void*)&P.partial,
-                    (void*)&itol, (void*)&maxit, (void*)&P.sc, (void*)&gbp};
+    // a sweep reduces the residual no further than the outer target needs
+    // (with a 0.3 margin), and at least by inner_tol
+    double itol = std::max(inner_tol, std::min(0.5, 0.3 * std::sqrt(eps / rr)));
+    void* args[] = {(void*)&P.sl_cta, (void*)&P.sl_perm, (void*)&P.sl_off, (void*)&P.sl_col, (void*)&P.sl_val,
+                    (void*)&rhs, (void*)&rhs_scale, (void*)&d32, (void*)&r32, (void*)&z32, (void*)&p4,
+                    (void*)&q32, (void*)&pkv, (void*)&pinv32, (void*)&P.partial, (void*)&itol, (void*)&maxit,
+                    (void*)&P.sc, (void*)&gbp};
     if (prof) OD_CUDA(cudaEventRecord(s->ctx->ev_pool[0], strm));
     OD_KL(s);
-    OD_CUDA(cudaLaunchCooperativeKernel((void*)pcg32_inner_kernel, dim3(G2), dim3(kPThreads), args, 0, strm));
+    OD_CUDA(cudaLaunchCooperativeKernel((void*)pcg32_ring_kernel, dim3(G2), dim3(kRingThreads), args, kRingSmem,
+                                        strm));
     if (prof) OD_CUDA(cudaEventRecord(s->ctx->ev_pool[1], strm));
     OD_KL(s);
-    refine_update_kernel<<<nblk(n, kThreads), kThreads, 0, strm>>>(n, d32, d_x);
+    sliced_update_kernel<<<nblk(3 * nrs, kThreads), kThreads, 0, strm>>>(nrs, P.sl_perm, d32,
+                                                                         rnorm > 0.0 ? rnorm : 1.0, d_x);
     OD_CUDA(cudaMemcpyAsync(P.timeout_host, &((GridBarrier*)P.gbar)->timeout, sizeof(int), cudaMemcpyDeviceToHost,
                             strm));
     OD_TRY(residual());  // also brings back the inner statistics
