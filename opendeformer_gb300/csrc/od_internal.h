@@ -89,28 +89,94 @@ struct Pcg {
   int* timeout_host = nullptr;  // pinned
   int coop_grid = 0;            // co-resident CTAs, 0 if cooperative launch is unavailable
   int disable_persistent = 0;
-  // mixed precision (lazily allocated).  The FP32 matrix is stored in slices
-  // of kSliceRows block rows (rows sorted by block count, longest first,
-  // within windows of kSliceWindow rows); the k-th blocks of a slice's rows
-  // sit together, values [step][j][lane] with lane = 3*row_in_slice + r, so a
-  // warp reads each step as three contiguous 120-byte runs.  Inner vectors
-  // are in slice order: element 30*slice + lane.
-  int sl_ns = 0;                // slices
-  long long sl_steps = 0;       // sum over slices of the (even) padded length
-  std::vector<int> sl_off_host; // sl_off on the host
-  int sl_cta_grid = 0;          // grid size sl_cta was cut for
-  int* sl_cta = nullptr;        // sl_cta_grid+1: first slice of each CTA
-  int* sl_perm = nullptr;       // sl_ns*kSliceRows: slice row -> block row, -1 padding
-  int* sl_off = nullptr;        // sl_ns+1: first step of each slice
-  int* sl_col = nullptr;        // sl_steps*kSliceRows: block column as a slice row
-  int* sl_src = nullptr;        // sl_steps*kSliceRows: full-BSR block, -1 padding
-  float* sl_val = nullptr;      // sl_steps*90
-  float* v32 = nullptr;         // p (float4 per slice row), d, r, z, q (30 per slice), preconditioner (90 per slice)
-  double* r64 = nullptr;        // outer FP64 residual
+  // mixed precision: the scene's own sliced FP32 system (lazily built)
+  struct MixedSys* mix = nullptr;
 };
 
 constexpr int kSliceRows = 10;      // block rows per slice (3 lanes each, 30 of a warp's 32)
 constexpr int kSliceWindow = 320;   // rows sorted by length inside windows of this many rows
+constexpr int kMaxLocalScenes = 32; // scenes one CTA of the inner FP32 solve may span
+
+// A contiguous piece of one scene's index space (elements, DOFs, block rows,
+// values ...) handled by one CTA of a multi-scene kernel.
+struct Tile {
+  int scene, begin, end, aux;
+};
+
+// Per-scene input / output of the inner FP32 PCG of a mixed solve.
+struct RingScene {
+  double rhs_scale;   // in: 1 / ||r64|| of the scene
+  double unscale;     // in: ||r64|| (the correction is unscale * d)
+  double itol2;       // in: squared relative inner tolerance
+  int max_iter;       // in
+  int active0;        // in: the scene takes part in this sweep
+  int iters;          // out
+  int status;         // out
+  double rr;          // out: final inner r.r
+};
+
+// Device view of one scene's operator for the mixed solve: the FP64 full BSR,
+// the right-hand side and the solution it refines.
+struct MixDesc {
+  const int* row_ptr;
+  const int* col;
+  const int* diag_pos;
+  const double* A64;
+  const double* b;
+  double* x;
+  int nb;
+  int row0;           // first entry of the scene in the concatenated FP64 residual
+  int tile0, ntiles;  // residual tiles of the scene
+};
+
+// Sliced FP32 system of one or more scenes (block diagonal): each scene's
+// block rows in slices of kSliceRows (rows sorted by block count, longest
+// first, within windows of kSliceWindow rows, every slice padded to an even
+// step count); the k-th blocks of a slice's rows sit together, values
+// [step][j][lane] with lane = 3*row_in_slice + r.  Inner vectors are in slice
+// order (element 30*slice + lane); column indices are slice rows of the
+// concatenation.
+struct MixedSys {
+  int n_sc = 0;                    // scenes
+  int ns = 0;                      // slices
+  long long steps = 0;
+  int n64 = 0;                     // entries of the concatenated FP64 residual
+  std::vector<int> off_host;       // ns+1
+  std::vector<int> sc_slice;       // n_sc+1 first slice of each scene
+  std::vector<int> sc_row0;        // n_sc first residual entry of each scene
+  std::vector<int> sc_nb;          // n_sc block rows
+  int* perm = nullptr;             // ns*kSliceRows: scene-local block row or -1
+  int* slice_sc = nullptr;         // ns: scene of each slice
+  int* sc_slice_dev = nullptr;     // n_sc+1: first slice of each scene
+  int* off = nullptr;              // ns+1
+  int* col = nullptr;              // steps*kSliceRows
+  int* src = nullptr;              // steps*kSliceRows: scene-local full-BSR block or -1
+  float* val = nullptr;            // steps*90
+  float* v32 = nullptr;            // p (40/slice), d, r, z, q (30/slice), preconditioner (90/slice)
+  double* r64 = nullptr;           // n64
+  // per scene
+  MixDesc* desc = nullptr;         // n_sc (device)
+  std::vector<MixDesc> desc_host;
+  RingScene* ring = nullptr;       // n_sc (device)
+  RingScene* ring_host = nullptr;  // n_sc (pinned)
+  double* rrbb = nullptr;          // 2*n_sc: residual r.r, b.b (device)
+  double* rrbb_host = nullptr;     // pinned
+  // tiles
+  Tile* res_tiles = nullptr;       // residual tiles (block rows)
+  int n_res_tiles = 0;
+  double* res_part = nullptr;      // 2 per residual tile
+  Tile* fill_tiles = nullptr;      // value tiles of the FP32 fill
+  int n_fill_tiles = 0;
+  // CTA partition of the ring kernel
+  int cta_grid = 0;
+  int* cta_first = nullptr;        // G+1 first slice of each CTA
+  int* cta_sc_lo = nullptr;        // G first scene of each CTA
+  int* sc_cta = nullptr;           // 2*n_sc: first, last CTA of each scene
+  double* part = nullptr;          // [3][n_sc][G] per-scene CTA partials + 2 G
+  void* gbar = nullptr;
+  int* timeout_host = nullptr;     // pinned
+  long long device_bytes = 0;
+};
 
 struct Ctx {
   int device = 0;
@@ -246,5 +312,16 @@ od_status launch_spmv_lower(Scene* s, const double* v1, double c1, const double*
 od_status launch_spmv_full(Scene* s, const double* x, double* y);
 // PCG on A64; b and x are device vectors of length n_pad
 od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm, od_solve_stats* st);
+
+// ---- mixed-precision systems (od_sparse.cu)
+// builds the sliced FP32 system of scenes (their full-BSR patterns) with the
+// given right-hand sides / solutions (nullptr: supplied per solve)
+od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::vector<const double*>& b,
+                      const std::vector<double*>& x, MixedSys** out);
+void mixed_free(MixedSys* m);
+// solves every scene's A64 x = b with FP64 refinement around the FP32 inner
+// PCG (same preconditioner kind for all); per-scene parameters and results
+od_status mixed_solve(Ctx* ctx, MixedSys* m, int precond, const std::vector<od_solver_params>& prm,
+                      std::vector<od_solve_stats>& st);
 
 }  // namespace od

@@ -699,43 +699,46 @@ __device__ __forceinline__ void comp_add_prod(Comp& a, float x, float y) {
 }
 __device__ __forceinline__ double comp_value(const Comp& a) { return (double)a.s + (double)a.c; }
 
-// ---- sliced FP32 matrix (the layout is described with Pcg::sl_val)
+// ---- sliced FP32 systems of one or more scenes (layout: MixedSys)
 
-// sl_val from the FP64 full-BSR values: value v = [step][j][lane]
-__global__ void sliced_fill_kernel(long long nval, const int* __restrict__ src, const double* __restrict__ A64,
-                                   float* __restrict__ val) {
-  const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (v >= nval) return;
-  const long long step = v / 90;
-  const int rem = (int)(v - step * 90);
-  const int j = rem / 30, lane = rem - 30 * j;
-  const int blk = src[step * kSliceRows + lane / 3];
-  val[v] = blk >= 0 ? (float)A64[(size_t)blk * 9 + 3 * (lane % 3) + j] : 0.f;
+// values of the sliced matrix from each scene's FP64 full BSR; a tile is a
+// step range [begin, end) of one scene
+__global__ void mix_fill_kernel(const Tile* __restrict__ tiles, const MixDesc* __restrict__ desc,
+                                const int* __restrict__ src, float* __restrict__ val) {
+  const Tile tl = tiles[blockIdx.x];
+  const double* __restrict__ A = desc[tl.scene].A64;
+  const int nv = (tl.end - tl.begin) * 90;
+  for (int q = threadIdx.x; q < nv; q += blockDim.x) {
+    const int st = tl.begin + q / 90, rem = q % 90;
+    const int j = rem / 30, lane = rem - 30 * j;
+    const int blk = src[(size_t)st * kSliceRows + lane / 3];
+    val[(size_t)st * 90 + rem] = blk >= 0 ? (float)A[(size_t)blk * 9 + 3 * (lane % 3) + j] : 0.f;
+  }
 }
 
 // FP32 Jacobi (30 per slice) or block-Jacobi (90 per slice, [j][lane]) from
 // the FP64 diagonal blocks, in slice order; padding rows get zeros
-__global__ void sliced_precond_kernel(int nrs, int kind, const int* __restrict__ perm,
-                                      const int* __restrict__ diag_pos, const double* __restrict__ A,
-                                      float* __restrict__ pinv) {
+__global__ void mix_precond_kernel(int nrs, int kind, const int* __restrict__ perm, const int* __restrict__ slice_sc,
+                                   const MixDesc* __restrict__ desc, float* __restrict__ pinv) {
   const int rs = blockIdx.x * blockDim.x + threadIdx.x;
   if (rs >= nrs) return;
   const int sl = rs / kSliceRows, t = rs - sl * kSliceRows;
   const int row = perm[rs];
+  const double* m = nullptr;
+  if (row >= 0) {
+    const MixDesc& D = desc[slice_sc[sl]];
+    m = D.A64 + (size_t)D.diag_pos[row] * 9;
+  }
   if (kind == OD_PRECOND_JACOBI) {
     for (int d = 0; d < 3; d++) {
       float v = 0.f;
-      if (row >= 0) {
-        const double a = A[(size_t)diag_pos[row] * 9 + 4 * d];
-        v = (float)(a > 0.0 ? 1.0 / a : 1.0);
-      }
+      if (m) v = (float)(m[4 * d] > 0.0 ? 1.0 / m[4 * d] : 1.0);
       pinv[(size_t)30 * sl + 3 * t + d] = v;
     }
     return;
   }
   double o[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  if (row >= 0) {
-    const double* m = A + (size_t)diag_pos[row] * 9;
+  if (m) {
     const double det = m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
                        m[2] * (m[3] * m[7] - m[4] * m[6]);
     const double inv = 1.0 / det;
@@ -753,56 +756,81 @@ __global__ void sliced_precond_kernel(int nrs, int kind, const int* __restrict__
     for (int j = 0; j < 3; j++) pinv[(size_t)90 * sl + 30 * j + 3 * t + r] = (float)o[3 * r + j];
 }
 
-// r64 = b - A64 x64 (FP64) and partials of r.r, b.b
-__global__ void refine_residual_kernel(int nb, const int* __restrict__ rp, const int* __restrict__ col,
-                                       const double* __restrict__ A, const double* __restrict__ b,
-                                       const double* __restrict__ x, double* __restrict__ r, double* __restrict__ part) {
+// r64 = b - A64 x (FP64) for the block rows [begin, end) of a tile (three
+// lanes per block row, ten block rows per warp) and the tile's partials of
+// r.r and b.b
+constexpr int kResRows = (kThreads / 32) * kRowsPerWarp;
+__global__ void mix_residual_kernel(const Tile* __restrict__ tiles, const MixDesc* __restrict__ desc,
+                                    double* __restrict__ r64, double* __restrict__ part) {
+  const Tile tl = tiles[blockIdx.x];
+  const MixDesc& D = desc[tl.scene];
   const int lane = threadIdx.x & 31;
-  const int warp_global = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+  const int row = tl.begin + (threadIdx.x >> 5) * kRowsPerWarp + lane / 3, rs = lane % 3;
   double rr = 0.0, bb = 0.0;
-  for (int wb = warp_global * kRowsPerWarp; wb < nb; wb += gridDim.x * kWarpRows) {
-    const int row = wb + lane / 3, rs = lane % 3;
-    if (lane < 30 && row < nb) {
-      const int i = 3 * row + rs;
-      const double rv = b[i] - bsr_subrow<double, double>(row, rs, rp, col, A, x);
-      r[i] = rv;
-      rr = fma(rv, rv, rr);
-      bb = fma(b[i], b[i], bb);
-    }
+  if (lane < 30 && row < tl.end) {
+    const int i = 3 * row + rs;
+    const double bv = D.b[i];
+    const double rv = bv - bsr_subrow<double, double>(row, rs, D.row_ptr, D.col, D.A64, D.x);
+    r64[D.row0 + i] = rv;
+    rr = rv * rv;
+    bb = bv * bv;
   }
-  double t0 = block_sum(rr), t1 = block_sum(bb);
-  if (threadIdx.x == 0) { part[2 * blockIdx.x] = t0; part[2 * blockIdx.x + 1] = t1; }
+  const double t0 = block_sum(rr), t1 = block_sum(bb);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = t0;
+    part[2 * blockIdx.x + 1] = t1;
+  }
 }
 
-__global__ void refine_norm_finish(const double* __restrict__ part, int g, SolveScalars* sc) {
+// per scene: r.r and b.b over the scene's residual tiles in a fixed order
+__global__ void mix_residual_finish(int n_sc, const MixDesc* __restrict__ desc, const double* __restrict__ part,
+                                    double* __restrict__ rrbb) {
+  const int s = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (s >= n_sc) return;
+  const int t0 = desc[s].tile0, nt = desc[s].ntiles;
   double a = 0.0, b = 0.0;
-  for (int j = threadIdx.x; j < g; j += blockDim.x) { a += part[2 * j]; b += part[2 * j + 1]; }
-  double t0 = block_sum(a), t1 = block_sum(b);
-  if (threadIdx.x == 0) { sc->tr_num = t0; sc->tr_den = t1; }
+  for (int k = lane; k < nt; k += 32) {
+    a += part[2 * (t0 + k)];
+    b += part[2 * (t0 + k) + 1];
+  }
+  a = warp_sum(a);
+  b = warp_sum(b);
+  if (lane == 0) {
+    rrbb[2 * s] = a;
+    rrbb[2 * s + 1] = b;
+  }
 }
 
-// x64[perm] += scale * d (slice order back to block rows)
-__global__ void sliced_update_kernel(int nrs, const int* __restrict__ perm, const float* __restrict__ d, double scale,
-                                     double* __restrict__ x) {
+// x += ||r64|| d for the scenes of the sweep (slice order back to block rows)
+__global__ void mix_update_kernel(int nrs, const int* __restrict__ perm, const int* __restrict__ slice_sc,
+                                  const MixDesc* __restrict__ desc, const RingScene* __restrict__ ring,
+                                  const float* __restrict__ d) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= 3 * nrs) return;
   const int rs = tid / 3, c = tid - 3 * rs;
   const int row = perm[rs];
   if (row < 0) return;
   const int sl = rs / kSliceRows, t = rs - sl * kSliceRows;
-  x[3 * (size_t)row + c] += scale * (double)d[(size_t)30 * sl + 3 * t + c];
+  const int s = slice_sc[sl];
+  if (!ring[s].active0) return;
+  desc[s].x[3 * (size_t)row + c] += ring[s].unscale * (double)d[(size_t)30 * sl + 3 * t + c];
 }
 
 // ---- bulk-copy ring of the inner FP32 PCG
-// Every CTA owns a contiguous range of slices; consumer warp w of the CTA
-// takes slices first + w, first + w + kRingWarps, ...  Producer lane w (of the
-// CTA's last warp) streams warp w's slices, cut into pieces of at most
-// kRingSteps steps, from global memory into a private two-stage ring in
-// shared memory with cp.async.bulk (evict-first in L2, so the vectors stay
-// resident), signalling a "full" mbarrier per stage; the consumer warp
-// releases a stage through its "empty" mbarrier.  The matrix does not change
-// during a solve, so the producer keeps cycling through the same pieces: the
-// next iteration's stream overlaps the vector phases and grid barriers.
+// Every CTA owns a contiguous range of slices (of one or more scenes);
+// consumer warp w of the CTA takes slices first + w, first + w + kRingWarps,
+// ...  Producer lane w (of the CTA's last warp) streams warp w's slices, cut
+// into pieces of at most kRingSteps steps, from global memory into a private
+// two-stage ring in shared memory with cp.async.bulk (evict-first in L2, so
+// the vectors stay resident), signalling a "full" mbarrier per stage; the
+// consumer warp releases a stage through its "empty" mbarrier.  The matrix
+// does not change during a solve, so the producer keeps cycling through the
+// same pieces: the next iteration's stream overlaps the vector phases and
+// grid barriers.  Pieces of a scene that has converged are no longer copied
+// (the stage is signalled without data): the producer reads the per-scene
+// activity the consumers publish, and may only see it late (it then copies
+// data the consumers skip), never early.
 constexpr int kRingWarps = 12;                       // consumer warps per CTA
 constexpr int kRingThreads = 32 * (kRingWarps + 1);  // + the producer warp
 constexpr int kRingConsumers = 32 * kRingWarps;
@@ -849,45 +877,82 @@ __device__ __forceinline__ void named_sync() {
   asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory");
 }
 
-// grid_sums / grid_barrier over the first NT threads of every CTA (the
-// consumer warps), with a named CTA barrier; same order of summation as
-// grid_sums, so every CTA obtains bitwise the same sums
-template <int NV, int NT>
-__device__ __forceinline__ bool grid_sums_named(double (&v)[NV], double* __restrict__ part, GridBarrier* gb) {
-  __shared__ double ws[NV][32];
-  __shared__ double res[NV];
-  __shared__ int ok_s;
-  constexpr int nw = NT / 32;
+// Shared state of one CTA of the ring kernel for the scenes it spans.
+struct RingShared {
+  double ws[2][kMaxLocalScenes][kRingWarps];  // per-warp partials
+  double res[2][kMaxLocalScenes];             // scene sums of the last reduction
+  double wg[kRingWarps];
+  double g;                                   // grid-wide sum of the last reduction
+  double rz[kMaxLocalScenes], rr[kMaxLocalScenes], eps[kMaxLocalScenes];
+  double scale[kMaxLocalScenes];
+  int row0[kMaxLocalScenes], it[kMaxLocalScenes], status[kMaxLocalScenes], maxit[kMaxLocalScenes];
+  int c0[kMaxLocalScenes], c1[kMaxLocalScenes];  // CTA range of each local scene
+  int lfirst[kMaxLocalScenes + 1];                // first slice of each local scene in the CTA range
+  volatile unsigned char act[2][kMaxLocalScenes];  // activity by iteration parity
+  volatile int pub;                           // last iteration whose activity is published
+  volatile int stop;
+  int ok;
+};
+
+// local scene of slice sl for a warp walking its slices in increasing order
+__device__ __forceinline__ int local_scene(const RingShared& sh, int sl, int& ls) {
+  while (sl >= sh.lfirst[ls + 1]) ls++;
+  return ls;
+}
+
+// Per-scene grid sums: CTA partials per local scene (fixed warp order) ->
+// part[j][scene][cta], one grid barrier, then every CTA sums each of its
+// scenes over the scene's CTA range in a fixed order (bitwise the same in
+// every CTA; entries of CTAs without the scene stay zero); gval is summed
+// over all CTAs.  Consumers only.
+template <int NV>
+__device__ __forceinline__ bool ring_sums(RingShared& sh, int L, int sc_lo, int n_sc, double gval,
+                                          double* __restrict__ part, double* __restrict__ part_g, GridBarrier* gb) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int G = gridDim.x;
-#pragma unroll
-  for (int j = 0; j < NV; j++) {
-    double t = warp_sum(v[j]);
-    if (lane == 0) ws[j][w] = t;
-  }
-  named_sync<NT>();
+  const int G = gridDim.x, b = blockIdx.x;
+  if (lane == 0) sh.wg[w] = gval;
+  named_sync<kRingConsumers>();
   if (w == 0) {
+    if (lane < L) {
 #pragma unroll
-    for (int j = 0; j < NV; j++) {
-      double t = warp_sum(lane < nw ? ws[j][lane] : 0.0);
-      if (lane == 0) part[(size_t)j * G + blockIdx.x] = t;
+      for (int j = 0; j < NV; j++) {
+        double t = 0.0;
+        for (int k = 0; k < kRingWarps; k++) t += sh.ws[j][lane][k];
+        part[((size_t)j * n_sc + sc_lo + lane) * G + b] = t;
+      }
     }
+    if (lane == 0) {
+      double t = 0.0;
+      for (int k = 0; k < kRingWarps; k++) t += sh.wg[k];
+      part_g[b] = t;
+    }
+    __threadfence();
+    __syncwarp();
     int ok = 1;
     if (lane == 0) ok = barrier_arrive_wait(gb);
     ok = __shfl_sync(0xffffffffu, ok, 0);
+    double accg = 0.0;
+    for (int c = lane; c < G; c += 32) accg += __ldcg(part_g + c);
+    for (int ls = 0; ls < L; ls++) {
+      const int s = sc_lo + ls;
+      const int c0 = sh.c0[ls], c1 = sh.c1[ls];
 #pragma unroll
-    for (int j = 0; j < NV; j++) {
-      double acc = 0.0;
-      for (int c = lane; c < G; c += 32) acc += __ldcg(part + (size_t)j * G + c);
-      acc = warp_sum(acc);
-      if (lane == 0) res[j] = acc;
+      for (int j = 0; j < NV; j++) {
+        const double* pp = part + ((size_t)j * n_sc + s) * G;
+        double acc = 0.0;
+        for (int c = c0 + lane; c <= c1; c += 32) acc += __ldcg(pp + c);
+        acc = warp_sum(acc);
+        if (lane == 0) sh.res[j][ls] = acc;
+      }
     }
-    if (lane == 0) ok_s = ok;
+    accg = warp_sum(accg);
+    if (lane == 0) {
+      sh.g = accg;
+      sh.ok = ok;
+    }
   }
-  named_sync<NT>();
-#pragma unroll
-  for (int j = 0; j < NV; j++) v[j] = res[j];
-  return ok_s != 0;
+  named_sync<kRingConsumers>();
+  return sh.ok != 0;
 }
 
 template <int NT>
@@ -899,31 +964,51 @@ __device__ __forceinline__ bool grid_barrier_named(GridBarrier* gb) {
   return okb_s != 0;
 }
 
-// Inner FP32 PCG on the sliced matrix, one cooperative launch of
-// kRingThreads per CTA: solves A32 d = rhs_scale * rhs from d = 0 until
-// ||r_inner|| <= inner_tol ||r_0|| or max_iter.  Lane l < 30 of a consumer
-// warp owns slice element 30*slice + l, i.e. component l%3 of slice row l/3
-// (lanes 30, 31 shadow lane 29 and store nothing).  Dot products accumulate
-// in compensated FP32 per lane and are summed in FP64 across the grid.
+// Inner FP32 PCG of every scene of a sliced system, one cooperative launch
+// of kRingThreads per CTA: scene s solves A32 d = rhs_scale * r64 from d = 0
+// until ||r_inner|| <= inner_tol ||r_0|| or max_iter, each scene with its own
+// step lengths; the loop runs while any scene is active.  Lane l < 30 of a
+// consumer warp owns slice element 30*slice + l, i.e. component l%3 of slice
+// row l/3 (lanes 30, 31 shadow lane 29 and store nothing).  Dot products
+// accumulate in compensated FP32 per lane and are summed in FP64.
 __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
-    const int* __restrict__ cta_first, const int* __restrict__ perm, const int* __restrict__ off,
-    const int* __restrict__ col, const float* __restrict__ val, const double* __restrict__ rhs, double rhs_scale,
-    float* __restrict__ d, float* __restrict__ r, float* __restrict__ z, float4* __restrict__ p4,
-    float* __restrict__ q, int pkind, const float* __restrict__ pinv, double* __restrict__ part, double inner_tol,
-    int max_iter, SolveScalars* sc, GridBarrier* gb) {
+    int n_sc, const int* __restrict__ cta_first, const int* __restrict__ cta_sc_lo, const int* __restrict__ sc_cta,
+    const int* __restrict__ sc_slice, const int* __restrict__ slice_sc, const int* __restrict__ perm,
+    const int* __restrict__ off,
+    const int* __restrict__ col, const float* __restrict__ val, const double* __restrict__ r64,
+    const MixDesc* __restrict__ desc, RingScene* __restrict__ ring, float* __restrict__ d, float* __restrict__ r,
+    float* __restrict__ z, float4* __restrict__ p4, float* __restrict__ q, int pkind, const float* __restrict__ pinv,
+    double* __restrict__ part, GridBarrier* gb) {
   extern __shared__ __align__(128) unsigned char ring_smem[];
   unsigned long long* full = reinterpret_cast<unsigned long long*>(ring_smem + kRingWarps * 2 * kRingStageBytes);
   unsigned long long* empty = full + 2 * kRingWarps;
-  __shared__ volatile int stop_s;
+  __shared__ RingShared sh;
   const int G = gridDim.x;
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   const int sfirst = cta_first[blockIdx.x], send = cta_first[blockIdx.x + 1];
-  if (threadIdx.x == 0) stop_s = 0;
+  const int sc_lo = cta_sc_lo[blockIdx.x];
+  const int L = send > sfirst ? slice_sc[send - 1] - sc_lo + 1 : 0;
+  if (threadIdx.x == 0) {
+    sh.stop = 0;
+    sh.pub = -1;
+  }
   if (threadIdx.x < 2 * kRingWarps) {
     mbar_init(full + threadIdx.x, 1);
     mbar_init(empty + threadIdx.x, 1);
   }
+  if (threadIdx.x < L) {
+    const int s = sc_lo + threadIdx.x;
+    sh.scale[threadIdx.x] = ring[s].rhs_scale;
+    sh.eps[threadIdx.x] = ring[s].itol2;  // relative until the first reduction
+    sh.maxit[threadIdx.x] = ring[s].max_iter;
+    sh.act[0][threadIdx.x] = (unsigned char)(ring[s].active0 != 0);
+    sh.row0[threadIdx.x] = desc[s].row0;
+    sh.c0[threadIdx.x] = sc_cta[2 * s];
+    sh.c1[threadIdx.x] = sc_cta[2 * s + 1];
+    sh.lfirst[threadIdx.x] = threadIdx.x == 0 ? sfirst : sc_slice[s];
+  }
+  if (threadIdx.x == 0) sh.lfirst[L] = send;
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   __syncthreads();
@@ -931,240 +1016,317 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
   if (w == kRingWarps) {
     // ---------------- producer: lane pw feeds consumer warp pw
     const int pw = lane;
-    if (pw >= kRingWarps) return;
+    if (pw >= kRingWarps || sfirst + pw >= send) return;
     unsigned long long policy;
     asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(policy));
-    unsigned pc = 0;            // pieces issued
+    unsigned pc = 0;  // pieces issued
+    int kit = 0;      // iteration the pieces belong to
     bool ok = true;
-    if (sfirst + pw < send) {
-      while (ok) {
-        for (int sl = sfirst + pw; sl < send && ok; sl += kRingWarps) {
-          const int k1 = off[sl + 1];
-          for (int k = off[sl]; k < k1; k += kRingSteps) {
-            const int n = min(kRingSteps, k1 - k);
-            const int j = pc & 1;
-            const unsigned par = ((pc >> 1) & 1) ^ 1;
-            bool got = false;
-            for (unsigned long long i = 0; i < kMbarSpinLimit; i++) {
-              if (mbar_try_wait(empty + 2 * pw + j, par)) { got = true; break; }
-              if (stop_s) break;
-            }
-            if (!got) { ok = false; break; }
+    while (ok) {
+      int ls = 0;
+      for (int sl = sfirst + pw; sl < send && ok; sl += kRingWarps) {
+        local_scene(sh, sl, ls);
+        bool copy = true;
+        if (sh.pub >= kit) {
+          __threadfence_block();
+          copy = sh.act[kit & 1][ls] != 0;
+        }
+        const int k1 = off[sl + 1];
+        for (int k = off[sl]; k < k1; k += kRingSteps) {
+          const int n = min(kRingSteps, k1 - k);
+          const int j = pc & 1;
+          const unsigned par = ((pc >> 1) & 1) ^ 1;
+          bool got = false;
+          for (unsigned long long i = 0; i < kMbarSpinLimit; i++) {
+            if (mbar_try_wait(empty + 2 * pw + j, par)) { got = true; break; }
+            if (sh.stop) break;
+          }
+          if (!got) { ok = false; break; }
+          if (copy) {
             unsigned char* st = ring_smem + (size_t)(2 * pw + j) * kRingStageBytes;
             mbar_expect_tx(full + 2 * pw + j, (unsigned)n * 400u);
             bulk_g2s(st, val + (size_t)k * 90, (unsigned)n * 360u, full + 2 * pw + j, policy);
             bulk_g2s(st + kRingSteps * 360, col + (size_t)k * kSliceRows, (unsigned)n * 40u, full + 2 * pw + j,
                      policy);
-            pc++;
+          } else {
+            mbar_arrive(full + 2 * pw + j);
           }
+          pc++;
         }
       }
-      // drain: the last arming of each stage must complete before the CTA exits
-      for (unsigned t = 0; t < 2 && t < pc; t++) {
-        const unsigned last = pc - 1 - t;
-        mbar_wait(full + 2 * pw + (last & 1), (last >> 1) & 1);
-      }
+      kit++;
+    }
+    // drain: the last arming of each stage must complete before the CTA exits
+    for (unsigned u = 0; u < 2 && u < pc; u++) {
+      const unsigned last = pc - 1 - u;
+      mbar_wait(full + 2 * pw + (last & 1), (last >> 1) & 1);
     }
     return;
   }
 
   // ---------------- consumers
-  double* part_1 = part;
-  double* part_2 = part + G;
-  const bool act = lane < 30;
-  const int ln = act ? lane : 29;
+  double* part_1 = part;                                    // [1][n_sc][G]
+  double* part_2 = part + (size_t)n_sc * G;                 // [2][n_sc][G]
+  double* part_g1 = part + (size_t)3 * n_sc * G;
+  double* part_g2 = part_g1 + G;
+  const bool act_l = lane < 30;
+  const int ln = act_l ? lane : 29;
   const int t = ln / 3, rsub = ln - 3 * t, lbase = 3 * t;
   float* pf = reinterpret_cast<float*>(p4);
   unsigned pc = 0;  // pieces consumed
+  bool alive = true;
 
-  auto precond = [&](int sl, float rl) -> float {
-    const float r0 = __shfl_sync(0xffffffffu, rl, lbase);
-    const float r1 = __shfl_sync(0xffffffffu, rl, lbase + 1);
-    const float r2 = __shfl_sync(0xffffffffu, rl, lbase + 2);
-    if (pkind == OD_PRECOND_JACOBI) return pinv[(size_t)30 * sl + ln] * rl;
-    if (pkind == OD_PRECOND_BLOCK_JACOBI) {
-      const float* m = pinv + (size_t)90 * sl + ln;
-      return fmaf(m[0], r0, fmaf(m[30], r1, m[60] * r2));
-    }
-    return rl;
+  // a warp's slices of local scene ls: first_slice(ls), + kRingWarps, ... < lfirst[ls + 1]
+  auto first_slice = [&](int ls) {
+    const int dlt = sh.lfirst[ls] - sfirst - w;
+    return dlt <= 0 ? sfirst + w : sfirst + w + ((dlt + kRingWarps - 1) / kRingWarps) * kRingWarps;
+  };
+  auto zero_ws = [&](int nv) {
+    if (lane < L)
+      for (int j = 0; j < nv; j++) sh.ws[j][lane][w] = 0.0;
+    __syncwarp();
+  };
+  auto flush = [&](int j, int ls, const Comp& c) {
+    const double tv = warp_sum(comp_value(c));
+    if (lane == 0) sh.ws[j][ls][w] = tv;
   };
 
-  int it = 0;
-  double rr = 0.0;
-  int status = OD_OK;
-  bool alive = true;
-  // init: d = 0, r = rhs, z = M^-1 r, p = z
-  Comp crz{0.f, 0.f}, crr{0.f, 0.f};
-  for (int sl = sfirst + w; sl < send; sl += kRingWarps) {
-    const int rs = sl * kSliceRows + t;
-    const int row = perm[rs];
-    const float rl = row >= 0 ? (float)(rhs[3 * (size_t)row + rsub] * rhs_scale) : 0.f;
-    const float zl = precond(sl, rl);
-    if (act) {
-      const size_t i = (size_t)30 * sl + lane;
-      r[i] = rl;
-      d[i] = 0.f;
-      z[i] = zl;
-      pf[4 * (size_t)rs + rsub] = zl;
-      comp_add_prod(crz, rl, zl);
-      comp_add_prod(crr, rl, rl);
+  // init: d = 0, r = rhs, z = M^-1 r, p = z (scenes outside the sweep: zeros)
+  zero_ws(2);
+  for (int ls = 0; ls < L; ls++) {
+    const bool a0 = sh.act[0][ls] != 0;
+    const double scale = sh.scale[ls];
+    const size_t row0 = (size_t)sh.row0[ls];
+    Comp crz{0.f, 0.f}, crr{0.f, 0.f};
+    for (int sl = first_slice(ls); sl < sh.lfirst[ls + 1]; sl += kRingWarps) {
+      const int rs = sl * kSliceRows + t;
+      const int row = perm[rs];
+      const float rl = (a0 && row >= 0) ? (float)(r64[row0 + 3 * (size_t)row + rsub] * scale) : 0.f;
+      const float r0 = __shfl_sync(0xffffffffu, rl, lbase);
+      const float r1 = __shfl_sync(0xffffffffu, rl, lbase + 1);
+      const float r2 = __shfl_sync(0xffffffffu, rl, lbase + 2);
+      float zl = rl;
+      if (pkind == OD_PRECOND_JACOBI) zl = pinv[(size_t)30 * sl + ln] * rl;
+      else if (pkind == OD_PRECOND_BLOCK_JACOBI) {
+        const float* m = pinv + (size_t)90 * sl + ln;
+        zl = fmaf(m[0], r0, fmaf(m[30], r1, m[60] * r2));
+      }
+      if (act_l) {
+        const size_t i = (size_t)30 * sl + lane;
+        r[i] = rl;
+        d[i] = 0.f;
+        z[i] = zl;
+        pf[4 * (size_t)rs + rsub] = zl;
+        comp_add_prod(crz, rl, zl);
+        comp_add_prod(crr, rl, rl);
+      }
     }
+    flush(0, ls, crz);
+    flush(1, ls, crr);
   }
-  double rz;
-  {
-    double v2[2] = {comp_value(crz), comp_value(crr)};
-    alive = grid_sums_named<2, kRingConsumers>(v2, part_2, gb);
-    rz = v2[0];
-    rr = v2[1];
+  alive = ring_sums<2>(sh, L, sc_lo, n_sc, 0.0, part_2, part_g2, gb);
+  if (w == 0 && lane < L) {
+    const double rz = sh.res[0][lane], rr = sh.res[1][lane];
+    const bool a0 = sh.act[0][lane] != 0;
+    sh.rz[lane] = rz;
+    sh.rr[lane] = rr;
+    sh.eps[lane] = rr * sh.eps[lane];
+    sh.it[lane] = 0;
+    sh.status[lane] = isfinite(rr) ? OD_OK : OD_ERR_NAN;
+    sh.act[0][lane] = (unsigned char)(a0 && isfinite(rr) && rr > sh.eps[lane] && sh.maxit[lane] > 0);
   }
-  const double eps = rr * inner_tol * inner_tol;
-  if (!isfinite(rr)) status = OD_ERR_NAN;
-  while (alive && status == OD_OK && it < max_iter && rr > eps) {
-    // q = A p (pieces from the ring), p.q
-    Comp cpq{0.f, 0.f};
-    for (int sl = sfirst + w; sl < send && alive; sl += kRingWarps) {
-      const int k1 = off[sl + 1];
-      float y0 = 0.f, y1 = 0.f, y2 = 0.f;  // partial rows 0, 1, 2 of block row t
-      for (int k = off[sl]; k < k1; k += kRingSteps) {
-        const int n = min(kRingSteps, k1 - k);
-        const int j = pc & 1;
-        if (!__all_sync(0xffffffffu, mbar_wait(full + 2 * w + j, (pc >> 1) & 1))) {
-          atomicExch(&gb->timeout, 1);
-          alive = false;
-          break;
-        }
-        const unsigned char* stg = ring_smem + (size_t)(2 * w + j) * kRingStageBytes;
-        const float* sv = reinterpret_cast<const float*>(stg);
-        const int* scol = reinterpret_cast<const int*>(stg + kRingSteps * 360);
-        // lane (t, rsub) takes steps rsub, rsub + 3, ... of the piece for all
-        // three rows of block row t: every gather is issued before any use
-        constexpr int kPer = (kRingSteps + 2) / 3;
-        float4 x[kPer];
+  __threadfence_block();
+  if (threadIdx.x == 0) sh.pub = 0;
+  named_sync<kRingConsumers>();
+
+  for (int k = 0; alive; k++) {
+    const int kp = k & 1;
+    // ---- q = A p (pieces from the ring), p.q
+    {
+      zero_ws(1);
+      for (int ls = 0; ls < L && alive; ls++) {
+        const bool on = sh.act[kp][ls] != 0;
+        Comp cpq{0.f, 0.f};
+        for (int sl = first_slice(ls); sl < sh.lfirst[ls + 1] && alive; sl += kRingWarps) {
+          const int k1 = off[sl + 1];
+          float y0 = 0.f, y1 = 0.f, y2 = 0.f;  // partial rows 0, 1, 2 of block row t
+          for (int kk = off[sl]; kk < k1; kk += kRingSteps) {
+            const int n = min(kRingSteps, k1 - kk);
+            const int j = pc & 1;
+            if (!__all_sync(0xffffffffu, mbar_wait(full + 2 * w + j, (pc >> 1) & 1))) {
+              atomicExch(&gb->timeout, 1);
+              alive = false;
+              break;
+            }
+            if (on) {
+              const unsigned char* stg = ring_smem + (size_t)(2 * w + j) * kRingStageBytes;
+              const float* sv = reinterpret_cast<const float*>(stg);
+              const int* scol = reinterpret_cast<const int*>(stg + kRingSteps * 360);
+              // lane (t, rsub) takes steps rsub, rsub + 3, ... of the piece
+              // for all three rows of block row t: every gather is issued first
+              constexpr int kPer = (kRingSteps + 2) / 3;
+              float4 x[kPer];
 #pragma unroll
-        for (int u = 0; u < kPer; u++) {
-          const int st = rsub + 3 * u;
-          x[u] = st < n ? p4[scol[st * kSliceRows + t]] : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
+              for (int u = 0; u < kPer; u++) {
+                const int st = rsub + 3 * u;
+                x[u] = st < n ? p4[scol[st * kSliceRows + t]] : make_float4(0.f, 0.f, 0.f, 0.f);
+              }
 #pragma unroll
-        for (int u = 0; u < kPer; u++) {
-          const int st = rsub + 3 * u;
-          if (st < n) {
-            const float* a = sv + st * 90 + lbase;  // a[30 j + r] = A[r][j]
-            y0 = fmaf(a[0], x[u].x, y0);
-            y0 = fmaf(a[30], x[u].y, y0);
-            y0 = fmaf(a[60], x[u].z, y0);
-            y1 = fmaf(a[1], x[u].x, y1);
-            y1 = fmaf(a[31], x[u].y, y1);
-            y1 = fmaf(a[61], x[u].z, y1);
-            y2 = fmaf(a[2], x[u].x, y2);
-            y2 = fmaf(a[32], x[u].y, y2);
-            y2 = fmaf(a[62], x[u].z, y2);
+              for (int u = 0; u < kPer; u++) {
+                const int st = rsub + 3 * u;
+                if (st < n) {
+                  const float* a = sv + st * 90 + lbase;  // a[30 j + r] = A[r][j]
+                  y0 = fmaf(a[0], x[u].x, y0);
+                  y0 = fmaf(a[30], x[u].y, y0);
+                  y0 = fmaf(a[60], x[u].z, y0);
+                  y1 = fmaf(a[1], x[u].x, y1);
+                  y1 = fmaf(a[31], x[u].y, y1);
+                  y1 = fmaf(a[61], x[u].z, y1);
+                  y2 = fmaf(a[2], x[u].x, y2);
+                  y2 = fmaf(a[32], x[u].y, y2);
+                  y2 = fmaf(a[62], x[u].z, y2);
+                }
+              }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(empty + 2 * w + j);
+            pc++;
+          }
+          if (on) {
+            // row rsub of block row t: own partial + the two neighbours' (fixed order)
+            const int l1 = lbase + (rsub == 2 ? 0 : rsub + 1), l2 = lbase + (rsub == 0 ? 2 : rsub - 1);
+            const float a0 = __shfl_sync(0xffffffffu, y0, l1), b0 = __shfl_sync(0xffffffffu, y0, l2);
+            const float a1 = __shfl_sync(0xffffffffu, y1, l1), b1 = __shfl_sync(0xffffffffu, y1, l2);
+            const float a2 = __shfl_sync(0xffffffffu, y2, l1), b2 = __shfl_sync(0xffffffffu, y2, l2);
+            const float own = rsub == 0 ? y0 : (rsub == 1 ? y1 : y2);
+            const float na = rsub == 0 ? a0 : (rsub == 1 ? a1 : a2);
+            const float nb = rsub == 0 ? b0 : (rsub == 1 ? b1 : b2);
+            const float y = (own + na) + nb;
+            if (act_l) {
+              q[(size_t)30 * sl + lane] = y;
+              comp_add_prod(cpq, pf[4 * (size_t)(sl * kSliceRows + t) + rsub], y);
+            }
           }
         }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(empty + 2 * w + j);
-        pc++;
+        if (on) flush(0, ls, cpq);
       }
-      // row rsub of block row t: own partial + the two neighbours' (fixed order)
-      const int l1 = lbase + (rsub == 2 ? 0 : rsub + 1), l2 = lbase + (rsub == 0 ? 2 : rsub - 1);
-      const float a0 = __shfl_sync(0xffffffffu, y0, l1), b0 = __shfl_sync(0xffffffffu, y0, l2);
-      const float a1 = __shfl_sync(0xffffffffu, y1, l1), b1 = __shfl_sync(0xffffffffu, y1, l2);
-      const float a2 = __shfl_sync(0xffffffffu, y2, l1), b2 = __shfl_sync(0xffffffffu, y2, l2);
-      const float own = rsub == 0 ? y0 : (rsub == 1 ? y1 : y2);
-      const float na = rsub == 0 ? a0 : (rsub == 1 ? a1 : a2);
-      const float nb = rsub == 0 ? b0 : (rsub == 1 ? b1 : b2);
-      const float y = (own + na) + nb;
-      if (act) {
-        q[(size_t)30 * sl + lane] = y;
-        comp_add_prod(cpq, pf[4 * (size_t)(sl * kSliceRows + t) + rsub], y);
-      }
+      // active scenes of this CTA at iteration k (grid-wide sum: 0 ends the loop)
+      double na = 0.0;
+      if (w == 0 && lane == 0)
+        for (int ls = 0; ls < L; ls++) na += sh.act[kp][ls] ? 1.0 : 0.0;
+      if (!ring_sums<1>(sh, L, sc_lo, n_sc, na, part_1, part_g1, gb)) alive = false;
     }
-    double v1[1] = {comp_value(cpq)};
-    if (!grid_sums_named<1, kRingConsumers>(v1, part_1, gb)) alive = false;
-    if (!alive) break;
-    const float alpha = (float)(rz / v1[0]);
-    // d += alpha p, r -= alpha q, z = M^-1 r, r.z, r.r: kUB slices per
+    if (!alive || sh.g == 0.0) break;
+    // ---- d += alpha p, r -= alpha q, z = M^-1 r, r.z, r.r: kUB slices per
     // batch, all loads of a batch issued before any use
-    constexpr int kUB = 4;
-    Comp cz{0.f, 0.f}, cr{0.f, 0.f};
-    for (int sl0 = sfirst + w; sl0 < send; sl0 += kUB * kRingWarps) {
-      float dv[kUB], pv[kUB], qv[kUB], rv[kUB], m0[kUB], m1[kUB], m2[kUB];
+    zero_ws(2);
+    for (int ls = 0; ls < L; ls++) {
+      if (!sh.act[kp][ls]) continue;  // warp-uniform; the partials stay zero
+      constexpr int kUB = 4;
+      const int hi = sh.lfirst[ls + 1];
+      const float alpha = (float)(sh.rz[ls] / sh.res[0][ls]);
+      Comp cz{0.f, 0.f}, cr{0.f, 0.f};
+      for (int sl0 = first_slice(ls); sl0 < hi; sl0 += kUB * kRingWarps) {
+        float dv[kUB], pv[kUB], qv[kUB], rv[kUB], m0[kUB], m1[kUB], m2[kUB];
 #pragma unroll
-      for (int u = 0; u < kUB; u++) {
-        const int sl = sl0 + u * kRingWarps;
-        if (sl < send) {
-          const size_t i = (size_t)30 * sl + ln;
-          dv[u] = d[i];
-          pv[u] = pf[4 * (size_t)(sl * kSliceRows + t) + rsub];
-          qv[u] = q[i];
-          rv[u] = r[i];
-          if (pkind == OD_PRECOND_BLOCK_JACOBI) {
-            const float* m = pinv + (size_t)90 * sl + ln;
-            m0[u] = m[0];
-            m1[u] = m[30];
-            m2[u] = m[60];
-          } else if (pkind == OD_PRECOND_JACOBI) {
-            m0[u] = pinv[(size_t)30 * sl + ln];
+        for (int u = 0; u < kUB; u++) {
+          const int sl = sl0 + u * kRingWarps;
+          if (sl < hi) {
+            const size_t i = (size_t)30 * sl + ln;
+            dv[u] = d[i];
+            pv[u] = pf[4 * (size_t)(sl * kSliceRows + t) + rsub];
+            qv[u] = q[i];
+            rv[u] = r[i];
+            if (pkind == OD_PRECOND_BLOCK_JACOBI) {
+              const float* m = pinv + (size_t)90 * sl + ln;
+              m0[u] = m[0];
+              m1[u] = m[30];
+              m2[u] = m[60];
+            } else if (pkind == OD_PRECOND_JACOBI) {
+              m0[u] = pinv[(size_t)30 * sl + ln];
+            }
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kUB; u++) {
+          const int sl = sl0 + u * kRingWarps;
+          if (sl < hi) {  // warp-uniform
+            const size_t i = (size_t)30 * sl + ln;
+            const float rl = act_l ? fmaf(-alpha, qv[u], rv[u]) : 0.f;
+            const float r0 = __shfl_sync(0xffffffffu, rl, lbase);
+            const float r1 = __shfl_sync(0xffffffffu, rl, lbase + 1);
+            const float r2 = __shfl_sync(0xffffffffu, rl, lbase + 2);
+            float zl = rl;
+            if (pkind == OD_PRECOND_BLOCK_JACOBI) zl = fmaf(m0[u], r0, fmaf(m1[u], r1, m2[u] * r2));
+            else if (pkind == OD_PRECOND_JACOBI) zl = m0[u] * rl;
+            if (act_l) {
+              d[i] = fmaf(alpha, pv[u], dv[u]);
+              r[i] = rl;
+              z[i] = zl;
+              comp_add_prod(cz, rl, zl);
+              comp_add_prod(cr, rl, rl);
+            }
           }
         }
       }
-#pragma unroll
-      for (int u = 0; u < kUB; u++) {
-        const int sl = sl0 + u * kRingWarps;
-        if (sl < send) {  // warp-uniform
-          const size_t i = (size_t)30 * sl + ln;
-          const float rl = act ? fmaf(-alpha, qv[u], rv[u]) : 0.f;
-          const float r0 = __shfl_sync(0xffffffffu, rl, lbase);
-          const float r1 = __shfl_sync(0xffffffffu, rl, lbase + 1);
-          const float r2 = __shfl_sync(0xffffffffu, rl, lbase + 2);
-          float zl = rl;
-          if (pkind == OD_PRECOND_BLOCK_JACOBI) zl = fmaf(m0[u], r0, fmaf(m1[u], r1, m2[u] * r2));
-          else if (pkind == OD_PRECOND_JACOBI) zl = m0[u] * rl;
-          if (act) {
-            d[i] = fmaf(alpha, pv[u], dv[u]);
-            r[i] = rl;
-            z[i] = zl;
-            comp_add_prod(cz, rl, zl);
-            comp_add_prod(cr, rl, rl);
-          }
-        }
-      }
+      flush(0, ls, cz);
+      flush(1, ls, cr);
     }
-    double v2[2] = {comp_value(cz), comp_value(cr)};
-    if (!grid_sums_named<2, kRingConsumers>(v2, part_2, gb)) { alive = false; break; }
-    const double beta = v2[0] / rz;
-    rz = v2[0];
-    rr = v2[1];
-    it++;
-    if (!isfinite(rr) || !isfinite(beta)) status = OD_ERR_NAN;
-    const float bf = (float)beta;
-    // p = z + beta p, kUD slices per batch
-    constexpr int kUD = 8;
-    for (int sl0 = sfirst + w; sl0 < send; sl0 += kUD * kRingWarps) {
-      float zv[kUD], pv[kUD];
-#pragma unroll
-      for (int u = 0; u < kUD; u++) {
-        const int sl = sl0 + u * kRingWarps;
-        if (sl < send) {
-          zv[u] = z[(size_t)30 * sl + ln];
-          pv[u] = pf[4 * (size_t)(sl * kSliceRows + t) + rsub];
-        }
+    // sh.res[0] (p.q) is read above by every warp; ring_sums rewrites sh.res
+    // only after its first named barrier
+    if (!ring_sums<2>(sh, L, sc_lo, n_sc, 0.0, part_2, part_g2, gb)) { alive = false; break; }
+    if (w == 0 && lane < L) {
+      const int ls = lane;
+      unsigned char na = 0;
+      if (sh.act[kp][ls]) {
+        const double rz = sh.res[0][ls], rr = sh.res[1][ls];
+        const double beta = rz / sh.rz[ls];
+        sh.res[0][ls] = beta;  // beta for the direction update
+        sh.rz[ls] = rz;
+        sh.rr[ls] = rr;
+        sh.it[ls]++;
+        if (!isfinite(rr) || !isfinite(beta)) sh.status[ls] = OD_ERR_NAN;
+        na = (unsigned char)(sh.status[ls] == OD_OK && rr > sh.eps[ls] && sh.it[ls] < sh.maxit[ls]);
       }
+      sh.act[kp ^ 1][ls] = na;
+    }
+    __threadfence_block();
+    named_sync<kRingConsumers>();
+    if (threadIdx.x == 0) sh.pub = k + 1;
+    // ---- p = z + beta p for the scenes active in this iteration
+    for (int ls = 0; ls < L; ls++) {
+      if (!sh.act[kp][ls]) continue;
+      constexpr int kUD = 8;
+      const int hi = sh.lfirst[ls + 1];
+      const float bf = (float)sh.res[0][ls];
+      for (int sl0 = first_slice(ls); sl0 < hi; sl0 += kUD * kRingWarps) {
+        float zv[kUD], pv[kUD];
 #pragma unroll
-      for (int u = 0; u < kUD; u++) {
-        const int sl = sl0 + u * kRingWarps;
-        if (sl < send && act) pf[4 * (size_t)(sl * kSliceRows + t) + rsub] = fmaf(bf, pv[u], zv[u]);
+        for (int u = 0; u < kUD; u++) {
+          const int sl = sl0 + u * kRingWarps;
+          if (sl < hi) {
+            zv[u] = z[(size_t)30 * sl + ln];
+            pv[u] = pf[4 * (size_t)(sl * kSliceRows + t) + rsub];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kUD; u++) {
+          const int sl = sl0 + u * kRingWarps;
+          if (sl < hi && act_l) pf[4 * (size_t)(sl * kSliceRows + t) + rsub] = fmaf(bf, pv[u], zv[u]);
+        }
       }
     }
     if (!grid_barrier_named<kRingConsumers>(gb)) { alive = false; break; }
   }
   named_sync<kRingConsumers>();
-  if (threadIdx.x == 0) stop_s = 1;
-  if (alive && blockIdx.x == 0 && threadIdx.x == 0) {
-    sc->iter = it;
-    sc->rr = rr;
-    sc->status = status;
-    sc->done = 1;
+  if (threadIdx.x == 0) sh.stop = 1;
+  if (alive && w == 0 && lane < L) {
+    const int s = sc_lo + lane;
+    if (sc_cta[2 * s] == (int)blockIdx.x) {
+      ring[s].iters = sh.it[lane];
+      ring[s].status = sh.status[lane];
+      ring[s].rr = sh.rr[lane];
+    }
   }
 }
 
@@ -1450,10 +1612,7 @@ void pcg_free(Scene* s) {
     cudaFree(v);
   cudaFree(P.sc);
   cudaFree(P.gbar);
-  cudaFree(P.v32);
-  cudaFree(P.r64);
-  cudaFree(P.sl_val);
-  for (int* v : {P.sl_perm, P.sl_off, P.sl_col, P.sl_src, P.sl_cta}) cudaFree(v);
+  mixed_free(P.mix);
   if (P.sc_host) cudaFreeHost(P.sc_host);
   if (P.timeout_host) cudaFreeHost(P.timeout_host);
   P = Pcg();
@@ -1500,38 +1659,8 @@ static od_status pcg_finish(Scene* s, const double* d_b, double* d_x, double shi
   return status == OD_ERR_DEVICE_TIMEOUT ? OD_ERR_DEVICE_TIMEOUT : OD_OK;
 }
 
-// Slice structure and FP32 storage of the mixed-precision inner solve,
-// built on first use (the pattern never changes for a scene).
-static od_status sliced_alloc(Scene* s) {
-  Pcg& P = s->pcg;
-  if (P.sl_val) return OD_OK;
-  HostSliced hs;
-  build_sliced(s->hbsr_rp, s->hbsr_col, s->bsr.nb, hs);
-  P.sl_ns = hs.ns;
-  P.sl_steps = hs.off[hs.ns];
-  P.sl_off_host = hs.off;
-  auto up = [&](int** dst, const std::vector<int>& v) -> od_status {
-    OD_CUDA(cudaMalloc(dst, sizeof(int) * std::max<size_t>(1, v.size())));
-    OD_CUDA(cudaMemcpy(*dst, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice));
-    s->device_bytes += (long long)sizeof(int) * v.size();
-    return OD_OK;
-  };
-  OD_TRY(up(&P.sl_perm, hs.perm));
-  OD_TRY(up(&P.sl_off, hs.off));
-  OD_TRY(up(&P.sl_col, hs.col));
-  OD_TRY(up(&P.sl_src, hs.src));
-  const size_t ns = (size_t)hs.ns;
-  const size_t nval = (size_t)std::max<long long>(1, P.sl_steps) * 90;
-  const size_t nvec = 40 * ns + 4 * 30 * ns + 90 * ns;
-  OD_CUDA(cudaMalloc(&P.sl_val, sizeof(float) * nval));
-  OD_CUDA(cudaMalloc(&P.v32, sizeof(float) * nvec));
-  OD_CUDA(cudaMemset(P.v32, 0, sizeof(float) * nvec));
-  OD_CUDA(cudaMalloc(&P.r64, sizeof(double) * (size_t)P.n_pad));
-  s->device_bytes += (long long)(sizeof(float) * (nval + nvec) + sizeof(double) * (size_t)P.n_pad);
-  return OD_OK;
-}
+// ---- mixed-precision systems: build, partition, solve
 
-// co-resident CTAs of the ring kernel (one per SM), 0 if it cannot launch
 static int ring_kernel_ctas(const Ctx* ctx) {
   if (cudaFuncSetAttribute(pcg32_ring_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kRingSmem) != cudaSuccess)
     return 0;
@@ -1542,130 +1671,313 @@ static int ring_kernel_ctas(const Ctx* ctx) {
   return std::min(per_sm, 1) * ctx->num_sms;
 }
 
-// contiguous slice ranges per CTA with about equal step counts
-static od_status ring_partition(Scene* s, int G) {
-  Pcg& P = s->pcg;
-  if (P.sl_cta && P.sl_cta_grid == G) return OD_OK;
-  const std::vector<int>& off = P.sl_off_host;
-  const int ns = P.sl_ns;
-  std::vector<int> first(G + 1, ns);
-  first[0] = 0;
-  int sl = 0;
-  for (int b = 1; b < G; b++) {
-    const long long target = (long long)off[ns] * b / G;
-    while (sl < ns && off[sl] < target) sl++;
-    first[b] = sl;
-  }
-  if (P.sl_cta) cudaFree(P.sl_cta);
-  P.sl_cta = nullptr;
-  OD_CUDA(cudaMalloc(&P.sl_cta, sizeof(int) * (G + 1)));
-  OD_CUDA(cudaMemcpy(P.sl_cta, first.data(), sizeof(int) * (G + 1), cudaMemcpyHostToDevice));
-  P.sl_cta_grid = G;
+void mixed_free(MixedSys* m) {
+  if (!m) return;
+  for (int* v : {m->perm, m->slice_sc, m->sc_slice_dev, m->off, m->col, m->src, m->cta_first, m->cta_sc_lo,
+                 m->sc_cta})
+    cudaFree(v);
+  cudaFree(m->val);
+  cudaFree(m->v32);
+  cudaFree(m->r64);
+  cudaFree(m->desc);
+  cudaFree(m->ring);
+  cudaFree(m->rrbb);
+  cudaFree(m->res_tiles);
+  cudaFree(m->res_part);
+  cudaFree(m->fill_tiles);
+  cudaFree(m->part);
+  cudaFree(m->gbar);
+  if (m->ring_host) cudaFreeHost(m->ring_host);
+  if (m->rrbb_host) cudaFreeHost(m->rrbb_host);
+  if (m->timeout_host) cudaFreeHost(m->timeout_host);
+  delete m;
+}
+
+template <class T>
+static od_status mix_upload(MixedSys* m, T** dst, const T* src, size_t n) {
+  OD_CUDA(cudaMalloc((void**)dst, sizeof(T) * std::max<size_t>(1, n)));
+  if (n) OD_CUDA(cudaMemcpy(*dst, src, sizeof(T) * n, cudaMemcpyHostToDevice));
+  m->device_bytes += (long long)(sizeof(T) * n);
   return OD_OK;
 }
 
-// Mixed-precision solve: FP64 iterative refinement around the FP32 inner
-// PCG.  Every outer sweep recomputes the true residual b - A x in FP64 (the
-// residual replacement), solves A32 d = r / ||r|| to inner_tol relative with
-// the FP32 sliced PCG, and adds ||r|| d to x in FP64; it stops when
-// ||b - A x|| <= tol ||b||.
-static od_status pcg_solve_mixed(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm,
-                                 od_solve_stats* st) {
-  Pcg& P = s->pcg;
-  cudaStream_t strm = s->ctx->stream;
-  const int nb = s->bsr.nb;
-  const int pk = prm->precond;
-  if (pk == OD_PRECOND_IC0) { set_error("mixed precision supports the none, Jacobi and block-Jacobi preconditioners"); return OD_ERR_UNSUPPORTED; }
-  const int G2 = P.coop_grid > 0 ? ring_kernel_ctas(s->ctx) : 0;
-  if (G2 <= 0) { set_error("mixed precision needs cooperative launch"); return OD_ERR_UNSUPPORTED; }
-  OD_TRY(sliced_alloc(s));
-  OD_TRY(ring_partition(s, G2));
-  const int ns = P.sl_ns, nrs = ns * kSliceRows;
-  float4* p4 = reinterpret_cast<float4*>(P.v32);
-  float* d32 = P.v32 + 40 * (size_t)ns;
+// Contiguous slice ranges per CTA with about equal step counts and at most
+// kMaxLocalScenes scenes each.
+static od_status mixed_partition(MixedSys* m, int G) {
+  const int ns = m->ns;
+  std::vector<int> sc_of(ns);
+  for (int s = 0; s < m->n_sc; s++)
+    for (int k = m->sc_slice[s]; k < m->sc_slice[s + 1]; k++) sc_of[k] = s;
+  const std::vector<int>& off = m->off_host;
+  std::vector<int> first(G + 1, ns), sc_lo(G, 0);
+  std::vector<int> sc_cta(2 * std::max(1, m->n_sc), -1);
+  for (int s = 0; s < m->n_sc; s++) sc_cta[2 * s + 1] = -2;  // empty range for scenes without slices
+  int sl = 0;
+  for (int b = 0; b < G; b++) {
+    first[b] = sl;
+    sc_lo[b] = sl < ns ? sc_of[sl] : 0;
+    const long long target = (long long)off[ns] * (b + 1) / G;
+    while (sl < ns && (off[sl] < target || b == G - 1)) {
+      if (sc_of[sl] - sc_lo[b] >= kMaxLocalScenes) break;
+      sl++;
+    }
+  }
+  first[G] = sl;
+  if (sl < ns) {
+    set_error("mixed solve: too many small scenes for one grid (at most " + std::to_string(kMaxLocalScenes) +
+              " per multiprocessor)");
+    return OD_ERR_UNSUPPORTED;
+  }
+  for (int b = 0; b < G; b++) {
+    if (first[b + 1] <= first[b]) continue;
+    for (int s = sc_of[first[b]]; s <= sc_of[first[b + 1] - 1]; s++) {
+      if (sc_cta[2 * s] < 0) sc_cta[2 * s] = b;
+      sc_cta[2 * s + 1] = b;
+    }
+  }
+  for (int* v : {m->cta_first, m->cta_sc_lo, m->sc_cta}) cudaFree(v);
+  cudaFree(m->part);
+  m->cta_first = m->cta_sc_lo = m->sc_cta = nullptr;
+  m->part = nullptr;
+  OD_TRY(mix_upload(m, &m->cta_first, first.data(), first.size()));
+  OD_TRY(mix_upload(m, &m->cta_sc_lo, sc_lo.data(), sc_lo.size()));
+  OD_TRY(mix_upload(m, &m->sc_cta, sc_cta.data(), sc_cta.size()));
+  const size_t npart = (size_t)3 * std::max(1, m->n_sc) * G + 2 * (size_t)G;
+  OD_CUDA(cudaMalloc(&m->part, sizeof(double) * npart));
+  OD_CUDA(cudaMemset(m->part, 0, sizeof(double) * npart));
+  m->cta_grid = G;
+  return OD_OK;
+}
+
+od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::vector<const double*>& b,
+                      const std::vector<double*>& x, MixedSys** out) {
+  MixedSys* m = new MixedSys();
+  m->n_sc = (int)scenes.size();
+  std::vector<int> perm, slice_sc, off{0}, col, src;
+  std::vector<Tile> res_tiles, fill_tiles;
+  m->sc_slice.push_back(0);
+  int row0 = 0;
+  for (int i = 0; i < m->n_sc; i++) {
+    Scene* s = scenes[i];
+    HostSliced hs;
+    build_sliced(s->hbsr_rp, s->hbsr_col, s->bsr.nb, hs);
+    const int slice0 = (int)slice_sc.size(), step0 = off.back();
+    perm.insert(perm.end(), hs.perm.begin(), hs.perm.end());
+    slice_sc.insert(slice_sc.end(), hs.ns, i);
+    for (int k = 1; k <= hs.ns; k++) off.push_back(step0 + hs.off[k]);
+    for (int c : hs.col) col.push_back(c + kSliceRows * slice0);
+    src.insert(src.end(), hs.src.begin(), hs.src.end());
+    m->sc_slice.push_back(slice0 + hs.ns);
+    m->sc_row0.push_back(row0);
+    m->sc_nb.push_back(s->bsr.nb);
+    MixDesc dsc{};
+    dsc.row_ptr = s->bsr.row_ptr;
+    dsc.col = s->bsr.col;
+    dsc.diag_pos = s->bsr.diag_pos;
+    dsc.A64 = s->A64;
+    dsc.b = i < (int)b.size() ? b[i] : nullptr;
+    dsc.x = i < (int)x.size() ? x[i] : nullptr;
+    dsc.nb = s->bsr.nb;
+    dsc.row0 = row0;
+    dsc.tile0 = (int)res_tiles.size();
+    for (int r = 0; r < s->bsr.nb; r += kResRows) res_tiles.push_back(Tile{i, r, std::min(s->bsr.nb, r + kResRows), 0});
+    dsc.ntiles = (int)res_tiles.size() - dsc.tile0;
+    for (int k = step0; k < off.back(); k += 32) fill_tiles.push_back(Tile{i, k, std::min(off.back(), k + 32), 0});
+    m->desc_host.push_back(dsc);
+    row0 += 3 * s->bsr.nb;
+  }
+  m->ns = (int)slice_sc.size();
+  m->steps = off.back();
+  m->n64 = row0;
+  m->off_host = off;
+  m->n_res_tiles = (int)res_tiles.size();
+  m->n_fill_tiles = (int)fill_tiles.size();
+  auto fail = [&](od_status st) { mixed_free(m); return st; };
+  od_status st;
+  if ((st = mix_upload(m, &m->perm, perm.data(), perm.size())) != OD_OK) return fail(st);
+  if ((st = mix_upload(m, &m->slice_sc, slice_sc.data(), slice_sc.size())) != OD_OK) return fail(st);
+  if ((st = mix_upload(m, &m->sc_slice_dev, m->sc_slice.data(), m->sc_slice.size())) != OD_OK) return fail(st);
+  if ((st = mix_upload(m, &m->off, off.data(), off.size())) != OD_OK) return fail(st);
+  if ((st = mix_upload(m, &m->col, col.data(), col.size())) != OD_OK) return fail(st);
+  if ((st = mix_upload(m, &m->src, src.data(), src.size())) != OD_OK) return fail(st);
+  if ((st = mix_upload(m, &m->desc, m->desc_host.data(), m->desc_host.size())) != OD_OK) return fail(st);
+  if ((st = mix_upload(m, &m->res_tiles, res_tiles.data(), res_tiles.size())) != OD_OK) return fail(st);
+  if ((st = mix_upload(m, &m->fill_tiles, fill_tiles.data(), fill_tiles.size())) != OD_OK) return fail(st);
+  const size_t ns = (size_t)m->ns;
+  const size_t nval = (size_t)std::max<long long>(1, m->steps) * 90;
+  const size_t nvec = (40 + 4 * 30 + 90) * std::max<size_t>(1, ns);
+  cudaError_t e = cudaMalloc(&m->val, sizeof(float) * nval);
+  if (e == cudaSuccess) e = cudaMalloc(&m->v32, sizeof(float) * nvec);
+  if (e == cudaSuccess) e = cudaMemset(m->v32, 0, sizeof(float) * nvec);
+  if (e == cudaSuccess) e = cudaMalloc(&m->r64, sizeof(double) * std::max(1, m->n64));
+  if (e == cudaSuccess) e = cudaMalloc(&m->ring, sizeof(RingScene) * std::max(1, m->n_sc));
+  if (e == cudaSuccess) e = cudaMallocHost(&m->ring_host, sizeof(RingScene) * std::max(1, m->n_sc));
+  if (e == cudaSuccess) e = cudaMalloc(&m->rrbb, sizeof(double) * 2 * std::max(1, m->n_sc));
+  if (e == cudaSuccess) e = cudaMallocHost(&m->rrbb_host, sizeof(double) * 2 * std::max(1, m->n_sc));
+  if (e == cudaSuccess) e = cudaMalloc(&m->res_part, sizeof(double) * 2 * std::max(1, m->n_res_tiles));
+  if (e == cudaSuccess) e = cudaMalloc(&m->gbar, sizeof(GridBarrier));
+  if (e == cudaSuccess) e = cudaMallocHost(&m->timeout_host, sizeof(int));
+  if (e != cudaSuccess) return fail(cuda_fail(e, "mixed_build"));
+  m->device_bytes += (long long)(sizeof(float) * (nval + nvec) + sizeof(double) * m->n64);
+  const int G = ring_kernel_ctas(ctx);
+  if (G <= 0) {
+    set_error("mixed precision needs a cooperative launch of the ring kernel");
+    return fail(OD_ERR_UNSUPPORTED);
+  }
+  if ((st = mixed_partition(m, G)) != OD_OK) return fail(st);
+  *out = m;
+  return OD_OK;
+}
+
+// FP64 residual of every scene and its norms; brings rrbb (and the ring
+// outputs) back to the host
+static od_status mixed_residual(Ctx* ctx, MixedSys* m, bool with_ring) {
+  cudaStream_t strm = ctx->stream;
+  if (m->n_res_tiles > 0) {
+    ctx->launches += 2;
+    mix_residual_kernel<<<m->n_res_tiles, kThreads, 0, strm>>>(m->res_tiles, m->desc, m->r64, m->res_part);
+    mix_residual_finish<<<nblk(m->n_sc, kThreads / 32), kThreads, 0, strm>>>(m->n_sc, m->desc, m->res_part, m->rrbb);
+    OD_CUDA(cudaGetLastError());
+  } else {
+    OD_CUDA(cudaMemsetAsync(m->rrbb, 0, sizeof(double) * 2 * m->n_sc, strm));
+  }
+  OD_CUDA(cudaMemcpyAsync(m->rrbb_host, m->rrbb, sizeof(double) * 2 * m->n_sc, cudaMemcpyDeviceToHost, strm));
+  if (with_ring)
+    OD_CUDA(cudaMemcpyAsync(m->ring_host, m->ring, sizeof(RingScene) * m->n_sc, cudaMemcpyDeviceToHost, strm));
+  ctx->host_syncs++;
+  OD_CUDA(cudaStreamSynchronize(strm));
+  return OD_OK;
+}
+
+od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver_params>& prm,
+                      std::vector<od_solve_stats>& st) {
+  cudaStream_t strm = ctx->stream;
+  const int n_sc = m->n_sc;
+  st.assign(n_sc, od_solve_stats{});
+  if (pk == OD_PRECOND_IC0 || pk < 0 || pk > OD_PRECOND_IC0) {
+    set_error("mixed precision supports the none, Jacobi and block-Jacobi preconditioners");
+    return OD_ERR_UNSUPPORTED;
+  }
+  const int ns = m->ns, nrs = ns * kSliceRows;
+  float4* p4 = reinterpret_cast<float4*>(m->v32);
+  float* d32 = m->v32 + 40 * (size_t)ns;
   float* r32 = d32 + 30 * (size_t)ns;
   float* z32 = r32 + 30 * (size_t)ns;
   float* q32 = z32 + 30 * (size_t)ns;
   float* pinv32 = q32 + 30 * (size_t)ns;
-  const long long nval = 90LL * P.sl_steps;
-  OD_KL(s);
-  sliced_fill_kernel<<<nblk(nval, kThreads), kThreads, 0, strm>>>(nval, P.sl_src, s->A64, P.sl_val);
-  if (pk != OD_PRECOND_NONE) {
-    OD_KL(s);
-    sliced_precond_kernel<<<nblk(nrs, kThreads), kThreads, 0, strm>>>(nrs, pk, P.sl_perm, s->bsr.diag_pos, s->A64,
-                                                                      pinv32);
+  if (m->n_fill_tiles > 0) {
+    ctx->launches++;
+    mix_fill_kernel<<<m->n_fill_tiles, kThreads, 0, strm>>>(m->fill_tiles, m->desc, m->src, m->val);
   }
-  const double inner_tol = prm->inner_tol > 0.0 ? prm->inner_tol : 1e-4;
-  const int max_refine = prm->max_refine > 0 ? prm->max_refine : 20;
-  const int g_res = std::min(P.grid / 2, nblk(nb, kWarpRows));
-  auto residual = [&]() -> od_status {
-    OD_KL(s);
-    refine_residual_kernel<<<g_res, kThreads, 0, strm>>>(nb, s->bsr.row_ptr, s->bsr.col, s->A64, d_b, d_x, P.r64,
-                                                         P.partial);
-    OD_KL(s);
-    refine_norm_finish<<<1, kThreads, 0, strm>>>(P.partial, g_res, P.sc);
-    OD_CUDA(cudaGetLastError());
-    OD_CUDA(cudaMemcpyAsync(P.sc_host, P.sc, sizeof(SolveScalars), cudaMemcpyDeviceToHost, strm));
-    OD_TRY(sync_stream(s));
-    return OD_OK;
-  };
-  OD_TRY(residual());
-  const double bb = P.sc_host->tr_den;
-  double rr = P.sc_host->tr_num;
-  const double eps = bb * prm->tol * prm->tol;
-  int total_it = 0, sweeps = 0;
-  od_status status = std::isfinite(rr) ? OD_OK : OD_ERR_NAN;
-  const bool prof = s->ctx->profiling && s->ctx->ev_pool.size() >= 2;
-  while (status == OD_OK && rr > eps && sweeps < max_refine && total_it < prm->max_iter) {
-    OD_CUDA(cudaMemsetAsync(P.gbar, 0, sizeof(GridBarrier), strm));
-    const double rnorm = std::sqrt(rr);
-    double rhs_scale = rnorm > 0.0 ? 1.0 / rnorm : 1.0;
-    int maxit = prm->max_iter - total_it;
-    GridBarrier* gbp = (GridBarrier*)P.gbar;
-    const double* rhs = P.r64;
+  if (pk != OD_PRECOND_NONE && nrs > 0) {
+    ctx->launches++;
+    mix_precond_kernel<<<nblk(nrs, kThreads), kThreads, 0, strm>>>(nrs, pk, m->perm, m->slice_sc, m->desc, pinv32);
+  }
+  OD_TRY(mixed_residual(ctx, m, false));
+  std::vector<double> eps(n_sc), rr(n_sc), bb(n_sc);
+  std::vector<int> total(n_sc, 0), sweeps(n_sc, 0), need(n_sc, 0), status(n_sc, OD_OK);
+  for (int s = 0; s < n_sc; s++) {
+    rr[s] = m->rrbb_host[2 * s];
+    bb[s] = m->rrbb_host[2 * s + 1];
+    eps[s] = bb[s] * prm[s].tol * prm[s].tol;
+    if (!std::isfinite(rr[s])) status[s] = OD_ERR_NAN;
+    need[s] = status[s] == OD_OK && rr[s] > eps[s] && prm[s].max_iter > 0 && m->sc_nb[s] > 0;
+  }
+  const bool prof = ctx->profiling && ctx->ev_pool.size() >= 2;
+  od_status rc = OD_OK;
+  for (int sweep = 0;; sweep++) {
+    bool any = false;
+    for (int s = 0; s < n_sc; s++) {
+      const int max_refine = prm[s].max_refine > 0 ? prm[s].max_refine : 20;
+      if (need[s] && (sweeps[s] >= max_refine || total[s] >= prm[s].max_iter)) need[s] = 0;
+      RingScene& R = m->ring_host[s];
+      R = RingScene{};
+      R.active0 = need[s];
+      if (need[s]) {
+        any = true;
+        const double rn = std::sqrt(rr[s]);
+        const double inner_tol = prm[s].inner_tol > 0.0 ? prm[s].inner_tol : 1e-4;
+        // a sweep reduces the residual no further than the outer target needs
+        // (with a 0.3 margin), and at least by inner_tol
+        const double itol = std::max(inner_tol, std::min(0.5, 0.3 * std::sqrt(eps[s] / rr[s])));
+        R.rhs_scale = rn > 0.0 ? 1.0 / rn : 1.0;
+        R.unscale = rn > 0.0 ? rn : 1.0;
+        R.itol2 = itol * itol;
+        R.max_iter = prm[s].max_iter - total[s];
+      }
+    }
+    if (!any) break;
+    OD_CUDA(cudaMemcpyAsync(m->ring, m->ring_host, sizeof(RingScene) * n_sc, cudaMemcpyHostToDevice, strm));
+    OD_CUDA(cudaMemsetAsync(m->gbar, 0, sizeof(GridBarrier), strm));
+    GridBarrier* gbp = (GridBarrier*)m->gbar;
     int pkv = pk;
-    // a sweep reduces the residual no further than the outer target needs
-    // (with a 0.3 margin), and at least by inner_tol
-    double itol = std::max(inner_tol, std::min(0.5, 0.3 * std::sqrt(eps / rr)));
-    void* args[] = {(void*)&P.sl_cta, (void*)&P.sl_perm, (void*)&P.sl_off, (void*)&P.sl_col, (void*)&P.sl_val,
-                    (void*)&rhs, (void*)&rhs_scale, (void*)&d32, (void*)&r32, (void*)&z32, (void*)&p4,
-                    (void*)&q32, (void*)&pkv, (void*)&pinv32, (void*)&P.partial, (void*)&itol, (void*)&maxit,
-                    (void*)&P.sc, (void*)&gbp};
-    if (prof) OD_CUDA(cudaEventRecord(s->ctx->ev_pool[0], strm));
-    OD_KL(s);
-    OD_CUDA(cudaLaunchCooperativeKernel((void*)pcg32_ring_kernel, dim3(G2), dim3(kRingThreads), args, kRingSmem,
-                                        strm));
-    if (prof) OD_CUDA(cudaEventRecord(s->ctx->ev_pool[1], strm));
-    OD_KL(s);
-    sliced_update_kernel<<<nblk(3 * nrs, kThreads), kThreads, 0, strm>>>(nrs, P.sl_perm, d32,
-                                                                         rnorm > 0.0 ? rnorm : 1.0, d_x);
-    OD_CUDA(cudaMemcpyAsync(P.timeout_host, &((GridBarrier*)P.gbar)->timeout, sizeof(int), cudaMemcpyDeviceToHost,
-                            strm));
-    OD_TRY(residual());  // also brings back the inner statistics
-    if (*P.timeout_host) { set_error("PCG grid barrier timed out"); status = OD_ERR_DEVICE_TIMEOUT; break; }
-    const int inner_it = P.sc_host->iter;
+    int nsc = n_sc;
+    void* args[] = {(void*)&nsc, (void*)&m->cta_first, (void*)&m->cta_sc_lo, (void*)&m->sc_cta,
+                    (void*)&m->sc_slice_dev, (void*)&m->slice_sc,
+                    (void*)&m->perm,      (void*)&m->off,       (void*)&m->col,    (void*)&m->val,
+                    (void*)&m->r64,       (void*)&m->desc,      (void*)&m->ring,   (void*)&d32,
+                    (void*)&r32,          (void*)&z32,          (void*)&p4,        (void*)&q32,
+                    (void*)&pkv,          (void*)&pinv32,       (void*)&m->part,   (void*)&gbp};
+    if (prof) OD_CUDA(cudaEventRecord(ctx->ev_pool[0], strm));
+    ctx->launches++;
+    OD_CUDA(cudaLaunchCooperativeKernel((void*)pcg32_ring_kernel, dim3(m->cta_grid), dim3(kRingThreads), args,
+                                        kRingSmem, strm));
+    if (prof) OD_CUDA(cudaEventRecord(ctx->ev_pool[1], strm));
+    ctx->launches++;
+    mix_update_kernel<<<nblk(3LL * nrs, kThreads), kThreads, 0, strm>>>(nrs, m->perm, m->slice_sc, m->desc, m->ring,
+                                                                         d32);
+    OD_CUDA(cudaMemcpyAsync(m->timeout_host, &gbp->timeout, sizeof(int), cudaMemcpyDeviceToHost, strm));
+    OD_TRY(mixed_residual(ctx, m, true));
+    if (*m->timeout_host) {
+      set_error("PCG grid barrier timed out");
+      rc = OD_ERR_DEVICE_TIMEOUT;
+      for (int s = 0; s < n_sc; s++)
+        if (need[s]) status[s] = OD_ERR_DEVICE_TIMEOUT;
+      break;
+    }
     if (prof) {
       float ms = 0.f;
-      OD_CUDA(cudaEventElapsedTime(&ms, s->ctx->ev_pool[0], s->ctx->ev_pool[1]));
-      s->ctx->pcg_kernel_ms += ms;
-      s->ctx->pcg_kernel_launches++;
-      s->ctx->pcg_kernel_iters += inner_it;
+      OD_CUDA(cudaEventElapsedTime(&ms, ctx->ev_pool[0], ctx->ev_pool[1]));
+      ctx->pcg_kernel_ms += ms;
+      ctx->pcg_kernel_launches++;
     }
-    total_it += inner_it;
-    sweeps++;
-    rr = P.sc_host->tr_num;
-    if (!std::isfinite(rr)) status = OD_ERR_NAN;
-    if (inner_it == 0) break;  // no progress possible
+    for (int s = 0; s < n_sc; s++) {
+      if (!need[s]) continue;
+      const RingScene& R = m->ring_host[s];
+      total[s] += R.iters;
+      if (prof) ctx->pcg_kernel_iters += R.iters;
+      sweeps[s]++;
+      rr[s] = m->rrbb_host[2 * s];
+      if (!std::isfinite(rr[s]) || R.status == OD_ERR_NAN) { status[s] = OD_ERR_NAN; need[s] = 0; continue; }
+      need[s] = rr[s] > eps[s] && R.iters > 0;  // no progress possible without an inner iteration
+    }
   }
-  if (status == OD_OK && rr > eps) status = OD_ERR_NOT_CONVERGED;
-  if (st) {
-    st->iterations = total_it;
-    st->refinements = sweeps;
-    st->rel_residual = bb > 0.0 ? std::sqrt(rr / bb) : std::sqrt(rr);
-    st->ic_shift = 0.0;
-    st->status = status;
+  for (int s = 0; s < n_sc; s++) {
+    if (status[s] == OD_OK && rr[s] > eps[s] && m->sc_nb[s] > 0) status[s] = OD_ERR_NOT_CONVERGED;
+    st[s].iterations = total[s];
+    st[s].refinements = sweeps[s];
+    st[s].rel_residual = bb[s] > 0.0 ? std::sqrt(rr[s] / bb[s]) : std::sqrt(rr[s]);
+    st[s].ic_shift = 0.0;
+    st[s].status = status[s];
   }
-  return status == OD_ERR_DEVICE_TIMEOUT ? OD_ERR_DEVICE_TIMEOUT : OD_OK;
+  return rc;
+}
+
+// single-scene mixed solve: the scene's own one-scene system
+static od_status pcg_solve_mixed(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm,
+                                 od_solve_stats* st) {
+  Pcg& P = s->pcg;
+  if (!P.mix) OD_TRY(mixed_build(s->ctx, {s}, {d_b}, {d_x}, &P.mix));
+  MixedSys* m = P.mix;
+  if (m->desc_host[0].b != d_b || m->desc_host[0].x != d_x) {
+    m->desc_host[0].b = d_b;
+    m->desc_host[0].x = d_x;
+    OD_CUDA(cudaMemcpyAsync(m->desc, m->desc_host.data(), sizeof(MixDesc), cudaMemcpyHostToDevice, s->ctx->stream));
+  }
+  std::vector<od_solve_stats> out;
+  od_status rc = mixed_solve(s->ctx, m, prm->precond, {*prm}, out);
+  if (st) *st = out[0];
+  return rc;
 }
 
 // Solve A64 x = b (device vectors of length n_pad; padding entries zero).
