@@ -235,6 +235,25 @@ od_status od_step(od_scene* scene, int n_steps, od_step_stats* stats);
 od_status od_get_state(od_scene* scene, double* d, double* v, double* a);
 od_status od_set_state(od_scene* scene, const double* d, const double* v, const double* a);
 
+/* ---- batches: many scenes stepped together on one GPU.  No reference
+ * counterpart (the reference steps one Simulator at a time,
+ * core/simulator.h:21-22); each scene advances by exactly the od_step
+ * sequence, with a fixed number of kernel launches per step for the whole
+ * batch and one mixed-precision solve (per-scene step lengths and
+ * convergence) per Newton iteration.  Every scene of a batch shares ctx, has
+ * a Newmark integrator with the mixed-precision solver, the same Newton count
+ * and the same preconditioner kind (none, Jacobi, block-Jacobi), and no
+ * external damping.  A batch owns device memory of its own (the scenes'
+ * concatenated FP32 systems, about 40 bytes per stored block); the scenes
+ * keep their state and may be stepped alone or in other batches between
+ * calls, never concurrently. */
+typedef struct od_batch od_batch;
+od_status od_batch_create(od_ctx* ctx, int n_scenes, od_scene* const* scenes, od_batch** out);
+/* stats: n_scenes entries (or NULL), in the order of od_batch_create;
+ * device_ms is the time of the whole call */
+od_status od_batch_step(od_batch* batch, int n_steps, od_step_stats* stats);
+od_status od_batch_destroy(od_batch* batch);
+
 /* Allocation-free PCG.  No counterpart in the reference.  For callers that
  * cannot allocate device memory -- a host application whose own allocator
  * owns the GPU's memory, or a plugin running inside another program's

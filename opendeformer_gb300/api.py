@@ -96,6 +96,7 @@ _lib = None
 
 # Live handles, released in a safe order (scenes before contexts) when the
 # interpreter exits, before the CUDA runtime itself is torn down.
+_live_batches: "weakref.WeakSet" = weakref.WeakSet()
 _live_scenes: "weakref.WeakSet" = weakref.WeakSet()
 _live_ctxs: "weakref.WeakSet" = weakref.WeakSet()
 _shutting_down = False
@@ -104,6 +105,11 @@ _shutting_down = False
 @atexit.register
 def _release_all():
     global _shutting_down
+    for bt in list(_live_batches):
+        try:
+            bt.close()
+        except Exception:
+            pass
     for sc in list(_live_scenes):
         try:
             sc.close()
@@ -149,6 +155,9 @@ SIGNATURES = {
     "od_step": (C.c_int, [_vp, C.c_int, C.POINTER(od_step_stats)]),
     "od_get_state": (C.c_int, [_vp, _dp, _dp, _dp]),
     "od_set_state": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "od_batch_create": (C.c_int, [_vp, C.c_int, C.POINTER(_vp), C.POINTER(_vp)]),
+    "od_batch_step": (C.c_int, [_vp, C.c_int, C.POINTER(od_step_stats)]),
+    "od_batch_destroy": (C.c_int, [_vp]),
     "od_bsr_pcg_noalloc": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, C.POINTER(od_solver_params), _vp,
                                      C.POINTER(od_solve_stats)]),
     "od_scene_save": (C.c_int, [_vp, _vp, C.POINTER(C.c_size_t)]),
@@ -473,6 +482,40 @@ class Scene:
     def load(self, blob: bytes):
         buf = C.create_string_buffer(blob, len(blob))
         _check(load_library().od_scene_load(self.h, C.cast(buf, _vp), len(blob)), "load")
+
+
+class Batch:
+    """Many scenes stepped together (od_batch_*): each scene advances exactly as
+    Scene.step would, with one set of kernel launches and one mixed-precision
+    solve per Newton iteration for the whole batch.  Scenes need a Newmark
+    integrator with CGSolver(precision="mixed"), the same Newton count and the
+    same preconditioner kind."""
+
+    def __init__(self, ctx: Context, scenes):
+        self.ctx = ctx
+        self.scenes = list(scenes)
+        arr = (_vp * len(self.scenes))(*[sc.h for sc in self.scenes])
+        h = _vp()
+        _check(load_library().od_batch_create(ctx.h, len(self.scenes), arr, C.byref(h)), "od_batch_create")
+        self.h = h
+        _live_batches.add(self)
+
+    def step(self, n: int = 1):
+        """Advance every scene n steps; returns one od_step_stats per scene."""
+        st = (od_step_stats * len(self.scenes))()
+        _check(load_library().od_batch_step(self.h, n, st), "od_batch_step")
+        return list(st)
+
+    def close(self):
+        if getattr(self, "h", None) and not _shutting_down:
+            load_library().od_batch_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Simulator:

@@ -19,7 +19,7 @@ LIB = os.path.join(OUT_DIR, "libodgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]
-SOURCES = ["od_host.cpp", "od_elements.cu", "od_sparse.cu", "od_api.cu", "od_noalloc.cu"]
+SOURCES = ["od_host.cpp", "od_elements.cu", "od_sparse.cu", "od_api.cu", "od_batch.cu", "od_noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -102,12 +102,6 @@ __global__ void nm_correct_kernel(int n, const int* __restrict__ free_pos, doubl
 
 using namespace od;
 
-struct od_ctx {
-  Ctx c;
-};
-struct od_scene {
-  Scene s;
-};
 
 #define OD_CHECK_ARG(cond, msg)              \
   do {                                       \

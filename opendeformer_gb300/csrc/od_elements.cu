@@ -167,15 +167,13 @@ __global__ void traction_kernel(int f0, int f1, const int* __restrict__ fids, co
 // MODE 2 stores them in the colour-ordered staging arrays (all elements in
 // one launch, scattered afterwards colour by colour).
 template <int MODE>
-__global__ void __launch_bounds__(128) corot_kernel(int e0, int e1, int ne, const int4* __restrict__ tets,
-                                                    const double* __restrict__ X, const double* __restrict__ u,
-                                                    const double* __restrict__ pre, double thr,
-                                                    const int* __restrict__ emap, const int* __restrict__ gdof,
-                                                    double* __restrict__ K, double* __restrict__ fint,
-                                                    double* __restrict__ out78, double* __restrict__ out12,
-                                                    const int* __restrict__ perm) {
-  int e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= e1) return;
+__device__ __forceinline__ void corot_elem(int e, int ne, const int4* __restrict__ tets,
+                                           const double* __restrict__ X, const double* __restrict__ u,
+                                           const double* __restrict__ pre, double thr,
+                                           const int* __restrict__ emap, const int* __restrict__ gdof,
+                                           double* __restrict__ K, double* __restrict__ fint,
+                                           double* __restrict__ out78, double* __restrict__ out12,
+                                           const int* __restrict__ perm) {
   int4 t = tets[e];
   const int nd[4] = {t.x, t.y, t.z, t.w};
   V3t<double> o[4], c[4];
@@ -294,15 +292,13 @@ __global__ void __launch_bounds__(128) corot_kernel(int e0, int e1, int ne, cons
 // (tetelement.cpp:282-342); f_a = P dN_a / 6, f_3 = -(f_0 + f_1 + f_2)
 // (tetelement.cpp:344-355).
 template <int MODE>
-__global__ void __launch_bounds__(128) invhyper_kernel(int e0, int e1, int ne, int stvk, const int4* __restrict__ tets,
-                                                       const double* __restrict__ X, const double* __restrict__ u,
-                                                       const double* __restrict__ pre, double thr, double lambda,
-                                                       double mu, const int* __restrict__ emap,
-                                                       const int* __restrict__ gdof, double* __restrict__ K,
-                                                       double* __restrict__ fint, double* __restrict__ out78,
-                                                       double* __restrict__ out12, const int* __restrict__ perm) {
-  int e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= e1) return;
+__device__ __forceinline__ void invhyper_elem(int e, int ne, int stvk, const int4* __restrict__ tets,
+                                              const double* __restrict__ X, const double* __restrict__ u,
+                                              const double* __restrict__ pre, double thr, double lambda, double mu,
+                                              const int* __restrict__ emap, const int* __restrict__ gdof,
+                                              double* __restrict__ K, double* __restrict__ fint,
+                                              double* __restrict__ out78, double* __restrict__ out12,
+                                              const int* __restrict__ perm) {
   int4 t = tets[e];
   const int nd[4] = {t.x, t.y, t.z, t.w};
   V3t<double> c[4];
@@ -465,6 +461,53 @@ __global__ void __launch_bounds__(128) invhyper_kernel(int e0, int e1, int ne, i
   }
 }
 
+template <int MODE>
+__global__ void __launch_bounds__(128) corot_kernel(int e0, int e1, int ne, const int4* __restrict__ tets,
+                                                    const double* __restrict__ X, const double* __restrict__ u,
+                                                    const double* __restrict__ pre, double thr,
+                                                    const int* __restrict__ emap, const int* __restrict__ gdof,
+                                                    double* __restrict__ K, double* __restrict__ fint,
+                                                    double* __restrict__ out78, double* __restrict__ out12,
+                                                    const int* __restrict__ perm) {
+  const int e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < e1) corot_elem<MODE>(e, ne, tets, X, u, pre, thr, emap, gdof, K, fint, out78, out12, perm);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128) invhyper_kernel(int e0, int e1, int ne, int stvk, const int4* __restrict__ tets,
+                                                       const double* __restrict__ X, const double* __restrict__ u,
+                                                       const double* __restrict__ pre, double thr, double lambda,
+                                                       double mu, const int* __restrict__ emap,
+                                                       const int* __restrict__ gdof, double* __restrict__ K,
+                                                       double* __restrict__ fint, double* __restrict__ out78,
+                                                       double* __restrict__ out12, const int* __restrict__ perm) {
+  const int e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < e1)
+    invhyper_elem<MODE>(e, ne, stvk, tets, X, u, pre, thr, lambda, mu, emap, gdof, K, fint, out78, out12, perm);
+}
+
+// ---- several scenes per launch: a tile is an element range of one scene,
+// every scene's values land in its own staging arrays
+__global__ void __launch_bounds__(128) corot_batch_kernel(const Tile* __restrict__ tiles,
+                                                          const SceneDev* __restrict__ sd) {
+  const Tile tl = tiles[blockIdx.x];
+  const int e = tl.begin + threadIdx.x;
+  if (e >= tl.end) return;
+  const SceneDev& D = sd[tl.scene];
+  corot_elem<2>(e, D.n_tets, D.tets, D.X, D.u, D.pre, D.thr, D.emap, D.gdof, nullptr, nullptr, D.stage_k, D.stage_f,
+                nullptr);
+}
+
+__global__ void __launch_bounds__(128) invhyper_batch_kernel(const Tile* __restrict__ tiles,
+                                                             const SceneDev* __restrict__ sd) {
+  const Tile tl = tiles[blockIdx.x];
+  const int e = tl.begin + threadIdx.x;
+  if (e >= tl.end) return;
+  const SceneDev& D = sd[tl.scene];
+  invhyper_elem<2>(e, D.n_tets, D.kind == OD_MATERIAL_STVK, D.tets, D.X, D.u, D.pre, D.thr, D.lambda, D.mu, D.emap,
+                   D.gdof, nullptr, nullptr, D.stage_k, D.stage_f, nullptr);
+}
+
 // atomic-free scatter of staged element values, one colour per launch
 // (corotationalHyperelastic.cpp:100-120): no two elements of a colour share
 // a matrix value or a force entry.  One thread per (element, entry): entries
@@ -484,6 +527,33 @@ __global__ void scatter_kernel(int e0, int cnt, int ne, const double* __restrict
     const int g = gdof[(size_t)(k - 78) * ne + e];
     if (g >= 0) fint[g] += f12[(size_t)(k - 78) * ne + e];
   }
+}
+
+// multi-scene scatter of colour c: a tile is a range [begin, end) of the
+// colour's thread space (90 per element) of one scene, aux = first element
+// of the colour, aux2 = its element count
+__global__ void scatter_batch_kernel(const Tile* __restrict__ tiles, const SceneDev* __restrict__ sd) {
+  const Tile tl = tiles[blockIdx.x];
+  const int t = tl.begin + threadIdx.x;
+  if (t >= tl.end) return;
+  const SceneDev& D = sd[tl.scene];
+  const int cnt = tl.aux2, ne = D.n_tets;
+  const int k = t / cnt;
+  const int e = tl.aux + (t - k * cnt);
+  if (k < 78) {
+    const int idx = D.emap[(size_t)k * ne + e];
+    if (idx >= 0) D.K[idx] += D.stage_k[(size_t)k * ne + e];
+  } else {
+    const int g = D.gdof[(size_t)(k - 78) * ne + e];
+    if (g >= 0) D.fint[g] += D.stage_f[(size_t)(k - 78) * ne + e];
+  }
+}
+
+// zero K values (aux 0) or f_int entries (aux 1) of a tile
+__global__ void zero_batch_kernel(const Tile* __restrict__ tiles, const SceneDev* __restrict__ sd) {
+  const Tile tl = tiles[blockIdx.x];
+  double* p = tl.aux == 0 ? sd[tl.scene].K : sd[tl.scene].fint;
+  for (int i = tl.begin + threadIdx.x; i < tl.end; i += blockDim.x) p[i] = 0.0;
 }
 
 // ---------------------------------------------------------------- launches
@@ -587,6 +657,36 @@ od_status launch_loads(Scene* s, const double* body, int n_facets_total, double 
       traction_kernel<<<nblk(f1 - f0, T), T, 0, st>>>(f0, f1, s->trac_facets, s->trac_vec, traction_scale,
                                                        s->facets_dev, s->X, s->u, s->node_dof, s->fext);
     }
+  }
+  OD_CUDA(cudaGetLastError());
+  return OD_OK;
+}
+
+}  // namespace od
+
+namespace od {
+
+od_status launch_eval_batch(Ctx* ctx, const SceneDev* sd, const Tile* zero_tiles, int n_zero,
+                            const Tile* corot_tiles, int n_corot, const Tile* inv_tiles, int n_inv,
+                            const Tile* scat_tiles, const std::vector<int>& scat_off) {
+  cudaStream_t st = ctx->stream;
+  if (n_zero > 0) {
+    ctx->launches++;
+    zero_batch_kernel<<<n_zero, 256, 0, st>>>(zero_tiles, sd);
+  }
+  if (n_corot > 0) {
+    ctx->launches++;
+    corot_batch_kernel<<<n_corot, 128, 0, st>>>(corot_tiles, sd);
+  }
+  if (n_inv > 0) {
+    ctx->launches++;
+    invhyper_batch_kernel<<<n_inv, 128, 0, st>>>(inv_tiles, sd);
+  }
+  for (size_t c = 0; c + 1 < scat_off.size(); c++) {
+    const int nt = scat_off[c + 1] - scat_off[c];
+    if (nt <= 0) continue;
+    ctx->launches++;
+    scatter_batch_kernel<<<nt, 256, 0, st>>>(scat_tiles + scat_off[c], sd);
   }
   OD_CUDA(cudaGetLastError());
   return OD_OK;

@@ -100,7 +100,26 @@ constexpr int kMaxLocalScenes = 32; // scenes one CTA of the inner FP32 solve ma
 // A contiguous piece of one scene's index space (elements, DOFs, block rows,
 // values ...) handled by one CTA of a multi-scene kernel.
 struct Tile {
-  int scene, begin, end, aux;
+  int scene, begin, end, aux, aux2;
+};
+
+// Device view of one scene for the multi-scene step kernels.
+struct SceneDev {
+  int n_tets, dofs, nb, n_pad, nvals, nnzb, kind;
+  double thr, lambda, mu;
+  const int4* tets;
+  const double* X;
+  double* u;
+  const double* pre;
+  const int* emap;
+  const int* gdof;
+  double *K, *fint, *stage_k, *stage_f;
+  const double *M, *fext;
+  const int *row_ptr, *col, *desc_kind, *desc_off, *gen;
+  double* A64;
+  const int* free_pos;
+  double *d, *v, *a, *dp, *vp, *dv, *rhs, *tmp, *tmp2;
+  double bh2, gh, h, c_ad, c_av, alpha_m, beta_k;  // Newmark constants
 };
 
 // Per-scene input / output of the inner FP32 PCG of a mixed solve.
@@ -297,6 +316,13 @@ od_status launch_mass(Scene* s);
 od_status launch_eval(Scene* s, bool zero_first);       // K, fint at current u
 od_status launch_element_values(Scene* s, double* d_k78, double* d_f12);
 od_status launch_loads(Scene* s, const double* body, int n_facets_total, double traction_scale);
+// multi-scene element evaluation: zero K / f_int (zero tiles: aux 0 values,
+// 1 padded DOFs), compute every element into the scenes' staging arrays,
+// then scatter colour by colour (scatter tiles of colour c at
+// [scat_off[c], scat_off[c+1]))
+od_status launch_eval_batch(Ctx* ctx, const SceneDev* sd, const Tile* zero_tiles, int n_zero,
+                            const Tile* corot_tiles, int n_corot, const Tile* inv_tiles, int n_inv,
+                            const Tile* scat_tiles, const std::vector<int>& scat_off);
 od_status sync_stream(Scene* s);
 
 // ---- kernels (od_sparse.cu) ----
@@ -310,6 +336,11 @@ od_status launch_spmv_lower(Scene* s, const double* v1, double c1, const double*
                             const double* x2, const double* v3, double c3, const double* x3, double* y,
                             bool accumulate);
 od_status launch_spmv_full(Scene* s, const double* x, double* y);
+// multi-scene: Newmark system A64 of every scene (value tiles) and
+// rhs = M tmp + beta_K K tmp2 (block-row tiles of kBatchRows rows)
+constexpr int kBatchRows = 80;
+od_status launch_expand_batch(Ctx* ctx, const SceneDev* sd, const Tile* tiles, int n);
+od_status launch_spmv_lower_batch(Ctx* ctx, const SceneDev* sd, const Tile* tiles, int n);
 // PCG on A64; b and x are device vectors of length n_pad
 od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm, od_solve_stats* st);
 
@@ -325,3 +356,11 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int precond, const std::vector<od_s
                       std::vector<od_solve_stats>& st);
 
 }  // namespace od
+
+// ABI handles (opaque in include/od_gb300.h)
+struct od_ctx {
+  od::Ctx c;
+};
+struct od_scene {
+  od::Scene s;
+};

@@ -111,6 +111,48 @@ __global__ void spmv_lower_kernel(int nb, const int* __restrict__ rp, const int*
   else y[3 * row + r] = acc;
 }
 
+// ---- several scenes per launch (Newmark system of each scene)
+// A = (1 + gamma h alpha_M) M + (gamma h beta_K + beta h^2) K; a tile is a
+// range of one scene's full-BSR values
+__global__ void expand_batch_kernel(const Tile* __restrict__ tiles, const SceneDev* __restrict__ sd) {
+  const Tile tl = tiles[blockIdx.x];
+  const SceneDev& D = sd[tl.scene];
+  const double cK = D.gh * D.beta_k + D.bh2, cM = 1.0 + D.gh * D.alpha_m;
+  for (int idx = tl.begin + threadIdx.x; idx < tl.end; idx += blockDim.x) {
+    const int k = idx / 9, e = idx - 9 * k;
+    const int src = lower_src(D.desc_kind[k], D.desc_off[k], e / 3, e % 3, D.gen);
+    D.A64[idx] = src >= 0 ? cK * D.K[src] + cM * D.M[src] : (src == -2 ? 1.0 : 0.0);
+  }
+}
+
+// rhs = M tmp + beta_K K tmp2 over the block rows [begin, end) of a tile of
+// one scene (three lanes per block row, ten block rows per warp)
+__global__ void spmv_lower_batch_kernel(const Tile* __restrict__ tiles, const SceneDev* __restrict__ sd) {
+  const Tile tl = tiles[blockIdx.x];
+  const SceneDev& D = sd[tl.scene];
+  const int lane = threadIdx.x & 31;
+  if (lane >= 30) return;
+  const int row = tl.begin + (threadIdx.x >> 5) * 10 + lane / 3;
+  const int r = lane % 3;
+  if (row >= tl.end) return;
+  const double c2 = D.beta_k;
+  double acc = 0.0;
+  for (int k = D.row_ptr[row]; k < D.row_ptr[row + 1]; k++) {
+    const int cb = 3 * D.col[k], kd = D.desc_kind[k], of = D.desc_off[k];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const int src = lower_src(kd, of, r, c, D.gen);
+      if (src >= 0) {
+        acc = fma(D.M[src], D.tmp[cb + c], acc);
+        acc = fma(c2 * D.K[src], D.tmp2[cb + c], acc);
+      } else if (src == -2) {
+        acc = fma(1.0, D.tmp[cb + c], acc);
+      }
+    }
+  }
+  D.rhs[3 * row + r] = acc;
+}
+
 // Row-block products of the full BSR.  Three lanes per block row, lane r
 // owning row r of the block row: it walks the row's blocks and does three
 // FMAs per block with the block's row r (three contiguous values) -- exactly
@@ -1437,6 +1479,22 @@ od_status launch_spmv_lower(Scene* s, const double* v1, double c1, const double*
     spmv_lower_kernel<1><<<g, kThreads, 0, s->ctx->stream>>>(nb, s->bsr.row_ptr, s->bsr.col, s->bsr.desc_kind,
                                                               s->bsr.desc_off, s->bsr.gen, v1, c1, x1, nullptr, 0.0,
                                                               nullptr, nullptr, 0.0, nullptr, y, accumulate ? 1 : 0);
+  OD_CUDA(cudaGetLastError());
+  return OD_OK;
+}
+
+od_status launch_expand_batch(Ctx* ctx, const SceneDev* sd, const Tile* tiles, int n) {
+  if (n <= 0) return OD_OK;
+  ctx->launches++;
+  expand_batch_kernel<<<n, kThreads, 0, ctx->stream>>>(tiles, sd);
+  OD_CUDA(cudaGetLastError());
+  return OD_OK;
+}
+
+od_status launch_spmv_lower_batch(Ctx* ctx, const SceneDev* sd, const Tile* tiles, int n) {
+  if (n <= 0) return OD_OK;
+  ctx->launches++;
+  spmv_lower_batch_kernel<<<n, kThreads, 0, ctx->stream>>>(tiles, sd);
   OD_CUDA(cudaGetLastError());
   return OD_OK;
 }
