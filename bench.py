@@ -14,6 +14,14 @@ is one Newmark step.  Synthetic seeded mesh (the reference ships no data).
 Prints one JSON line.  --impl reference times the reference's own CPU code
 (oracle/_ref, compiled from the reference sources) on the same workload;
 the reference has no block-Jacobi, so it runs its Jacobi PCG.
+
+Beside the headline the line carries two more workloads (skipped with
+--no-tiers): "precision_tier", the 2.6M-tet Neo-Hookean block with
+prescribed top displacements solved with the FP64 and with the mixed-precision
+PCG (steps/s of both, the displacement error between them, and the HBM
+roofline of the FP32 SpMV phase measured inside the solve), and
+"batched_tier", 512 uneven scenes stepped one by one with the FP64 solver and
+together through od_batch with the mixed solver.
 """
 from __future__ import annotations
 
@@ -224,6 +232,137 @@ def run_reference(args, wl):
     return 0
 
 
+def _rel(a, b):
+    return float(np.abs(a - b).max() / max(1e-300, np.abs(b).max()))
+
+
+def precision_tier(args, api, ctx):
+    """Mixed-precision large solve: 128x64x64 cubes x 5 tets (2,621,440 tets,
+    longest side 1 m, jitter 0.2 h), invertible Neo-Hookean (mu 3.4e4,
+    lambda 3.1e5), bottom face fixed, a seeded 20% of the top-face nodes
+    prescribed to -0.05 height along z; Newmark dt 1/120 s, Rayleigh
+    0.01 / 0.001, one Newton iteration, block-Jacobi PCG to 1e-10.  The
+    same steps run with the FP64 solver and the mixed one (FP32 sliced SpMV
+    and preconditioner, compensated dots summed in FP64, FP64 refinement)."""
+    g = meshgen.block_2m6()
+    bottom, top = g.face_nodes(2, 0), g.face_nodes(2, 1)
+    rng = np.random.default_rng(4)
+    presc = np.sort(rng.choice(top, size=int(0.2 * top.size), replace=False))
+    cd = meshgen.constrained_dofs_for_nodes(np.concatenate([bottom, presc]))
+    u0 = np.zeros((g.n_nodes, 3))
+    u0[presc, 2] = -0.05 * g.dims[2] * g.h
+    mat = api.InvertibleNeoHookeanMaterial(1000.0, NH_E, NH_NU, 0.1)
+    out, res = {}, {}
+    warm, steps = 2, args.tier_steps
+    for prec in ("fp64", "mixed"):
+        s = api.Scene(ctx, g.X, g.tets, g.facets, cd, mat)
+        s.set_displacements(u0)
+        s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, 0.01, 0.001, 1 / 120,
+                                                 api.CGSolver(1e-10, 20000, api.BlockJacobiPreconditioner(),
+                                                              precision=prec), 1))
+        for _ in range(warm):
+            s.step(1)
+        ctx.reset_counters()
+        ctx.set_profiling(True)
+        ms, it = [], 0
+        for _ in range(steps):
+            st = s.step(1)
+            if st.status != 0:
+                raise RuntimeError(f"precision tier: {prec} step status {st.status}")
+            ms.append(st.device_ms)
+            it += st.pcg_iterations
+        ctx.set_profiling(False)
+        c = ctx.counters()
+        out[prec] = s.displacements()
+        res[prec] = {"steps_per_s": 1000.0 / statistics.mean(ms), "ms_per_step": statistics.mean(ms),
+                     "pcg_iterations_per_step": it / steps, "mix": (c.mix_spmv_bytes, c.mix_spmv_ms,
+                                                                    c.mix_iterations)}
+        s.close()
+        del s
+    peak, peak_kind = peaks()
+    nbytes, sms, nit = res["mixed"].pop("mix")
+    res["fp64"].pop("mix")
+    spmv_gbs = nbytes / (sms * 1e-3) / 1e9 if sms else None
+    return {"workload": "block2m6_nh_prescribed_newmark", "n_tets": g.n_tets, "dofs": 3 * g.n_nodes - len(cd),
+            "newton_iters": 1, "tol": 1e-10, "precond": "block_jacobi", "warmup": warm, "steps": steps,
+            "fp64": res["fp64"], "mixed": res["mixed"],
+            "speedup_mixed_vs_fp64": res["mixed"]["steps_per_s"] / res["fp64"]["steps_per_s"],
+            "rel_err_mixed_vs_fp64": _rel(out["mixed"], out["fp64"]),
+            "spmv_roofline": {"kernel": "pcg32_ring_kernel SpMV + p.q phase (sliced FP32 matrix streamed by "
+                                        "cp.async.bulk, start to end of its grid-wide sum)",
+                              "bound": "hbm", "achieved": spmv_gbs, "peak": peak, "unit": "GB/s",
+                              "frac": spmv_gbs / peak if spmv_gbs else None, "peak_source": peak_kind,
+                              "algorithmic_bytes": nbytes, "phase_ms": sms, "phases": nit,
+                              "bytes_rule": "stored 3x3 blocks x 40 B (9 FP32 values + int32 column) + 24 B per "
+                                            "block row (own p read, q written)"}}
+
+
+def batched_tier(args, api, ctx):
+    """Batched uneven instances: 512 jittered grids (per-axis cube counts
+    log-uniform in [4, 40], 6 tets per cube), corotational / Neo-Hookean
+    with per-instance E and nu, x = 0 fixed, gravity; Newmark dt 1/60 s,
+    Rayleigh 0.01 / 0.001, one Newton iteration, block-Jacobi PCG to 1e-8.
+    Plain FP64 path: every scene stepped alone with the FP64 solver; batched
+    path: one od_batch step for all scenes with the mixed solver."""
+    insts = meshgen.batch_instances(512)
+    scenes = []
+    for inst in insts:
+        g = meshgen.instance_grid(inst)
+        cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+        kind = "corotational" if inst["kind"] == "corotational" else "neohookean"
+        s = api.Scene(ctx, g.X, g.tets, g.facets, cd, api.Material(kind, 1000.0, inst["E"], inst["nu"], 0.1))
+        s.set_loads(body=(0.0, 0.0, -9800.0))
+        scenes.append(s)
+
+    def setup(prec):
+        for s in scenes:
+            s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, 0.01, 0.001, 1 / 60,
+                                                     api.CGSolver(1e-8, 5000, api.BlockJacobiPreconditioner(),
+                                                                  precision=prec), 1))
+    warm, steps = 1, 3
+    setup("fp64")
+    for _ in range(warm):
+        for s in scenes:
+            s.step(1)
+    t0 = time.perf_counter()
+    fp_ms = 0.0
+    for _ in range(steps):
+        for s in scenes:
+            st = s.step(1)
+            fp_ms += st.device_ms
+            if st.status != 0:
+                raise RuntimeError(f"batched tier: FP64 step status {st.status}")
+    fp_wall = (time.perf_counter() - t0) / steps
+    u64 = [s.displacements() for s in scenes]
+    setup("mixed")
+    b = api.Batch(ctx, scenes)
+    for _ in range(warm):
+        b.step(1)
+    lat = []
+    for _ in range(steps):
+        st = b.step(1)
+        if any(x.status != 0 for x in st):
+            raise RuntimeError("batched tier: batch step failed")
+        lat.append(st[0].device_ms)
+    ub = [s.displacements() for s in scenes]
+    err = max(_rel(a, c) for a, c in zip(ub, u64))
+    n_tets = sum(s.n_tets for s in scenes)
+    b.close()
+    for s in scenes:
+        s.close()
+    bms = statistics.mean(lat)
+    lat.sort()
+    return {"workload": "batch512_uneven_newmark", "instances": len(scenes), "n_tets_total": n_tets,
+            "newton_iters": 1, "tol": 1e-8, "precond": "block_jacobi", "warmup": warm, "steps": steps,
+            "fp64_alone": {"batch_steps_per_s": 1.0 / fp_wall, "wall_ms_per_step": 1000.0 * fp_wall,
+                           "device_ms_per_step": fp_ms / steps},
+            "batched_mixed": {"batch_steps_per_s": 1000.0 / bms, "scene_steps_per_s": 1000.0 * len(scenes) / bms,
+                              "ms_per_step": bms, "p50_ms": lat[len(lat) // 2],
+                              "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
+            "speedup_batched_mixed_vs_fp64_alone": fp_wall * 1000.0 / bms,
+            "max_rel_err_vs_fp64": err}
+
+
 def run_gpu(args, wl):
     import torch
     from opendeformer_gb300 import api
@@ -356,6 +495,14 @@ def run_gpu(args, wl):
                              f"single thread, {secs:.1f} s"}
         except Exception as exc:
             cpu = {"value": None, "unit": "steps/s", "cores": 1, "kind": "reference", "sample": f"failed: {exc}"}
+    tiers = {}
+    if rank == 0 and not args.no_tiers:
+        del scene
+        for name, fn in (("precision_tier", precision_tier), ("batched_tier", batched_tier)):
+            try:
+                tiers[name] = fn(args, api, ctx)
+            except Exception as exc:
+                tiers[name] = {"error": str(exc)}
     if rank == 0:
         line = {"metric": "newmark_steps_per_s", "value": value, "unit": "steps/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -371,6 +518,7 @@ def run_gpu(args, wl):
                            "wall_s_timed_region": wall},
                 "e2e": e2e, "gpu_launches": counters.kernel_launches, "clocks": clocks, "roofline": roofline,
                 "cpu_baseline": cpu}
+        line.update(tiers)
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
@@ -388,6 +536,8 @@ def main():
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tiers", action="store_true", help="skip the mixed-precision and batched workloads")
+    ap.add_argument("--tier-steps", type=int, default=5)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

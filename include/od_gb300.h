@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define OD_ABI_VERSION 1
+#define OD_ABI_VERSION 2
 
 typedef enum od_status {
   OD_OK = 0,
@@ -124,6 +124,11 @@ typedef struct od_counters {
   long long pcg_launches;     /* persistent (one-launch) PCG solves timed while profiling */
   long long pcg_iterations;   /* their iterations */
   double pcg_ms;              /* their summed CUDA-event durations */
+  long long mix_iterations;   /* inner FP32 PCG loop iterations of mixed solves (profiling on) */
+  double mix_spmv_ms;         /* their SpMV + p.q phase, start to end of the grid-wide sum */
+  double mix_spmv_bytes;      /* algorithmic bytes of those phases: stored blocks x 40 B
+                                 (FP32 values + column index) + 24 B per block row (own p
+                                 read, q written), for the scenes active in each iteration */
 } od_counters;
 
 typedef struct od_scene_info {

@@ -193,6 +193,9 @@ od_status od_ctx_get_counters(od_ctx* ctx, od_counters* out) {
   out->pcg_launches = ctx->c.pcg_kernel_launches;
   out->pcg_iterations = ctx->c.pcg_kernel_iters;
   out->pcg_ms = ctx->c.pcg_kernel_ms;
+  out->mix_iterations = ctx->c.mix_iters;
+  out->mix_spmv_ms = ctx->c.mix_spmv_ms;
+  out->mix_spmv_bytes = ctx->c.mix_spmv_bytes;
   return OD_OK;
 }
 
@@ -201,6 +204,8 @@ od_status od_ctx_reset_counters(od_ctx* ctx) {
   ctx->c.launches = ctx->c.host_syncs = ctx->c.spmv_launches = 0;
   ctx->c.pcg_kernel_launches = ctx->c.pcg_kernel_iters = 0;
   ctx->c.spmv_ms = ctx->c.pcg_kernel_ms = 0.0;
+  ctx->c.mix_iters = 0;
+  ctx->c.mix_spmv_ms = ctx->c.mix_spmv_bytes = 0.0;
   return OD_OK;
 }
 

@@ -164,6 +164,9 @@ struct MixedSys {
   std::vector<int> sc_slice;       // n_sc+1 first slice of each scene
   std::vector<int> sc_row0;        // n_sc first residual entry of each scene
   std::vector<int> sc_nb;          // n_sc block rows
+  std::vector<double> sc_bytes;    // n_sc algorithmic bytes of one SpMV + p.q phase
+  unsigned long long* prof = nullptr;       // 2: phase time (ns), loop iterations (device)
+  unsigned long long* prof_host = nullptr;  // pinned
   int* perm = nullptr;             // ns*kSliceRows: scene-local block row or -1
   int* slice_sc = nullptr;         // ns: scene of each slice
   int* sc_slice_dev = nullptr;     // n_sc+1: first slice of each scene
@@ -209,6 +212,9 @@ struct Ctx {
   long long pcg_kernel_launches = 0;  // persistent solves timed while profiling
   long long pcg_kernel_iters = 0;
   double pcg_kernel_ms = 0.0;
+  long long mix_iters = 0;            // inner FP32 loop iterations (profiling)
+  double mix_spmv_ms = 0.0;
+  double mix_spmv_bytes = 0.0;
   int profiling = 0;
   std::vector<cudaEvent_t> ev_pool;   // event pairs for SpMV timing
 };

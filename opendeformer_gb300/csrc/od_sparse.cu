@@ -1020,7 +1020,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
     const int* __restrict__ col, const float* __restrict__ val, const double* __restrict__ r64,
     const MixDesc* __restrict__ desc, RingScene* __restrict__ ring, float* __restrict__ d, float* __restrict__ r,
     float* __restrict__ z, float4* __restrict__ p4, float* __restrict__ q, int pkind, const float* __restrict__ pinv,
-    double* __restrict__ part, GridBarrier* gb) {
+    double* __restrict__ part, GridBarrier* gb, unsigned long long* __restrict__ prof) {
   extern __shared__ __align__(128) unsigned char ring_smem[];
   unsigned long long* full = reinterpret_cast<unsigned long long*>(ring_smem + kRingWarps * 2 * kRingStageBytes);
   unsigned long long* empty = full + 2 * kRingWarps;
@@ -1181,8 +1181,13 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
   if (threadIdx.x == 0) sh.pub = 0;
   named_sync<kRingConsumers>();
 
+  // profiling (prof != nullptr): CTA 0 times each SpMV + p.q phase up to the
+  // end of its grid-wide sum, i.e. including the slowest CTA
+  const bool timer = prof && blockIdx.x == 0 && threadIdx.x == 0;
   for (int k = 0; alive; k++) {
     const int kp = k & 1;
+    unsigned long long t_a = 0;
+    if (timer) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_a));
     // ---- q = A p (pieces from the ring), p.q
     {
       zero_ws(1);
@@ -1259,6 +1264,12 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
       if (!ring_sums<1>(sh, L, sc_lo, n_sc, na, part_1, part_g1, gb)) alive = false;
     }
     if (!alive || sh.g == 0.0) break;
+    if (timer) {
+      unsigned long long t_b;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_b));
+      prof[0] += t_b - t_a;
+      prof[1] += 1;
+    }
     // ---- d += alpha p, r -= alpha q, z = M^-1 r, r.z, r.r: kUB slices per
     // batch, all loads of a batch issued before any use
     zero_ws(2);
@@ -1748,6 +1759,8 @@ void mixed_free(MixedSys* m) {
   if (m->ring_host) cudaFreeHost(m->ring_host);
   if (m->rrbb_host) cudaFreeHost(m->rrbb_host);
   if (m->timeout_host) cudaFreeHost(m->timeout_host);
+  cudaFree(m->prof);
+  if (m->prof_host) cudaFreeHost(m->prof_host);
   delete m;
 }
 
@@ -1828,6 +1841,7 @@ od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::ve
     m->sc_slice.push_back(slice0 + hs.ns);
     m->sc_row0.push_back(row0);
     m->sc_nb.push_back(s->bsr.nb);
+    m->sc_bytes.push_back(40.0 * s->bsr.nnzb + 24.0 * s->bsr.nb);
     MixDesc dsc{};
     dsc.row_ptr = s->bsr.row_ptr;
     dsc.col = s->bsr.col;
@@ -1875,6 +1889,8 @@ od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::ve
   if (e == cudaSuccess) e = cudaMalloc(&m->res_part, sizeof(double) * 2 * std::max(1, m->n_res_tiles));
   if (e == cudaSuccess) e = cudaMalloc(&m->gbar, sizeof(GridBarrier));
   if (e == cudaSuccess) e = cudaMallocHost(&m->timeout_host, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&m->prof, 2 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMallocHost(&m->prof_host, 2 * sizeof(unsigned long long));
   if (e != cudaSuccess) return fail(cuda_fail(e, "mixed_build"));
   m->device_bytes += (long long)(sizeof(float) * (nval + nvec) + sizeof(double) * m->n64);
   const int G = ring_kernel_ctas(ctx);
@@ -1968,6 +1984,8 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
     OD_CUDA(cudaMemcpyAsync(m->ring, m->ring_host, sizeof(RingScene) * n_sc, cudaMemcpyHostToDevice, strm));
     OD_CUDA(cudaMemsetAsync(m->gbar, 0, sizeof(GridBarrier), strm));
     GridBarrier* gbp = (GridBarrier*)m->gbar;
+    unsigned long long* profp = prof ? m->prof : nullptr;
+    if (prof) OD_CUDA(cudaMemsetAsync(m->prof, 0, 2 * sizeof(unsigned long long), strm));
     int pkv = pk;
     int nsc = n_sc;
     void* args[] = {(void*)&nsc, (void*)&m->cta_first, (void*)&m->cta_sc_lo, (void*)&m->sc_cta,
@@ -1975,7 +1993,8 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
                     (void*)&m->perm,      (void*)&m->off,       (void*)&m->col,    (void*)&m->val,
                     (void*)&m->r64,       (void*)&m->desc,      (void*)&m->ring,   (void*)&d32,
                     (void*)&r32,          (void*)&z32,          (void*)&p4,        (void*)&q32,
-                    (void*)&pkv,          (void*)&pinv32,       (void*)&m->part,   (void*)&gbp};
+                    (void*)&pkv,          (void*)&pinv32,       (void*)&m->part,   (void*)&gbp,
+                    (void*)&profp};
     if (prof) OD_CUDA(cudaEventRecord(ctx->ev_pool[0], strm));
     ctx->launches++;
     OD_CUDA(cudaLaunchCooperativeKernel((void*)pcg32_ring_kernel, dim3(m->cta_grid), dim3(kRingThreads), args,
@@ -1998,6 +2017,11 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
       OD_CUDA(cudaEventElapsedTime(&ms, ctx->ev_pool[0], ctx->ev_pool[1]));
       ctx->pcg_kernel_ms += ms;
       ctx->pcg_kernel_launches++;
+      OD_CUDA(cudaMemcpy(m->prof_host, m->prof, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+      ctx->mix_spmv_ms += 1e-6 * (double)m->prof_host[0];
+      ctx->mix_iters += (long long)m->prof_host[1];
+      for (int s = 0; s < n_sc; s++)
+        if (need[s]) ctx->mix_spmv_bytes += (double)m->ring_host[s].iters * m->sc_bytes[s];
     }
     for (int s = 0; s < n_sc; s++) {
       if (!need[s]) continue;

@@ -161,3 +161,27 @@ def beam_98k(seed: int = 2) -> TetGrid:
 def block_2m6(seed: int = 4) -> TetGrid:
     """128x64x64 cubes, 5 tets each (2,621,440 tets), longest side 1 m, jitter 0.2h."""
     return tet_grid(128, 64, 64, h=1.0 / 128, jitter=0.20, seed=seed, tets_per_cube=5)
+
+
+def batch_instances(n: int = 512, seed: int = 3):
+    """Uneven batch: n independent jittered grids (0.05 m cubes, 6 tets each,
+    interior jitter 0.1 h) whose cube counts are drawn per axis log-uniformly
+    in [4, 40]; per instance a corotational or invertible Neo-Hookean
+    material (probability 1/2), E log-uniform in [1e4, 1e6] Pa and nu uniform
+    in [0.3, 0.48].  Returns dicts (dims, kind, E, nu, seed); build a mesh
+    with instance_grid."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        dims = tuple(int(v) for v in np.rint(np.exp(rng.uniform(np.log(4.0), np.log(40.0), size=3))))
+        kind = "corotational" if rng.random() < 0.5 else "neohookean"
+        E = float(np.exp(rng.uniform(np.log(1e4), np.log(1e6))))
+        nu = float(rng.uniform(0.3, 0.48))
+        out.append(dict(dims=dims, kind=kind, E=E, nu=nu, seed=seed * 100000 + i))
+    return out
+
+
+def instance_grid(inst) -> TetGrid:
+    nx, ny, nz = inst["dims"]
+    return tet_grid(nx, ny, nz, h=0.05, jitter=0.10, seed=inst["seed"], tets_per_cube=6)
+

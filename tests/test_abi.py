@@ -7,10 +7,11 @@ import subprocess
 from opendeformer_gb300 import api
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "od_gb300.h")
 
 
 def declared():
-    hdr = open(os.path.join(ROOT, "include", "od_gb300.h")).read()
+    hdr = open(HEADER).read()
     return set(re.findall(r"^(?:od_status|const char\*|int)\s+(od_[a-z_0-9]+)\s*\(", hdr, re.M))
 
 
@@ -25,7 +26,9 @@ def test_library_exports_every_declared_symbol():
     assert declared() <= exported
     for name in declared():
         assert getattr(lib, name) is not None
-    assert lib.od_abi_version() == 1
+    with open(HEADER) as f:
+        version = int(re.search(r"#define OD_ABI_VERSION (\d+)", f.read()).group(1))
+    assert lib.od_abi_version() == version
     assert lib.od_status_string(4) == b"OD_ERR_NAN"
 
 
