@@ -226,7 +226,7 @@ static void scene_free(Scene* s) {
                   (void*)s->dv, (void*)s->rhs, (void*)s->tmp, (void*)s->trac_facets, (void*)s->trac_vec,
                   (void*)s->bsr.row_ptr, (void*)s->bsr.col, (void*)s->bsr.desc_off, (void*)s->bsr.desc_kind,
                   (void*)s->bsr.gen, (void*)s->bsr.diag_pos, (void*)s->tmp2, (void*)s->stage_k,
-                  (void*)s->stage_f})
+                  (void*)s->stage_f, (void*)s->color_off_dev})
     if (p) cudaFree(p);
   pcg_free(s);
   if (s->ev_step[0]) { cudaEventDestroy(s->ev_step[0]); cudaEventDestroy(s->ev_step[1]); }
@@ -306,6 +306,7 @@ static od_status scene_build(Scene* s, int n_nodes, const double* X, int n_tets,
   OD_TRY(dupload(s, &s->bsr.desc_kind, hb.desc_kind.data(), hb.desc_kind.size()));
   OD_TRY(dupload(s, &s->bsr.gen, hb.gen.data(), hb.gen.size()));
   OD_TRY(dupload(s, &s->bsr.diag_pos, hb.diag_pos.data(), hb.diag_pos.size()));
+  OD_TRY(dupload(s, &s->color_off_dev, s->color_off.data(), s->color_off.size()));
   s->hbsr_rp = std::move(hb.row_ptr);   // kept for the mixed-precision slice layout
   s->hbsr_col = std::move(hb.col);
   OD_TRY(dalloc(s, &s->A64, 9 * (size_t)s->bsr.nnzb));

@@ -20,12 +20,12 @@ namespace od {
 
 enum NmOp { NM_PREDICT = 0, NM_STAGE, NM_RESIDUAL, NM_ZERO_DV, NM_ADD, NM_CORRECT };
 
-// Newmark vector operations of od_step on a tile of padded DOFs of one scene
-__global__ void nm_batch_kernel(int op, const Tile* __restrict__ tiles, const SceneDev* __restrict__ sd) {
-  const Tile tl = tiles[blockIdx.x];
-  const int i = tl.begin + threadIdx.x;
-  if (i >= tl.end) return;
-  const SceneDev& D = sd[tl.scene];
+// Newmark vector operations of od_step on 256 padded DOFs of one scene
+__global__ void nm_batch_kernel(int op, int n_sc, const int* __restrict__ prefix, const SceneDev* __restrict__ sd) {
+  const int s = dir_scene(prefix, n_sc, blockIdx.x);
+  const SceneDev& D = sd[s];
+  const int i = (blockIdx.x - prefix[s]) * 256 + threadIdx.x;
+  if (i >= D.n_pad) return;
   if (op == NM_ZERO_DV) {
     D.dv[i] = 0.0;
     return;
@@ -63,11 +63,9 @@ struct Batch {
   std::vector<Scene*> sc;
   std::vector<SceneDev> sd_host;
   SceneDev* sd = nullptr;
-  Tile* tiles = nullptr;  // all tile lists in one allocation
-  int n_zero = 0, n_corot = 0, n_inv = 0, n_exp = 0, n_rows = 0, n_dof = 0;
-  Tile *t_zero = nullptr, *t_corot = nullptr, *t_inv = nullptr, *t_scat = nullptr, *t_exp = nullptr,
-       *t_rows = nullptr, *t_dof = nullptr;
-  std::vector<int> scat_off;
+  int* dirs = nullptr;  // all tile-directory prefixes in one allocation
+  TileDir zero_k, zero_f, corot, inv, expand, rows, dof;
+  std::vector<TileDir> scatter;  // per colour
   MixedSys* mix = nullptr;
   int newton = 1, precond = OD_PRECOND_BLOCK_JACOBI;
   std::vector<od_solver_params> prm;
@@ -77,7 +75,7 @@ struct Batch {
 static void batch_free(Batch* b) {
   if (!b) return;
   cudaFree(b->sd);
-  cudaFree(b->tiles);
+  cudaFree(b->dirs);
   mixed_free(b->mix);
   for (cudaEvent_t e : b->ev)
     if (e) cudaEventDestroy(e);
@@ -103,6 +101,7 @@ static SceneDev scene_dev(const Scene* s) {
   D.pre = s->pre;
   D.emap = s->emap;
   D.gdof = s->gdof;
+  D.color_off = s->color_off_dev;
   D.K = s->K;
   D.fint = s->fint;
   D.stage_k = s->stage_k;
@@ -136,54 +135,41 @@ static SceneDev scene_dev(const Scene* s) {
   return D;
 }
 
-static void chunk(std::vector<Tile>& out, int scene, int n, int step, int aux = 0, int aux2 = 0) {
-  for (int b = 0; b < n; b += step) out.push_back(Tile{scene, b, std::min(n, b + step), aux, aux2});
-}
+static int ceil_div(long long n, int d) { return (int)((n + d - 1) / d); }
 
+// the tile directories of every multi-scene kernel: O(scenes) host work
 static od_status batch_build(Batch* B) {
   const int n = (int)B->sc.size();
-  std::vector<Tile> zero, corot, inv, scat, exp, rows, dof;
   int max_colors = 0;
+  for (const Scene* s : B->sc) max_colors = std::max(max_colors, (int)s->color_off.size() - 1);
+  const int n_dirs = 7 + max_colors;
+  std::vector<int> pre((size_t)n_dirs * (n + 1), 0);
+  auto P = [&](int d) { return pre.data() + (size_t)d * (n + 1); };
   for (int i = 0; i < n; i++) {
     const Scene* s = B->sc[i];
     B->sd_host.push_back(scene_dev(s));
-    chunk(zero, i, s->nvals, 4096, 0);
-    chunk(zero, i, s->pcg.n_pad, 4096, 1);
-    chunk(s->mat.kind == OD_MATERIAL_COROTATIONAL ? corot : inv, i, s->n_tets, 128);
-    chunk(exp, i, 9 * s->bsr.nnzb, 2048);
-    chunk(rows, i, s->bsr.nb, kBatchRows);
-    chunk(dof, i, s->pcg.n_pad, 256);
-    max_colors = std::max(max_colors, (int)s->color_off.size() - 1);
-  }
-  B->scat_off.assign(1, 0);
-  for (int c = 0; c < max_colors; c++) {
-    for (int i = 0; i < n; i++) {
-      const Scene* s = B->sc[i];
-      if (c + 1 >= (int)s->color_off.size()) continue;
-      const int e0 = s->color_off[c], cnt = s->color_off[c + 1] - e0;
-      if (cnt <= 0) continue;
-      for (int t = 0; t < 90 * cnt; t += 256) scat.push_back(Tile{i, t, std::min(90 * cnt, t + 256), e0, cnt});
+    const bool corot = s->mat.kind == OD_MATERIAL_COROTATIONAL;
+    const int counts[7] = {ceil_div(s->nvals, kZeroTileValues), ceil_div(s->pcg.n_pad, kZeroTileValues),
+                           corot ? ceil_div(s->n_tets, 128) : 0, corot ? 0 : ceil_div(s->n_tets, 128),
+                           ceil_div(9LL * s->bsr.nnzb, kExpandTile), ceil_div(s->bsr.nb, kBatchRows),
+                           ceil_div(s->pcg.n_pad, 256)};
+    for (int d = 0; d < 7; d++) P(d)[i + 1] = P(d)[i] + counts[d];
+    for (int c = 0; c < max_colors; c++) {
+      const int cnt = c + 1 < (int)s->color_off.size() ? s->color_off[c + 1] - s->color_off[c] : 0;
+      P(7 + c)[i + 1] = P(7 + c)[i] + ceil_div(90LL * cnt, 256);
     }
-    B->scat_off.push_back((int)scat.size());
   }
-  B->n_zero = (int)zero.size();
-  B->n_corot = (int)corot.size();
-  B->n_inv = (int)inv.size();
-  B->n_exp = (int)exp.size();
-  B->n_rows = (int)rows.size();
-  B->n_dof = (int)dof.size();
-  std::vector<Tile> all;
-  for (auto* v : {&zero, &corot, &inv, &scat, &exp, &rows, &dof}) all.insert(all.end(), v->begin(), v->end());
-  OD_CUDA(cudaMalloc(&B->tiles, sizeof(Tile) * std::max<size_t>(1, all.size())));
-  if (!all.empty()) OD_CUDA(cudaMemcpy(B->tiles, all.data(), sizeof(Tile) * all.size(), cudaMemcpyHostToDevice));
-  Tile* p = B->tiles;
-  B->t_zero = p; p += zero.size();
-  B->t_corot = p; p += corot.size();
-  B->t_inv = p; p += inv.size();
-  B->t_scat = p; p += scat.size();
-  B->t_exp = p; p += exp.size();
-  B->t_rows = p; p += rows.size();
-  B->t_dof = p;
+  OD_CUDA(cudaMalloc(&B->dirs, sizeof(int) * pre.size()));
+  OD_CUDA(cudaMemcpy(B->dirs, pre.data(), sizeof(int) * pre.size(), cudaMemcpyHostToDevice));
+  auto dir = [&](int d, int size) { return TileDir{B->dirs + (size_t)d * (n + 1), P(d)[n], size}; };
+  B->zero_k = dir(0, kZeroTileValues);
+  B->zero_f = dir(1, kZeroTileValues);
+  B->corot = dir(2, 128);
+  B->inv = dir(3, 128);
+  B->expand = dir(4, kExpandTile);
+  B->rows = dir(5, kBatchRows);
+  B->dof = dir(6, 256);
+  for (int c = 0; c < max_colors; c++) B->scatter.push_back(dir(7 + c, 256));
   OD_CUDA(cudaMalloc(&B->sd, sizeof(SceneDev) * std::max(1, n)));
   OD_CUDA(cudaMemcpy(B->sd, B->sd_host.data(), sizeof(SceneDev) * n, cudaMemcpyHostToDevice));
   std::vector<const double*> rhs;
@@ -199,9 +185,9 @@ static od_status batch_build(Batch* B) {
 }
 
 static od_status nm_op(Batch* B, int op) {
-  if (B->n_dof <= 0) return OD_OK;
+  if (B->dof.tiles <= 0) return OD_OK;
   B->ctx->launches++;
-  nm_batch_kernel<<<B->n_dof, 256, 0, B->ctx->stream>>>(op, B->t_dof, B->sd);
+  nm_batch_kernel<<<B->dof.tiles, 256, 0, B->ctx->stream>>>(op, (int)B->sc.size(), B->dof.prefix, B->sd);
   OD_CUDA(cudaGetLastError());
   return OD_OK;
 }
@@ -219,11 +205,11 @@ static od_status batch_step(Batch* B, std::vector<od_step_stats>& acc) {
   std::vector<od_solve_stats> ss;
   for (int it = 0; it < B->newton; it++) {
     OD_TRY(nm_op(B, NM_STAGE));
-    OD_TRY(launch_eval_batch(ctx, B->sd, B->t_zero, B->n_zero, B->t_corot, B->n_corot, B->t_inv, B->n_inv,
-                             B->t_scat, B->scat_off));
-    OD_TRY(launch_spmv_lower_batch(ctx, B->sd, B->t_rows, B->n_rows));
+    const int n = (int)B->sc.size();
+    OD_TRY(launch_eval_batch(ctx, n, B->sd, B->zero_k, B->zero_f, B->corot, B->inv, B->scatter));
+    OD_TRY(launch_spmv_lower_batch(ctx, n, B->sd, B->rows));
     OD_TRY(nm_op(B, NM_RESIDUAL));
-    OD_TRY(launch_expand_batch(ctx, B->sd, B->t_exp, B->n_exp));
+    OD_TRY(launch_expand_batch(ctx, n, B->sd, B->expand));
     OD_TRY(nm_op(B, NM_ZERO_DV));
     OD_TRY(mixed_solve(ctx, B->mix, B->precond, B->prm, ss));
     OD_TRY(nm_op(B, NM_ADD));

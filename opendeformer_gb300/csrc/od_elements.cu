@@ -486,24 +486,25 @@ __global__ void __launch_bounds__(128) invhyper_kernel(int e0, int e1, int ne, i
     invhyper_elem<MODE>(e, ne, stvk, tets, X, u, pre, thr, lambda, mu, emap, gdof, K, fint, out78, out12, perm);
 }
 
-// ---- several scenes per launch: a tile is an element range of one scene,
-// every scene's values land in its own staging arrays
-__global__ void __launch_bounds__(128) corot_batch_kernel(const Tile* __restrict__ tiles,
+// ---- several scenes per launch: tile j of scene s (directory prefix) is
+// its elements [128 j, 128 j + 128); every scene's values land in its own
+// staging arrays
+__global__ void __launch_bounds__(128) corot_batch_kernel(int n_sc, const int* __restrict__ prefix,
                                                           const SceneDev* __restrict__ sd) {
-  const Tile tl = tiles[blockIdx.x];
-  const int e = tl.begin + threadIdx.x;
-  if (e >= tl.end) return;
-  const SceneDev& D = sd[tl.scene];
+  const int s = dir_scene(prefix, n_sc, blockIdx.x);
+  const SceneDev& D = sd[s];
+  const int e = (blockIdx.x - prefix[s]) * 128 + threadIdx.x;
+  if (e >= D.n_tets) return;
   corot_elem<2>(e, D.n_tets, D.tets, D.X, D.u, D.pre, D.thr, D.emap, D.gdof, nullptr, nullptr, D.stage_k, D.stage_f,
                 nullptr);
 }
 
-__global__ void __launch_bounds__(128) invhyper_batch_kernel(const Tile* __restrict__ tiles,
+__global__ void __launch_bounds__(128) invhyper_batch_kernel(int n_sc, const int* __restrict__ prefix,
                                                              const SceneDev* __restrict__ sd) {
-  const Tile tl = tiles[blockIdx.x];
-  const int e = tl.begin + threadIdx.x;
-  if (e >= tl.end) return;
-  const SceneDev& D = sd[tl.scene];
+  const int s = dir_scene(prefix, n_sc, blockIdx.x);
+  const SceneDev& D = sd[s];
+  const int e = (blockIdx.x - prefix[s]) * 128 + threadIdx.x;
+  if (e >= D.n_tets) return;
   invhyper_elem<2>(e, D.n_tets, D.kind == OD_MATERIAL_STVK, D.tets, D.X, D.u, D.pre, D.thr, D.lambda, D.mu, D.emap,
                    D.gdof, nullptr, nullptr, D.stage_k, D.stage_f, nullptr);
 }
@@ -529,17 +530,19 @@ __global__ void scatter_kernel(int e0, int cnt, int ne, const double* __restrict
   }
 }
 
-// multi-scene scatter of colour c: a tile is a range [begin, end) of the
-// colour's thread space (90 per element) of one scene, aux = first element
-// of the colour, aux2 = its element count
-__global__ void scatter_batch_kernel(const Tile* __restrict__ tiles, const SceneDev* __restrict__ sd) {
-  const Tile tl = tiles[blockIdx.x];
-  const int t = tl.begin + threadIdx.x;
-  if (t >= tl.end) return;
-  const SceneDev& D = sd[tl.scene];
-  const int cnt = tl.aux2, ne = D.n_tets;
+// multi-scene scatter of colour c: tile j of scene s covers the colour's
+// threads [256 j, 256 j + 256) (90 per element: 78 stiffness values, 12
+// forces)
+__global__ void scatter_batch_kernel(int n_sc, const int* __restrict__ prefix, int c,
+                                     const SceneDev* __restrict__ sd) {
+  const int s = dir_scene(prefix, n_sc, blockIdx.x);
+  const SceneDev& D = sd[s];
+  const int e0 = D.color_off[c], cnt = D.color_off[c + 1] - e0;
+  const int t = (blockIdx.x - prefix[s]) * 256 + threadIdx.x;
+  if (t >= 90 * cnt) return;
+  const int ne = D.n_tets;
   const int k = t / cnt;
-  const int e = tl.aux + (t - k * cnt);
+  const int e = e0 + (t - k * cnt);
   if (k < 78) {
     const int idx = D.emap[(size_t)k * ne + e];
     if (idx >= 0) D.K[idx] += D.stage_k[(size_t)k * ne + e];
@@ -549,11 +552,15 @@ __global__ void scatter_batch_kernel(const Tile* __restrict__ tiles, const Scene
   }
 }
 
-// zero K values (aux 0) or f_int entries (aux 1) of a tile
-__global__ void zero_batch_kernel(const Tile* __restrict__ tiles, const SceneDev* __restrict__ sd) {
-  const Tile tl = tiles[blockIdx.x];
-  double* p = tl.aux == 0 ? sd[tl.scene].K : sd[tl.scene].fint;
-  for (int i = tl.begin + threadIdx.x; i < tl.end; i += blockDim.x) p[i] = 0.0;
+// zero 4096 K values (which 0) or padded f_int entries (which 1) per tile
+__global__ void zero_batch_kernel(int n_sc, const int* __restrict__ prefix, int which,
+                                  const SceneDev* __restrict__ sd) {
+  const int s = dir_scene(prefix, n_sc, blockIdx.x);
+  const SceneDev& D = sd[s];
+  double* p = which == 0 ? D.K : D.fint;
+  const int n = which == 0 ? D.nvals : D.n_pad;
+  const int i0 = (blockIdx.x - prefix[s]) * kZeroTileValues, i1 = min(n, i0 + kZeroTileValues);
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) p[i] = 0.0;
 }
 
 // ---------------------------------------------------------------- launches
@@ -666,27 +673,29 @@ od_status launch_loads(Scene* s, const double* body, int n_facets_total, double 
 
 namespace od {
 
-od_status launch_eval_batch(Ctx* ctx, const SceneDev* sd, const Tile* zero_tiles, int n_zero,
-                            const Tile* corot_tiles, int n_corot, const Tile* inv_tiles, int n_inv,
-                            const Tile* scat_tiles, const std::vector<int>& scat_off) {
+od_status launch_eval_batch(Ctx* ctx, int n_sc, const SceneDev* sd, const TileDir& zero_k, const TileDir& zero_f,
+                            const TileDir& corot, const TileDir& inv, const std::vector<TileDir>& scatter) {
   cudaStream_t st = ctx->stream;
-  if (n_zero > 0) {
+  if (zero_k.tiles > 0) {
     ctx->launches++;
-    zero_batch_kernel<<<n_zero, 256, 0, st>>>(zero_tiles, sd);
+    zero_batch_kernel<<<zero_k.tiles, 256, 0, st>>>(n_sc, zero_k.prefix, 0, sd);
   }
-  if (n_corot > 0) {
+  if (zero_f.tiles > 0) {
     ctx->launches++;
-    corot_batch_kernel<<<n_corot, 128, 0, st>>>(corot_tiles, sd);
+    zero_batch_kernel<<<zero_f.tiles, 256, 0, st>>>(n_sc, zero_f.prefix, 1, sd);
   }
-  if (n_inv > 0) {
+  if (corot.tiles > 0) {
     ctx->launches++;
-    invhyper_batch_kernel<<<n_inv, 128, 0, st>>>(inv_tiles, sd);
+    corot_batch_kernel<<<corot.tiles, 128, 0, st>>>(n_sc, corot.prefix, sd);
   }
-  for (size_t c = 0; c + 1 < scat_off.size(); c++) {
-    const int nt = scat_off[c + 1] - scat_off[c];
-    if (nt <= 0) continue;
+  if (inv.tiles > 0) {
     ctx->launches++;
-    scatter_batch_kernel<<<nt, 256, 0, st>>>(scat_tiles + scat_off[c], sd);
+    invhyper_batch_kernel<<<inv.tiles, 128, 0, st>>>(n_sc, inv.prefix, sd);
+  }
+  for (size_t c = 0; c < scatter.size(); c++) {
+    if (scatter[c].tiles <= 0) continue;
+    ctx->launches++;
+    scatter_batch_kernel<<<scatter[c].tiles, 256, 0, st>>>(n_sc, scatter[c].prefix, (int)c, sd);
   }
   OD_CUDA(cudaGetLastError());
   return OD_OK;

@@ -52,6 +52,9 @@ struct SolveScalars {           // device-resident PCG scalars
   int iter, max_iter, done, status;
 };
 
+struct SliceSys;
+struct MixedSys;
+
 struct Pcg {
   int n_pad = 0;
   int precision = OD_PRECISION_FP64;
@@ -89,18 +92,23 @@ struct Pcg {
   int* timeout_host = nullptr;  // pinned
   int coop_grid = 0;            // co-resident CTAs, 0 if cooperative launch is unavailable
   int disable_persistent = 0;
-  // mixed precision: the scene's own sliced FP32 system (lazily built)
-  struct MixedSys* mix = nullptr;
+  // mixed precision: the scene's sliced FP32 operator and its one-scene
+  // solve (both built on first use)
+  SliceSys* slice = nullptr;
+  MixedSys* mix = nullptr;
 };
 
 constexpr int kSliceRows = 10;      // block rows per slice (3 lanes each, 30 of a warp's 32)
 constexpr int kSliceWindow = 320;   // rows sorted by length inside windows of this many rows
 constexpr int kMaxLocalScenes = 32; // scenes one CTA of the inner FP32 solve may span
 
-// A contiguous piece of one scene's index space (elements, DOFs, block rows,
-// values ...) handled by one CTA of a multi-scene kernel.
-struct Tile {
-  int scene, begin, end, aux, aux2;
+// Tiles of a multi-scene kernel: scene s owns the tiles [prefix[s],
+// prefix[s+1]) of the launch, tile j of the scene covering its indices
+// [j*size, min(n_s, (j+1)*size)); a CTA finds its scene by binary search.
+struct TileDir {
+  const int* prefix = nullptr;  // device, n_sc+1
+  int tiles = 0;                // prefix[n_sc]
+  int size = 0;                 // indices per tile
 };
 
 // Device view of one scene for the multi-scene step kernels.
@@ -113,6 +121,7 @@ struct SceneDev {
   const double* pre;
   const int* emap;
   const int* gdof;
+  const int* color_off;            // colour ranges of the (colour-ordered) elements
   double *K, *fint, *stage_k, *stage_f;
   const double *M, *fext;
   const int *row_ptr, *col, *desc_kind, *desc_off, *gen;
@@ -134,8 +143,30 @@ struct RingScene {
   double rr;          // out: final inner r.r
 };
 
-// Device view of one scene's operator for the mixed solve: the FP64 full BSR,
-// the right-hand side and the solution it refines.
+// A scene's sliced FP32 operator and inner-solve vectors, resident on the
+// device from the scene's first mixed-precision use on.  Block rows in
+// slices of kSliceRows (rows sorted by block count, longest first, within
+// windows of kSliceWindow rows, every slice padded to an even step count);
+// the k-th blocks of a slice's rows sit together, values [step][j][lane]
+// with lane = 3*row_in_slice + r, column indices are slice rows.  Inner
+// vectors are in slice order (element 30*slice + lane).
+struct SliceSys {
+  int ns = 0;                      // slices
+  long long steps = 0;
+  std::vector<int> off_host;       // ns+1
+  double bytes = 0.0;              // algorithmic bytes of one SpMV + p.q phase
+  int* perm = nullptr;             // ns*kSliceRows: block row or -1
+  int* off = nullptr;              // ns+1 first step of each slice
+  int* col = nullptr;              // steps*kSliceRows
+  int* src = nullptr;              // steps*kSliceRows: full-BSR block or -1
+  float* val = nullptr;            // steps*90
+  float* v32 = nullptr;            // p (40/slice), d, r, z, q (30/slice), preconditioner (90/slice)
+  double* r64 = nullptr;           // FP64 residual (n_pad)
+  long long device_bytes = 0;
+};
+
+// Device view of one scene of a mixed solve: the FP64 full BSR, the
+// right-hand side and solution it refines, and its sliced FP32 system.
 struct MixDesc {
   const int* row_ptr;
   const int* col;
@@ -144,51 +175,41 @@ struct MixDesc {
   const double* b;
   double* x;
   int nb;
-  int row0;           // first entry of the scene in the concatenated FP64 residual
-  int tile0, ntiles;  // residual tiles of the scene
+  int ns;                          // slices
+  int steps;                       // steps of the sliced matrix
+  int slice0;                      // first slice of the scene in the system's slice order
+  const int* sperm;
+  const int* soff;
+  const int* scol;
+  const int* ssrc;
+  float* sval;
+  float* v32;
+  double* r64;
 };
 
-// Sliced FP32 system of one or more scenes (block diagonal): each scene's
-// block rows in slices of kSliceRows (rows sorted by block count, longest
-// first, within windows of kSliceWindow rows, every slice padded to an even
-// step count); the k-th blocks of a slice's rows sit together, values
-// [step][j][lane] with lane = 3*row_in_slice + r.  Inner vectors are in slice
-// order (element 30*slice + lane); column indices are slice rows of the
-// concatenation.
+// A mixed-precision solve over one or more scenes (block diagonal): the
+// scenes' slices in a virtual concatenation cut into contiguous CTA ranges;
+// every scene keeps its own arrays (SliceSys), so building a system is
+// O(scenes).
 struct MixedSys {
   int n_sc = 0;                    // scenes
-  int ns = 0;                      // slices
-  long long steps = 0;
-  int n64 = 0;                     // entries of the concatenated FP64 residual
-  std::vector<int> off_host;       // ns+1
+  int ns = 0;                      // slices of all scenes
+  std::vector<int> off_host;       // ns+1 step offsets of the concatenation (partition)
   std::vector<int> sc_slice;       // n_sc+1 first slice of each scene
-  std::vector<int> sc_row0;        // n_sc first residual entry of each scene
   std::vector<int> sc_nb;          // n_sc block rows
   std::vector<double> sc_bytes;    // n_sc algorithmic bytes of one SpMV + p.q phase
   unsigned long long* prof = nullptr;       // 2: phase time (ns), loop iterations (device)
   unsigned long long* prof_host = nullptr;  // pinned
-  int* perm = nullptr;             // ns*kSliceRows: scene-local block row or -1
-  int* slice_sc = nullptr;         // ns: scene of each slice
-  int* sc_slice_dev = nullptr;     // n_sc+1: first slice of each scene
-  int* off = nullptr;              // ns+1
-  int* col = nullptr;              // steps*kSliceRows
-  int* src = nullptr;              // steps*kSliceRows: scene-local full-BSR block or -1
-  float* val = nullptr;            // steps*90
-  float* v32 = nullptr;            // p (40/slice), d, r, z, q (30/slice), preconditioner (90/slice)
-  double* r64 = nullptr;           // n64
-  // per scene
+  int* sc_slice_dev = nullptr;     // n_sc+1
   MixDesc* desc = nullptr;         // n_sc (device)
   std::vector<MixDesc> desc_host;
   RingScene* ring = nullptr;       // n_sc (device)
   RingScene* ring_host = nullptr;  // n_sc (pinned)
   double* rrbb = nullptr;          // 2*n_sc: residual r.r, b.b (device)
   double* rrbb_host = nullptr;     // pinned
-  // tiles
-  Tile* res_tiles = nullptr;       // residual tiles (block rows)
-  int n_res_tiles = 0;
+  int* dirs = nullptr;             // tile prefixes (device): residual, fill, precond, update
+  TileDir res_dir, fill_dir, pre_dir, upd_dir;
   double* res_part = nullptr;      // 2 per residual tile
-  Tile* fill_tiles = nullptr;      // value tiles of the FP32 fill
-  int n_fill_tiles = 0;
   // CTA partition of the ring kernel
   int cta_grid = 0;
   int* cta_first = nullptr;        // G+1 first slice of each CTA
@@ -197,7 +218,6 @@ struct MixedSys {
   double* part = nullptr;          // [3][n_sc][G] per-scene CTA partials + 2 G
   void* gbar = nullptr;
   int* timeout_host = nullptr;     // pinned
-  long long device_bytes = 0;
 };
 
 struct Ctx {
@@ -233,6 +253,7 @@ struct Scene {
   std::vector<int> hbsr_rp, hbsr_col;   // full BSR row pointers / block columns
   int nbc = 0, nrem = 0, nvals = 0;
   std::vector<int> color_off;      // element colour ranges (colour order)
+  int* color_off_dev = nullptr;    // the same on the device
   std::vector<int> elem_perm;      // colour-order position -> original element
   // device
   double* X = nullptr;
@@ -322,13 +343,12 @@ od_status launch_mass(Scene* s);
 od_status launch_eval(Scene* s, bool zero_first);       // K, fint at current u
 od_status launch_element_values(Scene* s, double* d_k78, double* d_f12);
 od_status launch_loads(Scene* s, const double* body, int n_facets_total, double traction_scale);
-// multi-scene element evaluation: zero K / f_int (zero tiles: aux 0 values,
-// 1 padded DOFs), compute every element into the scenes' staging arrays,
-// then scatter colour by colour (scatter tiles of colour c at
-// [scat_off[c], scat_off[c+1]))
-od_status launch_eval_batch(Ctx* ctx, const SceneDev* sd, const Tile* zero_tiles, int n_zero,
-                            const Tile* corot_tiles, int n_corot, const Tile* inv_tiles, int n_inv,
-                            const Tile* scat_tiles, const std::vector<int>& scat_off);
+// multi-scene element evaluation: zero K (values) and f_int (padded DOFs),
+// compute every element into the scenes' staging arrays (one launch per
+// material family), then scatter colour by colour (tiles over 90 threads
+// per element of the colour)
+od_status launch_eval_batch(Ctx* ctx, int n_sc, const SceneDev* sd, const TileDir& zero_k, const TileDir& zero_f,
+                            const TileDir& corot, const TileDir& inv, const std::vector<TileDir>& scatter);
 od_status sync_stream(Scene* s);
 
 // ---- kernels (od_sparse.cu) ----
@@ -345,14 +365,32 @@ od_status launch_spmv_full(Scene* s, const double* x, double* y);
 // multi-scene: Newmark system A64 of every scene (value tiles) and
 // rhs = M tmp + beta_K K tmp2 (block-row tiles of kBatchRows rows)
 constexpr int kBatchRows = 80;
-od_status launch_expand_batch(Ctx* ctx, const SceneDev* sd, const Tile* tiles, int n);
-od_status launch_spmv_lower_batch(Ctx* ctx, const SceneDev* sd, const Tile* tiles, int n);
+constexpr int kExpandTile = 2048;   // full-BSR values per tile of the multi-scene system combination
+constexpr int kZeroTileValues = 4096;  // values per tile of the multi-scene zeroing
+od_status launch_expand_batch(Ctx* ctx, int n_sc, const SceneDev* sd, const TileDir& dir);
+od_status launch_spmv_lower_batch(Ctx* ctx, int n_sc, const SceneDev* sd, const TileDir& dir);
+
+#ifdef __CUDACC__
+// scene of tile t of a directory over n scenes (largest s with prefix[s] <= t)
+__device__ __forceinline__ int dir_scene(const int* __restrict__ prefix, int n, int t) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= t) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+#endif
 // PCG on A64; b and x are device vectors of length n_pad
 od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm, od_solve_stats* st);
 
 // ---- mixed-precision systems (od_sparse.cu)
-// builds the sliced FP32 system of scenes (their full-BSR patterns) with the
-// given right-hand sides / solutions (nullptr: supplied per solve)
+// the scene's sliced FP32 operator (built once, kept with the scene)
+od_status slice_build(Scene* s);
+void slice_free(SliceSys* sl);
+// a solve over scenes (their slices built on demand) with the given
+// right-hand sides / solutions (nullptr: supplied per solve)
 od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::vector<const double*>& b,
                       const std::vector<double*>& x, MixedSys** out);
 void mixed_free(MixedSys* m);

@@ -112,29 +112,30 @@ __global__ void spmv_lower_kernel(int nb, const int* __restrict__ rp, const int*
 }
 
 // ---- several scenes per launch (Newmark system of each scene)
-// A = (1 + gamma h alpha_M) M + (gamma h beta_K + beta h^2) K; a tile is a
-// range of one scene's full-BSR values
-__global__ void expand_batch_kernel(const Tile* __restrict__ tiles, const SceneDev* __restrict__ sd) {
-  const Tile tl = tiles[blockIdx.x];
-  const SceneDev& D = sd[tl.scene];
+// A = (1 + gamma h alpha_M) M + (gamma h beta_K + beta h^2) K; a tile is
+// kExpandTile of one scene's full-BSR values
+__global__ void expand_batch_kernel(int n_sc, const int* __restrict__ prefix, const SceneDev* __restrict__ sd) {
+  const int s = dir_scene(prefix, n_sc, blockIdx.x);
+  const SceneDev& D = sd[s];
   const double cK = D.gh * D.beta_k + D.bh2, cM = 1.0 + D.gh * D.alpha_m;
-  for (int idx = tl.begin + threadIdx.x; idx < tl.end; idx += blockDim.x) {
+  const int v0 = (blockIdx.x - prefix[s]) * kExpandTile, v1 = min(9 * D.nnzb, v0 + kExpandTile);
+  for (int idx = v0 + threadIdx.x; idx < v1; idx += blockDim.x) {
     const int k = idx / 9, e = idx - 9 * k;
     const int src = lower_src(D.desc_kind[k], D.desc_off[k], e / 3, e % 3, D.gen);
     D.A64[idx] = src >= 0 ? cK * D.K[src] + cM * D.M[src] : (src == -2 ? 1.0 : 0.0);
   }
 }
 
-// rhs = M tmp + beta_K K tmp2 over the block rows [begin, end) of a tile of
-// one scene (three lanes per block row, ten block rows per warp)
-__global__ void spmv_lower_batch_kernel(const Tile* __restrict__ tiles, const SceneDev* __restrict__ sd) {
-  const Tile tl = tiles[blockIdx.x];
-  const SceneDev& D = sd[tl.scene];
+// rhs = M tmp + beta_K K tmp2 over kBatchRows block rows of one scene
+// (three lanes per block row, ten block rows per warp)
+__global__ void spmv_lower_batch_kernel(int n_sc, const int* __restrict__ prefix, const SceneDev* __restrict__ sd) {
+  const int s = dir_scene(prefix, n_sc, blockIdx.x);
+  const SceneDev& D = sd[s];
   const int lane = threadIdx.x & 31;
   if (lane >= 30) return;
-  const int row = tl.begin + (threadIdx.x >> 5) * 10 + lane / 3;
+  const int row = (blockIdx.x - prefix[s]) * kBatchRows + (threadIdx.x >> 5) * 10 + lane / 3;
   const int r = lane % 3;
-  if (row >= tl.end) return;
+  if (row >= D.nb) return;
   const double c2 = D.beta_k;
   double acc = 0.0;
   for (int k = D.row_ptr[row]; k < D.row_ptr[row + 1]; k++) {
@@ -741,36 +742,43 @@ __device__ __forceinline__ void comp_add_prod(Comp& a, float x, float y) {
 }
 __device__ __forceinline__ double comp_value(const Comp& a) { return (double)a.s + (double)a.c; }
 
-// ---- sliced FP32 systems of one or more scenes (layout: MixedSys)
+// ---- sliced FP32 systems of one or more scenes (layout: SliceSys)
+// Per-scene arrays are reached through MixDesc; every kernel below is one
+// launch for all scenes of a system, a CTA finding its scene in a tile
+// directory.
+constexpr int kFillSteps = 32;                              // steps per fill tile
+constexpr int kResRows = (kThreads / 32) * kRowsPerWarp;    // block rows per residual tile
 
-// values of the sliced matrix from each scene's FP64 full BSR; a tile is a
-// step range [begin, end) of one scene
-__global__ void mix_fill_kernel(const Tile* __restrict__ tiles, const MixDesc* __restrict__ desc,
-                                const int* __restrict__ src, float* __restrict__ val) {
-  const Tile tl = tiles[blockIdx.x];
-  const double* __restrict__ A = desc[tl.scene].A64;
-  const int nv = (tl.end - tl.begin) * 90;
+__device__ __forceinline__ float* mix_pinv(const MixDesc& D) { return D.v32 + 160 * (size_t)D.ns; }
+__device__ __forceinline__ float* mix_d(const MixDesc& D) { return D.v32 + 40 * (size_t)D.ns; }
+
+// values of each scene's sliced matrix from its FP64 full BSR
+__global__ void mix_fill_kernel(int n_sc, const int* __restrict__ prefix, const MixDesc* __restrict__ desc) {
+  const int s = dir_scene(prefix, n_sc, blockIdx.x);
+  const MixDesc& D = desc[s];
+  const int st0 = (blockIdx.x - prefix[s]) * kFillSteps;
+  const int nv = (min(D.steps, st0 + kFillSteps) - st0) * 90;
+  const double* __restrict__ A = D.A64;
   for (int q = threadIdx.x; q < nv; q += blockDim.x) {
-    const int st = tl.begin + q / 90, rem = q % 90;
+    const int st = st0 + q / 90, rem = q % 90;
     const int j = rem / 30, lane = rem - 30 * j;
-    const int blk = src[(size_t)st * kSliceRows + lane / 3];
-    val[(size_t)st * 90 + rem] = blk >= 0 ? (float)A[(size_t)blk * 9 + 3 * (lane % 3) + j] : 0.f;
+    const int blk = D.ssrc[(size_t)st * kSliceRows + lane / 3];
+    D.sval[(size_t)st * 90 + rem] = blk >= 0 ? (float)A[(size_t)blk * 9 + 3 * (lane % 3) + j] : 0.f;
   }
 }
 
 // FP32 Jacobi (30 per slice) or block-Jacobi (90 per slice, [j][lane]) from
 // the FP64 diagonal blocks, in slice order; padding rows get zeros
-__global__ void mix_precond_kernel(int nrs, int kind, const int* __restrict__ perm, const int* __restrict__ slice_sc,
-                                   const MixDesc* __restrict__ desc, float* __restrict__ pinv) {
-  const int rs = blockIdx.x * blockDim.x + threadIdx.x;
-  if (rs >= nrs) return;
+__global__ void mix_precond_kernel(int n_sc, const int* __restrict__ prefix, int kind,
+                                   const MixDesc* __restrict__ desc) {
+  const int s = dir_scene(prefix, n_sc, blockIdx.x);
+  const MixDesc& D = desc[s];
+  const int rs = (blockIdx.x - prefix[s]) * blockDim.x + threadIdx.x;
+  if (rs >= D.ns * kSliceRows) return;
   const int sl = rs / kSliceRows, t = rs - sl * kSliceRows;
-  const int row = perm[rs];
-  const double* m = nullptr;
-  if (row >= 0) {
-    const MixDesc& D = desc[slice_sc[sl]];
-    m = D.A64 + (size_t)D.diag_pos[row] * 9;
-  }
+  const int row = D.sperm[rs];
+  const double* m = row >= 0 ? D.A64 + (size_t)D.diag_pos[row] * 9 : nullptr;
+  float* pinv = mix_pinv(D);
   if (kind == OD_PRECOND_JACOBI) {
     for (int d = 0; d < 3; d++) {
       float v = 0.f;
@@ -798,22 +806,21 @@ __global__ void mix_precond_kernel(int nrs, int kind, const int* __restrict__ pe
     for (int j = 0; j < 3; j++) pinv[(size_t)90 * sl + 30 * j + 3 * t + r] = (float)o[3 * r + j];
 }
 
-// r64 = b - A64 x (FP64) for the block rows [begin, end) of a tile (three
-// lanes per block row, ten block rows per warp) and the tile's partials of
-// r.r and b.b
-constexpr int kResRows = (kThreads / 32) * kRowsPerWarp;
-__global__ void mix_residual_kernel(const Tile* __restrict__ tiles, const MixDesc* __restrict__ desc,
-                                    double* __restrict__ r64, double* __restrict__ part) {
-  const Tile tl = tiles[blockIdx.x];
-  const MixDesc& D = desc[tl.scene];
+// r64 = b - A64 x (FP64) over kResRows block rows of a scene (three lanes per
+// block row, ten block rows per warp) and the tile's partials of r.r, b.b
+__global__ void mix_residual_kernel(int n_sc, const int* __restrict__ prefix, const MixDesc* __restrict__ desc,
+                                    double* __restrict__ part) {
+  const int s = dir_scene(prefix, n_sc, blockIdx.x);
+  const MixDesc& D = desc[s];
   const int lane = threadIdx.x & 31;
-  const int row = tl.begin + (threadIdx.x >> 5) * kRowsPerWarp + lane / 3, rs = lane % 3;
+  const int row = (blockIdx.x - prefix[s]) * kResRows + (threadIdx.x >> 5) * kRowsPerWarp + lane / 3;
+  const int rs = lane % 3;
   double rr = 0.0, bb = 0.0;
-  if (lane < 30 && row < tl.end) {
+  if (lane < 30 && row < D.nb) {
     const int i = 3 * row + rs;
     const double bv = D.b[i];
     const double rv = bv - bsr_subrow<double, double>(row, rs, D.row_ptr, D.col, D.A64, D.x);
-    r64[D.row0 + i] = rv;
+    D.r64[i] = rv;
     rr = rv * rv;
     bb = bv * bv;
   }
@@ -825,16 +832,15 @@ __global__ void mix_residual_kernel(const Tile* __restrict__ tiles, const MixDes
 }
 
 // per scene: r.r and b.b over the scene's residual tiles in a fixed order
-__global__ void mix_residual_finish(int n_sc, const MixDesc* __restrict__ desc, const double* __restrict__ part,
+__global__ void mix_residual_finish(int n_sc, const int* __restrict__ prefix, const double* __restrict__ part,
                                     double* __restrict__ rrbb) {
   const int s = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (s >= n_sc) return;
-  const int t0 = desc[s].tile0, nt = desc[s].ntiles;
   double a = 0.0, b = 0.0;
-  for (int k = lane; k < nt; k += 32) {
-    a += part[2 * (t0 + k)];
-    b += part[2 * (t0 + k) + 1];
+  for (int k = prefix[s] + lane; k < prefix[s + 1]; k += 32) {
+    a += part[2 * k];
+    b += part[2 * k + 1];
   }
   a = warp_sum(a);
   b = warp_sum(b);
@@ -845,18 +851,18 @@ __global__ void mix_residual_finish(int n_sc, const MixDesc* __restrict__ desc, 
 }
 
 // x += ||r64|| d for the scenes of the sweep (slice order back to block rows)
-__global__ void mix_update_kernel(int nrs, const int* __restrict__ perm, const int* __restrict__ slice_sc,
-                                  const MixDesc* __restrict__ desc, const RingScene* __restrict__ ring,
-                                  const float* __restrict__ d) {
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= 3 * nrs) return;
+__global__ void mix_update_kernel(int n_sc, const int* __restrict__ prefix, const MixDesc* __restrict__ desc,
+                                  const RingScene* __restrict__ ring) {
+  const int s = dir_scene(prefix, n_sc, blockIdx.x);
+  if (!ring[s].active0) return;
+  const MixDesc& D = desc[s];
+  const int tid = (blockIdx.x - prefix[s]) * blockDim.x + threadIdx.x;
+  if (tid >= 3 * kSliceRows * D.ns) return;
   const int rs = tid / 3, c = tid - 3 * rs;
-  const int row = perm[rs];
+  const int row = D.sperm[rs];
   if (row < 0) return;
   const int sl = rs / kSliceRows, t = rs - sl * kSliceRows;
-  const int s = slice_sc[sl];
-  if (!ring[s].active0) return;
-  desc[s].x[3 * (size_t)row + c] += ring[s].unscale * (double)d[(size_t)30 * sl + 3 * t + c];
+  D.x[3 * (size_t)row + c] += ring[s].unscale * (double)mix_d(D)[(size_t)30 * sl + 3 * t + c];
 }
 
 // ---- bulk-copy ring of the inner FP32 PCG
@@ -927,7 +933,8 @@ struct RingShared {
   double g;                                   // grid-wide sum of the last reduction
   double rz[kMaxLocalScenes], rr[kMaxLocalScenes], eps[kMaxLocalScenes];
   double scale[kMaxLocalScenes];
-  int row0[kMaxLocalScenes], it[kMaxLocalScenes], status[kMaxLocalScenes], maxit[kMaxLocalScenes];
+  int it[kMaxLocalScenes], status[kMaxLocalScenes], maxit[kMaxLocalScenes];
+  MixDesc lp[kMaxLocalScenes];                // the local scenes' arrays
   int c0[kMaxLocalScenes], c1[kMaxLocalScenes];  // CTA range of each local scene
   int lfirst[kMaxLocalScenes + 1];                // first slice of each local scene in the CTA range
   volatile unsigned char act[2][kMaxLocalScenes];  // activity by iteration parity
@@ -1009,17 +1016,15 @@ __device__ __forceinline__ bool grid_barrier_named(GridBarrier* gb) {
 // Inner FP32 PCG of every scene of a sliced system, one cooperative launch
 // of kRingThreads per CTA: scene s solves A32 d = rhs_scale * r64 from d = 0
 // until ||r_inner|| <= inner_tol ||r_0|| or max_iter, each scene with its own
-// step lengths; the loop runs while any scene is active.  Lane l < 30 of a
-// consumer warp owns slice element 30*slice + l, i.e. component l%3 of slice
-// row l/3 (lanes 30, 31 shadow lane 29 and store nothing).  Dot products
-// accumulate in compensated FP32 per lane and are summed in FP64.
+// step lengths; the loop runs while any scene is active.  Slices are
+// numbered through the scenes (scene s owns [slice0, slice0 + ns)); every
+// scene's arrays are its own (MixDesc).  Lane l < 30 of a consumer warp owns
+// slice element 30*slice + l, i.e. component l%3 of slice row l/3 (lanes
+// 30, 31 shadow lane 29 and store nothing).  Dot products accumulate in
+// compensated FP32 per lane and are summed in FP64.
 __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
     int n_sc, const int* __restrict__ cta_first, const int* __restrict__ cta_sc_lo, const int* __restrict__ sc_cta,
-    const int* __restrict__ sc_slice, const int* __restrict__ slice_sc, const int* __restrict__ perm,
-    const int* __restrict__ off,
-    const int* __restrict__ col, const float* __restrict__ val, const double* __restrict__ r64,
-    const MixDesc* __restrict__ desc, RingScene* __restrict__ ring, float* __restrict__ d, float* __restrict__ r,
-    float* __restrict__ z, float4* __restrict__ p4, float* __restrict__ q, int pkind, const float* __restrict__ pinv,
+    const int* __restrict__ sc_slice, const MixDesc* __restrict__ desc, RingScene* __restrict__ ring, int pkind,
     double* __restrict__ part, GridBarrier* gb, unsigned long long* __restrict__ prof) {
   extern __shared__ __align__(128) unsigned char ring_smem[];
   unsigned long long* full = reinterpret_cast<unsigned long long*>(ring_smem + kRingWarps * 2 * kRingStageBytes);
@@ -1030,7 +1035,17 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
   const int w = threadIdx.x >> 5;
   const int sfirst = cta_first[blockIdx.x], send = cta_first[blockIdx.x + 1];
   const int sc_lo = cta_sc_lo[blockIdx.x];
-  const int L = send > sfirst ? slice_sc[send - 1] - sc_lo + 1 : 0;
+  int L = 0;
+  if (send > sfirst) {
+    int hi = n_sc;  // scene of slice send - 1: largest s with sc_slice[s] <= send - 1
+    int lo = sc_lo;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (sc_slice[mid] <= send - 1) lo = mid;
+      else hi = mid;
+    }
+    L = lo - sc_lo + 1;
+  }
   if (threadIdx.x == 0) {
     sh.stop = 0;
     sh.pub = -1;
@@ -1045,7 +1060,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
     sh.eps[threadIdx.x] = ring[s].itol2;  // relative until the first reduction
     sh.maxit[threadIdx.x] = ring[s].max_iter;
     sh.act[0][threadIdx.x] = (unsigned char)(ring[s].active0 != 0);
-    sh.row0[threadIdx.x] = desc[s].row0;
+    sh.lp[threadIdx.x] = desc[s];
     sh.c0[threadIdx.x] = sc_cta[2 * s];
     sh.c1[threadIdx.x] = sc_cta[2 * s + 1];
     sh.lfirst[threadIdx.x] = threadIdx.x == 0 ? sfirst : sc_slice[s];
@@ -1073,8 +1088,10 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
           __threadfence_block();
           copy = sh.act[kit & 1][ls] != 0;
         }
-        const int k1 = off[sl + 1];
-        for (int k = off[sl]; k < k1; k += kRingSteps) {
+        const MixDesc& P = sh.lp[ls];
+        const int lsl = sl - P.slice0;
+        const int k1 = P.soff[lsl + 1];
+        for (int k = P.soff[lsl]; k < k1; k += kRingSteps) {
           const int n = min(kRingSteps, k1 - k);
           const int j = pc & 1;
           const unsigned par = ((pc >> 1) & 1) ^ 1;
@@ -1087,8 +1104,8 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
           if (copy) {
             unsigned char* st = ring_smem + (size_t)(2 * pw + j) * kRingStageBytes;
             mbar_expect_tx(full + 2 * pw + j, (unsigned)n * 400u);
-            bulk_g2s(st, val + (size_t)k * 90, (unsigned)n * 360u, full + 2 * pw + j, policy);
-            bulk_g2s(st + kRingSteps * 360, col + (size_t)k * kSliceRows, (unsigned)n * 40u, full + 2 * pw + j,
+            bulk_g2s(st, P.sval + (size_t)k * 90, (unsigned)n * 360u, full + 2 * pw + j, policy);
+            bulk_g2s(st + kRingSteps * 360, P.scol + (size_t)k * kSliceRows, (unsigned)n * 40u, full + 2 * pw + j,
                      policy);
           } else {
             mbar_arrive(full + 2 * pw + j);
@@ -1114,7 +1131,6 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
   const bool act_l = lane < 30;
   const int ln = act_l ? lane : 29;
   const int t = ln / 3, rsub = ln - 3 * t, lbase = 3 * t;
-  float* pf = reinterpret_cast<float*>(p4);
   unsigned pc = 0;  // pieces consumed
   bool alive = true;
 
@@ -1132,33 +1148,56 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
     const double tv = warp_sum(comp_value(c));
     if (lane == 0) sh.ws[j][ls][w] = tv;
   };
+  // the scene's vectors, indexed by the scene-local slice
+  struct Vecs {
+    float4* p4;
+    float *pf, *d, *r, *z, *q, *pinv;
+    int s0;
+  };
+  auto vecs = [&](int ls) {
+    const MixDesc& P = sh.lp[ls];
+    Vecs v;
+    const size_t ns = (size_t)P.ns;
+    v.p4 = reinterpret_cast<float4*>(P.v32);
+    v.pf = P.v32;
+    v.d = P.v32 + 40 * ns;
+    v.r = v.d + 30 * ns;
+    v.z = v.r + 30 * ns;
+    v.q = v.z + 30 * ns;
+    v.pinv = v.q + 30 * ns;
+    v.s0 = P.slice0;
+    return v;
+  };
 
   // init: d = 0, r = rhs, z = M^-1 r, p = z (scenes outside the sweep: zeros)
   zero_ws(2);
   for (int ls = 0; ls < L; ls++) {
     const bool a0 = sh.act[0][ls] != 0;
     const double scale = sh.scale[ls];
-    const size_t row0 = (size_t)sh.row0[ls];
+    const Vecs V = vecs(ls);
+    const int* __restrict__ perm = sh.lp[ls].sperm;
+    const double* __restrict__ r64 = sh.lp[ls].r64;
     Comp crz{0.f, 0.f}, crr{0.f, 0.f};
     for (int sl = first_slice(ls); sl < sh.lfirst[ls + 1]; sl += kRingWarps) {
-      const int rs = sl * kSliceRows + t;
+      const int lsl = sl - V.s0;
+      const int rs = lsl * kSliceRows + t;
       const int row = perm[rs];
-      const float rl = (a0 && row >= 0) ? (float)(r64[row0 + 3 * (size_t)row + rsub] * scale) : 0.f;
+      const float rl = (a0 && row >= 0) ? (float)(r64[3 * (size_t)row + rsub] * scale) : 0.f;
       const float r0 = __shfl_sync(0xffffffffu, rl, lbase);
       const float r1 = __shfl_sync(0xffffffffu, rl, lbase + 1);
       const float r2 = __shfl_sync(0xffffffffu, rl, lbase + 2);
       float zl = rl;
-      if (pkind == OD_PRECOND_JACOBI) zl = pinv[(size_t)30 * sl + ln] * rl;
+      if (pkind == OD_PRECOND_JACOBI) zl = V.pinv[(size_t)30 * lsl + ln] * rl;
       else if (pkind == OD_PRECOND_BLOCK_JACOBI) {
-        const float* m = pinv + (size_t)90 * sl + ln;
+        const float* m = V.pinv + (size_t)90 * lsl + ln;
         zl = fmaf(m[0], r0, fmaf(m[30], r1, m[60] * r2));
       }
       if (act_l) {
-        const size_t i = (size_t)30 * sl + lane;
-        r[i] = rl;
-        d[i] = 0.f;
-        z[i] = zl;
-        pf[4 * (size_t)rs + rsub] = zl;
+        const size_t i = (size_t)30 * lsl + lane;
+        V.r[i] = rl;
+        V.d[i] = 0.f;
+        V.z[i] = zl;
+        V.pf[4 * (size_t)rs + rsub] = zl;
         comp_add_prod(crz, rl, zl);
         comp_add_prod(crr, rl, rl);
       }
@@ -1193,11 +1232,14 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
       zero_ws(1);
       for (int ls = 0; ls < L && alive; ls++) {
         const bool on = sh.act[kp][ls] != 0;
+        const Vecs V = vecs(ls);
+        const int* __restrict__ soff = sh.lp[ls].soff;
         Comp cpq{0.f, 0.f};
         for (int sl = first_slice(ls); sl < sh.lfirst[ls + 1] && alive; sl += kRingWarps) {
-          const int k1 = off[sl + 1];
+          const int lsl = sl - V.s0;
+          const int k1 = soff[lsl + 1];
           float y0 = 0.f, y1 = 0.f, y2 = 0.f;  // partial rows 0, 1, 2 of block row t
-          for (int kk = off[sl]; kk < k1; kk += kRingSteps) {
+          for (int kk = soff[lsl]; kk < k1; kk += kRingSteps) {
             const int n = min(kRingSteps, k1 - kk);
             const int j = pc & 1;
             if (!__all_sync(0xffffffffu, mbar_wait(full + 2 * w + j, (pc >> 1) & 1))) {
@@ -1216,7 +1258,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
 #pragma unroll
               for (int u = 0; u < kPer; u++) {
                 const int st = rsub + 3 * u;
-                x[u] = st < n ? p4[scol[st * kSliceRows + t]] : make_float4(0.f, 0.f, 0.f, 0.f);
+                x[u] = st < n ? V.p4[scol[st * kSliceRows + t]] : make_float4(0.f, 0.f, 0.f, 0.f);
               }
 #pragma unroll
               for (int u = 0; u < kPer; u++) {
@@ -1250,8 +1292,8 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
             const float nb = rsub == 0 ? b0 : (rsub == 1 ? b1 : b2);
             const float y = (own + na) + nb;
             if (act_l) {
-              q[(size_t)30 * sl + lane] = y;
-              comp_add_prod(cpq, pf[4 * (size_t)(sl * kSliceRows + t) + rsub], y);
+              V.q[(size_t)30 * lsl + lane] = y;
+              comp_add_prod(cpq, V.pf[4 * (size_t)(lsl * kSliceRows + t) + rsub], y);
             }
           }
         }
@@ -1277,6 +1319,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
       if (!sh.act[kp][ls]) continue;  // warp-uniform; the partials stay zero
       constexpr int kUB = 4;
       const int hi = sh.lfirst[ls + 1];
+      const Vecs V = vecs(ls);
       const float alpha = (float)(sh.rz[ls] / sh.res[0][ls]);
       Comp cz{0.f, 0.f}, cr{0.f, 0.f};
       for (int sl0 = first_slice(ls); sl0 < hi; sl0 += kUB * kRingWarps) {
@@ -1285,18 +1328,19 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
         for (int u = 0; u < kUB; u++) {
           const int sl = sl0 + u * kRingWarps;
           if (sl < hi) {
-            const size_t i = (size_t)30 * sl + ln;
-            dv[u] = d[i];
-            pv[u] = pf[4 * (size_t)(sl * kSliceRows + t) + rsub];
-            qv[u] = q[i];
-            rv[u] = r[i];
+            const int lsl = sl - V.s0;
+            const size_t i = (size_t)30 * lsl + ln;
+            dv[u] = V.d[i];
+            pv[u] = V.pf[4 * (size_t)(lsl * kSliceRows + t) + rsub];
+            qv[u] = V.q[i];
+            rv[u] = V.r[i];
             if (pkind == OD_PRECOND_BLOCK_JACOBI) {
-              const float* m = pinv + (size_t)90 * sl + ln;
+              const float* m = V.pinv + (size_t)90 * lsl + ln;
               m0[u] = m[0];
               m1[u] = m[30];
               m2[u] = m[60];
             } else if (pkind == OD_PRECOND_JACOBI) {
-              m0[u] = pinv[(size_t)30 * sl + ln];
+              m0[u] = V.pinv[(size_t)30 * lsl + ln];
             }
           }
         }
@@ -1304,7 +1348,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
         for (int u = 0; u < kUB; u++) {
           const int sl = sl0 + u * kRingWarps;
           if (sl < hi) {  // warp-uniform
-            const size_t i = (size_t)30 * sl + ln;
+            const size_t i = (size_t)30 * (sl - V.s0) + ln;
             const float rl = act_l ? fmaf(-alpha, qv[u], rv[u]) : 0.f;
             const float r0 = __shfl_sync(0xffffffffu, rl, lbase);
             const float r1 = __shfl_sync(0xffffffffu, rl, lbase + 1);
@@ -1313,9 +1357,9 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
             if (pkind == OD_PRECOND_BLOCK_JACOBI) zl = fmaf(m0[u], r0, fmaf(m1[u], r1, m2[u] * r2));
             else if (pkind == OD_PRECOND_JACOBI) zl = m0[u] * rl;
             if (act_l) {
-              d[i] = fmaf(alpha, pv[u], dv[u]);
-              r[i] = rl;
-              z[i] = zl;
+              V.d[i] = fmaf(alpha, pv[u], dv[u]);
+              V.r[i] = rl;
+              V.z[i] = zl;
               comp_add_prod(cz, rl, zl);
               comp_add_prod(cr, rl, rl);
             }
@@ -1351,6 +1395,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
       if (!sh.act[kp][ls]) continue;
       constexpr int kUD = 8;
       const int hi = sh.lfirst[ls + 1];
+      const Vecs V = vecs(ls);
       const float bf = (float)sh.res[0][ls];
       for (int sl0 = first_slice(ls); sl0 < hi; sl0 += kUD * kRingWarps) {
         float zv[kUD], pv[kUD];
@@ -1358,14 +1403,16 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
         for (int u = 0; u < kUD; u++) {
           const int sl = sl0 + u * kRingWarps;
           if (sl < hi) {
-            zv[u] = z[(size_t)30 * sl + ln];
-            pv[u] = pf[4 * (size_t)(sl * kSliceRows + t) + rsub];
+            const int lsl = sl - V.s0;
+            zv[u] = V.z[(size_t)30 * lsl + ln];
+            pv[u] = V.pf[4 * (size_t)(lsl * kSliceRows + t) + rsub];
           }
         }
 #pragma unroll
         for (int u = 0; u < kUD; u++) {
           const int sl = sl0 + u * kRingWarps;
-          if (sl < hi && act_l) pf[4 * (size_t)(sl * kSliceRows + t) + rsub] = fmaf(bf, pv[u], zv[u]);
+          if (sl < hi && act_l)
+            V.pf[4 * (size_t)((sl - V.s0) * kSliceRows + t) + rsub] = fmaf(bf, pv[u], zv[u]);
         }
       }
     }
@@ -1494,18 +1541,18 @@ od_status launch_spmv_lower(Scene* s, const double* v1, double c1, const double*
   return OD_OK;
 }
 
-od_status launch_expand_batch(Ctx* ctx, const SceneDev* sd, const Tile* tiles, int n) {
-  if (n <= 0) return OD_OK;
+od_status launch_expand_batch(Ctx* ctx, int n_sc, const SceneDev* sd, const TileDir& dir) {
+  if (dir.tiles <= 0) return OD_OK;
   ctx->launches++;
-  expand_batch_kernel<<<n, kThreads, 0, ctx->stream>>>(tiles, sd);
+  expand_batch_kernel<<<dir.tiles, kThreads, 0, ctx->stream>>>(n_sc, dir.prefix, sd);
   OD_CUDA(cudaGetLastError());
   return OD_OK;
 }
 
-od_status launch_spmv_lower_batch(Ctx* ctx, const SceneDev* sd, const Tile* tiles, int n) {
-  if (n <= 0) return OD_OK;
+od_status launch_spmv_lower_batch(Ctx* ctx, int n_sc, const SceneDev* sd, const TileDir& dir) {
+  if (dir.tiles <= 0) return OD_OK;
   ctx->launches++;
-  spmv_lower_batch_kernel<<<n, kThreads, 0, ctx->stream>>>(tiles, sd);
+  spmv_lower_batch_kernel<<<dir.tiles, kThreads, 0, ctx->stream>>>(n_sc, dir.prefix, sd);
   OD_CUDA(cudaGetLastError());
   return OD_OK;
 }
@@ -1682,6 +1729,7 @@ void pcg_free(Scene* s) {
   cudaFree(P.sc);
   cudaFree(P.gbar);
   mixed_free(P.mix);
+  slice_free(P.slice);
   if (P.sc_host) cudaFreeHost(P.sc_host);
   if (P.timeout_host) cudaFreeHost(P.timeout_host);
   P = Pcg();
@@ -1740,36 +1788,68 @@ static int ring_kernel_ctas(const Ctx* ctx) {
   return std::min(per_sm, 1) * ctx->num_sms;
 }
 
-void mixed_free(MixedSys* m) {
-  if (!m) return;
-  for (int* v : {m->perm, m->slice_sc, m->sc_slice_dev, m->off, m->col, m->src, m->cta_first, m->cta_sc_lo,
-                 m->sc_cta})
-    cudaFree(v);
-  cudaFree(m->val);
-  cudaFree(m->v32);
-  cudaFree(m->r64);
-  cudaFree(m->desc);
-  cudaFree(m->ring);
-  cudaFree(m->rrbb);
-  cudaFree(m->res_tiles);
-  cudaFree(m->res_part);
-  cudaFree(m->fill_tiles);
-  cudaFree(m->part);
-  cudaFree(m->gbar);
-  if (m->ring_host) cudaFreeHost(m->ring_host);
-  if (m->rrbb_host) cudaFreeHost(m->rrbb_host);
-  if (m->timeout_host) cudaFreeHost(m->timeout_host);
-  cudaFree(m->prof);
-  if (m->prof_host) cudaFreeHost(m->prof_host);
-  delete m;
+void slice_free(SliceSys* sl) {
+  if (!sl) return;
+  for (int* v : {sl->perm, sl->off, sl->col, sl->src}) cudaFree(v);
+  cudaFree(sl->val);
+  cudaFree(sl->v32);
+  cudaFree(sl->r64);
+  delete sl;
 }
 
 template <class T>
-static od_status mix_upload(MixedSys* m, T** dst, const T* src, size_t n) {
+static od_status dev_upload(T** dst, const T* src, size_t n, long long& bytes) {
   OD_CUDA(cudaMalloc((void**)dst, sizeof(T) * std::max<size_t>(1, n)));
   if (n) OD_CUDA(cudaMemcpy(*dst, src, sizeof(T) * n, cudaMemcpyHostToDevice));
-  m->device_bytes += (long long)(sizeof(T) * n);
+  bytes += (long long)(sizeof(T) * n);
   return OD_OK;
+}
+
+od_status slice_build(Scene* s) {
+  Pcg& P = s->pcg;
+  if (P.slice) return OD_OK;
+  SliceSys* sl = new SliceSys();
+  HostSliced hs;
+  build_sliced(s->hbsr_rp, s->hbsr_col, s->bsr.nb, hs);
+  sl->ns = hs.ns;
+  sl->steps = hs.off[hs.ns];
+  sl->off_host = hs.off;
+  sl->bytes = 40.0 * s->bsr.nnzb + 24.0 * s->bsr.nb;
+  auto fail = [&](od_status st) { slice_free(sl); return st; };
+  od_status st;
+  if ((st = dev_upload(&sl->perm, hs.perm.data(), hs.perm.size(), sl->device_bytes)) != OD_OK) return fail(st);
+  if ((st = dev_upload(&sl->off, hs.off.data(), hs.off.size(), sl->device_bytes)) != OD_OK) return fail(st);
+  if ((st = dev_upload(&sl->col, hs.col.data(), hs.col.size(), sl->device_bytes)) != OD_OK) return fail(st);
+  if ((st = dev_upload(&sl->src, hs.src.data(), hs.src.size(), sl->device_bytes)) != OD_OK) return fail(st);
+  const size_t ns = (size_t)std::max(1, sl->ns);
+  const size_t nval = (size_t)std::max<long long>(1, sl->steps) * 90;
+  const size_t nvec = (40 + 4 * 30 + 90) * ns;
+  cudaError_t e = cudaMalloc(&sl->val, sizeof(float) * nval);
+  if (e == cudaSuccess) e = cudaMalloc(&sl->v32, sizeof(float) * nvec);
+  if (e == cudaSuccess) e = cudaMemset(sl->v32, 0, sizeof(float) * nvec);
+  if (e == cudaSuccess) e = cudaMalloc(&sl->r64, sizeof(double) * std::max(1, P.n_pad));
+  if (e != cudaSuccess) return fail(cuda_fail(e, "slice_build"));
+  sl->device_bytes += (long long)(sizeof(float) * (nval + nvec) + sizeof(double) * P.n_pad);
+  s->device_bytes += sl->device_bytes;
+  P.slice = sl;
+  return OD_OK;
+}
+
+void mixed_free(MixedSys* m) {
+  if (!m) return;
+  for (int* v : {m->sc_slice_dev, m->dirs, m->cta_first, m->cta_sc_lo, m->sc_cta}) cudaFree(v);
+  cudaFree(m->desc);
+  cudaFree(m->ring);
+  cudaFree(m->rrbb);
+  cudaFree(m->res_part);
+  cudaFree(m->part);
+  cudaFree(m->gbar);
+  cudaFree(m->prof);
+  if (m->ring_host) cudaFreeHost(m->ring_host);
+  if (m->rrbb_host) cudaFreeHost(m->rrbb_host);
+  if (m->timeout_host) cudaFreeHost(m->timeout_host);
+  if (m->prof_host) cudaFreeHost(m->prof_host);
+  delete m;
 }
 
 // Contiguous slice ranges per CTA with about equal step counts and at most
@@ -1806,13 +1886,10 @@ static od_status mixed_partition(MixedSys* m, int G) {
       sc_cta[2 * s + 1] = b;
     }
   }
-  for (int* v : {m->cta_first, m->cta_sc_lo, m->sc_cta}) cudaFree(v);
-  cudaFree(m->part);
-  m->cta_first = m->cta_sc_lo = m->sc_cta = nullptr;
-  m->part = nullptr;
-  OD_TRY(mix_upload(m, &m->cta_first, first.data(), first.size()));
-  OD_TRY(mix_upload(m, &m->cta_sc_lo, sc_lo.data(), sc_lo.size()));
-  OD_TRY(mix_upload(m, &m->sc_cta, sc_cta.data(), sc_cta.size()));
+  long long scratch = 0;
+  OD_TRY(dev_upload(&m->cta_first, first.data(), first.size(), scratch));
+  OD_TRY(dev_upload(&m->cta_sc_lo, sc_lo.data(), sc_lo.size(), scratch));
+  OD_TRY(dev_upload(&m->sc_cta, sc_cta.data(), sc_cta.size(), scratch));
   const size_t npart = (size_t)3 * std::max(1, m->n_sc) * G + 2 * (size_t)G;
   OD_CUDA(cudaMalloc(&m->part, sizeof(double) * npart));
   OD_CUDA(cudaMemset(m->part, 0, sizeof(double) * npart));
@@ -1822,82 +1899,75 @@ static od_status mixed_partition(MixedSys* m, int G) {
 
 od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::vector<const double*>& b,
                       const std::vector<double*>& x, MixedSys** out) {
-  MixedSys* m = new MixedSys();
-  m->n_sc = (int)scenes.size();
-  std::vector<int> perm, slice_sc, off{0}, col, src;
-  std::vector<Tile> res_tiles, fill_tiles;
-  m->sc_slice.push_back(0);
-  int row0 = 0;
-  for (int i = 0; i < m->n_sc; i++) {
-    Scene* s = scenes[i];
-    HostSliced hs;
-    build_sliced(s->hbsr_rp, s->hbsr_col, s->bsr.nb, hs);
-    const int slice0 = (int)slice_sc.size(), step0 = off.back();
-    perm.insert(perm.end(), hs.perm.begin(), hs.perm.end());
-    slice_sc.insert(slice_sc.end(), hs.ns, i);
-    for (int k = 1; k <= hs.ns; k++) off.push_back(step0 + hs.off[k]);
-    for (int c : hs.col) col.push_back(c + kSliceRows * slice0);
-    src.insert(src.end(), hs.src.begin(), hs.src.end());
-    m->sc_slice.push_back(slice0 + hs.ns);
-    m->sc_row0.push_back(row0);
-    m->sc_nb.push_back(s->bsr.nb);
-    m->sc_bytes.push_back(40.0 * s->bsr.nnzb + 24.0 * s->bsr.nb);
-    MixDesc dsc{};
-    dsc.row_ptr = s->bsr.row_ptr;
-    dsc.col = s->bsr.col;
-    dsc.diag_pos = s->bsr.diag_pos;
-    dsc.A64 = s->A64;
-    dsc.b = i < (int)b.size() ? b[i] : nullptr;
-    dsc.x = i < (int)x.size() ? x[i] : nullptr;
-    dsc.nb = s->bsr.nb;
-    dsc.row0 = row0;
-    dsc.tile0 = (int)res_tiles.size();
-    for (int r = 0; r < s->bsr.nb; r += kResRows) res_tiles.push_back(Tile{i, r, std::min(s->bsr.nb, r + kResRows), 0});
-    dsc.ntiles = (int)res_tiles.size() - dsc.tile0;
-    for (int k = step0; k < off.back(); k += 32) fill_tiles.push_back(Tile{i, k, std::min(off.back(), k + 32), 0});
-    m->desc_host.push_back(dsc);
-    row0 += 3 * s->bsr.nb;
+  for (Scene* s : scenes) OD_TRY(slice_build(s));
+  const int G = ring_kernel_ctas(ctx);
+  if (G <= 0) {
+    set_error("mixed precision needs a cooperative launch of the ring kernel");
+    return OD_ERR_UNSUPPORTED;
   }
-  m->ns = (int)slice_sc.size();
-  m->steps = off.back();
-  m->n64 = row0;
-  m->off_host = off;
-  m->n_res_tiles = (int)res_tiles.size();
-  m->n_fill_tiles = (int)fill_tiles.size();
+  MixedSys* m = new MixedSys();
+  const int n = (int)scenes.size();
+  m->n_sc = n;
+  m->sc_slice.assign(1, 0);
+  m->off_host.assign(1, 0);
+  std::vector<int> dirs(4 * (n + 1), 0);
+  int* pres = dirs.data();
+  int* pfill = pres + (n + 1);
+  int* ppre = pfill + (n + 1);
+  int* pupd = ppre + (n + 1);
+  for (int i = 0; i < n; i++) {
+    Scene* s = scenes[i];
+    const SliceSys* sl = s->pcg.slice;
+    const int step0 = m->off_host.back();
+    for (int k = 1; k <= sl->ns; k++) m->off_host.push_back(step0 + sl->off_host[k]);
+    MixDesc d{};
+    d.row_ptr = s->bsr.row_ptr;
+    d.col = s->bsr.col;
+    d.diag_pos = s->bsr.diag_pos;
+    d.A64 = s->A64;
+    d.b = i < (int)b.size() ? b[i] : nullptr;
+    d.x = i < (int)x.size() ? x[i] : nullptr;
+    d.nb = s->bsr.nb;
+    d.ns = sl->ns;
+    d.steps = (int)sl->steps;
+    d.slice0 = m->sc_slice.back();
+    d.sperm = sl->perm;
+    d.soff = sl->off;
+    d.scol = sl->col;
+    d.ssrc = sl->src;
+    d.sval = sl->val;
+    d.v32 = sl->v32;
+    d.r64 = sl->r64;
+    m->desc_host.push_back(d);
+    m->sc_slice.push_back(d.slice0 + sl->ns);
+    m->sc_nb.push_back(s->bsr.nb);
+    m->sc_bytes.push_back(sl->bytes);
+    pres[i + 1] = pres[i] + (d.nb + kResRows - 1) / kResRows;
+    pfill[i + 1] = pfill[i] + (d.steps + kFillSteps - 1) / kFillSteps;
+    ppre[i + 1] = ppre[i] + (d.ns * kSliceRows + kThreads - 1) / kThreads;
+    pupd[i + 1] = pupd[i] + (3 * kSliceRows * d.ns + kThreads - 1) / kThreads;
+  }
+  m->ns = m->sc_slice.back();
   auto fail = [&](od_status st) { mixed_free(m); return st; };
+  long long scratch = 0;
   od_status st;
-  if ((st = mix_upload(m, &m->perm, perm.data(), perm.size())) != OD_OK) return fail(st);
-  if ((st = mix_upload(m, &m->slice_sc, slice_sc.data(), slice_sc.size())) != OD_OK) return fail(st);
-  if ((st = mix_upload(m, &m->sc_slice_dev, m->sc_slice.data(), m->sc_slice.size())) != OD_OK) return fail(st);
-  if ((st = mix_upload(m, &m->off, off.data(), off.size())) != OD_OK) return fail(st);
-  if ((st = mix_upload(m, &m->col, col.data(), col.size())) != OD_OK) return fail(st);
-  if ((st = mix_upload(m, &m->src, src.data(), src.size())) != OD_OK) return fail(st);
-  if ((st = mix_upload(m, &m->desc, m->desc_host.data(), m->desc_host.size())) != OD_OK) return fail(st);
-  if ((st = mix_upload(m, &m->res_tiles, res_tiles.data(), res_tiles.size())) != OD_OK) return fail(st);
-  if ((st = mix_upload(m, &m->fill_tiles, fill_tiles.data(), fill_tiles.size())) != OD_OK) return fail(st);
-  const size_t ns = (size_t)m->ns;
-  const size_t nval = (size_t)std::max<long long>(1, m->steps) * 90;
-  const size_t nvec = (40 + 4 * 30 + 90) * std::max<size_t>(1, ns);
-  cudaError_t e = cudaMalloc(&m->val, sizeof(float) * nval);
-  if (e == cudaSuccess) e = cudaMalloc(&m->v32, sizeof(float) * nvec);
-  if (e == cudaSuccess) e = cudaMemset(m->v32, 0, sizeof(float) * nvec);
-  if (e == cudaSuccess) e = cudaMalloc(&m->r64, sizeof(double) * std::max(1, m->n64));
-  if (e == cudaSuccess) e = cudaMalloc(&m->ring, sizeof(RingScene) * std::max(1, m->n_sc));
-  if (e == cudaSuccess) e = cudaMallocHost(&m->ring_host, sizeof(RingScene) * std::max(1, m->n_sc));
-  if (e == cudaSuccess) e = cudaMalloc(&m->rrbb, sizeof(double) * 2 * std::max(1, m->n_sc));
-  if (e == cudaSuccess) e = cudaMallocHost(&m->rrbb_host, sizeof(double) * 2 * std::max(1, m->n_sc));
-  if (e == cudaSuccess) e = cudaMalloc(&m->res_part, sizeof(double) * 2 * std::max(1, m->n_res_tiles));
+  if ((st = dev_upload(&m->sc_slice_dev, m->sc_slice.data(), m->sc_slice.size(), scratch)) != OD_OK) return fail(st);
+  if ((st = dev_upload(&m->desc, m->desc_host.data(), m->desc_host.size(), scratch)) != OD_OK) return fail(st);
+  if ((st = dev_upload(&m->dirs, dirs.data(), dirs.size(), scratch)) != OD_OK) return fail(st);
+  m->res_dir = TileDir{m->dirs, pres[n], kResRows};
+  m->fill_dir = TileDir{m->dirs + (n + 1), pfill[n], kFillSteps};
+  m->pre_dir = TileDir{m->dirs + 2 * (n + 1), ppre[n], kThreads};
+  m->upd_dir = TileDir{m->dirs + 3 * (n + 1), pupd[n], kThreads};
+  cudaError_t e = cudaMalloc(&m->ring, sizeof(RingScene) * std::max(1, n));
+  if (e == cudaSuccess) e = cudaMallocHost(&m->ring_host, sizeof(RingScene) * std::max(1, n));
+  if (e == cudaSuccess) e = cudaMalloc(&m->rrbb, sizeof(double) * 2 * std::max(1, n));
+  if (e == cudaSuccess) e = cudaMallocHost(&m->rrbb_host, sizeof(double) * 2 * std::max(1, n));
+  if (e == cudaSuccess) e = cudaMalloc(&m->res_part, sizeof(double) * 2 * std::max(1, pres[n]));
   if (e == cudaSuccess) e = cudaMalloc(&m->gbar, sizeof(GridBarrier));
   if (e == cudaSuccess) e = cudaMallocHost(&m->timeout_host, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&m->prof, 2 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMallocHost(&m->prof_host, 2 * sizeof(unsigned long long));
   if (e != cudaSuccess) return fail(cuda_fail(e, "mixed_build"));
-  m->device_bytes += (long long)(sizeof(float) * (nval + nvec) + sizeof(double) * m->n64);
-  const int G = ring_kernel_ctas(ctx);
-  if (G <= 0) {
-    set_error("mixed precision needs a cooperative launch of the ring kernel");
-    return fail(OD_ERR_UNSUPPORTED);
-  }
   if ((st = mixed_partition(m, G)) != OD_OK) return fail(st);
   *out = m;
   return OD_OK;
@@ -1907,10 +1977,11 @@ od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::ve
 // outputs) back to the host
 static od_status mixed_residual(Ctx* ctx, MixedSys* m, bool with_ring) {
   cudaStream_t strm = ctx->stream;
-  if (m->n_res_tiles > 0) {
+  if (m->res_dir.tiles > 0) {
     ctx->launches += 2;
-    mix_residual_kernel<<<m->n_res_tiles, kThreads, 0, strm>>>(m->res_tiles, m->desc, m->r64, m->res_part);
-    mix_residual_finish<<<nblk(m->n_sc, kThreads / 32), kThreads, 0, strm>>>(m->n_sc, m->desc, m->res_part, m->rrbb);
+    mix_residual_kernel<<<m->res_dir.tiles, kThreads, 0, strm>>>(m->n_sc, m->res_dir.prefix, m->desc, m->res_part);
+    mix_residual_finish<<<nblk(m->n_sc, kThreads / 32), kThreads, 0, strm>>>(m->n_sc, m->res_dir.prefix, m->res_part,
+                                                                             m->rrbb);
     OD_CUDA(cudaGetLastError());
   } else {
     OD_CUDA(cudaMemsetAsync(m->rrbb, 0, sizeof(double) * 2 * m->n_sc, strm));
@@ -1932,20 +2003,13 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
     set_error("mixed precision supports the none, Jacobi and block-Jacobi preconditioners");
     return OD_ERR_UNSUPPORTED;
   }
-  const int ns = m->ns, nrs = ns * kSliceRows;
-  float4* p4 = reinterpret_cast<float4*>(m->v32);
-  float* d32 = m->v32 + 40 * (size_t)ns;
-  float* r32 = d32 + 30 * (size_t)ns;
-  float* z32 = r32 + 30 * (size_t)ns;
-  float* q32 = z32 + 30 * (size_t)ns;
-  float* pinv32 = q32 + 30 * (size_t)ns;
-  if (m->n_fill_tiles > 0) {
+  if (m->fill_dir.tiles > 0) {
     ctx->launches++;
-    mix_fill_kernel<<<m->n_fill_tiles, kThreads, 0, strm>>>(m->fill_tiles, m->desc, m->src, m->val);
+    mix_fill_kernel<<<m->fill_dir.tiles, kThreads, 0, strm>>>(n_sc, m->fill_dir.prefix, m->desc);
   }
-  if (pk != OD_PRECOND_NONE && nrs > 0) {
+  if (pk != OD_PRECOND_NONE && m->pre_dir.tiles > 0) {
     ctx->launches++;
-    mix_precond_kernel<<<nblk(nrs, kThreads), kThreads, 0, strm>>>(nrs, pk, m->perm, m->slice_sc, m->desc, pinv32);
+    mix_precond_kernel<<<m->pre_dir.tiles, kThreads, 0, strm>>>(n_sc, m->pre_dir.prefix, pk, m->desc);
   }
   OD_TRY(mixed_residual(ctx, m, false));
   std::vector<double> eps(n_sc), rr(n_sc), bb(n_sc);
@@ -1986,23 +2050,19 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
     GridBarrier* gbp = (GridBarrier*)m->gbar;
     unsigned long long* profp = prof ? m->prof : nullptr;
     if (prof) OD_CUDA(cudaMemsetAsync(m->prof, 0, 2 * sizeof(unsigned long long), strm));
-    int pkv = pk;
-    int nsc = n_sc;
-    void* args[] = {(void*)&nsc, (void*)&m->cta_first, (void*)&m->cta_sc_lo, (void*)&m->sc_cta,
-                    (void*)&m->sc_slice_dev, (void*)&m->slice_sc,
-                    (void*)&m->perm,      (void*)&m->off,       (void*)&m->col,    (void*)&m->val,
-                    (void*)&m->r64,       (void*)&m->desc,      (void*)&m->ring,   (void*)&d32,
-                    (void*)&r32,          (void*)&z32,          (void*)&p4,        (void*)&q32,
-                    (void*)&pkv,          (void*)&pinv32,       (void*)&m->part,   (void*)&gbp,
-                    (void*)&profp};
+    int pkv = pk, nsc = n_sc;
+    void* args[] = {(void*)&nsc,       (void*)&m->cta_first, (void*)&m->cta_sc_lo, (void*)&m->sc_cta,
+                    (void*)&m->sc_slice_dev, (void*)&m->desc, (void*)&m->ring,    (void*)&pkv,
+                    (void*)&m->part,   (void*)&gbp,          (void*)&profp};
     if (prof) OD_CUDA(cudaEventRecord(ctx->ev_pool[0], strm));
     ctx->launches++;
     OD_CUDA(cudaLaunchCooperativeKernel((void*)pcg32_ring_kernel, dim3(m->cta_grid), dim3(kRingThreads), args,
                                         kRingSmem, strm));
     if (prof) OD_CUDA(cudaEventRecord(ctx->ev_pool[1], strm));
-    ctx->launches++;
-    mix_update_kernel<<<nblk(3LL * nrs, kThreads), kThreads, 0, strm>>>(nrs, m->perm, m->slice_sc, m->desc, m->ring,
-                                                                         d32);
+    if (m->upd_dir.tiles > 0) {
+      ctx->launches++;
+      mix_update_kernel<<<m->upd_dir.tiles, kThreads, 0, strm>>>(n_sc, m->upd_dir.prefix, m->desc, m->ring);
+    }
     OD_CUDA(cudaMemcpyAsync(m->timeout_host, &gbp->timeout, sizeof(int), cudaMemcpyDeviceToHost, strm));
     OD_TRY(mixed_residual(ctx, m, true));
     if (*m->timeout_host) {
