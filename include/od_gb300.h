@@ -231,6 +231,10 @@ od_status od_scene_get_external_forces(od_scene* scene, double* f_ext);
 /* Integrator (NonlinearImplicitBackwardEuler ctor, nonlinearImplicitBackwardEuler.h:48-73,
  * or the full-order Newmark).  Resets the state to rest. */
 od_status od_integrator_setup(od_scene* scene, const od_integrator_params* params);
+/* Change the parameters of the set-up integrator (same kind) and keep the
+ * state (d, v, a, time); no reference counterpart (the reference fixes them
+ * in the integrator's constructor). */
+od_status od_integrator_update(od_scene* scene, const od_integrator_params* params);
 /* Simulator::runTimeSteps (simulator.cpp:35-38): n steps, each followed by the
  * mesh displacement update (updateMeshVerticesDisplacements,
  * nonlinearImplicitBackwardEuler.h:103-116). */

@@ -156,6 +156,7 @@ SIGNATURES = {
     "od_step": (C.c_int, [_vp, C.c_int, C.POINTER(od_step_stats)]),
     "od_get_state": (C.c_int, [_vp, _dp, _dp, _dp]),
     "od_set_state": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "od_integrator_update": (C.c_int, [_vp, C.POINTER(od_integrator_params)]),
     "od_batch_create": (C.c_int, [_vp, C.c_int, C.POINTER(_vp), C.POINTER(_vp)]),
     "od_batch_step": (C.c_int, [_vp, C.c_int, C.POINTER(od_step_stats)]),
     "od_batch_destroy": (C.c_int, [_vp]),
@@ -290,6 +291,7 @@ class Context:
         h = _vp()
         _check(L.od_ctx_create(device, C.byref(h)), "od_ctx_create")
         self.h = h
+        self.device = device
         _live_ctxs.add(self)
 
     def synchronize(self):
@@ -370,6 +372,12 @@ class Scene:
     def set_displacements(self, u):
         u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1, 3)
         _check(load_library().od_scene_set_displacements(self.h, _d(u)), "set_displacements")
+
+    def info_now(self):
+        """od_scene_get_info now (device_bytes grows with the first mixed solve)."""
+        info = od_scene_info()
+        _check(load_library().od_scene_get_info(self.h, C.byref(info)), "od_scene_get_info")
+        return info
 
     def displacements(self):
         u = np.zeros((self.n_nodes, 3))
@@ -456,6 +464,11 @@ class Scene:
     def setup_integrator(self, integrator):
         p = integrator.to_c()
         _check(load_library().od_integrator_setup(self.h, C.byref(p)), "integrator_setup")
+
+    def update_integrator(self, integrator):
+        """New integrator parameters (same kind), state kept."""
+        p = integrator.to_c()
+        _check(load_library().od_integrator_update(self.h, C.byref(p)), "integrator_update")
 
     def step(self, n: int = 1):
         st = od_step_stats()

@@ -620,6 +620,19 @@ od_status od_integrator_setup(od_scene* scene, const od_integrator_params* p) {
   return OD_OK;
 }
 
+od_status od_integrator_update(od_scene* scene, const od_integrator_params* p) {
+  OD_CHECK_ARG(scene && p, "od_integrator_update: NULL argument");
+  Scene* s = &scene->s;
+  OD_CHECK_ARG(s->has_integrator, "od_integrator_update: call od_integrator_setup first");
+  OD_CHECK_ARG(p->kind == s->ip.kind, "od_integrator_update: the integrator kind cannot change");
+  OD_CHECK_ARG(p->dt > 0.0, "od_integrator_update: dt must be positive");
+  OD_CHECK_ARG(p->kind == OD_INTEGRATOR_BACKWARD_EULER || (p->newton_iters >= 1 && p->nm_beta > 0.0 && p->nm_gamma > 0.0),
+               "od_integrator_update: Newmark needs beta > 0, gamma > 0, newton_iters >= 1");
+  OD_TRY(check_solver(&p->solver));
+  s->ip = *p;
+  return OD_OK;
+}
+
 // one backward-Euler step (nonlinearImplicitBackwardEuler.h:82-101) followed
 // by the mesh update u += h v on free DOFs (:103-116)
 static od_status be_step(Scene* s, od_step_stats* acc) {

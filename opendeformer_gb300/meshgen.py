@@ -185,3 +185,28 @@ def instance_grid(inst) -> TetGrid:
     nx, ny, nz = inst["dims"]
     return tet_grid(nx, ny, nz, h=0.05, jitter=0.10, seed=inst["seed"], tets_per_cube=6)
 
+
+
+def serving_pool(n: int = 4096, seed: int = 5):
+    """Scene pool for serving: tet counts log-uniform in [1e3, 2e5], box
+    aspect ratios (x and y against z) uniform in [1, 8], 6 tets per cube,
+    longest side 1 m, interior jitter 0.1 h; corotational or invertible
+    Neo-Hookean (probability 1/2), E log-uniform in [1e4, 1e6] Pa, nu uniform
+    in [0.3, 0.48].  Returns dicts (dims, h, kind, E, nu, seed)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        tets = float(np.exp(rng.uniform(np.log(1e3), np.log(2e5))))
+        ax, ay = rng.uniform(1.0, 8.0, size=2)
+        s = (tets / 6.0 / (ax * ay)) ** (1.0 / 3.0)
+        dims = tuple(max(1, int(round(v))) for v in (ax * s, ay * s, s))
+        kind = "corotational" if rng.random() < 0.5 else "neohookean"
+        E = float(np.exp(rng.uniform(np.log(1e4), np.log(1e6))))
+        nu = float(rng.uniform(0.3, 0.48))
+        out.append(dict(dims=dims, h=1.0 / max(dims), kind=kind, E=E, nu=nu, seed=seed * 100000 + i))
+    return out
+
+
+def pool_grid(inst) -> TetGrid:
+    nx, ny, nz = inst["dims"]
+    return tet_grid(nx, ny, nz, h=inst["h"], jitter=0.10, seed=inst["seed"], tets_per_cube=6)
