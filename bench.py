@@ -363,6 +363,87 @@ def batched_tier(args, api, ctx):
             "max_rel_err_vs_fp64": err}
 
 
+def serving_tier(args, api, ctx):
+    """Serving: Poisson arrivals of step requests over a pool of scenes whose
+    sizes are log-uniform in [1e3, 2e5] tets (random aspect ratios 1-8),
+    corotational / Neo-Hookean; per request a time step (uniform 1/120 to
+    1/30 s), a gravity direction and a 10-1000 Pa surface load (log-uniform);
+    mixed-precision PCG at 1e-6; admission by a device-memory budget smaller
+    than the pool, LRU eviction.  The pool is the first args.serving_pool
+    scenes of the 4096-scene pool (building all of them on the host takes
+    minutes) and the budget scales with it; the same arrival sequence runs
+    through the batched server and through the plain path (each request
+    stepped alone with the FP64 solver)."""
+    from opendeformer_gb300 import serving
+    pool = meshgen.serving_pool(4096)[: args.serving_pool]
+    n_tets = sum(6 * int(np.prod(p["dims"])) for p in pool)
+    budget = int(args.serving_budget_frac * 2600 * n_tets)
+    rate, window = args.serving_rate, args.serving_seconds
+    rng = np.random.default_rng(9)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * window * 1.2) + 16))
+    arrivals = arrivals[arrivals < window]
+    reqs_proto = []
+    for t in arrivals:
+        gdir = rng.normal(size=3)
+        reqs_proto.append((float(t), int(rng.integers(len(pool))), float(rng.uniform(1 / 120, 1 / 30)),
+                           tuple(gdir / np.linalg.norm(gdir)),
+                           float(np.exp(rng.uniform(np.log(10.0), np.log(1000.0))))))
+
+    def build(inst):
+        g = meshgen.pool_grid(inst)
+        cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+        return g.X, g.tets, g.facets, cd, g.face_facets(0, 1)
+
+    def run(batched):
+        prec = "mixed" if batched else "fp64"
+        sv = serving.Server(ctx, budget_bytes=budget, batched=batched)
+        for inst in pool:
+            sv.add_scene(serving.SceneSpec(build=lambda inst=inst: build(inst),
+                                           material=api.Material(inst["kind"], 1000.0, inst["E"], inst["nu"], 0.1),
+                                           tol=1e-6, precision=prec))
+        tw = time.perf_counter()
+        warmed = sv.warm(range(len(pool)))
+        warm_s = time.perf_counter() - tw
+        t0 = time.perf_counter()
+        sv.clock = lambda: time.perf_counter() - t0
+        nxt, done, sizes = 0, [], []
+        while True:
+            now = sv.clock()
+            while nxt < len(reqs_proto) and reqs_proto[nxt][0] <= now:
+                a, sid, dt, gdir, tr = reqs_proto[nxt]
+                sv.submit(serving.StepRequest(scene=sid, arrival=a, dt=dt, gravity=gdir, traction=tr))
+                nxt += 1
+            if now >= window:
+                break
+            out = sv.tick()
+            if out:
+                sizes.append(len(out))
+                done += out
+            elif nxt < len(reqs_proto):
+                time.sleep(max(0.0, min(0.001, reqs_proto[nxt][0] - now)))
+        wall = sv.clock()
+        backlog = sv.pending()
+        stats = dict(sv.stats)
+        sv.close()
+        lat = sorted(1000.0 * (r.done - r.arrival) for r in done)
+        bad = sum(1 for r in done if r.status != 0)
+        return {"completed": len(done), "failed": bad, "offered": len(reqs_proto), "backlog_at_end": backlog,
+                "steps_per_s": len(done) / wall,
+                "p50_ms": lat[len(lat) // 2] if lat else None,
+                "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None,
+                "mean_batch": float(np.mean(sizes)) if sizes else 0.0, "warmed_scenes": warmed,
+                "warm_s": warm_s, **stats}
+
+    res = {"batched_mixed": run(True), "plain_fp64": run(False)}
+    return {"workload": "serving_pool_poisson", "pool_scenes": len(pool), "pool_tets": n_tets,
+            "budget_bytes": budget, "arrival_rate_per_s": rate, "window_s": window, "tol": 1e-6,
+            "note": "latency = completion - arrival on the host clock; requests past the window are not waited "
+                    "for (backlog_at_end)",
+            **res,
+            "throughput_ratio_batched_vs_plain": (res["batched_mixed"]["steps_per_s"] /
+                                                  max(1e-9, res["plain_fp64"]["steps_per_s"]))}
+
+
 def run_gpu(args, wl):
     import torch
     from opendeformer_gb300 import api
@@ -498,7 +579,8 @@ def run_gpu(args, wl):
     tiers = {}
     if rank == 0 and not args.no_tiers:
         del scene
-        for name, fn in (("precision_tier", precision_tier), ("batched_tier", batched_tier)):
+        for name, fn in (("precision_tier", precision_tier), ("batched_tier", batched_tier),
+                         ("serving_tier", serving_tier)):
             try:
                 tiers[name] = fn(args, api, ctx)
             except Exception as exc:
@@ -538,6 +620,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tiers", action="store_true", help="skip the mixed-precision and batched workloads")
     ap.add_argument("--tier-steps", type=int, default=5)
+    ap.add_argument("--serving-pool", type=int, default=512)
+    ap.add_argument("--serving-rate", type=float, default=2000.0)
+    ap.add_argument("--serving-seconds", type=float, default=15.0)
+    ap.add_argument("--serving-budget-frac", type=float, default=0.5,
+                    help="device budget as a fraction of the pool's estimated resident bytes")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

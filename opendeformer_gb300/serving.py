@@ -34,6 +34,7 @@ class SceneSpec:
     max_iter: int = 5000
     precond: str = "block_jacobi"
     rayleigh: tuple = (0.01, 0.001)
+    precision: str = "mixed"
 
 
 @dataclass
@@ -61,11 +62,15 @@ class _Slot:
 class Server:
     """Admission by device-memory budget, LRU eviction, one batched step per
     tick.  budget_bytes: memory the resident scenes may use (default: the
-    device's free memory at creation less reserve_bytes)."""
+    device's free memory at creation less reserve_bytes).  batched=False
+    steps the tick's requests one scene at a time with Scene.step instead
+    (the plain path, for comparison; the scenes' precision is their spec's)."""
 
     def __init__(self, ctx: api.Context, budget_bytes: int | None = None, reserve_bytes: int = 4 << 30,
-                 max_batch: int | None = None, clock: Callable[[], float] = time.perf_counter):
+                 max_batch: int | None = None, clock: Callable[[], float] = time.perf_counter,
+                 batched: bool = True):
         self.ctx = ctx
+        self.batched = batched
         if budget_bytes is None:
             import torch
             free, _ = torch.cuda.mem_get_info(ctx.device)
@@ -77,7 +82,8 @@ class Server:
         self.resident: "OrderedDict[int, None]" = OrderedDict()   # LRU order, most recent last
         self.used = 0
         self.bytes_per_tet = 2600.0   # first estimate; raised to the largest measured ratio
-        self.stats = {"ticks": 0, "steps": 0, "admissions": 0, "restores": 0, "evictions": 0, "deferred": 0}
+        self.stats = {"ticks": 0, "steps": 0, "admissions": 0, "restores": 0, "evictions": 0, "deferred": 0,
+                      "s_admit": 0.0, "s_loads": 0.0, "s_batch_create": 0.0, "s_step": 0.0, "s_other": 0.0}
 
     # -- registry and queue
     def add_scene(self, spec: SceneSpec) -> int:
@@ -140,7 +146,7 @@ class Server:
         sp = slot.spec
         integ = api.NewmarkIntegrator(0.25, 0.5, sp.rayleigh[0], sp.rayleigh[1], dt,
                                       api.CGSolver(sp.tol, sp.max_iter, api.Preconditioner(sp.precond),
-                                                   precision="mixed"), sp.newton_iters)
+                                                   precision=sp.precision), sp.newton_iters)
         if setup:
             sc.setup_integrator(integ)
         else:
@@ -159,11 +165,14 @@ class Server:
         chosen = [sid for _, sid in heads]
         keep = set(chosen)
         batch_ids = []
+        t0 = time.perf_counter()
         for sid in chosen:
             if self._admit(sid, keep):
                 batch_ids.append(sid)
             else:
                 self.stats["deferred"] += 1
+        t1 = time.perf_counter()
+        self.stats["s_admit"] += t1 - t0
         if not batch_ids:
             return []
         reqs = []
@@ -177,11 +186,21 @@ class Server:
             tr = [([0.0, -req.traction, 0.0], load_facets)] if req.traction and len(load_facets) else []
             slot.scene.set_loads(body=g, tractions=tr)
             reqs.append(req)
-        batch = api.Batch(self.ctx, [self.slots[sid].scene for sid in batch_ids])
-        try:
-            st = batch.step(1)
-        finally:
-            batch.close()
+        t2 = time.perf_counter()
+        self.stats["s_loads"] += t2 - t1
+        if self.batched:
+            batch = api.Batch(self.ctx, [self.slots[sid].scene for sid in batch_ids])
+            t3 = time.perf_counter()
+            self.stats["s_batch_create"] += t3 - t2
+            try:
+                st = batch.step(1)
+            finally:
+                batch.close()
+        else:
+            t3 = t2
+            st = [self.slots[sid].scene.step(1) for sid in batch_ids]
+        t4 = time.perf_counter()
+        self.stats["s_step"] += t4 - t3
         t = self.clock()
         for req, s in zip(reqs, st):
             req.done = t
@@ -195,9 +214,25 @@ class Server:
             self.bytes_per_tet = max(self.bytes_per_tet, real / slot.mesh[1].shape[0])
         while self.used > self.budget and self._evict_one(set()):   # an estimate fell short
             pass
+        self.stats["s_other"] += time.perf_counter() - t4
         self.stats["ticks"] += 1
         self.stats["steps"] += len(reqs)
         return reqs
+
+    def warm(self, scene_ids) -> int:
+        """Make scenes resident (in order) while they fit; returns how many."""
+        n = 0
+        for sid in scene_ids:
+            slot = self.slots[sid]
+            if slot.scene is not None:
+                continue
+            if slot.mesh is None:
+                slot.mesh = slot.spec.build()
+            if self.used + self._estimate(slot) > self.budget:
+                break
+            self._admit(sid, set())
+            n += 1
+        return n
 
     def close(self):
         for slot in self.slots:
