@@ -244,7 +244,9 @@ def precision_tier(args, api, ctx):
     0.01 / 0.001, one Newton iteration, block-Jacobi PCG to 1e-10.  The
     same steps run with the FP64 solver and the mixed one (FP32 sliced SpMV
     and preconditioner, compensated dots summed in FP64, FP64 refinement)."""
-    g = meshgen.block_2m6()
+    nz = args.precision_nz
+    g = meshgen.block_2m6() if nz == 64 else meshgen.tet_grid(128, 64, nz, h=1.0 / 128, jitter=0.20, seed=4,
+                                                              tets_per_cube=5)
     bottom, top = g.face_nodes(2, 0), g.face_nodes(2, 1)
     rng = np.random.default_rng(4)
     presc = np.sort(rng.choice(top, size=int(0.2 * top.size), replace=False))
@@ -283,7 +285,8 @@ def precision_tier(args, api, ctx):
     nbytes, sms, nit = res["mixed"].pop("mix")
     res["fp64"].pop("mix")
     spmv_gbs = nbytes / (sms * 1e-3) / 1e9 if sms else None
-    return {"workload": "block2m6_nh_prescribed_newmark", "n_tets": g.n_tets, "dofs": 3 * g.n_nodes - len(cd),
+    return {"workload": "block2m6_nh_prescribed_newmark" if nz == 64 else f"block128x64x{nz}_nh_prescribed_newmark",
+            "n_tets": g.n_tets, "dofs": 3 * g.n_nodes - len(cd),
             "newton_iters": 1, "tol": 1e-10, "precond": "block_jacobi", "warmup": warm, "steps": steps,
             "fp64": res["fp64"], "mixed": res["mixed"],
             "speedup_mixed_vs_fp64": res["mixed"]["steps_per_s"] / res["fp64"]["steps_per_s"],
@@ -579,8 +582,11 @@ def run_gpu(args, wl):
     tiers = {}
     if rank == 0 and not args.no_tiers:
         del scene
+        only = [t for t in args.only_tiers.split(",") if t]
         for name, fn in (("precision_tier", precision_tier), ("batched_tier", batched_tier),
                          ("serving_tier", serving_tier)):
+            if only and name.split("_")[0] not in only:
+                continue
             try:
                 tiers[name] = fn(args, api, ctx)
             except Exception as exc:
@@ -620,6 +626,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tiers", action="store_true", help="skip the mixed-precision and batched workloads")
     ap.add_argument("--tier-steps", type=int, default=5)
+    ap.add_argument("--only-tiers", default="", help="comma list of precision,batched,serving (default: all)")
+    ap.add_argument("--precision-nz", type=int, default=64,
+                    help="cube layers of the precision-tier block (64: 2,621,440 tets)")
     ap.add_argument("--serving-pool", type=int, default=512)
     ap.add_argument("--serving-rate", type=float, default=2000.0)
     ap.add_argument("--serving-seconds", type=float, default=15.0)
