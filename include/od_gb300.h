@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define OD_ABI_VERSION 2
+#define OD_ABI_VERSION 3
 
 typedef enum od_status {
   OD_OK = 0,
@@ -129,6 +129,10 @@ typedef struct od_counters {
   double mix_spmv_bytes;      /* algorithmic bytes of those phases: stored blocks x 40 B
                                  (FP32 values + column index) + 24 B per block row (own p
                                  read, q written), for the scenes active in each iteration */
+  double mix_spmv_work_ms;    /* the same phases up to the moment the last CTA finished its
+                                 SpMV work (without the grid-wide sum that follows) */
+  long long mix_fallbacks;    /* mixed solves whose refinement stalled and that the FP64 PCG
+                                 finished (counted whether profiling is on or not) */
 } od_counters;
 
 typedef struct od_scene_info {

@@ -80,7 +80,8 @@ class od_counters(C.Structure):
     _fields_ = [("kernel_launches", C.c_longlong), ("host_syncs", C.c_longlong),
                 ("spmv_launches", C.c_longlong), ("spmv_ms", C.c_double),
                 ("pcg_launches", C.c_longlong), ("pcg_iterations", C.c_longlong), ("pcg_ms", C.c_double),
-                ("mix_iterations", C.c_longlong), ("mix_spmv_ms", C.c_double), ("mix_spmv_bytes", C.c_double)]
+                ("mix_iterations", C.c_longlong), ("mix_spmv_ms", C.c_double), ("mix_spmv_bytes", C.c_double),
+                ("mix_spmv_work_ms", C.c_double), ("mix_fallbacks", C.c_longlong)]
 
 
 class od_scene_info(C.Structure):

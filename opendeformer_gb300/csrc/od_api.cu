@@ -195,6 +195,8 @@ od_status od_ctx_get_counters(od_ctx* ctx, od_counters* out) {
   out->pcg_ms = ctx->c.pcg_kernel_ms;
   out->mix_iterations = ctx->c.mix_iters;
   out->mix_spmv_ms = ctx->c.mix_spmv_ms;
+  out->mix_spmv_work_ms = ctx->c.mix_spmv_work_ms;
+  out->mix_fallbacks = ctx->c.mix_fallbacks;
   out->mix_spmv_bytes = ctx->c.mix_spmv_bytes;
   return OD_OK;
 }
@@ -204,8 +206,8 @@ od_status od_ctx_reset_counters(od_ctx* ctx) {
   ctx->c.launches = ctx->c.host_syncs = ctx->c.spmv_launches = 0;
   ctx->c.pcg_kernel_launches = ctx->c.pcg_kernel_iters = 0;
   ctx->c.spmv_ms = ctx->c.pcg_kernel_ms = 0.0;
-  ctx->c.mix_iters = 0;
-  ctx->c.mix_spmv_ms = ctx->c.mix_spmv_bytes = 0.0;
+  ctx->c.mix_iters = ctx->c.mix_fallbacks = 0;
+  ctx->c.mix_spmv_ms = ctx->c.mix_spmv_bytes = ctx->c.mix_spmv_work_ms = 0.0;
   return OD_OK;
 }
 

@@ -54,6 +54,7 @@ struct SolveScalars {           // device-resident PCG scalars
 
 struct SliceSys;
 struct MixedSys;
+struct Scene;
 
 struct Pcg {
   int n_pad = 0;
@@ -193,12 +194,13 @@ struct MixDesc {
 // O(scenes).
 struct MixedSys {
   int n_sc = 0;                    // scenes
+  std::vector<Scene*> scenes;      // for the FP64 fallback of a solve that does not converge
   int ns = 0;                      // slices of all scenes
   std::vector<int> off_host;       // ns+1 step offsets of the concatenation (partition)
   std::vector<int> sc_slice;       // n_sc+1 first slice of each scene
   std::vector<int> sc_nb;          // n_sc block rows
   std::vector<double> sc_bytes;    // n_sc algorithmic bytes of one SpMV + p.q phase
-  unsigned long long* prof = nullptr;       // 2: phase time (ns), loop iterations (device)
+  unsigned long long* prof = nullptr;       // phase time incl. its sum, iterations, SpMV work time (ns), per-CTA stamps
   unsigned long long* prof_host = nullptr;  // pinned
   int* sc_slice_dev = nullptr;     // n_sc+1
   MixDesc* desc = nullptr;         // n_sc (device)
@@ -233,7 +235,9 @@ struct Ctx {
   long long pcg_kernel_iters = 0;
   double pcg_kernel_ms = 0.0;
   long long mix_iters = 0;            // inner FP32 loop iterations (profiling)
+  long long mix_fallbacks = 0;        // mixed solves finished by the FP64 solver
   double mix_spmv_ms = 0.0;
+  double mix_spmv_work_ms = 0.0;
   double mix_spmv_bytes = 0.0;
   int profiling = 0;
   std::vector<cudaEvent_t> ev_pool;   // event pairs for SpMV timing

@@ -938,6 +938,7 @@ struct RingShared {
   int c0[kMaxLocalScenes], c1[kMaxLocalScenes];  // CTA range of each local scene
   int lfirst[kMaxLocalScenes + 1];                // first slice of each local scene in the CTA range
   volatile unsigned char act[2][kMaxLocalScenes];  // activity by iteration parity
+  unsigned long long tmax;                    // profiling: the last CTA's end of the SpMV phase
   volatile int pub;                           // last iteration whose activity is published
   volatile int stop;
   int ok;
@@ -956,11 +957,17 @@ __device__ __forceinline__ int local_scene(const RingShared& sh, int sl, int& ls
 // over all CTAs.  Consumers only.
 template <int NV>
 __device__ __forceinline__ bool ring_sums(RingShared& sh, int L, int sc_lo, int n_sc, double gval,
-                                          double* __restrict__ part, double* __restrict__ part_g, GridBarrier* gb) {
+                                          double* __restrict__ part, double* __restrict__ part_g, GridBarrier* gb,
+                                          unsigned long long* __restrict__ stamp = nullptr) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int G = gridDim.x, b = blockIdx.x;
   if (lane == 0) sh.wg[w] = gval;
   named_sync<kRingConsumers>();
+  if (stamp && threadIdx.x == 0) {  // profiling: when this CTA's warps finished the phase
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    stamp[b] = t;
+  }
   if (w == 0) {
     if (lane < L) {
 #pragma unroll
@@ -980,6 +987,13 @@ __device__ __forceinline__ bool ring_sums(RingShared& sh, int L, int sc_lo, int 
     int ok = 1;
     if (lane == 0) ok = barrier_arrive_wait(gb);
     ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (stamp) {  // profiling: the last CTA's end of the phase
+      unsigned long long tmax = 0;
+      for (int c = lane; c < G; c += 32) tmax = max(tmax, __ldcg(stamp + c));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+      if (lane == 0) sh.tmax = tmax;
+    }
     double accg = 0.0;
     for (int c = lane; c < G; c += 32) accg += __ldcg(part_g + c);
     for (int ls = 0; ls < L; ls++) {
@@ -1303,7 +1317,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
       double na = 0.0;
       if (w == 0 && lane == 0)
         for (int ls = 0; ls < L; ls++) na += sh.act[kp][ls] ? 1.0 : 0.0;
-      if (!ring_sums<1>(sh, L, sc_lo, n_sc, na, part_1, part_g1, gb)) alive = false;
+      if (!ring_sums<1>(sh, L, sc_lo, n_sc, na, part_1, part_g1, gb, prof ? prof + 3 : nullptr)) alive = false;
     }
     if (!alive || sh.g == 0.0) break;
     if (timer) {
@@ -1311,6 +1325,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
       asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_b));
       prof[0] += t_b - t_a;
       prof[1] += 1;
+      prof[2] += sh.tmax - t_a;  // up to the last CTA's end of the SpMV work
     }
     // ---- d += alpha p, r -= alpha q, z = M^-1 r, r.z, r.r: kUB slices per
     // batch, all loads of a batch issued before any use
@@ -1908,6 +1923,7 @@ od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::ve
   MixedSys* m = new MixedSys();
   const int n = (int)scenes.size();
   m->n_sc = n;
+  m->scenes = scenes;
   m->sc_slice.assign(1, 0);
   m->off_host.assign(1, 0);
   std::vector<int> dirs(4 * (n + 1), 0);
@@ -1965,8 +1981,8 @@ od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::ve
   if (e == cudaSuccess) e = cudaMalloc(&m->res_part, sizeof(double) * 2 * std::max(1, pres[n]));
   if (e == cudaSuccess) e = cudaMalloc(&m->gbar, sizeof(GridBarrier));
   if (e == cudaSuccess) e = cudaMallocHost(&m->timeout_host, sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc(&m->prof, 2 * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMallocHost(&m->prof_host, 2 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&m->prof, (3 + (size_t)ctx->num_sms) * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMallocHost(&m->prof_host, 3 * sizeof(unsigned long long));
   if (e != cudaSuccess) return fail(cuda_fail(e, "mixed_build"));
   if ((st = mixed_partition(m, G)) != OD_OK) return fail(st);
   *out = m;
@@ -2049,7 +2065,7 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
     OD_CUDA(cudaMemsetAsync(m->gbar, 0, sizeof(GridBarrier), strm));
     GridBarrier* gbp = (GridBarrier*)m->gbar;
     unsigned long long* profp = prof ? m->prof : nullptr;
-    if (prof) OD_CUDA(cudaMemsetAsync(m->prof, 0, 2 * sizeof(unsigned long long), strm));
+    if (prof) OD_CUDA(cudaMemsetAsync(m->prof, 0, 3 * sizeof(unsigned long long), strm));
     int pkv = pk, nsc = n_sc;
     void* args[] = {(void*)&nsc,       (void*)&m->cta_first, (void*)&m->cta_sc_lo, (void*)&m->sc_cta,
                     (void*)&m->sc_slice_dev, (void*)&m->desc, (void*)&m->ring,    (void*)&pkv,
@@ -2077,8 +2093,9 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
       OD_CUDA(cudaEventElapsedTime(&ms, ctx->ev_pool[0], ctx->ev_pool[1]));
       ctx->pcg_kernel_ms += ms;
       ctx->pcg_kernel_launches++;
-      OD_CUDA(cudaMemcpy(m->prof_host, m->prof, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+      OD_CUDA(cudaMemcpy(m->prof_host, m->prof, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
       ctx->mix_spmv_ms += 1e-6 * (double)m->prof_host[0];
+      ctx->mix_spmv_work_ms += 1e-6 * (double)m->prof_host[2];
       ctx->mix_iters += (long long)m->prof_host[1];
       for (int s = 0; s < n_sc; s++)
         if (need[s]) ctx->mix_spmv_bytes += (double)m->ring_host[s].iters * m->sc_bytes[s];
@@ -2096,6 +2113,24 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
   }
   for (int s = 0; s < n_sc; s++) {
     if (status[s] == OD_OK && rr[s] > eps[s] && m->sc_nb[s] > 0) status[s] = OD_ERR_NOT_CONVERGED;
+    if ((status[s] == OD_ERR_NOT_CONVERGED || status[s] == OD_ERR_NAN) && rc == OD_OK) {
+      // the FP32 inner solve could not carry the refinement (FP32 operator too
+      // far from the FP64 one for this system): finish with the FP64 PCG from
+      // the current iterate, same tolerance and preconditioner
+      od_solver_params p64 = prm[s];
+      p64.precision = OD_PRECISION_FP64;
+      p64.max_iter = std::max(1, prm[s].max_iter);
+      const MixDesc& D = m->desc_host[s];
+      od_solve_stats s64{};
+      if (!std::isfinite(rr[s])) OD_CUDA(cudaMemsetAsync(D.x, 0, sizeof(double) * 3 * (size_t)D.nb, strm));
+      const od_status rc64 = pcg_solve(m->scenes[s], D.b, D.x, &p64, &s64);
+      ctx->mix_fallbacks++;
+      if (rc64 == OD_OK) {
+        total[s] += s64.iterations;
+        status[s] = s64.status;
+        rr[s] = s64.rel_residual * s64.rel_residual * (bb[s] > 0.0 ? bb[s] : 1.0);
+      }
+    }
     st[s].iterations = total[s];
     st[s].refinements = sweeps[s];
     st[s].rel_residual = bb[s] > 0.0 ? std::sqrt(rr[s] / bb[s]) : std::sqrt(rr[s]);
