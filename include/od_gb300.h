@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define OD_ABI_VERSION 3
+#define OD_ABI_VERSION 4
 
 typedef enum od_status {
   OD_OK = 0,
@@ -46,7 +46,8 @@ typedef enum od_status {
 typedef enum od_material_kind {
   OD_MATERIAL_COROTATIONAL = 0, /* material/corotationalHyperelastic.h:11-21 */
   OD_MATERIAL_NEOHOOKEAN = 1,   /* material/invertibleNeoHookean.h */
-  OD_MATERIAL_STVK = 2          /* material/invertibleStVK.h */
+  OD_MATERIAL_STVK = 2,         /* material/invertibleStVK.h */
+  OD_MATERIAL_COROTATIONAL_PLASTIC = 3  /* material/corotationalPlastic.h:11-30 */
 } od_material_kind;
 
 typedef enum od_precond_kind {
@@ -75,6 +76,11 @@ typedef struct od_material {
   double youngs;     /* E, Pa */
   double poisson;    /* nu */
   double threshold;  /* corotational compressing threshold / invertible inversion threshold */
+  /* corotational plastic only (CorotationalPlasticMaterial ctor,
+     corotationalPlastic.cpp:8-22): */
+  double yield_criterion;     /* elastic-strain norm above which plastic strain grows */
+  double creep_ratio;         /* share of the excess strain moved to plastic strain per evaluation */
+  double max_plastic_strain;  /* cap on the plastic-strain norm */
 } od_material;
 
 typedef struct od_solver_params {
@@ -235,6 +241,13 @@ od_status od_scene_get_external_forces(od_scene* scene, double* f_ext);
 /* Integrator (NonlinearImplicitBackwardEuler ctor, nonlinearImplicitBackwardEuler.h:48-73,
  * or the full-order Newmark).  Resets the state to rest. */
 od_status od_integrator_setup(od_scene* scene, const od_integrator_params* params);
+
+/* Plastic strain of a corotational plastic scene, 9 per element (row-major),
+ * in the caller's element order.  The reference keeps it in the material's
+ * precompute cache (corotationalPlastic.cpp:46-47) and updates it at every
+ * evaluation of the element forces. */
+od_status od_scene_get_plastic_strain(od_scene* scene, double* plastic);
+od_status od_scene_set_plastic_strain(od_scene* scene, const double* plastic);
 /* Change the parameters of the set-up integrator (same kind) and keep the
  * state (d, v, a, time); no reference counterpart (the reference fixes them
  * in the integrator's constructor). */

@@ -39,7 +39,7 @@ STATUS = {0: "OD_OK", 1: "OD_ERR_INVALID_ARG", 2: "OD_ERR_OUT_OF_MEMORY", 3: "OD
           4: "OD_ERR_NAN", 5: "OD_ERR_DEVICE_TIMEOUT", 6: "OD_ERR_CUDA", 7: "OD_ERR_UNSUPPORTED",
           8: "OD_ERR_INTERNAL"}
 
-MATERIAL_KIND = {"corotational": 0, "neohookean": 1, "stvk": 2}
+MATERIAL_KIND = {"corotational": 0, "neohookean": 1, "stvk": 2, "corotational_plastic": 3}
 PRECOND_KIND = {"none": 0, "jacobi": 1, "block_jacobi": 2, "ic0": 3}
 PRECISION = {"fp64": 0, "mixed": 1}
 
@@ -52,7 +52,8 @@ class ODError(RuntimeError):
 
 class od_material(C.Structure):
     _fields_ = [("kind", C.c_int), ("density", C.c_double), ("youngs", C.c_double),
-                ("poisson", C.c_double), ("threshold", C.c_double)]
+                ("poisson", C.c_double), ("threshold", C.c_double), ("yield_criterion", C.c_double),
+                ("creep_ratio", C.c_double), ("max_plastic_strain", C.c_double)]
 
 
 class od_solver_params(C.Structure):
@@ -158,6 +159,8 @@ SIGNATURES = {
     "od_get_state": (C.c_int, [_vp, _dp, _dp, _dp]),
     "od_set_state": (C.c_int, [_vp, _dp, _dp, _dp]),
     "od_integrator_update": (C.c_int, [_vp, C.POINTER(od_integrator_params)]),
+    "od_scene_get_plastic_strain": (C.c_int, [_vp, _dp]),
+    "od_scene_set_plastic_strain": (C.c_int, [_vp, _dp]),
     "od_batch_create": (C.c_int, [_vp, C.c_int, C.POINTER(_vp), C.POINTER(_vp)]),
     "od_batch_step": (C.c_int, [_vp, C.c_int, C.POINTER(od_step_stats)]),
     "od_batch_destroy": (C.c_int, [_vp]),
@@ -207,9 +210,13 @@ class Material:
     youngs: float
     poisson: float
     threshold: float
+    yield_criterion: float = 0.0      # corotational plastic only
+    creep_ratio: float = 0.0
+    max_plastic_strain: float = 0.0
 
     def to_c(self):
-        return od_material(MATERIAL_KIND[self.kind], self.density, self.youngs, self.poisson, self.threshold)
+        return od_material(MATERIAL_KIND[self.kind], self.density, self.youngs, self.poisson, self.threshold,
+                           self.yield_criterion, self.creep_ratio, self.max_plastic_strain)
 
 
 def CorotationalHyperelasticMaterial(rho, youngs, poisson, compressingThreshold):
@@ -222,6 +229,13 @@ def InvertibleNeoHookeanMaterial(rho, youngs, poisson, inversionThreshold):
 
 def InvertibleStVKMaterial(rho, youngs, poisson, inversionThreshold):
     return Material("stvk", rho, youngs, poisson, inversionThreshold)
+
+
+def CorotationalPlasticMaterial(rho, youngs, poisson, yieldCriterion, creepRatio, maxPlasticStrain,
+                                compressingThreshold):
+    """CorotationalPlasticMaterial (material/corotationalPlastic.h:11-30), same argument order."""
+    return Material("corotational_plastic", rho, youngs, poisson, compressingThreshold, yieldCriterion, creepRatio,
+                    maxPlasticStrain)
 
 
 @dataclasses.dataclass
@@ -373,6 +387,16 @@ class Scene:
     def set_displacements(self, u):
         u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1, 3)
         _check(load_library().od_scene_set_displacements(self.h, _d(u)), "set_displacements")
+
+    def plastic_strain(self):
+        """Plastic strain of a corotational plastic scene, (n_tets, 9) row-major."""
+        out = np.zeros((self.n_tets, 9))
+        _check(load_library().od_scene_get_plastic_strain(self.h, _d(out)), "get_plastic_strain")
+        return out
+
+    def set_plastic_strain(self, plastic):
+        p = np.ascontiguousarray(plastic, dtype=np.float64).reshape(self.n_tets, 9)
+        _check(load_library().od_scene_set_plastic_strain(self.h, _d(p)), "set_plastic_strain")
 
     def info_now(self):
         """od_scene_get_info now (device_bytes grows with the first mixed solve)."""

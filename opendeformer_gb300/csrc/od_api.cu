@@ -228,7 +228,7 @@ static void scene_free(Scene* s) {
                   (void*)s->dv, (void*)s->rhs, (void*)s->tmp, (void*)s->trac_facets, (void*)s->trac_vec,
                   (void*)s->bsr.row_ptr, (void*)s->bsr.col, (void*)s->bsr.desc_off, (void*)s->bsr.desc_kind,
                   (void*)s->bsr.gen, (void*)s->bsr.diag_pos, (void*)s->tmp2, (void*)s->stage_k,
-                  (void*)s->stage_f, (void*)s->color_off_dev})
+                  (void*)s->stage_f, (void*)s->color_off_dev, (void*)s->plastic})
     if (p) cudaFree(p);
   pcg_free(s);
   if (s->ev_step[0]) { cudaEventDestroy(s->ev_step[0]); cudaEventDestroy(s->ev_step[1]); }
@@ -288,8 +288,12 @@ static od_status scene_build(Scene* s, int n_nodes, const double* X, int n_tets,
   OD_TRY(dupload(s, &s->node_dof, s->hnode_dof.data(), s->hnode_dof.size()));
   OD_TRY(dupload(s, &s->facets_dev, s->hfacets.data(), s->hfacets.size()));
   OD_TRY(dalloc(s, &s->node_vol4, (size_t)n_nodes));
-  s->n_pre = s->mat.kind == OD_MATERIAL_COROTATIONAL ? 100 : 22;
+  s->n_pre = s->mat.kind == OD_MATERIAL_COROTATIONAL ? 100 : (s->mat.kind == OD_MATERIAL_COROTATIONAL_PLASTIC ? 112 : 22);
   OD_TRY(dalloc(s, &s->pre, (size_t)s->n_pre * ne));
+  if (s->mat.kind == OD_MATERIAL_COROTATIONAL_PLASTIC) {  // zero plastic strain (corotationalPlastic.cpp:46-47)
+    OD_TRY(dalloc(s, &s->plastic, 9 * (size_t)ne));
+    OD_CUDA(cudaMemset(s->plastic, 0, sizeof(double) * 9 * std::max<size_t>(1, ne)));
+  }
   // matrices (reference layout) and full BSR
   OD_TRY(dalloc(s, &s->K, (size_t)s->nvals));
   OD_TRY(dalloc(s, &s->M, (size_t)s->nvals));
@@ -334,7 +338,10 @@ od_status od_scene_create(od_ctx* ctx, int n_nodes, const double* X, int n_tets,
   OD_CHECK_ARG(n_tets >= 0 && (n_tets == 0 || tets), "od_scene_create: bad element list");
   OD_CHECK_ARG(n_facets >= 0 && (n_facets == 0 || facets), "od_scene_create: bad facet list");
   OD_CHECK_ARG(n_cdofs >= 0 && (n_cdofs == 0 || cdofs), "od_scene_create: bad constraint list");
-  OD_CHECK_ARG(mat->kind >= 0 && mat->kind <= 2, "od_scene_create: unknown material kind");
+  OD_CHECK_ARG(mat->kind >= 0 && mat->kind <= 3, "od_scene_create: unknown material kind");
+  OD_CHECK_ARG(mat->kind != OD_MATERIAL_COROTATIONAL_PLASTIC ||
+                   (mat->yield_criterion >= 0.0 && mat->creep_ratio >= 0.0 && mat->max_plastic_strain >= 0.0),
+               "od_scene_create: plastic parameters must be non-negative");
   OD_CHECK_ARG(mat->density > 0 && mat->youngs > 0 && mat->poisson > -1.0 && mat->poisson < 0.5,
                "od_scene_create: material parameters out of range");
   if ((long long)n_nodes * 3 > 0x7fffffffLL) { set_error("od_scene_create: too many nodes"); return OD_ERR_UNSUPPORTED; }
@@ -765,15 +772,20 @@ od_status od_set_state(od_scene* scene, const double* d, const double* v, const 
 // blob: magic, version, n_nodes, dofs, time, u (3 n_nodes), d, v, a, dv, f_ext (dofs each)
 static const uint64_t kMagic = 0x3130305344474f44ull;  // "DOGSD001"
 
+static size_t blob_size(const Scene* s) {
+  return 4 * sizeof(uint64_t) +
+         sizeof(double) * (1 + 3 * (size_t)s->n_nodes + 5 * (size_t)s->dofs + (s->plastic ? 9 * (size_t)s->n_tets : 0));
+}
+
 od_status od_scene_save(od_scene* scene, void* buf, size_t* size) {
   OD_CHECK_ARG(scene && size, "od_scene_save: NULL argument");
   Scene* s = &scene->s;
-  const size_t need = 4 * sizeof(uint64_t) + sizeof(double) * (1 + 3 * (size_t)s->n_nodes + 5 * (size_t)s->dofs);
+  const size_t need = blob_size(s);
   if (!buf) { *size = need; return OD_OK; }
   OD_CHECK_ARG(*size >= need, "od_scene_save: buffer too small");
   OD_CUDA(cudaSetDevice(s->ctx->device));
   uint64_t* hd = (uint64_t*)buf;
-  hd[0] = kMagic; hd[1] = 1; hd[2] = (uint64_t)s->n_nodes; hd[3] = (uint64_t)s->dofs;
+  hd[0] = kMagic; hd[1] = s->plastic ? 2 : 1; hd[2] = (uint64_t)s->n_nodes; hd[3] = (uint64_t)s->dofs;
   double* p = (double*)(hd + 4);
   p[0] = s->time;
   p += 1;
@@ -784,6 +796,7 @@ od_status od_scene_save(od_scene* scene, void* buf, size_t* size) {
     OD_CUDA(cudaMemcpyAsync(p, v, sizeof(double) * s->dofs, cudaMemcpyDeviceToHost, st));
     p += s->dofs;
   }
+  if (s->plastic) OD_CUDA(cudaMemcpyAsync(p, s->plastic, sizeof(double) * 9 * s->n_tets, cudaMemcpyDeviceToHost, st));
   OD_TRY(sync_stream(s));
   *size = need;
   return OD_OK;
@@ -792,10 +805,10 @@ od_status od_scene_save(od_scene* scene, void* buf, size_t* size) {
 od_status od_scene_load(od_scene* scene, const void* buf, size_t size) {
   OD_CHECK_ARG(scene && buf, "od_scene_load: NULL argument");
   Scene* s = &scene->s;
-  const size_t need = 4 * sizeof(uint64_t) + sizeof(double) * (1 + 3 * (size_t)s->n_nodes + 5 * (size_t)s->dofs);
+  const size_t need = blob_size(s);
   OD_CHECK_ARG(size >= need, "od_scene_load: blob too small");
   const uint64_t* hd = (const uint64_t*)buf;
-  OD_CHECK_ARG(hd[0] == kMagic && hd[1] == 1, "od_scene_load: not a scene blob");
+  OD_CHECK_ARG(hd[0] == kMagic && hd[1] == (s->plastic ? 2u : 1u), "od_scene_load: not a blob of this kind of scene");
   OD_CHECK_ARG(hd[2] == (uint64_t)s->n_nodes && hd[3] == (uint64_t)s->dofs, "od_scene_load: blob is for another scene");
   OD_CUDA(cudaSetDevice(s->ctx->device));
   const double* p = (const double*)(hd + 4);
@@ -808,6 +821,37 @@ od_status od_scene_load(od_scene* scene, const void* buf, size_t size) {
     OD_CUDA(cudaMemcpyAsync(v, p, sizeof(double) * s->dofs, cudaMemcpyHostToDevice, st));
     p += s->dofs;
   }
+  if (s->plastic) OD_CUDA(cudaMemcpyAsync(s->plastic, p, sizeof(double) * 9 * s->n_tets, cudaMemcpyHostToDevice, st));
+  OD_TRY(sync_stream(s));
+  return OD_OK;
+}
+
+// plastic strain in the caller's element order (the device keeps it [9][tet]
+// in colour order)
+od_status od_scene_get_plastic_strain(od_scene* scene, double* out) {
+  OD_CHECK_ARG(scene && out, "od_scene_get_plastic_strain: NULL argument");
+  Scene* s = &scene->s;
+  OD_CHECK_ARG(s->plastic, "od_scene_get_plastic_strain: not a plastic scene");
+  OD_CUDA(cudaSetDevice(s->ctx->device));
+  std::vector<double> h(9 * (size_t)s->n_tets);
+  OD_CUDA(cudaMemcpyAsync(h.data(), s->plastic, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s->ctx->stream));
+  OD_TRY(sync_stream(s));
+  const size_t ne = s->n_tets;
+  for (size_t k = 0; k < ne; k++)
+    for (int i = 0; i < 9; i++) out[9 * (size_t)s->elem_perm[k] + i] = h[(size_t)i * ne + k];
+  return OD_OK;
+}
+
+od_status od_scene_set_plastic_strain(od_scene* scene, const double* in) {
+  OD_CHECK_ARG(scene && in, "od_scene_set_plastic_strain: NULL argument");
+  Scene* s = &scene->s;
+  OD_CHECK_ARG(s->plastic, "od_scene_set_plastic_strain: not a plastic scene");
+  OD_CUDA(cudaSetDevice(s->ctx->device));
+  const size_t ne = s->n_tets;
+  std::vector<double> h(9 * ne);
+  for (size_t k = 0; k < ne; k++)
+    for (int i = 0; i < 9; i++) h[(size_t)i * ne + k] = in[9 * (size_t)s->elem_perm[k] + i];
+  OD_CUDA(cudaMemcpyAsync(s->plastic, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, s->ctx->stream));
   OD_TRY(sync_stream(s));
   return OD_OK;
 }

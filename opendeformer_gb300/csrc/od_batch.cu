@@ -64,7 +64,7 @@ struct Batch {
   std::vector<SceneDev> sd_host;
   SceneDev* sd = nullptr;
   int* dirs = nullptr;  // all tile-directory prefixes in one allocation
-  TileDir zero_k, zero_f, corot, inv, expand, rows, dof;
+  TileDir zero_k, zero_f, corot, inv, plastic, expand, rows, dof;
   std::vector<TileDir> scatter;  // per colour
   MixedSys* mix = nullptr;
   int newton = 1, precond = OD_PRECOND_BLOCK_JACOBI;
@@ -95,6 +95,10 @@ static SceneDev scene_dev(const Scene* s) {
   D.thr = s->mat.threshold;
   D.lambda = s->lambda;
   D.mu = s->mu;
+  D.yield = s->mat.yield_criterion;
+  D.creep = s->mat.creep_ratio;
+  D.max_plastic = s->mat.max_plastic_strain;
+  D.plastic = s->plastic;
   D.tets = s->tets;
   D.X = s->X;
   D.u = s->u;
@@ -142,21 +146,23 @@ static od_status batch_build(Batch* B) {
   const int n = (int)B->sc.size();
   int max_colors = 0;
   for (const Scene* s : B->sc) max_colors = std::max(max_colors, (int)s->color_off.size() - 1);
-  const int n_dirs = 7 + max_colors;
+  const int n_dirs = 8 + max_colors;
   std::vector<int> pre((size_t)n_dirs * (n + 1), 0);
   auto P = [&](int d) { return pre.data() + (size_t)d * (n + 1); };
   for (int i = 0; i < n; i++) {
     const Scene* s = B->sc[i];
     B->sd_host.push_back(scene_dev(s));
-    const bool corot = s->mat.kind == OD_MATERIAL_COROTATIONAL;
-    const int counts[7] = {ceil_div(s->nvals, kZeroTileValues), ceil_div(s->pcg.n_pad, kZeroTileValues),
-                           corot ? ceil_div(s->n_tets, 128) : 0, corot ? 0 : ceil_div(s->n_tets, 128),
+    const int kind = s->mat.kind;
+    const bool corot = kind == OD_MATERIAL_COROTATIONAL, plastic = kind == OD_MATERIAL_COROTATIONAL_PLASTIC;
+    const int et = ceil_div(s->n_tets, 128);
+    const int counts[8] = {ceil_div(s->nvals, kZeroTileValues), ceil_div(s->pcg.n_pad, kZeroTileValues),
+                           corot ? et : 0, corot || plastic ? 0 : et, plastic ? et : 0,
                            ceil_div(9LL * s->bsr.nnzb, kExpandTile), ceil_div(s->bsr.nb, kBatchRows),
                            ceil_div(s->pcg.n_pad, 256)};
-    for (int d = 0; d < 7; d++) P(d)[i + 1] = P(d)[i] + counts[d];
+    for (int d = 0; d < 8; d++) P(d)[i + 1] = P(d)[i] + counts[d];
     for (int c = 0; c < max_colors; c++) {
       const int cnt = c + 1 < (int)s->color_off.size() ? s->color_off[c + 1] - s->color_off[c] : 0;
-      P(7 + c)[i + 1] = P(7 + c)[i] + ceil_div(90LL * cnt, 256);
+      P(8 + c)[i + 1] = P(8 + c)[i] + ceil_div(90LL * cnt, 256);
     }
   }
   OD_CUDA(cudaMalloc(&B->dirs, sizeof(int) * pre.size()));
@@ -166,10 +172,11 @@ static od_status batch_build(Batch* B) {
   B->zero_f = dir(1, kZeroTileValues);
   B->corot = dir(2, 128);
   B->inv = dir(3, 128);
-  B->expand = dir(4, kExpandTile);
-  B->rows = dir(5, kBatchRows);
-  B->dof = dir(6, 256);
-  for (int c = 0; c < max_colors; c++) B->scatter.push_back(dir(7 + c, 256));
+  B->plastic = dir(4, 128);
+  B->expand = dir(5, kExpandTile);
+  B->rows = dir(6, kBatchRows);
+  B->dof = dir(7, 256);
+  for (int c = 0; c < max_colors; c++) B->scatter.push_back(dir(8 + c, 256));
   OD_CUDA(cudaMalloc(&B->sd, sizeof(SceneDev) * std::max(1, n)));
   OD_CUDA(cudaMemcpy(B->sd, B->sd_host.data(), sizeof(SceneDev) * n, cudaMemcpyHostToDevice));
   std::vector<const double*> rhs;
@@ -206,7 +213,7 @@ static od_status batch_step(Batch* B, std::vector<od_step_stats>& acc) {
   for (int it = 0; it < B->newton; it++) {
     OD_TRY(nm_op(B, NM_STAGE));
     const int n = (int)B->sc.size();
-    OD_TRY(launch_eval_batch(ctx, n, B->sd, B->zero_k, B->zero_f, B->corot, B->inv, B->scatter));
+    OD_TRY(launch_eval_batch(ctx, n, B->sd, B->zero_k, B->zero_f, B->corot, B->inv, B->plastic, B->scatter));
     OD_TRY(launch_spmv_lower_batch(ctx, n, B->sd, B->rows));
     OD_TRY(nm_op(B, NM_RESIDUAL));
     OD_TRY(launch_expand_batch(ctx, n, B->sd, B->expand));

@@ -57,7 +57,7 @@ __global__ void precompute_kernel(int ne, int kind, const int4* __restrict__ tet
   Di[6] = (Dm[3] * Dm[7] - Dm[4] * Dm[6]) * inv;
   Di[7] = (Dm[1] * Dm[6] - Dm[0] * Dm[7]) * inv;
   Di[8] = (Dm[0] * Dm[4] - Dm[1] * Dm[3]) * inv;
-  if (kind == OD_MATERIAL_COROTATIONAL) {
+  if (kind == OD_MATERIAL_COROTATIONAL || kind == OD_MATERIAL_COROTATIONAL_PLASTIC) {
     const double f = 1.0 / (36.0 * vol);
     int k = 0;
     for (int a = 0; a < 4; a++) {
@@ -78,6 +78,12 @@ __global__ void precompute_kernel(int ne, int kind, const int4* __restrict__ tet
     }
     for (int i = 0; i < 9; i++) pre[(size_t)(90 + i) * ne + e] = Di[i];
     pre[(size_t)99 * ne + e] = vol;
+    if (kind == OD_MATERIAL_COROTATIONAL_PLASTIC)  // shape derivatives for the stress forces
+      for (int a = 0; a < 4; a++) {
+        pre[(size_t)(100 + 3 * a) * ne + e] = g[a].x;
+        pre[(size_t)(101 + 3 * a) * ne + e] = g[a].y;
+        pre[(size_t)(102 + 3 * a) * ne + e] = g[a].z;
+      }
   } else {
     for (int a = 0; a < 4; a++) {
       pre[(size_t)(3 * a) * ne + e] = g[a].x;
@@ -509,6 +515,183 @@ __global__ void __launch_bounds__(128) invhyper_batch_kernel(int n_sc, const int
                    D.gdof, nullptr, nullptr, D.stage_k, D.stage_f, nullptr);
 }
 
+// Corotational plastic element (corotationalPlastic.cpp:53-183,
+// tetelement.cpp:654-729).  F = R S: polar decomposition (S = R^T F), or QR
+// when the deformed volume falls below threshold x rest volume (S = Q^T F,
+// the upper factor).  Elastic strain e = sym(S) - I - plastic strain; stress
+// 2 mu e + lambda tr(e) I, rotated by R; forces f_a = (R stress) dN_a / 6
+// (a < 3), f_3 = -(f_0 + f_1 + f_2); stiffness R K0_ab R^T.  Every
+// evaluation updates the element's plastic strain (in place, as the
+// reference does): when the strain norm exceeds the yield criterion it grows
+// by creep (|e| - yield)/|e| e and is scaled back to the maximum.  Both
+// norms follow the reference, which adds the squares of the first three
+// entries three times (corotationalPlastic.cpp:156-160, 169-173).
+// pre: [90 K0][9 Dm^-1][V][12 dN] per element (SoA); plastic: [9][ne].
+template <int MODE>
+__device__ __forceinline__ void plastic_elem(int e, int ne, const int4* __restrict__ tets,
+                                             const double* __restrict__ X, const double* __restrict__ u,
+                                             const double* __restrict__ pre, double thr, double lambda, double mu,
+                                             double yield, double creep, double max_plastic,
+                                             double* __restrict__ plastic, double* __restrict__ out78,
+                                             double* __restrict__ out12, const int* __restrict__ perm) {
+  int4 t = tets[e];
+  const int nd[4] = {t.x, t.y, t.z, t.w};
+  V3t<double> c[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    V3t<double> x = ld3(X, nd[i]), du = ld3(u, nd[i]);
+    c[i] = {x.x + du.x, x.y + du.y, x.z + du.z};
+  }
+  double F[9];
+#pragma unroll
+  for (int i = 0; i < 9; i++) F[i] = 0.0;
+#pragma unroll
+  for (int i = 1; i < 4; i++) {
+    double ax[3] = {c[i].x - c[0].x, c[i].y - c[0].y, c[i].z - c[0].z};
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) F[j * 3 + k] += ax[j] * pre[(size_t)(90 + (i - 1) * 3 + k) * ne + e];
+  }
+  const double v0 = pre[(size_t)99 * ne + e];
+  const double v1 = tet_vol(c[0], c[1], c[2], c[3]);
+  double R[9], S[9];
+  if (v1 >= thr * v0) polar3<double>(F, R);
+  else qr3<double>(F, R);
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) S[i * 3 + j] = R[i] * F[j] + R[3 + i] * F[3 + j] + R[6 + i] * F[6 + j];
+  // elastic strain, stress, plastic update (computeElasticStress)
+  double ep[9], es[9];
+#pragma unroll
+  for (int i = 0; i < 9; i++) ep[i] = plastic[(size_t)i * ne + e];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) es[i * 3 + j] = 0.5 * (S[i * 3 + j] + S[j * 3 + i]) - ep[i * 3 + j];
+  es[0] -= 1.0;
+  es[4] -= 1.0;
+  es[8] -= 1.0;
+  const double mu2 = 2.0 * mu;
+  double st[9];
+#pragma unroll
+  for (int i = 0; i < 9; i++) st[i] = mu2 * es[i];
+  const double dg = lambda * (es[0] + es[4] + es[8]);
+  st[0] += dg;
+  st[4] += dg;
+  st[8] += dg;
+  double P[9];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) P[i * 3 + j] = R[i * 3] * st[j] + R[i * 3 + 1] * st[3 + j] + R[i * 3 + 2] * st[6 + j];
+  double en = 0.0;  // the reference's sum: each of the first three squares three times, in its order
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    en += es[i] * es[i];
+    en += es[i] * es[i];
+    en += es[i] * es[i];
+  }
+  en = sqrt(en);
+  if (en > yield) {
+    const double ratio = creep * (en - yield) / en;
+#pragma unroll
+    for (int i = 0; i < 9; i++) ep[i] += ratio * es[i];
+    double pn = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      pn += ep[i] * ep[i];
+      pn += ep[i] * ep[i];
+      pn += ep[i] * ep[i];
+    }
+    pn = sqrt(pn);
+    if (pn > max_plastic) {
+      const double fac = max_plastic / pn;
+#pragma unroll
+      for (int i = 0; i < 9; i++) ep[i] *= fac;
+    }
+#pragma unroll
+    for (int i = 0; i < 9; i++) plastic[(size_t)i * ne + e] = ep[i];
+  }
+  auto put = [&](int k, double val) {
+    if (MODE == 1) out78[(size_t)perm[e] * 78 + k] = val;
+    else out78[(size_t)k * ne + e] = val;
+  };
+  int blk = 0;
+#pragma unroll 1
+  for (int a = 0; a < 4; a++) {
+#pragma unroll 1
+    for (int b = a; b < 4; b++) {
+      double K0[9], QK[9], QKQT[9];
+#pragma unroll
+      for (int i = 0; i < 9; i++) K0[i] = pre[(size_t)(9 * blk + i) * ne + e];
+      blk++;
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) QK[i * 3 + j] = R[i * 3] * K0[j] + R[i * 3 + 1] * K0[3 + j] + R[i * 3 + 2] * K0[6 + j];
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+          QKQT[i * 3 + j] = QK[i * 3] * R[j * 3] + QK[i * 3 + 1] * R[j * 3 + 1] + QK[i * 3 + 2] * R[j * 3 + 2];
+      if (a == b) {
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3 - i; j++) put(c_diag12[a * 3 + i] + j, QKQT[i * 3 + i + j]);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++) put(c_diag12[a * 3 + i] + (b - a) * 3 - i + j, QKQT[i * 3 + j]);
+      }
+    }
+  }
+  double f[12];
+  const double sixth = 1.0 / 6.0;
+#pragma unroll
+  for (int n = 0; n < 3; n++) {
+    const double x = pre[(size_t)(100 + 3 * n) * ne + e], y = pre[(size_t)(101 + 3 * n) * ne + e],
+                 z = pre[(size_t)(102 + 3 * n) * ne + e];
+#pragma unroll
+    for (int i = 0; i < 3; i++) f[3 * n + i] = (P[i * 3] * x + P[i * 3 + 1] * y + P[i * 3 + 2] * z) * sixth;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) f[9 + i] = -(f[i] + f[3 + i] + f[6 + i]);
+  if (MODE == 1) {
+#pragma unroll
+    for (int k = 0; k < 12; k++) out12[(size_t)perm[e] * 12 + k] = f[k];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 12; k++) out12[(size_t)k * ne + e] = f[k];
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128) plastic_kernel(int ne, const int4* __restrict__ tets,
+                                                      const double* __restrict__ X, const double* __restrict__ u,
+                                                      const double* __restrict__ pre, double thr, double lambda,
+                                                      double mu, double yield, double creep, double max_plastic,
+                                                      double* __restrict__ plastic, double* __restrict__ out78,
+                                                      double* __restrict__ out12, const int* __restrict__ perm) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < ne)
+    plastic_elem<MODE>(e, ne, tets, X, u, pre, thr, lambda, mu, yield, creep, max_plastic, plastic, out78, out12,
+                       perm);
+}
+
+__global__ void __launch_bounds__(128) plastic_batch_kernel(int n_sc, const int* __restrict__ prefix,
+                                                            const SceneDev* __restrict__ sd) {
+  const int s = dir_scene(prefix, n_sc, blockIdx.x);
+  const SceneDev& D = sd[s];
+  const int e = (blockIdx.x - prefix[s]) * 128 + threadIdx.x;
+  if (e >= D.n_tets) return;
+  plastic_elem<2>(e, D.n_tets, D.tets, D.X, D.u, D.pre, D.thr, D.lambda, D.mu, D.yield, D.creep, D.max_plastic,
+                  D.plastic, D.stage_k, D.stage_f, nullptr);
+}
+
 // atomic-free scatter of staged element values, one colour per launch
 // (corotationalHyperelastic.cpp:100-120): no two elements of a colour share
 // a matrix value or a force entry.  One thread per (element, entry): entries
@@ -576,7 +759,9 @@ od_status launch_precompute(Scene* s) {
   return OD_OK;
 }
 
-static int vol_slot(const Scene* s) { return s->mat.kind == OD_MATERIAL_COROTATIONAL ? 99 : 21; }
+static int vol_slot(const Scene* s) {
+  return s->mat.kind == OD_MATERIAL_COROTATIONAL || s->mat.kind == OD_MATERIAL_COROTATIONAL_PLASTIC ? 99 : 21;
+}
 
 od_status launch_mass(Scene* s) {
   const int T = 128;
@@ -606,7 +791,12 @@ od_status launch_eval(Scene* s, bool zero_first) {
   if (s->n_tets == 0) return OD_OK;
   // 1) every element at full occupancy into the colour-ordered staging arrays
   OD_KL(s);
-  if (s->mat.kind == OD_MATERIAL_COROTATIONAL)
+  if (s->mat.kind == OD_MATERIAL_COROTATIONAL_PLASTIC)
+    plastic_kernel<2><<<nblk(s->n_tets, T), T, 0, st>>>(s->n_tets, s->tets, s->X, s->u, s->pre, s->mat.threshold,
+                                                         s->lambda, s->mu, s->mat.yield_criterion,
+                                                         s->mat.creep_ratio, s->mat.max_plastic_strain, s->plastic,
+                                                         s->stage_k, s->stage_f, nullptr);
+  else if (s->mat.kind == OD_MATERIAL_COROTATIONAL)
     corot_kernel<2><<<nblk(s->n_tets, T), T, 0, st>>>(0, s->n_tets, s->n_tets, s->tets, s->X, s->u, s->pre,
                                                        s->mat.threshold, s->emap, s->gdof, nullptr, nullptr, s->stage_k,
                                                        s->stage_f, nullptr);
@@ -632,7 +822,12 @@ od_status launch_element_values(Scene* s, double* d_k78, double* d_f12) {
   cudaStream_t st = s->ctx->stream;
   if (s->n_tets == 0) return OD_OK;
   OD_KL(s);
-  if (s->mat.kind == OD_MATERIAL_COROTATIONAL)
+  if (s->mat.kind == OD_MATERIAL_COROTATIONAL_PLASTIC)
+    plastic_kernel<1><<<nblk(s->n_tets, T), T, 0, st>>>(s->n_tets, s->tets, s->X, s->u, s->pre, s->mat.threshold,
+                                                         s->lambda, s->mu, s->mat.yield_criterion,
+                                                         s->mat.creep_ratio, s->mat.max_plastic_strain, s->plastic,
+                                                         d_k78, d_f12, s->perm);
+  else if (s->mat.kind == OD_MATERIAL_COROTATIONAL)
     corot_kernel<1><<<nblk(s->n_tets, T), T, 0, st>>>(0, s->n_tets, s->n_tets, s->tets, s->X, s->u, s->pre,
                                                        s->mat.threshold, s->emap, s->gdof, nullptr, nullptr, d_k78,
                                                        d_f12, s->perm);
@@ -674,7 +869,8 @@ od_status launch_loads(Scene* s, const double* body, int n_facets_total, double 
 namespace od {
 
 od_status launch_eval_batch(Ctx* ctx, int n_sc, const SceneDev* sd, const TileDir& zero_k, const TileDir& zero_f,
-                            const TileDir& corot, const TileDir& inv, const std::vector<TileDir>& scatter) {
+                            const TileDir& corot, const TileDir& inv, const TileDir& plastic,
+                            const std::vector<TileDir>& scatter) {
   cudaStream_t st = ctx->stream;
   if (zero_k.tiles > 0) {
     ctx->launches++;
@@ -691,6 +887,10 @@ od_status launch_eval_batch(Ctx* ctx, int n_sc, const SceneDev* sd, const TileDi
   if (inv.tiles > 0) {
     ctx->launches++;
     invhyper_batch_kernel<<<inv.tiles, 128, 0, st>>>(n_sc, inv.prefix, sd);
+  }
+  if (plastic.tiles > 0) {
+    ctx->launches++;
+    plastic_batch_kernel<<<plastic.tiles, 128, 0, st>>>(n_sc, plastic.prefix, sd);
   }
   for (size_t c = 0; c < scatter.size(); c++) {
     if (scatter[c].tiles <= 0) continue;

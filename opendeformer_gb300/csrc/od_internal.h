@@ -116,6 +116,8 @@ struct TileDir {
 struct SceneDev {
   int n_tets, dofs, nb, n_pad, nvals, nnzb, kind;
   double thr, lambda, mu;
+  double yield, creep, max_plastic;  // corotational plastic
+  double* plastic;                   // [9][n_tets] plastic strain (colour order) or null
   const int4* tets;
   const double* X;
   double* u;
@@ -265,6 +267,7 @@ struct Scene {
   int4* tets = nullptr;
   double* pre = nullptr;
   int n_pre = 0;
+  double* plastic = nullptr;       // corotational plastic: [9][n_tets] plastic strain (colour order)
   int* emap = nullptr;
   int* gdof = nullptr;
   int* perm = nullptr;
@@ -352,7 +355,8 @@ od_status launch_loads(Scene* s, const double* body, int n_facets_total, double 
 // material family), then scatter colour by colour (tiles over 90 threads
 // per element of the colour)
 od_status launch_eval_batch(Ctx* ctx, int n_sc, const SceneDev* sd, const TileDir& zero_k, const TileDir& zero_f,
-                            const TileDir& corot, const TileDir& inv, const std::vector<TileDir>& scatter);
+                            const TileDir& corot, const TileDir& inv, const TileDir& plastic,
+                            const std::vector<TileDir>& scatter);
 od_status sync_stream(Scene* s);
 
 // ---- kernels (od_sparse.cu) ----

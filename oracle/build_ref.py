@@ -59,7 +59,7 @@ FILES = {
                  "corotationalHyperelastic.cpp", "invertibleHyperelastic.h",
                  "invertibleHyperelastic.cpp", "invertibleNeoHookean.h",
                  "invertibleNeoHookean.cpp", "invertibleStVK.h",
-                 "invertibleStVK.cpp"],
+                 "invertibleStVK.cpp", "corotationalPlastic.h", "corotationalPlastic.cpp"],
     "solver": ["cgSolver.h", "cgSolver.cpp", "jacobiPreconditioner.h",
                "jacobiPreconditioner.cpp", "inCholeskyPreconditioner.h",
                "inCholeskyPreconditioner.cpp"],

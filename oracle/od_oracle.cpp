@@ -548,8 +548,10 @@ struct Scene {
   std::vector<int> facets;              // 3 per facet
   std::vector<int> cd;                  // sorted constrained DOFs
   std::vector<int> gidx;                // 12 per tet: compacted DOF or -1
-  int kind = 0;                         // 0 corot, 1 NH, 2 StVK
+  int kind = 0;                         // 0 corot, 1 NH, 2 StVK, 3 corotational plastic
   double rho = 0, lambda = 0, mu = 0, thr = 0, D[3] = {0, 0, 0};
+  double yield = 0, creep = 0, max_plastic = 0;  // plastic parameters
+  std::vector<double> plastic;          // plastic strain, 9 per tet (state, changes at every evaluation)
   // pattern (reference layout)
   int nbc = 0, nrem = 0;
   std::vector<int> pcol, rows, oris, emap;
@@ -652,9 +654,13 @@ inline V3 node_cur(const Scene& s, int n) { return add(s.X[n], s.u[n]); }
 // (element/tetelement.cpp:501-544): 10 blocks K0_ab (a <= b), 9 entries each,
 // then Dm^-1; invertible-hyperelastic getPrecomputes (tetelement.cpp:253-266):
 // 12 shape gradients then Dm^-1.
+// corotational (kind 0): [90 K0][9 Dm^-1] per tet; plastic (kind 3) adds the
+// 12 shape derivatives (getCorotationalTetElementPrecomputes,
+// tetelement.cpp:501-544); invertible: [12 dN][9 Dm^-1]
 void build_precomputes(Scene& s) {
   const int ne = s.n_tets;
   if (s.kind == 0) s.pre.assign((size_t)ne * 99, 0.0);
+  else if (s.kind == 3) s.pre.assign((size_t)ne * 111, 0.0);
   else s.pre.assign((size_t)ne * 21, 0.0);
   for (int e = 0; e < ne; e++) {
     const int* t = &s.tets[4 * e];
@@ -664,7 +670,7 @@ void build_precomputes(Scene& s) {
     V3 ab = sub(p1, p0), ac = sub(p2, p0), ad = sub(p3, p0);
     double Dm[9] = {ab.x, ac.x, ad.x, ab.y, ac.y, ad.y, ab.z, ac.z, ad.z}, Dmi[9];
     inverse3(Dm, Dmi);
-    if (s.kind == 0) {
+    if (s.kind == 0 || s.kind == 3) {
       double vol = tet_volume(p0, p1, p2, p3);
       double f = 1.0 / (36.0 * vol);
       double* K0 = &s.pre[(size_t)e * 90];
@@ -686,6 +692,7 @@ void build_precomputes(Scene& s) {
           k += 9;
         }
       memcpy(&s.pre[(size_t)ne * 90 + 9 * (size_t)e], Dmi, sizeof(Dmi));
+      if (s.kind == 3) memcpy(&s.pre[(size_t)ne * 99 + 12 * (size_t)e], dn, sizeof(dn));
     } else {
       memcpy(&s.pre[(size_t)e * 12], dn, sizeof(dn));
       memcpy(&s.pre[(size_t)ne * 12 + 9 * (size_t)e], Dmi, sizeof(Dmi));
@@ -753,6 +760,93 @@ void corot_element(const Scene& s, int e, double* K78, double* f12) {
       K += 9;
     }
   }
+}
+
+// corotational plastic element (corotationalPlastic.cpp:53-183,
+// tetelement.cpp:654-729): F = R S by polar decomposition (R Q-factor and
+// upper factor by QR when the deformed volume drops below threshold times
+// the rest volume); elastic strain e = sym(S) - I - plastic; stress
+// 2 mu e + lambda tr(e) I rotated by R; forces from the stress and the shape
+// derivatives; stiffness R K0 R^T.  The plastic strain is updated at every
+// evaluation: if |e| exceeds the yield criterion it grows by
+// creep (|e| - yield)/|e| e and is scaled back to the maximum plastic
+// strain.  Both norms follow the reference, which sums the squares of the
+// first three entries (one row) three times (corotationalPlastic.cpp:156-160,
+// 169-173).
+void plastic_element(Scene& s, int e, double* K78, double* f12) {
+  const int ne = s.n_tets;
+  const int* t = &s.tets[4 * e];
+  const double* K0 = &s.pre[(size_t)e * 90];
+  const double* Dmi = &s.pre[(size_t)ne * 90 + 9 * (size_t)e];
+  const double* dn = &s.pre[(size_t)ne * 99 + 12 * (size_t)e];
+  double* ep = &s.plastic[9 * (size_t)e];
+  double F[9], R[9], S[9];
+  deformation_gradient(s, t, Dmi, F);
+  V3 o[4], c[4];
+  for (int i = 0; i < 4; i++) { o[i] = node_pos(s, t[i]); c[i] = node_cur(s, t[i]); }
+  double v0 = tet_volume(o[0], o[1], o[2], o[3]);
+  double v1 = tet_volume(c[0], c[1], c[2], c[3]);
+  if (v1 >= s.thr * v0) polar3(F, R, S);
+  else qr3(F, R, S);
+  // computeElasticStress (corotationalPlastic.cpp:129-183)
+  const double lambda = s.D[1], mu2 = 2.0 * s.D[2];
+  double es[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) es[i * 3 + j] = 0.5 * (S[i * 3 + j] + S[j * 3 + i]) - ep[i * 3 + j];
+  es[0] -= 1.0;
+  es[4] -= 1.0;
+  es[8] -= 1.0;
+  double st[9];
+  for (int i = 0; i < 9; i++) st[i] = mu2 * es[i];
+  const double dg = lambda * (es[0] + es[4] + es[8]);
+  st[0] += dg;
+  st[4] += dg;
+  st[8] += dg;
+  double P[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) P[i * 3 + j] = R[i * 3] * st[j] + R[i * 3 + 1] * st[3 + j] + R[i * 3 + 2] * st[6 + j];
+  double en = 0.0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) en += es[i] * es[i];
+  en = sqrt(en);
+  if (en > s.yield) {
+    const double ratio = s.creep * (en - s.yield) / en;
+    for (int i = 0; i < 9; i++) ep[i] += ratio * es[i];
+    double pn = 0.0;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) pn += ep[i] * ep[i];
+    pn = sqrt(pn);
+    if (pn > s.max_plastic) {
+      const double fac = s.max_plastic / pn;
+      for (int i = 0; i < 9; i++) ep[i] *= fac;
+    }
+  }
+  // stiffness R K0_ab R^T (tetelement.cpp:665-716)
+  const double* K = K0;
+  double QK[9], QKQT[9];
+  for (int a = 0; a < 4; a++) {
+    for (int b = a; b < 4; b++) {
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) QK[i * 3 + j] = R[i * 3] * K[j] + R[i * 3 + 1] * K[3 + j] + R[i * 3 + 2] * K[6 + j];
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) QKQT[i * 3 + j] = QK[i * 3] * R[j * 3] + QK[i * 3 + 1] * R[j * 3 + 1] + QK[i * 3 + 2] * R[j * 3 + 2];
+      if (a == b) {
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3 - i; j++) K78[kDiag[a * 3 + i] + j] = QKQT[i * 3 + i + j];
+      } else {
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++) K78[kDiag[a * 3 + i] + (b - a) * 3 - i + j] = QKQT[i * 3 + j];
+      }
+      K += 9;
+    }
+  }
+  // generateNodalVirtualWorks (tetelement.cpp:718-729)
+  const double sixth = 1.0 / 6.0;
+  for (int n = 0; n < 3; n++) {
+    const double x = dn[3 * n], y = dn[3 * n + 1], z = dn[3 * n + 2];
+    for (int i = 0; i < 3; i++) f12[3 * n + i] = (P[i * 3] * x + P[i * 3 + 1] * y + P[i * 3 + 2] * z) * sixth;
+  }
+  for (int i = 0; i < 3; i++) f12[9 + i] = -(f12[i] + f12[3 + i] + f12[6 + i]);
 }
 
 // coordinateSystem (core/latool.h:542-552)
@@ -962,13 +1056,14 @@ void invhyper_element(const Scene& s, int e, double* K78, double* f12) {
   for (int i = 0; i < 3; i++) f12[9 + i] = -(f12[i] + f12[3 + i] + f12[6 + i]);
 }
 
-void element(const Scene& s, int e, double* K78, double* f12) {
+void element(Scene& s, int e, double* K78, double* f12) {
   if (s.kind == 0) corot_element(s, e, K78, f12);
+  else if (s.kind == 3) plastic_element(s, e, K78, f12);
   else invhyper_element(s, e, K78, f12);
 }
 
 // assembly into the reference layout (corotationalHyperelastic.cpp:100-120)
-void assemble(const Scene& s, double* values, double* fint) {
+void assemble(Scene& s, double* values, double* fint) {
   memset(values, 0, sizeof(double) * s.nvals);
   memset(fint, 0, sizeof(double) * s.dofs);
   double K[78], f[12];
@@ -1280,7 +1375,21 @@ odo_scene* odo_scene_create(int n_nodes, const double* X, int n_tets, const int*
   build_emap(s);
   build_precomputes(s);
   build_mass(s);
+  if (kind == 3) s.plastic.assign(9 * (size_t)n_tets, 0.0);
   return o;
+}
+
+// corotational plastic parameters and zero plastic strain for a kind-3
+// scene (CorotationalPlasticMaterial ctor, corotationalPlastic.cpp:8-22,
+// getPrecomputes :24-51)
+void odo_set_plastic(odo_scene* o, double yield, double creep, double max_strain) {
+  o->s.yield = yield;
+  o->s.creep = creep;
+  o->s.max_plastic = max_strain;
+  o->s.plastic.assign(9 * (size_t)o->s.n_tets, 0.0);
+}
+void odo_plastic_state(odo_scene* o, double* out) {
+  memcpy(out, o->s.plastic.data(), sizeof(double) * o->s.plastic.size());
 }
 
 void odo_scene_destroy(odo_scene* o) { delete o; }

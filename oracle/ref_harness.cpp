@@ -53,6 +53,7 @@
 #include "invertibleHyperelastic.h"
 #include "invertibleNeoHookean.h"
 #include "invertibleStVK.h"
+#include "corotationalPlastic.h"
 #include "preconditioner.h"
 #include "linearSolver.h"
 #include "cgSolver.h"
@@ -142,7 +143,17 @@ static void write_free_dofs_to_mesh(RefScene* s, const double* d) {
     }
 }
 
+// CorotationalPlasticMaterial parameters for the next scene of kind 3
+// (yieldCriterion, creepRatio, maxPlasticStrain)
+static double g_plastic[3] = {1e-3, 0.5, 0.05};
+
 extern "C" {
+
+void odref_plastic_params(double yield, double creep, double max_strain) {
+  g_plastic[0] = yield;
+  g_plastic[1] = creep;
+  g_plastic[2] = max_strain;
+}
 
 void* odref_scene_create(int n_nodes, const double* X, int n_tets, const int* tets,
                          int n_facets, const int* facets, int n_cdofs, const int* cdofs,
@@ -163,6 +174,9 @@ void* odref_scene_create(int n_nodes, const double* X, int n_tets, const int* te
   s->mat_kind = mat_kind;
   if (mat_kind == 0) s->material = new CorotationalHyperelasticMaterial(rho, youngs, poisson, threshold);
   else if (mat_kind == 1) s->material = new InvertibleNeoHookeanMaterial(rho, youngs, poisson, threshold);
+  else if (mat_kind == 3)
+    s->material = new CorotationalPlasticMaterial(rho, youngs, poisson, g_plastic[0], g_plastic[1], g_plastic[2],
+                                                  threshold);
   else s->material = new InvertibleStVKMaterial(rho, youngs, poisson, threshold);
 
   Mat::Assembler assembler(s->dofs);
@@ -233,6 +247,11 @@ void odref_get_displacements(void* p, double* u) {
 void odref_element_values(void* p, double* K78, double* f12) {
   RefScene* s = (RefScene*)p;
   int ne = s->n_tets;
+  if (s->mat_kind == 3) {  // the plastic material has no per-element entry; compare assembled values
+    memset(K78, 0, sizeof(double) * 78 * (size_t)ne);
+    memset(f12, 0, sizeof(double) * 12 * (size_t)ne);
+    return;
+  }
   if (s->mat_kind == 0) {
     auto* mat = (CorotationalHyperelasticMaterial*)&*s->material;
     auto* el = dynamic_cast<CorotationalHyperelasticElement*>(s->mesh->getMaterialElement(mat->type));
@@ -277,6 +296,17 @@ void odref_assemble(void* p, double* values, double* fint) {
   memset(fint, 0, sizeof(double) * s->dofs);
   s->material->generateMatrixAndVirtualWorks(s->mesh, s->indexer, s->cache, s->indices, *s->pattern, fint);
   memcpy(values, s->pattern->values, sizeof(double) * s->pattern->getNumEntries());
+}
+
+// plastic strain state of a kind-3 scene: 9 per element (the cache block
+// after 90 K0 + 9 Dm^-1 + 12 shape derivatives per element,
+// corotationalPlastic.cpp:24-51)
+void odref_plastic_state(void* p, double* out) {
+  RefScene* s = (RefScene*)p;
+  // the backward-Euler integrator evaluates the material with its own cache
+  // (nonlinearImplicitBackwardEuler.h:72); the other paths use the scene's
+  const double* pre = (const double*)(s->be ? s->be->materialCache.getMemoryBlock() : s->cache.getMemoryBlock());
+  memcpy(out, pre + (size_t)s->n_tets * (90 + 9 + 12), sizeof(double) * 9 * (size_t)s->n_tets);
 }
 
 void odref_mass(void* p, double* values) {

@@ -63,6 +63,8 @@ def lib():
         L.odref_polar.argtypes = [_dp, _dp, _dp]
         L.odref_qr.argtypes = [_dp, _dp, _dp]
         L.odref_eigsym.argtypes = [_dp, _dp, _dp]
+        L.odref_plastic_params.argtypes = [C.c_double, C.c_double, C.c_double]
+        L.odref_plastic_state.argtypes = [C.c_void_p, _dp]
         _lib = L
     return _lib
 
@@ -76,15 +78,18 @@ def _i(a):
 
 
 PRECOND = {"none": 0, "jacobi": 1, "ic": 2}
-MATERIAL = {"corotational": 0, "neohookean": 1, "stvk": 2}
+MATERIAL = {"corotational": 0, "neohookean": 1, "stvk": 2, "corotational_plastic": 3}
 
 
 class RefScene:
     """One reference scene: mesh, constraints, material, pattern and state."""
 
     def __init__(self, X, tets, facets, cdofs, material="corotational", density=1000.0,
-                 youngs=1e5, poisson=0.45, threshold=0.1):
+                 youngs=1e5, poisson=0.45, threshold=0.1, plastic=(1e-3, 0.5, 0.05)):
+        """plastic: (yieldCriterion, creepRatio, maxPlasticStrain) of the
+        corotational plastic material."""
         L = lib()
+        L.odref_plastic_params(*[float(v) for v in plastic])
         self.X = np.ascontiguousarray(X, dtype=np.float64)
         self.tets = np.ascontiguousarray(tets, dtype=np.int32)
         self.facets = np.ascontiguousarray(facets, dtype=np.int32).reshape(-1, 3)
@@ -138,6 +143,12 @@ class RefScene:
         f = np.zeros((self.n_tets, 12))
         lib().odref_element_values(self.h, _d(K), _d(f))
         return K, f
+
+    def plastic_state(self):
+        """Plastic strain, 9 per element (row-major), of a corotational plastic scene."""
+        out = np.zeros((self.n_tets, 9))
+        lib().odref_plastic_state(self.h, _d(out))
+        return out
 
     def assemble(self):
         v = np.zeros(self.n_values)

@@ -17,7 +17,7 @@ _ip = C.POINTER(C.c_int)
 _lib = None
 
 PRECOND = {"none": 0, "jacobi": 1, "block_jacobi": 2, "ic0": 3}
-MATERIAL = {"corotational": 0, "neohookean": 1, "stvk": 2}
+MATERIAL = {"corotational": 0, "neohookean": 1, "stvk": 2, "corotational_plastic": 3}
 
 
 def lib():
@@ -35,6 +35,8 @@ def lib():
         L.odo_pattern_sizes.argtypes = [C.c_void_p, _ip]
         L.odo_pattern.argtypes = [C.c_void_p, _ip, _ip, _ip, _ip]
         L.odo_set_displacements.argtypes = [C.c_void_p, _dp]
+        L.odo_set_plastic.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double]
+        L.odo_plastic_state.argtypes = [C.c_void_p, _dp]
         L.odo_get_displacements.argtypes = [C.c_void_p, _dp]
         L.odo_element_values.argtypes = [C.c_void_p, _dp, _dp]
         L.odo_assemble.argtypes = [C.c_void_p, _dp, _dp]
@@ -70,7 +72,9 @@ class OracleScene:
     """Restated scene with the same surface as ``reforacle.RefScene``."""
 
     def __init__(self, X, tets, facets, cdofs, material="corotational", density=1000.0,
-                 youngs=1e5, poisson=0.45, threshold=0.1):
+                 youngs=1e5, poisson=0.45, threshold=0.1, plastic=(1e-3, 0.5, 0.05)):
+        """plastic: (yieldCriterion, creepRatio, maxPlasticStrain) of the
+        corotational plastic material."""
         L = lib()
         self.X = np.ascontiguousarray(X, dtype=np.float64)
         self.tets = np.ascontiguousarray(tets, dtype=np.int32)
@@ -83,6 +87,8 @@ class OracleScene:
                                     _i(self.cdofs), MATERIAL[material], density, youngs, poisson,
                                     threshold)
         self.dofs = L.odo_dofs(self.h)
+        if material == "corotational_plastic":
+            L.odo_set_plastic(self.h, *[float(v) for v in plastic])
         s = np.zeros(5, np.int32)
         L.odo_pattern_sizes(self.h, _i(s))
         self.sizes = s
@@ -125,6 +131,12 @@ class OracleScene:
         f = np.zeros((self.n_tets, 12))
         lib().odo_element_values(self.h, _d(K), _d(f))
         return K, f
+
+    def plastic_state(self):
+        """Plastic strain, 9 per element (row-major), of a corotational plastic scene."""
+        out = np.zeros((self.n_tets, 9))
+        lib().odo_plastic_state(self.h, _d(out))
+        return out
 
     def assemble(self):
         v = np.zeros(self.n_values)

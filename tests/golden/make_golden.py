@@ -18,7 +18,12 @@ the GPU path against them.  Cases:
 * ``nm_<material>``: displacements after Newmark steps (restated integrator on
   reference components, Jacobi CG);
 * ``kat_math``: polar decomposition, Givens QR and symmetric eigensolve on
-  random and near-singular matrices.
+  random and near-singular matrices;
+* ``plastic``: the corotational plastic material: assembled values, f_int and
+  plastic strain after three evaluations at growing displacements (each
+  evaluation updates the plastic strain), and backward-Euler steps.
+
+``--only NAME`` writes one group (pattern, elements, integrators, kat, plastic).
 """
 from __future__ import annotations
 
@@ -56,7 +61,45 @@ def save(name, **arrays):
     np.savez_compressed(os.path.join(OUT, name + ".npz"), **arrays)
 
 
+PLASTIC = (1000.0, 1e5, 0.45, 0.1)              # rho, E, nu, compressing threshold
+PLASTIC_PARAMS = (2e-3, 0.5, 0.02)              # yield criterion, creep ratio, max plastic strain
+PLASTIC_SCALES = (0.1, 0.3, 1.0)                # displacement scales of the three evaluations
+
+
+def plastic_case():
+    g = small_mesh()
+    cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+    rho, E, nu, thr = PLASTIC
+    s = R.RefScene(g.X, g.tets, g.facets, cd, "corotational_plastic", rho, E, nu, thr, plastic=PLASTIC_PARAMS)
+    rng = np.random.default_rng(99)
+    u = rng.normal(scale=0.0015, size=(g.n_nodes, 3))
+    u[g.face_nodes(0, 0)] = 0.0
+    out = {}
+    for k, scale in enumerate(PLASTIC_SCALES):
+        s.set_displacements(u * scale)
+        vals, fint = s.assemble()
+        out[f"values_{k}"] = vals
+        out[f"fint_{k}"] = fint
+        out[f"plastic_{k}"] = s.plastic_state()
+    s = R.RefScene(g.X, g.tets, g.facets, cd, "corotational_plastic", rho, E, nu, thr, plastic=PLASTIC_PARAMS)
+    s.be_setup(1.0 / 60.0, 0.01, 0.001, tol=1e-10, maxit=2000, precond="jacobi")
+    fext = s.loads(body=[0.0, 0.0, -9800.0 * 20])
+    s.be_apply_loads()
+    iters = s.be_step(20)
+    save("plastic", X=g.X, tets=g.tets, facets=g.facets, cdofs=cd, u=u, scales=np.array(PLASTIC_SCALES),
+         material=np.array(PLASTIC), plastic_params=np.array(PLASTIC_PARAMS), be_fext=fext,
+         be_u=s.displacements(), be_v=s.be_velocity(), be_plastic=s.plastic_state(), be_steps=20, be_iters=iters,
+         be_params=np.array([1.0 / 60.0, 0.01, 0.001, 1e-10]), **out)
+
+
 def main():
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    if only == "plastic":
+        plastic_case()
+        print("golden fixture plastic written to", OUT)
+        return
+    if only is not None:
+        raise SystemExit(f"--only {only}: only 'plastic' writes a single group")
     g = small_mesh()
     cases = {"full": meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0)),
              "partial": partial_constraints(g)}
@@ -131,6 +174,7 @@ def main():
     evec = np.array([R.eigsym(t)[1] for t in tri])
     save("kat_math", F=Fs, polar_R=polR, polar_S=polS, qr_Q=qrQ, qr_R=qrR, tri=tri, eig_vals=ev,
          eig_vecs=evec)
+    plastic_case()
     print("golden fixtures written to", OUT)
 
 

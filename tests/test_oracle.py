@@ -170,3 +170,34 @@ def test_restatement_matches_compiled_reference_live():
         Ko, fo = o.element_values()
         np.testing.assert_allclose(Ko, Kr, rtol=0, atol=1e-12 * np.abs(Kr).max())
         np.testing.assert_allclose(fo, fr, rtol=0, atol=1e-12 * np.abs(fr).max())
+
+
+def test_plastic_restatement_matches_reference(golden):
+    """Corotational plastic material: assembled values, f_int and the plastic
+    strain after three evaluations at growing displacements (each evaluation
+    updates the plastic strain, corotationalPlastic.cpp:129-183)."""
+    d = golden("plastic")
+    rho, E, nu, thr = d["material"]
+    o = O.OracleScene(d["X"], d["tets"], d["facets"], d["cdofs"], "corotational_plastic", rho, E, nu, thr,
+                      plastic=tuple(d["plastic_params"]))
+    for k, scale in enumerate(d["scales"]):
+        o.set_displacements(d["u"] * scale)
+        vals, fint = o.assemble()
+        assert np.abs(vals - d[f"values_{k}"]).max() <= 1e-13 * np.abs(d[f"values_{k}"]).max()
+        assert np.abs(fint - d[f"fint_{k}"]).max() <= 1e-12 * np.abs(d[f"fint_{k}"]).max()
+        p = o.plastic_state()
+        assert np.abs(p - d[f"plastic_{k}"]).max() <= 1e-13 * np.abs(d[f"plastic_{k}"]).max()
+
+
+def test_plastic_backward_euler_restatement_matches_reference(golden):
+    d = golden("plastic")
+    rho, E, nu, thr = d["material"]
+    dt, am, bk, tol = d["be_params"]
+    o = O.OracleScene(d["X"], d["tets"], d["facets"], d["cdofs"], "corotational_plastic", rho, E, nu, thr,
+                      plastic=tuple(d["plastic_params"]))
+    o.integrator_setup(dt, am, bk, tol=tol, maxit=2000, precond="jacobi")
+    o.set_fext(d["be_fext"])
+    its = o.be_step(int(d["be_steps"]))
+    assert abs(its - int(d["be_iters"])) <= 0.01 * int(d["be_iters"])
+    assert np.abs(o.displacements() - d["be_u"]).max() <= 1e-8 * np.abs(d["be_u"]).max()
+    assert np.abs(o.plastic_state() - d["be_plastic"]).max() <= 1e-8 * np.abs(d["be_plastic"]).max()
