@@ -13,6 +13,7 @@
 // batch of iterations can be queued (or captured) without host round trips.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 
@@ -938,6 +939,7 @@ struct RingShared {
   int c0[kMaxLocalScenes], c1[kMaxLocalScenes];  // CTA range of each local scene
   int lfirst[kMaxLocalScenes + 1];                // first slice of each local scene in the CTA range
   volatile unsigned char act[2][kMaxLocalScenes];  // activity by iteration parity
+  unsigned char act_in[kMaxLocalScenes];      // activity given to the launch (before iteration 0)
   unsigned long long tmax;                    // profiling: the last CTA's end of the SpMV phase
   volatile int pub;                           // last iteration whose activity is published
   volatile int stop;
@@ -1074,6 +1076,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
     sh.eps[threadIdx.x] = ring[s].itol2;  // relative until the first reduction
     sh.maxit[threadIdx.x] = ring[s].max_iter;
     sh.act[0][threadIdx.x] = (unsigned char)(ring[s].active0 != 0);
+    sh.act_in[threadIdx.x] = (unsigned char)(ring[s].active0 != 0);
     sh.lp[threadIdx.x] = desc[s];
     sh.c0[threadIdx.x] = sc_cta[2 * s];
     sh.c1[threadIdx.x] = sc_cta[2 * s + 1];
@@ -1093,10 +1096,26 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
     unsigned pc = 0;  // pieces issued
     int kit = 0;      // iteration the pieces belong to
     bool ok = true;
-    while (ok) {
+    while (ok && !sh.stop) {  // (when every scene is done, no piece is issued: poll stop here)
+      // never more than one iteration ahead of the consumers: the activity of
+      // iteration kit - 1 must be published before pass kit (a warp whose
+      // scenes have all converged issues nothing and would otherwise run
+      // ahead and read another iteration's activity)
+      if (kit > 0) {
+        unsigned long long spins = 0;
+        while (sh.pub < kit - 1 && !sh.stop && ++spins < kMbarSpinLimit) {
+        }
+        if (sh.pub < kit - 1) break;
+      }
       int ls = 0;
       for (int sl = sfirst + pw; sl < send && ok; sl += kRingWarps) {
         local_scene(sh, sl, ls);
+        // pieces of iteration kit exist for the scenes active in iteration
+        // kit - 1 (published before the consumers start iteration kit - 1,
+        // hence before the producer reaches iteration kit): consumers apply
+        // the same rule, so a converged scene costs nothing after one pass
+        __threadfence_block();
+        if (!(kit == 0 ? sh.act_in[ls] : sh.act[(kit - 1) & 1][ls])) continue;
         bool copy = true;
         if (sh.pub >= kit) {
           __threadfence_block();
@@ -1245,6 +1264,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
     {
       zero_ws(1);
       for (int ls = 0; ls < L && alive; ls++) {
+        if (!(k == 0 ? sh.act_in[ls] : sh.act[kp ^ 1][ls])) continue;  // no pieces this iteration
         const bool on = sh.act[kp][ls] != 0;
         const Vecs V = vecs(ls);
         const int* __restrict__ soff = sh.lp[ls].soff;
@@ -1867,10 +1887,16 @@ void mixed_free(MixedSys* m) {
   delete m;
 }
 
-// Contiguous slice ranges per CTA with about equal step counts and at most
-// kMaxLocalScenes scenes each.
+// Contiguous slice ranges per CTA with about equal cost and at most
+// kMaxLocalScenes scenes each.  Cost of a slice = its steps + kSliceCost
+// (the fixed work of a slice: ring hand-offs, shuffles, the q store), so
+// regions of short rows (boundary layers) do not make their CTAs the last to
+// finish.  OD_GB300_SLICE_COST overrides the constant.
+constexpr double kSliceCost = 8.0;
 static od_status mixed_partition(MixedSys* m, int G) {
   const int ns = m->ns;
+  double c_slice = kSliceCost;
+  if (const char* e = std::getenv("OD_GB300_SLICE_COST")) c_slice = std::atof(e);
   std::vector<int> sc_of(ns);
   for (int s = 0; s < m->n_sc; s++)
     for (int k = m->sc_slice[s]; k < m->sc_slice[s + 1]; k++) sc_of[k] = s;
@@ -1882,8 +1908,8 @@ static od_status mixed_partition(MixedSys* m, int G) {
   for (int b = 0; b < G; b++) {
     first[b] = sl;
     sc_lo[b] = sl < ns ? sc_of[sl] : 0;
-    const long long target = (long long)off[ns] * (b + 1) / G;
-    while (sl < ns && (off[sl] < target || b == G - 1)) {
+    const double target = ((double)off[ns] + c_slice * ns) * (b + 1) / G;
+    while (sl < ns && ((double)off[sl] + c_slice * sl < target || b == G - 1)) {
       if (sc_of[sl] - sc_lo[b] >= kMaxLocalScenes) break;
       sl++;
     }
