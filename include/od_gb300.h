@@ -13,6 +13,7 @@
  *   BlockedSymSparseMatrix + SpMDV         core/sparseMatrix.h:183-274, core/numerMethod.h:134-262
  *   LinearSolver / CGSolver                core/linearSolver.h:12-20, solver/cgSolver.h:16-17
  *   Preconditioner (+ Jacobi, IC)          core/preconditioner.h:12-22
+ *   InLDLTPreconditioner                   solver/inLDLTPreconditioner.h:12-44
  *   Forcer                                 core/forcer.h:13-22
  *   Intergrator / NonlinearImplicitBackwardEuler
  *                                          core/intergrator.h:13-35,
@@ -29,7 +30,7 @@
 extern "C" {
 #endif
 
-#define OD_ABI_VERSION 4
+#define OD_ABI_VERSION 5
 
 typedef enum od_status {
   OD_OK = 0,
@@ -54,8 +55,11 @@ typedef enum od_precond_kind {
   OD_PRECOND_NONE = 0,         /* Preconditioner (identity), core/preconditioner.h:14-16 */
   OD_PRECOND_JACOBI = 1,       /* solver/jacobiPreconditioner.cpp:12-26 */
   OD_PRECOND_BLOCK_JACOBI = 2, /* 3x3 diagonal blocks (no reference counterpart) */
-  OD_PRECOND_IC0 = 3           /* shifted IC(0), level-scheduled (no reference counterpart;
+  OD_PRECOND_IC0 = 3,          /* shifted IC(0), level-scheduled (no reference counterpart;
                                   the reference's fill-in IC is inCholeskyPreconditioner.cpp) */
+  OD_PRECOND_LDLT = 4          /* incomplete LDL^T, solver/inLDLTPreconditioner.cpp:34-184:
+                                  factor on the host (bit-identical to the reference's),
+                                  triangular sweeps on the device */
 } od_precond_kind;
 
 typedef enum od_precision {
@@ -91,6 +95,9 @@ typedef struct od_solver_params {
   int replace_every;  /* mixed: true-residual recompute period (0 = 25) */
   double inner_tol;   /* mixed: inner FP32 solve tolerance (0 = 1e-4) */
   int max_refine;     /* mixed: max outer refinement sweeps (0 = 20) */
+  double sainv_eps;   /* LDL^T: sainvEpsilon, drop bound of the inverse factor's
+                         entries (0 = 0.1; InLDLTPreconditioner(sainvEpsilon, ldltEpsilon)) */
+  double ldlt_eps;    /* LDL^T: ldltEpsilon, drop bound of L's entries (0 = 0.01) */
 } od_solver_params;
 
 typedef struct od_solve_stats {
@@ -139,6 +146,13 @@ typedef struct od_counters {
                                  SpMV work (without the grid-wide sum that follows) */
   long long mix_fallbacks;    /* mixed solves whose refinement stalled and that the FP64 PCG
                                  finished (counted whether profiling is on or not) */
+  long long ldlt_factors;     /* incomplete LDL^T factorisations (always counted) */
+  double ldlt_factor_ms;      /* their host time: rebuild of A in the reference layout, the
+                                 factorisation and the upload of the sweep arrays */
+  long long ldlt_nnz;         /* stored L entries of the last factor */
+  long long ldlt_applies;     /* LDL^T applies timed while profiling is on */
+  double ldlt_apply_ms;       /* their summed CUDA-event durations */
+  double ldlt_apply_bytes;    /* their algorithmic bytes: 2 x (nnz x 12 B) + 6 x 8 B per row */
 } od_counters;
 
 typedef struct od_scene_info {
@@ -215,6 +229,19 @@ od_status od_scene_spmdv(od_scene* scene, const double* values, const double* x,
  * values); x is the warm start and the result. */
 od_status od_scene_pcg(od_scene* scene, const double* values, const double* b, double* x,
                        const od_solver_params* params, od_solve_stats* stats);
+
+/* InLDLTPreconditioner (solver/inLDLTPreconditioner.cpp) as a stand-alone
+ * preconditioner.  od_scene_ldlt_factor is Preprocess (:27-149) on A given by
+ * reference-layout values, with InLDLTPreconditioner(sainv_eps, ldlt_eps)'s
+ * drop bounds taken as given (>= 0); *nnz receives the stored L entries.
+ * od_scene_ldlt_get copies the factor out in the reference's storage:
+ * values[nnz], rows[nnz], pcol[dofs] (L columns 0..dofs-2), inv_diag[dofs].
+ * od_scene_ldlt_apply is solvePreconditionerSystem (:151-184) on the device
+ * with the last factor: result = (L D L^T)^-1 rhs (dofs entries each). */
+od_status od_scene_ldlt_factor(od_scene* scene, const double* values, double sainv_eps, double ldlt_eps,
+                               long long* nnz);
+od_status od_scene_ldlt_get(od_scene* scene, double* values, int* rows, int* pcol, double* inv_diag);
+od_status od_scene_ldlt_apply(od_scene* scene, const double* rhs, double* result);
 
 /* Forcer + Intergrator::setExternalVirtualWork (core/forcer.cpp:8-96,
  * nonlinearImplicitBackwardEuler.h:118-120): body force density (N/m^3, may be

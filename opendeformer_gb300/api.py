@@ -9,7 +9,8 @@ reference reads the same:
   poisson, inversionThreshold)`` (material/invertibleNeoHookean.h,
   material/invertibleStVK.h);
 * preconditioners / solver: ``JacobiPreconditioner()``,
-  ``BlockJacobiPreconditioner()``, ``IC0Preconditioner()`` and
+  ``BlockJacobiPreconditioner()``, ``IC0Preconditioner()``,
+  ``InLDLTPreconditioner(sainvEpsilon, ldltEpsilon)`` and
   ``CGSolver(tol, maxIter, preconditioner)`` (solver/cgSolver.h:16-17);
 * integrators: ``NonlinearImplicitBackwardEuler(massDamp, stiffDamp, ts,
   solver)`` (intergrator/nonlinearImplicitBackwardEuler.h:48-73) and
@@ -40,7 +41,7 @@ STATUS = {0: "OD_OK", 1: "OD_ERR_INVALID_ARG", 2: "OD_ERR_OUT_OF_MEMORY", 3: "OD
           8: "OD_ERR_INTERNAL"}
 
 MATERIAL_KIND = {"corotational": 0, "neohookean": 1, "stvk": 2, "corotational_plastic": 3}
-PRECOND_KIND = {"none": 0, "jacobi": 1, "block_jacobi": 2, "ic0": 3}
+PRECOND_KIND = {"none": 0, "jacobi": 1, "block_jacobi": 2, "ic0": 3, "ldlt": 4}
 PRECISION = {"fp64": 0, "mixed": 1}
 
 
@@ -58,7 +59,8 @@ class od_material(C.Structure):
 
 class od_solver_params(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("precond", C.c_int), ("precision", C.c_int),
-                ("replace_every", C.c_int), ("inner_tol", C.c_double), ("max_refine", C.c_int)]
+                ("replace_every", C.c_int), ("inner_tol", C.c_double), ("max_refine", C.c_int),
+                ("sainv_eps", C.c_double), ("ldlt_eps", C.c_double)]
 
 
 class od_solve_stats(C.Structure):
@@ -82,7 +84,9 @@ class od_counters(C.Structure):
                 ("spmv_launches", C.c_longlong), ("spmv_ms", C.c_double),
                 ("pcg_launches", C.c_longlong), ("pcg_iterations", C.c_longlong), ("pcg_ms", C.c_double),
                 ("mix_iterations", C.c_longlong), ("mix_spmv_ms", C.c_double), ("mix_spmv_bytes", C.c_double),
-                ("mix_spmv_work_ms", C.c_double), ("mix_fallbacks", C.c_longlong)]
+                ("mix_spmv_work_ms", C.c_double), ("mix_fallbacks", C.c_longlong),
+                ("ldlt_factors", C.c_longlong), ("ldlt_factor_ms", C.c_double), ("ldlt_nnz", C.c_longlong),
+                ("ldlt_applies", C.c_longlong), ("ldlt_apply_ms", C.c_double), ("ldlt_apply_bytes", C.c_double)]
 
 
 class od_scene_info(C.Structure):
@@ -149,6 +153,9 @@ SIGNATURES = {
     "od_scene_mass": (C.c_int, [_vp, _dp]),
     "od_scene_spmdv": (C.c_int, [_vp, _dp, _dp, _dp]),
     "od_scene_pcg": (C.c_int, [_vp, _dp, _dp, _dp, C.POINTER(od_solver_params), C.POINTER(od_solve_stats)]),
+    "od_scene_ldlt_factor": (C.c_int, [_vp, _dp, C.c_double, C.c_double, C.POINTER(C.c_longlong)]),
+    "od_scene_ldlt_get": (C.c_int, [_vp, _dp, _ip, _ip, _dp]),
+    "od_scene_ldlt_apply": (C.c_int, [_vp, _dp, _dp]),
     "od_scene_set_loads": (C.c_int, [_vp, _dp, C.c_int, _dp, _ip, _ip]),
     "od_scene_update_loads": (C.c_int, [_vp, C.c_double]),
     "od_scene_set_traction_schedule": (C.c_int, [_vp, C.c_double, C.c_double]),
@@ -241,6 +248,8 @@ def CorotationalPlasticMaterial(rho, youngs, poisson, yieldCriterion, creepRatio
 @dataclasses.dataclass
 class Preconditioner:
     kind: str = "none"
+    sainvEpsilon: float = 0.0   # LDL^T drop bounds (0: 0.1 and 0.01)
+    ldltEpsilon: float = 0.0
 
 
 def JacobiPreconditioner():
@@ -253,6 +262,11 @@ def BlockJacobiPreconditioner():
 
 def IC0Preconditioner():
     return Preconditioner("ic0")
+
+
+def InLDLTPreconditioner(sainvEpsilon=0.1, ldltEpsilon=0.01):
+    """InLDLTPreconditioner(sainvEpsilon, ldltEpsilon) (solver/inLDLTPreconditioner.h:14-15)."""
+    return Preconditioner("ldlt", float(sainvEpsilon), float(ldltEpsilon))
 
 
 @dataclasses.dataclass
@@ -268,7 +282,8 @@ class CGSolver:
     def to_c(self):
         return od_solver_params(self.tol, self.maxIter, PRECOND_KIND[self.preconditioner.kind],
                                 PRECISION[self.precision], self.replace_every, self.inner_tol,
-                                self.max_refine)
+                                self.max_refine, self.preconditioner.sainvEpsilon,
+                                self.preconditioner.ldltEpsilon)
 
 
 @dataclasses.dataclass
@@ -449,6 +464,31 @@ class Scene:
         st = od_solve_stats()
         _check(load_library().od_scene_pcg(self.h, _d(values), _d(b), _d(x), C.byref(p), C.byref(st)), "pcg")
         return x, st
+
+    def ldlt_factor(self, values, sainv_eps=0.1, ldlt_eps=0.01):
+        """InLDLTPreconditioner::Preprocess on A = values (reference layout);
+        returns the factor in the reference's storage: (L values, L rows,
+        pcol (dofs entries), inverted diagonal).  The factor stays with the
+        scene for ldlt_apply."""
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        nnz = C.c_longlong(0)
+        L = load_library()
+        _check(L.od_scene_ldlt_factor(self.h, _d(values), float(sainv_eps), float(ldlt_eps), C.byref(nnz)),
+               "ldlt_factor")
+        n = nnz.value
+        lv = np.zeros(max(n, 1))
+        lr = np.zeros(max(n, 1), np.int32)
+        pc = np.zeros(max(self.dofs, 1), np.int32)
+        dinv = np.zeros(max(self.dofs, 1))
+        _check(L.od_scene_ldlt_get(self.h, _d(lv), _i(lr), _i(pc), _d(dinv)), "ldlt_get")
+        return lv[:n], lr[:n], pc[: self.dofs], dinv[: self.dofs]
+
+    def ldlt_apply(self, rhs):
+        """(L D L^T)^-1 rhs on the device with the last ldlt_factor."""
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64)
+        out = np.zeros(self.dofs)
+        _check(load_library().od_scene_ldlt_apply(self.h, _d(rhs), _d(out)), "ldlt_apply")
+        return out
 
     def set_loads(self, body=None, tractions=()):
         """Forcer: body force density (N/m^3) then (traction Pa, facet ids) groups."""

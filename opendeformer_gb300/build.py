@@ -19,7 +19,8 @@ LIB = os.path.join(OUT_DIR, "libodgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]
-SOURCES = ["od_host.cpp", "od_elements.cu", "od_sparse.cu", "od_api.cu", "od_batch.cu", "od_noalloc.cu"]
+SOURCES = ["od_host.cpp", "od_rif.cpp", "od_elements.cu", "od_sparse.cu", "od_api.cu", "od_batch.cu",
+           "od_noalloc.cu", "od_ldlt.cu"]
 
 
 def nvcc() -> str:
@@ -49,7 +50,10 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
         if not _stale(obj, [path, *headers, __file__]):
             continue
         if src.endswith(".cpp"):
-            cmd = [cc, "-x", "c++", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-c", path, "-o", obj]
+            # no contraction into FMA: the host factorisations give the same
+            # bits on x86-64 and aarch64
+            cmd = [cc, "-x", "c++", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+                   "-c", path, "-o", obj]
         else:
             cmd = [cc, *ARCH, *NVCC_FLAGS, *(extra or []), "-c", path, "-o", obj]
         if verbose:

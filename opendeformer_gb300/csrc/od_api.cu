@@ -103,13 +103,6 @@ __global__ void nm_correct_kernel(int n, const int* __restrict__ free_pos, doubl
 using namespace od;
 
 
-#define OD_CHECK_ARG(cond, msg)              \
-  do {                                       \
-    if (!(cond)) {                           \
-      ::od::set_error(msg);                  \
-      return OD_ERR_INVALID_ARG;             \
-    }                                        \
-  } while (0)
 
 
 template <class T>
@@ -198,6 +191,12 @@ od_status od_ctx_get_counters(od_ctx* ctx, od_counters* out) {
   out->mix_spmv_work_ms = ctx->c.mix_spmv_work_ms;
   out->mix_fallbacks = ctx->c.mix_fallbacks;
   out->mix_spmv_bytes = ctx->c.mix_spmv_bytes;
+  out->ldlt_factors = ctx->c.ldlt_factors;
+  out->ldlt_factor_ms = ctx->c.ldlt_factor_ms;
+  out->ldlt_nnz = ctx->c.ldlt_nnz;
+  out->ldlt_applies = ctx->c.ldlt_applies;
+  out->ldlt_apply_ms = ctx->c.ldlt_apply_ms;
+  out->ldlt_apply_bytes = ctx->c.ldlt_apply_bytes;
   return OD_OK;
 }
 
@@ -208,6 +207,8 @@ od_status od_ctx_reset_counters(od_ctx* ctx) {
   ctx->c.spmv_ms = ctx->c.pcg_kernel_ms = 0.0;
   ctx->c.mix_iters = ctx->c.mix_fallbacks = 0;
   ctx->c.mix_spmv_ms = ctx->c.mix_spmv_bytes = ctx->c.mix_spmv_work_ms = 0.0;
+  ctx->c.ldlt_factors = ctx->c.ldlt_nnz = ctx->c.ldlt_applies = 0;
+  ctx->c.ldlt_factor_ms = ctx->c.ldlt_apply_ms = ctx->c.ldlt_apply_bytes = 0.0;
   return OD_OK;
 }
 
@@ -502,8 +503,13 @@ od_status od_scene_spmdv(od_scene* scene, const double* values, const double* x,
 static od_status check_solver(const od_solver_params* p) {
   OD_CHECK_ARG(p, "solver params are NULL");
   OD_CHECK_ARG(p->tol >= 0.0 && p->max_iter >= 0, "solver tolerance / max_iter out of range");
-  OD_CHECK_ARG(p->precond >= 0 && p->precond <= OD_PRECOND_IC0, "unknown preconditioner");
+  OD_CHECK_ARG(p->precond >= 0 && p->precond <= OD_PRECOND_LDLT, "unknown preconditioner");
   OD_CHECK_ARG(p->precision == OD_PRECISION_FP64 || p->precision == OD_PRECISION_MIXED, "unknown precision");
+  OD_CHECK_ARG(p->precision == OD_PRECISION_FP64 || p->precond < OD_PRECOND_IC0,
+               "mixed precision supports the none, Jacobi and block-Jacobi preconditioners");
+  OD_CHECK_ARG(p->sainv_eps >= 0.0 && p->ldlt_eps >= 0.0 && std::isfinite(p->sainv_eps) &&
+                   std::isfinite(p->ldlt_eps),
+               "LDL^T drop bounds must be finite and >= 0");
   return OD_OK;
 }
 

@@ -54,6 +54,7 @@ struct SolveScalars {           // device-resident PCG scalars
 
 struct SliceSys;
 struct MixedSys;
+struct LdltSys;
 struct Scene;
 
 struct Pcg {
@@ -97,6 +98,8 @@ struct Pcg {
   // solve (both built on first use)
   SliceSys* slice = nullptr;
   MixedSys* mix = nullptr;
+  // incomplete LDL^T (factor on the host, sweeps on the device)
+  LdltSys* ldlt = nullptr;
 };
 
 constexpr int kSliceRows = 10;      // block rows per slice (3 lanes each, 30 of a warp's 32)
@@ -238,6 +241,8 @@ struct Ctx {
   double pcg_kernel_ms = 0.0;
   long long mix_iters = 0;            // inner FP32 loop iterations (profiling)
   long long mix_fallbacks = 0;        // mixed solves finished by the FP64 solver
+  long long ldlt_factors = 0, ldlt_nnz = 0, ldlt_applies = 0;
+  double ldlt_factor_ms = 0.0, ldlt_apply_ms = 0.0, ldlt_apply_bytes = 0.0;
   double mix_spmv_ms = 0.0;
   double mix_spmv_work_ms = 0.0;
   double mix_spmv_bytes = 0.0;
@@ -287,6 +292,12 @@ struct Scene {
   FullBsr bsr;
   void* A = nullptr;               // full BSR values (double or float)
   double* A64 = nullptr;           // FP64 full values
+  // sources of the last A64 expansion (A = c1 V1 + c2 V2 + c3 V3, lower
+  // layout), from which the LDL^T factor rebuilds A in the reference layout
+  struct {
+    const double *v1 = nullptr, *v2 = nullptr, *v3 = nullptr;
+    double c1 = 0.0, c2 = 0.0, c3 = 0.0;
+  } lo;
   Pcg pcg;
   // integrator
   od_integrator_params ip{};
@@ -321,6 +332,15 @@ od_status cuda_fail(cudaError_t e, const char* what);
     if (_e != cudaSuccess) return ::od::cuda_fail(_e, #call); \
   } while (0)
 
+// argument check of an ABI entry point
+#define OD_CHECK_ARG(cond, msg)              \
+  do {                                       \
+    if (!(cond)) {                           \
+      ::od::set_error(msg);                  \
+      return OD_ERR_INVALID_ARG;             \
+    }                                        \
+  } while (0)
+
 // ---- host algorithms (od_host.cpp) ----
 int global_index(const std::vector<int>& cd, int node, int axis);
 void build_pattern(const std::vector<int>& gidx, int n_tets, int dofs, std::vector<int>& pcol,
@@ -343,6 +363,22 @@ struct HostSliced {
 void build_sliced(const std::vector<int>& row_ptr, const std::vector<int>& col, int nb, HostSliced& out);
 void build_ic_levels(const std::vector<int>& rp, const std::vector<int>& ci, int n,
                      std::vector<int>& rows_by_level, std::vector<int>& lvl_ptr, bool forward);
+// incomplete LDL^T (od_rif.cpp): scalar columns of the symmetric matrix in
+// getFullIndices order, and the factor in the reference's storage (L
+// columns 0..n-2 with rows in production order, pcol with n entries, the
+// inverted diagonal)
+struct RifColumns {
+  int n = 0;
+  std::vector<int> ptr, row, src;
+};
+struct RifFactor {
+  int n = 0;
+  std::vector<double> val;
+  std::vector<int> row, pcol;
+  std::vector<double> dinv;
+};
+void rif_columns(int n, int nbc, const std::vector<int>& pcol, const std::vector<int>& rows, RifColumns& out);
+void rif_factor(const RifColumns& A, const double* values, double sainv_eps, double ldlt_eps, RifFactor& F);
 
 // ---- kernels (od_elements.cu) ----
 od_status launch_precompute(Scene* s);
@@ -390,6 +426,19 @@ __device__ __forceinline__ int dir_scene(const int* __restrict__ prefix, int n, 
   return lo;
 }
 #endif
+// ---- incomplete LDL^T (od_ldlt.cu)
+constexpr double kLdltSainvDefault = 0.1;
+constexpr double kLdltDropDefault = 0.01;
+// factor of A given in the reference's lower layout on the host, or (NULL)
+// of the last A64 expansion
+od_status ldlt_factor(Scene* s, const double* host_values, double sainv_eps, double ldlt_eps);
+// z = (L D L^T)^-1 r on the device (length n_pad; padding rows copied);
+// returns at once when sc->done is set
+od_status ldlt_apply(Scene* s, const double* r, double* z, const SolveScalars* sc);
+// OD_ERR_DEVICE_TIMEOUT if a sweep's bounded wait ran out since the last check
+od_status ldlt_check(Scene* s);
+void ldlt_free(LdltSys* l);
+
 // PCG on A64; b and x are device vectors of length n_pad
 od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm, od_solve_stats* st);
 

@@ -291,7 +291,8 @@ __global__ void pcg_init_kernel(int nb, const int* __restrict__ rp, const int* _
         const int lb = threadIdx.x - r;
         zv = m[0] * rsh[lb] + m[1] * rsh[lb + 1] + m[2] * rsh[lb + 2];
       }
-      if (pkind != OD_PRECOND_IC0) { z[3 * row + r] = zv; p[3 * row + r] = zv; rz += rv * zv; }
+      // (IC(0) and LDL^T are applied by their own sweeps)
+      if (pkind < OD_PRECOND_IC0) { z[3 * row + r] = zv; p[3 * row + r] = zv; rz += rv * zv; }
       bb += bv * bv;
       rr += rv * rv;
     }
@@ -371,7 +372,7 @@ __global__ void __launch_bounds__(kUpdThreads) pcg_update_kernel(int n, double* 
     rs[threadIdx.x] = rv;
     __syncthreads();
     rr += rv * rv;
-    if (valid && pkind != OD_PRECOND_IC0) {
+    if (valid && pkind < OD_PRECOND_IC0) {
       double zv;
       if (pkind == OD_PRECOND_JACOBI) {
         zv = pinv[i] * rv;
@@ -1543,6 +1544,9 @@ od_status launch_expand(Scene* s, const double* v1, double c1, const double* v2,
   const long long total = 9LL * s->bsr.nnzb;
   if (total == 0) return OD_OK;
   if (v3 && !s->has_damping) v3 = nullptr;
+  s->lo.v1 = v1; s->lo.c1 = c1;
+  s->lo.v2 = v2; s->lo.c2 = c2;
+  s->lo.v3 = v3; s->lo.c3 = c3;
   OD_KL(s);
   expand_kernel<double><<<nblk(total, kThreads), kThreads, 0, s->ctx->stream>>>(
       total, s->bsr.desc_kind, s->bsr.desc_off, s->bsr.gen, v1, c1, v2, c2, v3, c3, s->A64);
@@ -1765,6 +1769,7 @@ void pcg_free(Scene* s) {
   cudaFree(P.gbar);
   mixed_free(P.mix);
   slice_free(P.slice);
+  ldlt_free(P.ldlt);
   if (P.sc_host) cudaFreeHost(P.sc_host);
   if (P.timeout_host) cudaFreeHost(P.timeout_host);
   P = Pcg();
@@ -2041,7 +2046,7 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
   cudaStream_t strm = ctx->stream;
   const int n_sc = m->n_sc;
   st.assign(n_sc, od_solve_stats{});
-  if (pk == OD_PRECOND_IC0 || pk < 0 || pk > OD_PRECOND_IC0) {
+  if (pk < 0 || pk >= OD_PRECOND_IC0) {
     set_error("mixed precision supports the none, Jacobi and block-Jacobi preconditioners");
     return OD_ERR_UNSUPPORTED;
   }
@@ -2191,7 +2196,7 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
   cudaStream_t strm = s->ctx->stream;
   const int nb = s->bsr.nb, n = P.n_pad;
   const int pk = prm->precond;
-  if (pk < 0 || pk > OD_PRECOND_IC0) { set_error("unknown preconditioner"); return OD_ERR_INVALID_ARG; }
+  if (pk < 0 || pk > OD_PRECOND_LDLT) { set_error("unknown preconditioner"); return OD_ERR_INVALID_ARG; }
   if (nb == 0) {
     if (st) *st = od_solve_stats{};
     return OD_OK;
@@ -2213,8 +2218,14 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
     od_status e = ic0_factor(s);
     if (e != OD_OK) return e;
     shift = P.ic_shift;
+  } else if (pk == OD_PRECOND_LDLT) {
+    // InLDLTPreconditioner::Preprocess runs inside every solve (cgSolver.cpp:23)
+    od_status e = ldlt_factor(s, nullptr, prm->sainv_eps > 0.0 ? prm->sainv_eps : kLdltSainvDefault,
+                              prm->ldlt_eps > 0.0 ? prm->ldlt_eps : kLdltDropDefault);
+    if (e != OD_OK) return e;
   }
-  if (pk != OD_PRECOND_IC0 && P.coop_grid > 0 && !P.disable_persistent) {
+  const bool swept = pk == OD_PRECOND_IC0 || pk == OD_PRECOND_LDLT;   // applied by triangular sweeps
+  if (!swept && P.coop_grid > 0 && !P.disable_persistent) {
     // one cooperative launch for the whole solve
     OD_CUDA(cudaMemsetAsync(P.gbar, 0, sizeof(GridBarrier), strm));
     const int G2 = P.coop_grid;
@@ -2247,8 +2258,9 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
   pcg_init_kernel<double><<<g_rows, kThreads, 0, strm>>>(nb, s->bsr.row_ptr, s->bsr.col, s->A64, d_b, d_x, P.r, P.z,
                                                           P.p, pk, P.pinv, part_c, part_d, part_b);
   int g_rz0 = g_rows;
-  if (pk == OD_PRECOND_IC0) {
-    ic0_apply(s, P.r, P.z, nullptr);
+  if (swept) {
+    if (pk == OD_PRECOND_IC0) ic0_apply(s, P.r, P.z, nullptr);
+    else OD_TRY(ldlt_apply(s, P.r, P.z, nullptr));
     OD_KL(s);
     pcg_rz_kernel<<<g_vec, kThreads, 0, strm>>>(n, P.r, P.z, part_c, nullptr);
     g_rz0 = g_vec;
@@ -2276,8 +2288,9 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
       pcg_update_kernel<<<g_upd, kUpdThreads, 0, strm>>>(n, d_x, P.r, P.z, P.p, P.q, pk, P.pinv, part_a, g_rows,
                                                          part_c, part_b, P.sc, slot);
       int g_rz = g_upd;
-      if (pk == OD_PRECOND_IC0) {
-        ic0_apply(s, P.r, P.z, P.sc);
+      if (swept) {
+        if (pk == OD_PRECOND_IC0) ic0_apply(s, P.r, P.z, P.sc);
+        else OD_TRY(ldlt_apply(s, P.r, P.z, P.sc));
         OD_KL(s);
         pcg_rz_kernel<<<g_vec, kThreads, 0, strm>>>(n, P.r, P.z, part_c, P.sc);
         g_rz = g_vec;
@@ -2299,6 +2312,7 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
     ev_used = 0;
     if (P.sc_host->done) break;
   }
+  if (pk == OD_PRECOND_LDLT) OD_TRY(ldlt_check(s));
   return pcg_finish(s, d_b, d_x, shift, st, false, false);
 }
 

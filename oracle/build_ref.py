@@ -62,7 +62,8 @@ FILES = {
                  "invertibleStVK.cpp", "corotationalPlastic.h", "corotationalPlastic.cpp"],
     "solver": ["cgSolver.h", "cgSolver.cpp", "jacobiPreconditioner.h",
                "jacobiPreconditioner.cpp", "inCholeskyPreconditioner.h",
-               "inCholeskyPreconditioner.cpp"],
+               "inCholeskyPreconditioner.cpp", "inLDLTPreconditioner.h",
+               "inLDLTPreconditioner.cpp"],
     "intergrator": ["nonlinearImplicitBackwardEuler.h"],
 }
 

@@ -552,6 +552,7 @@ struct Scene {
   double rho = 0, lambda = 0, mu = 0, thr = 0, D[3] = {0, 0, 0};
   double yield = 0, creep = 0, max_plastic = 0;  // plastic parameters
   std::vector<double> plastic;          // plastic strain, 9 per tet (state, changes at every evaluation)
+  double ldlt_sainv = 0.1, ldlt_drop = 0.01;  // InLDLTPreconditioner(sainvEpsilon, ldltEpsilon)
   // pattern (reference layout)
   int nbc = 0, nrem = 0;
   std::vector<int> pcol, rows, oris, emap;
@@ -1164,7 +1165,147 @@ struct Precond {
   std::vector<int> rp, ci;
   std::vector<double> lv;
   double shift = 0.0;
+  // incomplete LDL^T (kind 4) in the reference's storage
+  double sainv_eps = 0.1, ldlt_eps = 0.01;
+  std::vector<double> lval, dinv;
+  std::vector<int> lrow, lpcol;
 };
+
+// Scalar columns of the symmetric matrix, both triangles, as
+// BlockedSymSparseMatrix::getFullIndices lists them (core/sparseMatrix.h:
+// 454-523): walking the stored values in index order, value k at lower
+// position (R, C) is appended to column C as (R, k) and, off the diagonal,
+// to column R as (C, k).
+void full_columns(const Scene& s, std::vector<std::vector<std::pair<int, int>>>& cols) {
+  const int n = s.dofs;
+  cols.assign(n, {});
+  auto put = [&](int R, int Cc, int k) {
+    cols[Cc].push_back({R, k});
+    if (R != Cc) cols[R].push_back({Cc, k});
+  };
+  for (int bc = 0; bc < s.nbc; bc++) {
+    int c0 = 3 * bc, off = s.oris[bc];
+    for (int k = s.pcol[bc]; k < s.pcol[bc + 1]; k++) {
+      int r0 = s.rows[k];
+      if (r0 == c0) {
+        static const int di[3] = {0, 3, 5};
+        for (int sc = 0; sc < 3; sc++)
+          for (int sr = sc; sr < 3; sr++) put(c0 + sr, c0 + sc, off + sr - sc + di[sc]);
+        off += 6;
+      } else {
+        int w = std::min(3, n - r0);
+        for (int sc = 0; sc < 3; sc++)
+          for (int sr = 0; sr < w; sr++) put(r0 + sr, c0 + sc, off + sc * w + sr);
+        off += 3 * w;
+      }
+    }
+  }
+  for (int k = 0; k < s.nrem; k++) {
+    int col = s.nbc + k, c = 3 * s.nbc + k, off = s.oris[col];
+    for (int q = s.pcol[col]; q < s.pcol[col + 1]; q++, off++) put(s.rows[q], c, off);
+  }
+}
+
+// sparse vector with entries in first-touch order (the reference's
+// FastSparseVector, core/latool.h:453-520)
+struct TouchVec {
+  std::vector<int> at, idx;
+  std::vector<double> val;
+  explicit TouchVec(int n) : at(n, -1) {}
+  void add(int i, double x) {
+    if (at[i] >= 0) { val[at[i]] += x; return; }
+    at[i] = (int)idx.size(); idx.push_back(i); val.push_back(x);
+  }
+  double get(int i) const { return at[i] >= 0 ? val[at[i]] : 0.0; }
+  void clear() { for (int i : idx) at[i] = -1; idx.clear(); val.clear(); }
+};
+
+// InLDLTPreconditioner::incompleteLDLTDecomposition
+// (solver/inLDLTPreconditioner.cpp:34-149).  Z starts as the identity; step
+// i takes column z_i, forms v = A z_i (SpMSV over the full columns), d_i =
+// z_i . v, then p_j = v . z_j for every later column meeting v's rows (rows
+// visited in v's first-touch order, each row's Z entries newest first),
+// stores L_ji = p_j / d_i when |L_ji| > ldltEpsilon, and replaces z_j by
+// z_j - (p_j / d_i) z_i keeping entries with |.| > sainvEpsilon.  Each row
+// keeps every entry ever written to it with the column's generation at the
+// time; an entry is live while its column is still pending and the
+// generation is current.
+void ldlt_factor(const Scene& s, const double* val, Precond& P) {
+  const int n = s.dofs;
+  std::vector<std::vector<std::pair<int, int>>> cols;
+  full_columns(s, cols);
+  struct RowEntry { int col, gen; double v; };
+  std::vector<std::vector<std::pair<int, double>>> Z(n);
+  std::vector<std::vector<RowEntry>> rowsZ(n);
+  std::vector<int> gen(n, 0);
+  std::vector<char> done(n, 0);
+  for (int j = 0; j < n; j++) { Z[j].push_back({j, 1.0}); rowsZ[j].push_back({j, 0, 1.0}); }
+  P.lval.clear(); P.lrow.clear(); P.lpcol.assign(n > 0 ? 1 : 0, 0); P.dinv.assign(n, 0.0);
+  if (n == 0) return;
+  TouchVec v(n), low(n), w(n);
+  auto a_times = [&](const std::vector<std::pair<int, double>>& zi) {
+    for (auto& e : zi)
+      for (auto& pr : cols[e.first]) v.add(pr.first, val[pr.second] * e.second);
+    double d = 0.0;
+    for (auto& e : zi) d += e.second * v.get(e.first);
+    return d;
+  };
+  for (int i = 0; i + 1 < n; i++) {
+    std::vector<std::pair<int, double>> zi;
+    zi.swap(Z[i]);
+    done[i] = 1;
+    const double inv = 1.0 / a_times(zi);
+    P.dinv[i] = inv;
+    for (size_t k = 0; k < v.idx.size(); k++) {
+      const double x = v.val[k];
+      if (x == 0.0) continue;
+      const std::vector<RowEntry>& re = rowsZ[v.idx[k]];
+      for (size_t q = re.size(); q-- > 0;) {
+        const RowEntry& e = re[q];
+        if (!done[e.col] && e.gen == gen[e.col]) low.add(e.col, x * e.v);
+      }
+    }
+    for (size_t k = 0; k < low.idx.size(); k++) {
+      const double l = low.val[k] * inv;
+      if (fabs(l) > P.ldlt_eps) { P.lval.push_back(l); P.lrow.push_back(low.idx[k]); }
+    }
+    P.lpcol.push_back((int)P.lval.size());
+    v.clear();
+    for (size_t k = 0; k < low.idx.size(); k++) {
+      if (low.val[k] == 0.0) continue;
+      const double f = low.val[k] * inv;
+      const int j = low.idx[k];
+      for (auto& e : Z[j]) w.add(e.first, e.second);
+      gen[j]++;
+      for (auto& e : zi) w.add(e.first, -f * e.second);
+      Z[j].clear();
+      for (size_t m = 0; m < w.idx.size(); m++)
+        if (fabs(w.val[m]) > P.sainv_eps) {
+          Z[j].push_back({w.idx[m], w.val[m]});
+          rowsZ[w.idx[m]].push_back({j, gen[j], w.val[m]});
+        }
+      w.clear();
+    }
+    low.clear();
+  }
+  P.dinv[n - 1] = 1.0 / a_times(Z[n - 1]);
+}
+
+// InLDLTPreconditioner::solvePreconditionerSystem (:151-184): L y = r by
+// columns, y *= D^-1, L^T z = y by row dots from the last row up.
+void ldlt_apply(int n, const Precond& P, const double* r, double* z) {
+  memcpy(z, r, sizeof(double) * n);
+  for (int c = 0; c + 1 < n; c++) {
+    const double sub = z[c];
+    for (int q = P.lpcol[c]; q < P.lpcol[c + 1]; q++) z[P.lrow[q]] -= P.lval[q] * sub;
+  }
+  for (int i = 0; i < n; i++) z[i] *= P.dinv[i];
+  for (int i = n - 2; i >= 0; i--) {
+    double dot = 0.0;
+    for (int q = P.lpcol[i]; q < P.lpcol[i + 1]; q++) dot += z[P.lrow[q]] * P.lval[q];
+    z[i] -= dot;
+  }
+}
 
 // row-oriented (up-looking) IC(0) of A + alpha diag(A) on the stored lower
 // pattern: for row i and each stored column j < i,
@@ -1259,6 +1400,8 @@ void precond_setup(const Scene& s, const double* val, Precond& P) {
       alpha = alpha == 0.0 ? 1e-3 : 2.0 * alpha;
     }
     P.shift = alpha;
+  } else if (P.kind == 4) {
+    ldlt_factor(s, val, P);
   }
 }
 
@@ -1273,6 +1416,8 @@ void precond_apply(const Scene& s, const Precond& P, const double* r, double* z)
       for (int i = 0; i < 3; i++) z[3 * bc + i] = m[3 * i] * rr[0] + m[3 * i + 1] * rr[1] + m[3 * i + 2] * rr[2];
     }
     for (int k = 0; k < s.nrem; k++) z[3 * s.nbc + k] = P.inv[9 * s.nbc + k] * r[3 * s.nbc + k];
+  } else if (P.kind == 4) {
+    ldlt_apply(n, P, r, z);
   } else {
     for (int i = 0; i < n; i++) {
       double sum = r[i];
@@ -1298,6 +1443,8 @@ int pcg(const Scene& s, const double* val, const double* b, double* x, double to
   for (int i = 0; i < n; i++) r[i] = b[i] - r[i];
   Precond P;
   P.kind = pkind;
+  P.sainv_eps = s.ldlt_sainv;
+  P.ldlt_eps = s.ldlt_drop;
   precond_setup(s, val, P);
   precond_apply(s, P, r.data(), d.data());
   auto dotp = [n](const double* a, const double* c) { double acc = 0; for (int i = 0; i < n; i++) acc += a[i] * c[i]; return acc; };
@@ -1342,6 +1489,7 @@ struct odo_scene {
   std::vector<double> v, dv, a, d, fext, K;
   double h = 0, alphaM = 0, betaK = 0, beta = 0.25, gamma = 0.5, tol = 1e-8;
   int maxit = 1000, pkind = 1, newton = 1;
+  Precond ldlt;   // stand-alone incomplete LDL^T factor (odo_ldlt_*)
 };
 
 odo_scene* odo_scene_create(int n_nodes, const double* X, int n_tets, const int* tets, int n_facets,
@@ -1425,6 +1573,33 @@ void odo_spmdv(odo_scene* o, const double* values, const double* x, double* y) {
 int odo_pcg(odo_scene* o, const double* values, const double* b, double* x, double tol, int maxit, int pkind) {
   return pcg(o->s, values, b, x, tol, maxit, pkind);
 }
+
+// drop bounds of the incomplete LDL^T (preconditioner kind 4)
+void odo_set_ldlt(odo_scene* o, double sainv_eps, double ldlt_eps) {
+  o->s.ldlt_sainv = sainv_eps;
+  o->s.ldlt_drop = ldlt_eps;
+}
+
+// stand-alone factor of A = values (kept for odo_ldlt_get / odo_ldlt_apply);
+// returns the number of stored L entries
+int odo_ldlt_factor(odo_scene* o, const double* values) {
+  o->ldlt = Precond();
+  o->ldlt.kind = 4;
+  o->ldlt.sainv_eps = o->s.ldlt_sainv;
+  o->ldlt.ldlt_eps = o->s.ldlt_drop;
+  ldlt_factor(o->s, values, o->ldlt);
+  return (int)o->ldlt.lval.size();
+}
+
+void odo_ldlt_get(odo_scene* o, double* values, int* rows, int* pcol, double* inv_diag) {
+  const Precond& P = o->ldlt;
+  if (!P.lval.empty()) memcpy(values, P.lval.data(), sizeof(double) * P.lval.size());
+  if (!P.lrow.empty()) memcpy(rows, P.lrow.data(), sizeof(int) * P.lrow.size());
+  if (!P.lpcol.empty()) memcpy(pcol, P.lpcol.data(), sizeof(int) * P.lpcol.size());
+  if (!P.dinv.empty()) memcpy(inv_diag, P.dinv.data(), sizeof(double) * P.dinv.size());
+}
+
+void odo_ldlt_apply(odo_scene* o, const double* rhs, double* out) { ldlt_apply(o->s.dofs, o->ldlt, rhs, out); }
 
 // Loads (Forcer, core/forcer.cpp:8-96): body force density times V/4 per
 // node (tetelement.cpp:68-77), tractions times the deformed facet area / 3

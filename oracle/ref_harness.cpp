@@ -59,6 +59,7 @@
 #include "cgSolver.h"
 #include "jacobiPreconditioner.h"
 #include "inCholeskyPreconditioner.h"
+#include "inLDLTPreconditioner.h"
 #include "intergrator.h"
 #include "nonlinearImplicitBackwardEuler.h"
 #undef private
@@ -88,6 +89,7 @@ Preconditioner* make_preconditioner(int kind, double eps, double relax) {
   switch (kind) {
     case 1: return new JacobiPreconditioner();
     case 2: return new InCholeskyPreconditioner(eps, relax);
+    case 3: return new InLDLTPreconditioner(eps, relax);  // (sainvEpsilon, ldltEpsilon)
     default: return new Preconditioner();
   }
 }
@@ -130,6 +132,8 @@ struct RefScene {
   // Newmark
   RefNewmark* nm = nullptr;
   CountingPreconditioner* nm_precond = nullptr;
+  // a stand-alone incomplete LDL^T factor (odref_ldlt_*)
+  InLDLTPreconditioner* ldlt = nullptr;
 };
 
 static void write_free_dofs_to_mesh(RefScene* s, const double* d) {
@@ -195,6 +199,7 @@ void odref_scene_destroy(void* p) {
   if (s->nm) { delete s->nm->K; delete s->nm; }
   delete s->pattern;
   delete s->mass;
+  delete s->ldlt;
   delete s;
 }
 
@@ -334,6 +339,37 @@ int odref_cg(void* p, const double* values, const double* b, double* x, double t
   solver.resetLinearSystem(s->pattern);
   solver.solveLinearSystem(b, x);
   return cp->applications - 1;
+}
+
+// InLDLTPreconditioner::Preprocess on A (scene pattern, given values) with
+// (sainvEpsilon, ldltEpsilon); returns the number of stored L entries.  The
+// factor is kept for odref_ldlt_get / odref_ldlt_apply.
+int odref_ldlt_factor(void* p, const double* values, double sainv_eps, double ldlt_eps) {
+  RefScene* s = (RefScene*)p;
+  memcpy(s->pattern->values, values, sizeof(double) * s->pattern->getNumEntries());
+  delete s->ldlt;
+  s->ldlt = new InLDLTPreconditioner(sainv_eps, ldlt_eps);
+  s->ldlt->resetPreconditionerSystem(*s->pattern);
+  s->ldlt->Preprocess(*s->pattern);
+  return (int)s->ldlt->values.size();
+}
+
+// the factor in the reference's storage: L columns 0..dofs-2 (pcol has
+// dofs entries; rows in each column in the order they were produced) and
+// the inverted diagonal (dofs entries)
+void odref_ldlt_get(void* p, double* values, int* rows, int* pcol, double* inv_diag) {
+  RefScene* s = (RefScene*)p;
+  const InLDLTPreconditioner* f = s->ldlt;
+  memcpy(values, f->values.data(), sizeof(double) * f->values.size());
+  memcpy(rows, f->rows.data(), sizeof(int) * f->rows.size());
+  memcpy(pcol, f->pcol.data(), sizeof(int) * f->pcol.size());
+  memcpy(inv_diag, f->invDiagonal.data(), sizeof(double) * f->invDiagonal.size());
+}
+
+// result = (L D L^T)^-1 rhs with the kept factor (solvePreconditionerSystem)
+void odref_ldlt_apply(void* p, const double* rhs, double* result) {
+  RefScene* s = (RefScene*)p;
+  s->ldlt->solvePreconditionerSystem(s->dofs, rhs, result);
 }
 
 // Loads: body force density (N/m^3) over all elements, then uniform

@@ -65,6 +65,10 @@ def lib():
         L.odref_eigsym.argtypes = [_dp, _dp, _dp]
         L.odref_plastic_params.argtypes = [C.c_double, C.c_double, C.c_double]
         L.odref_plastic_state.argtypes = [C.c_void_p, _dp]
+        L.odref_ldlt_factor.restype = C.c_int
+        L.odref_ldlt_factor.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double]
+        L.odref_ldlt_get.argtypes = [C.c_void_p, _dp, _ip, _ip, _dp]
+        L.odref_ldlt_apply.argtypes = [C.c_void_p, _dp, _dp]
         _lib = L
     return _lib
 
@@ -77,7 +81,7 @@ def _i(a):
     return a.ctypes.data_as(_ip)
 
 
-PRECOND = {"none": 0, "jacobi": 1, "ic": 2}
+PRECOND = {"none": 0, "jacobi": 1, "ic": 2, "ldlt": 3}
 MATERIAL = {"corotational": 0, "neohookean": 1, "stvk": 2, "corotational_plastic": 3}
 
 
@@ -174,6 +178,25 @@ class RefScene:
         x = np.zeros(self.dofs) if x0 is None else np.array(x0, dtype=np.float64)
         it = lib().odref_cg(self.h, _d(values), _d(b), _d(x), tol, maxit, PRECOND[precond], eps, relax)
         return x, it
+
+    def ldlt(self, values, sainv_eps, ldlt_eps):
+        """InLDLTPreconditioner::Preprocess on A = values: returns (L values,
+        L rows, pcol, inverted diagonal) in the reference's storage."""
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        nnz = lib().odref_ldlt_factor(self.h, _d(values), sainv_eps, ldlt_eps)
+        lv = np.zeros(max(nnz, 1))
+        lr = np.zeros(max(nnz, 1), dtype=np.int32)
+        pc = np.zeros(max(self.dofs, 1), dtype=np.int32)
+        dinv = np.zeros(self.dofs)
+        lib().odref_ldlt_get(self.h, _d(lv), _i(lr), _i(pc), _d(dinv))
+        return lv[:nnz], lr[:nnz], pc, dinv
+
+    def ldlt_apply(self, rhs):
+        """(L D L^T)^-1 rhs with the factor of the last ldlt() call."""
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64)
+        out = np.zeros(self.dofs)
+        lib().odref_ldlt_apply(self.h, _d(rhs), _d(out))
+        return out
 
     def loads(self, body=None, tractions=()):
         """Rebuild the load set: body force density then (traction, facets) pairs."""

@@ -16,7 +16,7 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _lib = None
 
-PRECOND = {"none": 0, "jacobi": 1, "block_jacobi": 2, "ic0": 3}
+PRECOND = {"none": 0, "jacobi": 1, "block_jacobi": 2, "ic0": 3, "ldlt": 4}
 MATERIAL = {"corotational": 0, "neohookean": 1, "stvk": 2, "corotational_plastic": 3}
 
 
@@ -56,6 +56,11 @@ def lib():
         L.odo_polar.argtypes = [_dp, _dp, _dp]
         L.odo_qr.argtypes = [_dp, _dp, _dp]
         L.odo_eigsym.argtypes = [_dp, _dp, _dp]
+        L.odo_set_ldlt.argtypes = [C.c_void_p, C.c_double, C.c_double]
+        L.odo_ldlt_factor.restype = C.c_int
+        L.odo_ldlt_factor.argtypes = [C.c_void_p, _dp]
+        L.odo_ldlt_get.argtypes = [C.c_void_p, _dp, _ip, _ip, _dp]
+        L.odo_ldlt_apply.argtypes = [C.c_void_p, _dp, _dp]
         _lib = L
     return _lib
 
@@ -162,6 +167,28 @@ class OracleScene:
         x = np.zeros(self.dofs) if x0 is None else np.array(x0, dtype=np.float64)
         it = lib().odo_pcg(self.h, _d(values), _d(b), _d(x), tol, maxit, PRECOND[precond])
         return x, it
+
+    def set_ldlt(self, sainv_eps=0.1, ldlt_eps=0.01):
+        """Drop bounds of the incomplete LDL^T (precond "ldlt")."""
+        lib().odo_set_ldlt(self.h, float(sainv_eps), float(ldlt_eps))
+
+    def ldlt(self, values):
+        """Incomplete LDL^T of A = values with the bounds of set_ldlt: (L
+        values, L rows, pcol, inverted diagonal) in the reference's storage."""
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        nnz = lib().odo_ldlt_factor(self.h, _d(values))
+        lv = np.zeros(max(nnz, 1))
+        lr = np.zeros(max(nnz, 1), np.int32)
+        pc = np.zeros(max(self.dofs, 1), np.int32)
+        dinv = np.zeros(max(self.dofs, 1))
+        lib().odo_ldlt_get(self.h, _d(lv), _i(lr), _i(pc), _d(dinv))
+        return lv[:nnz], lr[:nnz], pc[: self.dofs], dinv[: self.dofs]
+
+    def ldlt_apply(self, rhs):
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64)
+        out = np.zeros(self.dofs)
+        lib().odo_ldlt_apply(self.h, _d(rhs), _d(out))
+        return out
 
     def loads(self, body=None, tractions=()):
         t = np.zeros((max(len(tractions), 1), 3))

@@ -21,9 +21,13 @@ the GPU path against them.  Cases:
   random and near-singular matrices;
 * ``plastic``: the corotational plastic material: assembled values, f_int and
   plastic strain after three evaluations at growing displacements (each
-  evaluation updates the plastic strain), and backward-Euler steps.
+  evaluation updates the plastic strain), and backward-Euler steps;
+* ``ldlt_<material>_<constraints>``: InLDLTPreconditioner: the factor (L
+  values, rows, pcol, inverted diagonal) of A = K/3600 + M at two drop-bound
+  pairs, its apply on a seeded vector, CG with it, and backward-Euler steps
+  preconditioned by it.
 
-``--only NAME`` writes one group (pattern, elements, integrators, kat, plastic).
+``--only NAME`` writes one group (plastic or ldlt; the full run writes all).
 """
 from __future__ import annotations
 
@@ -92,14 +96,55 @@ def plastic_case():
          be_params=np.array([1.0 / 60.0, 0.01, 0.001, 1e-10]), **out)
 
 
+LDLT_EPS = ((0.1, 0.01), (0.05, 0.005))         # (sainvEpsilon, ldltEpsilon) pairs
+
+
+def ldlt_cases():
+    g = small_mesh()
+    cases = {"full": meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0)),
+             "partial": partial_constraints(g)}
+    rng = np.random.default_rng(321)
+    u = rng.normal(scale=0.002, size=(g.n_nodes, 3))
+    for mat in ("corotational", "neohookean"):
+        rho, E, nu, thr = MATS[mat]
+        for cname, cd in cases.items():
+            s = R.RefScene(g.X, g.tets, g.facets, cd, mat, rho, E, nu, thr)
+            s.set_displacements(u)
+            vals, _ = s.assemble()
+            A = vals * (1.0 / 3600.0) + s.mass()
+            out = {}
+            for k, (se, le) in enumerate(LDLT_EPS):
+                lv, lr, pc, dinv = s.ldlt(A, se, le)
+                r = rng.normal(size=s.dofs)
+                out.update({f"l_values_{k}": lv, f"l_rows_{k}": lr, f"l_pcol_{k}": pc, f"inv_diag_{k}": dinv,
+                            f"apply_r_{k}": r, f"apply_z_{k}": s.ldlt_apply(r)})
+                b = rng.normal(size=s.dofs)
+                x, its = s.cg(A, b, tol=1e-10, maxit=2000, precond="ldlt", eps=se, relax=le)
+                out.update({f"cg_b_{k}": b, f"cg_x_{k}": x, f"cg_iters_{k}": its})
+            se, le = LDLT_EPS[0]
+            s = R.RefScene(g.X, g.tets, g.facets, cd, mat, rho, E, nu, thr)
+            s.be_setup(1.0 / 60.0, 0.01, 0.001, tol=1e-10, maxit=2000, precond="ldlt", eps=se, relax=le)
+            fext = s.loads(body=[0.0, 0.0, -9800.0])
+            s.be_apply_loads()
+            iters = s.be_step(10)
+            save(f"ldlt_{mat}_{cname}", X=g.X, tets=g.tets, facets=g.facets, cdofs=cd, u=u, A=A,
+                 eps=np.array(LDLT_EPS), material=np.array([rho, E, nu, thr]), be_fext=fext,
+                 be_u=s.displacements(), be_v=s.be_velocity(), be_steps=10, be_iters=iters,
+                 be_params=np.array([1.0 / 60.0, 0.01, 0.001, 1e-10]), **out)
+
+
 def main():
     only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
     if only == "plastic":
         plastic_case()
         print("golden fixture plastic written to", OUT)
         return
+    if only == "ldlt":
+        ldlt_cases()
+        print("golden fixtures ldlt_* written to", OUT)
+        return
     if only is not None:
-        raise SystemExit(f"--only {only}: only 'plastic' writes a single group")
+        raise SystemExit(f"--only {only}: single groups are 'plastic' and 'ldlt'")
     g = small_mesh()
     cases = {"full": meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0)),
              "partial": partial_constraints(g)}
@@ -175,6 +220,7 @@ def main():
     save("kat_math", F=Fs, polar_R=polR, polar_S=polS, qr_Q=qrQ, qr_R=qrR, tri=tri, eig_vals=ev,
          eig_vecs=evec)
     plastic_case()
+    ldlt_cases()
     print("golden fixtures written to", OUT)
 
 
