@@ -21,7 +21,9 @@ prescribed top displacements solved with the FP64 and with the mixed-precision
 PCG (steps/s of both, the displacement error between them, and the HBM
 roofline of the FP32 SpMV phase measured inside the solve), and
 "batched_tier", 512 uneven scenes stepped one by one with the FP64 solver and
-together through od_batch with the mixed solver.
+together through od_batch with the mixed solver; "serving_tier", Poisson step
+requests over a pool of scenes; "ldlt_tier", the headline step preconditioned
+by the reference's incomplete LDL^T, beside the reference's CPU code for it.
 """
 from __future__ import annotations
 
@@ -304,6 +306,87 @@ def precision_tier(args, api, ctx):
                                                 "phase_ms": sms},
                               "bytes_rule": "stored 3x3 blocks x 40 B (9 FP32 values + int32 column) + 24 B per "
                                             "block row (own p read, q written)"}}
+
+
+def ldlt_tier(args, api, ctx):
+    """The headline beam workload (98,304 tets, Newmark, 3 Newton iterations,
+    tolerance 1e-8) preconditioned by the reference's incomplete LDL^T
+    (InLDLTPreconditioner(0.1, 0.01)): the factor is remade on the host for
+    every solve as the reference does (bit-identical to it), the two
+    triangular sweeps of every apply run on the device.  Wall time per step
+    (the host factorisations are inside it), the apply's device time from a
+    profiled step, and the reference's own CPU code on the same step."""
+    wl = WORKLOADS["beam98k_nh_newmark"]
+    g = wl["mesh"]()
+    cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+    kind, rho, E, nu, thr = wl["material"]
+    se, le = 0.1, 0.01
+    s = api.Scene(ctx, g.X, g.tets, g.facets, cd, api.Material(kind, rho, E, nu, thr))
+    s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, wl["alpha_m"], wl["beta_k"], wl["dt"],
+                                             api.CGSolver(wl["tol"], 5000, api.InLDLTPreconditioner(se, le)),
+                                             wl["newton"]))
+    s.set_loads(body=wl["body"], tractions=traction_groups(g, wl["traction"]))
+    s.set_traction_schedule(wl["freq"])
+    s.step(1)
+    steps = max(2, min(args.tier_steps, 4))
+    ctx.reset_counters()
+    walls, it, solves = [], 0, 0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        st = s.step(1)
+        walls.append(time.perf_counter() - t0)
+        if st.status != 0:
+            raise RuntimeError(f"ldlt tier: step status {st.status}")
+        it += st.pcg_iterations
+        solves += st.solves
+    c = ctx.counters()
+    factor_ms = c.ldlt_factor_ms / max(1, c.ldlt_factors)
+    ctx.reset_counters()
+    ctx.set_profiling(True)
+    s.step(1)
+    ctx.set_profiling(False)
+    p = ctx.counters()
+    s.close()
+    apply_ms = p.ldlt_apply_ms / max(1, p.ldlt_applies)
+    peak, peak_kind = peaks()
+    gbs = p.ldlt_apply_bytes / (p.ldlt_apply_ms * 1e-3) / 1e9 if p.ldlt_apply_ms else None
+    out = {"workload": "beam98k_nh_newmark_ldlt", "n_tets": g.n_tets, "precond": f"InLDLTPreconditioner({se}, {le})",
+           "steps": steps, "wall_ms_per_step": 1000 * statistics.mean(walls),
+           "steps_per_s": 1.0 / statistics.mean(walls), "pcg_iterations_per_step": it / steps,
+           "solves_per_step": solves / steps, "factor_ms_per_solve": factor_ms, "factor_nnz": c.ldlt_nnz,
+           "apply": {"kernel": "ldlt_apply_kernel (forward and backward sweeps, one cooperative launch)",
+                     "bound": "latency: dependency chain", "levels": p.ldlt_levels, "avg_launch_ms": apply_ms,
+                     "us_per_level": 1000.0 * apply_ms / max(1, p.ldlt_levels), "launches": p.ldlt_applies,
+                     "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak if gbs else None,
+                     "peak_source": peak_kind,
+                     "bytes_rule": "L entries x 12 B (value + index) per sweep + 6 x 8 B per row"},
+           "share_of_step": {"host_factor": factor_ms * solves / steps / (1000 * statistics.mean(walls))}}
+    if not args.no_cpu_baseline:
+        try:
+            from oracle import build_ref, reforacle
+            if not reforacle.available():
+                build_ref.build()
+            r = reforacle.RefScene(g.X, g.tets, g.facets, cd, kind, rho, E, nu, thr)
+            r.nm_setup(wl["dt"], wl["alpha_m"], wl["beta_k"], newton=wl["newton"], tol=wl["tol"], maxit=5000,
+                       precond="ldlt", eps=se, relax=le)
+            t, n_ref, used = 0.0, 0, 0.0
+            while n_ref < 2:
+                t += wl["dt"]
+                scale = math.sin(2 * math.pi * wl["freq"] * t)
+                t0 = time.perf_counter()
+                r.loads(body=wl["body"], tractions=[(np.array(tr) * scale, fac) for tr, fac in
+                                                    traction_groups(g, wl["traction"])])
+                r.nm_apply_loads()
+                r.nm_step(1)
+                used += time.perf_counter() - t0
+                n_ref += 1
+            out["cpu_reference"] = {"steps_per_s": n_ref / used, "cores": 1, "kind": "reference",
+                                    "sample": f"{n_ref} Newmark steps, reference code with its "
+                                              "InLDLTPreconditioner, single thread"}
+            out["speedup_vs_cpu_reference"] = out["steps_per_s"] / out["cpu_reference"]["steps_per_s"]
+        except Exception as exc:
+            out["cpu_reference"] = {"error": str(exc)}
+    return out
 
 
 def batched_tier(args, api, ctx):
@@ -596,7 +679,7 @@ def run_gpu(args, wl):
         del scene
         only = [t for t in args.only_tiers.split(",") if t]
         for name, fn in (("precision_tier", precision_tier), ("batched_tier", batched_tier),
-                         ("serving_tier", serving_tier)):
+                         ("serving_tier", serving_tier), ("ldlt_tier", ldlt_tier)):
             if only and name.split("_")[0] not in only:
                 continue
             try:
@@ -638,7 +721,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tiers", action="store_true", help="skip the mixed-precision and batched workloads")
     ap.add_argument("--tier-steps", type=int, default=5)
-    ap.add_argument("--only-tiers", default="", help="comma list of precision,batched,serving (default: all)")
+    ap.add_argument("--only-tiers", default="", help="comma list of precision,batched,serving,ldlt (default: all)")
     ap.add_argument("--precision-nz", type=int, default=64,
                     help="cube layers of the precision-tier block (64: 2,621,440 tets)")
     ap.add_argument("--serving-pool", type=int, default=512)

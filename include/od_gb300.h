@@ -153,6 +153,8 @@ typedef struct od_counters {
   long long ldlt_applies;     /* LDL^T applies timed while profiling is on */
   double ldlt_apply_ms;       /* their summed CUDA-event durations */
   double ldlt_apply_bytes;    /* their algorithmic bytes: 2 x (nnz x 12 B) + 6 x 8 B per row */
+  long long ldlt_levels;      /* dependency levels of the last factor's two sweeps (the apply's
+                                 critical path, in rows) */
 } od_counters;
 
 typedef struct od_scene_info {

@@ -86,7 +86,8 @@ class od_counters(C.Structure):
                 ("mix_iterations", C.c_longlong), ("mix_spmv_ms", C.c_double), ("mix_spmv_bytes", C.c_double),
                 ("mix_spmv_work_ms", C.c_double), ("mix_fallbacks", C.c_longlong),
                 ("ldlt_factors", C.c_longlong), ("ldlt_factor_ms", C.c_double), ("ldlt_nnz", C.c_longlong),
-                ("ldlt_applies", C.c_longlong), ("ldlt_apply_ms", C.c_double), ("ldlt_apply_bytes", C.c_double)]
+                ("ldlt_applies", C.c_longlong), ("ldlt_apply_ms", C.c_double), ("ldlt_apply_bytes", C.c_double),
+                ("ldlt_levels", C.c_longlong)]
 
 
 class od_scene_info(C.Structure):

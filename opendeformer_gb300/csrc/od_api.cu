@@ -197,6 +197,7 @@ od_status od_ctx_get_counters(od_ctx* ctx, od_counters* out) {
   out->ldlt_applies = ctx->c.ldlt_applies;
   out->ldlt_apply_ms = ctx->c.ldlt_apply_ms;
   out->ldlt_apply_bytes = ctx->c.ldlt_apply_bytes;
+  out->ldlt_levels = ctx->c.ldlt_levels;
   return OD_OK;
 }
 
@@ -207,7 +208,7 @@ od_status od_ctx_reset_counters(od_ctx* ctx) {
   ctx->c.spmv_ms = ctx->c.pcg_kernel_ms = 0.0;
   ctx->c.mix_iters = ctx->c.mix_fallbacks = 0;
   ctx->c.mix_spmv_ms = ctx->c.mix_spmv_bytes = ctx->c.mix_spmv_work_ms = 0.0;
-  ctx->c.ldlt_factors = ctx->c.ldlt_nnz = ctx->c.ldlt_applies = 0;
+  ctx->c.ldlt_factors = ctx->c.ldlt_nnz = ctx->c.ldlt_applies = ctx->c.ldlt_levels = 0;
   ctx->c.ldlt_factor_ms = ctx->c.ldlt_apply_ms = ctx->c.ldlt_apply_bytes = 0.0;
   return OD_OK;
 }

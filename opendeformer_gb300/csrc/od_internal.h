@@ -241,7 +241,7 @@ struct Ctx {
   double pcg_kernel_ms = 0.0;
   long long mix_iters = 0;            // inner FP32 loop iterations (profiling)
   long long mix_fallbacks = 0;        // mixed solves finished by the FP64 solver
-  long long ldlt_factors = 0, ldlt_nnz = 0, ldlt_applies = 0;
+  long long ldlt_factors = 0, ldlt_nnz = 0, ldlt_applies = 0, ldlt_levels = 0;
   double ldlt_factor_ms = 0.0, ldlt_apply_ms = 0.0, ldlt_apply_bytes = 0.0;
   double mix_spmv_ms = 0.0;
   double mix_spmv_work_ms = 0.0;

@@ -314,6 +314,7 @@ od_status ldlt_factor(Scene* s, const double* host_values, double sainv_eps, dou
   Ctx* ctx = s->ctx;
   ctx->ldlt_factors++;
   ctx->ldlt_nnz = nnz;
+  ctx->ldlt_levels = (long long)l->depth_f + l->depth_b;
   ctx->ldlt_factor_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return OD_OK;
 }
