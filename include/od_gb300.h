@@ -15,6 +15,7 @@
  *   Preconditioner (+ Jacobi, IC)          core/preconditioner.h:12-22
  *   InLDLTPreconditioner                   solver/inLDLTPreconditioner.h:12-44
  *   Forcer                                 core/forcer.h:13-22
+ *   MeshPlaneCollisionDampingForcer        collision/penaltyDampingForcer.h:25-35
  *   Intergrator / NonlinearImplicitBackwardEuler
  *                                          core/intergrator.h:13-35,
  *                                          intergrator/nonlinearImplicitBackwardEuler.h:48-128
@@ -244,6 +245,24 @@ od_status od_scene_ldlt_factor(od_scene* scene, const double* values, double sai
                                long long* nnz);
 od_status od_scene_ldlt_get(od_scene* scene, double* values, int* rows, int* pcol, double* inv_diag);
 od_status od_scene_ldlt_apply(od_scene* scene, const double* rhs, double* result);
+
+/* Collision damping (collision/penaltyDampingForcer.cpp:8-61,
+ * intergrator/nonlinearImplicitBackwardEuler.h:122-128).
+ * od_scene_add_plane_damping is MeshPlaneCollisionDampingForcer: for every
+ * element of elems (original element ids; an id listed twice is added
+ * twice) against the plane normal.x + constant = 0 it adds the forcer's
+ * damping block to the scene's external damping matrix, at the current
+ * displacements, with node velocities node_velocities (n_nodes x 3) or,
+ * when NULL, the integrator's current velocities (constrained DOFs 0, as
+ * getMeshVerticesVelocities gives them) -- addExternalDampingForceMatrix.
+ * od_scene_clear_damping is clearExternalDampingForceMatrix.  Both
+ * integrators use the matrix (backward Euler as the reference does; the
+ * Newmark step in C = alpha_M M + beta_K K + D). */
+od_status od_scene_add_plane_damping(od_scene* scene, const double* normal, double constant, double damping,
+                                     int n_elems, const int* elems, const double* node_velocities);
+od_status od_scene_clear_damping(od_scene* scene);
+/* the external damping matrix values (reference layout, num_values entries) */
+od_status od_scene_get_damping(od_scene* scene, double* values);
 
 /* Forcer + Intergrator::setExternalVirtualWork (core/forcer.cpp:8-96,
  * nonlinearImplicitBackwardEuler.h:118-120): body force density (N/m^3, may be

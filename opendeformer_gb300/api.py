@@ -157,6 +157,9 @@ SIGNATURES = {
     "od_scene_ldlt_factor": (C.c_int, [_vp, _dp, C.c_double, C.c_double, C.POINTER(C.c_longlong)]),
     "od_scene_ldlt_get": (C.c_int, [_vp, _dp, _ip, _ip, _dp]),
     "od_scene_ldlt_apply": (C.c_int, [_vp, _dp, _dp]),
+    "od_scene_add_plane_damping": (C.c_int, [_vp, _dp, C.c_double, C.c_double, C.c_int, _ip, _dp]),
+    "od_scene_clear_damping": (C.c_int, [_vp]),
+    "od_scene_get_damping": (C.c_int, [_vp, _dp]),
     "od_scene_set_loads": (C.c_int, [_vp, _dp, C.c_int, _dp, _ip, _ip]),
     "od_scene_update_loads": (C.c_int, [_vp, C.c_double]),
     "od_scene_set_traction_schedule": (C.c_int, [_vp, C.c_double, C.c_double]),
@@ -490,6 +493,30 @@ class Scene:
         out = np.zeros(self.dofs)
         _check(load_library().od_scene_ldlt_apply(self.h, _d(rhs), _d(out)), "ldlt_apply")
         return out
+
+    def add_plane_damping(self, normal, constant, dampingCoefficient, elements, node_velocities=None):
+        """MeshPlaneCollisionDampingForcer for each element against the plane
+        normal.x + constant = 0, added to the external damping matrix
+        (addExternalDampingForceMatrix); velocities: the integrator's unless
+        given (n_nodes x 3)."""
+        nrm = np.ascontiguousarray(normal, dtype=np.float64)
+        el = np.ascontiguousarray(elements, dtype=np.int32)
+        vel = None
+        if node_velocities is not None:
+            vel = np.ascontiguousarray(node_velocities, dtype=np.float64).reshape(-1)
+        _check(load_library().od_scene_add_plane_damping(self.h, _d(nrm), float(constant), float(dampingCoefficient),
+                                                          el.size, _i(el), _d(vel) if vel is not None else None),
+               "add_plane_damping")
+
+    def clear_damping(self):
+        """clearExternalDampingForceMatrix."""
+        _check(load_library().od_scene_clear_damping(self.h), "clear_damping")
+
+    def damping_values(self):
+        """The external damping matrix values (reference layout)."""
+        v = np.zeros(self.n_values)
+        _check(load_library().od_scene_get_damping(self.h, _d(v)), "damping_values")
+        return v
 
     def set_loads(self, body=None, tractions=()):
         """Forcer: body force density (N/m^3) then (traction Pa, facet ids) groups."""

@@ -20,7 +20,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]
 SOURCES = ["od_host.cpp", "od_rif.cpp", "od_elements.cu", "od_sparse.cu", "od_api.cu", "od_batch.cu",
-           "od_noalloc.cu", "od_ldlt.cu"]
+           "od_noalloc.cu", "od_ldlt.cu", "od_collision.cu"]
+# per-file flags: the collision geometry rounds every operation separately,
+# as the reference's compiled code does
+FILE_FLAGS = {"od_collision.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -55,7 +58,7 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
             cmd = [cc, "-x", "c++", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
                    "-c", path, "-o", obj]
         else:
-            cmd = [cc, *ARCH, *NVCC_FLAGS, *(extra or []), "-c", path, "-o", obj]
+            cmd = [cc, *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(src, []), *(extra or []), "-c", path, "-o", obj]
         if verbose:
             print(" ".join(cmd))
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))

@@ -30,6 +30,13 @@ Fixes applied (each is a compile error under g++ 13 otherwise):
    ``intergrator/nonlinearImplicitBackwardEuler.h``: add ``typename``.
 7. compile with ``-DODER_CORE_DATASTRUCTURE_H`` so ``core/datastructure.h``
    (mesher-only templates that shadow ``T``) is skipped.
+8. ``collision/intersection.cpp``: keep the plane-tetrahedron intersection and
+   the barycentric coordinates; drop the tetrahedron-tetrahedron
+   intersection after them and its mesher includes (the mesher's exact
+   arithmetic uses MSVC-only in-class specialisations);
+   ``collision/penaltyDampingForcer.cpp``: drop
+   MeshMeshCollisionDampingForcer::addDampingMatrix, its only caller (it
+   computes an intersection and adds nothing to the matrix).
 
 No ``-ffast-math``: the oracle is defined as this IEEE-strict g++ build.
 """
@@ -65,6 +72,8 @@ FILES = {
                "inCholeskyPreconditioner.cpp", "inLDLTPreconditioner.h",
                "inLDLTPreconditioner.cpp"],
     "intergrator": ["nonlinearImplicitBackwardEuler.h"],
+    "collision": ["collisionShapes.h", "intersection.h", "intersection.cpp", "penaltyDampingForcer.h",
+                  "penaltyDampingForcer.cpp"],
 }
 
 
@@ -124,7 +133,23 @@ def _patch(root: str) -> None:
         return _replace(t, "using AssemblerType = SpMatrix::Assembler;",
                         "using AssemblerType = typename SpMatrix::Assembler;", p)
 
+    def intersection(t, p):
+        # keep the plane-tetrahedron part; the tetrahedron-tetrahedron
+        # intersection below it needs the mesher's exact arithmetic, which
+        # does not compile under g++
+        t = _replace(t, '#include "delPrimitive.h"\n#include "predicate.h"\n#include "geometer.h"\n', "", p)
+        cut = t.index("\t\tvoid digCavity(")
+        return t[:cut] + "\t}\n}\n"
+
+    def damping(t, p):
+        # MeshMeshCollisionDampingForcer::addDampingMatrix calls that
+        # tetrahedron-tetrahedron intersection (and adds nothing)
+        cut = t.index("\t\tvoid MeshMeshCollisionDampingForcer::addDampingMatrix")
+        return t[:cut] + "\t}\n}\n"
+
     rw("core/oder.h", oder)
+    rw("collision/intersection.cpp", intersection)
+    rw("collision/penaltyDampingForcer.cpp", damping)
     rw("core/memory.h", memory)
     rw("core/sparseMatrix.h", sparse)
     rw("core/intergrator.h", integ)

@@ -1468,6 +1468,150 @@ int pcg(const Scene& s, const double* val, const double* b, double* x, double to
   return it;
 }
 
+// ------------------------------------------------- plane collision damping
+// Plane n.x + c = 0 against a deformed tetrahedron P[4]
+// (collision/intersection.cpp:12-117): the part of the tetrahedron on the
+// negative side (n.x + c < 1e-6) gives a centroid and a direction whose
+// length is six times that part's volume (all four vertices inside: the
+// plane normal times the full volume; none: the vertex nearest the plane
+// and a zero direction).  Edge points are clamped to the edge.
+V3 plane_edge_point(V3 n, double c, V3 pa, V3 pb) {
+  V3 ab = sub(pb, pa);
+  double t = (-c - dot(n, pa)) / dot(n, ab);
+  t = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
+  return add(pa, scale(ab, t));
+}
+
+V3 unit(V3 a) { return divv(a, sqrt(len2(a))); }
+
+void plane_tet(V3 n, double c, const V3* P, V3& centroid, V3& dir) {
+  V3 neg[4], pos[4];
+  int nn = 0, np = 0;
+  for (int i = 0; i < 4; i++) {
+    if (dot(n, P[i]) + c < 1e-6) neg[nn++] = P[i];
+    else pos[np++] = P[i];
+  }
+  if (nn == 0) {
+    double best = 1.7976931348623157e308;
+    for (int i = 0; i < 4; i++) {
+      double d = dot(n, P[i]) + c;
+      if (d < best) { best = d; centroid = P[i]; }
+    }
+    dir = {0.0, 0.0, 0.0};
+  } else if (nn == 1) {
+    V3 q0 = plane_edge_point(n, c, neg[0], pos[0]);
+    V3 q1 = plane_edge_point(n, c, neg[0], pos[1]);
+    V3 q2 = plane_edge_point(n, c, neg[0], pos[2]);
+    centroid = scale(add(add(add(neg[0], q0), q1), q2), 0.25);
+    V3 ab = sub(q0, neg[0]), ac = sub(q1, neg[0]), ad = sub(q2, neg[0]);
+    double sv = dot(ab, cross(ac, ad));
+    dir = scale(unit(add(add(cross(ab, ac), cross(ac, ad)), cross(ad, ab))), fabs(sv));
+    if (sv < 0.0) dir = scale(dir, -1.0);
+  } else if (nn == 2) {
+    V3 q0 = plane_edge_point(n, c, neg[0], pos[0]);
+    V3 q1 = plane_edge_point(n, c, neg[0], pos[1]);
+    V3 q2 = plane_edge_point(n, c, neg[1], pos[0]);
+    V3 q3 = plane_edge_point(n, c, neg[1], pos[1]);
+    V3 ab = sub(neg[1], neg[0]);
+    V3 c0 = add(add(add(neg[0], neg[1]), q2), q3);
+    double v0 = fabs(dot(sub(neg[1], neg[0]), cross(sub(q2, neg[0]), sub(q3, neg[0]))));
+    V3 c1 = add(add(add(neg[0], q0), q1), q2);
+    double v1 = fabs(dot(sub(q0, neg[0]), cross(sub(q1, neg[0]), sub(q2, neg[0]))));
+    V3 c2 = add(add(add(neg[0], q1), q2), q3);
+    double v2 = fabs(dot(sub(q1, neg[0]), cross(sub(q2, neg[0]), sub(q3, neg[0]))));
+    centroid = scale(divv(add(add(scale(c0, v0), scale(c1, v1)), scale(c2, v2)), v0 + v1 + v2), 0.25);
+    V3 d = add(add(add(add(add(cross(sub(q0, neg[0]), sub(q1, neg[0])), cross(sub(q3, neg[1]), sub(q2, neg[1]))),
+                       cross(ab, sub(q2, neg[0]))), cross(sub(q2, neg[0]), sub(q0, neg[0]))),
+                   cross(sub(q3, neg[0]), ab)), cross(sub(q1, neg[0]), sub(q3, neg[0])));
+    dir = scale(unit(d), v0 + v1 + v2);
+    if (dot(sub(neg[1], neg[0]), cross(sub(pos[0], neg[0]), sub(pos[1], neg[0]))) < 0.0) dir = scale(dir, -1.0);
+  } else if (nn == 3) {
+    V3 q0 = plane_edge_point(n, c, neg[0], pos[0]);
+    V3 q1 = plane_edge_point(n, c, neg[1], pos[0]);
+    V3 q2 = plane_edge_point(n, c, neg[2], pos[0]);
+    V3 ab = sub(q0, pos[0]), ac = sub(q1, pos[0]), ad = sub(q2, pos[0]);
+    V3 cs = add(add(add(P[0], P[1]), P[2]), P[3]);
+    double sv = dot(sub(neg[0], pos[0]), cross(sub(neg[1], pos[0]), sub(neg[2], pos[0])));
+    double v = fabs(sv);
+    V3 c0 = add(add(add(pos[0], q0), q1), q2);
+    double v0 = fabs(dot(ab, cross(ac, ad)));
+    centroid = scale(divv(sub(scale(cs, v), scale(c0, v0)), v - v0), 0.25);
+    dir = scale(unit(add(add(cross(ab, ac), cross(ac, ad)), cross(ad, ab))), v - v0);
+    if (sv > 0.0) dir = scale(dir, -1.0);
+  } else {
+    centroid = scale(add(add(add(P[0], P[1]), P[2]), P[3]), 0.25);
+    double vol = fabs(dot(sub(P[1], P[0]), cross(sub(P[2], P[0]), sub(P[3], P[0]))));
+    dir = scale(n, vol);
+  }
+}
+
+// barycentric coordinates from sub-volumes (intersection.cpp:119-148); all
+// 0.25 when six times the volume is at most 1e-6
+void barycentric(const V3* P, V3 p, double w[4]) {
+  V3 ab = sub(P[1], P[0]), ac = sub(P[2], P[0]), ad = sub(P[3], P[0]);
+  V3 bc = sub(P[2], P[1]), bd = sub(P[3], P[1]);
+  V3 ap = sub(p, P[0]), bp = sub(p, P[1]);
+  double va = fabs(dot(bp, cross(bc, bd)));
+  double vb = fabs(dot(ap, cross(ac, ad)));
+  double vc = fabs(dot(ap, cross(ab, ad)));
+  double vd = fabs(dot(ap, cross(ab, ac)));
+  double vol = fabs(dot(ab, cross(ac, ad)));
+  if (vol <= 1e-6) { w[0] = w[1] = w[2] = w[3] = 0.25; return; }
+  double inv = 1.0 / vol;
+  w[0] = va * inv; w[1] = vb * inv; w[2] = vc * inv; w[3] = vd * inv;
+}
+
+// MeshPlaneCollisionDampingForcer::addDampingMatrix
+// (collision/penaltyDampingForcer.cpp:8-61) for element e: with w the
+// barycentric coordinates of the centroid, u = dir / |dir| and the velocity
+// there approaching the plane (v.u < 0), the 12x12 block (a, b) of the
+// element matrix receives w_a w_b T with T = (coeff dir) u^T; packed entries
+// (row-wise upper triangle).  In the reference the diagonal blocks take
+// T(i, j) for the entry (i, i + j) -- kept as it is.  Returns false when
+// nothing is added.
+bool plane_damping_element(const Scene& s, int e, const V3* vel, V3 n, double c, double coeff, double out[78]) {
+  static const int diag[12] = {0, 12, 23, 33, 42, 50, 57, 63, 68, 72, 75, 77};
+  const int* t = &s.tets[4 * e];
+  V3 P[4];
+  for (int i = 0; i < 4; i++) P[i] = add(s.X[t[i]], s.u[t[i]]);
+  V3 cen = {0.0, 0.0, 0.0}, dir = {0.0, 0.0, 0.0};   // (the reference's Vector3 starts at zero)
+  plane_tet(n, c, P, cen, dir);
+  double w[4];
+  barycentric(P, cen, w);
+  V3 u = {0.0, 0.0, 0.0};
+  if (len2(dir) != 0.0) u = unit(dir);
+  V3 v = {0.0, 0.0, 0.0};
+  for (int i = 0; i < 4; i++) v = add(v, scale(vel[t[i]], w[i]));
+  if (!(dot(v, u) < 0.0)) return false;
+  V3 cd = scale(dir, coeff);
+  double T[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) T[i][j] = at(cd, i) * at(u, j);
+  for (int k = 0; k < 78; k++) out[k] = 0.0;
+  for (int a = 0; a < 4; a++) {
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3 - i; j++) out[diag[3 * a + i] + j] = w[a] * w[a] * T[i][j];
+    for (int b = a + 1; b < 4; b++)
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) out[diag[3 * a + i] + (b - a) * 3 - i + j] = w[a] * w[b] * T[i][j];
+  }
+  return true;
+}
+
+// values += the forcer's contributions of elements elems (in that order)
+void plane_damping(const Scene& s, const V3* vel, V3 n, double c, double coeff, int count, const int* elems,
+                   double* values) {
+  double blk[78];
+  for (int k = 0; k < count; k++) {
+    const int e = elems[k];
+    if (!plane_damping_element(s, e, vel, n, c, coeff, blk)) continue;
+    for (int q = 0; q < 78; q++) {
+      const int idx = s.emap[78 * (size_t)e + q];
+      if (idx >= 0) values[idx] += blk[q];
+    }
+  }
+}
+
 void write_free(Scene& s, const double* d) {
   for (int nd = 0; nd < s.n_nodes; nd++)
     for (int ax = 0; ax < 3; ax++) {
@@ -1490,6 +1634,7 @@ struct odo_scene {
   double h = 0, alphaM = 0, betaK = 0, beta = 0.25, gamma = 0.5, tol = 1e-8;
   int maxit = 1000, pkind = 1, newton = 1;
   Precond ldlt;   // stand-alone incomplete LDL^T factor (odo_ldlt_*)
+  std::vector<double> D;   // external damping matrix values (empty: none)
 };
 
 odo_scene* odo_scene_create(int n_nodes, const double* X, int n_tets, const int* tets, int n_facets,
@@ -1601,6 +1746,35 @@ void odo_ldlt_get(odo_scene* o, double* values, int* rows, int* pcol, double* in
 
 void odo_ldlt_apply(odo_scene* o, const double* rhs, double* out) { ldlt_apply(o->s.dofs, o->ldlt, rhs, out); }
 
+// plane collision damping values (reference layout, from zero) for elements
+// elems against the plane normal.x + constant = 0, node velocities vel
+void odo_plane_damping(odo_scene* o, const double* vel, const double* normal, double constant, double coeff, int n,
+                       const int* elems, double* values) {
+  const Scene& s = o->s;
+  std::vector<V3> v(s.n_nodes);
+  for (int i = 0; i < s.n_nodes; i++) v[i] = {vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]};
+  memset(values, 0, sizeof(double) * s.nvals);
+  plane_damping(s, v.data(), {normal[0], normal[1], normal[2]}, constant, coeff, n, elems, values);
+}
+
+// the integrators' external damping matrix: cleared (clearExternalDampingForceMatrix),
+// or replaced by the plane forcer with the integrator's node velocities
+// (getMeshVerticesVelocities: constrained DOFs 0)
+void odo_clear_damping(odo_scene* o) { o->D.clear(); }
+void odo_integrator_plane_damping(odo_scene* o, const double* normal, double constant, double coeff, int n,
+                                  const int* elems) {
+  const Scene& s = o->s;
+  std::vector<V3> v(s.n_nodes, V3{0.0, 0.0, 0.0});
+  for (int nd = 0; nd < s.n_nodes; nd++)
+    for (int ax = 0; ax < 3; ax++) {
+      const int g = global_index(s.cd, nd, ax);
+      const double x = g >= 0 ? o->v[g] : 0.0;
+      if (ax == 0) v[nd].x = x; else if (ax == 1) v[nd].y = x; else v[nd].z = x;
+    }
+  o->D.assign(s.nvals, 0.0);
+  plane_damping(s, v.data(), {normal[0], normal[1], normal[2]}, constant, coeff, n, elems, o->D.data());
+}
+
 // Loads (Forcer, core/forcer.cpp:8-96): body force density times V/4 per
 // node (tetelement.cpp:68-77), tractions times the deformed facet area / 3
 // per vertex (tetelement.cpp:79-89); constrained DOFs dropped.
@@ -1660,6 +1834,8 @@ int odo_be_step(odo_scene* o, int nsteps) {
   for (int st = 0; st < nsteps; st++) {
     assemble(s, o->K.data(), fint.data());
     for (int i = 0; i < s.nvals; i++) o->K[i] = o->K[i] * (o->h + o->betaK) + o->alphaM * s.mass[i];
+    if (!o->D.empty())   // tagentMatrix->Add(1, *dampMatrix) (nonlinearImplicitBackwardEuler.h:88)
+      for (int i = 0; i < s.nvals; i++) o->K[i] += o->D[i];
     std::fill(rhs.begin(), rhs.end(), 0.0);
     spmdv(s, o->K.data(), o->v.data(), rhs.data());
     for (int i = 0; i < n; i++) rhs[i] = o->h * (o->fext[i] - fint[i] - rhs[i]);
@@ -1679,8 +1855,8 @@ int odo_be_step(odo_scene* o, int nsteps) {
 // Full-order Newmark (beta, gamma) with a Newton loop on the acceleration.
 // No reference counterpart at full order; the predictor/corrector formulas are
 // those of the reference's modal integrator (intergrator/linearNewmark.cpp:
-// 27-30, 57-79) applied to every DOF, with Rayleigh damping
-// C = alpha_M M + beta_K K(d):
+// 27-30, 57-79) applied to every DOF, with damping C = alpha_M M + beta_K K(d)
+// (+ the external damping matrix D when one is set, in r and in A as gamma h D):
 //   d~ = d + h v + (1/2 - beta) h^2 a;   v~ = v + (1 - gamma) h a
 //   a_0 = a; for k < newton:
 //     d_k = d~ + beta h^2 a_k;  v_k = v~ + gamma h a_k   (d_k written to the mesh)
@@ -1712,9 +1888,12 @@ int odo_nm_step(odo_scene* o, int nsteps) {
       spmdv(s, s.mass.data(), t1.data(), y.data());
       std::fill(t1.begin(), t1.end(), 0.0);
       spmdv(s, o->K.data(), t2.data(), t1.data());
+      if (!o->D.empty()) spmdv(s, o->D.data(), t2.data(), y.data());   // + D v_k
       for (int i = 0; i < n; i++) r[i] = o->fext[i] - fint[i] - (y[i] + o->betaK * t1[i]);
       const double cK = gh * o->betaK + bh2, cM = 1.0 + gh * o->alphaM;
       for (int i = 0; i < s.nvals; i++) o->K[i] = o->K[i] * cK + cM * s.mass[i];
+      if (!o->D.empty())
+        for (int i = 0; i < s.nvals; i++) o->K[i] += gh * o->D[i];
       std::fill(da.begin(), da.end(), 0.0);
       iters += pcg(s, o->K.data(), r.data(), da.data(), o->tol, o->maxit, o->pkind);
       for (int i = 0; i < n; i++) o->a[i] += da[i];

@@ -60,6 +60,7 @@
 #include "jacobiPreconditioner.h"
 #include "inCholeskyPreconditioner.h"
 #include "inLDLTPreconditioner.h"
+#include "penaltyDampingForcer.h"
 #include "intergrator.h"
 #include "nonlinearImplicitBackwardEuler.h"
 #undef private
@@ -370,6 +371,45 @@ void odref_ldlt_get(void* p, double* values, int* rows, int* pcol, double* inv_d
 void odref_ldlt_apply(void* p, const double* rhs, double* result) {
   RefScene* s = (RefScene*)p;
   s->ldlt->solvePreconditionerSystem(s->dofs, rhs, result);
+}
+
+// MeshPlaneCollisionDampingForcer (collision/penaltyDampingForcer.cpp:8-61):
+// the damping-matrix values (reference layout) the forcer adds for each
+// element of elems against the plane normal.x + constant = 0, with node
+// velocities vel (3 per node), at the scene's current displacements.
+void odref_plane_damping(void* p, const double* vel, const double* normal, double constant, double coeff, int n,
+                         const int* elems, double* values) {
+  RefScene* s = (RefScene*)p;
+  std::vector<Vector3> v(s->n_nodes);
+  for (int i = 0; i < s->n_nodes; i++) v[i] = Vector3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+  Collision::StaticPlaneShape plane;
+  plane.planeNormal = Vector3(normal[0], normal[1], normal[2]);
+  plane.planeConstant = constant;
+  Collision::MeshPlaneCollisionDampingForcer f(coeff, s->mesh, s->indexer, v.data());
+  s->pattern->setZeros();
+  for (int k = 0; k < n; k++) {
+    f.setCollisionPair(plane, elems[k]);
+    f.addDampingMatrix(s->indices, *s->pattern);
+  }
+  memcpy(values, s->pattern->values, sizeof(double) * s->pattern->getNumEntries());
+}
+
+// backward Euler: clearExternalDampingForceMatrix, then the plane forcer for
+// each element with the integrator's current node velocities
+// (getMeshVerticesVelocities) through addExternalDampingForceMatrix
+void odref_be_plane_damping(void* p, const double* normal, double constant, double coeff, int n, const int* elems) {
+  RefScene* s = (RefScene*)p;
+  s->be->clearExternalDampingForceMatrix();
+  std::vector<Vector3> v(s->n_nodes);
+  s->be->getMeshVerticesVelocities(s->indexer, s->mesh, v.data());
+  Collision::StaticPlaneShape plane;
+  plane.planeNormal = Vector3(normal[0], normal[1], normal[2]);
+  plane.planeConstant = constant;
+  Collision::MeshPlaneCollisionDampingForcer f(coeff, s->mesh, s->indexer, v.data());
+  for (int k = 0; k < n; k++) {
+    f.setCollisionPair(plane, elems[k]);
+    s->be->addExternalDampingForceMatrix(f);
+  }
 }
 
 // Loads: body force density (N/m^3) over all elements, then uniform

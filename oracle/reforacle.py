@@ -69,6 +69,8 @@ def lib():
         L.odref_ldlt_factor.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double]
         L.odref_ldlt_get.argtypes = [C.c_void_p, _dp, _ip, _ip, _dp]
         L.odref_ldlt_apply.argtypes = [C.c_void_p, _dp, _dp]
+        L.odref_plane_damping.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_double, C.c_int, _ip, _dp]
+        L.odref_be_plane_damping.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double, C.c_int, _ip]
         _lib = L
     return _lib
 
@@ -197,6 +199,23 @@ class RefScene:
         out = np.zeros(self.dofs)
         lib().odref_ldlt_apply(self.h, _d(rhs), _d(out))
         return out
+
+    def plane_damping(self, vel, normal, constant, coeff, elems):
+        """MeshPlaneCollisionDampingForcer values for elems against the plane
+        normal.x + constant = 0 with node velocities vel (n_nodes x 3)."""
+        vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1)
+        nrm = np.ascontiguousarray(normal, dtype=np.float64)
+        el = np.ascontiguousarray(elems, dtype=np.int32)
+        out = np.zeros(self.n_values)
+        lib().odref_plane_damping(self.h, _d(vel), _d(nrm), float(constant), float(coeff), el.size, _i(el), _d(out))
+        return out
+
+    def be_plane_damping(self, normal, constant, coeff, elems):
+        """Backward Euler: replace the damping matrix by the plane forcer's,
+        with the integrator's current node velocities."""
+        nrm = np.ascontiguousarray(normal, dtype=np.float64)
+        el = np.ascontiguousarray(elems, dtype=np.int32)
+        lib().odref_be_plane_damping(self.h, _d(nrm), float(constant), float(coeff), el.size, _i(el))
 
     def loads(self, body=None, tractions=()):
         """Rebuild the load set: body force density then (traction, facets) pairs."""

@@ -61,6 +61,9 @@ def lib():
         L.odo_ldlt_factor.argtypes = [C.c_void_p, _dp]
         L.odo_ldlt_get.argtypes = [C.c_void_p, _dp, _ip, _ip, _dp]
         L.odo_ldlt_apply.argtypes = [C.c_void_p, _dp, _dp]
+        L.odo_plane_damping.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_double, C.c_int, _ip, _dp]
+        L.odo_clear_damping.argtypes = [C.c_void_p]
+        L.odo_integrator_plane_damping.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double, C.c_int, _ip]
         _lib = L
     return _lib
 
@@ -189,6 +192,25 @@ class OracleScene:
         out = np.zeros(self.dofs)
         lib().odo_ldlt_apply(self.h, _d(rhs), _d(out))
         return out
+
+    def plane_damping(self, vel, normal, constant, coeff, elems):
+        """Plane collision damping values (reference layout) for elems."""
+        vel = np.ascontiguousarray(vel, dtype=np.float64).reshape(-1)
+        nrm = np.ascontiguousarray(normal, dtype=np.float64)
+        el = np.ascontiguousarray(elems, dtype=np.int32)
+        out = np.zeros(self.n_values)
+        lib().odo_plane_damping(self.h, _d(vel), _d(nrm), float(constant), float(coeff), el.size, _i(el), _d(out))
+        return out
+
+    def clear_damping(self):
+        lib().odo_clear_damping(self.h)
+
+    def integrator_plane_damping(self, normal, constant, coeff, elems):
+        """Replace the integrators' damping matrix by the plane forcer's, with
+        the integrator's current node velocities."""
+        nrm = np.ascontiguousarray(normal, dtype=np.float64)
+        el = np.ascontiguousarray(elems, dtype=np.int32)
+        lib().odo_integrator_plane_damping(self.h, _d(nrm), float(constant), float(coeff), el.size, _i(el))
 
     def loads(self, body=None, tractions=()):
         t = np.zeros((max(len(tractions), 1), 3))

@@ -25,9 +25,14 @@ the GPU path against them.  Cases:
 * ``ldlt_<material>_<constraints>``: InLDLTPreconditioner: the factor (L
   values, rows, pcol, inverted diagonal) of A = K/3600 + M at two drop-bound
   pairs, its apply on a seeded vector, CG with it, and backward-Euler steps
-  preconditioned by it.
+  preconditioned by it;
+* ``damping``: MeshPlaneCollisionDampingForcer: damping values against two
+  planes (a tilted one cutting elements with 0-3 vertices below it, a
+  horizontal one with whole elements below it), with a repeated element,
+  and backward-Euler steps with the forcer re-applied every step.
 
-``--only NAME`` writes one group (plastic or ldlt; the full run writes all).
+``--only NAME`` writes one group (plastic, ldlt or damping; the full run
+writes all).
 """
 from __future__ import annotations
 
@@ -133,8 +138,48 @@ def ldlt_cases():
                  be_params=np.array([1.0 / 60.0, 0.01, 0.001, 1e-10]), **out)
 
 
+DAMP_PLANES = ((0.1, 0.2, 1.0, -0.05), (0.0, 0.0, 1.0, -0.07))   # normal (normalised), constant
+DAMP_COEFF = 50.0
+DAMP_BE = (2000.0, 15)          # coefficient, steps (plane z = 0, all elements, 20 g)
+
+
+def damping_case():
+    g = small_mesh()
+    cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+    rho, E, nu, thr = MATS["corotational"]
+    s = R.RefScene(g.X, g.tets, g.facets, cd, "corotational", rho, E, nu, thr)
+    rng = np.random.default_rng(77)
+    u = rng.normal(scale=0.004, size=(g.n_nodes, 3))
+    vel = rng.normal(size=(g.n_nodes, 3))
+    s.set_displacements(u)
+    elems = np.concatenate([np.arange(g.n_tets), [3, 3, 17]]).astype(np.int32)
+    planes = []
+    out = {}
+    for k, (a, b, c, const) in enumerate(DAMP_PLANES):
+        nrm = np.array([a, b, c]) / np.linalg.norm([a, b, c])
+        planes.append(list(nrm) + [const])
+        out[f"values_{k}"] = s.plane_damping(vel, nrm, const, DAMP_COEFF, elems)
+    s = R.RefScene(g.X, g.tets, g.facets, cd, "corotational", rho, E, nu, thr)
+    s.be_setup(1.0 / 60.0, 0.01, 0.001, tol=1e-10, maxit=2000, precond="jacobi")
+    fext = s.loads(body=[0.0, 0.0, -9800.0 * 20])
+    s.be_apply_loads()
+    coeff, steps = DAMP_BE
+    iters = 0
+    for _ in range(steps):
+        s.be_plane_damping([0.0, 0.0, 1.0], 0.0, coeff, np.arange(g.n_tets))
+        iters += s.be_step(1)
+    save("damping", X=g.X, tets=g.tets, facets=g.facets, cdofs=cd, u=u, vel=vel, elems=elems,
+         planes=np.array(planes), coeff=DAMP_COEFF, material=np.array([rho, E, nu, thr]), be_fext=fext,
+         be_u=s.displacements(), be_v=s.be_velocity(), be_steps=steps, be_iters=iters, be_coeff=coeff,
+         be_params=np.array([1.0 / 60.0, 0.01, 0.001, 1e-10]), **out)
+
+
 def main():
     only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    if only == "damping":
+        damping_case()
+        print("golden fixture damping written to", OUT)
+        return
     if only == "plastic":
         plastic_case()
         print("golden fixture plastic written to", OUT)
@@ -144,7 +189,7 @@ def main():
         print("golden fixtures ldlt_* written to", OUT)
         return
     if only is not None:
-        raise SystemExit(f"--only {only}: single groups are 'plastic' and 'ldlt'")
+        raise SystemExit(f"--only {only}: single groups are 'plastic', 'ldlt' and 'damping'")
     g = small_mesh()
     cases = {"full": meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0)),
              "partial": partial_constraints(g)}
@@ -221,6 +266,7 @@ def main():
          eig_vecs=evec)
     plastic_case()
     ldlt_cases()
+    damping_case()
     print("golden fixtures written to", OUT)
 
 
