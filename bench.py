@@ -22,8 +22,9 @@ PCG (steps/s of both, the displacement error between them, and the HBM
 roofline of the FP32 SpMV phase measured inside the solve), and
 "batched_tier", 512 uneven scenes stepped one by one with the FP64 solver and
 together through od_batch with the mixed solver; "serving_tier", Poisson step
-requests over a pool of scenes; "ldlt_tier", the headline step preconditioned
-by the reference's incomplete LDL^T, beside the reference's CPU code for it.
+requests over a pool of scenes; "sweep_tier", the headline step preconditioned
+by the reference's incomplete LDL^T and by its threshold incomplete Cholesky,
+beside the reference's CPU code for each.
 """
 from __future__ import annotations
 
@@ -308,10 +309,11 @@ def precision_tier(args, api, ctx):
                                             "block row (own p read, q written)"}}
 
 
-def ldlt_tier(args, api, ctx):
+def sweep_tier(args, api, ctx):
     """The headline beam workload (98,304 tets, Newmark, 3 Newton iterations,
-    tolerance 1e-8) preconditioned by the reference's incomplete LDL^T
-    (InLDLTPreconditioner(0.1, 0.01)): the factor is remade on the host for
+    tolerance 1e-8) preconditioned by the reference's two factored
+    preconditioners, InLDLTPreconditioner(0.1, 0.01) and
+    InCholeskyPreconditioner(0.01, 0): each factor is remade on the host for
     every solve as the reference does (bit-identical to it), the two
     triangular sweeps of every apply run on the device.  Wall time per step
     (the host factorisations are inside it), the apply's device time from a
@@ -320,73 +322,77 @@ def ldlt_tier(args, api, ctx):
     g = wl["mesh"]()
     cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
     kind, rho, E, nu, thr = wl["material"]
-    se, le = 0.1, 0.01
-    s = api.Scene(ctx, g.X, g.tets, g.facets, cd, api.Material(kind, rho, E, nu, thr))
-    s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, wl["alpha_m"], wl["beta_k"], wl["dt"],
-                                             api.CGSolver(wl["tol"], 5000, api.InLDLTPreconditioner(se, le)),
-                                             wl["newton"]))
-    s.set_loads(body=wl["body"], tractions=traction_groups(g, wl["traction"]))
-    s.set_traction_schedule(wl["freq"])
-    s.step(1)
-    steps = max(2, min(args.tier_steps, 4))
-    ctx.reset_counters()
-    walls, it, solves = [], 0, 0
-    for _ in range(steps):
-        t0 = time.perf_counter()
-        st = s.step(1)
-        walls.append(time.perf_counter() - t0)
-        if st.status != 0:
-            raise RuntimeError(f"ldlt tier: step status {st.status}")
-        it += st.pcg_iterations
-        solves += st.solves
-    c = ctx.counters()
-    factor_ms = c.ldlt_factor_ms / max(1, c.ldlt_factors)
-    ctx.reset_counters()
-    ctx.set_profiling(True)
-    s.step(1)
-    ctx.set_profiling(False)
-    p = ctx.counters()
-    s.close()
-    apply_ms = p.ldlt_apply_ms / max(1, p.ldlt_applies)
     peak, peak_kind = peaks()
-    gbs = p.ldlt_apply_bytes / (p.ldlt_apply_ms * 1e-3) / 1e9 if p.ldlt_apply_ms else None
-    out = {"workload": "beam98k_nh_newmark_ldlt", "n_tets": g.n_tets, "precond": f"InLDLTPreconditioner({se}, {le})",
-           "steps": steps, "wall_ms_per_step": 1000 * statistics.mean(walls),
-           "steps_per_s": 1.0 / statistics.mean(walls), "pcg_iterations_per_step": it / steps,
-           "solves_per_step": solves / steps, "factor_ms_per_solve": factor_ms, "factor_nnz": c.ldlt_nnz,
-           "apply": {"kernel": "ldlt_apply_kernel (forward and backward sweeps, one cooperative launch)",
-                     "bound": "latency: dependency chain", "levels": p.ldlt_levels, "avg_launch_ms": apply_ms,
-                     "us_per_level": 1000.0 * apply_ms / max(1, p.ldlt_levels), "launches": p.ldlt_applies,
-                     "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak if gbs else None,
-                     "peak_source": peak_kind,
-                     "bytes_rule": "L entries x 12 B (value + index) per sweep + 6 x 8 B per row"},
-           "share_of_step": {"host_factor": factor_ms * solves / steps / (1000 * statistics.mean(walls))}}
-    if not args.no_cpu_baseline:
-        try:
-            from oracle import build_ref, reforacle
-            if not reforacle.available():
-                build_ref.build()
-            r = reforacle.RefScene(g.X, g.tets, g.facets, cd, kind, rho, E, nu, thr)
-            r.nm_setup(wl["dt"], wl["alpha_m"], wl["beta_k"], newton=wl["newton"], tol=wl["tol"], maxit=5000,
-                       precond="ldlt", eps=se, relax=le)
-            t, n_ref, used = 0.0, 0, 0.0
-            while n_ref < 2:
-                t += wl["dt"]
-                scale = math.sin(2 * math.pi * wl["freq"] * t)
-                t0 = time.perf_counter()
-                r.loads(body=wl["body"], tractions=[(np.array(tr) * scale, fac) for tr, fac in
-                                                    traction_groups(g, wl["traction"])])
-                r.nm_apply_loads()
-                r.nm_step(1)
-                used += time.perf_counter() - t0
-                n_ref += 1
-            out["cpu_reference"] = {"steps_per_s": n_ref / used, "cores": 1, "kind": "reference",
-                                    "sample": f"{n_ref} Newmark steps, reference code with its "
-                                              "InLDLTPreconditioner, single thread"}
-            out["speedup_vs_cpu_reference"] = out["steps_per_s"] / out["cpu_reference"]["steps_per_s"]
-        except Exception as exc:
-            out["cpu_reference"] = {"error": str(exc)}
-    return out
+    result = {"workload": "beam98k_nh_newmark", "n_tets": g.n_tets}
+    for name, prec, ref_args in (("ldlt", api.InLDLTPreconditioner(0.1, 0.01), ("ldlt", 0.1, 0.01)),
+                                 ("ic", api.InCholeskyPreconditioner(0.01, 0.0), ("ic", 0.01, 0.0))):
+        s = api.Scene(ctx, g.X, g.tets, g.facets, cd, api.Material(kind, rho, E, nu, thr))
+        s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, wl["alpha_m"], wl["beta_k"], wl["dt"],
+                                                 api.CGSolver(wl["tol"], 5000, prec), wl["newton"]))
+        s.set_loads(body=wl["body"], tractions=traction_groups(g, wl["traction"]))
+        s.set_traction_schedule(wl["freq"])
+        s.step(1)
+        steps = max(2, min(args.tier_steps, 4))
+        ctx.reset_counters()
+        walls, it, solves = [], 0, 0
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            st = s.step(1)
+            walls.append(time.perf_counter() - t0)
+            if st.status != 0:
+                raise RuntimeError(f"sweep tier ({name}): step status {st.status}")
+            it += st.pcg_iterations
+            solves += st.solves
+        c = ctx.counters()
+        factor_ms = c.sweep_factor_ms / max(1, c.sweep_factors)
+        ctx.reset_counters()
+        ctx.set_profiling(True)
+        s.step(1)
+        ctx.set_profiling(False)
+        p = ctx.counters()
+        s.close()
+        apply_ms = p.sweep_apply_ms / max(1, p.sweep_applies)
+        gbs = p.sweep_apply_bytes / (p.sweep_apply_ms * 1e-3) / 1e9 if p.sweep_apply_ms else None
+        wall = statistics.mean(walls)
+        label = {"ldlt": "InLDLTPreconditioner", "ic": "InCholeskyPreconditioner"}[name]
+        out = {"precond": f"{label}({ref_args[1]}, {ref_args[2]})", "steps": steps, "wall_ms_per_step": 1000 * wall, "steps_per_s": 1.0 / wall,
+               "pcg_iterations_per_step": it / steps, "solves_per_step": solves / steps,
+               "factor_ms_per_solve": factor_ms, "factor_nnz": c.sweep_nnz,
+               "apply": {"kernel": f"sweep_apply_kernel<{1 if name == 'ic' else 0}> (forward and backward sweeps, "
+                                   "one cooperative launch)",
+                         "bound": "latency: dependency chain", "levels": p.sweep_levels, "avg_launch_ms": apply_ms,
+                         "us_per_level": 1000.0 * apply_ms / max(1, p.sweep_levels), "launches": p.sweep_applies,
+                         "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak if gbs else None,
+                         "peak_source": peak_kind,
+                         "bytes_rule": "L entries x 12 B (value + index) per sweep + 7 x 8 B per row"},
+               "share_of_step": {"host_factor": factor_ms * solves / steps / (1000 * wall)}}
+        if not args.no_cpu_baseline:
+            try:
+                from oracle import build_ref, reforacle
+                if not reforacle.available():
+                    build_ref.build()
+                r = reforacle.RefScene(g.X, g.tets, g.facets, cd, kind, rho, E, nu, thr)
+                r.nm_setup(wl["dt"], wl["alpha_m"], wl["beta_k"], newton=wl["newton"], tol=wl["tol"], maxit=5000,
+                           precond=ref_args[0], eps=ref_args[1], relax=ref_args[2])
+                t, n_ref, used = 0.0, 0, 0.0
+                while n_ref < 2:
+                    t += wl["dt"]
+                    scale = math.sin(2 * math.pi * wl["freq"] * t)
+                    t0 = time.perf_counter()
+                    r.loads(body=wl["body"], tractions=[(np.array(tr) * scale, fac) for tr, fac in
+                                                        traction_groups(g, wl["traction"])])
+                    r.nm_apply_loads()
+                    r.nm_step(1)
+                    used += time.perf_counter() - t0
+                    n_ref += 1
+                out["cpu_reference"] = {"steps_per_s": n_ref / used, "cores": 1, "kind": "reference",
+                                        "sample": f"{n_ref} Newmark steps, reference code with the same "
+                                                  "preconditioner, single thread"}
+                out["speedup_vs_cpu_reference"] = out["steps_per_s"] / out["cpu_reference"]["steps_per_s"]
+            except Exception as exc:
+                out["cpu_reference"] = {"error": str(exc)}
+        result[name] = out
+    return result
 
 
 def batched_tier(args, api, ctx):
@@ -679,7 +685,7 @@ def run_gpu(args, wl):
         del scene
         only = [t for t in args.only_tiers.split(",") if t]
         for name, fn in (("precision_tier", precision_tier), ("batched_tier", batched_tier),
-                         ("serving_tier", serving_tier), ("ldlt_tier", ldlt_tier)):
+                         ("serving_tier", serving_tier), ("sweep_tier", sweep_tier)):
             if only and name.split("_")[0] not in only:
                 continue
             try:
@@ -721,7 +727,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tiers", action="store_true", help="skip the mixed-precision and batched workloads")
     ap.add_argument("--tier-steps", type=int, default=5)
-    ap.add_argument("--only-tiers", default="", help="comma list of precision,batched,serving,ldlt (default: all)")
+    ap.add_argument("--only-tiers", default="", help="comma list of precision,batched,serving,sweep (default: all)")
     ap.add_argument("--precision-nz", type=int, default=64,
                     help="cube layers of the precision-tier block (64: 2,621,440 tets)")
     ap.add_argument("--serving-pool", type=int, default=512)

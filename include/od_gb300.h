@@ -14,6 +14,7 @@
  *   LinearSolver / CGSolver                core/linearSolver.h:12-20, solver/cgSolver.h:16-17
  *   Preconditioner (+ Jacobi, IC)          core/preconditioner.h:12-22
  *   InLDLTPreconditioner                   solver/inLDLTPreconditioner.h:12-44
+ *   InCholeskyPreconditioner               solver/inCholeskyPreconditioner.h
  *   Forcer                                 core/forcer.h:13-22
  *   MeshPlaneCollisionDampingForcer        collision/penaltyDampingForcer.h:25-35
  *   Intergrator / NonlinearImplicitBackwardEuler
@@ -58,9 +59,12 @@ typedef enum od_precond_kind {
   OD_PRECOND_BLOCK_JACOBI = 2, /* 3x3 diagonal blocks (no reference counterpart) */
   OD_PRECOND_IC0 = 3,          /* shifted IC(0), level-scheduled (no reference counterpart;
                                   the reference's fill-in IC is inCholeskyPreconditioner.cpp) */
-  OD_PRECOND_LDLT = 4          /* incomplete LDL^T, solver/inLDLTPreconditioner.cpp:34-184:
+  OD_PRECOND_LDLT = 4,         /* incomplete LDL^T, solver/inLDLTPreconditioner.cpp:34-184:
                                   factor on the host (bit-identical to the reference's),
                                   triangular sweeps on the device */
+  OD_PRECOND_IC = 5            /* threshold incomplete Cholesky with fill,
+                                  solver/inCholeskyPreconditioner.cpp:18-162: factor on the host
+                                  (bit-identical to the reference's), sweeps on the device */
 } od_precond_kind;
 
 typedef enum od_precision {
@@ -99,6 +103,8 @@ typedef struct od_solver_params {
   double sainv_eps;   /* LDL^T: sainvEpsilon, drop bound of the inverse factor's
                          entries (0 = 0.1; InLDLTPreconditioner(sainvEpsilon, ldltEpsilon)) */
   double ldlt_eps;    /* LDL^T: ldltEpsilon, drop bound of L's entries (0 = 0.01) */
+  double ic_eps;      /* IC: epsilon of InCholeskyPreconditioner(epsilon, relaxedScale) (0 = 1e-3) */
+  double ic_relax;    /* IC: relaxedScale, taken as given (0: dropped entries are not compensated) */
 } od_solver_params;
 
 typedef struct od_solve_stats {
@@ -147,14 +153,15 @@ typedef struct od_counters {
                                  SpMV work (without the grid-wide sum that follows) */
   long long mix_fallbacks;    /* mixed solves whose refinement stalled and that the FP64 PCG
                                  finished (counted whether profiling is on or not) */
-  long long ldlt_factors;     /* incomplete LDL^T factorisations (always counted) */
-  double ldlt_factor_ms;      /* their host time: rebuild of A in the reference layout, the
+  /* preconditioners applied by triangular sweeps (LDL^T, IC): */
+  long long sweep_factors;    /* host factorisations (always counted) */
+  double sweep_factor_ms;     /* their host time: rebuild of A in the reference layout, the
                                  factorisation and the upload of the sweep arrays */
-  long long ldlt_nnz;         /* stored L entries of the last factor */
-  long long ldlt_applies;     /* LDL^T applies timed while profiling is on */
-  double ldlt_apply_ms;       /* their summed CUDA-event durations */
-  double ldlt_apply_bytes;    /* their algorithmic bytes: 2 x (nnz x 12 B) + 6 x 8 B per row */
-  long long ldlt_levels;      /* dependency levels of the last factor's two sweeps (the apply's
+  long long sweep_nnz;        /* strictly lower entries of the last factor */
+  long long sweep_applies;    /* applies timed while profiling is on */
+  double sweep_apply_ms;      /* their summed CUDA-event durations */
+  double sweep_apply_bytes;   /* their algorithmic bytes: 2 x (nnz x 12 B) + 7 x 8 B per row */
+  long long sweep_levels;     /* dependency levels of the last factor's two sweeps (the apply's
                                  critical path, in rows) */
 } od_counters;
 
@@ -245,6 +252,17 @@ od_status od_scene_ldlt_factor(od_scene* scene, const double* values, double sai
                                long long* nnz);
 od_status od_scene_ldlt_get(od_scene* scene, double* values, int* rows, int* pcol, double* inv_diag);
 od_status od_scene_ldlt_apply(od_scene* scene, const double* rhs, double* result);
+/* InCholeskyPreconditioner (solver/inCholeskyPreconditioner.cpp) the same
+ * way: od_scene_ic_factor is Preprocess (:76-130) with
+ * InCholeskyPreconditioner(eps, relax) (both >= 0; dofs >= 2); *nnz receives
+ * the stored entries, diagonals included.  od_scene_ic_get copies the factor
+ * out in the reference's storage: values[nnz], rows[nnz] (column c holds its
+ * diagonal, then its rows below ascending), pcol[dofs + 1].
+ * od_scene_ic_apply is solvePreconditionerSystem (:132-162) on the device:
+ * result = (L L^T)^-1 rhs. */
+od_status od_scene_ic_factor(od_scene* scene, const double* values, double eps, double relax, long long* nnz);
+od_status od_scene_ic_get(od_scene* scene, double* values, int* rows, int* pcol);
+od_status od_scene_ic_apply(od_scene* scene, const double* rhs, double* result);
 
 /* Collision damping (collision/penaltyDampingForcer.cpp:8-61,
  * intergrator/nonlinearImplicitBackwardEuler.h:122-128).

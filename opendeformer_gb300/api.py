@@ -10,7 +10,8 @@ reference reads the same:
   material/invertibleStVK.h);
 * preconditioners / solver: ``JacobiPreconditioner()``,
   ``BlockJacobiPreconditioner()``, ``IC0Preconditioner()``,
-  ``InLDLTPreconditioner(sainvEpsilon, ldltEpsilon)`` and
+  ``InLDLTPreconditioner(sainvEpsilon, ldltEpsilon)``,
+  ``InCholeskyPreconditioner(epsilon, relaxedScale)`` and
   ``CGSolver(tol, maxIter, preconditioner)`` (solver/cgSolver.h:16-17);
 * integrators: ``NonlinearImplicitBackwardEuler(massDamp, stiffDamp, ts,
   solver)`` (intergrator/nonlinearImplicitBackwardEuler.h:48-73) and
@@ -41,7 +42,7 @@ STATUS = {0: "OD_OK", 1: "OD_ERR_INVALID_ARG", 2: "OD_ERR_OUT_OF_MEMORY", 3: "OD
           8: "OD_ERR_INTERNAL"}
 
 MATERIAL_KIND = {"corotational": 0, "neohookean": 1, "stvk": 2, "corotational_plastic": 3}
-PRECOND_KIND = {"none": 0, "jacobi": 1, "block_jacobi": 2, "ic0": 3, "ldlt": 4}
+PRECOND_KIND = {"none": 0, "jacobi": 1, "block_jacobi": 2, "ic0": 3, "ldlt": 4, "ic": 5}
 PRECISION = {"fp64": 0, "mixed": 1}
 
 
@@ -60,7 +61,8 @@ class od_material(C.Structure):
 class od_solver_params(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("precond", C.c_int), ("precision", C.c_int),
                 ("replace_every", C.c_int), ("inner_tol", C.c_double), ("max_refine", C.c_int),
-                ("sainv_eps", C.c_double), ("ldlt_eps", C.c_double)]
+                ("sainv_eps", C.c_double), ("ldlt_eps", C.c_double), ("ic_eps", C.c_double),
+                ("ic_relax", C.c_double)]
 
 
 class od_solve_stats(C.Structure):
@@ -85,9 +87,9 @@ class od_counters(C.Structure):
                 ("pcg_launches", C.c_longlong), ("pcg_iterations", C.c_longlong), ("pcg_ms", C.c_double),
                 ("mix_iterations", C.c_longlong), ("mix_spmv_ms", C.c_double), ("mix_spmv_bytes", C.c_double),
                 ("mix_spmv_work_ms", C.c_double), ("mix_fallbacks", C.c_longlong),
-                ("ldlt_factors", C.c_longlong), ("ldlt_factor_ms", C.c_double), ("ldlt_nnz", C.c_longlong),
-                ("ldlt_applies", C.c_longlong), ("ldlt_apply_ms", C.c_double), ("ldlt_apply_bytes", C.c_double),
-                ("ldlt_levels", C.c_longlong)]
+                ("sweep_factors", C.c_longlong), ("sweep_factor_ms", C.c_double), ("sweep_nnz", C.c_longlong),
+                ("sweep_applies", C.c_longlong), ("sweep_apply_ms", C.c_double), ("sweep_apply_bytes", C.c_double),
+                ("sweep_levels", C.c_longlong)]
 
 
 class od_scene_info(C.Structure):
@@ -157,6 +159,9 @@ SIGNATURES = {
     "od_scene_ldlt_factor": (C.c_int, [_vp, _dp, C.c_double, C.c_double, C.POINTER(C.c_longlong)]),
     "od_scene_ldlt_get": (C.c_int, [_vp, _dp, _ip, _ip, _dp]),
     "od_scene_ldlt_apply": (C.c_int, [_vp, _dp, _dp]),
+    "od_scene_ic_factor": (C.c_int, [_vp, _dp, C.c_double, C.c_double, C.POINTER(C.c_longlong)]),
+    "od_scene_ic_get": (C.c_int, [_vp, _dp, _ip, _ip]),
+    "od_scene_ic_apply": (C.c_int, [_vp, _dp, _dp]),
     "od_scene_add_plane_damping": (C.c_int, [_vp, _dp, C.c_double, C.c_double, C.c_int, _ip, _dp]),
     "od_scene_clear_damping": (C.c_int, [_vp]),
     "od_scene_get_damping": (C.c_int, [_vp, _dp]),
@@ -254,6 +259,8 @@ class Preconditioner:
     kind: str = "none"
     sainvEpsilon: float = 0.0   # LDL^T drop bounds (0: 0.1 and 0.01)
     ldltEpsilon: float = 0.0
+    epsilon: float = 0.0        # IC: (epsilon, relaxedScale); epsilon 0: 1e-3
+    relaxedScale: float = 0.0
 
 
 def JacobiPreconditioner():
@@ -273,6 +280,12 @@ def InLDLTPreconditioner(sainvEpsilon=0.1, ldltEpsilon=0.01):
     return Preconditioner("ldlt", float(sainvEpsilon), float(ldltEpsilon))
 
 
+def InCholeskyPreconditioner(epsilon=1e-3, relaxedScale=0.0):
+    """InCholeskyPreconditioner(epsilon, relaxedScale) (solver/inCholeskyPreconditioner.h):
+    threshold incomplete Cholesky with fill."""
+    return Preconditioner("ic", epsilon=float(epsilon), relaxedScale=float(relaxedScale))
+
+
 @dataclasses.dataclass
 class CGSolver:
     tol: float = 1e-8
@@ -287,7 +300,8 @@ class CGSolver:
         return od_solver_params(self.tol, self.maxIter, PRECOND_KIND[self.preconditioner.kind],
                                 PRECISION[self.precision], self.replace_every, self.inner_tol,
                                 self.max_refine, self.preconditioner.sainvEpsilon,
-                                self.preconditioner.ldltEpsilon)
+                                self.preconditioner.ldltEpsilon, self.preconditioner.epsilon,
+                                self.preconditioner.relaxedScale)
 
 
 @dataclasses.dataclass
@@ -486,6 +500,28 @@ class Scene:
         dinv = np.zeros(max(self.dofs, 1))
         _check(L.od_scene_ldlt_get(self.h, _d(lv), _i(lr), _i(pc), _d(dinv)), "ldlt_get")
         return lv[:n], lr[:n], pc[: self.dofs], dinv[: self.dofs]
+
+    def ic_factor(self, values, eps=1e-3, relax=0.0):
+        """InCholeskyPreconditioner::Preprocess on A = values (reference
+        layout); returns (L values, L rows, pcol (dofs + 1)) in the
+        reference's storage.  The factor stays with the scene for ic_apply."""
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        nnz = C.c_longlong(0)
+        L = load_library()
+        _check(L.od_scene_ic_factor(self.h, _d(values), float(eps), float(relax), C.byref(nnz)), "ic_factor")
+        n = nnz.value
+        lv = np.zeros(max(n, 1))
+        lr = np.zeros(max(n, 1), np.int32)
+        pc = np.zeros(self.dofs + 1, np.int32)
+        _check(L.od_scene_ic_get(self.h, _d(lv), _i(lr), _i(pc)), "ic_get")
+        return lv[:n], lr[:n], pc
+
+    def ic_apply(self, rhs):
+        """(L L^T)^-1 rhs on the device with the last ic_factor."""
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64)
+        out = np.zeros(self.dofs)
+        _check(load_library().od_scene_ic_apply(self.h, _d(rhs), _d(out)), "ic_apply")
+        return out
 
     def ldlt_apply(self, rhs):
         """(L D L^T)^-1 rhs on the device with the last ldlt_factor."""

@@ -191,13 +191,13 @@ od_status od_ctx_get_counters(od_ctx* ctx, od_counters* out) {
   out->mix_spmv_work_ms = ctx->c.mix_spmv_work_ms;
   out->mix_fallbacks = ctx->c.mix_fallbacks;
   out->mix_spmv_bytes = ctx->c.mix_spmv_bytes;
-  out->ldlt_factors = ctx->c.ldlt_factors;
-  out->ldlt_factor_ms = ctx->c.ldlt_factor_ms;
-  out->ldlt_nnz = ctx->c.ldlt_nnz;
-  out->ldlt_applies = ctx->c.ldlt_applies;
-  out->ldlt_apply_ms = ctx->c.ldlt_apply_ms;
-  out->ldlt_apply_bytes = ctx->c.ldlt_apply_bytes;
-  out->ldlt_levels = ctx->c.ldlt_levels;
+  out->sweep_factors = ctx->c.sweep_factors;
+  out->sweep_factor_ms = ctx->c.sweep_factor_ms;
+  out->sweep_nnz = ctx->c.sweep_nnz;
+  out->sweep_applies = ctx->c.sweep_applies;
+  out->sweep_apply_ms = ctx->c.sweep_apply_ms;
+  out->sweep_apply_bytes = ctx->c.sweep_apply_bytes;
+  out->sweep_levels = ctx->c.sweep_levels;
   return OD_OK;
 }
 
@@ -208,8 +208,8 @@ od_status od_ctx_reset_counters(od_ctx* ctx) {
   ctx->c.spmv_ms = ctx->c.pcg_kernel_ms = 0.0;
   ctx->c.mix_iters = ctx->c.mix_fallbacks = 0;
   ctx->c.mix_spmv_ms = ctx->c.mix_spmv_bytes = ctx->c.mix_spmv_work_ms = 0.0;
-  ctx->c.ldlt_factors = ctx->c.ldlt_nnz = ctx->c.ldlt_applies = ctx->c.ldlt_levels = 0;
-  ctx->c.ldlt_factor_ms = ctx->c.ldlt_apply_ms = ctx->c.ldlt_apply_bytes = 0.0;
+  ctx->c.sweep_factors = ctx->c.sweep_nnz = ctx->c.sweep_applies = ctx->c.sweep_levels = 0;
+  ctx->c.sweep_factor_ms = ctx->c.sweep_apply_ms = ctx->c.sweep_apply_bytes = 0.0;
   return OD_OK;
 }
 
@@ -504,13 +504,15 @@ od_status od_scene_spmdv(od_scene* scene, const double* values, const double* x,
 static od_status check_solver(const od_solver_params* p) {
   OD_CHECK_ARG(p, "solver params are NULL");
   OD_CHECK_ARG(p->tol >= 0.0 && p->max_iter >= 0, "solver tolerance / max_iter out of range");
-  OD_CHECK_ARG(p->precond >= 0 && p->precond <= OD_PRECOND_LDLT, "unknown preconditioner");
+  OD_CHECK_ARG(p->precond >= 0 && p->precond <= OD_PRECOND_IC, "unknown preconditioner");
   OD_CHECK_ARG(p->precision == OD_PRECISION_FP64 || p->precision == OD_PRECISION_MIXED, "unknown precision");
   OD_CHECK_ARG(p->precision == OD_PRECISION_FP64 || p->precond < OD_PRECOND_IC0,
                "mixed precision supports the none, Jacobi and block-Jacobi preconditioners");
   OD_CHECK_ARG(p->sainv_eps >= 0.0 && p->ldlt_eps >= 0.0 && std::isfinite(p->sainv_eps) &&
                    std::isfinite(p->ldlt_eps),
                "LDL^T drop bounds must be finite and >= 0");
+  OD_CHECK_ARG(p->ic_eps >= 0.0 && p->ic_relax >= 0.0 && std::isfinite(p->ic_eps) && std::isfinite(p->ic_relax),
+               "incomplete Cholesky epsilon / relaxedScale must be finite and >= 0");
   return OD_OK;
 }
 

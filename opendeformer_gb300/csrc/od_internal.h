@@ -54,7 +54,7 @@ struct SolveScalars {           // device-resident PCG scalars
 
 struct SliceSys;
 struct MixedSys;
-struct LdltSys;
+struct SweepSys;
 struct Scene;
 
 struct Pcg {
@@ -98,8 +98,9 @@ struct Pcg {
   // solve (both built on first use)
   SliceSys* slice = nullptr;
   MixedSys* mix = nullptr;
-  // incomplete LDL^T (factor on the host, sweeps on the device)
-  LdltSys* ldlt = nullptr;
+  // incomplete LDL^T / threshold incomplete Cholesky (factor on the host,
+  // triangular sweeps on the device)
+  SweepSys* sweep = nullptr;
 };
 
 constexpr int kSliceRows = 10;      // block rows per slice (3 lanes each, 30 of a warp's 32)
@@ -241,8 +242,8 @@ struct Ctx {
   double pcg_kernel_ms = 0.0;
   long long mix_iters = 0;            // inner FP32 loop iterations (profiling)
   long long mix_fallbacks = 0;        // mixed solves finished by the FP64 solver
-  long long ldlt_factors = 0, ldlt_nnz = 0, ldlt_applies = 0, ldlt_levels = 0;
-  double ldlt_factor_ms = 0.0, ldlt_apply_ms = 0.0, ldlt_apply_bytes = 0.0;
+  long long sweep_factors = 0, sweep_nnz = 0, sweep_applies = 0, sweep_levels = 0;
+  double sweep_factor_ms = 0.0, sweep_apply_ms = 0.0, sweep_apply_bytes = 0.0;
   double mix_spmv_ms = 0.0;
   double mix_spmv_work_ms = 0.0;
   double mix_spmv_bytes = 0.0;
@@ -379,6 +380,21 @@ struct RifFactor {
 };
 void rif_columns(int n, int nbc, const std::vector<int>& pcol, const std::vector<int>& rows, RifColumns& out);
 void rif_factor(const RifColumns& A, const double* values, double sainv_eps, double ldlt_eps, RifFactor& F);
+// threshold incomplete Cholesky (od_ric.cpp): value positions of every
+// stored lower column in getColumn order, and the factor in the reference's
+// storage (column c = its diagonal then its rows below ascending; pcol n + 1)
+struct RicColumns {
+  int n = 0;
+  std::vector<int> ptr, row, src;
+};
+struct RicFactor {
+  int n = 0;
+  std::vector<double> val;
+  std::vector<int> row, pcol;
+};
+void ric_columns(int n, int nbc, const std::vector<int>& pcol, const std::vector<int>& rows,
+                 const std::vector<int>& oris, RicColumns& out);
+void ric_factor(const RicColumns& A, const double* values, double eps, double relax, RicFactor& F);
 
 // ---- kernels (od_elements.cu) ----
 od_status launch_precompute(Scene* s);
@@ -426,18 +442,20 @@ __device__ __forceinline__ int dir_scene(const int* __restrict__ prefix, int n, 
   return lo;
 }
 #endif
-// ---- incomplete LDL^T (od_ldlt.cu)
+// ---- preconditioners applied by triangular sweeps (od_sweep.cu)
 constexpr double kLdltSainvDefault = 0.1;
 constexpr double kLdltDropDefault = 0.01;
+constexpr double kIcEpsDefault = 1e-3;
 // factor of A given in the reference's lower layout on the host, or (NULL)
 // of the last A64 expansion
 od_status ldlt_factor(Scene* s, const double* host_values, double sainv_eps, double ldlt_eps);
-// z = (L D L^T)^-1 r on the device (length n_pad; padding rows copied);
-// returns at once when sc->done is set
-od_status ldlt_apply(Scene* s, const double* r, double* z, const SolveScalars* sc);
+od_status ic_factor(Scene* s, const double* host_values, double eps, double relax);
+// z = (L D L^T)^-1 r or (L L^T)^-1 r with the loaded factor, on the device
+// (length n_pad; padding rows copied); returns at once when sc->done is set
+od_status sweep_apply(Scene* s, const double* r, double* z, const SolveScalars* sc);
 // OD_ERR_DEVICE_TIMEOUT if a sweep's bounded wait ran out since the last check
-od_status ldlt_check(Scene* s);
-void ldlt_free(LdltSys* l);
+od_status sweep_check(Scene* s);
+void sweep_free(SweepSys* l);
 
 // PCG on A64; b and x are device vectors of length n_pad
 od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm, od_solve_stats* st);

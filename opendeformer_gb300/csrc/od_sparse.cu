@@ -1769,7 +1769,7 @@ void pcg_free(Scene* s) {
   cudaFree(P.gbar);
   mixed_free(P.mix);
   slice_free(P.slice);
-  ldlt_free(P.ldlt);
+  sweep_free(P.sweep);
   if (P.sc_host) cudaFreeHost(P.sc_host);
   if (P.timeout_host) cudaFreeHost(P.timeout_host);
   P = Pcg();
@@ -2196,7 +2196,7 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
   cudaStream_t strm = s->ctx->stream;
   const int nb = s->bsr.nb, n = P.n_pad;
   const int pk = prm->precond;
-  if (pk < 0 || pk > OD_PRECOND_LDLT) { set_error("unknown preconditioner"); return OD_ERR_INVALID_ARG; }
+  if (pk < 0 || pk > OD_PRECOND_IC) { set_error("unknown preconditioner"); return OD_ERR_INVALID_ARG; }
   if (nb == 0) {
     if (st) *st = od_solve_stats{};
     return OD_OK;
@@ -2219,12 +2219,20 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
     if (e != OD_OK) return e;
     shift = P.ic_shift;
   } else if (pk == OD_PRECOND_LDLT) {
-    // InLDLTPreconditioner::Preprocess runs inside every solve (cgSolver.cpp:23)
+    // Preconditioner::Preprocess runs inside every solve (cgSolver.cpp:23)
     od_status e = ldlt_factor(s, nullptr, prm->sainv_eps > 0.0 ? prm->sainv_eps : kLdltSainvDefault,
                               prm->ldlt_eps > 0.0 ? prm->ldlt_eps : kLdltDropDefault);
     if (e != OD_OK) return e;
+  } else if (pk == OD_PRECOND_IC) {
+    if (s->dofs < 2) {
+      set_error("the incomplete Cholesky preconditioner needs at least 2 DOFs");
+      return OD_ERR_INVALID_ARG;
+    }
+    od_status e = ic_factor(s, nullptr, prm->ic_eps > 0.0 ? prm->ic_eps : kIcEpsDefault, prm->ic_relax);
+    if (e != OD_OK) return e;
   }
-  const bool swept = pk == OD_PRECOND_IC0 || pk == OD_PRECOND_LDLT;   // applied by triangular sweeps
+  // applied by triangular sweeps
+  const bool swept = pk == OD_PRECOND_IC0 || pk == OD_PRECOND_LDLT || pk == OD_PRECOND_IC;
   if (!swept && P.coop_grid > 0 && !P.disable_persistent) {
     // one cooperative launch for the whole solve
     OD_CUDA(cudaMemsetAsync(P.gbar, 0, sizeof(GridBarrier), strm));
@@ -2260,7 +2268,7 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
   int g_rz0 = g_rows;
   if (swept) {
     if (pk == OD_PRECOND_IC0) ic0_apply(s, P.r, P.z, nullptr);
-    else OD_TRY(ldlt_apply(s, P.r, P.z, nullptr));
+    else OD_TRY(sweep_apply(s, P.r, P.z, nullptr));
     OD_KL(s);
     pcg_rz_kernel<<<g_vec, kThreads, 0, strm>>>(n, P.r, P.z, part_c, nullptr);
     g_rz0 = g_vec;
@@ -2290,7 +2298,7 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
       int g_rz = g_upd;
       if (swept) {
         if (pk == OD_PRECOND_IC0) ic0_apply(s, P.r, P.z, P.sc);
-        else OD_TRY(ldlt_apply(s, P.r, P.z, P.sc));
+        else OD_TRY(sweep_apply(s, P.r, P.z, P.sc));
         OD_KL(s);
         pcg_rz_kernel<<<g_vec, kThreads, 0, strm>>>(n, P.r, P.z, part_c, P.sc);
         g_rz = g_vec;
@@ -2312,7 +2320,7 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
     ev_used = 0;
     if (P.sc_host->done) break;
   }
-  if (pk == OD_PRECOND_LDLT) OD_TRY(ldlt_check(s));
+  if (pk == OD_PRECOND_LDLT || pk == OD_PRECOND_IC) OD_TRY(sweep_check(s));
   return pcg_finish(s, d_b, d_x, shift, st, false, false);
 }
 

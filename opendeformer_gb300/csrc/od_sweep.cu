@@ -1,13 +1,20 @@
-// Incomplete LDL^T preconditioner (solver/inLDLTPreconditioner.cpp).
+// Preconditioners applied by two triangular sweeps, with the factor made on
+// the host: the reference's incomplete LDL^T (solver/inLDLTPreconditioner.cpp,
+// factor in od_rif.cpp) and its threshold incomplete Cholesky
+// (solver/inCholeskyPreconditioner.cpp, factor in od_ric.cpp).  Both
+// factorisations are strictly sequential sweeps with data-dependent fill,
+// so they run on the host, bit-identical to the reference's; the device
+// takes the part that runs every PCG iteration.
 //
-// The factor is made on the host (od_rif.cpp: a strictly sequential sweep
-// with data-dependent fill) from A in the reference's lower value layout,
-// then uploaded as
+// A factor is uploaded as its strictly lower part L (unit diagonal for
+// LDL^T) and a diagonal array:
 //   forward  : L by rows (CSR, columns ascending)       -> L y = r
-//   backward : L by columns (the reference's storage)   -> L^T z = D^-1 y
-// and applied on the device by one cooperative launch per apply.  Rows are
-// listed by dependency level (level of a row = 1 + the highest level of the
-// rows it reads; forward and backward levels apart), and warp w of the W
+//   backward : L by columns (the reference's order)     -> L^T z = y
+//   LDL^T    : y_j = r_j - sum L_jc y_c;          z_i = y_i D_ii^-1 - sum z_r L_ri
+//   IC       : y_j = (r_j - sum L_jc y_c) / L_jj;  z_i = (y_i - sum z_r L_ri) / L_ii
+// and applied by one cooperative launch per apply.  Rows are listed by
+// dependency level (level of a row = 1 + the highest level of the rows it
+// reads; forward and backward levels apart), and warp w of the W
 // co-resident warps takes entries w, w+W, ... of the forward list, then of
 // the backward list.  y and z are filled with an all-ones NaN before the
 // launch (a pattern no arithmetic result has); a row waits (bounded) until
@@ -21,8 +28,7 @@
 // Dependent FP64 operations cost 64 cycles each on this part (a shuffle
 // plus an add about 108), so a row's products are summed by a fixed
 // 5-level butterfly over the warp rather than one after another: the result
-// is deterministic and within rounding of the reference's sequential sums
-// (solvePreconditionerSystem, :151-184).
+// is deterministic and within rounding of the reference's sequential sums.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -33,28 +39,32 @@
 
 namespace od {
 
-struct LdltSys {
-  RifColumns cols;
-  RifFactor f;
+struct SweepSys {
+  int kind = -1;                     // factor loaded: OD_PRECOND_LDLT or OD_PRECOND_IC, -1 none
+  RifColumns rif_cols;               // (built on first use of each kind)
+  RicColumns ric_cols;
+  RifFactor rif;                     // the last factors in the reference's storage
+  RicFactor ric;
   int n = 0, n_pad = 0, nvals = 0;
+  long long nnz = 0;                 // strictly lower entries of the loaded factor
   long long cap = 0;                 // entry capacity of the device arrays
   double* lo_dev = nullptr;          // A in the reference lower layout (device)
   double* lo_host = nullptr;         // pinned mirror
   int *f_rp = nullptr, *f_ci = nullptr, *b_cp = nullptr, *b_ri = nullptr;
   int *ord_f = nullptr, *ord_b = nullptr;   // rows by forward / backward level
-  double *f_val = nullptr, *b_val = nullptr, *dinv = nullptr, *y = nullptr;
+  double *f_val = nullptr, *b_val = nullptr, *diag = nullptr, *y = nullptr;
   int *err = nullptr, *err_host = nullptr;
   int grid = 0;                      // co-resident CTAs of the apply
   int depth_f = 0, depth_b = 0;      // longest dependency chains of the two sweeps (rows)
-  bool have = false;                 // a factor is loaded
-  std::vector<int> h_rp, h_ci, h_cp, h_of, h_ob;  // host staging of the sweep arrays
-  std::vector<double> h_fval;
+  // host staging of the sweep arrays
+  std::vector<int> h_rp, h_ci, h_cp, h_ri, h_of, h_ob;
+  std::vector<double> h_fval, h_bval, h_diag;
 };
 
 namespace {
 
-constexpr int kLdltThreads = 256;
-constexpr unsigned kLdltSpinLimit = 1u << 21;
+constexpr int kSweepThreads = 256;
+constexpr unsigned kSweepSpinLimit = 1u << 21;
 constexpr unsigned long long kPending = 0xffffffffffffffffull;   // "not yet written" (a NaN)
 
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const double* p) {
@@ -71,7 +81,7 @@ __device__ __forceinline__ void st_release_f64(double* p, double x) {
 // thread waits any more, so the launch ends promptly and the host reports it
 __device__ __forceinline__ double wait_value(const double* p, int* err) {
   unsigned long long v = ld_acquire_u64(p);
-  for (unsigned k = 1; v == kPending && k < kLdltSpinLimit; k++) {
+  for (unsigned k = 1; v == kPending && k < kSweepSpinLimit; k++) {
     if ((k & 1023u) == 0 && *(volatile int*)err) return 0.0;
     v = ld_acquire_u64(p);
   }
@@ -87,10 +97,12 @@ __device__ __forceinline__ double warp_sum(double x) {
   return x;
 }
 
-__global__ void __launch_bounds__(kLdltThreads) ldlt_apply_kernel(
+// IC = 0: LDL^T (diag = D^-1), IC = 1: Cholesky (diag = L_ii)
+template <int IC>
+__global__ void __launch_bounds__(kSweepThreads) sweep_apply_kernel(
     int n, int n_pad, const int* __restrict__ frp, const int* __restrict__ fci, const double* __restrict__ fval,
     const int* __restrict__ bcp, const int* __restrict__ bri, const double* __restrict__ bval,
-    const int* __restrict__ ord_f, const int* __restrict__ ord_b, const double* __restrict__ dinv,
+    const int* __restrict__ ord_f, const int* __restrict__ ord_b, const double* __restrict__ diag,
     const double* __restrict__ r, double* y, double* z, int* __restrict__ err, const SolveScalars* sc) {
   if (sc && *(volatile const int*)&sc->done) return;
   const int lane = threadIdx.x & 31;
@@ -100,7 +112,7 @@ __global__ void __launch_bounds__(kLdltThreads) ldlt_apply_kernel(
   // padding rows carry the identity
   for (int i = n + blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += gridDim.x * blockDim.x) z[i] = r[i];
 
-  // forward: y_j = r_j - sum_c L_jc y_c
+  // forward
   for (int t = w; t < n; t += W) {
     const int j = ord_f[t];
     double s = r[j];
@@ -115,10 +127,10 @@ __global__ void __launch_bounds__(kLdltThreads) ldlt_apply_kernel(
       }
       s -= warp_sum(prod);
     }
-    if (lane == 0) st_release_f64(y + j, s);
+    if (lane == 0) st_release_f64(y + j, IC ? s / diag[j] : s);
   }
 
-  // backward: z_i = y_i d_i^-1 - sum_r z_r L_ri
+  // backward
   for (int t = w; t < n; t += W) {
     const int i = ord_b[t];
     const int e = bcp[i + 1];
@@ -133,7 +145,10 @@ __global__ void __launch_bounds__(kLdltThreads) ldlt_apply_kernel(
       }
       dot += warp_sum(prod);
     }
-    if (lane == 0) st_release_f64(z + i, wait_value(y + i, err) * dinv[i] - dot);
+    if (lane == 0) {
+      const double yi = wait_value(y + i, err);
+      st_release_f64(z + i, IC ? (yi - dot) / diag[i] : yi * diag[i] - dot);
+    }
   }
 }
 
@@ -158,94 +173,89 @@ od_status grow(T** p, long long need, long long& bytes) {
   return OD_OK;
 }
 
-od_status ldlt_alloc(Scene* s) {
+od_status sweep_alloc(Scene* s) {
   Pcg& P = s->pcg;
-  if (P.ldlt) return OD_OK;
-  LdltSys* l = new LdltSys();
-  P.ldlt = l;
+  if (P.sweep) return OD_OK;
+  SweepSys* l = new SweepSys();
+  P.sweep = l;
   l->n = s->dofs;
   l->n_pad = P.n_pad;
   l->nvals = s->nvals;
-  rif_columns(s->dofs, s->nbc, s->hpcol, s->hrows, l->cols);
   const int n = l->n;
   OD_CUDA(cudaMalloc(&l->lo_dev, sizeof(double) * (size_t)std::max(1, l->nvals)));
   OD_CUDA(cudaMallocHost(&l->lo_host, sizeof(double) * (size_t)std::max(1, l->nvals)));
   for (int** a : {&l->f_rp, &l->b_cp, &l->ord_f, &l->ord_b}) OD_CUDA(cudaMalloc(a, sizeof(int) * (size_t)(n + 1)));
-  for (double** a : {&l->dinv, &l->y}) OD_CUDA(cudaMalloc(a, sizeof(double) * (size_t)std::max(1, n)));
+  for (double** a : {&l->diag, &l->y}) OD_CUDA(cudaMalloc(a, sizeof(double) * (size_t)std::max(1, n)));
   OD_CUDA(cudaMalloc(&l->err, sizeof(int)));
   OD_CUDA(cudaMemset(l->err, 0, sizeof(int)));
   OD_CUDA(cudaMallocHost(&l->err_host, sizeof(int)));
   s->device_bytes += (long long)sizeof(double) * l->nvals + (long long)(sizeof(int) * 4 + sizeof(double) * 2) * n;
-  // co-resident CTAs for the cooperative apply
-  int dev_coop = 0, per_sm = 0;
+  // co-resident CTAs for the cooperative apply (both instantiations share
+  // the launch bounds; the smaller occupancy is used)
+  int dev_coop = 0, per0 = 0, per1 = 0;
   OD_CUDA(cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, s->ctx->device));
-  OD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ldlt_apply_kernel, kLdltThreads, 0));
+  OD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, sweep_apply_kernel<0>, kSweepThreads, 0));
+  OD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, sweep_apply_kernel<1>, kSweepThreads, 0));
+  const int per_sm = std::min(per0, per1);
   if (!dev_coop || per_sm < 1) {
-    set_error("the LDL^T apply needs cooperative launch");
+    set_error("the triangular-sweep apply needs cooperative launch");
     return OD_ERR_UNSUPPORTED;
   }
   // two CTAs (16 warps) per SM: each level's rows spread over 4864 warps;
   // more warps only add polling traffic
   int per = 2;
-  if (const char* e = std::getenv("OD_GB300_LDLT_CTAS_PER_SM")) per = std::max(1, std::atoi(e));
-  const int want = (n + (kLdltThreads / 32) - 1) / (kLdltThreads / 32);   // one warp per row at most
+  if (const char* e = std::getenv("OD_GB300_SWEEP_CTAS_PER_SM")) per = std::max(1, std::atoi(e));
+  const int want = (n + (kSweepThreads / 32) - 1) / (kSweepThreads / 32);   // one warp per row at most
   l->grid = std::max(1, std::min(std::min(per, per_sm) * s->ctx->num_sms, want));
   return OD_OK;
 }
 
-}  // namespace
-
-void ldlt_free(LdltSys* l) {
-  if (!l) return;
-  for (double* p : {l->lo_dev, l->f_val, l->b_val, l->dinv, l->y}) cudaFree(p);
-  for (int* p : {l->f_rp, l->f_ci, l->b_cp, l->b_ri, l->ord_f, l->ord_b, l->err}) cudaFree(p);
-  if (l->lo_host) cudaFreeHost(l->lo_host);
-  if (l->err_host) cudaFreeHost(l->err_host);
-  delete l;
+// A on the host in the reference's lower layout: given, or rebuilt from
+// the last expansion on the device
+od_status lower_values(Scene* s, SweepSys* l, const double* host_values, const double** out) {
+  if (host_values) {
+    *out = host_values;
+    return OD_OK;
+  }
+  if (!s->lo.v1) {
+    set_error("preconditioner factor: no system matrix has been formed");
+    return OD_ERR_INTERNAL;
+  }
+  cudaStream_t strm = s->ctx->stream;
+  if (l->nvals > 0) {
+    OD_KL(s);
+    combine_lower_kernel<<<(l->nvals + 255) / 256, 256, 0, strm>>>(l->nvals, s->lo.v1, s->lo.c1, s->lo.v2, s->lo.c2,
+                                                                   s->lo.v3, s->lo.c3, l->lo_dev);
+    OD_CUDA(cudaGetLastError());
+    OD_CUDA(cudaMemcpyAsync(l->lo_host, l->lo_dev, sizeof(double) * l->nvals, cudaMemcpyDeviceToHost, strm));
+  }
+  OD_TRY(sync_stream(s));
+  *out = l->lo_host;
+  return OD_OK;
 }
 
-od_status ldlt_factor(Scene* s, const double* host_values, double sainv_eps, double ldlt_eps) {
-  OD_TRY(ldlt_alloc(s));
-  LdltSys* l = s->pcg.ldlt;
-  cudaStream_t strm = s->ctx->stream;
-  const auto t0 = std::chrono::steady_clock::now();
-  const double* vals = host_values;
-  if (!vals) {
-    if (!s->lo.v1) {
-      set_error("LDL^T factor: no system matrix has been formed");
-      return OD_ERR_INTERNAL;
-    }
-    if (l->nvals > 0) {
-      OD_KL(s);
-      combine_lower_kernel<<<(l->nvals + 255) / 256, 256, 0, strm>>>(l->nvals, s->lo.v1, s->lo.c1, s->lo.v2, s->lo.c2,
-                                                                     s->lo.v3, s->lo.c3, l->lo_dev);
-      OD_CUDA(cudaGetLastError());
-      OD_CUDA(cudaMemcpyAsync(l->lo_host, l->lo_dev, sizeof(double) * l->nvals, cudaMemcpyDeviceToHost, strm));
-    }
-    OD_TRY(sync_stream(s));
-    vals = l->lo_host;
-  }
+// upload the staged strictly lower part (h_cp / h_ri / h_bval, by columns)
+// and diagonal (h_diag): forward CSR, dependency levels and row lists
+od_status upload(Scene* s, SweepSys* l, int kind) {
   const int n = l->n;
-  rif_factor(l->cols, vals, sainv_eps, ldlt_eps, l->f);
-  const RifFactor& F = l->f;
-  const long long nnz = (long long)F.val.size();
+  const long long nnz = (long long)l->h_ri.size();
   if (nnz > 0x7fffffffLL) {
-    set_error("LDL^T factor exceeds 2^31 entries");
+    set_error("preconditioner factor exceeds 2^31 entries");
     return OD_ERR_OUT_OF_MEMORY;
   }
   // forward CSR (columns ascending in every row) by a counting transpose
   l->h_rp.assign(n + 1, 0);
-  for (long long q = 0; q < nnz; q++) l->h_rp[F.row[q] + 1]++;
+  for (long long q = 0; q < nnz; q++) l->h_rp[l->h_ri[q] + 1]++;
   for (int i = 0; i < n; i++) l->h_rp[i + 1] += l->h_rp[i];
   l->h_ci.resize(nnz);
   l->h_fval.resize(nnz);
   {
     std::vector<int> fill(l->h_rp.begin(), l->h_rp.end() - 1);
-    for (int c = 0; c + 1 < n; c++)
-      for (int q = F.pcol[c]; q < F.pcol[c + 1]; q++) {
-        const int at = fill[F.row[q]]++;
+    for (int c = 0; c < n; c++)
+      for (int q = l->h_cp[c]; q < l->h_cp[c + 1]; q++) {
+        const int at = fill[l->h_ri[q]]++;
         l->h_ci[at] = c;
-        l->h_fval[at] = F.val[q];
+        l->h_fval[at] = l->h_bval[q];
       }
   }
   // dependency levels of the two sweeps and the rows listed by level (a
@@ -271,20 +281,17 @@ od_status ldlt_factor(Scene* s, const double* host_values, double sainv_eps, dou
     }
     list_by_level(df, true, l->h_of);
     std::fill(lev.begin(), lev.end(), 0);
-    for (int i = n - 2; i >= 0; i--) {
+    for (int i = n - 1; i >= 0; i--) {
       int m = 0;
-      for (int q = F.pcol[i]; q < F.pcol[i + 1]; q++) m = std::max(m, lev[F.row[q]] + 1);
+      for (int q = l->h_cp[i]; q < l->h_cp[i + 1]; q++) m = std::max(m, lev[l->h_ri[q]] + 1);
       lev[i] = m;
       db = std::max(db, m + 1);
     }
-    if (n > 0) db = std::max(db, 1);
     list_by_level(db, false, l->h_ob);
     l->depth_f = df;
     l->depth_b = db;
   }
-  // backward column pointers: the reference's pcol (n entries) closed by nnz
-  l->h_cp.assign(F.pcol.begin(), F.pcol.end());
-  l->h_cp.resize(n + 1, (int)nnz);
+  cudaStream_t strm = s->ctx->stream;
   if (nnz > l->cap) {
     long long cap = std::max(nnz, l->cap + l->cap / 2);
     long long bytes = 0;
@@ -298,31 +305,92 @@ od_status ldlt_factor(Scene* s, const double* host_values, double sainv_eps, dou
   if (n > 0) {
     OD_CUDA(cudaMemcpyAsync(l->f_rp, l->h_rp.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, strm));
     OD_CUDA(cudaMemcpyAsync(l->b_cp, l->h_cp.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, strm));
-    OD_CUDA(cudaMemcpyAsync(l->dinv, F.dinv.data(), sizeof(double) * n, cudaMemcpyHostToDevice, strm));
+    OD_CUDA(cudaMemcpyAsync(l->diag, l->h_diag.data(), sizeof(double) * n, cudaMemcpyHostToDevice, strm));
     OD_CUDA(cudaMemcpyAsync(l->ord_f, l->h_of.data(), sizeof(int) * n, cudaMemcpyHostToDevice, strm));
     OD_CUDA(cudaMemcpyAsync(l->ord_b, l->h_ob.data(), sizeof(int) * n, cudaMemcpyHostToDevice, strm));
   }
   if (nnz > 0) {
     OD_CUDA(cudaMemcpyAsync(l->f_ci, l->h_ci.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, strm));
     OD_CUDA(cudaMemcpyAsync(l->f_val, l->h_fval.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice, strm));
-    OD_CUDA(cudaMemcpyAsync(l->b_ri, F.row.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, strm));
-    OD_CUDA(cudaMemcpyAsync(l->b_val, F.val.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice, strm));
+    OD_CUDA(cudaMemcpyAsync(l->b_ri, l->h_ri.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, strm));
+    OD_CUDA(cudaMemcpyAsync(l->b_val, l->h_bval.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice, strm));
   }
   // the staging vectors are read by the copies: finish them before returning
   OD_TRY(sync_stream(s));
-  l->have = true;
+  l->kind = kind;
+  l->nnz = nnz;
   Ctx* ctx = s->ctx;
-  ctx->ldlt_factors++;
-  ctx->ldlt_nnz = nnz;
-  ctx->ldlt_levels = (long long)l->depth_f + l->depth_b;
-  ctx->ldlt_factor_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  ctx->sweep_factors++;
+  ctx->sweep_nnz = nnz;
+  ctx->sweep_levels = (long long)l->depth_f + l->depth_b;
   return OD_OK;
 }
 
-od_status ldlt_apply(Scene* s, const double* r, double* z, const SolveScalars* sc) {
-  LdltSys* l = s->pcg.ldlt;
-  if (!l || !l->have) {
-    set_error("LDL^T apply without a factor");
+}  // namespace
+
+void sweep_free(SweepSys* l) {
+  if (!l) return;
+  for (double* p : {l->lo_dev, l->f_val, l->b_val, l->diag, l->y}) cudaFree(p);
+  for (int* p : {l->f_rp, l->f_ci, l->b_cp, l->b_ri, l->ord_f, l->ord_b, l->err}) cudaFree(p);
+  if (l->lo_host) cudaFreeHost(l->lo_host);
+  if (l->err_host) cudaFreeHost(l->err_host);
+  delete l;
+}
+
+od_status ldlt_factor(Scene* s, const double* host_values, double sainv_eps, double ldlt_eps) {
+  OD_TRY(sweep_alloc(s));
+  SweepSys* l = s->pcg.sweep;
+  const auto t0 = std::chrono::steady_clock::now();
+  const double* vals = nullptr;
+  OD_TRY(lower_values(s, l, host_values, &vals));
+  if (l->rif_cols.n != l->n || l->rif_cols.ptr.empty()) rif_columns(l->n, s->nbc, s->hpcol, s->hrows, l->rif_cols);
+  rif_factor(l->rif_cols, vals, sainv_eps, ldlt_eps, l->rif);
+  const RifFactor& F = l->rif;
+  const int n = l->n;
+  // strictly lower by columns: the reference's storage (pcol n entries) closed by nnz
+  l->h_cp.assign(F.pcol.begin(), F.pcol.end());
+  l->h_cp.resize(n + 1, (int)F.val.size());
+  l->h_ri.assign(F.row.begin(), F.row.end());
+  l->h_bval.assign(F.val.begin(), F.val.end());
+  l->h_diag.assign(F.dinv.begin(), F.dinv.end());
+  OD_TRY(upload(s, l, OD_PRECOND_LDLT));
+  s->ctx->sweep_factor_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return OD_OK;
+}
+
+od_status ic_factor(Scene* s, const double* host_values, double eps, double relax) {
+  OD_TRY(sweep_alloc(s));
+  SweepSys* l = s->pcg.sweep;
+  const auto t0 = std::chrono::steady_clock::now();
+  const double* vals = nullptr;
+  OD_TRY(lower_values(s, l, host_values, &vals));
+  if (l->ric_cols.n != l->n || l->ric_cols.ptr.empty())
+    ric_columns(l->n, s->nbc, s->hpcol, s->hrows, s->horis, l->ric_cols);
+  ric_factor(l->ric_cols, vals, eps, relax, l->ric);
+  const RicFactor& F = l->ric;
+  const int n = l->n;
+  // split every column into its diagonal (first) and the rows below it
+  l->h_cp.assign(n + 1, 0);
+  l->h_ri.clear();
+  l->h_bval.clear();
+  l->h_diag.assign(n, 0.0);
+  for (int c = 0; c < n; c++) {
+    l->h_diag[c] = F.val[F.pcol[c]];
+    for (int q = F.pcol[c] + 1; q < F.pcol[c + 1]; q++) {
+      l->h_ri.push_back(F.row[q]);
+      l->h_bval.push_back(F.val[q]);
+    }
+    l->h_cp[c + 1] = (int)l->h_ri.size();
+  }
+  OD_TRY(upload(s, l, OD_PRECOND_IC));
+  s->ctx->sweep_factor_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return OD_OK;
+}
+
+od_status sweep_apply(Scene* s, const double* r, double* z, const SolveScalars* sc) {
+  SweepSys* l = s->pcg.sweep;
+  if (!l || l->kind < 0) {
+    set_error("triangular-sweep apply without a factor");
     return OD_ERR_INTERNAL;
   }
   Ctx* ctx = s->ctx;
@@ -338,11 +406,11 @@ od_status ldlt_apply(Scene* s, const double* r, double* z, const SolveScalars* s
   const double* bval = l->b_val;
   const int* of = l->ord_f;
   const int* ob = l->ord_b;
-  const double* dinv = l->dinv;
+  const double* dg = l->diag;
   double* y = l->y;
   int* err = l->err;
   void* args[] = {(void*)&n,   (void*)&n_pad, (void*)&frp, (void*)&fci, (void*)&fval, (void*)&bcp,
-                  (void*)&bri, (void*)&bval,  (void*)&of,  (void*)&ob,  (void*)&dinv, (void*)&r,
+                  (void*)&bri, (void*)&bval,  (void*)&of,  (void*)&ob,  (void*)&dg,   (void*)&r,
                   (void*)&y,   (void*)&z,     (void*)&err, (void*)&sc};
   // every value starts "not yet written" (all-ones bytes)
   if (n > 0) {
@@ -350,7 +418,8 @@ od_status ldlt_apply(Scene* s, const double* r, double* z, const SolveScalars* s
     OD_CUDA(cudaMemsetAsync(z, 0xff, sizeof(double) * (size_t)n, strm));
   }
   OD_KL(s);
-  OD_CUDA(cudaLaunchCooperativeKernel((void*)ldlt_apply_kernel, dim3(l->grid), dim3(kLdltThreads), args, 0, strm));
+  void* fn = l->kind == OD_PRECOND_IC ? (void*)sweep_apply_kernel<1> : (void*)sweep_apply_kernel<0>;
+  OD_CUDA(cudaLaunchCooperativeKernel(fn, dim3(l->grid), dim3(kSweepThreads), args, 0, strm));
   if (prof) {
     OD_CUDA(cudaEventRecord(ctx->ev_pool[ctx->ev_pool.size() - 1], strm));
     OD_CUDA(cudaEventSynchronize(ctx->ev_pool[ctx->ev_pool.size() - 1]));
@@ -364,23 +433,23 @@ od_status ldlt_apply(Scene* s, const double* r, double* z, const SolveScalars* s
       ran = !h.done;
     }
     if (ran) {
-      ctx->ldlt_applies++;
-      ctx->ldlt_apply_ms += ms;
-      ctx->ldlt_apply_bytes += 2.0 * 12.0 * (double)l->f.val.size() + 48.0 * n;
+      ctx->sweep_applies++;
+      ctx->sweep_apply_ms += ms;
+      ctx->sweep_apply_bytes += 2.0 * 12.0 * (double)l->nnz + 56.0 * n;
     }
   }
   return OD_OK;
 }
 
-od_status ldlt_check(Scene* s) {
-  LdltSys* l = s->pcg.ldlt;
+od_status sweep_check(Scene* s) {
+  SweepSys* l = s->pcg.sweep;
   if (!l) return OD_OK;
   cudaStream_t strm = s->ctx->stream;
   OD_CUDA(cudaMemcpyAsync(l->err_host, l->err, sizeof(int), cudaMemcpyDeviceToHost, strm));
   OD_TRY(sync_stream(s));
   if (*l->err_host) {
     OD_CUDA(cudaMemsetAsync(l->err, 0, sizeof(int), strm));
-    set_error("LDL^T sweep: a bounded wait on a row flag ran out");
+    set_error("triangular sweep: a bounded wait on a row value ran out");
     return OD_ERR_DEVICE_TIMEOUT;
   }
   return OD_OK;
@@ -391,6 +460,28 @@ od_status ldlt_check(Scene* s) {
 // ------------------------------------------------------------------ C ABI
 using namespace od;
 
+namespace {
+
+od_status apply_host(od_scene* scene, int kind, const double* rhs, double* result, const char* what) {
+  Scene* s = &scene->s;
+  SweepSys* l = s->pcg.sweep;
+  if (!l || l->kind != kind) {
+    set_error(what);
+    return OD_ERR_INVALID_ARG;
+  }
+  OD_CUDA(cudaSetDevice(s->ctx->device));
+  Pcg& P = s->pcg;
+  cudaStream_t strm = s->ctx->stream;
+  OD_CUDA(cudaMemsetAsync(P.r, 0, sizeof(double) * P.n_pad, strm));
+  if (s->dofs > 0) OD_CUDA(cudaMemcpyAsync(P.r, rhs, sizeof(double) * s->dofs, cudaMemcpyHostToDevice, strm));
+  OD_TRY(sweep_apply(s, P.r, P.z, nullptr));
+  if (s->dofs > 0) OD_CUDA(cudaMemcpyAsync(result, P.z, sizeof(double) * s->dofs, cudaMemcpyDeviceToHost, strm));
+  OD_TRY(sync_stream(s));
+  return sweep_check(s);
+}
+
+}  // namespace
+
 extern "C" od_status od_scene_ldlt_factor(od_scene* scene, const double* values, double sainv_eps, double ldlt_eps,
                                           long long* nnz) {
   OD_CHECK_ARG(scene && values, "od_scene_ldlt_factor: NULL argument");
@@ -399,16 +490,15 @@ extern "C" od_status od_scene_ldlt_factor(od_scene* scene, const double* values,
   Scene* s = &scene->s;
   OD_CUDA(cudaSetDevice(s->ctx->device));
   OD_TRY(ldlt_factor(s, values, sainv_eps, ldlt_eps));
-  if (nnz) *nnz = (long long)s->pcg.ldlt->f.val.size();
+  if (nnz) *nnz = (long long)s->pcg.sweep->rif.val.size();
   return OD_OK;
 }
 
 extern "C" od_status od_scene_ldlt_get(od_scene* scene, double* values, int* rows, int* pcol, double* inv_diag) {
   OD_CHECK_ARG(scene, "od_scene_ldlt_get: scene is NULL");
-  Scene* s = &scene->s;
-  LdltSys* l = s->pcg.ldlt;
-  OD_CHECK_ARG(l && l->have, "od_scene_ldlt_get: no factor (call od_scene_ldlt_factor first)");
-  const RifFactor& F = l->f;
+  SweepSys* l = scene->s.pcg.sweep;
+  OD_CHECK_ARG(l && l->kind == OD_PRECOND_LDLT, "od_scene_ldlt_get: no LDL^T factor (call od_scene_ldlt_factor)");
+  const RifFactor& F = l->rif;
   if (values && !F.val.empty()) std::copy(F.val.begin(), F.val.end(), values);
   if (rows && !F.row.empty()) std::copy(F.row.begin(), F.row.end(), rows);
   if (pcol && !F.pcol.empty()) std::copy(F.pcol.begin(), F.pcol.end(), pcol);
@@ -418,18 +508,34 @@ extern "C" od_status od_scene_ldlt_get(od_scene* scene, double* values, int* row
 
 extern "C" od_status od_scene_ldlt_apply(od_scene* scene, const double* rhs, double* result) {
   OD_CHECK_ARG(scene && rhs && result, "od_scene_ldlt_apply: NULL argument");
+  return apply_host(scene, OD_PRECOND_LDLT, rhs, result, "od_scene_ldlt_apply: no LDL^T factor loaded");
+}
+
+extern "C" od_status od_scene_ic_factor(od_scene* scene, const double* values, double eps, double relax,
+                                        long long* nnz) {
+  OD_CHECK_ARG(scene && values, "od_scene_ic_factor: NULL argument");
+  OD_CHECK_ARG(eps >= 0.0 && relax >= 0.0 && std::isfinite(eps) && std::isfinite(relax),
+               "od_scene_ic_factor: epsilon and relaxedScale must be finite and >= 0");
   Scene* s = &scene->s;
-  LdltSys* l = s->pcg.ldlt;
-  OD_CHECK_ARG(l && l->have, "od_scene_ldlt_apply: no factor (call od_scene_ldlt_factor first)");
+  OD_CHECK_ARG(s->dofs >= 2, "od_scene_ic_factor: needs at least 2 DOFs");
   OD_CUDA(cudaSetDevice(s->ctx->device));
-  Pcg& P = s->pcg;
-  cudaStream_t strm = s->ctx->stream;
-  OD_CUDA(cudaMemsetAsync(P.r, 0, sizeof(double) * P.n_pad, strm));
-  if (s->dofs > 0)
-    OD_CUDA(cudaMemcpyAsync(P.r, rhs, sizeof(double) * s->dofs, cudaMemcpyHostToDevice, strm));
-  OD_TRY(ldlt_apply(s, P.r, P.z, nullptr));
-  if (s->dofs > 0)
-    OD_CUDA(cudaMemcpyAsync(result, P.z, sizeof(double) * s->dofs, cudaMemcpyDeviceToHost, strm));
-  OD_TRY(sync_stream(s));
-  return ldlt_check(s);
+  OD_TRY(ic_factor(s, values, eps, relax));
+  if (nnz) *nnz = (long long)s->pcg.sweep->ric.val.size();
+  return OD_OK;
+}
+
+extern "C" od_status od_scene_ic_get(od_scene* scene, double* values, int* rows, int* pcol) {
+  OD_CHECK_ARG(scene, "od_scene_ic_get: scene is NULL");
+  SweepSys* l = scene->s.pcg.sweep;
+  OD_CHECK_ARG(l && l->kind == OD_PRECOND_IC, "od_scene_ic_get: no incomplete Cholesky factor (call od_scene_ic_factor)");
+  const RicFactor& F = l->ric;
+  if (values && !F.val.empty()) std::copy(F.val.begin(), F.val.end(), values);
+  if (rows && !F.row.empty()) std::copy(F.row.begin(), F.row.end(), rows);
+  if (pcol && !F.pcol.empty()) std::copy(F.pcol.begin(), F.pcol.end(), pcol);
+  return OD_OK;
+}
+
+extern "C" od_status od_scene_ic_apply(od_scene* scene, const double* rhs, double* result) {
+  OD_CHECK_ARG(scene && rhs && result, "od_scene_ic_apply: NULL argument");
+  return apply_host(scene, OD_PRECOND_IC, rhs, result, "od_scene_ic_apply: no incomplete Cholesky factor loaded");
 }

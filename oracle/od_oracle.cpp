@@ -553,6 +553,7 @@ struct Scene {
   double yield = 0, creep = 0, max_plastic = 0;  // plastic parameters
   std::vector<double> plastic;          // plastic strain, 9 per tet (state, changes at every evaluation)
   double ldlt_sainv = 0.1, ldlt_drop = 0.01;  // InLDLTPreconditioner(sainvEpsilon, ldltEpsilon)
+  double ic_eps = 1e-3, ic_relax = 0.0;       // InCholeskyPreconditioner(epsilon, relaxedScale)
   // pattern (reference layout)
   int nbc = 0, nrem = 0;
   std::vector<int> pcol, rows, oris, emap;
@@ -1146,6 +1147,20 @@ void diagonal(const Scene& s, const double* val, double* d) {
   for (int k = 0; k < s.nrem; k++) d[3 * s.nbc + k] = val[s.oris[s.nbc + k]];
 }
 
+// sparse vector with entries in first-touch order (the reference's
+// FastSparseVector, core/latool.h:453-520)
+struct TouchVec {
+  std::vector<int> at, idx;
+  std::vector<double> val;
+  explicit TouchVec(int n) : at(n, -1) {}
+  void add(int i, double x) {
+    if (at[i] >= 0) { val[at[i]] += x; return; }
+    at[i] = (int)idx.size(); idx.push_back(i); val.push_back(x);
+  }
+  double get(int i) const { return at[i] >= 0 ? val[at[i]] : 0.0; }
+  void clear() { for (int i : idx) at[i] = -1; idx.clear(); val.clear(); }
+};
+
 // ---------------------------------------------------------- preconditioners
 // 0 identity (preconditioner.h:14-16), 1 Jacobi (jacobiPreconditioner.cpp:
 // 12-26: 1/d, or 1 when d <= 0), 2 3x3 block-Jacobi, 3 IC(0).
@@ -1169,7 +1184,159 @@ struct Precond {
   double sainv_eps = 0.1, ldlt_eps = 0.01;
   std::vector<double> lval, dinv;
   std::vector<int> lrow, lpcol;
+  // threshold incomplete Cholesky (kind 5), reference storage: column c =
+  // its diagonal then its rows below ascending; pcol n + 1 entries
+  double ic_eps = 1e-3, ic_relax = 0.0;
+  std::vector<double> cval;
+  std::vector<int> crow, cpcol;
 };
+
+// Column c of the stored lower triangle as BlockedSymSparseMatrix::getColumn
+// gives it (core/sparseMatrix.h:297-365): rows c and below in storage
+// (ascending) order, zero values left out.
+void lower_column(const Scene& s, const double* val, int c, std::vector<std::pair<int, double>>& out) {
+  out.clear();
+  const int n = s.dofs;
+  if (c / 3 < s.nbc) {
+    const int bc = c / 3, off = c - 3 * bc;
+    const double* v = val + s.oris[bc];
+    int k = s.pcol[bc];
+    const int e = s.pcol[bc + 1];
+    if (k == e) return;
+    if (s.rows[k] == 3 * bc) {   // diagonal block, packed (0,0),(1,0),(2,0),(1,1),(2,1),(2,2)
+      static const int first[3] = {0, 3, 5};
+      for (int i = 0; i < 3 - off; i++)
+        if (v[first[off] + i] != 0.0) out.push_back({c + i, v[first[off] + i]});
+      k++;
+      v += 6;
+    }
+    for (; k < e; k++) {
+      const int r0 = s.rows[k];
+      const int w = k == e - 1 ? std::min(3, n - r0) : 3;
+      for (int i = 0; i < w; i++)
+        if (v[off * w + i] != 0.0) out.push_back({r0 + i, v[off * w + i]});
+      v += 3 * w;
+    }
+  } else {
+    const int col = s.nbc + (c - 3 * s.nbc);
+    const double* v = val + s.oris[col];
+    for (int q = s.pcol[col]; q < s.pcol[col + 1]; q++)
+      if (v[q - s.pcol[col]] != 0.0) out.push_back({s.rows[q], v[q - s.pcol[col]]});
+  }
+}
+
+// InCholeskyPreconditioner::incompleteCholeskyDecomposition and
+// proccessSingleColumn (solver/inCholeskyPreconditioner.cpp:18-130): a
+// left-looking column factorisation.  Column i starts from A's column i
+// (getColumn: diagonal first); every earlier column j with a stored entry
+// in row i subtracts L_ij times its entries below row i (the columns are
+// found through per-row chains: chain[r] lists the columns whose next
+// unprocessed entry is in row r, with that entry's position).  Then, with d
+// the running diagonal of column i (A_ii minus the squares of the entries
+// already stored in row i), each off-diagonal v of row r is dropped when
+// v^2 < |eps^2 d d_r| -- adding |v| relaxedScale to both d and d_r -- or
+// kept; L_ii = sqrt(d) (d <= 0 replaced by eps^2 d^2), L_ri = v / L_ii, and
+// d_r -= L_ri^2.  The last column takes sqrt(d) only.
+void ric_factor(const Scene& s, const double* val, Precond& P) {
+  const int n = s.dofs;
+  P.cval.clear(); P.crow.clear(); P.cpcol.assign(1, 0);
+  if (n == 0) return;
+  std::vector<double> d(n, 0.0);
+  std::vector<std::pair<int, double>> col;
+  for (int c = 0; c < n; c++) {   // getDiagonal: the stored (c, c) entry or 0
+    lower_column(s, val, c, col);
+    d[c] = (!col.empty() && col[0].first == c) ? col[0].second : 0.0;
+  }
+  std::vector<std::pair<int, int>> chain(n, {-1, -1});
+  const double eps2 = P.ic_eps * P.ic_eps;
+  TouchVec w(n);
+  std::vector<std::pair<int, double>> kept;
+  auto column = [&](int c) {
+    double diag = d[c];
+    kept.clear();
+    for (size_t k = 1; k < w.idx.size(); k++) {   // every entry after the first (the diagonal)
+      const int r = w.idx[k];
+      const double v = w.val[k];
+      if (v == 0.0) continue;
+      if (v * v < fabs(eps2 * diag * d[r])) {
+        const double comp = fabs(v) * P.ic_relax;
+        diag += comp;
+        d[r] += comp;
+      } else {
+        kept.push_back({r, v});
+      }
+    }
+    const int start = P.cpcol[c];
+    P.cpcol.push_back(start + 1 + (int)kept.size());
+    std::sort(kept.begin(), kept.end(), [](const std::pair<int, double>& a, const std::pair<int, double>& b) {
+      return a.first < b.first;
+    });
+    if (!kept.empty()) {
+      const int r = kept[0].first;
+      chain[c] = chain[r];
+      chain[r] = {c, start + 1};
+    }
+    if (diag <= 0.0) diag = eps2 * diag * diag;
+    const double root = sqrt(diag);
+    P.cval.push_back(root);
+    P.crow.push_back(c);
+    const double inv = 1.0 / root;
+    for (auto& e : kept) {
+      const double l = e.second * inv;
+      P.crow.push_back(e.first);
+      P.cval.push_back(e.second * inv);
+      d[e.first] -= l * l;
+    }
+  };
+  auto load = [&](int c) {
+    w.clear();
+    lower_column(s, val, c, col);
+    for (auto& e : col) w.add(e.first, e.second);
+  };
+  load(0);
+  column(0);
+  for (int i = 1; i < n - 1; i++) {
+    load(i);
+    std::pair<int, int> link = chain[i];
+    while (link.first >= 0) {
+      const int j = link.first, at = link.second, next = at + 1;
+      const double upper = P.cval[at];
+      for (int k = next; k < P.cpcol[j + 1]; k++) w.add(P.crow[k], -upper * P.cval[k]);
+      link = chain[j];
+      if (next < P.cpcol[j + 1]) {
+        const int r = P.crow[next];
+        chain[j] = chain[r];
+        chain[r] = {j, next};
+      }
+    }
+    column(i);
+  }
+  P.cval.push_back(sqrt(d[n - 1]));
+  P.crow.push_back(n - 1);
+  P.cpcol.push_back(P.cpcol[n - 1] + 1);
+}
+
+// solvePreconditionerSystem (:132-162): L y = r by columns, L^T z = y by
+// row dots from the last row up
+void ric_apply(int n, const Precond& P, const double* r, double* z) {
+  const double sub0 = r[0] / P.cval[0];
+  z[0] = sub0;
+  for (int j = 1; j < n; j++) z[j] = r[j];
+  for (int q = 1; q < P.cpcol[1]; q++) z[P.crow[q]] -= P.cval[q] * sub0;
+  for (int c = 1; c < n; c++) {
+    const int st = P.cpcol[c], en = P.cpcol[c + 1];
+    const double sub = z[c] / P.cval[st];
+    z[c] = sub;
+    for (int q = st + 1; q < en; q++) z[P.crow[q]] -= P.cval[q] * sub;
+  }
+  z[n - 1] /= P.cval[P.cpcol[n - 1]];
+  for (int i = n - 2; i >= 0; i--) {
+    double dot = 0.0;
+    const int st = P.cpcol[i], en = P.cpcol[i + 1];
+    for (int q = st + 1; q < en; q++) dot += z[P.crow[q]] * P.cval[q];
+    z[i] = (z[i] - dot) / P.cval[st];
+  }
+}
 
 // Scalar columns of the symmetric matrix, both triangles, as
 // BlockedSymSparseMatrix::getFullIndices lists them (core/sparseMatrix.h:
@@ -1205,20 +1372,6 @@ void full_columns(const Scene& s, std::vector<std::vector<std::pair<int, int>>>&
     for (int q = s.pcol[col]; q < s.pcol[col + 1]; q++, off++) put(s.rows[q], c, off);
   }
 }
-
-// sparse vector with entries in first-touch order (the reference's
-// FastSparseVector, core/latool.h:453-520)
-struct TouchVec {
-  std::vector<int> at, idx;
-  std::vector<double> val;
-  explicit TouchVec(int n) : at(n, -1) {}
-  void add(int i, double x) {
-    if (at[i] >= 0) { val[at[i]] += x; return; }
-    at[i] = (int)idx.size(); idx.push_back(i); val.push_back(x);
-  }
-  double get(int i) const { return at[i] >= 0 ? val[at[i]] : 0.0; }
-  void clear() { for (int i : idx) at[i] = -1; idx.clear(); val.clear(); }
-};
 
 // InLDLTPreconditioner::incompleteLDLTDecomposition
 // (solver/inLDLTPreconditioner.cpp:34-149).  Z starts as the identity; step
@@ -1402,6 +1555,8 @@ void precond_setup(const Scene& s, const double* val, Precond& P) {
     P.shift = alpha;
   } else if (P.kind == 4) {
     ldlt_factor(s, val, P);
+  } else if (P.kind == 5) {
+    ric_factor(s, val, P);
   }
 }
 
@@ -1418,6 +1573,8 @@ void precond_apply(const Scene& s, const Precond& P, const double* r, double* z)
     for (int k = 0; k < s.nrem; k++) z[3 * s.nbc + k] = P.inv[9 * s.nbc + k] * r[3 * s.nbc + k];
   } else if (P.kind == 4) {
     ldlt_apply(n, P, r, z);
+  } else if (P.kind == 5) {
+    ric_apply(n, P, r, z);
   } else {
     for (int i = 0; i < n; i++) {
       double sum = r[i];
@@ -1445,6 +1602,8 @@ int pcg(const Scene& s, const double* val, const double* b, double* x, double to
   P.kind = pkind;
   P.sainv_eps = s.ldlt_sainv;
   P.ldlt_eps = s.ldlt_drop;
+  P.ic_eps = s.ic_eps;
+  P.ic_relax = s.ic_relax;
   precond_setup(s, val, P);
   precond_apply(s, P, r.data(), d.data());
   auto dotp = [n](const double* a, const double* c) { double acc = 0; for (int i = 0; i < n; i++) acc += a[i] * c[i]; return acc; };
@@ -1634,6 +1793,7 @@ struct odo_scene {
   double h = 0, alphaM = 0, betaK = 0, beta = 0.25, gamma = 0.5, tol = 1e-8;
   int maxit = 1000, pkind = 1, newton = 1;
   Precond ldlt;   // stand-alone incomplete LDL^T factor (odo_ldlt_*)
+  Precond ic;     // stand-alone threshold incomplete Cholesky factor (odo_ic_*)
   std::vector<double> D;   // external damping matrix values (empty: none)
 };
 
@@ -1745,6 +1905,29 @@ void odo_ldlt_get(odo_scene* o, double* values, int* rows, int* pcol, double* in
 }
 
 void odo_ldlt_apply(odo_scene* o, const double* rhs, double* out) { ldlt_apply(o->s.dofs, o->ldlt, rhs, out); }
+
+// threshold incomplete Cholesky (preconditioner kind 5): parameters, a
+// stand-alone factor of A = values (returns its stored entries), its
+// arrays and its apply
+void odo_set_ic(odo_scene* o, double eps, double relax) {
+  o->s.ic_eps = eps;
+  o->s.ic_relax = relax;
+}
+int odo_ic_factor(odo_scene* o, const double* values) {
+  o->ic = Precond();
+  o->ic.kind = 5;
+  o->ic.ic_eps = o->s.ic_eps;
+  o->ic.ic_relax = o->s.ic_relax;
+  ric_factor(o->s, values, o->ic);
+  return (int)o->ic.cval.size();
+}
+void odo_ic_get(odo_scene* o, double* values, int* rows, int* pcol) {
+  const Precond& P = o->ic;
+  if (!P.cval.empty()) memcpy(values, P.cval.data(), sizeof(double) * P.cval.size());
+  if (!P.crow.empty()) memcpy(rows, P.crow.data(), sizeof(int) * P.crow.size());
+  if (!P.cpcol.empty()) memcpy(pcol, P.cpcol.data(), sizeof(int) * P.cpcol.size());
+}
+void odo_ic_apply(odo_scene* o, const double* rhs, double* out) { ric_apply(o->s.dofs, o->ic, rhs, out); }
 
 // plane collision damping values (reference layout, from zero) for elements
 // elems against the plane normal.x + constant = 0, node velocities vel

@@ -135,6 +135,8 @@ struct RefScene {
   CountingPreconditioner* nm_precond = nullptr;
   // a stand-alone incomplete LDL^T factor (odref_ldlt_*)
   InLDLTPreconditioner* ldlt = nullptr;
+  // a stand-alone threshold incomplete Cholesky factor (odref_ic_*)
+  InCholeskyPreconditioner* ic = nullptr;
 };
 
 static void write_free_dofs_to_mesh(RefScene* s, const double* d) {
@@ -201,6 +203,7 @@ void odref_scene_destroy(void* p) {
   delete s->pattern;
   delete s->mass;
   delete s->ldlt;
+  delete s->ic;
   delete s;
 }
 
@@ -410,6 +413,34 @@ void odref_be_plane_damping(void* p, const double* normal, double constant, doub
     f.setCollisionPair(plane, elems[k]);
     s->be->addExternalDampingForceMatrix(f);
   }
+}
+
+// InCholeskyPreconditioner::Preprocess (inCholeskyPreconditioner.cpp:76-130)
+// on A (scene pattern, given values) with (epsilon, relaxedScale); returns
+// the number of stored L entries (diagonals included)
+int odref_ic_factor(void* p, const double* values, double eps, double relax) {
+  RefScene* s = (RefScene*)p;
+  memcpy(s->pattern->values, values, sizeof(double) * s->pattern->getNumEntries());
+  delete s->ic;
+  s->ic = new InCholeskyPreconditioner(eps, relax);
+  s->ic->resetPreconditionerSystem(*s->pattern);
+  s->ic->Preprocess(*s->pattern);
+  return (int)s->ic->values.size();
+}
+
+// the factor in the reference's storage: column c holds its diagonal first,
+// then its rows below in ascending order; pcol has dofs + 1 entries
+void odref_ic_get(void* p, double* values, int* rows, int* pcol) {
+  RefScene* s = (RefScene*)p;
+  const InCholeskyPreconditioner* f = s->ic;
+  memcpy(values, f->values.data(), sizeof(double) * f->values.size());
+  memcpy(rows, f->rows.data(), sizeof(int) * f->rows.size());
+  memcpy(pcol, f->pcol.data(), sizeof(int) * f->pcol.size());
+}
+
+void odref_ic_apply(void* p, const double* rhs, double* result) {
+  RefScene* s = (RefScene*)p;
+  s->ic->solvePreconditionerSystem(s->dofs, rhs, result);
 }
 
 // Loads: body force density (N/m^3) over all elements, then uniform

@@ -69,6 +69,10 @@ def lib():
         L.odref_ldlt_factor.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double]
         L.odref_ldlt_get.argtypes = [C.c_void_p, _dp, _ip, _ip, _dp]
         L.odref_ldlt_apply.argtypes = [C.c_void_p, _dp, _dp]
+        L.odref_ic_factor.restype = C.c_int
+        L.odref_ic_factor.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double]
+        L.odref_ic_get.argtypes = [C.c_void_p, _dp, _ip, _ip]
+        L.odref_ic_apply.argtypes = [C.c_void_p, _dp, _dp]
         L.odref_plane_damping.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_double, C.c_int, _ip, _dp]
         L.odref_be_plane_damping.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double, C.c_int, _ip]
         _lib = L
@@ -192,6 +196,25 @@ class RefScene:
         dinv = np.zeros(self.dofs)
         lib().odref_ldlt_get(self.h, _d(lv), _i(lr), _i(pc), _d(dinv))
         return lv[:nnz], lr[:nnz], pc, dinv
+
+    def ic(self, values, eps, relax):
+        """InCholeskyPreconditioner::Preprocess on A = values: returns (L
+        values, L rows, pcol) in the reference's storage (diagonal first in
+        every column)."""
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        nnz = lib().odref_ic_factor(self.h, _d(values), eps, relax)
+        lv = np.zeros(max(nnz, 1))
+        lr = np.zeros(max(nnz, 1), dtype=np.int32)
+        pc = np.zeros(self.dofs + 1, dtype=np.int32)
+        lib().odref_ic_get(self.h, _d(lv), _i(lr), _i(pc))
+        return lv[:nnz], lr[:nnz], pc
+
+    def ic_apply(self, rhs):
+        """(L L^T)^-1 rhs with the factor of the last ic() call."""
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64)
+        out = np.zeros(self.dofs)
+        lib().odref_ic_apply(self.h, _d(rhs), _d(out))
+        return out
 
     def ldlt_apply(self, rhs):
         """(L D L^T)^-1 rhs with the factor of the last ldlt() call."""

@@ -16,7 +16,7 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _lib = None
 
-PRECOND = {"none": 0, "jacobi": 1, "block_jacobi": 2, "ic0": 3, "ldlt": 4}
+PRECOND = {"none": 0, "jacobi": 1, "block_jacobi": 2, "ic0": 3, "ldlt": 4, "ic": 5}
 MATERIAL = {"corotational": 0, "neohookean": 1, "stvk": 2, "corotational_plastic": 3}
 
 
@@ -61,6 +61,11 @@ def lib():
         L.odo_ldlt_factor.argtypes = [C.c_void_p, _dp]
         L.odo_ldlt_get.argtypes = [C.c_void_p, _dp, _ip, _ip, _dp]
         L.odo_ldlt_apply.argtypes = [C.c_void_p, _dp, _dp]
+        L.odo_set_ic.argtypes = [C.c_void_p, C.c_double, C.c_double]
+        L.odo_ic_factor.restype = C.c_int
+        L.odo_ic_factor.argtypes = [C.c_void_p, _dp]
+        L.odo_ic_get.argtypes = [C.c_void_p, _dp, _ip, _ip]
+        L.odo_ic_apply.argtypes = [C.c_void_p, _dp, _dp]
         L.odo_plane_damping.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_double, C.c_int, _ip, _dp]
         L.odo_clear_damping.argtypes = [C.c_void_p]
         L.odo_integrator_plane_damping.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double, C.c_int, _ip]
@@ -186,6 +191,27 @@ class OracleScene:
         dinv = np.zeros(max(self.dofs, 1))
         lib().odo_ldlt_get(self.h, _d(lv), _i(lr), _i(pc), _d(dinv))
         return lv[:nnz], lr[:nnz], pc[: self.dofs], dinv[: self.dofs]
+
+    def set_ic(self, eps=1e-3, relax=0.0):
+        """(epsilon, relaxedScale) of the threshold incomplete Cholesky (precond "ic")."""
+        lib().odo_set_ic(self.h, float(eps), float(relax))
+
+    def ic(self, values):
+        """Threshold incomplete Cholesky of A = values: (L values, L rows,
+        pcol) in the reference's storage."""
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        nnz = lib().odo_ic_factor(self.h, _d(values))
+        lv = np.zeros(max(nnz, 1))
+        lr = np.zeros(max(nnz, 1), np.int32)
+        pc = np.zeros(self.dofs + 1, np.int32)
+        lib().odo_ic_get(self.h, _d(lv), _i(lr), _i(pc))
+        return lv[:nnz], lr[:nnz], pc
+
+    def ic_apply(self, rhs):
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64)
+        out = np.zeros(self.dofs)
+        lib().odo_ic_apply(self.h, _d(rhs), _d(out))
+        return out
 
     def ldlt_apply(self, rhs):
         rhs = np.ascontiguousarray(rhs, dtype=np.float64)

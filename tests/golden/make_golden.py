@@ -26,13 +26,17 @@ the GPU path against them.  Cases:
   values, rows, pcol, inverted diagonal) of A = K/3600 + M at two drop-bound
   pairs, its apply on a seeded vector, CG with it, and backward-Euler steps
   preconditioned by it;
+* ``ic_<material>_<constraints>``: InCholeskyPreconditioner (threshold IC
+  with fill): the factor (values, rows, pcol) of A = K/3600 + M at two
+  (epsilon, relaxedScale) pairs, its apply, CG with it, and backward-Euler
+  steps preconditioned by it;
 * ``damping``: MeshPlaneCollisionDampingForcer: damping values against two
   planes (a tilted one cutting elements with 0-3 vertices below it, a
   horizontal one with whole elements below it), with a repeated element,
   and backward-Euler steps with the forcer re-applied every step.
 
-``--only NAME`` writes one group (plastic, ldlt or damping; the full run
-writes all).
+``--only NAME`` writes one group (plastic, ldlt, ic or damping; the full
+run writes all).
 """
 from __future__ import annotations
 
@@ -138,6 +142,43 @@ def ldlt_cases():
                  be_params=np.array([1.0 / 60.0, 0.01, 0.001, 1e-10]), **out)
 
 
+IC_EPS = ((1e-3, 0.0), (1e-2, 0.5))              # (epsilon, relaxedScale) pairs
+
+
+def ic_cases():
+    g = small_mesh()
+    cases = {"full": meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0)),
+             "partial": partial_constraints(g)}
+    rng = np.random.default_rng(654)
+    u = rng.normal(scale=0.002, size=(g.n_nodes, 3))
+    for mat in ("corotational", "neohookean"):
+        rho, E, nu, thr = MATS[mat]
+        for cname, cd in cases.items():
+            s = R.RefScene(g.X, g.tets, g.facets, cd, mat, rho, E, nu, thr)
+            s.set_displacements(u)
+            vals, _ = s.assemble()
+            A = vals * (1.0 / 3600.0) + s.mass()
+            out = {}
+            for k, (eps, relax) in enumerate(IC_EPS):
+                lv, lr, pc = s.ic(A, eps, relax)
+                r = rng.normal(size=s.dofs)
+                out.update({f"l_values_{k}": lv, f"l_rows_{k}": lr, f"l_pcol_{k}": pc,
+                            f"apply_r_{k}": r, f"apply_z_{k}": s.ic_apply(r)})
+                b = rng.normal(size=s.dofs)
+                x, its = s.cg(A, b, tol=1e-10, maxit=2000, precond="ic", eps=eps, relax=relax)
+                out.update({f"cg_b_{k}": b, f"cg_x_{k}": x, f"cg_iters_{k}": its})
+            eps, relax = IC_EPS[0]
+            s = R.RefScene(g.X, g.tets, g.facets, cd, mat, rho, E, nu, thr)
+            s.be_setup(1.0 / 60.0, 0.01, 0.001, tol=1e-10, maxit=2000, precond="ic", eps=eps, relax=relax)
+            fext = s.loads(body=[0.0, 0.0, -9800.0])
+            s.be_apply_loads()
+            iters = s.be_step(10)
+            save(f"ic_{mat}_{cname}", X=g.X, tets=g.tets, facets=g.facets, cdofs=cd, u=u, A=A,
+                 eps=np.array(IC_EPS), material=np.array([rho, E, nu, thr]), be_fext=fext,
+                 be_u=s.displacements(), be_v=s.be_velocity(), be_steps=10, be_iters=iters,
+                 be_params=np.array([1.0 / 60.0, 0.01, 0.001, 1e-10]), **out)
+
+
 DAMP_PLANES = ((0.1, 0.2, 1.0, -0.05), (0.0, 0.0, 1.0, -0.07))   # normal (normalised), constant
 DAMP_COEFF = 50.0
 DAMP_BE = (2000.0, 15)          # coefficient, steps (plane z = 0, all elements, 20 g)
@@ -176,6 +217,10 @@ def damping_case():
 
 def main():
     only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    if only == "ic":
+        ic_cases()
+        print("golden fixtures ic_* written to", OUT)
+        return
     if only == "damping":
         damping_case()
         print("golden fixture damping written to", OUT)
@@ -189,7 +234,7 @@ def main():
         print("golden fixtures ldlt_* written to", OUT)
         return
     if only is not None:
-        raise SystemExit(f"--only {only}: single groups are 'plastic', 'ldlt' and 'damping'")
+        raise SystemExit(f"--only {only}: single groups are 'plastic', 'ldlt', 'ic' and 'damping'")
     g = small_mesh()
     cases = {"full": meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0)),
              "partial": partial_constraints(g)}
@@ -266,6 +311,7 @@ def main():
          eig_vecs=evec)
     plastic_case()
     ldlt_cases()
+    ic_cases()
     damping_case()
     print("golden fixtures written to", OUT)
 
