@@ -929,11 +929,12 @@ __device__ __forceinline__ void named_sync() {
 
 // Shared state of one CTA of the ring kernel for the scenes it spans.
 struct RingShared {
-  double ws[2][kMaxLocalScenes][kRingWarps];  // per-warp partials
-  double res[2][kMaxLocalScenes];             // scene sums of the last reduction
+  double ws[3][kMaxLocalScenes][kRingWarps];  // per-warp partials
+  double res[3][kMaxLocalScenes];             // scene sums of the last reduction
   double wg[kRingWarps];
   double g;                                   // grid-wide sum of the last reduction
   double rz[kMaxLocalScenes], rr[kMaxLocalScenes], eps[kMaxLocalScenes];
+  double alpha[kMaxLocalScenes], beta[kMaxLocalScenes];   // step lengths of the current iteration
   double scale[kMaxLocalScenes];
   int it[kMaxLocalScenes], status[kMaxLocalScenes], maxit[kMaxLocalScenes];
   MixDesc lp[kMaxLocalScenes];                // the local scenes' arrays
@@ -1158,10 +1159,16 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
   }
 
   // ---------------- consumers
-  double* part_1 = part;                                    // [1][n_sc][G]
-  double* part_2 = part + (size_t)n_sc * G;                 // [2][n_sc][G]
-  double* part_g1 = part + (size_t)3 * n_sc * G;
-  double* part_g2 = part_g1 + G;
+  // Chronopoulos-Gear PCG: one grid-wide sum per iteration.  Roles of the
+  // FP32 vectors: u = M^-1 r is the one the SpMV gathers (float4 layout),
+  // w = A u, p and s = A p are the directions, d the solution.  Iteration k:
+  //   w = A u, (w, u)  -> one sum with the (r, u), (r, r) of the last update
+  //   k = 0: alpha = (r,u) / (w,u), beta = 0
+  //   k > 0: beta = (r,u) / (r,u)_prev, alpha = (r,u) / ((w,u) - beta (r,u) / alpha_prev)
+  //   p = u + beta p, s = w + beta s, d += alpha p, r -= alpha s, u = M^-1 r,
+  //   partial (r, u), (r, r); grid barrier (u complete for the next gathers)
+  double* part_3 = part;                                    // [3][n_sc][G]
+  double* part_g = part + (size_t)3 * n_sc * G;             // [G]
   const bool act_l = lane < 30;
   const int ln = act_l ? lane : 29;
   const int t = ln / 3, rsub = ln - 3 * t, lbase = 3 * t;
@@ -1184,34 +1191,35 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
   };
   // the scene's vectors, indexed by the scene-local slice
   struct Vecs {
-    float4* p4;
-    float *pf, *d, *r, *z, *q, *pinv;
+    float4* u4;
+    float *uf, *d, *r, *p, *w, *pinv, *s;
     int s0;
   };
   auto vecs = [&](int ls) {
     const MixDesc& P = sh.lp[ls];
     Vecs v;
     const size_t ns = (size_t)P.ns;
-    v.p4 = reinterpret_cast<float4*>(P.v32);
-    v.pf = P.v32;
+    v.u4 = reinterpret_cast<float4*>(P.v32);
+    v.uf = P.v32;
     v.d = P.v32 + 40 * ns;
     v.r = v.d + 30 * ns;
-    v.z = v.r + 30 * ns;
-    v.q = v.z + 30 * ns;
-    v.pinv = v.q + 30 * ns;
+    v.p = v.r + 30 * ns;
+    v.w = v.p + 30 * ns;
+    v.pinv = v.w + 30 * ns;
+    v.s = v.pinv + 90 * ns;
     v.s0 = P.slice0;
     return v;
   };
 
-  // init: d = 0, r = rhs, z = M^-1 r, p = z (scenes outside the sweep: zeros)
-  zero_ws(2);
+  // init: d = p = s = 0, r = rhs, u = M^-1 r; partials (r, u), (r, r)
+  zero_ws(3);
   for (int ls = 0; ls < L; ls++) {
     const bool a0 = sh.act[0][ls] != 0;
     const double scale = sh.scale[ls];
     const Vecs V = vecs(ls);
     const int* __restrict__ perm = sh.lp[ls].sperm;
     const double* __restrict__ r64 = sh.lp[ls].r64;
-    Comp crz{0.f, 0.f}, crr{0.f, 0.f};
+    Comp cru{0.f, 0.f}, crr{0.f, 0.f};
     for (int sl = first_slice(ls); sl < sh.lfirst[ls + 1]; sl += kRingWarps) {
       const int lsl = sl - V.s0;
       const int rs = lsl * kSliceRows + t;
@@ -1220,56 +1228,50 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
       const float r0 = __shfl_sync(0xffffffffu, rl, lbase);
       const float r1 = __shfl_sync(0xffffffffu, rl, lbase + 1);
       const float r2 = __shfl_sync(0xffffffffu, rl, lbase + 2);
-      float zl = rl;
-      if (pkind == OD_PRECOND_JACOBI) zl = V.pinv[(size_t)30 * lsl + ln] * rl;
+      float ul = rl;
+      if (pkind == OD_PRECOND_JACOBI) ul = V.pinv[(size_t)30 * lsl + ln] * rl;
       else if (pkind == OD_PRECOND_BLOCK_JACOBI) {
         const float* m = V.pinv + (size_t)90 * lsl + ln;
-        zl = fmaf(m[0], r0, fmaf(m[30], r1, m[60] * r2));
+        ul = fmaf(m[0], r0, fmaf(m[30], r1, m[60] * r2));
       }
       if (act_l) {
         const size_t i = (size_t)30 * lsl + lane;
         V.r[i] = rl;
         V.d[i] = 0.f;
-        V.z[i] = zl;
-        V.pf[4 * (size_t)rs + rsub] = zl;
-        comp_add_prod(crz, rl, zl);
+        V.p[i] = 0.f;
+        V.s[i] = 0.f;
+        V.uf[4 * (size_t)rs + rsub] = ul;
+        comp_add_prod(cru, rl, ul);
         comp_add_prod(crr, rl, rl);
       }
     }
-    flush(0, ls, crz);
-    flush(1, ls, crr);
+    flush(1, ls, cru);
+    flush(2, ls, crr);
   }
-  alive = ring_sums<2>(sh, L, sc_lo, n_sc, 0.0, part_2, part_g2, gb);
   if (w == 0 && lane < L) {
-    const double rz = sh.res[0][lane], rr = sh.res[1][lane];
-    const bool a0 = sh.act[0][lane] != 0;
-    sh.rz[lane] = rz;
-    sh.rr[lane] = rr;
-    sh.eps[lane] = rr * sh.eps[lane];
     sh.it[lane] = 0;
-    sh.status[lane] = isfinite(rr) ? OD_OK : OD_ERR_NAN;
-    sh.act[0][lane] = (unsigned char)(a0 && isfinite(rr) && rr > sh.eps[lane] && sh.maxit[lane] > 0);
+    sh.status[lane] = OD_OK;
   }
   __threadfence_block();
-  if (threadIdx.x == 0) sh.pub = 0;
-  named_sync<kRingConsumers>();
+  if (threadIdx.x == 0) sh.pub = 0;   // act[0] (= the launch's activity) is final
+  // u complete everywhere before the first gathers
+  if (!grid_barrier_named<kRingConsumers>(gb)) alive = false;
 
-  // profiling (prof != nullptr): CTA 0 times each SpMV + p.q phase up to the
+  // profiling (prof != nullptr): CTA 0 times each SpMV + sum phase up to the
   // end of its grid-wide sum, i.e. including the slowest CTA
   const bool timer = prof && blockIdx.x == 0 && threadIdx.x == 0;
   for (int k = 0; alive; k++) {
     const int kp = k & 1;
     unsigned long long t_a = 0;
     if (timer) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_a));
-    // ---- q = A p (pieces from the ring), p.q
+    // ---- w = A u (pieces from the ring), (w, u)
     {
-      zero_ws(1);
       for (int ls = 0; ls < L && alive; ls++) {
         if (!(k == 0 ? sh.act_in[ls] : sh.act[kp ^ 1][ls])) continue;  // no pieces this iteration
         const bool on = sh.act[kp][ls] != 0;
         const Vecs V = vecs(ls);
         const int* __restrict__ soff = sh.lp[ls].soff;
-        Comp cpq{0.f, 0.f};
+        Comp cwu{0.f, 0.f};
         for (int sl = first_slice(ls); sl < sh.lfirst[ls + 1] && alive; sl += kRingWarps) {
           const int lsl = sl - V.s0;
           const int k1 = soff[lsl + 1];
@@ -1293,7 +1295,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
 #pragma unroll
               for (int u = 0; u < kPer; u++) {
                 const int st = rsub + 3 * u;
-                x[u] = st < n ? V.p4[scol[st * kSliceRows + t]] : make_float4(0.f, 0.f, 0.f, 0.f);
+                x[u] = st < n ? V.u4[scol[st * kSliceRows + t]] : make_float4(0.f, 0.f, 0.f, 0.f);
               }
 #pragma unroll
               for (int u = 0; u < kPer; u++) {
@@ -1327,18 +1329,18 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
             const float nb = rsub == 0 ? b0 : (rsub == 1 ? b1 : b2);
             const float y = (own + na) + nb;
             if (act_l) {
-              V.q[(size_t)30 * lsl + lane] = y;
-              comp_add_prod(cpq, V.pf[4 * (size_t)(lsl * kSliceRows + t) + rsub], y);
+              V.w[(size_t)30 * lsl + lane] = y;
+              comp_add_prod(cwu, V.uf[4 * (size_t)(lsl * kSliceRows + t) + rsub], y);
             }
           }
         }
-        if (on) flush(0, ls, cpq);
+        if (on) flush(0, ls, cwu);
       }
       // active scenes of this CTA at iteration k (grid-wide sum: 0 ends the loop)
       double na = 0.0;
       if (w == 0 && lane == 0)
         for (int ls = 0; ls < L; ls++) na += sh.act[kp][ls] ? 1.0 : 0.0;
-      if (!ring_sums<1>(sh, L, sc_lo, n_sc, na, part_1, part_g1, gb, prof ? prof + 3 : nullptr)) alive = false;
+      if (!ring_sums<3>(sh, L, sc_lo, n_sc, na, part_3, part_g, gb, prof ? prof + 3 : nullptr)) alive = false;
     }
     if (!alive || sh.g == 0.0) break;
     if (timer) {
@@ -1348,18 +1350,48 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
       prof[1] += 1;
       prof[2] += sh.tmax - t_a;  // up to the last CTA's end of the SpMV work
     }
-    // ---- d += alpha p, r -= alpha q, z = M^-1 r, r.z, r.r: kUB slices per
-    // batch, all loads of a batch issued before any use
-    zero_ws(2);
+    // step lengths and the activity of iteration k + 1 (which also gates
+    // this iteration's update)
+    if (w == 0 && lane < L) {
+      const int ls = lane;
+      unsigned char na = 0;
+      if (sh.act[kp][ls]) {
+        const double wu = sh.res[0][ls], ru = sh.res[1][ls], rr = sh.res[2][ls];
+        double alpha, beta;
+        if (k == 0) {
+          sh.eps[ls] = rr * sh.eps[ls];   // relative to the initial residual
+          beta = 0.0;
+          alpha = ru / wu;
+        } else {
+          beta = ru / sh.rz[ls];
+          alpha = ru / (wu - beta * ru / sh.alpha[ls]);
+        }
+        sh.rz[ls] = ru;
+        sh.rr[ls] = rr;
+        sh.alpha[ls] = alpha;
+        sh.beta[ls] = beta;
+        if (!isfinite(rr) || !isfinite(alpha) || !isfinite(beta)) sh.status[ls] = OD_ERR_NAN;
+        na = (unsigned char)(sh.status[ls] == OD_OK && rr > sh.eps[ls] && sh.it[ls] < sh.maxit[ls]);
+        if (na) sh.it[ls]++;
+      }
+      sh.act[kp ^ 1][ls] = na;
+    }
+    __threadfence_block();
+    named_sync<kRingConsumers>();
+    if (threadIdx.x == 0) sh.pub = k + 1;
+    // ---- p = u + beta p, s = w + beta s, d += alpha p, r -= alpha s,
+    // u = M^-1 r, (r, u), (r, r): kUB slices per batch, all loads of a batch
+    // issued before any use
+    zero_ws(3);
     for (int ls = 0; ls < L; ls++) {
-      if (!sh.act[kp][ls]) continue;  // warp-uniform; the partials stay zero
+      if (!sh.act[kp ^ 1][ls]) continue;  // warp-uniform; the partials stay zero
       constexpr int kUB = 4;
       const int hi = sh.lfirst[ls + 1];
       const Vecs V = vecs(ls);
-      const float alpha = (float)(sh.rz[ls] / sh.res[0][ls]);
-      Comp cz{0.f, 0.f}, cr{0.f, 0.f};
+      const float alpha = (float)sh.alpha[ls], beta = (float)sh.beta[ls];
+      Comp cru{0.f, 0.f}, crr{0.f, 0.f};
       for (int sl0 = first_slice(ls); sl0 < hi; sl0 += kUB * kRingWarps) {
-        float dv[kUB], pv[kUB], qv[kUB], rv[kUB], m0[kUB], m1[kUB], m2[kUB];
+        float dv[kUB], pv[kUB], sv[kUB], uv[kUB], wv[kUB], rv[kUB], m0[kUB], m1[kUB], m2[kUB];
 #pragma unroll
         for (int u = 0; u < kUB; u++) {
           const int sl = sl0 + u * kRingWarps;
@@ -1367,8 +1399,10 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
             const int lsl = sl - V.s0;
             const size_t i = (size_t)30 * lsl + ln;
             dv[u] = V.d[i];
-            pv[u] = V.pf[4 * (size_t)(lsl * kSliceRows + t) + rsub];
-            qv[u] = V.q[i];
+            pv[u] = V.p[i];
+            sv[u] = V.s[i];
+            uv[u] = V.uf[4 * (size_t)(lsl * kSliceRows + t) + rsub];
+            wv[u] = V.w[i];
             rv[u] = V.r[i];
             if (pkind == OD_PRECOND_BLOCK_JACOBI) {
               const float* m = V.pinv + (size_t)90 * lsl + ln;
@@ -1384,74 +1418,34 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
         for (int u = 0; u < kUB; u++) {
           const int sl = sl0 + u * kRingWarps;
           if (sl < hi) {  // warp-uniform
-            const size_t i = (size_t)30 * (sl - V.s0) + ln;
-            const float rl = act_l ? fmaf(-alpha, qv[u], rv[u]) : 0.f;
+            const int lsl = sl - V.s0;
+            const size_t i = (size_t)30 * lsl + ln;
+            const float pn = fmaf(beta, pv[u], uv[u]);
+            const float sn = fmaf(beta, sv[u], wv[u]);
+            const float rl = act_l ? fmaf(-alpha, sn, rv[u]) : 0.f;
             const float r0 = __shfl_sync(0xffffffffu, rl, lbase);
             const float r1 = __shfl_sync(0xffffffffu, rl, lbase + 1);
             const float r2 = __shfl_sync(0xffffffffu, rl, lbase + 2);
-            float zl = rl;
-            if (pkind == OD_PRECOND_BLOCK_JACOBI) zl = fmaf(m0[u], r0, fmaf(m1[u], r1, m2[u] * r2));
-            else if (pkind == OD_PRECOND_JACOBI) zl = m0[u] * rl;
+            float ul = rl;
+            if (pkind == OD_PRECOND_BLOCK_JACOBI) ul = fmaf(m0[u], r0, fmaf(m1[u], r1, m2[u] * r2));
+            else if (pkind == OD_PRECOND_JACOBI) ul = m0[u] * rl;
             if (act_l) {
-              V.d[i] = fmaf(alpha, pv[u], dv[u]);
+              V.p[i] = pn;
+              V.s[i] = sn;
+              V.d[i] = fmaf(alpha, pn, dv[u]);
               V.r[i] = rl;
-              V.z[i] = zl;
-              comp_add_prod(cz, rl, zl);
-              comp_add_prod(cr, rl, rl);
+              V.uf[4 * (size_t)(lsl * kSliceRows + t) + rsub] = ul;
+              comp_add_prod(cru, rl, ul);
+              comp_add_prod(crr, rl, rl);
             }
           }
         }
       }
-      flush(0, ls, cz);
-      flush(1, ls, cr);
+      flush(1, ls, cru);
+      flush(2, ls, crr);
     }
-    // sh.res[0] (p.q) is read above by every warp; ring_sums rewrites sh.res
-    // only after its first named barrier
-    if (!ring_sums<2>(sh, L, sc_lo, n_sc, 0.0, part_2, part_g2, gb)) { alive = false; break; }
-    if (w == 0 && lane < L) {
-      const int ls = lane;
-      unsigned char na = 0;
-      if (sh.act[kp][ls]) {
-        const double rz = sh.res[0][ls], rr = sh.res[1][ls];
-        const double beta = rz / sh.rz[ls];
-        sh.res[0][ls] = beta;  // beta for the direction update
-        sh.rz[ls] = rz;
-        sh.rr[ls] = rr;
-        sh.it[ls]++;
-        if (!isfinite(rr) || !isfinite(beta)) sh.status[ls] = OD_ERR_NAN;
-        na = (unsigned char)(sh.status[ls] == OD_OK && rr > sh.eps[ls] && sh.it[ls] < sh.maxit[ls]);
-      }
-      sh.act[kp ^ 1][ls] = na;
-    }
-    __threadfence_block();
-    named_sync<kRingConsumers>();
-    if (threadIdx.x == 0) sh.pub = k + 1;
-    // ---- p = z + beta p for the scenes active in this iteration
-    for (int ls = 0; ls < L; ls++) {
-      if (!sh.act[kp][ls]) continue;
-      constexpr int kUD = 8;
-      const int hi = sh.lfirst[ls + 1];
-      const Vecs V = vecs(ls);
-      const float bf = (float)sh.res[0][ls];
-      for (int sl0 = first_slice(ls); sl0 < hi; sl0 += kUD * kRingWarps) {
-        float zv[kUD], pv[kUD];
-#pragma unroll
-        for (int u = 0; u < kUD; u++) {
-          const int sl = sl0 + u * kRingWarps;
-          if (sl < hi) {
-            const int lsl = sl - V.s0;
-            zv[u] = V.z[(size_t)30 * lsl + ln];
-            pv[u] = V.pf[4 * (size_t)(lsl * kSliceRows + t) + rsub];
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < kUD; u++) {
-          const int sl = sl0 + u * kRingWarps;
-          if (sl < hi && act_l)
-            V.pf[4 * (size_t)((sl - V.s0) * kSliceRows + t) + rsub] = fmaf(bf, pv[u], zv[u]);
-        }
-      }
-    }
+    // u complete everywhere before the next gathers (also keeps this
+    // iteration's sums from being overwritten before every CTA read them)
     if (!grid_barrier_named<kRingConsumers>(gb)) { alive = false; break; }
   }
   named_sync<kRingConsumers>();
@@ -1863,7 +1857,7 @@ od_status slice_build(Scene* s) {
   if ((st = dev_upload(&sl->src, hs.src.data(), hs.src.size(), sl->device_bytes)) != OD_OK) return fail(st);
   const size_t ns = (size_t)std::max(1, sl->ns);
   const size_t nval = (size_t)std::max<long long>(1, sl->steps) * 90;
-  const size_t nvec = (40 + 4 * 30 + 90) * ns;
+  const size_t nvec = (40 + 4 * 30 + 90 + 30) * ns;   // u (float4 rows), d, r, p, w, preconditioner, s
   cudaError_t e = cudaMalloc(&sl->val, sizeof(float) * nval);
   if (e == cudaSuccess) e = cudaMalloc(&sl->v32, sizeof(float) * nvec);
   if (e == cudaSuccess) e = cudaMemset(sl->v32, 0, sizeof(float) * nvec);
