@@ -24,7 +24,9 @@ roofline of the FP32 SpMV phase measured inside the solve), and
 together through od_batch with the mixed solver; "serving_tier", Poisson step
 requests over a pool of scenes; "sweep_tier", the headline step preconditioned
 by the reference's incomplete LDL^T and by its threshold incomplete Cholesky,
-beside the reference's CPU code for each.
+beside the reference's CPU code for each; "relabel_tier", the step and the
+triangular sweeps on the generator's node order, a shuffled order and the
+shuffle relabeled by od_mesh_relabel.
 """
 from __future__ import annotations
 
@@ -395,6 +397,59 @@ def sweep_tier(args, api, ctx):
     return result
 
 
+def relabel_tier(args, api, ctx):
+    """Node order on the headline beam step: the generator's order, a seeded
+    random shuffle of the node ids, and the shuffle relabeled by
+    od_mesh_relabel (MeshRelabeler's Gibbs-Poole-Stockmeyer pass).  Per
+    order: element colours, the FP64 block-Jacobi step (device ms), and the
+    dependency depth and device time of one apply of the reference's IC
+    factor (0.01, 0) of the step's system -- bandwidth-reducing orders help
+    the SpMV but lengthen the triangular sweeps' chains."""
+    wl = WORKLOADS["beam98k_nh_newmark"]
+    g = wl["mesh"]()
+    kind, rho, E, nu, thr = wl["material"]
+    mat = api.Material(kind, rho, E, nu, thr)
+    perm = np.random.default_rng(1).permutation(g.n_nodes)
+    Xs = np.empty_like(g.X)
+    Xs[perm] = g.X
+    ts = perm[g.tets].astype(np.int32)
+    fs = perm[g.facets].astype(np.int32)
+    cds = meshgen.constrained_dofs_for_nodes(perm[g.face_nodes(0, 0)])
+    load = np.where(np.isin(fs, perm[g.face_nodes(0, 1)]).all(axis=1))[0]
+    t0 = time.perf_counter()
+    Xr, tr, fr, cdr, _ = api.relabel_mesh(Xs, ts, fs, cds)
+    relabel_s = time.perf_counter() - t0
+    cases = {"generator": (g.X, g.tets, g.facets, meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0)),
+                           g.face_facets(0, 1)),
+             "shuffled": (Xs, ts, fs, cds, load), "relabeled": (Xr, tr, fr, cdr, load)}
+    out = {"workload": "beam98k_nh_newmark", "relabel_host_s": relabel_s}
+    for name, (X, T, F, C, L) in cases.items():
+        s = api.Scene(ctx, X, T, F, C, mat)
+        s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, wl["alpha_m"], wl["beta_k"], wl["dt"],
+                                                 api.CGSolver(wl["tol"], 5000, api.BlockJacobiPreconditioner()),
+                                                 wl["newton"]))
+        s.set_loads(tractions=[([0.0, -wl["traction"], 0.0], L)])
+        s.set_traction_schedule(wl["freq"])
+        for _ in range(3):
+            s.step(1)
+        ms = [s.step(1).device_ms for _ in range(max(5, args.tier_steps))]
+        vals, _ = s.evaluate()
+        h = wl["dt"]
+        A = (1 + h * wl["alpha_m"]) * s.mass() + (h * h + h * wl["beta_k"]) * vals
+        s.ic_factor(A, 1e-2, 0.0)
+        levels = ctx.counters().sweep_levels
+        r = np.random.default_rng(2).normal(size=s.dofs)
+        ctx.set_profiling(True)
+        ctx.reset_counters()
+        s.ic_apply(r)
+        apply_ms = ctx.counters().sweep_apply_ms
+        ctx.set_profiling(False)
+        out[name] = {"colours": s.info.num_colors, "fp64_step_ms": statistics.median(ms),
+                     "ic_sweep_levels": levels, "ic_apply_ms": apply_ms}
+        s.close()
+    return out
+
+
 def batched_tier(args, api, ctx):
     """Batched uneven instances: 512 jittered grids (per-axis cube counts
     log-uniform in [4, 40], 6 tets per cube), corotational / Neo-Hookean
@@ -686,7 +741,8 @@ def run_gpu(args, wl):
         del scene
         only = [t for t in args.only_tiers.split(",") if t]
         for name, fn in (("precision_tier", precision_tier), ("batched_tier", batched_tier),
-                         ("serving_tier", serving_tier), ("sweep_tier", sweep_tier)):
+                         ("serving_tier", serving_tier), ("sweep_tier", sweep_tier),
+                         ("relabel_tier", relabel_tier)):
             if only and name.split("_")[0] not in only:
                 continue
             try:
@@ -728,7 +784,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tiers", action="store_true", help="skip the mixed-precision and batched workloads")
     ap.add_argument("--tier-steps", type=int, default=5)
-    ap.add_argument("--only-tiers", default="", help="comma list of precision,batched,serving,sweep (default: all)")
+    ap.add_argument("--only-tiers", default="", help="comma list of precision,batched,serving,sweep,relabel (default: all)")
     ap.add_argument("--precision-nz", type=int, default=64,
                     help="cube layers of the precision-tier block (64: 2,621,440 tets)")
     ap.add_argument("--serving-pool", type=int, default=512)

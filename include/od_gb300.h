@@ -17,6 +17,7 @@
  *   InCholeskyPreconditioner               solver/inCholeskyPreconditioner.h
  *   Forcer                                 core/forcer.h:13-22
  *   MeshPlaneCollisionDampingForcer        collision/penaltyDampingForcer.h:25-35
+ *   MeshRelabeler                          core/meshRelabeler.h:103-135
  *   Intergrator / NonlinearImplicitBackwardEuler
  *                                          core/intergrator.h:13-35,
  *                                          intergrator/nonlinearImplicitBackwardEuler.h:48-128
@@ -365,6 +366,17 @@ od_status od_batch_destroy(od_batch* batch);
 od_status od_bsr_pcg_noalloc(int nb, const int* d_row_ptr, const int* d_col, const double* d_values,
                              const double* d_b, double* d_x, const od_solver_params* params,
                              void* stream, od_solve_stats* stats);
+
+/* MeshRelabeler::getNewLables (core/meshRelabler.cpp:192-505) on the host,
+ * before a scene is created: Gibbs-Poole-Stockmeyer relabeling of the nodes of
+ * n_elems elements of nodes_per_elem nodes (elems[n_elems * nodes_per_elem]).
+ * new_labels[old node] receives the new label; elems is rewritten with the new
+ * labels and reordered by the sum of each element's labels.  Ties go to the
+ * lower node index (deterministic; the reference's follow its standard
+ * library's hash and heap orders); every connected component is labelled
+ * (the reference labels the first only); nodes in no element go last.
+ * Node arrays (positions, constraints, facets) are the caller's to permute. */
+od_status od_mesh_relabel(int n_nodes, int n_elems, int nodes_per_elem, int* elems, int* new_labels);
 
 /* Checkpoint / resume: mesh displacement + integrator vectors as a host blob.
  * Call with buf == NULL to query the size. */

@@ -182,6 +182,7 @@ SIGNATURES = {
     "od_batch_destroy": (C.c_int, [_vp]),
     "od_bsr_pcg_noalloc": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, C.POINTER(od_solver_params), _vp,
                                      C.POINTER(od_solve_stats)]),
+    "od_mesh_relabel": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip]),
     "od_scene_save": (C.c_int, [_vp, _vp, C.POINTER(C.c_size_t)]),
     "od_scene_load": (C.c_int, [_vp, _vp, C.c_size_t]),
 }
@@ -328,6 +329,29 @@ class NewmarkIntegrator:
     def to_c(self):
         return od_integrator_params(1, self.ts, self.massDamp, self.stiffDamp, self.beta, self.gamma,
                                     self.newton_iters, self.solver.to_c())
+
+
+def mesh_relabel(n_nodes, elements):
+    """MeshRelabeler::getNewLables (core/meshRelabler.cpp): Gibbs-Poole-
+    Stockmeyer node relabeling.  Returns (new label of every node, elements
+    rewritten with the new labels, reordered by the sum of their labels)."""
+    e = np.ascontiguousarray(elements, dtype=np.int32).copy()
+    labels = np.zeros(int(n_nodes), dtype=np.int32)
+    _check(load_library().od_mesh_relabel(int(n_nodes), e.shape[0], e.shape[1], _i(e), _i(labels)), "mesh_relabel")
+    return labels, e
+
+
+def relabel_mesh(X, tets, facets, constrained_dofs):
+    """A whole mesh under mesh_relabel: positions, elements, facets and the
+    constrained DOFs in the new node order (plus the labels)."""
+    X = np.asarray(X, dtype=np.float64).reshape(-1, 3)
+    labels, t2 = mesh_relabel(X.shape[0], tets)
+    X2 = np.empty_like(X)
+    X2[labels] = X
+    f2 = labels[np.asarray(facets, dtype=np.int64)].astype(np.int32)
+    cd = np.asarray(constrained_dofs, dtype=np.int64)
+    cd2 = np.sort(3 * labels[cd // 3] + cd % 3).astype(np.int32)
+    return X2, t2, f2, cd2, labels
 
 
 # ----------------------------------------------------------------- handles

@@ -37,6 +37,8 @@ Fixes applied (each is a compile error under g++ 13 otherwise):
    ``collision/penaltyDampingForcer.cpp``: drop
    MeshMeshCollisionDampingForcer::addDampingMatrix, its only caller (it
    computes an intersection and adds nothing to the matrix).
+9. ``core/allocator.h``: add ``template`` before the dependent member-template
+   calls ``alloc->Alloc<value_type>`` / ``alloc->Dealloc<value_type>``.
 
 No ``-ffast-math``: the oracle is defined as this IEEE-strict g++ build.
 """
@@ -59,7 +61,8 @@ FILES = {
              "constrainer.h", "constrainer.cpp", "forcer.h", "forcer.cpp",
              "mechMaterial.h", "mechMaterial.cpp", "intergrator.h",
              "linearSolver.h", "preconditioner.h", "simulator.h",
-             "simulator.cpp", "stdafx.h", "datastructure.h"],
+             "simulator.cpp", "stdafx.h", "datastructure.h", "allocator.h", "meshRelabeler.h",
+             "meshRelabler.cpp"],
     "element": ["tetelement.h", "tetelement.cpp"],
     "mesh": ["tetmesh.h", "tetmesh.cpp"],
     "material": ["fullOrderNonlinear.h", "corotationalHyperelastic.h",
@@ -147,7 +150,12 @@ def _patch(root: str) -> None:
         cut = t.index("\t\tvoid MeshMeshCollisionDampingForcer::addDampingMatrix")
         return t[:cut] + "\t}\n}\n"
 
+    def allocator(t, p):
+        t = _replace(t, "alloc->Alloc<value_type>(n)", "alloc->template Alloc<value_type>(n)", p)
+        return _replace(t, "alloc->Dealloc<value_type>(p, n)", "alloc->template Dealloc<value_type>(p, n)", p)
+
     rw("core/oder.h", oder)
+    rw("core/allocator.h", allocator)
     rw("collision/intersection.cpp", intersection)
     rw("collision/penaltyDampingForcer.cpp", damping)
     rw("core/memory.h", memory)

@@ -61,6 +61,7 @@
 #include "inCholeskyPreconditioner.h"
 #include "inLDLTPreconditioner.h"
 #include "penaltyDampingForcer.h"
+#include "meshRelabeler.h"
 #include "intergrator.h"
 #include "nonlinearImplicitBackwardEuler.h"
 #undef private
@@ -441,6 +442,14 @@ void odref_ic_get(void* p, double* values, int* rows, int* pcol) {
 void odref_ic_apply(void* p, const double* rhs, double* result) {
   RefScene* s = (RefScene*)p;
   s->ic->solvePreconditionerSystem(s->dofs, rhs, result);
+}
+
+// MeshRelabeler::getNewLables(elementCount, nodePerElementCount,
+// newNodeLables, elements) (core/meshRelabler.cpp:482-505): labels[old] =
+// new node label; elems rewritten with the new labels and reordered
+void odref_relabel(int n_nodes, int n_elems, int per, int* elems, int* labels) {
+  MeshRelabeler r(n_nodes);
+  r.getNewLables(n_elems, per, labels, elems);
 }
 
 // Loads: body force density (N/m^3) over all elements, then uniform

@@ -73,6 +73,7 @@ def lib():
         L.odref_ic_factor.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double]
         L.odref_ic_get.argtypes = [C.c_void_p, _dp, _ip, _ip]
         L.odref_ic_apply.argtypes = [C.c_void_p, _dp, _dp]
+        L.odref_relabel.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip]
         L.odref_plane_damping.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_double, C.c_int, _ip, _dp]
         L.odref_be_plane_damping.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double, C.c_int, _ip]
         _lib = L
@@ -284,6 +285,15 @@ class RefScene:
         d, v, a = np.zeros(self.dofs), np.zeros(self.dofs), np.zeros(self.dofs)
         lib().odref_nm_state(self.h, _d(d), _d(v), _d(a))
         return d, v, a
+
+
+def relabel(n_nodes, elems):
+    """MeshRelabeler::getNewLables: (new label of every node, elements with
+    the new labels in the reference's new order)."""
+    e = np.ascontiguousarray(elems, dtype=np.int32).copy()
+    labels = np.zeros(n_nodes, dtype=np.int32)
+    lib().odref_relabel(int(n_nodes), e.shape[0], e.shape[1], _i(e), _i(labels))
+    return labels, e
 
 
 def polar(F):
