@@ -226,6 +226,14 @@ struct MixedSys {
   double* part = nullptr;          // [3][n_sc][G] per-scene CTA partials + 2 G
   void* gbar = nullptr;
   int* timeout_host = nullptr;     // pinned
+  // measured balance (single-scene systems): every CTA adds the time of its
+  // SpMV phases; after a solve the slice weights of each CTA are scaled by
+  // its measured time per weight and the slices re-partitioned
+  std::vector<double> slice_w;     // cost weight of every slice (steps + a per-slice cost at first)
+  std::vector<int> first_host;     // G+1 first slice of each CTA (host copy of cta_first)
+  unsigned long long* cta_ns = nullptr;       // G (device)
+  unsigned long long* cta_ns_host = nullptr;  // G (pinned)
+  int rebalances = 0;
 };
 
 struct Ctx {

@@ -943,6 +943,7 @@ struct RingShared {
   volatile unsigned char act[2][kMaxLocalScenes];  // activity by iteration parity
   unsigned char act_in[kMaxLocalScenes];      // activity given to the launch (before iteration 0)
   unsigned long long tmax;                    // profiling: the last CTA's end of the SpMV phase
+  unsigned long long t_phase;                 // start of this CTA's current SpMV phase
   volatile int pub;                           // last iteration whose activity is published
   volatile int stop;
   int ok;
@@ -962,11 +963,17 @@ __device__ __forceinline__ int local_scene(const RingShared& sh, int sl, int& ls
 template <int NV>
 __device__ __forceinline__ bool ring_sums(RingShared& sh, int L, int sc_lo, int n_sc, double gval,
                                           double* __restrict__ part, double* __restrict__ part_g, GridBarrier* gb,
-                                          unsigned long long* __restrict__ stamp = nullptr) {
+                                          unsigned long long* __restrict__ stamp = nullptr,
+                                          unsigned long long* __restrict__ work_ns = nullptr) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int G = gridDim.x, b = blockIdx.x;
   if (lane == 0) sh.wg[w] = gval;
   named_sync<kRingConsumers>();
+  if (work_ns && threadIdx.x == 0) {  // this CTA's share of the phase (its own slot)
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    work_ns[b] += t - sh.t_phase;
+  }
   if (stamp && threadIdx.x == 0) {  // profiling: when this CTA's warps finished the phase
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -1043,7 +1050,8 @@ __device__ __forceinline__ bool grid_barrier_named(GridBarrier* gb) {
 __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
     int n_sc, const int* __restrict__ cta_first, const int* __restrict__ cta_sc_lo, const int* __restrict__ sc_cta,
     const int* __restrict__ sc_slice, const MixDesc* __restrict__ desc, RingScene* __restrict__ ring, int pkind,
-    double* __restrict__ part, GridBarrier* gb, unsigned long long* __restrict__ prof) {
+    double* __restrict__ part, GridBarrier* gb, unsigned long long* __restrict__ prof,
+    unsigned long long* __restrict__ cta_ns) {
   extern __shared__ __align__(128) unsigned char ring_smem[];
   unsigned long long* full = reinterpret_cast<unsigned long long*>(ring_smem + kRingWarps * 2 * kRingStageBytes);
   unsigned long long* empty = full + 2 * kRingWarps;
@@ -1264,6 +1272,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
     const int kp = k & 1;
     unsigned long long t_a = 0;
     if (timer) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_a));
+    if (cta_ns && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(sh.t_phase));
     // ---- w = A u (pieces from the ring), (w, u)
     {
       for (int ls = 0; ls < L && alive; ls++) {
@@ -1340,7 +1349,8 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
       double na = 0.0;
       if (w == 0 && lane == 0)
         for (int ls = 0; ls < L; ls++) na += sh.act[kp][ls] ? 1.0 : 0.0;
-      if (!ring_sums<3>(sh, L, sc_lo, n_sc, na, part_3, part_g, gb, prof ? prof + 3 : nullptr)) alive = false;
+      if (!ring_sums<3>(sh, L, sc_lo, n_sc, na, part_3, part_g, gb, prof ? prof + 3 : nullptr, cta_ns))
+        alive = false;
     }
     if (!alive || sh.g == 0.0) break;
     if (timer) {
@@ -1877,6 +1887,8 @@ void mixed_free(MixedSys* m) {
   cudaFree(m->rrbb);
   cudaFree(m->res_part);
   cudaFree(m->part);
+  cudaFree(m->cta_ns);
+  if (m->cta_ns_host) cudaFreeHost(m->cta_ns_host);
   cudaFree(m->gbar);
   cudaFree(m->prof);
   if (m->ring_host) cudaFreeHost(m->ring_host);
@@ -1892,14 +1904,22 @@ void mixed_free(MixedSys* m) {
 // regions of short rows (boundary layers) do not make their CTAs the last to
 // finish.  OD_GB300_SLICE_COST overrides the constant.
 constexpr double kSliceCost = 8.0;
+// Contiguous slice ranges of equal total weight, one per CTA (at most
+// kMaxLocalScenes scenes per CTA).  The weight of a slice is its steps plus a
+// per-slice cost at first; measured times refine it (mixed_rebalance).
 static od_status mixed_partition(MixedSys* m, int G) {
   const int ns = m->ns;
-  double c_slice = kSliceCost;
-  if (const char* e = std::getenv("OD_GB300_SLICE_COST")) c_slice = std::atof(e);
+  if ((int)m->slice_w.size() != ns) {
+    double c_slice = kSliceCost;
+    if (const char* e = std::getenv("OD_GB300_SLICE_COST")) c_slice = std::atof(e);
+    m->slice_w.resize(ns);
+    for (int k = 0; k < ns; k++) m->slice_w[k] = (double)(m->off_host[k + 1] - m->off_host[k]) + c_slice;
+  }
   std::vector<int> sc_of(ns);
   for (int s = 0; s < m->n_sc; s++)
     for (int k = m->sc_slice[s]; k < m->sc_slice[s + 1]; k++) sc_of[k] = s;
-  const std::vector<int>& off = m->off_host;
+  std::vector<double> cum(ns + 1, 0.0);
+  for (int k = 0; k < ns; k++) cum[k + 1] = cum[k] + m->slice_w[k];
   std::vector<int> first(G + 1, ns), sc_lo(G, 0);
   std::vector<int> sc_cta(2 * std::max(1, m->n_sc), -1);
   for (int s = 0; s < m->n_sc; s++) sc_cta[2 * s + 1] = -2;  // empty range for scenes without slices
@@ -1907,8 +1927,8 @@ static od_status mixed_partition(MixedSys* m, int G) {
   for (int b = 0; b < G; b++) {
     first[b] = sl;
     sc_lo[b] = sl < ns ? sc_of[sl] : 0;
-    const double target = ((double)off[ns] + c_slice * ns) * (b + 1) / G;
-    while (sl < ns && ((double)off[sl] + c_slice * sl < target || b == G - 1)) {
+    const double target = cum[ns] * (b + 1) / G;
+    while (sl < ns && (cum[sl] < target || b == G - 1)) {
       if (sc_of[sl] - sc_lo[b] >= kMaxLocalScenes) break;
       sl++;
     }
@@ -1926,15 +1946,63 @@ static od_status mixed_partition(MixedSys* m, int G) {
       sc_cta[2 * s + 1] = b;
     }
   }
-  long long scratch = 0;
-  OD_TRY(dev_upload(&m->cta_first, first.data(), first.size(), scratch));
-  OD_TRY(dev_upload(&m->cta_sc_lo, sc_lo.data(), sc_lo.size(), scratch));
-  OD_TRY(dev_upload(&m->sc_cta, sc_cta.data(), sc_cta.size(), scratch));
+  m->first_host = first;
   const size_t npart = (size_t)3 * std::max(1, m->n_sc) * G + 2 * (size_t)G;
-  OD_CUDA(cudaMalloc(&m->part, sizeof(double) * npart));
+  if (!m->cta_first) {
+    long long scratch = 0;
+    OD_TRY(dev_upload(&m->cta_first, first.data(), first.size(), scratch));
+    OD_TRY(dev_upload(&m->cta_sc_lo, sc_lo.data(), sc_lo.size(), scratch));
+    OD_TRY(dev_upload(&m->sc_cta, sc_cta.data(), sc_cta.size(), scratch));
+    OD_CUDA(cudaMalloc(&m->part, sizeof(double) * npart));
+    OD_CUDA(cudaMalloc(&m->cta_ns, sizeof(unsigned long long) * G));
+    OD_CUDA(cudaMallocHost(&m->cta_ns_host, sizeof(unsigned long long) * G));
+  } else {
+    OD_CUDA(cudaMemcpy(m->cta_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice));
+    OD_CUDA(cudaMemcpy(m->cta_sc_lo, sc_lo.data(), sizeof(int) * sc_lo.size(), cudaMemcpyHostToDevice));
+    OD_CUDA(cudaMemcpy(m->sc_cta, sc_cta.data(), sizeof(int) * sc_cta.size(), cudaMemcpyHostToDevice));
+  }
   OD_CUDA(cudaMemset(m->part, 0, sizeof(double) * npart));
+  OD_CUDA(cudaMemset(m->cta_ns, 0, sizeof(unsigned long long) * G));
   m->cta_grid = G;
   return OD_OK;
+}
+
+// After a solve of a one-scene system: scale the weights of each CTA's
+// slices by the CTA's measured SpMV time per weight (relative to the
+// median) and re-partition, while the slowest CTA is more than 3% behind
+// the median (at most three times per system).  The slowness is a property
+// of the slices (boundary layers: short rows, padding) and moves with them.
+static od_status mixed_rebalance(Ctx* ctx, MixedSys* m) {
+  const int G = m->cta_grid;
+  OD_CUDA(cudaMemcpyAsync(m->cta_ns_host, m->cta_ns, sizeof(unsigned long long) * G, cudaMemcpyDeviceToHost,
+                          ctx->stream));
+  OD_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<double> t(G), rate(G, 0.0);
+  for (int b = 0; b < G; b++) t[b] = (double)m->cta_ns_host[b];
+  std::vector<double> sorted = t;
+  std::sort(sorted.begin(), sorted.end());
+  const double median = sorted[G / 2], worst = sorted[G - 1];
+  OD_CUDA(cudaMemsetAsync(m->cta_ns, 0, sizeof(unsigned long long) * G, ctx->stream));
+  if (m->n_sc != 1 || m->rebalances >= 3 || median <= 0.0 || worst < 1.03 * median) return OD_OK;
+  std::vector<double> rates;
+  for (int b = 0; b < G; b++) {
+    double w = 0.0;
+    for (int k = m->first_host[b]; k < m->first_host[b + 1]; k++) w += m->slice_w[k];
+    if (w > 0.0 && t[b] > 0.0) {
+      rate[b] = t[b] / w;
+      rates.push_back(rate[b]);
+    }
+  }
+  if (rates.empty()) return OD_OK;
+  std::sort(rates.begin(), rates.end());
+  const double mid = rates[rates.size() / 2];
+  for (int b = 0; b < G; b++) {
+    if (rate[b] <= 0.0) continue;
+    const double f = std::min(2.0, std::max(0.5, rate[b] / mid));
+    for (int k = m->first_host[b]; k < m->first_host[b + 1]; k++) m->slice_w[k] *= f;
+  }
+  m->rebalances++;
+  return mixed_partition(m, G);
 }
 
 od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::vector<const double*>& b,
@@ -2094,7 +2162,7 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
     int pkv = pk, nsc = n_sc;
     void* args[] = {(void*)&nsc,       (void*)&m->cta_first, (void*)&m->cta_sc_lo, (void*)&m->sc_cta,
                     (void*)&m->sc_slice_dev, (void*)&m->desc, (void*)&m->ring,    (void*)&pkv,
-                    (void*)&m->part,   (void*)&gbp,          (void*)&profp};
+                    (void*)&m->part,   (void*)&gbp,          (void*)&profp,       (void*)&m->cta_ns};
     if (prof) OD_CUDA(cudaEventRecord(ctx->ev_pool[0], strm));
     ctx->launches++;
     OD_CUDA(cudaLaunchCooperativeKernel((void*)pcg32_ring_kernel, dim3(m->cta_grid), dim3(kRingThreads), args,
@@ -2136,6 +2204,7 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
       need[s] = rr[s] > eps[s] && R.iters > 0;  // no progress possible without an inner iteration
     }
   }
+  if (rc == OD_OK) OD_TRY(mixed_rebalance(ctx, m));
   for (int s = 0; s < n_sc; s++) {
     if (status[s] == OD_OK && rr[s] > eps[s] && m->sc_nb[s] > 0) status[s] = OD_ERR_NOT_CONVERGED;
     if ((status[s] == OD_ERR_NOT_CONVERGED || status[s] == OD_ERR_NAN) && rc == OD_OK) {
