@@ -230,7 +230,8 @@ static void scene_free(Scene* s) {
                   (void*)s->dv, (void*)s->rhs, (void*)s->tmp, (void*)s->trac_facets, (void*)s->trac_vec,
                   (void*)s->bsr.row_ptr, (void*)s->bsr.col, (void*)s->bsr.desc_off, (void*)s->bsr.desc_kind,
                   (void*)s->bsr.gen, (void*)s->bsr.diag_pos, (void*)s->tmp2, (void*)s->stage_k,
-                  (void*)s->stage_f, (void*)s->color_off_dev, (void*)s->plastic})
+                  (void*)s->stage_f, (void*)s->color_off_dev, (void*)s->plastic, (void*)s->gat_kptr,
+                  (void*)s->gat_ksrc, (void*)s->gat_fptr, (void*)s->gat_fsrc})
     if (p) cudaFree(p);
   pcg_free(s);
   if (s->ev_step[0]) { cudaEventDestroy(s->ev_step[0]); cudaEventDestroy(s->ev_step[1]); }
@@ -325,6 +326,41 @@ static od_status scene_build(Scene* s, int n_nodes, const double* X, int n_tets,
   for (double** v : {&s->fint, &s->fext, &s->v, &s->d, &s->a, &s->dp, &s->vp, &s->dv, &s->rhs, &s->tmp, &s->tmp2}) {
     OD_TRY(dalloc(s, v, np));
     OD_CUDA(cudaMemset(*v, 0, sizeof(double) * np));
+  }
+  if (ne > 0 && 78LL * ne < (long long)INT32_MAX) {
+    // gather lists of the assembly: per destination its (entry, staged
+    // element) sources in element index order, counting sort on the host
+    std::vector<int> pos(ne), kptr((size_t)s->nvals + 1, 0), fptr(np + 1, 0);
+    for (int e = 0; e < ne; e++) pos[s->elem_perm[e]] = e;
+    for (int o = 0; o < ne; o++) {
+      for (int k = 0; k < 78; k++) {
+        const int idx = s->hemap[78 * (size_t)o + k];
+        if (idx >= 0) kptr[(size_t)idx + 1]++;
+      }
+      for (int k = 0; k < 12; k++) {
+        const int g = gidx[12 * (size_t)o + k];
+        if (g >= 0) fptr[(size_t)g + 1]++;
+      }
+    }
+    for (size_t i = 0; i < kptr.size() - 1; i++) kptr[i + 1] += kptr[i];
+    for (size_t i = 0; i < fptr.size() - 1; i++) fptr[i + 1] += fptr[i];
+    std::vector<int> ksrc(std::max(1, kptr.back())), fsrc(std::max(1, fptr.back()));
+    std::vector<int> kcur(kptr.begin(), kptr.end() - 1), fcur(fptr.begin(), fptr.end() - 1);
+    for (int o = 0; o < ne; o++) {
+      const int e = pos[o];
+      for (int k = 0; k < 78; k++) {
+        const int idx = s->hemap[78 * (size_t)o + k];
+        if (idx >= 0) ksrc[kcur[idx]++] = k * ne + e;
+      }
+      for (int k = 0; k < 12; k++) {
+        const int g = gidx[12 * (size_t)o + k];
+        if (g >= 0) fsrc[fcur[g]++] = k * ne + e;
+      }
+    }
+    OD_TRY(dupload(s, &s->gat_kptr, kptr.data(), kptr.size()));
+    OD_TRY(dupload(s, &s->gat_ksrc, ksrc.data(), ksrc.size()));
+    OD_TRY(dupload(s, &s->gat_fptr, fptr.data(), fptr.size()));
+    OD_TRY(dupload(s, &s->gat_fsrc, fsrc.data(), fsrc.size()));
   }
   OD_TRY(launch_precompute(s));
   OD_TRY(launch_mass(s));

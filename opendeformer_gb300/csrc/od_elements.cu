@@ -713,6 +713,33 @@ __global__ void scatter_kernel(int e0, int cnt, int ne, const double* __restrict
   }
 }
 
+// gathered assembly: value i of K (and entry i of the forces) is the sum of
+// its element contributions in the reference's assembly order (element
+// index, then the element's entry index; the loops of
+// material/corotationalHyperelastic.cpp:67-97), started from zero, so the
+// additions happen in the reference's sequence.  One thread per destination,
+// no atomics, no colour passes.
+__global__ void __launch_bounds__(256) gather_kernel(int nk, const int* __restrict__ kptr,
+                                                     const int* __restrict__ ksrc, const double* __restrict__ k78,
+                                                     double* __restrict__ K, int nf, const int* __restrict__ fptr,
+                                                     const int* __restrict__ fsrc, const double* __restrict__ f12,
+                                                     double* __restrict__ fint, int accumulate) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int* ptr = kptr;
+  const int* src = ksrc;
+  const double* val = k78;
+  double* out = K;
+  if (i >= nk) {
+    i -= nk;
+    if (i >= nf) return;
+    ptr = fptr; src = fsrc; val = f12; out = fint;
+  }
+  const int j1 = ptr[i + 1];
+  double acc = accumulate ? out[i] : 0.0;
+  for (int j = ptr[i]; j < j1; j++) acc += val[src[j]];
+  out[i] = acc;
+}
+
 // multi-scene scatter of colour c: tile j of scene s covers the colour's
 // threads [256 j, 256 j + 256) (90 per element: 78 stiffness values, 12
 // forces)
@@ -784,7 +811,7 @@ od_status launch_mass(Scene* s) {
 od_status launch_eval(Scene* s, bool zero_first) {
   const int T = 128;
   cudaStream_t st = s->ctx->stream;
-  if (zero_first) {
+  if (zero_first && (!s->gat_kptr || s->n_tets == 0)) {
     OD_CUDA(cudaMemsetAsync(s->K, 0, sizeof(double) * (size_t)s->nvals, st));
     OD_CUDA(cudaMemsetAsync(s->fint, 0, sizeof(double) * (size_t)s->pcg.n_pad, st));
   }
@@ -805,7 +832,16 @@ od_status launch_eval(Scene* s, bool zero_first) {
                                                           s->tets, s->X, s->u, s->pre, s->mat.threshold, s->lambda,
                                                           s->mu, s->emap, s->gdof, nullptr, nullptr, s->stage_k,
                                                           s->stage_f, nullptr);
-  // 2) atomic-free scatter, one colour per launch
+  // 2) assembly: one gather launch; one scatter launch per colour for meshes
+  //    whose gather lists do not fit 32-bit indices
+  if (s->gat_kptr) {
+    const long long nd = (long long)s->nvals + s->pcg.n_pad;
+    OD_KL(s);
+    gather_kernel<<<nblk(nd, 256), 256, 0, st>>>(s->nvals, s->gat_kptr, s->gat_ksrc, s->stage_k, s->K, s->pcg.n_pad,
+                                                 s->gat_fptr, s->gat_fsrc, s->stage_f, s->fint, zero_first ? 0 : 1);
+    OD_CUDA(cudaGetLastError());
+    return OD_OK;
+  }
   for (size_t c = 0; c + 1 < s->color_off.size(); c++) {
     int e0 = s->color_off[c], e1 = s->color_off[c + 1];
     if (e1 <= e0) continue;

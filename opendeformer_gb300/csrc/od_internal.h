@@ -274,6 +274,12 @@ struct Scene {
   int nbc = 0, nrem = 0, nvals = 0;
   std::vector<int> color_off;      // element colour ranges (colour order)
   int* color_off_dev = nullptr;    // the same on the device
+  // gathered assembly (CSR over the destinations, sources in the reference's
+  // element order; null when 78 x elements overflows a 32-bit index)
+  int* gat_kptr = nullptr;  // nvals + 1
+  int* gat_ksrc = nullptr;  // k * n_tets + staged element position
+  int* gat_fptr = nullptr;  // n_pad + 1
+  int* gat_fsrc = nullptr;  // (k - 78) * n_tets + staged element position
   std::vector<int> elem_perm;      // colour-order position -> original element
   // device
   double* X = nullptr;

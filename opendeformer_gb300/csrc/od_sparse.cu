@@ -18,6 +18,7 @@
 #include <cstring>
 
 #include "od_internal.h"
+#include "od_grid.cuh"
 
 namespace od {
 
@@ -447,44 +448,7 @@ __global__ void residual_norm_kernel(int n, const double* __restrict__ b, const 
 // are bounded: after kSpinLimit polls the waiting CTA records a timeout and
 // every CTA leaves the solve at the next barrier, so the kernel always
 // returns and the host reports OD_ERR_DEVICE_TIMEOUT.
-struct GridBarrier {
-  unsigned int arrive;
-  unsigned int gen;
-  int timeout;
-  int pad;
-};
-constexpr unsigned long long kSpinLimit = 1ull << 22;  // polls (about 1-2 s of L2 round trips) before a timeout
 constexpr int kPThreads = 768;                          // 24 warps; multiple of 3
-
-// arrival of one thread per CTA (acquire/release atomics: measured 1.9 us
-// per barrier over 152 CTAs on GB300, against 2.3 us with full fences);
-// returns 0 after a timeout
-__device__ __forceinline__ int barrier_arrive_wait(GridBarrier* gb) {
-  unsigned int g, a;
-  asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(g) : "l"(&gb->gen) : "memory");
-  asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;" : "=r"(a) : "l"(&gb->arrive) : "memory");
-  int ok = 1;
-  if (a == gridDim.x - 1) {
-    gb->arrive = 0;
-    asm volatile("red.release.gpu.add.u32 [%0], 1;" ::"l"(&gb->gen) : "memory");
-  } else {
-    unsigned long long spins = 0;
-    unsigned int cur;
-    do {
-      asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(cur) : "l"(&gb->gen) : "memory");
-      if (++spins > kSpinLimit) { atomicExch(&gb->timeout, 1); ok = 0; break; }
-    } while (cur == g);
-  }
-  return ok && !*(volatile int*)&gb->timeout;
-}
-
-__device__ __forceinline__ bool grid_barrier(GridBarrier* gb) {
-  __shared__ int ok_s;
-  __syncthreads();
-  if (threadIdx.x == 0) ok_s = barrier_arrive_wait(gb);
-  __syncthreads();
-  return ok_s != 0;
-}
 
 // sum of part[0..m) by every CTA in the same order, broadcast to the CTA
 __device__ __forceinline__ double cta_sum(const double* __restrict__ part, int m) {
