@@ -66,6 +66,7 @@ struct Batch {
   int* dirs = nullptr;  // all tile-directory prefixes in one allocation
   TileDir zero_k, zero_f, corot, inv, plastic, expand, rows, dof;
   std::vector<TileDir> scatter;  // per colour
+  TileDir gather{nullptr, -1, 256};  // gathered assembly (tiles -1: some scene has no lists)
   MixedSys* mix = nullptr;
   int newton = 1, precond = OD_PRECOND_BLOCK_JACOBI;
   std::vector<od_solver_params> prm;
@@ -106,6 +107,10 @@ static SceneDev scene_dev(const Scene* s) {
   D.emap = s->emap;
   D.gdof = s->gdof;
   D.color_off = s->color_off_dev;
+  D.gat_kptr = s->gat_kptr;
+  D.gat_ksrc = s->gat_ksrc;
+  D.gat_fptr = s->gat_fptr;
+  D.gat_fsrc = s->gat_fsrc;
   D.K = s->K;
   D.fint = s->fint;
   D.stage_k = s->stage_k;
@@ -146,7 +151,9 @@ static od_status batch_build(Batch* B) {
   const int n = (int)B->sc.size();
   int max_colors = 0;
   for (const Scene* s : B->sc) max_colors = std::max(max_colors, (int)s->color_off.size() - 1);
-  const int n_dirs = 8 + max_colors;
+  const int n_dirs = 9 + max_colors;
+  bool gathered = true;
+  for (const Scene* s : B->sc) gathered = gathered && (s->gat_kptr || s->n_tets == 0);
   std::vector<int> pre((size_t)n_dirs * (n + 1), 0);
   auto P = [&](int d) { return pre.data() + (size_t)d * (n + 1); };
   for (int i = 0; i < n; i++) {
@@ -160,9 +167,10 @@ static od_status batch_build(Batch* B) {
                            ceil_div(9LL * s->bsr.nnzb, kExpandTile), ceil_div(s->bsr.nb, kBatchRows),
                            ceil_div(s->pcg.n_pad, 256)};
     for (int d = 0; d < 8; d++) P(d)[i + 1] = P(d)[i] + counts[d];
+    P(8)[i + 1] = P(8)[i] + (s->gat_kptr ? ceil_div((long long)s->nvals + s->pcg.n_pad, 256) : 0);
     for (int c = 0; c < max_colors; c++) {
       const int cnt = c + 1 < (int)s->color_off.size() ? s->color_off[c + 1] - s->color_off[c] : 0;
-      P(8 + c)[i + 1] = P(8 + c)[i] + ceil_div(90LL * cnt, 256);
+      P(9 + c)[i + 1] = P(9 + c)[i] + ceil_div(90LL * cnt, 256);
     }
   }
   OD_CUDA(cudaMalloc(&B->dirs, sizeof(int) * pre.size()));
@@ -176,7 +184,8 @@ static od_status batch_build(Batch* B) {
   B->expand = dir(5, kExpandTile);
   B->rows = dir(6, kBatchRows);
   B->dof = dir(7, 256);
-  for (int c = 0; c < max_colors; c++) B->scatter.push_back(dir(8 + c, 256));
+  for (int c = 0; c < max_colors; c++) B->scatter.push_back(dir(9 + c, 256));
+  if (gathered) B->gather = dir(8, 256);
   OD_CUDA(cudaMalloc(&B->sd, sizeof(SceneDev) * std::max(1, n)));
   OD_CUDA(cudaMemcpy(B->sd, B->sd_host.data(), sizeof(SceneDev) * n, cudaMemcpyHostToDevice));
   std::vector<const double*> rhs;
@@ -213,7 +222,7 @@ static od_status batch_step(Batch* B, std::vector<od_step_stats>& acc) {
   for (int it = 0; it < B->newton; it++) {
     OD_TRY(nm_op(B, NM_STAGE));
     const int n = (int)B->sc.size();
-    OD_TRY(launch_eval_batch(ctx, n, B->sd, B->zero_k, B->zero_f, B->corot, B->inv, B->plastic, B->scatter));
+    OD_TRY(launch_eval_batch(ctx, n, B->sd, B->zero_k, B->zero_f, B->corot, B->inv, B->plastic, B->scatter, B->gather));
     OD_TRY(launch_spmv_lower_batch(ctx, n, B->sd, B->rows));
     OD_TRY(nm_op(B, NM_RESIDUAL));
     OD_TRY(launch_expand_batch(ctx, n, B->sd, B->expand));

@@ -719,12 +719,11 @@ __global__ void scatter_kernel(int e0, int cnt, int ne, const double* __restrict
 // material/corotationalHyperelastic.cpp:67-97), started from zero, so the
 // additions happen in the reference's sequence.  One thread per destination,
 // no atomics, no colour passes.
-__global__ void __launch_bounds__(256) gather_kernel(int nk, const int* __restrict__ kptr,
-                                                     const int* __restrict__ ksrc, const double* __restrict__ k78,
-                                                     double* __restrict__ K, int nf, const int* __restrict__ fptr,
-                                                     const int* __restrict__ fsrc, const double* __restrict__ f12,
-                                                     double* __restrict__ fint, int accumulate) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void gather_one(long long i, int nk, const int* __restrict__ kptr,
+                                           const int* __restrict__ ksrc, const double* __restrict__ k78,
+                                           double* __restrict__ K, int nf, const int* __restrict__ fptr,
+                                           const int* __restrict__ fsrc, const double* __restrict__ f12,
+                                           double* __restrict__ fint, int accumulate) {
   const int* ptr = kptr;
   const int* src = ksrc;
   const double* val = k78;
@@ -738,6 +737,15 @@ __global__ void __launch_bounds__(256) gather_kernel(int nk, const int* __restri
   double acc = accumulate ? out[i] : 0.0;
   for (int j = ptr[i]; j < j1; j++) acc += val[src[j]];
   out[i] = acc;
+}
+
+__global__ void __launch_bounds__(256) gather_kernel(int nk, const int* __restrict__ kptr,
+                                                     const int* __restrict__ ksrc, const double* __restrict__ k78,
+                                                     double* __restrict__ K, int nf, const int* __restrict__ fptr,
+                                                     const int* __restrict__ fsrc, const double* __restrict__ f12,
+                                                     double* __restrict__ fint, int accumulate) {
+  gather_one((long long)blockIdx.x * blockDim.x + threadIdx.x, nk, kptr, ksrc, k78, K, nf, fptr, fsrc, f12, fint,
+             accumulate);
 }
 
 // multi-scene scatter of colour c: tile j of scene s covers the colour's
@@ -760,6 +768,16 @@ __global__ void scatter_batch_kernel(int n_sc, const int* __restrict__ prefix, i
     const int g = D.gdof[(size_t)(k - 78) * ne + e];
     if (g >= 0) D.fint[g] += D.stage_f[(size_t)(k - 78) * ne + e];
   }
+}
+
+// multi-scene gathered assembly: tile j of scene s covers its destinations
+// [256 j, 256 j + 256) (K values, then the padded f_int entries)
+__global__ void __launch_bounds__(256) gather_batch_kernel(int n_sc, const int* __restrict__ prefix,
+                                                           const SceneDev* __restrict__ sd) {
+  const int s = dir_scene(prefix, n_sc, blockIdx.x);
+  const SceneDev& D = sd[s];
+  gather_one((long long)(blockIdx.x - prefix[s]) * 256 + threadIdx.x, D.nvals, D.gat_kptr, D.gat_ksrc, D.stage_k,
+             D.K, D.n_pad, D.gat_fptr, D.gat_fsrc, D.stage_f, D.fint, 0);
 }
 
 // zero 4096 K values (which 0) or padded f_int entries (which 1) per tile
@@ -906,13 +924,14 @@ namespace od {
 
 od_status launch_eval_batch(Ctx* ctx, int n_sc, const SceneDev* sd, const TileDir& zero_k, const TileDir& zero_f,
                             const TileDir& corot, const TileDir& inv, const TileDir& plastic,
-                            const std::vector<TileDir>& scatter) {
+                            const std::vector<TileDir>& scatter, const TileDir& gather) {
   cudaStream_t st = ctx->stream;
-  if (zero_k.tiles > 0) {
+  const bool gathered = gather.tiles >= 0;  // every scene has gather lists
+  if (!gathered && zero_k.tiles > 0) {
     ctx->launches++;
     zero_batch_kernel<<<zero_k.tiles, 256, 0, st>>>(n_sc, zero_k.prefix, 0, sd);
   }
-  if (zero_f.tiles > 0) {
+  if (!gathered && zero_f.tiles > 0) {
     ctx->launches++;
     zero_batch_kernel<<<zero_f.tiles, 256, 0, st>>>(n_sc, zero_f.prefix, 1, sd);
   }
@@ -927,6 +946,14 @@ od_status launch_eval_batch(Ctx* ctx, int n_sc, const SceneDev* sd, const TileDi
   if (plastic.tiles > 0) {
     ctx->launches++;
     plastic_batch_kernel<<<plastic.tiles, 128, 0, st>>>(n_sc, plastic.prefix, sd);
+  }
+  if (gathered) {
+    if (gather.tiles > 0) {
+      ctx->launches++;
+      gather_batch_kernel<<<gather.tiles, 256, 0, st>>>(n_sc, gather.prefix, sd);
+    }
+    OD_CUDA(cudaGetLastError());
+    return OD_OK;
   }
   for (size_t c = 0; c < scatter.size(); c++) {
     if (scatter[c].tiles <= 0) continue;

@@ -129,6 +129,7 @@ struct SceneDev {
   const int* emap;
   const int* gdof;
   const int* color_off;            // colour ranges of the (colour-ordered) elements
+  const int *gat_kptr, *gat_ksrc, *gat_fptr, *gat_fsrc;  // gathered assembly lists
   double *K, *fint, *stage_k, *stage_f;
   const double *M, *fext;
   const int *row_ptr, *col, *desc_kind, *desc_off, *gen;
@@ -422,7 +423,8 @@ od_status launch_loads(Scene* s, const double* body, int n_facets_total, double 
 // per element of the colour)
 od_status launch_eval_batch(Ctx* ctx, int n_sc, const SceneDev* sd, const TileDir& zero_k, const TileDir& zero_f,
                             const TileDir& corot, const TileDir& inv, const TileDir& plastic,
-                            const std::vector<TileDir>& scatter);
+                            const std::vector<TileDir>& scatter,
+                            const TileDir& gather);
 od_status sync_stream(Scene* s);
 
 // ---- kernels (od_sparse.cu) ----
