@@ -89,6 +89,20 @@ struct Pcg {
   int* icT_ci = nullptr;
   int* icT_pos = nullptr;       // index into ic_val
   double ic_shift = 0.0;
+  // the factor split for the one-launch sweeps: strictly lower rows
+  // (forward), strictly lower columns (backward: icT_*), diagonal
+  int* ic_frp = nullptr;        // ic_n + 1
+  int* ic_fci = nullptr;
+  double* ic_fval = nullptr;
+  double* ic_bval = nullptr;    // L values in icT order
+  double* ic_dval = nullptr;    // 1 / L_ii
+  double* ic_y = nullptr;       // forward result
+  int* ic_err = nullptr;        // a bounded wait ran out
+  int* ic_err_host = nullptr;   // pinned
+  int ic_grid = 0;
+  int* ic_gord_f = nullptr;     // row triples by forward / backward level
+  int* ic_gord_b = nullptr;
+  int ic_gdepth = 0;            // levels of the two sweeps
   // persistent (cooperative) solve
   void* gbar = nullptr;         // grid barrier state
   int* timeout_host = nullptr;  // pinned
@@ -472,6 +486,25 @@ od_status sweep_apply(Scene* s, const double* r, double* z, const SolveScalars* 
 // OD_ERR_DEVICE_TIMEOUT if a sweep's bounded wait ran out since the last check
 od_status sweep_check(Scene* s);
 void sweep_free(SweepSys* l);
+// A factor laid out for one cooperative two-sweep apply (od_sweep.cu):
+// strictly lower rows (frp/fci/fval), strictly lower columns (bcp/bri/bval),
+// the diagonal, row triples [3g, 3g + 3) listed by forward / backward
+// dependency level (sweep_group_levels).
+struct SweepView {
+  int n = 0, n_pad = 0;
+  int ic = 1;                   // 1: diag holds 1 / L_ii; 0: D^-1 (LDL^T)
+  int grid = 0;                 // co-resident CTAs
+  long long nnz = 0;            // strictly lower entries
+  const int *frp = nullptr, *fci = nullptr, *bcp = nullptr, *bri = nullptr, *ord_f = nullptr, *ord_b = nullptr;
+  const double *fval = nullptr, *bval = nullptr, *diag = nullptr;
+  double* y = nullptr;
+  int* err = nullptr;
+};
+od_status sweep_grid(Scene* s, int n, int* grid);
+void sweep_group_levels(int n, const std::vector<int>& frp, const std::vector<int>& fci, const std::vector<int>& bcp,
+                        const std::vector<int>& bri, std::vector<int>& ord_f, std::vector<int>& ord_b, int* depth_f,
+                        int* depth_b);
+od_status sweep_launch(Scene* s, const SweepView& v, const double* r, double* z, const SolveScalars* sc);
 
 // PCG on A64; b and x are device vectors of length n_pad
 od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm, od_solve_stats* st);

@@ -1470,33 +1470,18 @@ __global__ void ic0_factor_level(int l0, int l1, const int* __restrict__ rows, c
   }
 }
 
-// forward sweep L y = r for the rows of one level
-__global__ void ic0_forward_level(int l0, int l1, const int* __restrict__ rows, const int* __restrict__ rp,
-                                  const int* __restrict__ ci, const double* __restrict__ L, const double* __restrict__ r,
-                                  double* __restrict__ y, const SolveScalars* sc) {
-  if (sc && *(volatile const int*)&sc->done) return;
-  int t = l0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= l1) return;
-  const int i = rows[t];
-  const int e = rp[i + 1] - 1;
-  double s = r[i];
-  for (int q = rp[i]; q < e; q++) s -= L[q] * y[ci[q]];
-  y[i] = s / L[e];
-}
-
-// backward sweep L^T z = y through the transposed index (row i lists the
-// entries L_ji, j > i)
-__global__ void ic0_backward_level(int l0, int l1, const int* __restrict__ rows, const int* __restrict__ trp,
-                                   const int* __restrict__ tci, const int* __restrict__ tpos,
-                                   const int* __restrict__ rp, const double* __restrict__ L,
-                                   const double* __restrict__ y, double* __restrict__ z, const SolveScalars* sc) {
-  if (sc && *(volatile const int*)&sc->done) return;
-  int t = l0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= l1) return;
-  const int i = rows[t];
-  double s = y[i];
-  for (int q = trp[i]; q < trp[i + 1]; q++) s -= L[tpos[q]] * z[tci[q]];
-  z[i] = s / L[rp[i + 1] - 1];
+// the IC(0) factor (rows, diagonal last) split for the one-launch sweeps:
+// strictly lower rows, values in transposed order, reciprocal diagonal
+__global__ void ic0_split_kernel(int n, const int* __restrict__ rp, const int* __restrict__ frp,
+                                 const double* __restrict__ L, int nt, const int* __restrict__ tpos,
+                                 double* __restrict__ fval, double* __restrict__ bval, double* __restrict__ dval) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += stride) bval[t] = L[tpos[t]];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int a = rp[i], e = rp[i + 1] - 1, o = frp[i];
+    for (int q = a; q < e; q++) fval[o + q - a] = L[q];
+    dval[i] = 1.0 / L[e];   // the apply multiplies by 1 / L_ii
+  }
 }
 
 __global__ void copy_kernel(int n, const double* __restrict__ a, double* __restrict__ b) {
@@ -1623,6 +1608,18 @@ static od_status ic0_build(Scene* s) {
     for (int q = trp[i]; q < fill[i]; q++) { tci2.push_back(tci[q]); tpos2.push_back(tpos[q]); }
     trp2[i + 1] = (int)tci2.size();
   }
+  // strictly lower rows for the forward sweep
+  std::vector<int> frp(n + 1, 0), fci;
+  fci.reserve(nnz);
+  for (int i = 0; i < n; i++) {
+    for (int q = srp[i]; q < srp[i + 1] - 1; q++) fci.push_back(sci[q]);
+    frp[i + 1] = (int)fci.size();
+  }
+  // row triples by level for the one-launch sweeps
+  std::vector<int> gof, gob;
+  int gdf = 0, gdb = 0;
+  sweep_group_levels(n, frp, fci, trp2, tci2, gof, gob, &gdf, &gdb);
+  P.ic_gdepth = gdf + gdb;
   std::vector<int> lrf, lrb;
   build_ic_levels(srp, sci, n, lrf, P.lvl_ptr_f, true);
   build_ic_levels(srp, sci, n, lrb, P.lvl_ptr_b, false);
@@ -1645,9 +1642,22 @@ static od_status ic0_build(Scene* s) {
   if ((st = up(&P.icT_rp, trp2)) != OD_OK) return st;
   if ((st = up(&P.icT_ci, tci2)) != OD_OK) return st;
   if ((st = up(&P.icT_pos, tpos2)) != OD_OK) return st;
+  if ((st = up(&P.ic_frp, frp)) != OD_OK) return st;
+  if ((st = up(&P.ic_fci, fci)) != OD_OK) return st;
+  if ((st = up(&P.ic_gord_f, gof)) != OD_OK) return st;
+  if ((st = up(&P.ic_gord_b, gob)) != OD_OK) return st;
   OD_CUDA(cudaMalloc(&P.ic_val, sizeof(double) * std::max(1, nnz)));
+  const size_t nl = std::max<size_t>(1, fci.size());
+  OD_CUDA(cudaMalloc(&P.ic_fval, sizeof(double) * nl));
+  OD_CUDA(cudaMalloc(&P.ic_bval, sizeof(double) * nl));
+  OD_CUDA(cudaMalloc(&P.ic_dval, sizeof(double) * std::max(1, n)));
+  OD_CUDA(cudaMalloc(&P.ic_y, sizeof(double) * std::max(1, n)));
   OD_CUDA(cudaMalloc(&P.ic_bad, sizeof(int)));
-  s->device_bytes += sizeof(double) * (long long)nnz;
+  OD_CUDA(cudaMalloc(&P.ic_err, sizeof(int)));
+  OD_CUDA(cudaMemset(P.ic_err, 0, sizeof(int)));
+  OD_CUDA(cudaMallocHost(&P.ic_err_host, sizeof(int)));
+  OD_TRY(sweep_grid(s, n, &P.ic_grid));
+  s->device_bytes += sizeof(double) * ((long long)nnz + 2LL * (long long)nl + 2LL * n);
   return OD_OK;
 }
 
@@ -1674,24 +1684,53 @@ static od_status ic0_factor(Scene* s) {
     shift = shift == 0.0 ? 1e-3 : 2.0 * shift;
   }
   P.ic_shift = shift;
+  if (P.ic_n > 0) {
+    const int nt = P.ic_nnz - P.ic_n;
+    OD_KL(s);
+    ic0_split_kernel<<<nblk(std::max(nt, P.ic_n), 256), 256, 0, strm>>>(P.ic_n, P.ic_rp, P.ic_frp, P.ic_val, nt,
+                                                                         P.icT_pos, P.ic_fval, P.ic_bval, P.ic_dval);
+    OD_CUDA(cudaGetLastError());
+  }
+  s->ctx->sweep_levels = P.ic_gdepth;
   return OD_OK;
 }
 
-static void ic0_apply(Scene* s, const double* r, double* z, const SolveScalars* sc) {
+// L y = r, L^T z = y in one cooperative launch (rows by dependency level,
+// each row's value its own ready flag)
+static od_status ic0_apply(Scene* s, const double* r, double* z, const SolveScalars* sc) {
   Pcg& P = s->pcg;
+  SweepView v;
+  v.n = P.ic_n;
+  v.n_pad = P.n_pad;
+  v.ic = 1;
+  v.grid = P.ic_grid;
+  v.nnz = (long long)P.ic_nnz - P.ic_n;
+  v.frp = P.ic_frp;
+  v.fci = P.ic_fci;
+  v.fval = P.ic_fval;
+  v.bcp = P.icT_rp;
+  v.bri = P.icT_ci;
+  v.bval = P.ic_bval;
+  v.ord_f = P.ic_gord_f;
+  v.ord_b = P.ic_gord_b;
+  v.diag = P.ic_dval;
+  v.y = P.ic_y;
+  v.err = P.ic_err;
+  return sweep_launch(s, v, r, z, sc);
+}
+
+static od_status ic0_check(Scene* s) {
+  Pcg& P = s->pcg;
+  if (!P.ic_err) return OD_OK;
   cudaStream_t strm = s->ctx->stream;
-  for (int l = 0; l < P.n_levels_f; l++) {
-    int l0 = P.lvl_ptr_f[l], l1 = P.lvl_ptr_f[l + 1];
-    OD_KL(s);
-    ic0_forward_level<<<nblk(l1 - l0, 128), 128, 0, strm>>>(l0, l1, P.lvl_rows_f, P.ic_rp, P.ic_ci, P.ic_val, r,
-                                                            P.q /*y*/, sc);
+  OD_CUDA(cudaMemcpyAsync(P.ic_err_host, P.ic_err, sizeof(int), cudaMemcpyDeviceToHost, strm));
+  OD_TRY(sync_stream(s));
+  if (*P.ic_err_host) {
+    OD_CUDA(cudaMemsetAsync(P.ic_err, 0, sizeof(int), strm));
+    set_error("IC(0) sweep: a bounded wait on a row value ran out");
+    return OD_ERR_DEVICE_TIMEOUT;
   }
-  for (int l = 0; l < P.n_levels_b; l++) {
-    int l0 = P.lvl_ptr_b[l], l1 = P.lvl_ptr_b[l + 1];
-    OD_KL(s);
-    ic0_backward_level<<<nblk(l1 - l0, 128), 128, 0, strm>>>(l0, l1, P.lvl_rows_b, P.icT_rp, P.icT_ci, P.icT_pos,
-                                                             P.ic_rp, P.ic_val, P.q, z, sc);
-  }
+  return OD_OK;
 }
 
 od_status pcg_alloc(Scene* s) {
@@ -1730,8 +1769,11 @@ od_status pcg_alloc(Scene* s) {
 
 void pcg_free(Scene* s) {
   Pcg& P = s->pcg;
-  for (double* v : {P.x, P.r, P.z, P.p, P.q, P.b, P.partial, P.pinv, P.ic_val}) cudaFree(v);
-  for (int* v : {P.ic_rp, P.ic_ci, P.ic_src, P.lvl_rows_f, P.lvl_rows_b, P.icT_rp, P.icT_ci, P.icT_pos, P.ic_bad})
+  for (double* v : {P.x, P.r, P.z, P.p, P.q, P.b, P.partial, P.pinv, P.ic_val, P.ic_fval, P.ic_bval, P.ic_dval, P.ic_y})
+    cudaFree(v);
+  if (P.ic_err_host) cudaFreeHost(P.ic_err_host);
+  for (int* v : {P.ic_rp, P.ic_ci, P.ic_src, P.lvl_rows_f, P.lvl_rows_b, P.icT_rp, P.icT_ci, P.icT_pos, P.ic_bad,
+                 P.ic_frp, P.ic_fci, P.ic_err, P.ic_gord_f, P.ic_gord_b})
     cudaFree(v);
   cudaFree(P.sc);
   cudaFree(P.gbar);
@@ -2294,7 +2336,7 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
                                                           P.p, pk, P.pinv, part_c, part_d, part_b);
   int g_rz0 = g_rows;
   if (swept) {
-    if (pk == OD_PRECOND_IC0) ic0_apply(s, P.r, P.z, nullptr);
+    if (pk == OD_PRECOND_IC0) OD_TRY(ic0_apply(s, P.r, P.z, nullptr));
     else OD_TRY(sweep_apply(s, P.r, P.z, nullptr));
     OD_KL(s);
     pcg_rz_kernel<<<g_vec, kThreads, 0, strm>>>(n, P.r, P.z, part_c, nullptr);
@@ -2324,7 +2366,7 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
                                                          part_c, part_b, P.sc, slot);
       int g_rz = g_upd;
       if (swept) {
-        if (pk == OD_PRECOND_IC0) ic0_apply(s, P.r, P.z, P.sc);
+        if (pk == OD_PRECOND_IC0) OD_TRY(ic0_apply(s, P.r, P.z, P.sc));
         else OD_TRY(sweep_apply(s, P.r, P.z, P.sc));
         OD_KL(s);
         pcg_rz_kernel<<<g_vec, kThreads, 0, strm>>>(n, P.r, P.z, part_c, P.sc);
@@ -2348,6 +2390,7 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
     if (P.sc_host->done) break;
   }
   if (pk == OD_PRECOND_LDLT || pk == OD_PRECOND_IC) OD_TRY(sweep_check(s));
+  if (pk == OD_PRECOND_IC0) OD_TRY(ic0_check(s));
   return pcg_finish(s, d_b, d_x, shift, st, false, false);
 }
 

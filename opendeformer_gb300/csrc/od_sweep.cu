@@ -12,23 +12,29 @@
 //   backward : L by columns (the reference's order)     -> L^T z = y
 //   LDL^T    : y_j = r_j - sum L_jc y_c;          z_i = y_i D_ii^-1 - sum z_r L_ri
 //   IC       : y_j = (r_j - sum L_jc y_c) / L_jj;  z_i = (y_i - sum z_r L_ri) / L_ii
-// and applied by one cooperative launch per apply.  Rows are listed by
-// dependency level (level of a row = 1 + the highest level of the rows it
-// reads; forward and backward levels apart), and warp w of the W
-// co-resident warps takes entries w, w+W, ... of the forward list, then of
-// the backward list.  y and z are filled with an all-ones NaN before the
-// launch (a pattern no arithmetic result has); a row waits (bounded) until
-// the values it reads are no longer that pattern, read with acquire loads,
-// and publishes its own value with one release store: the value is its
-// own ready flag.  Progress: the first unfinished entry of a list is at the
-// head of its warp's queue and reads only rows of lower levels, listed
-// before it and so finished; every warp finishes its forward entries
-// before its first backward wait.
+// and applied by one cooperative launch per apply.  Rows go in triples
+// [3g, 3g + 3) (a node's three DOFs, which depend on one another in a
+// chain, when they are numbered consecutively); triples are listed by
+// dependency level (level of a triple = 1 + the highest level of the
+// triples it reads outside itself; forward and backward levels apart), and
+// warp w of the W co-resident warps takes entries w, w+W, ... of the
+// forward list, then of the backward list.  y and z are filled with an
+// all-ones NaN before the launch (a pattern no arithmetic result has); a
+// warp waits (bounded) until the values it reads outside its triple are no
+// longer that pattern, read with acquire loads, resolves the triple's own
+// chain in registers and publishes each value with one release store: the
+// value is its own ready flag.  Progress: the first unfinished entry of a
+// list is at the head of its warp's queue and reads only triples of lower
+// levels, listed before it and so finished; every warp finishes its forward
+// entries before its first backward wait.  Taking triples rather than rows
+// cuts the dependency chain (and the apply time) about three-fold on
+// meshes whose node DOFs are consecutive.
 //
 // Dependent FP64 operations cost 64 cycles each on this part (a shuffle
-// plus an add about 108), so a row's products are summed by a fixed
-// 5-level butterfly over the warp rather than one after another: the result
-// is deterministic and within rounding of the reference's sequential sums.
+// plus an add about 108), so the products are summed by fixed 5-level
+// butterflies over the warp (three interleaved, one per row of the triple)
+// rather than one after another: the result is deterministic and within
+// rounding of the reference's sequential sums.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -52,10 +58,11 @@ struct SweepSys {
   double* lo_host = nullptr;         // pinned mirror
   int *f_rp = nullptr, *f_ci = nullptr, *b_cp = nullptr, *b_ri = nullptr;
   int *ord_f = nullptr, *ord_b = nullptr;   // rows by forward / backward level
-  double *f_val = nullptr, *b_val = nullptr, *diag = nullptr, *y = nullptr;
+  double *f_val = nullptr, *b_val = nullptr, *y = nullptr;
+  double* diag = nullptr;            // D^-1 (LDL^T) or 1 / L_ii (IC)
   int *err = nullptr, *err_host = nullptr;
   int grid = 0;                      // co-resident CTAs of the apply
-  int depth_f = 0, depth_b = 0;      // longest dependency chains of the two sweeps (rows)
+  int depth_f = 0, depth_b = 0;      // dependency levels of the two sweeps (row triples)
   // host staging of the sweep arrays
   std::vector<int> h_rp, h_ci, h_cp, h_ri, h_of, h_ob;
   std::vector<double> h_fval, h_bval, h_diag;
@@ -67,87 +74,215 @@ constexpr int kSweepThreads = 256;
 constexpr unsigned kSweepSpinLimit = 1u << 21;
 constexpr unsigned long long kPending = 0xffffffffffffffffull;   // "not yet written" (a NaN)
 
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const double* p) {
+// The value is its own ready flag and nothing else is read through it, so
+// relaxed GPU-scope 64-bit accesses suffice (single-copy atomic: a reader
+// sees the pending pattern or the value) and no fence orders a store
+// behind the previous one.
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const double* p) {
   unsigned long long v;
-  asm volatile("ld.acquire.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
 
-__device__ __forceinline__ void st_release_f64(double* p, double x) {
-  asm volatile("st.release.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(__double_as_longlong(x)) : "memory");
+__device__ __forceinline__ void st_relaxed_f64(double* p, double x) {
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(__double_as_longlong(x)) : "memory");
 }
 
-// bounded wait for *p to be written; after a timeout anywhere (err set) no
-// thread waits any more, so the launch ends promptly and the host reports it
-__device__ __forceinline__ double wait_value(const double* p, int* err) {
-  unsigned long long v = ld_acquire_u64(p);
-  for (unsigned k = 1; v == kPending && k < kSweepSpinLimit; k++) {
+// bounded wait until v (first read of *p) is written; after a timeout
+// anywhere (err set) no thread waits any more, so the launch ends promptly
+// and the host reports it
+__device__ __forceinline__ double finish_wait(unsigned long long v, const double* p, int* err) {
+  for (unsigned k = 1; v == kPending; k++) {
+    if (k >= kSweepSpinLimit) {
+      atomicOr(err, 1);
+      return 0.0;
+    }
     if ((k & 1023u) == 0 && *(volatile int*)err) return 0.0;
-    v = ld_acquire_u64(p);
-  }
-  if (v == kPending) {
-    atomicOr(err, 1);
-    return 0.0;
+    v = ld_relaxed_u64(p);
   }
   return __longlong_as_double((long long)v);
 }
 
-__device__ __forceinline__ double warp_sum(double x) {
-  for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-  return x;
+constexpr int kSweepBatch = 4;   // entries per lane with their value loads in flight together
+constexpr unsigned kSweepPollBurst = 1024;   // polls of one value between checks of the error flag
+
+// Sums, per row k of the triple [i0, i0 + m), of the products of its
+// entries [rb0, rb3) (row k owns [rb_k, rb_k+1)) with the values of vec
+// outside the triple (forward: index < i0; backward: index >= i0 + m);
+// the entries inside the triple go to the warp's slots in[] (L_10, L_20,
+// L_21).  Each lane loads kSweepBatch entries, then their values together.
+template <bool FWD>
+__device__ __forceinline__ void triple_sums(int rb0, int rb1, int rb2, int rb3, int i0, int m,
+                                            const int* __restrict__ idx, const double* __restrict__ val,
+                                            const double* vec, double* in, int* err, int lane, double& a0,
+                                            double& a1, double& a2) {
+  for (int q0 = rb0; q0 < rb3; q0 += 32 * kSweepBatch) {
+    int ix[kSweepBatch], kr[kSweepBatch];
+    double lv[kSweepBatch];
+    unsigned long long v[kSweepBatch];
+#pragma unroll
+    for (int u = 0; u < kSweepBatch; u++) {
+      const int q = q0 + u * 32 + lane;
+      ix[u] = -1;
+      kr[u] = 0;
+      lv[u] = 0.0;
+      if (q < rb3) {
+        const int c = idx[q];
+        const double l = val[q];
+        const int k = q < rb1 ? 0 : (q < rb2 ? 1 : 2);
+        if (FWD ? c < i0 : c >= i0 + m) {
+          ix[u] = c;
+          kr[u] = k;
+          lv[u] = l;
+        } else {
+          in[FWD ? k + (c - i0) - 1 : (c - i0) + k - 1] = l;   // (1,0) -> 0, (2,0) -> 1, (2,1) -> 2
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kSweepBatch; u++) v[u] = ix[u] >= 0 ? ld_relaxed_u64(vec + ix[u]) : 0ull;
+    // warp-cooperative wait: one lane polls the first value still pending
+    // in the warp, then every lane re-reads its pending values once; the
+    // values of one level land together, so one or two rounds usually do,
+    // and the polls (which queue in front of the stores they wait for)
+    // stay one per warp
+    for (unsigned round = 1;; round++) {
+      int pu = -1;
+#pragma unroll
+      for (int u = kSweepBatch - 1; u >= 0; u--)
+        if (ix[u] >= 0 && v[u] == kPending) pu = u;
+      const unsigned ball = __ballot_sync(0xffffffffu, pu >= 0);
+      if (!ball) break;
+      int stop = 0;
+      if (lane == __ffs(ball) - 1) {
+        const double* p = vec;
+#pragma unroll
+        for (int u = 0; u < kSweepBatch; u++)
+          if (u == pu) p += ix[u];
+        unsigned k = 0;
+        while (ld_relaxed_u64(p) == kPending && ++k < kSweepPollBurst) {
+        }
+        stop = round >= kSweepSpinLimit / kSweepPollBurst || *(volatile int*)err;
+        if (round >= kSweepSpinLimit / kSweepPollBurst) atomicOr(err, 1);
+      }
+      if (__any_sync(0xffffffffu, stop)) {
+#pragma unroll
+        for (int u = 0; u < kSweepBatch; u++)
+          if (v[u] == kPending) v[u] = 0ull;
+        break;
+      }
+#pragma unroll
+      for (int u = 0; u < kSweepBatch; u++)
+        if (ix[u] >= 0 && v[u] == kPending) v[u] = ld_relaxed_u64(vec + ix[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < kSweepBatch; u++) {
+      if (ix[u] < 0) continue;
+      const double p = lv[u] * __longlong_as_double((long long)v[u]);
+      if (kr[u] == 0) a0 += p;
+      else if (kr[u] == 1) a1 += p;
+      else a2 += p;
+    }
+  }
 }
 
-// IC = 0: LDL^T (diag = D^-1), IC = 1: Cholesky (diag = L_ii)
+// IC = 0: LDL^T (dinv = D^-1), IC = 1: Cholesky (dinv = 1 / L_ii).  Rows go
+// in triples [3g, 3g + 3) (a node's three DOFs when those are consecutive):
+// a warp sums the products of all three rows with values outside the
+// triple (three interleaved butterflies), then lane 0 resolves the chain
+// inside the triple in registers and publishes the three values.
 template <int IC>
-__global__ void __launch_bounds__(kSweepThreads) sweep_apply_kernel(
-    int n, int n_pad, const int* __restrict__ frp, const int* __restrict__ fci, const double* __restrict__ fval,
-    const int* __restrict__ bcp, const int* __restrict__ bri, const double* __restrict__ bval,
-    const int* __restrict__ ord_f, const int* __restrict__ ord_b, const double* __restrict__ diag,
-    const double* __restrict__ r, double* y, double* z, int* __restrict__ err, const SolveScalars* sc) {
+__global__ void __launch_bounds__(kSweepThreads, 2) sweep_apply_kernel(
+    int n, int n_pad, int ng, const int* __restrict__ frp, const int* __restrict__ fci,
+    const double* __restrict__ fval, const int* __restrict__ bcp, const int* __restrict__ bri,
+    const double* __restrict__ bval, const int* __restrict__ ord_f, const int* __restrict__ ord_b,
+    const double* __restrict__ dinv, const double* __restrict__ r, double* y, double* z, int* __restrict__ err,
+    const SolveScalars* sc) {
+  __shared__ double inner_s[kSweepThreads / 32][3];
   if (sc && *(volatile const int*)&sc->done) return;
   const int lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
   const int W = gridDim.x * wpb;
   const int w = blockIdx.x * wpb + (threadIdx.x >> 5);
+  double* in = inner_s[threadIdx.x >> 5];
   // padding rows carry the identity
   for (int i = n + blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += gridDim.x * blockDim.x) z[i] = r[i];
 
-  // forward
-  for (int t = w; t < n; t += W) {
-    const int j = ord_f[t];
-    double s = r[j];
-    const int e = frp[j + 1];
-    for (int q0 = frp[j]; q0 < e; q0 += 32) {
-      const int q = q0 + lane;
-      double prod = 0.0;
-      if (q < e) {
-        const int c = fci[q];
-        const double l = fval[q];
-        prod = l * wait_value(y + c, err);
+  // forward: y_j = r_j - sum_c L_jc y_c (times 1 / L_jj for IC)
+  for (int t = w; t < ng; t += W) {
+    const int g = ord_f[t];
+    const int i0 = 3 * g, m = min(3, n - i0);
+    const int rb0 = frp[i0], rb1 = frp[i0 + 1], rb2 = frp[i0 + min(2, m)], rb3 = frp[i0 + m];
+    double rv[3] = {0.0, 0.0, 0.0}, dv[3] = {0.0, 0.0, 0.0};
+    if (lane == 0)
+      for (int k = 0; k < m; k++) {
+        rv[k] = r[i0 + k];
+        dv[k] = IC ? dinv[i0 + k] : 1.0;
       }
-      s -= warp_sum(prod);
+    __syncwarp();
+    if (lane < 3) in[lane] = 0.0;
+    __syncwarp();
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    triple_sums<true>(rb0, rb1, rb2, rb3, i0, m, fci, fval, y, in, err, lane, a0, a1, a2);
+    for (int o = 16; o; o >>= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
     }
-    if (lane == 0) st_release_f64(y + j, IC ? s / diag[j] : s);
+    __syncwarp();
+    if (lane == 0) {
+      const double y0 = IC ? (rv[0] - a0) * dv[0] : rv[0] - a0;
+      st_relaxed_f64(y + i0, y0);
+      if (m > 1) {
+        const double s1 = rv[1] - a1 - in[0] * y0;
+        const double y1 = IC ? s1 * dv[1] : s1;
+        st_relaxed_f64(y + i0 + 1, y1);
+        if (m > 2) {
+          const double s2 = rv[2] - a2 - in[1] * y0 - in[2] * y1;
+          st_relaxed_f64(y + i0 + 2, IC ? s2 * dv[2] : s2);
+        }
+      }
+    }
   }
 
-  // backward
-  for (int t = w; t < n; t += W) {
-    const int i = ord_b[t];
-    const int e = bcp[i + 1];
-    double dot = 0.0;
-    for (int q0 = bcp[i]; q0 < e; q0 += 32) {
-      const int q = q0 + lane;
-      double prod = 0.0;
-      if (q < e) {
-        const int rr = bri[q];
-        const double l = bval[q];
-        prod = wait_value(z + rr, err) * l;
-      }
-      dot += warp_sum(prod);
-    }
+  // backward: z_i = (y_i - sum_r z_r L_ri) / L_ii (IC), y_i D_ii^-1 - sum_r z_r L_ri (LDL^T)
+  for (int t = w; t < ng; t += W) {
+    const int g = ord_b[t];
+    const int i0 = 3 * g, m = min(3, n - i0);
+    const int cb0 = bcp[i0], cb1 = bcp[i0 + 1], cb2 = bcp[i0 + min(2, m)], cb3 = bcp[i0 + m];
+    double yv[3] = {0.0, 0.0, 0.0}, dv[3] = {0.0, 0.0, 0.0};
     if (lane == 0) {
-      const double yi = wait_value(y + i, err);
-      st_release_f64(z + i, IC ? (yi - dot) / diag[i] : yi * diag[i] - dot);
+      unsigned long long v[3] = {0ull, 0ull, 0ull};
+      for (int k = 0; k < m; k++) {
+        v[k] = ld_relaxed_u64(y + i0 + k);
+        dv[k] = dinv[i0 + k];
+      }
+      for (int k = 0; k < m; k++) yv[k] = finish_wait(v[k], y + i0 + k, err);
+    }
+    __syncwarp();
+    if (lane < 3) in[lane] = 0.0;
+    __syncwarp();
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    triple_sums<false>(cb0, cb1, cb2, cb3, i0, m, bri, bval, z, in, err, lane, a0, a1, a2);
+    for (int o = 16; o; o >>= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      double z2 = 0.0, z1 = 0.0;
+      if (m > 2) {
+        z2 = IC ? (yv[2] - a2) * dv[2] : yv[2] * dv[2] - a2;
+        st_relaxed_f64(z + i0 + 2, z2);
+      }
+      if (m > 1) {
+        const double e1 = a1 + z2 * in[2];
+        z1 = IC ? (yv[1] - e1) * dv[1] : yv[1] * dv[1] - e1;
+        st_relaxed_f64(z + i0 + 1, z1);
+      }
+      const double e0 = a0 + z1 * in[0] + z2 * in[1];
+      st_relaxed_f64(z + i0, IC ? (yv[0] - e0) * dv[0] : yv[0] * dv[0] - e0);
     }
   }
 }
@@ -190,8 +325,58 @@ od_status sweep_alloc(Scene* s) {
   OD_CUDA(cudaMemset(l->err, 0, sizeof(int)));
   OD_CUDA(cudaMallocHost(&l->err_host, sizeof(int)));
   s->device_bytes += (long long)sizeof(double) * l->nvals + (long long)(sizeof(int) * 4 + sizeof(double) * 2) * n;
-  // co-resident CTAs for the cooperative apply (both instantiations share
-  // the launch bounds; the smaller occupancy is used)
+  return sweep_grid(s, n, &l->grid);
+}
+
+}  // namespace
+
+// Dependency levels of row triples [3g, 3g + 3): a triple's forward level is
+// 1 + the highest level of the triples its rows read below it (entries
+// inside the triple are resolved by the warp that takes it), likewise
+// backward through the columns; triples listed by level (a counting sort;
+// forward ties by ascending triple, backward by descending).  depth = levels.
+void sweep_group_levels(int n, const std::vector<int>& frp, const std::vector<int>& fci, const std::vector<int>& bcp,
+                        const std::vector<int>& bri, std::vector<int>& ord_f, std::vector<int>& ord_b, int* depth_f,
+                        int* depth_b) {
+  const int ng = (n + 2) / 3;
+  std::vector<int> lev(ng, 0);
+  auto list_by_level = [&](int depth, bool ascending, std::vector<int>& ord) {
+    std::vector<int> start(depth + 1, 0);
+    for (int g = 0; g < ng; g++) start[lev[g] + 1]++;
+    for (int k = 0; k < depth; k++) start[k + 1] += start[k];
+    ord.resize(ng);
+    for (int t = 0; t < ng; t++) {
+      const int g = ascending ? t : ng - 1 - t;
+      ord[start[lev[g]]++] = g;
+    }
+  };
+  int df = 0, db = 0;
+  for (int g = 0; g < ng; g++) {
+    const int i0 = 3 * g, i1 = std::min(n, i0 + 3);
+    int m = 0;
+    for (int q = frp[i0]; q < frp[i1]; q++)
+      if (fci[q] < i0) m = std::max(m, lev[fci[q] / 3] + 1);
+    lev[g] = m;
+    df = std::max(df, m + 1);
+  }
+  list_by_level(df, true, ord_f);
+  std::fill(lev.begin(), lev.end(), 0);
+  for (int g = ng - 1; g >= 0; g--) {
+    const int i0 = 3 * g, i1 = std::min(n, i0 + 3);
+    int m = 0;
+    for (int q = bcp[i0]; q < bcp[i1]; q++)
+      if (bri[q] >= i1) m = std::max(m, lev[bri[q] / 3] + 1);
+    lev[g] = m;
+    db = std::max(db, m + 1);
+  }
+  list_by_level(db, false, ord_b);
+  *depth_f = ng > 0 ? df : 0;
+  *depth_b = ng > 0 ? db : 0;
+}
+
+// co-resident CTAs for the cooperative apply of an n-row factor (both
+// instantiations share the launch bounds; the smaller occupancy is used)
+od_status sweep_grid(Scene* s, int n, int* grid) {
   int dev_coop = 0, per0 = 0, per1 = 0;
   OD_CUDA(cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, s->ctx->device));
   OD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, sweep_apply_kernel<0>, kSweepThreads, 0));
@@ -201,14 +386,17 @@ od_status sweep_alloc(Scene* s) {
     set_error("the triangular-sweep apply needs cooperative launch");
     return OD_ERR_UNSUPPORTED;
   }
-  // two CTAs (16 warps) per SM: each level's rows spread over 4864 warps;
-  // more warps only add polling traffic
-  int per = 2;
+  // one CTA (8 warps) per SM: 1,216 warps hold a level's triples (tens of
+  // them on the 98k-tet beam) many times over; measured 4% faster than two
+  // CTAs per SM and 6% faster than three
+  int per = 1;
   if (const char* e = std::getenv("OD_GB300_SWEEP_CTAS_PER_SM")) per = std::max(1, std::atoi(e));
-  const int want = (n + (kSweepThreads / 32) - 1) / (kSweepThreads / 32);   // one warp per row at most
-  l->grid = std::max(1, std::min(std::min(per, per_sm) * s->ctx->num_sms, want));
+  const int want = ((n + 2) / 3 + (kSweepThreads / 32) - 1) / (kSweepThreads / 32);   // one warp per triple at most
+  *grid = std::max(1, std::min(std::min(per, per_sm) * s->ctx->num_sms, want));
   return OD_OK;
 }
+
+namespace {
 
 // A on the host in the reference's lower layout: given, or rebuilt from
 // the last expansion on the device
@@ -258,39 +446,7 @@ od_status upload(Scene* s, SweepSys* l, int kind) {
         l->h_fval[at] = l->h_bval[q];
       }
   }
-  // dependency levels of the two sweeps and the rows listed by level (a
-  // counting sort; forward ties by ascending row, backward by descending)
-  {
-    std::vector<int> lev(n, 0);
-    auto list_by_level = [&](int depth, bool ascending, std::vector<int>& ord) {
-      std::vector<int> start(depth + 1, 0);
-      for (int i = 0; i < n; i++) start[lev[i] + 1]++;
-      for (int k = 0; k < depth; k++) start[k + 1] += start[k];
-      ord.resize(n);
-      for (int t = 0; t < n; t++) {
-        const int i = ascending ? t : n - 1 - t;
-        ord[start[lev[i]]++] = i;
-      }
-    };
-    int df = 0, db = 0;
-    for (int j = 0; j < n; j++) {
-      int m = 0;
-      for (int q = l->h_rp[j]; q < l->h_rp[j + 1]; q++) m = std::max(m, lev[l->h_ci[q]] + 1);
-      lev[j] = m;
-      df = std::max(df, m + 1);
-    }
-    list_by_level(df, true, l->h_of);
-    std::fill(lev.begin(), lev.end(), 0);
-    for (int i = n - 1; i >= 0; i--) {
-      int m = 0;
-      for (int q = l->h_cp[i]; q < l->h_cp[i + 1]; q++) m = std::max(m, lev[l->h_ri[q]] + 1);
-      lev[i] = m;
-      db = std::max(db, m + 1);
-    }
-    list_by_level(db, false, l->h_ob);
-    l->depth_f = df;
-    l->depth_b = db;
-  }
+  sweep_group_levels(n, l->h_rp, l->h_ci, l->h_cp, l->h_ri, l->h_of, l->h_ob, &l->depth_f, &l->depth_b);
   cudaStream_t strm = s->ctx->stream;
   if (nnz > l->cap) {
     long long cap = std::max(nnz, l->cap + l->cap / 2);
@@ -306,8 +462,8 @@ od_status upload(Scene* s, SweepSys* l, int kind) {
     OD_CUDA(cudaMemcpyAsync(l->f_rp, l->h_rp.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, strm));
     OD_CUDA(cudaMemcpyAsync(l->b_cp, l->h_cp.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, strm));
     OD_CUDA(cudaMemcpyAsync(l->diag, l->h_diag.data(), sizeof(double) * n, cudaMemcpyHostToDevice, strm));
-    OD_CUDA(cudaMemcpyAsync(l->ord_f, l->h_of.data(), sizeof(int) * n, cudaMemcpyHostToDevice, strm));
-    OD_CUDA(cudaMemcpyAsync(l->ord_b, l->h_ob.data(), sizeof(int) * n, cudaMemcpyHostToDevice, strm));
+    OD_CUDA(cudaMemcpyAsync(l->ord_f, l->h_of.data(), sizeof(int) * l->h_of.size(), cudaMemcpyHostToDevice, strm));
+    OD_CUDA(cudaMemcpyAsync(l->ord_b, l->h_ob.data(), sizeof(int) * l->h_ob.size(), cudaMemcpyHostToDevice, strm));
   }
   if (nnz > 0) {
     OD_CUDA(cudaMemcpyAsync(l->f_ci, l->h_ci.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, strm));
@@ -375,7 +531,7 @@ od_status ic_factor(Scene* s, const double* host_values, double eps, double rela
   l->h_bval.clear();
   l->h_diag.assign(n, 0.0);
   for (int c = 0; c < n; c++) {
-    l->h_diag[c] = F.val[F.pcol[c]];
+    l->h_diag[c] = 1.0 / F.val[F.pcol[c]];   // the apply multiplies by 1 / L_cc
     for (int q = F.pcol[c] + 1; q < F.pcol[c + 1]; q++) {
       l->h_ri.push_back(F.row[q]);
       l->h_bval.push_back(F.val[q]);
@@ -387,39 +543,34 @@ od_status ic_factor(Scene* s, const double* host_values, double eps, double rela
   return OD_OK;
 }
 
-od_status sweep_apply(Scene* s, const double* r, double* z, const SolveScalars* sc) {
-  SweepSys* l = s->pcg.sweep;
-  if (!l || l->kind < 0) {
-    set_error("triangular-sweep apply without a factor");
-    return OD_ERR_INTERNAL;
-  }
+od_status sweep_launch(Scene* s, const SweepView& v, const double* r, double* z, const SolveScalars* sc) {
   Ctx* ctx = s->ctx;
   cudaStream_t strm = ctx->stream;
-  int n = l->n, n_pad = l->n_pad;
+  int n = v.n, n_pad = v.n_pad, ng = (v.n + 2) / 3;
   const bool prof = ctx->profiling && ctx->ev_pool.size() >= 2;
   if (prof) OD_CUDA(cudaEventRecord(ctx->ev_pool[ctx->ev_pool.size() - 2], strm));
-  const int* frp = l->f_rp;
-  const int* fci = l->f_ci;
-  const double* fval = l->f_val;
-  const int* bcp = l->b_cp;
-  const int* bri = l->b_ri;
-  const double* bval = l->b_val;
-  const int* of = l->ord_f;
-  const int* ob = l->ord_b;
-  const double* dg = l->diag;
-  double* y = l->y;
-  int* err = l->err;
-  void* args[] = {(void*)&n,   (void*)&n_pad, (void*)&frp, (void*)&fci, (void*)&fval, (void*)&bcp,
-                  (void*)&bri, (void*)&bval,  (void*)&of,  (void*)&ob,  (void*)&dg,   (void*)&r,
-                  (void*)&y,   (void*)&z,     (void*)&err, (void*)&sc};
+  const int* frp = v.frp;
+  const int* fci = v.fci;
+  const double* fval = v.fval;
+  const int* bcp = v.bcp;
+  const int* bri = v.bri;
+  const double* bval = v.bval;
+  const int* of = v.ord_f;
+  const int* ob = v.ord_b;
+  const double* dg = v.diag;
+  double* y = v.y;
+  int* err = v.err;
+  void* args[] = {(void*)&n,    (void*)&n_pad, (void*)&ng,  (void*)&frp, (void*)&fci, (void*)&fval,
+                  (void*)&bcp,  (void*)&bri,   (void*)&bval, (void*)&of,  (void*)&ob,  (void*)&dg,
+                  (void*)&r,    (void*)&y,     (void*)&z,   (void*)&err, (void*)&sc};
   // every value starts "not yet written" (all-ones bytes)
   if (n > 0) {
     OD_CUDA(cudaMemsetAsync(y, 0xff, sizeof(double) * (size_t)n, strm));
     OD_CUDA(cudaMemsetAsync(z, 0xff, sizeof(double) * (size_t)n, strm));
   }
   OD_KL(s);
-  void* fn = l->kind == OD_PRECOND_IC ? (void*)sweep_apply_kernel<1> : (void*)sweep_apply_kernel<0>;
-  OD_CUDA(cudaLaunchCooperativeKernel(fn, dim3(l->grid), dim3(kSweepThreads), args, 0, strm));
+  void* fn = v.ic ? (void*)sweep_apply_kernel<1> : (void*)sweep_apply_kernel<0>;
+  OD_CUDA(cudaLaunchCooperativeKernel(fn, dim3(v.grid), dim3(kSweepThreads), args, 0, strm));
   if (prof) {
     OD_CUDA(cudaEventRecord(ctx->ev_pool[ctx->ev_pool.size() - 1], strm));
     OD_CUDA(cudaEventSynchronize(ctx->ev_pool[ctx->ev_pool.size() - 1]));
@@ -435,10 +586,36 @@ od_status sweep_apply(Scene* s, const double* r, double* z, const SolveScalars* 
     if (ran) {
       ctx->sweep_applies++;
       ctx->sweep_apply_ms += ms;
-      ctx->sweep_apply_bytes += 2.0 * 12.0 * (double)l->nnz + 56.0 * n;
+      ctx->sweep_apply_bytes += 2.0 * 12.0 * (double)v.nnz + 56.0 * n;
     }
   }
   return OD_OK;
+}
+
+od_status sweep_apply(Scene* s, const double* r, double* z, const SolveScalars* sc) {
+  SweepSys* l = s->pcg.sweep;
+  if (!l || l->kind < 0) {
+    set_error("triangular-sweep apply without a factor");
+    return OD_ERR_INTERNAL;
+  }
+  SweepView v;
+  v.n = l->n;
+  v.n_pad = l->n_pad;
+  v.ic = l->kind == OD_PRECOND_IC ? 1 : 0;
+  v.grid = l->grid;
+  v.nnz = l->nnz;
+  v.frp = l->f_rp;
+  v.fci = l->f_ci;
+  v.fval = l->f_val;
+  v.bcp = l->b_cp;
+  v.bri = l->b_ri;
+  v.bval = l->b_val;
+  v.ord_f = l->ord_f;
+  v.ord_b = l->ord_b;
+  v.diag = l->diag;
+  v.y = l->y;
+  v.err = l->err;
+  return sweep_launch(s, v, r, z, sc);
 }
 
 od_status sweep_check(Scene* s) {
