@@ -225,10 +225,11 @@ def test_mixed_precision_solve_reaches_fp64_tolerance(golden, precond):
     assert rel_err(xm, x64) <= 1e-8
 
 
-def test_mixed_precision_newmark_within_1e6_of_fp64():
+@pytest.mark.parametrize("kind", ["neohookean", "stvk"])
+def test_mixed_precision_newmark_within_1e6_of_fp64(kind):
     g = meshgen.tet_grid(12, 4, 4, h=0.05, jitter=0.15, seed=2)
     cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
-    mat = api.InvertibleNeoHookeanMaterial(1000.0, 98640.0, 0.4506, 0.1)
+    mat = material(kind, 1000.0, 98640.0, 0.4506, 0.1)
     out = {}
     for prec in ("fp64", "mixed"):
         s = api.Scene(ctx(), g.X, g.tets, g.facets, cd, mat)
