@@ -39,6 +39,23 @@ __device__ __forceinline__ int barrier_arrive_wait(GridBarrier* gb) {
   return ok && !*(volatile int*)&gb->timeout;
 }
 
+// Values that double as their own ready flags: filled with an all-ones NaN
+// (a pattern no arithmetic result has) before a launch and published once.
+// Nothing else is read through such a value, so relaxed GPU-scope 64-bit
+// accesses suffice (single-copy atomic: a reader sees the pending pattern
+// or the value) and no fence orders a store behind the previous one.
+constexpr unsigned long long kPending = 0xffffffffffffffffull;
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const double* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_relaxed_f64(double* p, double x) {
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(__double_as_longlong(x)) : "memory");
+}
+
 __device__ __forceinline__ bool grid_barrier(GridBarrier* gb) {
   __shared__ int ok_s;
   __syncthreads();

@@ -100,6 +100,14 @@ struct Pcg {
   int* ic_err = nullptr;        // a bounded wait ran out
   int* ic_err_host = nullptr;   // pinned
   int ic_grid = 0;
+  // one-launch factorisation: per off-diagonal entry (i, j) the pairs
+  // (L_ik, L_jk), k < j, as (position in row i, global position in row j)
+  int* ic_pp = nullptr;         // ic_nnz + 1
+  int* ic_pa = nullptr;
+  int* ic_pb = nullptr;
+  int ic_fgrid = 0;             // co-resident CTAs; 0: one launch per level
+  int ic_fmaxrow = 0, ic_fmaxpairs = 0;
+  size_t ic_fsmem = 0;          // dynamic shared memory per CTA
   int* ic_gord_f = nullptr;     // row triples by forward / backward level
   int* ic_gord_b = nullptr;
   int ic_gdepth = 0;            // levels of the two sweeps

@@ -1470,6 +1470,113 @@ __global__ void ic0_factor_level(int l0, int l1, const int* __restrict__ rows, c
   }
 }
 
+// IC(0) factorisation in one cooperative launch: rows listed by forward
+// level, one warp per row.  The warp first reads every value of other rows
+// the row needs -- for each off-diagonal entry (i, j) the L_jk paired with
+// the row's own L_ik (k < j), and L_jj -- into shared memory, each waited
+// for (bounded) until it is no longer the pending pattern; then it forms
+// its entries in order from shared memory:
+//   L_ij = (A_ij - sum_k L_ik L_jk) / L_jj,   L_ii = sqrt((1 + shift) A_ii - sum_k L_ik^2)
+// with the breakdown test of ic0_factor_level, and publishes each value
+// (relaxed store; the value is its own ready flag).
+constexpr int kIcfThreads = 128;
+constexpr int kIcfWarps = kIcfThreads / 32;
+constexpr unsigned kIcfSpinLimit = 1u << 21;
+
+constexpr unsigned kIcfPollBurst = 1024;
+
+// warp-cooperative bounded read of one value per lane (p null: none): one
+// lane polls the first value still pending in the warp, then every lane
+// re-reads its own once, so waiting warps send one poll at a time; called
+// by all 32 lanes
+__device__ __forceinline__ double icf_warp_read(const double* p, int* err) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long v = p ? ld_relaxed_u64(p) : 0ull;
+  for (unsigned round = 1;; round++) {
+    const bool pend = p && v == kPending;
+    const unsigned ball = __ballot_sync(0xffffffffu, pend);
+    if (!ball) break;
+    int stop = 0;
+    if (lane == __ffs(ball) - 1) {
+      unsigned k = 0;
+      while (ld_relaxed_u64(p) == kPending && ++k < kIcfPollBurst) {
+      }
+      stop = round >= kIcfSpinLimit / kIcfPollBurst || *(volatile int*)err;
+      if (round >= kIcfSpinLimit / kIcfPollBurst) atomicOr(err, 1);
+    }
+    if (__any_sync(0xffffffffu, stop)) {
+      if (pend) v = 0ull;
+      break;
+    }
+    if (pend) v = ld_relaxed_u64(p);
+  }
+  return __longlong_as_double((long long)v);
+}
+
+__global__ void __launch_bounds__(kIcfThreads) ic0_factor_coop_kernel(
+    int n, const int* __restrict__ rows, const int* __restrict__ rp, const int* __restrict__ ci,
+    const int* __restrict__ src, const double* __restrict__ A, const int* __restrict__ pp,
+    const int* __restrict__ pa, const int* __restrict__ pb, double* L, double shift, int maxrow, int maxpairs,
+    int* __restrict__ bad, int* __restrict__ err) {
+  extern __shared__ double icf_s[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  double* rowL = icf_s + (size_t)wib * (3 * maxrow + maxpairs);
+  double* aval = rowL + maxrow;
+  double* dval = aval + maxrow;
+  double* pv = dval + maxrow;
+  const int W = gridDim.x * kIcfWarps;
+  for (int t = blockIdx.x * kIcfWarps + wib; t < n; t += W) {
+    const int i = rows[t];
+    const int bi = rp[i], m = rp[i + 1] - bi;
+    const int p0 = pp[bi], np = pp[bi + m] - p0;
+    __syncwarp();
+    for (int q0 = 0; q0 < m; q0 += 32) {
+      const int q = q0 + lane;
+      const double* dp = nullptr;
+      if (q < m) {
+        aval[q] = A[src[bi + q]];
+        const int j = ci[bi + q];
+        if (j < i) dp = L + rp[j + 1] - 1;
+      }
+      const double d = icf_warp_read(dp, err);
+      if (q < m) dval[q] = dp ? d : 1.0;
+    }
+    for (int b0 = 0; b0 < np; b0 += 32) {
+      const int p = b0 + lane;
+      const double v = icf_warp_read(p < np ? L + pb[p0 + p] : nullptr, err);
+      if (p < np) pv[p] = v;
+    }
+    __syncwarp();
+    for (int q = 0; q < m; q++) {
+      double s = 0.0;
+      if (q < m - 1) {
+        const int a1 = pp[bi + q + 1] - p0;
+        for (int p = pp[bi + q] - p0 + lane; p < a1; p += 32) s += rowL[pa[p0 + p]] * pv[p];
+      } else {
+        for (int k = lane; k < m - 1; k += 32) s += rowL[k] * rowL[k];
+      }
+      for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) {
+        double v;
+        if (q < m - 1) {
+          v = (aval[q] - s) / dval[q];
+        } else {
+          const double d = aval[q] * (1.0 + shift);
+          double sum = d - s;
+          if (!(sum > 1e-12 * d)) {
+            *bad = 1;
+            sum = d > 0.0 ? d : 1.0;
+          }
+          v = sqrt(sum);
+        }
+        rowL[q] = v;
+        st_relaxed_f64(L + bi + q, v);
+      }
+      __syncwarp();
+    }
+  }
+}
+
 // the IC(0) factor (rows, diagonal last) split for the one-launch sweeps:
 // strictly lower rows, values in transposed order, reciprocal diagonal
 __global__ void ic0_split_kernel(int n, const int* __restrict__ rp, const int* __restrict__ frp,
@@ -1608,6 +1715,36 @@ static od_status ic0_build(Scene* s) {
     for (int q = trp[i]; q < fill[i]; q++) { tci2.push_back(tci[q]); tpos2.push_back(tpos[q]); }
     trp2[i + 1] = (int)tci2.size();
   }
+  // pair lists of the one-launch factorisation (merge of row i before the
+  // entry with row j without its diagonal, as ic0_factor_level walks them)
+  std::vector<int> pp(nnz + 1, 0), pa, pb;
+  int maxrow = 0, maxpairs = 0;
+  for (int i = 0; i < n; i++) {
+    const int bi = srp[i], ei = srp[i + 1];
+    maxrow = std::max(maxrow, ei - bi);
+    const size_t row0 = pa.size();
+    for (int q = bi; q < ei; q++) {
+      const int j = sci[q];
+      if (j < i) {
+        int a = bi, b = srp[j];
+        const int eb = srp[j + 1] - 1;
+        while (a < q && b < eb) {
+          if (sci[a] == sci[b]) {
+            pa.push_back(a - bi);
+            pb.push_back(b);
+            a++;
+            b++;
+          } else if (sci[a] < sci[b]) {
+            a++;
+          } else {
+            b++;
+          }
+        }
+      }
+      pp[q + 1] = (int)pa.size();
+    }
+    maxpairs = std::max(maxpairs, (int)(pa.size() - row0));
+  }
   // strictly lower rows for the forward sweep
   std::vector<int> frp(n + 1, 0), fci;
   fci.reserve(nnz);
@@ -1645,6 +1782,27 @@ static od_status ic0_build(Scene* s) {
   if ((st = up(&P.ic_frp, frp)) != OD_OK) return st;
   if ((st = up(&P.ic_fci, fci)) != OD_OK) return st;
   if ((st = up(&P.ic_gord_f, gof)) != OD_OK) return st;
+  {
+    // one-launch factorisation when a row and its pairs fit the shared memory
+    const size_t smem = sizeof(double) * (size_t)kIcfWarps * (3 * (size_t)maxrow + (size_t)maxpairs);
+    int dev_coop = 0, per_sm = 0;
+    OD_CUDA(cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, s->ctx->device));
+    if (dev_coop && pa.size() < (size_t)INT32_MAX && smem <= 96 * 1024) {
+      OD_CUDA(cudaFuncSetAttribute(ic0_factor_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      OD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ic0_factor_coop_kernel, kIcfThreads, smem));
+      if (per_sm > 0) {
+        if ((st = up(&P.ic_pp, pp)) != OD_OK) return st;
+        if ((st = up(&P.ic_pa, pa)) != OD_OK) return st;
+        if ((st = up(&P.ic_pb, pb)) != OD_OK) return st;
+        // two CTAs (8 warps) per SM: 1,216 warps hold a level's rows (a
+        // few hundred on the 98k-tet beam) many times over; more only poll
+        P.ic_fgrid = std::min(per_sm, 2) * s->ctx->num_sms;
+        P.ic_fmaxrow = maxrow;
+        P.ic_fmaxpairs = maxpairs;
+        P.ic_fsmem = smem;
+      }
+    }
+  }
   if ((st = up(&P.ic_gord_b, gob)) != OD_OK) return st;
   OD_CUDA(cudaMalloc(&P.ic_val, sizeof(double) * std::max(1, nnz)));
   const size_t nl = std::max<size_t>(1, fci.size());
@@ -1661,6 +1819,8 @@ static od_status ic0_build(Scene* s) {
   return OD_OK;
 }
 
+static od_status ic0_check(Scene* s);
+
 // shifted IC(0) factorisation of the current A64 with the Manteuffel retry
 static od_status ic0_factor(Scene* s) {
   Pcg& P = s->pcg;
@@ -1670,16 +1830,40 @@ static od_status ic0_factor(Scene* s) {
   double shift = 0.0;
   for (int attempt = 0; attempt < 40; attempt++) {
     OD_CUDA(cudaMemsetAsync(P.ic_bad, 0, sizeof(int), strm));
-    for (int l = 0; l < P.n_levels_f; l++) {
-      int l0 = P.lvl_ptr_f[l], l1 = P.lvl_ptr_f[l + 1];
+    if (P.ic_fgrid > 0) {
+      // every value starts "not yet written" (all-ones bytes)
+      OD_CUDA(cudaMemsetAsync(P.ic_val, 0xff, sizeof(double) * (size_t)P.ic_nnz, strm));
+      int nrow = P.ic_n, mr = P.ic_fmaxrow, mp = P.ic_fmaxpairs;
+      const int* rows = P.lvl_rows_f;
+      const int* rp = P.ic_rp;
+      const int* ci = P.ic_ci;
+      const int* src = P.ic_src;
+      const double* A = s->A64;
+      const int* pp = P.ic_pp;
+      const int* pa = P.ic_pa;
+      const int* pb = P.ic_pb;
+      double* L = P.ic_val;
+      int* badp = P.ic_bad;
+      int* errp = P.ic_err;
+      void* args[] = {(void*)&nrow, (void*)&rows, (void*)&rp,    (void*)&ci, (void*)&src,   (void*)&A,
+                      (void*)&pp,   (void*)&pa,   (void*)&pb,    (void*)&L,  (void*)&shift, (void*)&mr,
+                      (void*)&mp,   (void*)&badp, (void*)&errp};
       OD_KL(s);
-      ic0_factor_level<double><<<nblk(l1 - l0, 128), 128, 0, strm>>>(l0, l1, P.lvl_rows_f, P.ic_rp, P.ic_ci, P.ic_src,
-                                                                      s->A64, P.ic_val, shift, P.ic_bad);
+      OD_CUDA(cudaLaunchCooperativeKernel((void*)ic0_factor_coop_kernel, dim3(P.ic_fgrid), dim3(kIcfThreads), args,
+                                          P.ic_fsmem, strm));
+    } else {
+      for (int l = 0; l < P.n_levels_f; l++) {
+        int l0 = P.lvl_ptr_f[l], l1 = P.lvl_ptr_f[l + 1];
+        OD_KL(s);
+        ic0_factor_level<double><<<nblk(l1 - l0, 128), 128, 0, strm>>>(l0, l1, P.lvl_rows_f, P.ic_rp, P.ic_ci,
+                                                                        P.ic_src, s->A64, P.ic_val, shift, P.ic_bad);
+      }
     }
     OD_CUDA(cudaGetLastError());
     int bad = 0;
     OD_CUDA(cudaMemcpyAsync(&bad, P.ic_bad, sizeof(int), cudaMemcpyDeviceToHost, strm));
     OD_TRY(sync_stream(s));
+    if (P.ic_fgrid > 0) OD_TRY(ic0_check(s));
     if (!bad) break;
     shift = shift == 0.0 ? 1e-3 : 2.0 * shift;
   }
@@ -1773,7 +1957,7 @@ void pcg_free(Scene* s) {
     cudaFree(v);
   if (P.ic_err_host) cudaFreeHost(P.ic_err_host);
   for (int* v : {P.ic_rp, P.ic_ci, P.ic_src, P.lvl_rows_f, P.lvl_rows_b, P.icT_rp, P.icT_ci, P.icT_pos, P.ic_bad,
-                 P.ic_frp, P.ic_fci, P.ic_err, P.ic_gord_f, P.ic_gord_b})
+                 P.ic_frp, P.ic_fci, P.ic_err, P.ic_gord_f, P.ic_gord_b, P.ic_pp, P.ic_pa, P.ic_pb})
     cudaFree(v);
   cudaFree(P.sc);
   cudaFree(P.gbar);

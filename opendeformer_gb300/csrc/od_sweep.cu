@@ -41,6 +41,7 @@
 #include <cstdlib>
 #include <vector>
 
+#include "od_grid.cuh"
 #include "od_internal.h"
 
 namespace od {
@@ -72,21 +73,6 @@ namespace {
 
 constexpr int kSweepThreads = 256;
 constexpr unsigned kSweepSpinLimit = 1u << 21;
-constexpr unsigned long long kPending = 0xffffffffffffffffull;   // "not yet written" (a NaN)
-
-// The value is its own ready flag and nothing else is read through it, so
-// relaxed GPU-scope 64-bit accesses suffice (single-copy atomic: a reader
-// sees the pending pattern or the value) and no fence orders a store
-// behind the previous one.
-__device__ __forceinline__ unsigned long long ld_relaxed_u64(const double* p) {
-  unsigned long long v;
-  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ void st_relaxed_f64(double* p, double x) {
-  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(__double_as_longlong(x)) : "memory");
-}
 
 // bounded wait until v (first read of *p) is written; after a timeout
 // anywhere (err set) no thread waits any more, so the launch ends promptly
