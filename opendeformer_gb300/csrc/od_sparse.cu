@@ -1474,11 +1474,15 @@ __global__ void ic0_factor_level(int l0, int l1, const int* __restrict__ rows, c
 // level, one warp per row.  The warp first reads every value of other rows
 // the row needs -- for each off-diagonal entry (i, j) the L_jk paired with
 // the row's own L_ik (k < j), and L_jj -- into shared memory, each waited
-// for (bounded) until it is no longer the pending pattern; then it forms
-// its entries in order from shared memory:
-//   L_ij = (A_ij - sum_k L_ik L_jk) / L_jj,   L_ii = sqrt((1 + shift) A_ii - sum_k L_ik^2)
-// with the breakdown test of ic0_factor_level, and publishes each value
-// (relaxed store; the value is its own ready flag).
+// for (bounded) until it is no longer the pending pattern.  Then it forms
+// the row right-looking: lane q % 32 owns entry q and its running value
+// (A_ij, or (1 + shift) A_ii); when entry k is formed,
+//   L_ij = running_ij / L_jj,   L_ii = sqrt(running_ii)  (breakdown test of ic0_factor_level)
+// it is published (relaxed store; the value is its own ready flag) and
+// broadcast, and every later entry paired with it subtracts L_ik L_jk, the
+// diagonal L_ik^2 -- the subtractions of each entry in ascending k, as the
+// sequential factorisation makes them.  A step of the row is one multiply,
+// one shuffle and one FMA.
 constexpr int kIcfThreads = 128;
 constexpr int kIcfWarps = kIcfThreads / 32;
 constexpr unsigned kIcfSpinLimit = 1u << 21;
@@ -1513,6 +1517,8 @@ __device__ __forceinline__ double icf_warp_read(const double* p, int* err) {
   return __longlong_as_double((long long)v);
 }
 
+constexpr int kIcfSlots = 4;   // entries per lane: rows of up to 128 entries
+
 __global__ void __launch_bounds__(kIcfThreads) ic0_factor_coop_kernel(
     int n, const int* __restrict__ rows, const int* __restrict__ rp, const int* __restrict__ ci,
     const int* __restrict__ src, const double* __restrict__ A, const int* __restrict__ pp,
@@ -1520,8 +1526,7 @@ __global__ void __launch_bounds__(kIcfThreads) ic0_factor_coop_kernel(
     int* __restrict__ bad, int* __restrict__ err) {
   extern __shared__ double icf_s[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  double* rowL = icf_s + (size_t)wib * (3 * maxrow + maxpairs);
-  double* aval = rowL + maxrow;
+  double* aval = icf_s + (size_t)wib * (2 * maxrow + maxpairs);
   double* dval = aval + maxrow;
   double* pv = dval + maxrow;
   const int W = gridDim.x * kIcfWarps;
@@ -1530,6 +1535,7 @@ __global__ void __launch_bounds__(kIcfThreads) ic0_factor_coop_kernel(
     const int bi = rp[i], m = rp[i + 1] - bi;
     const int p0 = pp[bi], np = pp[bi + m] - p0;
     __syncwarp();
+    // 1) the row's A values, the other rows' diagonals and paired values
     for (int q0 = 0; q0 < m; q0 += 32) {
       const int q = q0 + lane;
       const double* dp = nullptr;
@@ -1547,32 +1553,61 @@ __global__ void __launch_bounds__(kIcfThreads) ic0_factor_coop_kernel(
       if (p < np) pv[p] = v;
     }
     __syncwarp();
-    for (int q = 0; q < m; q++) {
-      double s = 0.0;
-      if (q < m - 1) {
-        const int a1 = pp[bi + q + 1] - p0;
-        for (int p = pp[bi + q] - p0 + lane; p < a1; p += 32) s += rowL[pa[p0 + p]] * pv[p];
-      } else {
-        for (int k = lane; k < m - 1; k += 32) s += rowL[k] * rowL[k];
+    // 2) right-looking over the row's entries
+    double sv[kIcfSlots], rinv[kIcfSlots];
+    int cur[kIcfSlots], cend[kIcfSlots], nxt[kIcfSlots];
+#pragma unroll
+    for (int r = 0; r < kIcfSlots; r++) {
+      const int q = lane + 32 * r;
+      sv[r] = 0.0;
+      rinv[r] = 0.0;
+      cur[r] = cend[r] = 0;
+      nxt[r] = -1;
+      if (q < m) {
+        sv[r] = q < m - 1 ? aval[q] : aval[q] * (1.0 + shift);
+        rinv[r] = 1.0 / dval[q];
+        cur[r] = pp[bi + q] - p0;
+        cend[r] = pp[bi + q + 1] - p0;
+        nxt[r] = cur[r] < cend[r] ? pa[p0 + cur[r]] : -1;
       }
-      for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) {
-        double v;
-        if (q < m - 1) {
-          v = (aval[q] - s) / dval[q];
-        } else {
-          const double d = aval[q] * (1.0 + shift);
-          double sum = d - s;
-          if (!(sum > 1e-12 * d)) {
-            *bad = 1;
-            sum = d > 0.0 ? d : 1.0;
+    }
+    for (int k = 0; k < m; k++) {
+      const int ko = k & 31, rk = k >> 5;
+      double v = 0.0;
+      if (lane == ko) {
+        double s = 0.0, rv = 0.0;
+#pragma unroll
+        for (int r = 0; r < kIcfSlots; r++)
+          if (r == rk) {
+            s = sv[r];
+            rv = rinv[r];
           }
-          v = sqrt(sum);
+        if (k < m - 1) {
+          v = s * rv;
+        } else {
+          const double d = aval[k] * (1.0 + shift);
+          if (!(s > 1e-12 * d)) {
+            *bad = 1;
+            s = d > 0.0 ? d : 1.0;
+          }
+          v = sqrt(s);
         }
-        rowL[q] = v;
-        st_relaxed_f64(L + bi + q, v);
+        st_relaxed_f64(L + bi + k, v);
       }
-      __syncwarp();
+      v = __shfl_sync(0xffffffffu, v, ko);
+#pragma unroll
+      for (int r = 0; r < kIcfSlots; r++) {
+        const int q = lane + 32 * r;
+        if (q > k && q < m) {
+          if (q == m - 1) {
+            sv[r] -= v * v;
+          } else if (nxt[r] == k) {
+            sv[r] -= v * pv[cur[r]];
+            cur[r]++;
+            nxt[r] = cur[r] < cend[r] ? pa[p0 + cur[r]] : -1;
+          }
+        }
+      }
     }
   }
 }
@@ -1784,10 +1819,10 @@ static od_status ic0_build(Scene* s) {
   if ((st = up(&P.ic_gord_f, gof)) != OD_OK) return st;
   {
     // one-launch factorisation when a row and its pairs fit the shared memory
-    const size_t smem = sizeof(double) * (size_t)kIcfWarps * (3 * (size_t)maxrow + (size_t)maxpairs);
+    const size_t smem = sizeof(double) * (size_t)kIcfWarps * (2 * (size_t)maxrow + (size_t)maxpairs);
     int dev_coop = 0, per_sm = 0;
     OD_CUDA(cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, s->ctx->device));
-    if (dev_coop && pa.size() < (size_t)INT32_MAX && smem <= 96 * 1024) {
+    if (dev_coop && pa.size() < (size_t)INT32_MAX && smem <= 96 * 1024 && maxrow <= 32 * kIcfSlots) {
       OD_CUDA(cudaFuncSetAttribute(ic0_factor_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       OD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ic0_factor_coop_kernel, kIcfThreads, smem));
       if (per_sm > 0) {
