@@ -24,7 +24,9 @@ roofline of the FP32 SpMV phase measured inside the solve), and
 together through od_batch with the mixed solver; "serving_tier", Poisson step
 requests over a pool of scenes; "sweep_tier", the headline step preconditioned
 by the reference's incomplete LDL^T and by its threshold incomplete Cholesky,
-beside the reference's CPU code for each; "relabel_tier", the step and the
+beside the reference's CPU code for each; "ic0_tier", the headline step with
+the IC(0)-preconditioned PCG (the configuration's second preconditioner)
+beside the oracle's CPU restatement of it; "relabel_tier", the step and the
 triangular sweeps on the generator's node order, a shuffled order and the
 shuffle relabeled by od_mesh_relabel.
 """
@@ -397,6 +399,72 @@ def sweep_tier(args, api, ctx):
     return result
 
 
+def ic0_tier(args, api, ctx):
+    """The headline beam workload with the IC(0)-preconditioned PCG: the
+    shifted IC(0) factor of every solve and the two triangular sweeps of
+    every apply on the device, each one cooperative launch.  Device time per
+    step, PCG iterations, the apply's time per dependency level from a
+    profiled step, and the oracle's CPU restatement of the same step (the
+    reference has no IC(0); single thread, two steps)."""
+    wl = WORKLOADS["beam98k_nh_newmark"]
+    g = wl["mesh"]()
+    cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+    kind, rho, E, nu, thr = wl["material"]
+    s = api.Scene(ctx, g.X, g.tets, g.facets, cd, api.Material(kind, rho, E, nu, thr))
+    s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, wl["alpha_m"], wl["beta_k"], wl["dt"],
+                                             api.CGSolver(wl["tol"], 5000, api.IC0Preconditioner()), wl["newton"]))
+    s.set_loads(body=wl["body"], tractions=traction_groups(g, wl["traction"]))
+    s.set_traction_schedule(wl["freq"])
+    for _ in range(3):
+        s.step(1)
+    steps = max(3, args.tier_steps)
+    ms, it, solves = [], 0, 0
+    for _ in range(steps):
+        st = s.step(1)
+        if st.status != 0:
+            raise RuntimeError(f"ic0 tier: step status {st.status}")
+        ms.append(st.device_ms)
+        it += st.pcg_iterations
+        solves += st.solves
+    ctx.reset_counters()
+    ctx.set_profiling(True)
+    s.step(1)
+    ctx.set_profiling(False)
+    p = ctx.counters()
+    s.close()
+    apply_ms = p.sweep_apply_ms / max(1, p.sweep_applies)
+    out = {"workload": "beam98k_nh_newmark", "n_tets": g.n_tets, "precond": "IC0Preconditioner (shifted IC(0))",
+           "steps": steps, "ms_per_step": statistics.mean(ms), "steps_per_s": 1000.0 / statistics.mean(ms),
+           "pcg_iterations_per_step": it / steps, "solves_per_step": solves / steps,
+           "apply": {"kernel": "sweep_apply_kernel<1> over row triples (one cooperative launch)",
+                     "levels": p.sweep_levels, "avg_launch_ms": apply_ms,
+                     "us_per_level": 1000.0 * apply_ms / max(1, p.sweep_levels), "launches": p.sweep_applies},
+           "factor_kernel": "ic0_factor_coop_kernel (warp per row, rows by level, one cooperative launch)"}
+    if not args.no_cpu_baseline:
+        try:
+            from oracle import restated as O
+            o = O.OracleScene(g.X, g.tets, g.facets, cd, kind, rho, E, nu, thr)
+            o.integrator_setup(wl["dt"], wl["alpha_m"], wl["beta_k"], newton=wl["newton"], tol=wl["tol"],
+                               maxit=5000, precond="ic0")
+            t, n_cpu, used = 0.0, 0, 0.0
+            while n_cpu < 2:
+                t += wl["dt"]
+                scale = math.sin(2 * math.pi * wl["freq"] * t)
+                t0 = time.perf_counter()
+                o.set_fext(o.loads(body=wl["body"], tractions=[(np.array(tr) * scale, fac) for tr, fac in
+                                                               traction_groups(g, wl["traction"])]))
+                o.nm_step(1)
+                used += time.perf_counter() - t0
+                n_cpu += 1
+            o.close()
+            out["cpu_port"] = {"steps_per_s": n_cpu / used, "cores": 1, "kind": "port",
+                               "sample": f"{n_cpu} Newmark steps, the oracle's restatement with IC(0), single thread"}
+            out["speedup_vs_cpu_port"] = out["steps_per_s"] / out["cpu_port"]["steps_per_s"]
+        except Exception as exc:
+            out["cpu_port"] = {"error": str(exc)}
+    return out
+
+
 def relabel_tier(args, api, ctx):
     """Node order on the headline beam step: the generator's order, a seeded
     random shuffle of the node ids, and the shuffle relabeled by
@@ -742,7 +810,7 @@ def run_gpu(args, wl):
         only = [t for t in args.only_tiers.split(",") if t]
         for name, fn in (("precision_tier", precision_tier), ("batched_tier", batched_tier),
                          ("serving_tier", serving_tier), ("sweep_tier", sweep_tier),
-                         ("relabel_tier", relabel_tier)):
+                         ("ic0_tier", ic0_tier), ("relabel_tier", relabel_tier)):
             if only and name.split("_")[0] not in only:
                 continue
             try:
@@ -784,7 +852,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tiers", action="store_true", help="skip the mixed-precision and batched workloads")
     ap.add_argument("--tier-steps", type=int, default=5)
-    ap.add_argument("--only-tiers", default="", help="comma list of precision,batched,serving,sweep,relabel (default: all)")
+    ap.add_argument("--only-tiers", default="", help="comma list of precision,batched,serving,sweep,ic0,relabel (default: all)")
     ap.add_argument("--precision-nz", type=int, default=64,
                     help="cube layers of the precision-tier block (64: 2,621,440 tets)")
     ap.add_argument("--serving-pool", type=int, default=512)
