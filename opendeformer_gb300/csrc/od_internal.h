@@ -78,11 +78,9 @@ struct Pcg {
   int* ic_ci = nullptr;
   int* ic_src = nullptr;        // source entry in the full BSR A (block*9 + r*3 + c)
   double* ic_val = nullptr;
-  int* ic_diag = nullptr;       // position of the diagonal in each row
-  int n_levels_f = 0, n_levels_b = 0;
+  int n_levels_f = 0;
   int* lvl_rows_f = nullptr;    // rows sorted by forward level
-  int* lvl_rows_b = nullptr;
-  std::vector<int> lvl_ptr_f, lvl_ptr_b;  // host level offsets
+  std::vector<int> lvl_ptr_f;   // host level offsets (per-level factorisation)
   int* ic_bad = nullptr;        // breakdown flag
   // upper (transposed) CSR for the backward sweep: for row i, entries L_ji j > i
   int* icT_rp = nullptr;

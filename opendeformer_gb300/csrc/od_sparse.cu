@@ -1792,13 +1792,11 @@ static od_status ic0_build(Scene* s) {
   int gdf = 0, gdb = 0;
   sweep_group_levels(n, frp, fci, trp2, tci2, gof, gob, &gdf, &gdb);
   P.ic_gdepth = gdf + gdb;
-  std::vector<int> lrf, lrb;
+  std::vector<int> lrf;
   build_ic_levels(srp, sci, n, lrf, P.lvl_ptr_f, true);
-  build_ic_levels(srp, sci, n, lrb, P.lvl_ptr_b, false);
   P.ic_n = n;
   P.ic_nnz = nnz;
   P.n_levels_f = (int)P.lvl_ptr_f.size() - 1;
-  P.n_levels_b = (int)P.lvl_ptr_b.size() - 1;
   auto up = [&](int** d, const std::vector<int>& h) -> od_status {
     OD_CUDA(cudaMalloc(d, sizeof(int) * std::max<size_t>(1, h.size())));
     if (!h.empty()) OD_CUDA(cudaMemcpy(*d, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice));
@@ -1810,7 +1808,6 @@ static od_status ic0_build(Scene* s) {
   if ((st = up(&P.ic_ci, sci)) != OD_OK) return st;
   if ((st = up(&P.ic_src, ssrc)) != OD_OK) return st;
   if ((st = up(&P.lvl_rows_f, lrf)) != OD_OK) return st;
-  if ((st = up(&P.lvl_rows_b, lrb)) != OD_OK) return st;
   if ((st = up(&P.icT_rp, trp2)) != OD_OK) return st;
   if ((st = up(&P.icT_ci, tci2)) != OD_OK) return st;
   if ((st = up(&P.icT_pos, tpos2)) != OD_OK) return st;
@@ -1991,7 +1988,7 @@ void pcg_free(Scene* s) {
   for (double* v : {P.x, P.r, P.z, P.p, P.q, P.b, P.partial, P.pinv, P.ic_val, P.ic_fval, P.ic_bval, P.ic_dval, P.ic_y})
     cudaFree(v);
   if (P.ic_err_host) cudaFreeHost(P.ic_err_host);
-  for (int* v : {P.ic_rp, P.ic_ci, P.ic_src, P.lvl_rows_f, P.lvl_rows_b, P.icT_rp, P.icT_ci, P.icT_pos, P.ic_bad,
+  for (int* v : {P.ic_rp, P.ic_ci, P.ic_src, P.lvl_rows_f, P.icT_rp, P.icT_ci, P.icT_pos, P.ic_bad,
                  P.ic_frp, P.ic_fci, P.ic_err, P.ic_gord_f, P.ic_gord_b, P.ic_pp, P.ic_pa, P.ic_pb})
     cudaFree(v);
   cudaFree(P.sc);
