@@ -295,6 +295,7 @@ struct Scene {
   int nbc = 0, nrem = 0, nvals = 0;
   std::vector<int> color_off;      // element colour ranges (colour order)
   int* color_off_dev = nullptr;    // the same on the device
+  double mix_iters_last = 0.0;     // inner iterations of the scene's last mixed solve
   // gathered assembly (CSR over the destinations, sources in the reference's
   // element order; null when 78 x elements overflows a 32-bit index)
   int* gat_kptr = nullptr;  // nvals + 1

@@ -2189,6 +2189,41 @@ static od_status mixed_partition(MixedSys* m, int G) {
   return OD_OK;
 }
 
+// Weights of a multi-scene system's slices: the slice's steps plus the
+// per-slice cost, times its scene's expected inner iterations relative to
+// the median (those of the scene's last mixed solve; the median for a scene
+// without one; clamped to [1/16, 256] x the median), so that each scene's
+// share of the CTAs follows its work and the scenes finish together rather
+// than the slowest one running its last iterations on the few CTAs a
+// size-proportional share gives it.  Leaves the weights alone when no scene
+// has a history.
+static void mixed_work_weights(MixedSys* m) {
+  std::vector<double> known;
+  for (Scene* s : m->scenes)
+    if (s->mix_iters_last > 0.0) known.push_back(s->mix_iters_last);
+  if (known.empty()) return;
+  std::nth_element(known.begin(), known.begin() + known.size() / 2, known.end());
+  const double med = std::max(1.0, known[known.size() / 2]);
+  double c_slice = kSliceCost;
+  if (const char* e = std::getenv("OD_GB300_SLICE_COST")) c_slice = std::atof(e);
+  m->slice_w.resize(m->ns);
+  for (int s = 0; s < m->n_sc; s++) {
+    const double it = m->scenes[s]->mix_iters_last > 0.0 ? m->scenes[s]->mix_iters_last : med;
+    const double f = std::min(256.0, std::max(1.0 / 16.0, it / med));
+    for (int k = m->sc_slice[s]; k < m->sc_slice[s + 1]; k++)
+      m->slice_w[k] = ((double)(m->off_host[k + 1] - m->off_host[k]) + c_slice) * f;
+  }
+}
+
+// the partition with the work weights, else (too many scenes for a CTA)
+// with the size weights
+static od_status mixed_partition_work(MixedSys* m, int G) {
+  mixed_work_weights(m);
+  if (mixed_partition(m, G) == OD_OK) return OD_OK;
+  m->slice_w.clear();
+  return mixed_partition(m, G);
+}
+
 // After a solve of a one-scene system: scale the weights of each CTA's
 // slices by the CTA's measured SpMV time per weight (relative to the
 // median) and re-partition, while the slowest CTA is more than 3% behind
@@ -2299,7 +2334,7 @@ od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::ve
   if (e == cudaSuccess) e = cudaMalloc(&m->prof, (3 + (size_t)ctx->num_sms) * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMallocHost(&m->prof_host, 3 * sizeof(unsigned long long));
   if (e != cudaSuccess) return fail(cuda_fail(e, "mixed_build"));
-  if ((st = mixed_partition(m, G)) != OD_OK) return fail(st);
+  if ((st = n > 1 ? mixed_partition_work(m, G) : mixed_partition(m, G)) != OD_OK) return fail(st);
   *out = m;
   return OD_OK;
 }
@@ -2448,11 +2483,15 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
       }
     }
     st[s].iterations = total[s];
+    m->scenes[s]->mix_iters_last = (double)total[s];
     st[s].refinements = sweeps[s];
     st[s].rel_residual = bb[s] > 0.0 ? std::sqrt(rr[s] / bb[s]) : std::sqrt(rr[s]);
     st[s].ic_shift = 0.0;
     st[s].status = status[s];
   }
+  // a multi-scene system solved again (a reused batch) starts from the
+  // partition its scenes' iterations ask for
+  if (rc == OD_OK && n_sc > 1) OD_TRY(mixed_partition_work(m, m->cta_grid));
   return rc;
 }
 
