@@ -1,0 +1,282 @@
+// End-to-end check of the C++ drop-in classes (include/od_gb300_dropin.hpp)
+// inside the reference's own time loop: the same mesh stepped by the
+// reference's backward Euler (intergrator/nonlinearImplicitBackwardEuler.h)
+//   A  as shipped (reference material, CGSolver with Jacobi),
+//   B  with GpuMaterial in place of the reference material,
+//   C  with GpuCGSolver in place of CGSolver,
+//   D  GpuIntergrator in place of the whole integrator,
+//   E  as shipped with InCholeskyPreconditioner, and
+//   F  CGSolver with GpuInCholeskyPreconditioner;
+// prints the relative displacement differences B, C, D against A and F
+// against E, and exits 0 when all are within the given tolerance.
+//
+// usage: dropin_check <dir> <tolerance>; <dir> holds params.txt (n_nodes
+// n_tets n_facets n_cdofs rho youngs poisson threshold dt alpha_m beta_k tol
+// max_iter steps gx gy gz), X.bin (double), tets.bin, facets.bin, cdofs.bin
+// (int32).  Test infrastructure: compiled and run by tests/test_gpu_dropin.py
+// against the compiled reference (oracle/_ref) and libodgpu.so.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <climits>
+#include <cstdint>
+#include <functional>
+#include <limits>
+#include <map>
+#include <memory>
+#include <set>
+#include <string>
+#include <tuple>
+#include <type_traits>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+#include "od_gb300_dropin.hpp"
+
+#include "cgSolver.h"
+#include "constrainer.h"
+#include "inCholeskyPreconditioner.h"
+#include "invertibleNeoHookean.h"
+#include "jacobiPreconditioner.h"
+#include "nonlinearImplicitBackwardEuler.h"
+#include "tetmesh.h"
+
+using namespace ODER;
+using Mat = BlockedSymSpMatrix;
+
+namespace {
+
+struct Params {
+  int n_nodes, n_tets, n_facets, n_cdofs;
+  double rho, youngs, poisson, thr, dt, alpha_m, beta_k, tol;
+  int max_iter, steps;
+  double g[3];
+};
+
+template <class T>
+std::vector<T> read_bin(const std::string& path, size_t n) {
+  std::vector<T> v(n);
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f || fread(v.data(), sizeof(T), n, f) != n) {
+    fprintf(stderr, "cannot read %s\n", path.c_str());
+    exit(2);
+  }
+  fclose(f);
+  return v;
+}
+
+struct Input {
+  Params p;
+  std::vector<double> X;
+  std::vector<int> tets, facets, cdofs;
+};
+
+struct RefSetup {
+  Reference<Mesh> mesh;
+  Reference<NodeIndexer> indexer;
+  int dofs = 0;
+};
+
+RefSetup make_setup(const Input& in) {
+  RefSetup s;
+  TetMesh* m = new TetMesh(in.p.n_nodes, in.p.n_tets, in.p.n_facets);
+  s.mesh = m;
+  for (int i = 0; i < in.p.n_nodes; i++) m->setVertex(i, Vector3(in.X[3 * i], in.X[3 * i + 1], in.X[3 * i + 2]));
+  for (int e = 0; e < in.p.n_tets; e++) m->setElement(e, const_cast<int*>(in.tets.data() + 4 * e));
+  for (int f = 0; f < in.p.n_facets; f++) m->setFacet(f, const_cast<int*>(in.facets.data() + 3 * f));
+  // whole-node constraints through the public API (Constrainer::setConstrains
+  // with no types fixes every axis, core/constrainer.cpp:43-50)
+  std::vector<int> nodes;
+  for (size_t k = 0; k + 2 < in.cdofs.size(); k += 3) {
+    if (in.cdofs[k] % 3 != 0 || in.cdofs[k + 1] != in.cdofs[k] + 1 || in.cdofs[k + 2] != in.cdofs[k] + 2) {
+      fprintf(stderr, "constrained DOFs must be whole nodes\n");
+      exit(2);
+    }
+    nodes.push_back(in.cdofs[k] / 3);
+  }
+  Constrainer c(s.mesh);
+  c.setConstrains((int)nodes.size(), nodes.data());
+  s.indexer = new NodeIndexer(c);
+  s.dofs = s.indexer->getMatrixOrder(s.mesh);
+  return s;
+}
+
+std::vector<double> displacements(const RefSetup& s, int n_nodes) {
+  std::vector<double> u(3 * (size_t)n_nodes);
+  for (int i = 0; i < n_nodes; i++) {
+    const Vector3& d = s.mesh->getVertexDisplacementConst(i);
+    u[3 * i] = d.x;
+    u[3 * i + 1] = d.y;
+    u[3 * i + 2] = d.z;
+  }
+  return u;
+}
+
+double rel_diff(const std::vector<double>& a, const std::vector<double>& b) {
+  double num = 0.0, den = 0.0;
+  for (size_t i = 0; i < a.size(); i++) {
+    num += (a[i] - b[i]) * (a[i] - b[i]);
+    den += b[i] * b[i];
+  }
+  return den > 0.0 ? sqrt(num / den) : sqrt(num);
+}
+
+// the reference's backward Euler with the given material and solver
+std::vector<double> run_reference_loop(const Input& in, RefSetup& s,
+                                       const Reference<FullOrderNonlinearMaterial<Mat>>& material,
+                                       const Reference<LinearSolver<Mat>>& solver) {
+  NonlinearImplicitBackwardEuler<Mat> be(s.dofs, in.p.alpha_m, in.p.beta_k, in.p.dt, s.mesh, s.indexer, material,
+                                         solver);
+  Forcer f;
+  Scalar g[3] = {in.p.g[0], in.p.g[1], in.p.g[2]};
+  f.addBodyForce(s.mesh, g, s.indexer);
+  be.setExternalVirtualWork(f);
+  for (int k = 0; k < in.p.steps; k++) {
+    be.runOneTimeStep();
+    be.updateMeshVerticesDisplacements(s.indexer, s.mesh);
+  }
+  return displacements(s, in.p.n_nodes);
+}
+
+Reference<FullOrderNonlinearMaterial<Mat>> reference_material(const Input& in) {
+  return Reference<FullOrderNonlinearMaterial<Mat>>(
+      new InvertibleNeoHookeanMaterial(in.p.rho, in.p.youngs, in.p.poisson, in.p.thr));
+}
+
+od_scene* new_scene(od_ctx* ctx, const Input& in) {
+  od_material mat{};
+  mat.kind = OD_MATERIAL_NEOHOOKEAN;
+  mat.density = in.p.rho;
+  mat.youngs = in.p.youngs;
+  mat.poisson = in.p.poisson;
+  mat.threshold = in.p.thr;
+  od_scene* scene = nullptr;
+  if (od_scene_create(ctx, in.p.n_nodes, in.X.data(), in.p.n_tets, in.tets.data(), in.p.n_facets, in.facets.data(),
+                      in.p.n_cdofs, in.cdofs.data(), &mat, &scene) != OD_OK) {
+    fprintf(stderr, "od_scene_create failed\n");
+    exit(3);
+  }
+  return scene;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc < 3) {
+    fprintf(stderr, "usage: dropin_check <dir> <tolerance>\n");
+    return 2;
+  }
+  const std::string dir = argv[1];
+  const double tol_ok = atof(argv[2]);
+  Input in;
+  {
+    FILE* f = fopen((dir + "/params.txt").c_str(), "r");
+    Params& p = in.p;
+    if (!f || fscanf(f, "%d %d %d %d %lf %lf %lf %lf %lf %lf %lf %lf %d %d %lf %lf %lf", &p.n_nodes, &p.n_tets,
+                     &p.n_facets, &p.n_cdofs, &p.rho, &p.youngs, &p.poisson, &p.thr, &p.dt, &p.alpha_m, &p.beta_k,
+                     &p.tol, &p.max_iter, &p.steps, &p.g[0], &p.g[1], &p.g[2]) != 17) {
+      fprintf(stderr, "cannot read params.txt\n");
+      return 2;
+    }
+    fclose(f);
+  }
+  in.X = read_bin<double>(dir + "/X.bin", 3 * (size_t)in.p.n_nodes);
+  in.tets = read_bin<int>(dir + "/tets.bin", 4 * (size_t)in.p.n_tets);
+  in.facets = read_bin<int>(dir + "/facets.bin", 3 * (size_t)in.p.n_facets);
+  in.cdofs = read_bin<int>(dir + "/cdofs.bin", (size_t)in.p.n_cdofs);
+
+  od_ctx* ctx = nullptr;
+  if (od_ctx_create(0, &ctx) != OD_OK) {
+    fprintf(stderr, "od_ctx_create failed\n");
+    return 3;
+  }
+  int bad = 0;
+  auto check = [&](od_status st, const char* what) {
+    if (st != OD_OK) {
+      fprintf(stderr, "%s: status %d\n", what, (int)st);
+      bad = 1;
+    }
+  };
+  auto jacobi_cg = [&]() {
+    return Reference<LinearSolver<Mat>>(new CGSolver(in.p.tol, in.p.max_iter, Reference<Preconditioner>(new JacobiPreconditioner())));
+  };
+
+  // A: the reference as shipped
+  RefSetup sa = make_setup(in);
+  const std::vector<double> ua = run_reference_loop(in, sa, reference_material(in), jacobi_cg());
+
+  // B: GpuMaterial inside the reference integrator
+  od_scene* sb_scene = new_scene(ctx, in);
+  RefSetup sb = make_setup(in);
+  // the reference's intrusive Reference owns each drop-in; the handles
+  // below keep them alive until their statuses are read
+  auto* gm = new od_dropin::GpuMaterial(sb_scene, in.p.rho, MarterialType(Marterial_Isotropic | Marterial_Invertible));
+  Reference<FullOrderNonlinearMaterial<Mat>> gm_ref(gm);
+  const std::vector<double> ub = run_reference_loop(in, sb, gm_ref, jacobi_cg());
+
+  // C: GpuCGSolver inside the reference integrator
+  od_scene* sc_scene = new_scene(ctx, in);
+  RefSetup sc = make_setup(in);
+  auto* gcg = new od_dropin::GpuCGSolver(sc_scene, in.p.tol, in.p.max_iter, OD_PRECOND_JACOBI);
+  Reference<LinearSolver<Mat>> gcg_ref(gcg);
+  const std::vector<double> uc = run_reference_loop(in, sc, reference_material(in), gcg_ref);
+
+  // D: GpuIntergrator in place of the integrator
+  od_scene* sd_scene = new_scene(ctx, in);
+  RefSetup sd = make_setup(in);
+  od_integrator_params ip{};
+  ip.kind = OD_INTEGRATOR_BACKWARD_EULER;
+  ip.dt = in.p.dt;
+  ip.alpha_m = in.p.alpha_m;
+  ip.beta_k = in.p.beta_k;
+  ip.solver.tol = in.p.tol;
+  ip.solver.max_iter = in.p.max_iter;
+  ip.solver.precond = OD_PRECOND_JACOBI;
+  ip.solver.precision = OD_PRECISION_FP64;
+  std::vector<double> ud;
+  {
+    od_dropin::GpuIntergrator gi(sd_scene, sd.dofs, ip);
+    check(gi.last_status, "GpuIntergrator setup");
+    Forcer f;
+    Scalar g[3] = {in.p.g[0], in.p.g[1], in.p.g[2]};
+    f.addBodyForce(sd.mesh, g, sd.indexer);
+    gi.setExternalVirtualWork(f);
+    check(gi.last_status, "setExternalVirtualWork");
+    for (int k = 0; k < in.p.steps; k++) {
+      gi.runOneTimeStep();
+      check(gi.last_status, "runOneTimeStep");
+      gi.updateMeshVerticesDisplacements(sd.indexer, sd.mesh);
+    }
+    ud = displacements(sd, in.p.n_nodes);
+  }
+
+  // E, F: threshold incomplete Cholesky, the reference's and the drop-in
+  RefSetup se = make_setup(in);
+  const std::vector<double> ue = run_reference_loop(
+      in, se, reference_material(in),
+      Reference<LinearSolver<Mat>>(
+          new CGSolver(in.p.tol, in.p.max_iter, Reference<Preconditioner>(new InCholeskyPreconditioner(1e-3, 0.0)))));
+  od_scene* sf_scene = new_scene(ctx, in);
+  RefSetup sf = make_setup(in);
+  auto* gic = new od_dropin::GpuInCholeskyPreconditioner(sf_scene, 1e-3, 0.0);
+  Reference<Preconditioner> gic_ref(gic);
+  const std::vector<double> uf = run_reference_loop(
+      in, sf, reference_material(in), Reference<LinearSolver<Mat>>(new CGSolver(in.p.tol, in.p.max_iter, gic_ref)));
+
+  check(gm->last_status, "GpuMaterial");
+  check(gcg->last_status, "GpuCGSolver");
+  check(gic->last_status, "GpuInCholeskyPreconditioner");
+  const double eb = rel_diff(ub, ua), ec = rel_diff(uc, ua), ed = rel_diff(ud, ua), ef = rel_diff(uf, ue);
+  double umax = 0.0;
+  for (double x : ua) umax = std::max(umax, fabs(x));
+  printf("umax %.6e material %.3e solver %.3e integrator %.3e ic_preconditioner %.3e\n", umax, eb, ec, ed, ef);
+  for (od_scene* s : {sb_scene, sc_scene, sd_scene, sf_scene}) od_scene_destroy(s);
+  od_ctx_destroy(ctx);
+  const bool ok = !bad && umax > 0.0 && eb <= tol_ok && ec <= tol_ok && ed <= tol_ok && ef <= tol_ok;
+  return ok ? 0 : 1;
+}
