@@ -5,10 +5,16 @@
 //   B  with GpuMaterial in place of the reference material,
 //   C  with GpuCGSolver in place of CGSolver,
 //   D  GpuIntergrator in place of the whole integrator,
-//   E  as shipped with InCholeskyPreconditioner, and
-//   F  CGSolver with GpuInCholeskyPreconditioner;
-// prints the relative displacement differences B, C, D against A and F
-// against E, and exits 0 when all are within the given tolerance.
+//   E  as shipped with InCholeskyPreconditioner,
+//   F  CGSolver with GpuInCholeskyPreconditioner,
+//   G  as shipped with InLDLTPreconditioner,
+//   H  CGSolver with GpuInLDLTPreconditioner,
+//   I  as shipped with plane collision damping (MeshPlaneCollisionDampingForcer
+//      on every element, the integrator's velocities, before every step), and
+//   J  GpuIntergrator with the same damping;
+// prints the relative displacement differences B, C, D against A, F against
+// E, H against G and J against I, and exits 0 when all are within the given
+// tolerance.
 //
 // usage: dropin_check <dir> <tolerance>; <dir> holds params.txt (n_nodes
 // n_tets n_facets n_cdofs rho youngs poisson threshold dt alpha_m beta_k tol
@@ -41,6 +47,7 @@
 #include "cgSolver.h"
 #include "constrainer.h"
 #include "inCholeskyPreconditioner.h"
+#include "inLDLTPreconditioner.h"
 #include "invertibleNeoHookean.h"
 #include "jacobiPreconditioner.h"
 #include "nonlinearImplicitBackwardEuler.h"
@@ -139,6 +146,32 @@ std::vector<double> run_reference_loop(const Input& in, RefSetup& s,
   for (int k = 0; k < in.p.steps; k++) {
     be.runOneTimeStep();
     be.updateMeshVerticesDisplacements(s.indexer, s.mesh);
+  }
+  return displacements(s, in.p.n_nodes);
+}
+
+// any integrator (the reference's or the drop-in, through the base class)
+// with plane damping on every element, set up before every step as a
+// collision loop does (odref_be_plane_damping in oracle/ref_harness.cpp)
+std::vector<double> damped_loop(const Input& in, RefSetup& s, Intergrator& it) {
+  Forcer f;
+  Scalar g[3] = {in.p.g[0], in.p.g[1], in.p.g[2]};
+  f.addBodyForce(s.mesh, g, s.indexer);
+  it.setExternalVirtualWork(f);
+  std::vector<Vector3> vel((size_t)in.p.n_nodes);
+  Collision::StaticPlaneShape plane;
+  plane.planeNormal = Vector3(0.0, 0.0, 1.0);
+  plane.planeConstant = 0.0;
+  for (int k = 0; k < in.p.steps; k++) {
+    it.clearExternalDampingForceMatrix();
+    it.getMeshVerticesVelocities(s.indexer, s.mesh, vel.data());
+    Collision::MeshPlaneCollisionDampingForcer fd(100.0, s.mesh, s.indexer, vel.data());
+    for (int e = 0; e < in.p.n_tets; e++) {
+      fd.setCollisionPair(plane, e);
+      it.addExternalDampingForceMatrix(fd);
+    }
+    it.runOneTimeStep();
+    it.updateMeshVerticesDisplacements(s.indexer, s.mesh);
   }
   return displacements(s, in.p.n_nodes);
 }
@@ -268,15 +301,50 @@ int main(int argc, char** argv) {
   const std::vector<double> uf = run_reference_loop(
       in, sf, reference_material(in), Reference<LinearSolver<Mat>>(new CGSolver(in.p.tol, in.p.max_iter, gic_ref)));
 
+  // G, H: incomplete LDL^T, the reference's and the drop-in
+  RefSetup sg = make_setup(in);
+  const std::vector<double> ug = run_reference_loop(
+      in, sg, reference_material(in),
+      Reference<LinearSolver<Mat>>(
+          new CGSolver(in.p.tol, in.p.max_iter, Reference<Preconditioner>(new InLDLTPreconditioner(0.1, 0.01)))));
+  od_scene* sh_scene = new_scene(ctx, in);
+  RefSetup sh = make_setup(in);
+  auto* gld = new od_dropin::GpuInLDLTPreconditioner(sh_scene, 0.1, 0.01);
+  Reference<Preconditioner> gld_ref(gld);
+  const std::vector<double> uh = run_reference_loop(
+      in, sh, reference_material(in), Reference<LinearSolver<Mat>>(new CGSolver(in.p.tol, in.p.max_iter, gld_ref)));
+
+  // I, J: plane collision damping through the integrator seam
+  RefSetup si = make_setup(in);
+  std::vector<double> ui;
+  {
+    NonlinearImplicitBackwardEuler<Mat> be(si.dofs, in.p.alpha_m, in.p.beta_k, in.p.dt, si.mesh, si.indexer,
+                                           reference_material(in), jacobi_cg());
+    ui = damped_loop(in, si, be);
+  }
+  od_scene* sj_scene = new_scene(ctx, in);
+  RefSetup sj = make_setup(in);
+  std::vector<double> uj;
+  {
+    od_dropin::GpuIntergrator gi(sj_scene, sj.dofs, ip);
+    uj = damped_loop(in, sj, gi);
+    check(gi.last_status, "GpuIntergrator with damping");
+  }
+
   check(gm->last_status, "GpuMaterial");
+  check(gld->last_status, "GpuInLDLTPreconditioner");
   check(gcg->last_status, "GpuCGSolver");
   check(gic->last_status, "GpuInCholeskyPreconditioner");
   const double eb = rel_diff(ub, ua), ec = rel_diff(uc, ua), ed = rel_diff(ud, ua), ef = rel_diff(uf, ue);
+  const double eh = rel_diff(uh, ug), ej = rel_diff(uj, ui), edamp = rel_diff(ui, ua);
   double umax = 0.0;
   for (double x : ua) umax = std::max(umax, fabs(x));
-  printf("umax %.6e material %.3e solver %.3e integrator %.3e ic_preconditioner %.3e\n", umax, eb, ec, ed, ef);
-  for (od_scene* s : {sb_scene, sc_scene, sd_scene, sf_scene}) od_scene_destroy(s);
+  printf("umax %.6e material %.3e solver %.3e integrator %.3e ic_preconditioner %.3e ldlt_preconditioner %.3e "
+         "damped_integrator %.3e (damping changes the reference's motion by %.3e)\n",
+         umax, eb, ec, ed, ef, eh, ej, edamp);
+  for (od_scene* s : {sb_scene, sc_scene, sd_scene, sf_scene, sh_scene, sj_scene}) od_scene_destroy(s);
   od_ctx_destroy(ctx);
-  const bool ok = !bad && umax > 0.0 && eb <= tol_ok && ec <= tol_ok && ed <= tol_ok && ef <= tol_ok;
+  const bool ok = !bad && umax > 0.0 && edamp > 10.0 * tol_ok && eb <= tol_ok && ec <= tol_ok && ed <= tol_ok &&
+                  ef <= tol_ok && eh <= tol_ok && ej <= tol_ok;
   return ok ? 0 : 1;
 }

@@ -1,9 +1,11 @@
 """The C++ drop-in classes run inside the reference's own time loop and give
 the reference's results: tests/dropin/dropin_check.cpp steps one
 Neo-Hookean cantilever with the reference's backward Euler as shipped, then
-with GpuMaterial, GpuCGSolver and GpuInCholeskyPreconditioner swapped in,
-and with GpuIntergrator in place of the integrator; every variant's
-displacements stay within 1e-8 of the reference's.  Needs the compiled
+with GpuMaterial, GpuCGSolver, GpuInCholeskyPreconditioner and
+GpuInLDLTPreconditioner swapped in, and with GpuIntergrator in place of the
+integrator, with and without plane collision damping handed over the
+integrator seam; every variant's displacements stay within 1e-8 of the
+reference's (and the damping does change the motion).  Needs the compiled
 reference (oracle/_ref, made by oracle/build_ref.py) and a GPU.
 """
 import os
