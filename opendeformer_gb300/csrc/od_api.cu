@@ -327,7 +327,11 @@ static od_status scene_build(Scene* s, int n_nodes, const double* X, int n_tets,
     OD_TRY(dalloc(s, v, np));
     OD_CUDA(cudaMemset(*v, 0, sizeof(double) * np));
   }
-  if (ne > 0 && 78LL * ne < (long long)INT32_MAX) {
+  // OD_GB300_ASSEMBLY=scatter keeps the per-colour scatter (the path of
+  // meshes whose gather lists overflow 32-bit indices) for every scene
+  const char* asm_env = std::getenv("OD_GB300_ASSEMBLY");
+  const bool scatter_only = asm_env && std::strcmp(asm_env, "scatter") == 0;
+  if (ne > 0 && 78LL * ne < (long long)INT32_MAX && !scatter_only) {
     // gather lists of the assembly: per destination its (entry, staged
     // element) sources in element index order, counting sort on the host
     std::vector<int> pos(ne), kptr((size_t)s->nvals + 1, 0), fptr(np + 1, 0);

@@ -103,3 +103,37 @@ def test_batch_rejects_what_it_cannot_batch():
     s = make_scene(0)
     with pytest.raises(RuntimeError):
         api.Batch(ctx(), [s, s])
+
+
+def test_colour_scatter_assembly_matches_the_gather(monkeypatch):
+    """OD_GB300_ASSEMBLY=scatter keeps the per-colour scatter (the assembly of
+    meshes whose gather lists would overflow 32-bit indices) for every scene:
+    the same element values summed in colour order instead of element order
+    give the same steps within rounding, for a scene alone (plastic material
+    included) and for a batch."""
+    g = meshgen.tet_grid(10, 4, 4, h=0.05, jitter=0.1, seed=21)
+    cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+    out = {}
+    for mode in ("gather", "scatter"):
+        if mode == "scatter":
+            monkeypatch.setenv("OD_GB300_ASSEMBLY", "scatter")
+        else:
+            monkeypatch.delenv("OD_GB300_ASSEMBLY", raising=False)
+        res = []
+        for mat in (api.InvertibleNeoHookeanMaterial(1000.0, 98640.0, 0.45, 0.1),
+                    api.CorotationalPlasticMaterial(1000.0, 1e5, 0.45, 1e-3, 0.5, 0.05, 0.1)):
+            s = api.Scene(ctx(), g.X, g.tets, g.facets, cd, mat)
+            s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, 0.01, 0.001, 1 / 60,
+                                                   api.CGSolver(1e-10, 3000, api.BlockJacobiPreconditioner()), 2))
+            s.set_loads(body=[0.0, 0.0, -9800.0])
+            assert s.step(8).status == 0
+            res.append(s.displacements())
+        batched = [make_scene(k) for k in range(len(SPECS))]
+        b = api.Batch(ctx(), batched)
+        st = b.step(4)
+        b.close()
+        assert all(x.status == 0 for x in st)
+        res += [s.displacements() for s in batched]
+        out[mode] = res
+    for a, b in zip(out["scatter"], out["gather"]):
+        assert rel_err(a, b) <= 1e-8
