@@ -1819,7 +1819,12 @@ static od_status ic0_build(Scene* s) {
     const size_t smem = sizeof(double) * (size_t)kIcfWarps * (2 * (size_t)maxrow + (size_t)maxpairs);
     int dev_coop = 0, per_sm = 0;
     OD_CUDA(cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, s->ctx->device));
-    if (dev_coop && pa.size() < (size_t)INT32_MAX && smem <= 96 * 1024 && maxrow <= 32 * kIcfSlots) {
+    // OD_GB300_IC0_FACTOR=levels keeps the one-launch-per-level factorisation
+    // (the path of rows too long for the warp's registers or shared memory)
+    const char* fenv = std::getenv("OD_GB300_IC0_FACTOR");
+    const bool levels_only = fenv && std::strcmp(fenv, "levels") == 0;
+    if (dev_coop && !levels_only && pa.size() < (size_t)INT32_MAX && smem <= 96 * 1024 &&
+        maxrow <= 32 * kIcfSlots) {
       OD_CUDA(cudaFuncSetAttribute(ic0_factor_coop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       OD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ic0_factor_coop_kernel, kIcfThreads, smem));
       if (per_sm > 0) {

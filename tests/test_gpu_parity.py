@@ -267,3 +267,22 @@ def test_relabeled_mesh_gives_the_same_motion():
         out.append(s.displacements())
     # facet ids keep their meaning (facets are permuted node-wise, not reordered)
     assert rel_err(out[1][labels], out[0]) <= 1e-8
+
+
+def test_ic0_factor_paths_agree(golden, monkeypatch):
+    """The one-launch IC(0) factorisation and the one-launch-per-level one
+    (OD_GB300_IC0_FACTOR=levels, kept for rows too long for the warp) give
+    the same PCG: iterations within 1, solutions within 1e-10."""
+    out = {}
+    for mode in ("coop", "levels"):
+        if mode == "levels":
+            monkeypatch.setenv("OD_GB300_IC0_FACTOR", "levels")
+        else:
+            monkeypatch.delenv("OD_GB300_IC0_FACTOR", raising=False)
+        s, p, e = gpu_scene(golden, "neohookean", "full")
+        A = e["values"] * (1.0 / 3600.0) + e["mass"]
+        out[mode] = s.pcg(A, e["cg_b"], solver=api.CGSolver(1e-11, 5000, api.Preconditioner("ic0")))
+    (x1, s1), (x0, s0) = out["coop"], out["levels"]
+    assert s1.status == 0 and s0.status == 0
+    assert abs(s1.iterations - s0.iterations) <= 1
+    assert rel_err(x1, x0) <= 1e-10
