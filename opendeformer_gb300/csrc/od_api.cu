@@ -331,41 +331,9 @@ static od_status scene_build(Scene* s, int n_nodes, const double* X, int n_tets,
   // meshes whose gather lists overflow 32-bit indices) for every scene
   const char* asm_env = std::getenv("OD_GB300_ASSEMBLY");
   const bool scatter_only = asm_env && std::strcmp(asm_env, "scatter") == 0;
-  if (ne > 0 && 78LL * ne < (long long)INT32_MAX && !scatter_only) {
-    // gather lists of the assembly: per destination its (entry, staged
-    // element) sources in element index order, counting sort on the host
-    std::vector<int> pos(ne), kptr((size_t)s->nvals + 1, 0), fptr(np + 1, 0);
-    for (int e = 0; e < ne; e++) pos[s->elem_perm[e]] = e;
-    for (int o = 0; o < ne; o++) {
-      for (int k = 0; k < 78; k++) {
-        const int idx = s->hemap[78 * (size_t)o + k];
-        if (idx >= 0) kptr[(size_t)idx + 1]++;
-      }
-      for (int k = 0; k < 12; k++) {
-        const int g = gidx[12 * (size_t)o + k];
-        if (g >= 0) fptr[(size_t)g + 1]++;
-      }
-    }
-    for (size_t i = 0; i < kptr.size() - 1; i++) kptr[i + 1] += kptr[i];
-    for (size_t i = 0; i < fptr.size() - 1; i++) fptr[i + 1] += fptr[i];
-    std::vector<int> ksrc(std::max(1, kptr.back())), fsrc(std::max(1, fptr.back()));
-    std::vector<int> kcur(kptr.begin(), kptr.end() - 1), fcur(fptr.begin(), fptr.end() - 1);
-    for (int o = 0; o < ne; o++) {
-      const int e = pos[o];
-      for (int k = 0; k < 78; k++) {
-        const int idx = s->hemap[78 * (size_t)o + k];
-        if (idx >= 0) ksrc[kcur[idx]++] = k * ne + e;
-      }
-      for (int k = 0; k < 12; k++) {
-        const int g = gidx[12 * (size_t)o + k];
-        if (g >= 0) fsrc[fcur[g]++] = k * ne + e;
-      }
-    }
-    OD_TRY(dupload(s, &s->gat_kptr, kptr.data(), kptr.size()));
-    OD_TRY(dupload(s, &s->gat_ksrc, ksrc.data(), ksrc.size()));
-    OD_TRY(dupload(s, &s->gat_fptr, fptr.data(), fptr.size()));
-    OD_TRY(dupload(s, &s->gat_fsrc, fsrc.data(), fsrc.size()));
-  }
+  // gather lists of the assembly (per destination its (entry, staged
+  // element) sources in element index order), built on the device
+  if (!scatter_only) OD_TRY(build_gather_lists(s, (int)np));
   OD_TRY(launch_precompute(s));
   OD_TRY(launch_mass(s));
   OD_TRY(sync_stream(s));

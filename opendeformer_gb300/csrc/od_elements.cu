@@ -770,6 +770,127 @@ __global__ void scatter_batch_kernel(int n_sc, const int* __restrict__ prefix, i
   }
 }
 
+// ---- the gather lists, built on the device once per scene: count the
+// contributions of every destination, scan the counts into the list
+// offsets, place every source with an atomic cursor, then sort each list
+// by (original element index, entry index) -- the reference's assembly
+// order, whatever order the atomics placed them in.
+constexpr int kScanBlock = 1024;
+
+__global__ void gl_count_kernel(long long n, const int* __restrict__ dest, int* __restrict__ cnt) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int d = dest[t];
+    if (d >= 0) atomicAdd(&cnt[d + 1], 1);
+  }
+}
+
+// inclusive scan of each 1024-entry block in place; the block's total to sums
+__global__ void __launch_bounds__(kScanBlock) gl_scan_block_kernel(int n, int* __restrict__ data,
+                                                                   int* __restrict__ sums) {
+  __shared__ int warp_tot[kScanBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int i = blockIdx.x * kScanBlock + threadIdx.x;
+  int v = i < n ? data[i] : 0;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += y;
+  }
+  if (lane == 31) warp_tot[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    int w = warp_tot[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    warp_tot[lane] = w;
+  }
+  __syncthreads();
+  if (warp > 0) v += warp_tot[warp - 1];
+  if (i < n) data[i] = v;
+  if (threadIdx.x == kScanBlock - 1) sums[blockIdx.x] = v;
+}
+
+__global__ void __launch_bounds__(kScanBlock) gl_add_kernel(int n, int* __restrict__ data,
+                                                            const int* __restrict__ offs) {
+  const int i = blockIdx.x * kScanBlock + threadIdx.x;
+  if (i < n) data[i] += offs[blockIdx.x];
+}
+
+__global__ void gl_fill_kernel(long long n, const int* __restrict__ dest, int* __restrict__ cur,
+                               int* __restrict__ src) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int d = dest[t];
+    if (d >= 0) src[atomicAdd(&cur[d], 1)] = (int)t;
+  }
+}
+
+// source t = k * ne + e (e the staged position) sorts by perm[e] * kk + k
+__global__ void gl_sort_kernel(int nd, const int* __restrict__ ptr, int* __restrict__ src,
+                               const int* __restrict__ perm, int ne, int kk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nd) return;
+  const int a = ptr[i], b = ptr[i + 1];
+  for (int j = a + 1; j < b; j++) {
+    const int v = src[j];
+    const long long key = (long long)perm[v % ne] * kk + v / ne;
+    int q = j - 1;
+    while (q >= a) {
+      const int w = src[q];
+      if ((long long)perm[w % ne] * kk + w / ne <= key) break;
+      src[q + 1] = w;
+      q--;
+    }
+    src[q + 1] = v;
+  }
+}
+
+static od_status gather_list(Scene* s, const int* dest, int kk, int nd, int** ptr_out, int** src_out) {
+  const int ne = s->n_tets;
+  cudaStream_t st = s->ctx->stream;
+  const long long n = (long long)kk * ne;
+  const int grid = std::max(1, (int)std::min<long long>((n + 255) / 256, 64LL * std::max(1, s->ctx->num_sms)));
+  int *ptr = nullptr, *sums = nullptr, *cur = nullptr, *src = nullptr;
+  const int nscan = nd + 1, nb = (nscan + kScanBlock - 1) / kScanBlock;
+  OD_CUDA(cudaMalloc(&ptr, sizeof(int) * (size_t)nscan));
+  OD_CUDA(cudaMalloc(&sums, sizeof(int) * (size_t)nb));
+  OD_CUDA(cudaMemsetAsync(ptr, 0, sizeof(int) * (size_t)nscan, st));
+  gl_count_kernel<<<grid, 256, 0, st>>>(n, dest, ptr);
+  gl_scan_block_kernel<<<nb, kScanBlock, 0, st>>>(nscan, ptr, sums);
+  std::vector<int> hs(nb);
+  OD_CUDA(cudaMemcpyAsync(hs.data(), sums, sizeof(int) * (size_t)nb, cudaMemcpyDeviceToHost, st));
+  OD_TRY(sync_stream(s));
+  long long run = 0;
+  for (int b = 0; b < nb; b++) {
+    const long long t = hs[b];
+    hs[b] = (int)run;
+    run += t;
+  }
+  const int total = (int)run;
+  OD_CUDA(cudaMemcpyAsync(sums, hs.data(), sizeof(int) * (size_t)nb, cudaMemcpyHostToDevice, st));
+  gl_add_kernel<<<nb, kScanBlock, 0, st>>>(nscan, ptr, sums);
+  OD_CUDA(cudaMalloc(&src, sizeof(int) * (size_t)std::max(1, total)));
+  OD_CUDA(cudaMalloc(&cur, sizeof(int) * (size_t)std::max(1, nd)));
+  if (nd > 0) OD_CUDA(cudaMemcpyAsync(cur, ptr, sizeof(int) * (size_t)nd, cudaMemcpyDeviceToDevice, st));
+  gl_fill_kernel<<<grid, 256, 0, st>>>(n, dest, cur, src);
+  if (nd > 0) gl_sort_kernel<<<(nd + 255) / 256, 256, 0, st>>>(nd, ptr, src, s->perm, ne, kk);
+  OD_CUDA(cudaGetLastError());
+  OD_TRY(sync_stream(s));   // hs is read by the copy above; the temporaries go next
+  cudaFree(sums);
+  cudaFree(cur);
+  s->device_bytes += (long long)sizeof(int) * ((long long)nscan + std::max(1, total));
+  *ptr_out = ptr;
+  *src_out = src;
+  return OD_OK;
+}
+
+od_status build_gather_lists(Scene* s, int n_pad) {
+  if (s->n_tets <= 0 || 78LL * s->n_tets >= (long long)INT32_MAX) return OD_OK;
+  OD_TRY(gather_list(s, s->emap, 78, s->nvals, &s->gat_kptr, &s->gat_ksrc));
+  OD_TRY(gather_list(s, s->gdof, 12, n_pad, &s->gat_fptr, &s->gat_fsrc));
+  return OD_OK;
+}
+
 // multi-scene gathered assembly: tile j of scene s covers its destinations
 // [256 j, 256 j + 256) (K values, then the padded f_int entries)
 __global__ void __launch_bounds__(256) gather_batch_kernel(int n_sc, const int* __restrict__ prefix,
