@@ -58,7 +58,7 @@ struct SweepSys {
   double* lo_dev = nullptr;          // A in the reference lower layout (device)
   double* lo_host = nullptr;         // pinned mirror
   int *f_rp = nullptr, *f_ci = nullptr, *b_cp = nullptr, *b_ri = nullptr;
-  int *ord_f = nullptr, *ord_b = nullptr;   // rows by forward / backward level
+  int *ord_f = nullptr, *ord_b = nullptr;   // row triples by forward / backward level
   double *f_val = nullptr, *b_val = nullptr, *y = nullptr;
   double* diag = nullptr;            // D^-1 (LDL^T) or 1 / L_ii (IC)
   int *err = nullptr, *err_host = nullptr;
@@ -409,7 +409,7 @@ od_status lower_values(Scene* s, SweepSys* l, const double* host_values, const d
 }
 
 // upload the staged strictly lower part (h_cp / h_ri / h_bval, by columns)
-// and diagonal (h_diag): forward CSR, dependency levels and row lists
+// and diagonal (h_diag): forward CSR, dependency levels and row-triple lists
 od_status upload(Scene* s, SweepSys* l, int kind) {
   const int n = l->n;
   const long long nnz = (long long)l->h_ri.size();
