@@ -142,6 +142,15 @@ def pcg_iteration_bytes(info, precond):
     return spmv_bytes(info) + (16 + 8 + 8 + 16 + 8) * n + pre + (16 + 8) * n
 
 
+def pcg_iteration_fmas(info, precond):
+    """FP64 multiply-adds of one PCG iteration: 9 per stored block (SpMV), 9
+    per block row (block-Jacobi) or 1 per DOF (Jacobi), and 6 per DOF for
+    x, r, p and the three dot products."""
+    nb = (info.dofs + 2) // 3
+    pre = {"block_jacobi": 9 * nb, "jacobi": 3 * nb}.get(precond, 0)
+    return 9 * info.num_full_blocks + pre + 6 * 3 * nb
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -788,11 +797,18 @@ def run_gpu(args, wl):
         tkey = "pcg_spmv_kernel"
     achieved = nbytes / (avg_ms * 1e-3) / 1e9 if kl else None
     traffic = traffic_from_profiles(args.workload, tkey)
+    fp64 = None
+    if counters.pcg_launches:
+        fmas = 9 * info.num_full_blocks + avg_iters * pcg_iteration_fmas(info, args.precond)
+        fp64 = {"fma_per_launch": fmas, "achieved_gflops": 2.0 * fmas / (avg_ms * 1e-3) / 1e9,
+                "pipe_active_pct": 43.8,
+                "pipe_source": "ncu sm__pipe_fp64_cycles_active of this kernel on this workload "
+                               "(profiles/pcg_persistent_kernel_beam98k_nh_newmark_fp64.md)"}
     roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": nbytes,
                 "avg_launch_ms": avg_ms, "launches": kl,
-                "share_of_step_time": kms / total_ms if total_ms else None,
+                "share_of_step_time": kms / total_ms if total_ms else None, "fp64": fp64,
                 "note": "FP64 on GB300 runs at about one operation per SM per cycle: the FP64 solve is bound "
                         "by the FP64 pipe, not HBM, and the 98k-tet system (18.6 MB) stays L2-resident"}
     cpu = None
