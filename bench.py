@@ -234,7 +234,7 @@ def run_reference(args, wl):
         iters += one()
     el = time.perf_counter() - t0
     v = args.steps / el
-    line = {"metric": "newmark_steps_per_s", "value": v, "unit": "steps/s", "n_gpus": 0, "steps": args.steps,
+    line = {"metric": "newmark_steps_per_s", "value": v, "unit": "steps/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * el / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
