@@ -802,8 +802,8 @@ def run_gpu(args, wl):
         fmas = 9 * info.num_full_blocks + avg_iters * pcg_iteration_fmas(info, args.precond)
         fp64 = {"fma_per_launch": fmas, "achieved_gflops": 2.0 * fmas / (avg_ms * 1e-3) / 1e9,
                 "pipe_active_pct": 43.8,
-                "pipe_source": "ncu sm__pipe_fp64_cycles_active of this kernel on this workload "
-                               "(profiles/pcg_persistent_kernel_beam98k_nh_newmark_fp64.md)"}
+                "pipe_source": "ncu --set full capture of this kernel on this workload "
+                               "(sm__pipe_fp64_cycles_active, of peak, active cycles)"}
     roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": nbytes,
