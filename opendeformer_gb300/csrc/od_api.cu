@@ -746,7 +746,8 @@ od_status od_step(od_scene* scene, int n_steps, od_step_stats* stats) {
                         std::sin(2.0 * 3.14159265358979323846 * s->sched_freq * t + s->sched_phase));
       if (st != OD_OK) break;
     }
-    st = s->ip.kind == OD_INTEGRATOR_NEWMARK ? nm_step(s, &acc) : be_step(s, &acc);
+    // no free DOF: nothing moves (every displacement is prescribed)
+    if (s->dofs > 0) st = s->ip.kind == OD_INTEGRATOR_NEWMARK ? nm_step(s, &acc) : be_step(s, &acc);
     if (st == OD_OK) { acc.steps++; s->time += s->ip.dt; }
   }
   cudaEventRecord(s->ev_step[1], s->ctx->stream);

@@ -975,6 +975,7 @@ od_status launch_eval(Scene* s, bool zero_first) {
   //    whose gather lists do not fit 32-bit indices
   if (s->gat_kptr) {
     const long long nd = (long long)s->nvals + s->pcg.n_pad;
+    if (nd == 0) return OD_OK;
     OD_KL(s);
     gather_kernel<<<nblk(nd, 256), 256, 0, st>>>(s->nvals, s->gat_kptr, s->gat_ksrc, s->stage_k, s->K, s->pcg.n_pad,
                                                  s->gat_fptr, s->gat_fsrc, s->stage_f, s->fint, zero_first ? 0 : 1);

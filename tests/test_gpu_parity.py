@@ -286,3 +286,38 @@ def test_ic0_factor_paths_agree(golden, monkeypatch):
     assert s1.status == 0 and s0.status == 0
     assert abs(s1.iterations - s0.iterations) <= 1
     assert rel_err(x1, x0) <= 1e-10
+
+
+def test_degenerate_scenes_step():
+    """Edge cases of the setup and assembly paths: a single tetrahedron, and
+    a mesh with every DOF constrained (no free DOF, empty force lists); both
+    evaluate and step with status OK, the single element matching the
+    oracle's values."""
+    from oracle import restated as O
+    X = np.array([[0.0, 0.0, 0.0], [0.1, 0.0, 0.0], [0.0, 0.1, 0.0], [0.0, 0.0, 0.1]])
+    tets = np.array([[0, 1, 2, 3]], dtype=np.int32)
+    facets = np.array([[0, 2, 1], [0, 1, 3], [0, 3, 2], [1, 2, 3]], dtype=np.int32)
+    cd = meshgen.constrained_dofs_for_nodes(np.array([0]))
+    mat = api.InvertibleNeoHookeanMaterial(1000.0, 1e5, 0.45, 0.1)
+    s = api.Scene(ctx(), X, tets, facets, cd, mat)
+    u = np.zeros((4, 3))
+    u[1:, :] = [[0.002, -0.001, 0.0], [0.0, 0.003, 0.001], [-0.001, 0.0, 0.002]]
+    s.set_displacements(u)
+    vals, f = s.evaluate()
+    o = O.OracleScene(X, tets, facets, cd, "neohookean", 1000.0, 1e5, 0.45, 0.1)
+    o.set_displacements(u)
+    ov, of = o.assemble()
+    assert rel_err(vals, ov) <= 1e-12 and rel_err(f, of) <= 1e-12
+    s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, 0.01, 0.001, 1 / 60,
+                                             api.CGSolver(1e-10, 100, api.BlockJacobiPreconditioner()), 2))
+    s.set_loads(body=[0.0, 0.0, -9800.0])
+    assert s.step(3).status == 0
+    g = meshgen.tet_grid(2, 2, 2, h=0.05)
+    all_dofs = np.arange(3 * g.n_nodes, dtype=np.int32)
+    s2 = api.Scene(ctx(), g.X, g.tets, g.facets, all_dofs, mat)
+    assert s2.dofs == 0
+    v2, f2 = s2.evaluate()
+    assert f2.size == 0
+    s2.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, 0.01, 0.001, 1 / 60,
+                                              api.CGSolver(1e-10, 100, api.BlockJacobiPreconditioner()), 1))
+    assert s2.step(2).status == 0
