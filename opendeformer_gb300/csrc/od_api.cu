@@ -228,6 +228,7 @@ static void scene_free(Scene* s) {
                   (void*)s->K, (void*)s->M, (void*)s->Dm, (void*)s->fint, (void*)s->fext, (void*)s->work_vals,
                   (void*)s->A64, (void*)s->v, (void*)s->d, (void*)s->a, (void*)s->dp, (void*)s->vp,
                   (void*)s->dv, (void*)s->rhs, (void*)s->tmp, (void*)s->trac_facets, (void*)s->trac_vec,
+                  (void*)s->load_ptr, (void*)s->load_src,
                   (void*)s->bsr.row_ptr, (void*)s->bsr.col, (void*)s->bsr.desc_off, (void*)s->bsr.desc_kind,
                   (void*)s->bsr.gen, (void*)s->bsr.diag_pos, (void*)s->tmp2, (void*)s->stage_k,
                   (void*)s->stage_f, (void*)s->color_off_dev, (void*)s->plastic, (void*)s->gat_kptr,
@@ -549,8 +550,9 @@ od_status od_scene_set_loads(od_scene* scene, const double* body, int n_groups, 
   OD_CHECK_ARG(n_groups >= 0 && (n_groups == 0 || (tractions && group_sizes)), "od_scene_set_loads: bad groups");
   Scene* s = &scene->s;
   OD_CUDA(cudaSetDevice(s->ctx->device));
-  // flatten (facet, traction) pairs and colour them on shared nodes
-  std::vector<int> fid, nodes;
+  // flatten the (facet, traction) pairs in the order given, and list for
+  // every free DOF the pairs that load it, in that order
+  std::vector<int> fid;
   std::vector<double> tv;
   int q = 0;
   for (int g = 0; g < n_groups; g++) {
@@ -560,19 +562,27 @@ od_status od_scene_set_loads(od_scene* scene, const double* body, int n_groups, 
       int f = facet_ids[q];
       OD_CHECK_ARG(f >= 0 && f < s->n_facets, "od_scene_set_loads: facet id out of range");
       fid.push_back(f);
-      for (int i = 0; i < 3; i++) { nodes.push_back(s->hfacets[3 * (size_t)f + i]); tv.push_back(tractions[3 * g + i]); }
+      for (int i = 0; i < 3; i++) tv.push_back(tractions[3 * g + i]);
     }
   }
   const int nf = (int)fid.size();
   if (nf > 0) {
-    std::vector<int> perm;
-    color_elements(nodes, 3, nf, s->n_nodes, perm, s->trac_color_off);
-    std::vector<int> fo(nf);
-    std::vector<double> to(3 * (size_t)nf);
-    for (int i = 0; i < nf; i++) {
-      fo[i] = fid[perm[i]];
-      for (int d = 0; d < 3; d++) to[3 * i + d] = tv[3 * perm[i] + d];
-    }
+    const int np = std::max(1, s->pcg.n_pad);
+    std::vector<int> lptr((size_t)np + 1, 0);
+    for (int k = 0; k < nf; k++)
+      for (int v = 0; v < 3; v++)
+        for (int ax = 0; ax < 3; ax++) {
+          const int gd = s->hnode_dof[3 * (size_t)s->hfacets[3 * (size_t)fid[k] + v] + ax];
+          if (gd >= 0) lptr[(size_t)gd + 1]++;
+        }
+    for (int i = 0; i < np; i++) lptr[i + 1] += lptr[i];
+    std::vector<int> lsrc(std::max(1, lptr[np])), cur(lptr.begin(), lptr.end() - 1);
+    for (int k = 0; k < nf; k++)
+      for (int v = 0; v < 3; v++)
+        for (int ax = 0; ax < 3; ax++) {
+          const int gd = s->hnode_dof[3 * (size_t)s->hfacets[3 * (size_t)fid[k] + v] + ax];
+          if (gd >= 0) lsrc[cur[gd]++] = k;
+        }
     if (nf > s->trac_cap) {
       cudaFree(s->trac_facets);
       cudaFree(s->trac_vec);
@@ -582,8 +592,19 @@ od_status od_scene_set_loads(od_scene* scene, const double* body, int n_groups, 
       OD_TRY(dalloc(s, &s->trac_vec, 3 * (size_t)nf));
       s->trac_cap = nf;
     }
-    OD_CUDA(cudaMemcpyAsync(s->trac_facets, fo.data(), sizeof(int) * nf, cudaMemcpyHostToDevice, s->ctx->stream));
-    OD_CUDA(cudaMemcpyAsync(s->trac_vec, to.data(), sizeof(double) * 3 * nf, cudaMemcpyHostToDevice, s->ctx->stream));
+    if (!s->load_ptr) OD_TRY(dalloc(s, &s->load_ptr, (size_t)np + 1));
+    if ((int)lsrc.size() > s->load_cap) {
+      cudaFree(s->load_src);
+      s->load_src = nullptr;
+      OD_TRY(dalloc(s, &s->load_src, lsrc.size()));
+      s->load_cap = (int)lsrc.size();
+    }
+    OD_CUDA(cudaMemcpyAsync(s->trac_facets, fid.data(), sizeof(int) * nf, cudaMemcpyHostToDevice, s->ctx->stream));
+    OD_CUDA(cudaMemcpyAsync(s->trac_vec, tv.data(), sizeof(double) * 3 * nf, cudaMemcpyHostToDevice, s->ctx->stream));
+    OD_CUDA(cudaMemcpyAsync(s->load_ptr, lptr.data(), sizeof(int) * lptr.size(), cudaMemcpyHostToDevice,
+                            s->ctx->stream));
+    OD_CUDA(cudaMemcpyAsync(s->load_src, lsrc.data(), sizeof(int) * lsrc.size(), cudaMemcpyHostToDevice,
+                            s->ctx->stream));
   }
   s->n_trac = nf;
   s->has_body = body != nullptr;

@@ -128,39 +128,41 @@ __global__ void node_vol_kernel(int e0, int e1, int ne, int vslot, const int4* _
 
 // body force density times the node's volume share (Forcer::addBodyForce,
 // core/forcer.cpp:8-33 with TetElement::getBodyVirtualWorks, tetelement.cpp:68-77)
-__global__ void body_force_kernel(int n, const int* __restrict__ free_pos, const double* __restrict__ nv,
-                                  double bx, double by, double bz, double* __restrict__ fext) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+// external forces in one launch: per padded DOF its body force (nodal
+// volume x force density, TetElement::getBodyVirtualWorks,
+// tetelement.cpp:68-77), then its uniform traction entries over deformed
+// facets, area / 3 per vertex (TetFacet::getSurfVirtualWorks,
+// tetelement.cpp:79-89), added in the order the loads were given -- the
+// order in which Forcer accumulates them (forcer.cpp:8-96)
+__global__ void loads_kernel(int n, int dofs, const int* __restrict__ free_pos, const double* __restrict__ nv,
+                             double bx, double by, double bz, const int* __restrict__ lptr,
+                             const int* __restrict__ lsrc, const int* __restrict__ fids,
+                             const double* __restrict__ tvec, double scale, const int* __restrict__ facets,
+                             const double* __restrict__ X, const double* __restrict__ u,
+                             double* __restrict__ fext) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  int p = free_pos[i];
-  int ax = p % 3;
-  double b = ax == 0 ? bx : (ax == 1 ? by : bz);
-  fext[i] = nv[p / 3] * b;
-}
-
-// uniform traction over deformed facets, area / 3 per vertex
-// (TetFacet::getSurfVirtualWorks, tetelement.cpp:79-89); one facet colour
-__global__ void traction_kernel(int f0, int f1, const int* __restrict__ fids, const double* __restrict__ tvec,
-                                double scale, const int* __restrict__ facets, const double* __restrict__ X,
-                                const double* __restrict__ u, const int* __restrict__ node_dof,
-                                double* __restrict__ fext) {
-  int k = f0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= f1) return;
-  int f = fids[k];
-  int n[3] = {facets[3 * f], facets[3 * f + 1], facets[3 * f + 2]};
-  V3t<double> p[3];
-  for (int i = 0; i < 3; i++) {
-    p[i] = {X[3 * n[i]] + u[3 * n[i]], X[3 * n[i] + 1] + u[3 * n[i] + 1], X[3 * n[i] + 2] + u[3 * n[i] + 2]};
-  }
-  V3t<double> cr = v_cross(v_sub(p[1], p[0]), v_sub(p[2], p[0]));
-  double area = sqrt(v_len2(cr)) * 0.5;
-  double fac = area / 3.0;
-  for (int i = 0; i < 3; i++)
-    for (int ax = 0; ax < 3; ax++) {
-      double w = fac * (scale * tvec[3 * k + ax]);
-      int g = node_dof[3 * n[i] + ax];
-      if (w != 0.0 && g >= 0) fext[g] += w;
+  double acc = 0.0;
+  if (i < dofs) {
+    const int p = free_pos[i];
+    const int ax = p % 3;
+    acc = nv[p / 3] * (ax == 0 ? bx : (ax == 1 ? by : bz));
+    if (lptr) {
+      for (int j = lptr[i]; j < lptr[i + 1]; j++) {
+        const int k = lsrc[j];
+        const int f = fids[k];
+        const int nd[3] = {facets[3 * f], facets[3 * f + 1], facets[3 * f + 2]};
+        V3t<double> q[3];
+        for (int v = 0; v < 3; v++)
+          q[v] = {X[3 * nd[v]] + u[3 * nd[v]], X[3 * nd[v] + 1] + u[3 * nd[v] + 1], X[3 * nd[v] + 2] + u[3 * nd[v] + 2]};
+        const V3t<double> cr = v_cross(v_sub(q[1], q[0]), v_sub(q[2], q[0]));
+        const double fac = (sqrt(v_len2(cr)) * 0.5) / 3.0;
+        const double w = fac * (scale * tvec[3 * k + ax]);
+        if (w != 0.0) acc += w;
+      }
     }
+  }
+  fext[i] = acc;
 }
 
 // -------------------------------------------------- corotational element
@@ -1020,22 +1022,15 @@ od_status launch_element_values(Scene* s, double* d_k78, double* d_f12) {
 od_status launch_loads(Scene* s, const double* body, int n_facets_total, double traction_scale) {
   const int T = 128;
   cudaStream_t st = s->ctx->stream;
+  const int n = s->pcg.n_pad;
+  if (n <= 0) return OD_OK;
   double b[3] = {0, 0, 0};
   if (body) { b[0] = body[0]; b[1] = body[1]; b[2] = body[2]; }
-  OD_CUDA(cudaMemsetAsync(s->fext, 0, sizeof(double) * (size_t)s->pcg.n_pad, st));
-  if (s->dofs > 0) {
-    OD_KL(s);
-    body_force_kernel<<<nblk(s->dofs, T), T, 0, st>>>(s->dofs, s->free_pos, s->node_vol4, b[0], b[1], b[2], s->fext);
-  }
-  if (n_facets_total > 0) {
-    for (size_t c = 0; c + 1 < s->trac_color_off.size(); c++) {
-      int f0 = s->trac_color_off[c], f1 = s->trac_color_off[c + 1];
-      if (f1 <= f0) continue;
-      OD_KL(s);
-      traction_kernel<<<nblk(f1 - f0, T), T, 0, st>>>(f0, f1, s->trac_facets, s->trac_vec, traction_scale,
-                                                       s->facets_dev, s->X, s->u, s->node_dof, s->fext);
-    }
-  }
+  const bool trac = n_facets_total > 0 && s->load_ptr;
+  OD_KL(s);
+  loads_kernel<<<nblk(n, T), T, 0, st>>>(n, s->dofs, s->free_pos, s->node_vol4, b[0], b[1], b[2],
+                                         trac ? s->load_ptr : nullptr, s->load_src, s->trac_facets, s->trac_vec,
+                                         traction_scale, s->facets_dev, s->X, s->u, s->fext);
   OD_CUDA(cudaGetLastError());
   return OD_OK;
 }

@@ -344,10 +344,12 @@ struct Scene {
   double time = 0.0;
   long long device_bytes = 0;
   // traction loads (per call)
-  int* trac_facets = nullptr;      // colour-ordered facet ids
-  double* trac_vec = nullptr;      // per facet traction (3)
+  int* trac_facets = nullptr;      // facet ids of the (facet, traction) pairs, in load order
+  double* trac_vec = nullptr;      // per pair traction (3)
   int trac_cap = 0;
-  std::vector<int> trac_color_off;
+  int* load_ptr = nullptr;         // per padded DOF: its traction entries (n_pad + 1)
+  int* load_src = nullptr;         // the (facet, traction) pair of each entry, in load order
+  int load_cap = 0;
   int n_trac = 0;                  // facet entries of the last od_scene_set_loads
   double load_body[3] = {0, 0, 0};
   bool has_body = false;
