@@ -126,8 +126,6 @@ __global__ void node_vol_kernel(int e0, int e1, int ne, int vslot, const int4* _
   nv[t.x] += q; nv[t.y] += q; nv[t.z] += q; nv[t.w] += q;
 }
 
-// body force density times the node's volume share (Forcer::addBodyForce,
-// core/forcer.cpp:8-33 with TetElement::getBodyVirtualWorks, tetelement.cpp:68-77)
 // external forces in one launch: per padded DOF its body force (nodal
 // volume x force density, TetElement::getBodyVirtualWorks,
 // tetelement.cpp:68-77), then its uniform traction entries over deformed
