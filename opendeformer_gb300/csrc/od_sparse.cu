@@ -1518,6 +1518,48 @@ __device__ __forceinline__ double icf_warp_read(const double* p, int* err) {
 }
 
 constexpr int kIcfSlots = 4;   // entries per lane: rows of up to 128 entries
+constexpr int kIcfBatch = 8;   // paired values per lane read before one cooperative wait
+
+// warp-cooperative bounded read of up to kIcfBatch values per lane (null:
+// none), all loads issued before the first wait; called by all 32 lanes
+__device__ __forceinline__ void icf_warp_read_batch(const double* const (&p)[kIcfBatch], double (&out)[kIcfBatch],
+                                                    int* err) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long v[kIcfBatch];
+#pragma unroll
+  for (int u = 0; u < kIcfBatch; u++) v[u] = p[u] ? ld_relaxed_u64(p[u]) : 0ull;
+  for (unsigned round = 1;; round++) {
+    int pu = -1;
+#pragma unroll
+    for (int u = kIcfBatch - 1; u >= 0; u--)
+      if (p[u] && v[u] == kPending) pu = u;
+    const unsigned ball = __ballot_sync(0xffffffffu, pu >= 0);
+    if (!ball) break;
+    int stop = 0;
+    if (lane == __ffs(ball) - 1) {
+      const double* q = nullptr;
+#pragma unroll
+      for (int u = 0; u < kIcfBatch; u++)
+        if (u == pu) q = p[u];
+      unsigned k = 0;
+      while (ld_relaxed_u64(q) == kPending && ++k < kIcfPollBurst) {
+      }
+      stop = round >= kIcfSpinLimit / kIcfPollBurst || *(volatile int*)err;
+      if (round >= kIcfSpinLimit / kIcfPollBurst) atomicOr(err, 1);
+    }
+    if (__any_sync(0xffffffffu, stop)) {
+#pragma unroll
+      for (int u = 0; u < kIcfBatch; u++)
+        if (v[u] == kPending) v[u] = 0ull;
+      break;
+    }
+#pragma unroll
+    for (int u = 0; u < kIcfBatch; u++)
+      if (p[u] && v[u] == kPending) v[u] = ld_relaxed_u64(p[u]);
+  }
+#pragma unroll
+  for (int u = 0; u < kIcfBatch; u++) out[u] = __longlong_as_double((long long)v[u]);
+}
 
 __global__ void __launch_bounds__(kIcfThreads) ic0_factor_coop_kernel(
     int n, const int* __restrict__ rows, const int* __restrict__ rp, const int* __restrict__ ci,
@@ -1547,10 +1589,20 @@ __global__ void __launch_bounds__(kIcfThreads) ic0_factor_coop_kernel(
       const double d = icf_warp_read(dp, err);
       if (q < m) dval[q] = dp ? d : 1.0;
     }
-    for (int b0 = 0; b0 < np; b0 += 32) {
-      const int p = b0 + lane;
-      const double v = icf_warp_read(p < np ? L + pb[p0 + p] : nullptr, err);
-      if (p < np) pv[p] = v;
+    for (int b0 = 0; b0 < np; b0 += 32 * kIcfBatch) {
+      const double* ptrs[kIcfBatch];
+      double vals[kIcfBatch];
+#pragma unroll
+      for (int u = 0; u < kIcfBatch; u++) {
+        const int p = b0 + u * 32 + lane;
+        ptrs[u] = p < np ? L + pb[p0 + p] : nullptr;
+      }
+      icf_warp_read_batch(ptrs, vals, err);
+#pragma unroll
+      for (int u = 0; u < kIcfBatch; u++) {
+        const int p = b0 + u * 32 + lane;
+        if (p < np) pv[p] = vals[u];
+      }
     }
     __syncwarp();
     // 2) right-looking over the row's entries
