@@ -1571,6 +1571,9 @@ __global__ void __launch_bounds__(kIcfThreads) ic0_factor_coop_kernel(
   double* aval = icf_s + (size_t)wib * (2 * maxrow + maxpairs);
   double* dval = aval + maxrow;
   double* pv = dval + maxrow;
+  // the pairs' row positions, staged beside the values (ints after all
+  // the warps' doubles)
+  int* pa_s = reinterpret_cast<int*>(icf_s + (size_t)kIcfWarps * (2 * maxrow + maxpairs)) + (size_t)wib * maxpairs;
   const int W = gridDim.x * kIcfWarps;
   for (int t = blockIdx.x * kIcfWarps + wib; t < n; t += W) {
     const int i = rows[t];
@@ -1601,7 +1604,10 @@ __global__ void __launch_bounds__(kIcfThreads) ic0_factor_coop_kernel(
 #pragma unroll
       for (int u = 0; u < kIcfBatch; u++) {
         const int p = b0 + u * 32 + lane;
-        if (p < np) pv[p] = vals[u];
+        if (p < np) {
+          pv[p] = vals[u];
+          pa_s[p] = pa[p0 + p];
+        }
       }
     }
     __syncwarp();
@@ -1620,7 +1626,7 @@ __global__ void __launch_bounds__(kIcfThreads) ic0_factor_coop_kernel(
         rinv[r] = 1.0 / dval[q];
         cur[r] = pp[bi + q] - p0;
         cend[r] = pp[bi + q + 1] - p0;
-        nxt[r] = cur[r] < cend[r] ? pa[p0 + cur[r]] : -1;
+        nxt[r] = cur[r] < cend[r] ? pa_s[cur[r]] : -1;
       }
     }
     for (int k = 0; k < m; k++) {
@@ -1656,7 +1662,7 @@ __global__ void __launch_bounds__(kIcfThreads) ic0_factor_coop_kernel(
           } else if (nxt[r] == k) {
             sv[r] -= v * pv[cur[r]];
             cur[r]++;
-            nxt[r] = cur[r] < cend[r] ? pa[p0 + cur[r]] : -1;
+            nxt[r] = cur[r] < cend[r] ? pa_s[cur[r]] : -1;
           }
         }
       }
@@ -1868,7 +1874,8 @@ static od_status ic0_build(Scene* s) {
   if ((st = up(&P.ic_gord_f, gof)) != OD_OK) return st;
   {
     // one-launch factorisation when a row and its pairs fit the shared memory
-    const size_t smem = sizeof(double) * (size_t)kIcfWarps * (2 * (size_t)maxrow + (size_t)maxpairs);
+    const size_t smem = sizeof(double) * (size_t)kIcfWarps * (2 * (size_t)maxrow + (size_t)maxpairs) +
+                        sizeof(int) * (size_t)kIcfWarps * (size_t)maxpairs;
     int dev_coop = 0, per_sm = 0;
     OD_CUDA(cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, s->ctx->device));
     // OD_GB300_IC0_FACTOR=levels keeps the one-launch-per-level factorisation
