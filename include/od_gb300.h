@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define OD_ABI_VERSION 5
+#define OD_ABI_VERSION 6
 
 typedef enum od_status {
   OD_OK = 0,
@@ -190,6 +190,13 @@ int od_abi_version(void);
 od_status od_ctx_create(int device, od_ctx** out);
 od_status od_ctx_destroy(od_ctx* ctx);
 od_status od_ctx_synchronize(od_ctx* ctx);
+/* Failure detection, tested without a GPU fault: runs the bounded device
+ * waits against conditions that never clear -- a grid barrier one CTA never
+ * reaches, a triangular-sweep wait on a value nobody writes -- and reports
+ * whether each ran out and raised its timeout flag (the flag the calls
+ * above turn into OD_ERR_DEVICE_TIMEOUT).  Takes a few seconds; the context
+ * stays usable. */
+od_status od_selftest_bounded_waits(od_ctx* ctx, int* barrier_timed_out, int* value_wait_timed_out);
 /* Counters (no reference counterpart).  With profiling on, every PCG SpMV
  * launch is bracketed by CUDA events on the context stream. */
 od_status od_ctx_set_profiling(od_ctx* ctx, int enable);

@@ -137,6 +137,7 @@ SIGNATURES = {
     "od_status_string": (C.c_char_p, [C.c_int]),
     "od_last_error": (C.c_char_p, []),
     "od_abi_version": (C.c_int, []),
+    "od_selftest_bounded_waits": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "od_ctx_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),
     "od_ctx_destroy": (C.c_int, [_vp]),
     "od_ctx_synchronize": (C.c_int, [_vp]),
@@ -371,6 +372,14 @@ class Context:
 
     def set_profiling(self, enable: bool):
         _check(load_library().od_ctx_set_profiling(self.h, 1 if enable else 0), "od_ctx_set_profiling")
+
+    def selftest_bounded_waits(self):
+        """od_selftest_bounded_waits: runs the grid-barrier and triangular-sweep
+        waits against conditions that never clear; returns (barrier wait ran
+        out, sweep wait ran out).  Takes a few seconds."""
+        b, v = C.c_int(0), C.c_int(0)
+        _check(load_library().od_selftest_bounded_waits(self.h, C.byref(b), C.byref(v)), "selftest_bounded_waits")
+        return bool(b.value), bool(v.value)
 
     def counters(self):
         c = od_counters()

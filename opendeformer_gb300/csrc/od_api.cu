@@ -166,6 +166,14 @@ od_status od_ctx_destroy(od_ctx* ctx) {
   return OD_OK;
 }
 
+od_status od_selftest_bounded_waits(od_ctx* ctx, int* barrier_timed_out, int* value_wait_timed_out) {
+  OD_CHECK_ARG(ctx && barrier_timed_out && value_wait_timed_out, "od_selftest_bounded_waits: NULL argument");
+  OD_CUDA(cudaSetDevice(ctx->c.device));
+  OD_TRY(selftest_barrier_timeout(&ctx->c, barrier_timed_out));
+  OD_TRY(selftest_value_wait_timeout(&ctx->c, value_wait_timed_out));
+  return OD_OK;
+}
+
 od_status od_ctx_set_profiling(od_ctx* ctx, int enable) {
   OD_CHECK_ARG(ctx, "od_ctx_set_profiling: ctx is NULL");
   OD_CUDA(cudaSetDevice(ctx->c.device));

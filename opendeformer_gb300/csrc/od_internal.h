@@ -445,6 +445,8 @@ od_status launch_loads(Scene* s, const double* body, int n_facets_total, double 
 // material family), then scatter colour by colour (tiles over 90 threads
 // per element of the colour)
 od_status build_gather_lists(Scene* s, int n_pad);
+od_status selftest_barrier_timeout(Ctx* c, int* timed_out);
+od_status selftest_value_wait_timeout(Ctx* c, int* timed_out);
 od_status launch_eval_batch(Ctx* ctx, int n_sc, const SceneDev* sd, const TileDir& zero_k, const TileDir& zero_f,
                             const TileDir& corot, const TileDir& inv, const TileDir& plastic,
                             const std::vector<TileDir>& scatter,

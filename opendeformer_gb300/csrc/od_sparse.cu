@@ -2713,4 +2713,38 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
   return pcg_finish(s, d_b, d_x, shift, st, false, false);
 }
 
+// Self-test of the bounded grid barrier: a cooperative launch of two CTAs
+// in which CTA 0 never arrives, so the other's wait runs out (kSpinLimit
+// polls) and it leaves with the barrier's timeout flag set -- the path every
+// persistent kernel takes when a CTA stops answering.
+__global__ void selftest_barrier_kernel(GridBarrier* gb, int* failed) {
+  if (blockIdx.x == 0) return;
+  if (!grid_barrier(gb) && threadIdx.x == 0) atomicAdd(failed, 1);
+}
+
+od_status selftest_barrier_timeout(Ctx* c, int* timed_out) {
+  *timed_out = 0;
+  int dev_coop = 0;
+  OD_CUDA(cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, c->device));
+  if (!dev_coop) return OD_OK;
+  GridBarrier* gb = nullptr;
+  int* failed = nullptr;
+  OD_CUDA(cudaMalloc(&gb, sizeof(GridBarrier)));
+  OD_CUDA(cudaMalloc(&failed, sizeof(int)));
+  OD_CUDA(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), c->stream));
+  OD_CUDA(cudaMemsetAsync(failed, 0, sizeof(int), c->stream));
+  void* args[] = {(void*)&gb, (void*)&failed};
+  cudaError_t e = cudaLaunchCooperativeKernel((void*)selftest_barrier_kernel, dim3(2), dim3(32), args, 0, c->stream);
+  GridBarrier h{};
+  int hf = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, gb, sizeof(GridBarrier), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&hf, failed, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(gb);
+  cudaFree(failed);
+  if (e != cudaSuccess) return cuda_fail(e, "barrier self-test");
+  *timed_out = h.timeout == 1 && hf == 1;
+  return OD_OK;
+}
+
 }  // namespace od

@@ -529,6 +529,52 @@ od_status ic_factor(Scene* s, const double* host_values, double eps, double rela
   return OD_OK;
 }
 
+namespace {
+// one warp in the apply's cooperative wait on a value nobody writes: row 0
+// of the triple [3, 6) reads column 0, still the pending pattern
+__global__ void __launch_bounds__(32) selftest_value_wait_kernel(const int* idx, const double* val,
+                                                                 const double* vec, int* err) {
+  __shared__ double in[3];
+  const int lane = threadIdx.x & 31;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  if (lane < 3) in[lane] = 0.0;
+  __syncwarp();
+  triple_sums<true>(0, 1, 1, 1, 3, 3, idx, val, vec, in, err, lane, a0, a1, a2);
+}
+}  // namespace
+
+// Self-test of the triangular sweeps' bounded wait: the wait runs out
+// (kSweepSpinLimit polls) and sets the error flag the host reports as
+// OD_ERR_DEVICE_TIMEOUT.
+od_status selftest_value_wait_timeout(Ctx* c, int* timed_out) {
+  *timed_out = 0;
+  int* idx = nullptr;
+  int* err = nullptr;
+  double *val = nullptr, *vec = nullptr;
+  OD_CUDA(cudaMalloc(&idx, sizeof(int)));
+  OD_CUDA(cudaMalloc(&err, sizeof(int)));
+  OD_CUDA(cudaMalloc(&val, sizeof(double)));
+  OD_CUDA(cudaMalloc(&vec, sizeof(double)));
+  const int zero = 0;
+  const double one = 1.0;
+  OD_CUDA(cudaMemcpyAsync(idx, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  OD_CUDA(cudaMemcpyAsync(val, &one, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  OD_CUDA(cudaMemsetAsync(vec, 0xff, sizeof(double), c->stream));
+  OD_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+  selftest_value_wait_kernel<<<1, 32, 0, c->stream>>>(idx, val, vec, err);
+  cudaError_t e = cudaGetLastError();
+  int he = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&he, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(idx);
+  cudaFree(err);
+  cudaFree(val);
+  cudaFree(vec);
+  if (e != cudaSuccess) return cuda_fail(e, "value-wait self-test");
+  *timed_out = he == 1;
+  return OD_OK;
+}
+
 od_status sweep_launch(Scene* s, const SweepView& v, const double* r, double* z, const SolveScalars* sc) {
   Ctx* ctx = s->ctx;
   cudaStream_t strm = ctx->stream;
