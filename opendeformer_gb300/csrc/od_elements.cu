@@ -850,7 +850,18 @@ static od_status gather_list(Scene* s, const int* dest, int kk, int nd, int** pt
   cudaStream_t st = s->ctx->stream;
   const long long n = (long long)kk * ne;
   const int grid = std::max(1, (int)std::min<long long>((n + 255) / 256, 64LL * std::max(1, s->ctx->num_sms)));
-  int *ptr = nullptr, *sums = nullptr, *cur = nullptr, *src = nullptr;
+  // every buffer is freed on an early error return; ptr and src are handed
+  // over on success
+  struct Bufs {
+    int *ptr = nullptr, *sums = nullptr, *cur = nullptr, *src = nullptr;
+    ~Bufs() {
+      for (int* p : {ptr, sums, cur, src}) cudaFree(p);
+    }
+  } b;
+  int*& ptr = b.ptr;
+  int*& sums = b.sums;
+  int*& cur = b.cur;
+  int*& src = b.src;
   const int nscan = nd + 1, nb = (nscan + kScanBlock - 1) / kScanBlock;
   OD_CUDA(cudaMalloc(&ptr, sizeof(int) * (size_t)nscan));
   OD_CUDA(cudaMalloc(&sums, sizeof(int) * (size_t)nb));
@@ -876,11 +887,10 @@ static od_status gather_list(Scene* s, const int* dest, int kk, int nd, int** pt
   if (nd > 0) gl_sort_kernel<<<(nd + 255) / 256, 256, 0, st>>>(nd, ptr, src, s->perm, ne, kk);
   OD_CUDA(cudaGetLastError());
   OD_TRY(sync_stream(s));   // hs is read by the copy above; the temporaries go next
-  cudaFree(sums);
-  cudaFree(cur);
   s->device_bytes += (long long)sizeof(int) * ((long long)nscan + std::max(1, total));
   *ptr_out = ptr;
   *src_out = src;
+  ptr = src = nullptr;
   return OD_OK;
 }
 
