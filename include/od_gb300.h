@@ -197,6 +197,13 @@ od_status od_ctx_synchronize(od_ctx* ctx);
  * above turn into OD_ERR_DEVICE_TIMEOUT).  Takes a few seconds; the context
  * stays usable. */
 od_status od_selftest_bounded_waits(od_ctx* ctx, int* barrier_timed_out, int* value_wait_timed_out);
+/* Multiply-add throughput of the context's device (no reference
+ * counterpart): fixed chains of independent multiply-adds on every SM at full
+ * occupancy, iters per chain, timed with CUDA events on the context stream
+ * (best of three launches after one warm-up).  fp64 = 1 measures FP64, 0
+ * FP32; *fma_per_s receives multiply-adds per second (2 operations each),
+ * *ms the launch time.  The roofline of the FP64 kernels. */
+od_status od_measure_fma_rate(od_ctx* ctx, int fp64, int iters, double* fma_per_s, double* ms);
 /* Counters (no reference counterpart).  With profiling on, every PCG SpMV
  * launch is bracketed by CUDA events on the context stream. */
 od_status od_ctx_set_profiling(od_ctx* ctx, int enable);
@@ -354,21 +361,106 @@ od_status od_batch_create(od_ctx* ctx, int n_scenes, od_scene* const* scenes, od
 od_status od_batch_step(od_batch* batch, int n_steps, od_step_stats* stats);
 od_status od_batch_destroy(od_batch* batch);
 
+/* ---- serving: step requests over a pool of scenes.  No reference
+ * counterpart (the reference steps one Simulator at a time,
+ * core/simulator.h:21-22).  A request is one Newmark step of one scene with
+ * its own time step, body force density and surface traction.  Every
+ * od_server_tick takes the oldest pending request of each scene (oldest
+ * first, at most max_batch), and steps the resident scenes among them
+ * together (batched: one od_batch step with the scenes' mixed-precision
+ * solvers; plain: od_step scene by scene).  Requests arriving meanwhile join
+ * a later tick (continuous batching at step granularity).  Scenes stay on
+ * the device while the byte budget allows; a request for a scene that is not
+ * resident evicts least-recently-used scenes the tick does not step (to a
+ * host checkpoint, as od_scene_save) and admits the scene: with
+ * admission_thread = 1 a host worker thread with its own context builds it
+ * while ticks run and it joins a later tick; otherwise the tick builds it
+ * before stepping.  The server belongs to the thread that created it (its
+ * context's thread); the worker only builds scenes. */
+typedef struct od_server od_server;
+typedef struct od_server_config {
+  long long budget_bytes;   /* device bytes the resident scenes may hold (<= 0: free memory less reserve_bytes) */
+  long long reserve_bytes;  /* kept free when budget_bytes <= 0 */
+  int max_batch;            /* scenes stepped per tick at most (0: no limit) */
+  int batched;              /* 1: one batch step per tick; 0: scene by scene (plain path) */
+  int admission_thread;     /* 1: build admitted scenes on a host worker thread */
+} od_server_config;
+typedef struct od_scene_spec {
+  int n_nodes;
+  const double* X;          /* n_nodes x 3 */
+  int n_tets;
+  const int* tets;          /* n_tets x 4 */
+  int n_facets;
+  const int* facets;        /* n_facets x 3 */
+  int n_cdofs;
+  const int* cdofs;         /* sorted constrained DOFs */
+  int n_load_facets;
+  const int* load_facets;   /* facets that take each request's traction */
+  od_material material;
+  od_integrator_params integrator;  /* Newmark; each request sets dt */
+} od_scene_spec;
+typedef struct od_step_request {
+  int scene;
+  double dt;
+  double body[3];           /* body force density, N/m^3 */
+  double traction[3];       /* Pa, on the scene's load facets */
+  double arrival;           /* seconds on the server clock (od_server_now) */
+} od_step_request;
+typedef struct od_step_result {
+  long long ticket;
+  int scene;
+  int status;               /* od_status of the step */
+  int pcg_iterations;
+  double arrival, done;     /* server clock */
+} od_step_result;
+typedef struct od_server_stats {
+  long long ticks, steps, admissions, restores, evictions, deferred;
+  double s_admit;           /* caller's thread: adoption, eviction and (without the worker) building */
+  double s_loads;           /* request parameters and loads */
+  double s_step;            /* batch / scene steps */
+  double s_worker;          /* worker thread: building scenes (overlaps the ticks) */
+  long long resident, resident_bytes, budget_bytes;
+} od_server_stats;
+od_status od_server_create(od_ctx* ctx, const od_server_config* cfg, od_server** out);
+od_status od_server_destroy(od_server* server);
+/* registers a scene (copies the arrays); all scenes before the first request */
+od_status od_server_add_scene(od_server* server, const od_scene_spec* spec, int* scene_id);
+/* seconds since the server was created */
+od_status od_server_now(od_server* server, double* t);
+od_status od_server_submit(od_server* server, const od_step_request* req, long long* ticket);
+/* one tick; results receives at most capacity completed requests (capacity
+ * also caps the scenes stepped) */
+od_status od_server_tick(od_server* server, int capacity, od_step_result* results, int* n_results);
+od_status od_server_pending(od_server* server, long long* pending);
+/* makes scenes resident (in order, on the caller's thread) while they fit without eviction */
+od_status od_server_warm(od_server* server, int n, const int* scene_ids, int* admitted);
+/* the scene of scene_id, made resident first if it is not (built on the
+ * caller's thread, evicting as the budget requires); the server keeps it:
+ * the handle is valid until the next od_server_tick or od_server_destroy */
+od_status od_server_get_scene(od_server* server, int scene_id, od_scene** out);
+od_status od_server_get_stats(od_server* server, od_server_stats* out);
+
 /* Allocation-free PCG.  No counterpart in the reference.  For callers that
  * cannot allocate device memory -- a host application whose own allocator
- * owns the GPU's memory, or a plugin running inside another program's
- * capture or real-time loop -- this solves A x = b with the none, Jacobi or
- * block-Jacobi preconditioner (FP64) for a full block-CSR matrix the caller
- * already holds on the device: nb block rows, row pointers d_row_ptr[nb+1],
- * block columns d_col[], 9 row-major values per 3x3 block in d_values[];
- * d_b and d_x have 3*nb entries, d_x is the warm start and the result.
+ * owns the GPU's memory, or a plugin whose host forbids allocation once it
+ * is running -- this solves A x = b with the none, Jacobi or block-Jacobi
+ * preconditioner (FP64) for a full block-CSR matrix the caller already holds
+ * on the device: nb block rows, row pointers d_row_ptr[nb+1] (starting at 0,
+ * d_row_ptr[nb] = the length of d_col), block columns d_col[] in 0..nb-1,
+ * 9 row-major values per 3x3 block in d_values[]; d_b and d_x have 3*nb
+ * entries, d_x is the warm start and the result.  A malformed structure is
+ * detected on the device before it is used and returns OD_ERR_INVALID_ARG.
  * Every work vector lives in one fixed device array inside the library
  * (OD_NOALLOC_MAX_BLOCK_ROWS block rows at most, about 5.5 MB, held by every
  * GPU that loads the library until exit); the call allocates nothing.
- * Larger systems are rejected with OD_ERR_INVALID_ARG.  The array is shared:
- * calls that overlap on the GPU race, so callers serialise them.  The first
- * call on a device looks up the array's device address; make it before any
- * stream capture.  stream is a cudaStream_t (NULL: the default stream). */
+ * Larger systems are rejected with OD_ERR_INVALID_ARG.  The call is
+ * synchronous: it waits on the stream to test convergence and returns when
+ * the solve is done (stats->status OD_ERR_NOT_CONVERGED, with OD_OK
+ * returned, when max_iter ran out).  The array is shared: calls that overlap
+ * on the GPU race, so callers serialise them.  The first call on a device
+ * looks up the array's device address and keeps it for the process (a
+ * cudaDeviceReset after it is not supported); make that first call before
+ * any stream capture.  stream is a cudaStream_t (NULL: the default stream). */
 #define OD_NOALLOC_MAX_BLOCK_ROWS 32768
 od_status od_bsr_pcg_noalloc(int nb, const int* d_row_ptr, const int* d_col, const double* d_values,
                              const double* d_b, double* d_x, const od_solver_params* params,

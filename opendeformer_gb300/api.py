@@ -99,6 +99,36 @@ class od_scene_info(C.Structure):
                 ("num_colors", C.c_int), ("device_bytes", C.c_longlong)]
 
 
+class od_server_config(C.Structure):
+    _fields_ = [("budget_bytes", C.c_longlong), ("reserve_bytes", C.c_longlong), ("max_batch", C.c_int),
+                ("batched", C.c_int), ("admission_thread", C.c_int)]
+
+
+class od_scene_spec(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("X", C.POINTER(C.c_double)), ("n_tets", C.c_int),
+                ("tets", C.POINTER(C.c_int)), ("n_facets", C.c_int), ("facets", C.POINTER(C.c_int)),
+                ("n_cdofs", C.c_int), ("cdofs", C.POINTER(C.c_int)), ("n_load_facets", C.c_int),
+                ("load_facets", C.POINTER(C.c_int)), ("material", od_material),
+                ("integrator", od_integrator_params)]
+
+
+class od_step_request(C.Structure):
+    _fields_ = [("scene", C.c_int), ("dt", C.c_double), ("body", C.c_double * 3), ("traction", C.c_double * 3),
+                ("arrival", C.c_double)]
+
+
+class od_step_result(C.Structure):
+    _fields_ = [("ticket", C.c_longlong), ("scene", C.c_int), ("status", C.c_int), ("pcg_iterations", C.c_int),
+                ("arrival", C.c_double), ("done", C.c_double)]
+
+
+class od_server_stats(C.Structure):
+    _fields_ = [("ticks", C.c_longlong), ("steps", C.c_longlong), ("admissions", C.c_longlong),
+                ("restores", C.c_longlong), ("evictions", C.c_longlong), ("deferred", C.c_longlong),
+                ("s_admit", C.c_double), ("s_loads", C.c_double), ("s_step", C.c_double), ("s_worker", C.c_double),
+                ("resident", C.c_longlong), ("resident_bytes", C.c_longlong), ("budget_bytes", C.c_longlong)]
+
+
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _vp = C.c_void_p
@@ -138,6 +168,7 @@ SIGNATURES = {
     "od_last_error": (C.c_char_p, []),
     "od_abi_version": (C.c_int, []),
     "od_selftest_bounded_waits": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "od_measure_fma_rate": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "od_ctx_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),
     "od_ctx_destroy": (C.c_int, [_vp]),
     "od_ctx_synchronize": (C.c_int, [_vp]),
@@ -184,6 +215,16 @@ SIGNATURES = {
     "od_bsr_pcg_noalloc": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, C.POINTER(od_solver_params), _vp,
                                      C.POINTER(od_solve_stats)]),
     "od_mesh_relabel": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip]),
+    "od_server_create": (C.c_int, [_vp, C.POINTER(od_server_config), C.POINTER(_vp)]),
+    "od_server_destroy": (C.c_int, [_vp]),
+    "od_server_add_scene": (C.c_int, [_vp, C.POINTER(od_scene_spec), C.POINTER(C.c_int)]),
+    "od_server_now": (C.c_int, [_vp, C.POINTER(C.c_double)]),
+    "od_server_submit": (C.c_int, [_vp, C.POINTER(od_step_request), C.POINTER(C.c_longlong)]),
+    "od_server_tick": (C.c_int, [_vp, C.c_int, C.POINTER(od_step_result), C.POINTER(C.c_int)]),
+    "od_server_pending": (C.c_int, [_vp, C.POINTER(C.c_longlong)]),
+    "od_server_warm": (C.c_int, [_vp, C.c_int, _ip, C.POINTER(C.c_int)]),
+    "od_server_get_scene": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
+    "od_server_get_stats": (C.c_int, [_vp, C.POINTER(od_server_stats)]),
     "od_scene_save": (C.c_int, [_vp, _vp, C.POINTER(C.c_size_t)]),
     "od_scene_load": (C.c_int, [_vp, _vp, C.c_size_t]),
 }
@@ -380,6 +421,14 @@ class Context:
         b, v = C.c_int(0), C.c_int(0)
         _check(load_library().od_selftest_bounded_waits(self.h, C.byref(b), C.byref(v)), "selftest_bounded_waits")
         return bool(b.value), bool(v.value)
+
+    def measure_fma_rate(self, fp64: bool = True, iters: int = 1 << 14):
+        """od_measure_fma_rate: (multiply-adds per second, launch ms) of
+        independent FP64 (or FP32) multiply-add chains on every SM."""
+        r, ms = C.c_double(0.0), C.c_double(0.0)
+        _check(load_library().od_measure_fma_rate(self.h, int(bool(fp64)), int(iters), C.byref(r), C.byref(ms)),
+               "od_measure_fma_rate")
+        return r.value, ms.value
 
     def counters(self):
         c = od_counters()

@@ -109,6 +109,11 @@ struct Pcg {
   int* ic_gord_f = nullptr;     // row triples by forward / backward level
   int* ic_gord_b = nullptr;
   int ic_gdepth = 0;            // levels of the two sweeps
+  // node order of the factor: block rows by colour (greedy colouring of
+  // the block graph), or the natural order
+  int ic_colours = 0;           // colours (0: natural order)
+  int* ic_pdof = nullptr;       // factor DOF -> the system's DOF (colour order only)
+  double* ic_zp = nullptr;      // the backward sweep's values in factor order
   // persistent (cooperative) solve
   void* gbar = nullptr;         // grid barrier state
   int* timeout_host = nullptr;  // pinned
@@ -371,6 +376,21 @@ od_status cuda_fail(cudaError_t e, const char* what);
     if (_e != cudaSuccess) return ::od::cuda_fail(_e, #call); \
   } while (0)
 
+// temporary device buffers freed on every return path
+struct DeviceTemps {
+  std::vector<void*> ptrs;
+  template <class T>
+  cudaError_t alloc(T** p, size_t bytes) {
+    *p = nullptr;
+    cudaError_t e = cudaMalloc((void**)p, bytes);
+    if (e == cudaSuccess) ptrs.push_back((void*)*p);
+    return e;
+  }
+  ~DeviceTemps() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+};
+
 // argument check of an ABI entry point
 #define OD_CHECK_ARG(cond, msg)              \
   do {                                       \
@@ -511,6 +531,11 @@ struct SweepView {
   const double *fval = nullptr, *bval = nullptr, *diag = nullptr;
   double* y = nullptr;
   int* err = nullptr;
+  // factor in a permuted DOF order (IC(0) by colours): perm[new DOF] = the
+  // caller's DOF; the sweeps keep z in the permuted order in zperm (the
+  // ready flags) and also write every value to the caller's z at perm[]
+  const int* perm = nullptr;
+  double* zperm = nullptr;
 };
 od_status sweep_grid(Scene* s, int n, int* grid);
 void sweep_group_levels(int n, const std::vector<int>& frp, const std::vector<int>& fci, const std::vector<int>& bcp,

@@ -1,12 +1,14 @@
 // Allocation-free PCG entry point (od_bsr_pcg_noalloc, include/od_gb300.h).
 //
 // For callers that must not allocate device memory themselves or through
-// this library -- a host application whose allocator owns every byte of the
-// GPU, a plugin running inside someone else's capture or real-time loop --
-// this entry point solves A x = b for a full block-CSR matrix the caller
-// already holds on the device, with every work vector kept in one file-scope
-// device array (g_pcg_scratch) of fixed size.  It calls no cudaMalloc,
-// cudaFree or allocating library routine.
+// this library -- a host application whose own allocator owns every byte of
+// the GPU, or a plugin whose host forbids allocation after start-up -- this
+// entry point solves A x = b for a full block-CSR matrix the caller already
+// holds on the device, with every work vector kept in one file-scope device
+// array (g_pcg_scratch) of fixed size.  It calls no cudaMalloc, cudaFree or
+// allocating library routine.  The call is synchronous: it waits on the
+// caller's stream every 16 iterations to read the convergence test, and
+// returns when the solve has finished.
 //
 // The array is shared by every call on a device and keeps the contents of
 // the last call; the scalars and counters that must start at zero are reset
@@ -18,7 +20,14 @@
 // name is a host-side stand-in, not a device address).  The device address
 // is looked up with cudaGetSymbolAddress once per device, on the first call
 // made with that device current; that first call should therefore come
-// before any stream capture.
+// before any stream capture.  The address is kept for the life of the
+// process: a cudaDeviceReset of that device after the first call is not
+// supported.
+//
+// The matrix comes from the caller, so the first kernel checks it before
+// any other reads it: a row pointer that does not start at 0 or decreases,
+// or a block column outside 0..nb-1, stops the solve with
+// OD_ERR_INVALID_ARG (d_row_ptr[nb] must be the length of d_col).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -109,11 +118,33 @@ __device__ __forceinline__ double precond_row(int pk, int i, const double* __res
   return r[i];
 }
 
+// Structure check, before any kernel reads x through the columns: row
+// pointers start at 0 and never decrease, every block column lies in
+// 0..nb-1.  A violation stops the solve with OD_ERR_INVALID_ARG (the rows
+// are not walked further).
+__global__ void validate_kernel(int nb, const int* __restrict__ rp, const int* __restrict__ col,
+                                double* __restrict__ scratch) {
+  Scal* sc = reinterpret_cast<Scal*>(scratch + kOffScal);
+  const int br = blockIdx.x * blockDim.x + threadIdx.x;
+  if (br >= nb) return;
+  const int k0 = rp[br], k1 = rp[br + 1];
+  bool bad = (br == 0 && k0 != 0) || k1 < k0;
+  for (int k = k0; !bad && k < k1; k++) bad = col[k] < 0 || col[k] >= nb;
+  if (bad) {
+    sc->status = OD_ERR_INVALID_ARG;
+    sc->done = 1;
+  }
+}
+
+__device__ __forceinline__ bool stopped(const double* scratch) {
+  return *(volatile const int*)&reinterpret_cast<const Scal*>(scratch + kOffScal)->done != 0;
+}
+
 // Jacobi (1/d, or 1 when d <= 0) or inverse 3x3 diagonal blocks
 __global__ void setup_kernel(int nb, int pk, const int* __restrict__ rp, const int* __restrict__ col,
                              const double* __restrict__ A, double* __restrict__ scratch) {
   int br = blockIdx.x * blockDim.x + threadIdx.x;
-  if (br >= nb) return;
+  if (br >= nb || stopped(scratch)) return;
   double* pinv = scratch + kOffPinv;
   const double* a = nullptr;
   for (int k = rp[br]; k < rp[br + 1]; k++)
@@ -144,6 +175,7 @@ __global__ void setup_kernel(int nb, int pk, const int* __restrict__ rp, const i
 __global__ void init_r_kernel(int n, const int* __restrict__ rp, const int* __restrict__ col,
                               const double* __restrict__ A, const double* __restrict__ b,
                               const double* __restrict__ x, double* __restrict__ scratch) {
+  if (stopped(scratch)) return;  // CTA-uniform
   double* r = scratch + kOffR;
   double* part = scratch + kOffPart;
   double bb = 0.0, rr = 0.0;
@@ -159,6 +191,7 @@ __global__ void init_r_kernel(int n, const int* __restrict__ rp, const int* __re
 
 // z = M^-1 r; p = z; partial r.z
 __global__ void init_z_kernel(int n, int pk, double* __restrict__ scratch) {
+  if (stopped(scratch)) return;
   const double* r = scratch + kOffR;
   double* z = scratch + kOffZ;
   double* p = scratch + kOffP;
@@ -176,6 +209,7 @@ __global__ void init_z_kernel(int n, int pk, double* __restrict__ scratch) {
 }
 
 __global__ void init_finish_kernel(int g, double tol, int max_iter, double* __restrict__ scratch) {
+  if (stopped(scratch)) return;  // the structure check failed: its status stands
   const double* part = scratch + kOffPart;
   Scal* sc = reinterpret_cast<Scal*>(scratch + kOffScal);
   const double bb = sum_parts(part, g), rr = sum_parts(part + kMaxGrid, g), rz = sum_parts(part + 2 * kMaxGrid, g);
@@ -268,19 +302,30 @@ __global__ void direction_kernel(int n, int g, int slot, double* __restrict__ sc
   }
 }
 
-// true residual ||b - A x||^2 and ||b||^2 (single CTA)
+// true residual: partials of ||b - A x||^2 and ||b||^2 per CTA (skipped when
+// the structure check failed)
 __global__ void residual_kernel(int n, const int* __restrict__ rp, const int* __restrict__ col,
                                 const double* __restrict__ A, const double* __restrict__ b,
                                 const double* __restrict__ x, double* __restrict__ scratch) {
-  Scal* sc = reinterpret_cast<Scal*>(scratch + kOffScal);
+  const Scal* sc = reinterpret_cast<const Scal*>(scratch + kOffScal);
+  if (sc->status == OD_ERR_INVALID_ARG) return;
+  double* part = scratch + kOffPart;
   double d2 = 0.0, bb = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double d = b[i] - row_dot(i, rp, col, A, x);
     d2 = fma(d, d, d2);
     bb = fma(b[i], b[i], bb);
   }
   double t0 = block_sum_na(d2), t1 = block_sum_na(bb);
-  if (threadIdx.x == 0) { sc->tr_num = t0; sc->tr_den = t1; }
+  if (threadIdx.x == 0) { part[blockIdx.x] = t0; part[kMaxGrid + blockIdx.x] = t1; }
+}
+
+__global__ void residual_finish_kernel(int g, double* __restrict__ scratch) {
+  Scal* sc = reinterpret_cast<Scal*>(scratch + kOffScal);
+  if (sc->status == OD_ERR_INVALID_ARG) return;
+  const double* part = scratch + kOffPart;
+  const double d2 = sum_parts(part, g), bb = sum_parts(part + kMaxGrid, g);
+  if (threadIdx.x == 0) { sc->tr_num = d2; sc->tr_den = bb; }
 }
 
 // device address of g_pcg_scratch, looked up once per device
@@ -339,6 +384,7 @@ extern "C" od_status od_bsr_pcg_noalloc(int nb, const int* d_row_ptr, const int*
   const int pk = params->precond;
   // scalars start from zero on every call (the array keeps the last call's contents)
   OD_CUDA(cudaMemsetAsync(scratch + kOffScal, 0, 16 * sizeof(double), strm));
+  validate_kernel<<<(nb + kT - 1) / kT, kT, 0, strm>>>(nb, d_row_ptr, d_col, scratch);
   if (pk != OD_PRECOND_NONE) setup_kernel<<<(nb + kT - 1) / kT, kT, 0, strm>>>(nb, pk, d_row_ptr, d_col, d_values, scratch);
   init_r_kernel<<<g, kT, 0, strm>>>(n, d_row_ptr, d_col, d_values, d_b, d_x, scratch);
   init_z_kernel<<<g, kT, 0, strm>>>(n, pk, scratch);
@@ -360,11 +406,21 @@ extern "C" od_status od_bsr_pcg_noalloc(int nb, const int* d_row_ptr, const int*
     OD_CUDA(cudaStreamSynchronize(strm));
     if (h.done) break;
   }
-  residual_kernel<<<1, 1024, 0, strm>>>(n, d_row_ptr, d_col, d_values, d_b, d_x, scratch);
+  residual_kernel<<<g, kT, 0, strm>>>(n, d_row_ptr, d_col, d_values, d_b, d_x, scratch);
+  residual_finish_kernel<<<1, kT, 0, strm>>>(g, scratch);
   OD_CUDA(cudaGetLastError());
   OD_CUDA(cudaMemcpyAsync(&h, dsc, sizeof(Scal), cudaMemcpyDeviceToHost, strm));
   OD_CUDA(cudaStreamSynchronize(strm));
   od_status status = (od_status)h.status;
+  if (status == OD_ERR_INVALID_ARG) {
+    set_error("od_bsr_pcg_noalloc: row pointers must start at 0 and not decrease, and every block column "
+              "must lie in 0..nb-1");
+    if (stats) {
+      *stats = od_solve_stats{};
+      stats->status = status;
+    }
+    return status;
+  }
   if (status == OD_OK && h.iter >= h.max_iter && h.rr > h.eps) status = OD_ERR_NOT_CONVERGED;
   if (stats) {
     stats->iterations = h.iter;

@@ -1761,6 +1761,34 @@ od_status launch_spmv_full(Scene* s, const double* x, double* y) {
 
 // IC(0) structure: scalar CSR of the padded lower pattern of the full BSR
 // (columns sorted, diagonal last), level sets, and the transposed index.
+// Greedy colouring of the block graph (block rows coupled by a stored
+// block), blocks visited in index order, each taking the lowest colour no
+// coloured neighbour has; order[] lists the blocks by colour, then index.
+// Returns the number of colours.  The oracle's IC(0) orders the same way.
+static int ic0_colour_order(int nb, const std::vector<int>& rp, const std::vector<int>& col, std::vector<int>& order) {
+  std::vector<int> colour(nb, -1), mark;
+  int nc = 0;
+  for (int b = 0; b < nb; b++) {
+    for (int k = rp[b]; k < rp[b + 1]; k++) {
+      const int c = colour[col[k]];
+      if (c >= 0) {
+        if ((int)mark.size() <= c) mark.resize(c + 1, -1);
+        mark[c] = b;
+      }
+    }
+    int c = 0;
+    while (c < (int)mark.size() && mark[c] == b) c++;
+    colour[b] = c;
+    nc = std::max(nc, c + 1);
+  }
+  std::vector<int> start(nc + 1, 0);
+  for (int b = 0; b < nb; b++) start[colour[b] + 1]++;
+  for (int c = 0; c < nc; c++) start[c + 1] += start[c];
+  order.assign(nb, 0);
+  for (int b = 0; b < nb; b++) order[start[colour[b]]++] = b;
+  return nc;
+}
+
 static od_status ic0_build(Scene* s) {
   Pcg& P = s->pcg;
   if (P.ic_rp) return OD_OK;
@@ -1770,17 +1798,35 @@ static od_status ic0_build(Scene* s) {
   OD_CUDA(cudaMemcpy(rp.data(), s->bsr.row_ptr, sizeof(int) * (nb + 1), cudaMemcpyDeviceToHost));
   OD_CUDA(cudaMemcpy(col.data(), s->bsr.col, sizeof(int) * s->bsr.nnzb, cudaMemcpyDeviceToHost));
   const int n = 3 * nb;
+  // Node order of the factor.  By default block rows are ordered by colour
+  // (ic0_colour_order): no two blocks of a colour are coupled, so a block
+  // row depends only on blocks of earlier colours and the two sweeps have
+  // as many dependency levels as there are colours.  OD_GB300_IC0_ORDER=natural
+  // keeps the system's order (one level per step of the mesh's longest
+  // dependency chain).
+  std::vector<int> bperm(nb), binv(nb);
+  const char* oenv = std::getenv("OD_GB300_IC0_ORDER");
+  const bool natural = oenv && std::strcmp(oenv, "natural") == 0;
+  P.ic_colours = natural ? 0 : ic0_colour_order(nb, rp, col, bperm);
+  if (natural)
+    for (int b = 0; b < nb; b++) bperm[b] = b;
+  for (int b = 0; b < nb; b++) binv[bperm[b]] = b;
   std::vector<int> srp(n + 1, 0), sci, ssrc;
   sci.reserve((size_t)s->bsr.nnzb * 5);
   ssrc.reserve((size_t)s->bsr.nnzb * 5);
-  for (int br = 0; br < nb; br++)
+  std::vector<std::pair<int, int>> blk;   // (factor block column, BSR block) of one block row
+  for (int R = 0; R < nb; R++) {
+    const int br = bperm[R];
+    blk.clear();
+    for (int k = rp[br]; k < rp[br + 1]; k++)
+      if (binv[col[k]] <= R) blk.push_back({binv[col[k]], k});
+    std::sort(blk.begin(), blk.end());
     for (int r = 0; r < 3; r++) {
-      const int i = 3 * br + r;
-      for (int k = rp[br]; k < rp[br + 1]; k++) {
-        const int bc = col[k];
-        if (bc > br) break;
+      const int i = 3 * R + r;
+      for (const auto& e : blk) {
+        const int C = e.first, k = e.second;
         for (int c = 0; c < 3; c++) {
-          const int j = 3 * bc + c;
+          const int j = 3 * C + c;
           if (j > i) break;
           sci.push_back(j);
           ssrc.push_back(9 * k + 3 * r + c);
@@ -1788,6 +1834,7 @@ static od_status ic0_build(Scene* s) {
       }
       srp[i + 1] = (int)sci.size();
     }
+  }
   const int nnz = (int)sci.size();
   // transposed index: for row i the entries (row j > i, column i)
   std::vector<int> trp(n + 1, 0), tci(nnz), tpos(nnz);
@@ -1900,6 +1947,14 @@ static od_status ic0_build(Scene* s) {
     }
   }
   if ((st = up(&P.ic_gord_b, gob)) != OD_OK) return st;
+  if (!natural) {
+    std::vector<int> pdof(n);
+    for (int R = 0; R < nb; R++)
+      for (int r = 0; r < 3; r++) pdof[3 * R + r] = 3 * bperm[R] + r;
+    if ((st = up(&P.ic_pdof, pdof)) != OD_OK) return st;
+    OD_CUDA(cudaMalloc(&P.ic_zp, sizeof(double) * std::max(1, n)));
+    s->device_bytes += sizeof(double) * (long long)n;
+  }
   OD_CUDA(cudaMalloc(&P.ic_val, sizeof(double) * std::max(1, nnz)));
   const size_t nl = std::max<size_t>(1, fci.size());
   OD_CUDA(cudaMalloc(&P.ic_fval, sizeof(double) * nl));
@@ -1996,6 +2051,8 @@ static od_status ic0_apply(Scene* s, const double* r, double* z, const SolveScal
   v.diag = P.ic_dval;
   v.y = P.ic_y;
   v.err = P.ic_err;
+  v.perm = P.ic_pdof;
+  v.zperm = P.ic_zp;
   return sweep_launch(s, v, r, z, sc);
 }
 
@@ -2049,11 +2106,12 @@ od_status pcg_alloc(Scene* s) {
 
 void pcg_free(Scene* s) {
   Pcg& P = s->pcg;
-  for (double* v : {P.x, P.r, P.z, P.p, P.q, P.b, P.partial, P.pinv, P.ic_val, P.ic_fval, P.ic_bval, P.ic_dval, P.ic_y})
+  for (double* v : {P.x, P.r, P.z, P.p, P.q, P.b, P.partial, P.pinv, P.ic_val, P.ic_fval, P.ic_bval, P.ic_dval, P.ic_y,
+                    P.ic_zp})
     cudaFree(v);
   if (P.ic_err_host) cudaFreeHost(P.ic_err_host);
   for (int* v : {P.ic_rp, P.ic_ci, P.ic_src, P.lvl_rows_f, P.icT_rp, P.icT_ci, P.icT_pos, P.ic_bad,
-                 P.ic_frp, P.ic_fci, P.ic_err, P.ic_gord_f, P.ic_gord_b, P.ic_pp, P.ic_pa, P.ic_pb})
+                 P.ic_frp, P.ic_fci, P.ic_err, P.ic_gord_f, P.ic_gord_b, P.ic_pp, P.ic_pa, P.ic_pb, P.ic_pdof})
     cudaFree(v);
   cudaFree(P.sc);
   cudaFree(P.gbar);
@@ -2727,10 +2785,11 @@ od_status selftest_barrier_timeout(Ctx* c, int* timed_out) {
   int dev_coop = 0;
   OD_CUDA(cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, c->device));
   if (!dev_coop) return OD_OK;
+  DeviceTemps tmp;
   GridBarrier* gb = nullptr;
   int* failed = nullptr;
-  OD_CUDA(cudaMalloc(&gb, sizeof(GridBarrier)));
-  OD_CUDA(cudaMalloc(&failed, sizeof(int)));
+  OD_CUDA(tmp.alloc(&gb, sizeof(GridBarrier)));
+  OD_CUDA(tmp.alloc(&failed, sizeof(int)));
   OD_CUDA(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), c->stream));
   OD_CUDA(cudaMemsetAsync(failed, 0, sizeof(int), c->stream));
   void* args[] = {(void*)&gb, (void*)&failed};
@@ -2740,8 +2799,6 @@ od_status selftest_barrier_timeout(Ctx* c, int* timed_out) {
   if (e == cudaSuccess) e = cudaMemcpyAsync(&h, gb, sizeof(GridBarrier), cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&hf, failed, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  cudaFree(gb);
-  cudaFree(failed);
   if (e != cudaSuccess) return cuda_fail(e, "barrier self-test");
   *timed_out = h.timeout == 1 && hf == 1;
   return OD_OK;

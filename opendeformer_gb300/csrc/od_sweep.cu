@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(kSweepThreads, 2) sweep_apply_kernel(
     const double* __restrict__ fval, const int* __restrict__ bcp, const int* __restrict__ bri,
     const double* __restrict__ bval, const int* __restrict__ ord_f, const int* __restrict__ ord_b,
     const double* __restrict__ dinv, const double* __restrict__ r, double* y, double* z, int* __restrict__ err,
-    const SolveScalars* sc) {
+    const SolveScalars* sc, const int* __restrict__ perm, double* __restrict__ zout) {
   __shared__ double inner_s[kSweepThreads / 32][3];
   if (sc && *(volatile const int*)&sc->done) return;
   const int lane = threadIdx.x & 31;
@@ -192,7 +192,10 @@ __global__ void __launch_bounds__(kSweepThreads, 2) sweep_apply_kernel(
   const int w = blockIdx.x * wpb + (threadIdx.x >> 5);
   double* in = inner_s[threadIdx.x >> 5];
   // padding rows carry the identity
-  for (int i = n + blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += gridDim.x * blockDim.x) z[i] = r[i];
+  for (int i = n + blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += gridDim.x * blockDim.x) {
+    if (perm) zout[perm[i]] = r[perm[i]];
+    else z[i] = r[i];
+  }
 
   // forward: y_j = r_j - sum_c L_jc y_c (times 1 / L_jj for IC)
   for (int t = w; t < ng; t += W) {
@@ -202,7 +205,7 @@ __global__ void __launch_bounds__(kSweepThreads, 2) sweep_apply_kernel(
     double rv[3] = {0.0, 0.0, 0.0}, dv[3] = {0.0, 0.0, 0.0};
     if (lane == 0)
       for (int k = 0; k < m; k++) {
-        rv[k] = r[i0 + k];
+        rv[k] = r[perm ? perm[i0 + k] : i0 + k];
         dv[k] = IC ? dinv[i0 + k] : 1.0;
       }
     __syncwarp();
@@ -268,7 +271,13 @@ __global__ void __launch_bounds__(kSweepThreads, 2) sweep_apply_kernel(
         st_relaxed_f64(z + i0 + 1, z1);
       }
       const double e0 = a0 + z1 * in[0] + z2 * in[1];
-      st_relaxed_f64(z + i0, IC ? (yv[0] - e0) * dv[0] : yv[0] * dv[0] - e0);
+      const double z0 = IC ? (yv[0] - e0) * dv[0] : yv[0] * dv[0] - e0;
+      st_relaxed_f64(z + i0, z0);
+      if (perm) {  // the caller's order
+        zout[perm[i0]] = z0;
+        if (m > 1) zout[perm[i0 + 1]] = z1;
+        if (m > 2) zout[perm[i0 + 2]] = z2;
+      }
     }
   }
 }
@@ -548,13 +557,14 @@ __global__ void __launch_bounds__(32) selftest_value_wait_kernel(const int* idx,
 // OD_ERR_DEVICE_TIMEOUT.
 od_status selftest_value_wait_timeout(Ctx* c, int* timed_out) {
   *timed_out = 0;
+  DeviceTemps tmp;
   int* idx = nullptr;
   int* err = nullptr;
   double *val = nullptr, *vec = nullptr;
-  OD_CUDA(cudaMalloc(&idx, sizeof(int)));
-  OD_CUDA(cudaMalloc(&err, sizeof(int)));
-  OD_CUDA(cudaMalloc(&val, sizeof(double)));
-  OD_CUDA(cudaMalloc(&vec, sizeof(double)));
+  OD_CUDA(tmp.alloc(&idx, sizeof(int)));
+  OD_CUDA(tmp.alloc(&err, sizeof(int)));
+  OD_CUDA(tmp.alloc(&val, sizeof(double)));
+  OD_CUDA(tmp.alloc(&vec, sizeof(double)));
   const int zero = 0;
   const double one = 1.0;
   OD_CUDA(cudaMemcpyAsync(idx, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
@@ -566,10 +576,6 @@ od_status selftest_value_wait_timeout(Ctx* c, int* timed_out) {
   int he = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&he, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  cudaFree(idx);
-  cudaFree(err);
-  cudaFree(val);
-  cudaFree(vec);
   if (e != cudaSuccess) return cuda_fail(e, "value-wait self-test");
   *timed_out = he == 1;
   return OD_OK;
@@ -592,13 +598,17 @@ od_status sweep_launch(Scene* s, const SweepView& v, const double* r, double* z,
   const double* dg = v.diag;
   double* y = v.y;
   int* err = v.err;
-  void* args[] = {(void*)&n,    (void*)&n_pad, (void*)&ng,  (void*)&frp, (void*)&fci, (void*)&fval,
+  const int* perm = v.perm;
+  double* zflag = perm ? v.zperm : z;   // z in the factor's order: the values other rows wait on
+  double* zout = z;
+  void* args[] = {(void*)&n,    (void*)&n_pad, (void*)&ng,   (void*)&frp, (void*)&fci, (void*)&fval,
                   (void*)&bcp,  (void*)&bri,   (void*)&bval, (void*)&of,  (void*)&ob,  (void*)&dg,
-                  (void*)&r,    (void*)&y,     (void*)&z,   (void*)&err, (void*)&sc};
+                  (void*)&r,    (void*)&y,     (void*)&zflag, (void*)&err, (void*)&sc, (void*)&perm,
+                  (void*)&zout};
   // every value starts "not yet written" (all-ones bytes)
   if (n > 0) {
     OD_CUDA(cudaMemsetAsync(y, 0xff, sizeof(double) * (size_t)n, strm));
-    OD_CUDA(cudaMemsetAsync(z, 0xff, sizeof(double) * (size_t)n, strm));
+    OD_CUDA(cudaMemsetAsync(zflag, 0xff, sizeof(double) * (size_t)n, strm));
   }
   OD_KL(s);
   void* fn = v.ic ? (void*)sweep_apply_kernel<1> : (void*)sweep_apply_kernel<0>;

@@ -5,7 +5,8 @@ mechanical portability fixes (the original project targets MSVC 2015).  This
 script
 
 1. copies the hot-path translation units and headers from the reference tree
-   (``$OD_REFERENCE``, default ``/root/reference/OpenDeformer``) into
+   (the argument, else ``$OD_REFERENCE``, else ``reference/OpenDeformer`` in
+   the directory that holds this repository) into
    ``oracle/_ref/src/`` -- a git-ignored build directory, never the product;
 2. applies the portability fixes to that copy (never to the reference tree);
 3. compiles it together with ``oracle/ref_harness.cpp`` (a C API written for
@@ -202,7 +203,8 @@ def compile_lib(jobs: int = 8) -> str:
 
 def build(ref_root: str | None = None) -> str | None:
     """Build ``oracle/_ref/libodref.so``; returns its path or None if impossible."""
-    ref_root = ref_root or os.environ.get("OD_REFERENCE", "/root/reference/OpenDeformer")
+    ref_root = ref_root or os.environ.get("OD_REFERENCE") or os.path.join(
+        os.path.dirname(os.path.dirname(HERE)), "reference", "OpenDeformer")
     if os.path.isdir(ref_root):
         copy_and_patch(ref_root)
     elif not os.path.isdir(SRC_OUT):

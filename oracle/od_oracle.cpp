@@ -554,6 +554,7 @@ struct Scene {
   std::vector<double> plastic;          // plastic strain, 9 per tet (state, changes at every evaluation)
   double ldlt_sainv = 0.1, ldlt_drop = 0.01;  // InLDLTPreconditioner(sainvEpsilon, ldltEpsilon)
   double ic_eps = 1e-3, ic_relax = 0.0;       // InCholeskyPreconditioner(epsilon, relaxedScale)
+  int ic0_natural = 0;                  // IC(0) in the DOF order (1) or by block colours (0)
   // pattern (reference layout)
   int nbc = 0, nrem = 0;
   std::vector<int> pcol, rows, oris, emap;
@@ -1170,16 +1171,23 @@ struct TouchVec {
 // tail uses point Jacobi.  Inverse by the adjugate formula.
 //
 // IC(0) (no reference counterpart): scalar incomplete Cholesky with zero fill
-// on the stored lower pattern (every stored value position, in compacted-DOF
-// order), L L^T ~ A.  A non-positive pivot is replaced by the original
-// diagonal entry.  Apply: forward L y = r, backward L^T z = y.
+// on the blocked pattern -- every scalar position between two blocks of
+// three compacted DOFs (the last block may hold fewer) that a stored entry
+// couples, zero where the reference layout stores nothing -- L L^T ~ P A P^T.
+// P orders the blocks by a greedy colouring of the block graph (blocks in
+// index order, each taking the lowest colour none of its coloured
+// neighbours has; then by colour, by index), or keeps the DOF order.  A
+// pivot not above 1e-12 times its diagonal restarts the factorisation with a
+// diagonal shift.  Apply: z = P^T (L L^T)^-1 P r.
 struct Precond {
   int kind = 0;
   std::vector<double> inv;        // Jacobi: n; block-Jacobi: 9 per block + tail
-  // IC(0) in scalar CSR (rows sorted; diagonal last in each row)
-  std::vector<int> rp, ci;
+  // IC(0) in scalar CSR (rows sorted; diagonal last in each row), in the
+  // factor's DOF order: newdof[DOF] = its factor row
+  std::vector<int> rp, ci, newdof;
   std::vector<double> lv;
   double shift = 0.0;
+  int natural = 0;
   // incomplete LDL^T (kind 4) in the reference's storage
   double sainv_eps = 0.1, ldlt_eps = 0.01;
   std::vector<double> lval, dinv;
@@ -1466,7 +1474,7 @@ void ldlt_apply(int n, const Precond& P, const double* r, double* z) {
 //   L_ii = sqrt(A_ii (1 + alpha) - sum_{k<i} L_ik^2).
 // Returns false on breakdown (a pivot not above 1e-12 times its diagonal).
 bool ic0_factor(Precond& P, const double* val, const std::vector<int>& src, int n, double alpha) {
-  for (size_t k = 0; k < src.size(); k++) P.lv[k] = val[src[k]];
+  for (size_t k = 0; k < src.size(); k++) P.lv[k] = src[k] >= 0 ? val[src[k]] : 0.0;
   for (int i = 0; i < n; i++) {
     int bi = P.rp[i], ei = P.rp[i + 1];
     for (int q = bi; q < ei; q++) {
@@ -1524,6 +1532,72 @@ void scalar_lower_csr(const Scene& s, std::vector<int>& rp, std::vector<int>& ci
   }
 }
 
+// The IC(0) pattern in the factor's order (see Precond): rows rp/ci, the
+// reference-layout position of every entry (src, -1 where none is stored)
+// and newdof.
+void ic0_pattern(const Scene& s, bool natural, std::vector<int>& rp, std::vector<int>& ci, std::vector<int>& src,
+                 std::vector<int>& newdof) {
+  const int n = s.dofs, nb = (n + 2) / 3;
+  std::vector<int> lrp, lci, lsrc;
+  scalar_lower_csr(s, lrp, lci, lsrc);
+  std::vector<std::vector<int>> adj(nb);
+  for (int i = 0; i < n; i++)
+    for (int q = lrp[i]; q < lrp[i + 1]; q++) {
+      const int bi = i / 3, bj = lci[q] / 3;
+      if (bi != bj) { adj[bi].push_back(bj); adj[bj].push_back(bi); }
+    }
+  for (auto& a : adj) {
+    std::sort(a.begin(), a.end());
+    a.erase(std::unique(a.begin(), a.end()), a.end());
+  }
+  std::vector<int> order(nb);
+  for (int b = 0; b < nb; b++) order[b] = b;
+  if (!natural) {
+    std::vector<int> colour(nb, -1);
+    for (int b = 0; b < nb; b++) {
+      std::vector<char> used;
+      for (int c : adj[b])
+        if (colour[c] >= 0) {
+          if ((int)used.size() <= colour[c]) used.resize(colour[c] + 1, 0);
+          used[colour[c]] = 1;
+        }
+      int c = 0;
+      while (c < (int)used.size() && used[c]) c++;
+      colour[b] = c;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return colour[a] < colour[b]; });
+  }
+  std::vector<int> newblock(nb);
+  for (int R = 0; R < nb; R++) newblock[order[R]] = R;
+  newdof.assign(n, 0);
+  int next = 0;
+  for (int R = 0; R < nb; R++)
+    for (int d = 3 * order[R]; d < std::min(n, 3 * order[R] + 3); d++) newdof[d] = next++;
+  auto lookup = [&](int i, int j) {   // reference-layout position of (i, j), j <= i, or -1
+    const int* b = &lci[lrp[i]];
+    const int* e = &lci[lrp[i + 1]];
+    const int* f = std::lower_bound(b, e, j);
+    return (f != e && *f == j) ? lsrc[lrp[i] + (int)(f - b)] : -1;
+  };
+  std::vector<std::vector<std::pair<int, int>>> rowsv(n);
+  for (int b = 0; b < nb; b++) {
+    std::vector<int> nbrs = adj[b];
+    nbrs.push_back(b);
+    for (int i = 3 * b; i < std::min(n, 3 * b + 3); i++)
+      for (int b2 : nbrs)
+        for (int j = 3 * b2; j < std::min(n, 3 * b2 + 3); j++)
+          if (newdof[j] <= newdof[i]) rowsv[newdof[i]].push_back({newdof[j], lookup(std::max(i, j), std::min(i, j))});
+  }
+  rp.assign(n + 1, 0);
+  ci.clear();
+  src.clear();
+  for (int r = 0; r < n; r++) {
+    std::sort(rowsv[r].begin(), rowsv[r].end());
+    for (auto& e : rowsv[r]) { ci.push_back(e.first); src.push_back(e.second); }
+    rp[r + 1] = (int)ci.size();
+  }
+}
+
 void precond_setup(const Scene& s, const double* val, Precond& P) {
   const int n = s.dofs;
   if (P.kind == 1) {
@@ -1543,7 +1617,7 @@ void precond_setup(const Scene& s, const double* val, Precond& P) {
     }
   } else if (P.kind == 3) {
     std::vector<int> src;
-    scalar_lower_csr(s, P.rp, P.ci, src);
+    ic0_pattern(s, P.natural != 0, P.rp, P.ci, src, P.newdof);
     P.lv.resize(P.ci.size());
     // shifted IC(0): factor A + alpha diag(A) with alpha = 0, 1e-3, 2e-3, ...
     // until every pivot exceeds 1e-12 times its shifted diagonal
@@ -1576,18 +1650,21 @@ void precond_apply(const Scene& s, const Precond& P, const double* r, double* z)
   } else if (P.kind == 5) {
     ric_apply(n, P, r, z);
   } else {
+    std::vector<double> y(n);   // in the factor's order
+    for (int i = 0; i < n; i++) y[P.newdof[i]] = r[i];
     for (int i = 0; i < n; i++) {
-      double sum = r[i];
+      double sum = y[i];
       int e = P.rp[i + 1] - 1;
-      for (int q = P.rp[i]; q < e; q++) sum -= P.lv[q] * z[P.ci[q]];
-      z[i] = sum / P.lv[e];
+      for (int q = P.rp[i]; q < e; q++) sum -= P.lv[q] * y[P.ci[q]];
+      y[i] = sum / P.lv[e];
     }
     for (int i = n - 1; i >= 0; i--) {
       int e = P.rp[i + 1] - 1;
-      z[i] /= P.lv[e];
-      double zi = z[i];
-      for (int q = P.rp[i]; q < e; q++) z[P.ci[q]] -= P.lv[q] * zi;
+      y[i] /= P.lv[e];
+      double yi = y[i];
+      for (int q = P.rp[i]; q < e; q++) y[P.ci[q]] -= P.lv[q] * yi;
     }
+    for (int i = 0; i < n; i++) z[i] = y[P.newdof[i]];
   }
 }
 
@@ -1604,6 +1681,7 @@ int pcg(const Scene& s, const double* val, const double* b, double* x, double to
   P.ldlt_eps = s.ldlt_drop;
   P.ic_eps = s.ic_eps;
   P.ic_relax = s.ic_relax;
+  P.natural = s.ic0_natural;
   precond_setup(s, val, P);
   precond_apply(s, P, r.data(), d.data());
   auto dotp = [n](const double* a, const double* c) { double acc = 0; for (int i = 0; i < n; i++) acc += a[i] * c[i]; return acc; };
@@ -1875,6 +1953,9 @@ void odo_element_values(odo_scene* o, double* K78, double* f12) {
 void odo_assemble(odo_scene* o, double* values, double* fint) { assemble(o->s, values, fint); }
 void odo_mass(odo_scene* o, double* values) { memcpy(values, o->s.mass.data(), sizeof(double) * o->s.nvals); }
 void odo_spmdv(odo_scene* o, const double* values, const double* x, double* y) { spmdv(o->s, values, x, y); }
+// IC(0) node order: 1 keeps the DOF order, 0 (default) orders blocks by colour
+void odo_set_ic0_natural(odo_scene* o, int natural) { o->s.ic0_natural = natural; }
+
 int odo_pcg(odo_scene* o, const double* values, const double* b, double* x, double tol, int maxit, int pkind) {
   return pcg(o->s, values, b, x, tol, maxit, pkind);
 }

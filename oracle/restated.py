@@ -42,6 +42,7 @@ def lib():
         L.odo_assemble.argtypes = [C.c_void_p, _dp, _dp]
         L.odo_mass.argtypes = [C.c_void_p, _dp]
         L.odo_spmdv.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.odo_set_ic0_natural.argtypes = [C.c_void_p, C.c_int]
         L.odo_pcg.restype = C.c_int
         L.odo_pcg.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int]
         L.odo_loads.argtypes = [C.c_void_p, _dp, C.c_int, _dp, _ip, _ip, _dp]
@@ -191,6 +192,10 @@ class OracleScene:
         dinv = np.zeros(max(self.dofs, 1))
         lib().odo_ldlt_get(self.h, _d(lv), _i(lr), _i(pc), _d(dinv))
         return lv[:nnz], lr[:nnz], pc[: self.dofs], dinv[: self.dofs]
+
+    def set_ic0_natural(self, natural=True):
+        """IC(0) (precond "ic0") in the DOF order instead of by block colours."""
+        lib().odo_set_ic0_natural(self.h, int(bool(natural)))
 
     def set_ic(self, eps=1e-3, relax=0.0):
         """(epsilon, relaxedScale) of the threshold incomplete Cholesky (precond "ic")."""

@@ -76,14 +76,22 @@ def test_preconditioners_converge(golden, precond):
     assert rel_err(x, e["cg_x"]) <= 1e-7
 
 
-@pytest.mark.parametrize("precond", ["block_jacobi", "ic0"])
-def test_preconditioner_iterations_match_oracle(golden, precond):
+@pytest.mark.parametrize("precond", ["block_jacobi", "ic0", "ic0_natural"])
+def test_preconditioner_iterations_match_oracle(golden, precond, monkeypatch):
+    """Partial constraints (DOF blocks straddling nodes, a short last block).
+    IC(0) factors its blocks in colour order by default and in the DOF order
+    with OD_GB300_IC0_ORDER=natural; the oracle orders the same way."""
     from oracle import restated as O
+    natural = precond == "ic0_natural"
+    if natural:
+        monkeypatch.setenv("OD_GB300_IC0_ORDER", "natural")
+        precond = "ic0"
     p = golden("pattern_partial")
     e = golden("elements_stvk_partial")
     s, _, _ = gpu_scene(golden, "stvk", "partial")
     A = e["values"] * (1.0 / 3600.0) + e["mass"]
     o = O.OracleScene(p["X"], p["tets"], p["facets"], p["cdofs"], "stvk", *e["material"])
+    o.set_ic0_natural(natural)
     xo, ito = o.pcg(A, e["cg_b"], tol=1e-10, maxit=2000, precond=precond)
     x, st = s.pcg(A, e["cg_b"], solver=api.CGSolver(1e-10, 2000, api.Preconditioner(precond)))
     assert abs(st.iterations - ito) <= 2

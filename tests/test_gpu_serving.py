@@ -1,6 +1,7 @@
 """Serving (opendeformer_gb300.serving): step requests for many scenes,
-continuous batching, admission by a device-memory budget, LRU eviction
-through checkpoints.  Each scene's result through the server, in the mix and
+continuous batching, admission by a device-memory budget (scenes built on
+the library's admission thread while ticks run, or inside the tick), LRU
+eviction through checkpoints.  Each scene's result through the server, in the mix and
 across evictions, equals the same request sequence applied to the scene
 alone (both mixed-precision solves reach 1e-10, so the tolerance on the
 displacements is 1e-7 relative)."""
@@ -62,33 +63,30 @@ def alone(sid, reqs):
     return s.displacements()
 
 
-def run_server(reqs, budget):
-    sv = serving.Server(ctx(), budget_bytes=budget, clock=lambda: 1.0)
+def run_server(reqs, budget, admission_thread=True):
+    import time
+    sv = serving.Server(ctx(), budget_bytes=budget, admission_thread=admission_thread)
     for inst in POOL:
         sv.add_scene(spec(inst))
     for r in reqs:
         sv.submit(r)
     done = []
     peak = 0
-    for _ in range(100):
-        if not sv.pending():
-            break
+    t_end = time.time() + 120
+    while sv.pending() and time.time() < t_end:
         done += sv.tick()
-        peak = max(peak, sv.used)
+        peak = max(peak, sv.stats["resident_bytes"])
     assert not sv.pending()
-    out = {}
-    for sid, slot in enumerate(sv.slots):
-        if slot.scene is None:   # evicted at the end: bring it back to read it
-            sv._admit(sid, set())
-        out[sid] = slot.scene.displacements()
-    stats = dict(sv.stats)
+    out = {sid: sv.displacements(sid) for sid in range(len(POOL))}
+    stats = sv.stats
     sv.close()
     return done, out, peak, stats
 
 
-def test_server_results_equal_each_scene_alone():
+@pytest.mark.parametrize("admission_thread", [True, False])
+def test_server_results_equal_each_scene_alone(admission_thread):
     reqs = requests(7, 3)
-    done, out, _, stats = run_server(reqs, budget=1 << 40)
+    done, out, _, stats = run_server(reqs, budget=1 << 40, admission_thread=admission_thread)
     assert len(done) == len(reqs) and all(r.status == 0 for r in done)
     assert stats["evictions"] == 0
     for sid in range(len(POOL)):
@@ -98,11 +96,12 @@ def test_server_results_equal_each_scene_alone():
         assert rel_err(out[sid], ua) <= 1e-7, sid
 
 
-def test_server_evicts_within_budget_and_restores_state():
+@pytest.mark.parametrize("admission_thread", [True, False])
+def test_server_evicts_within_budget_and_restores_state(admission_thread):
     reqs = requests(11, 3)
     # about half of the pool fits
     budget = int(0.5 * 2600 * sum(6 * np.prod(i["dims"]) for i in POOL))
-    done, out, peak, stats = run_server(reqs, budget=budget)
+    done, out, peak, stats = run_server(reqs, budget=budget, admission_thread=admission_thread)
     assert stats["evictions"] > 0 and stats["restores"] > 0
     assert peak <= budget
     assert all(r.status == 0 for r in done) and len(done) == len(reqs)
