@@ -393,16 +393,21 @@ def precision_tier(args, api, ctx):
     mat = api.InvertibleNeoHookeanMaterial(1000.0, NH_E, NH_NU, 0.1)
     out, res, first = {}, {}, {}
     warm, steps = 2, args.tier_steps
-    for prec in ("fp64", "mixed"):
+    # mixed: the inner SpMV streams the lower triangle (transposed products by
+    # reductions); mixed_full: both triangles (OD_GB300_MIXED_SPMV=full)
+    for prec in ("fp64", "mixed", "mixed_full"):
+        if prec == "mixed_full":
+            os.environ["OD_GB300_MIXED_SPMV"] = "full"
         s = api.Scene(ctx, g.X, g.tets, g.facets, cd, mat)
         s.set_displacements(u0)
         s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, 0.01, 0.001, 1 / 120,
                                                  api.CGSolver(1e-10, 20000, api.BlockJacobiPreconditioner(),
-                                                              precision=prec), 1))
+                                                              precision=prec.split("_")[0]), 1))
         for w in range(warm):
             s.step(1)
             if w == 0:
                 first[prec] = s.displacements()   # after the first step from rest (oracle check)
+        os.environ.pop("OD_GB300_MIXED_SPMV", None)
         ms, it = [], 0
         for _ in range(steps):
             st = s.step(1)
@@ -425,6 +430,10 @@ def precision_tier(args, api, ctx):
     peak, peak_kind = peaks()
     nbytes, sms, nit, wms = res["mixed"].pop("mix")
     res["fp64"].pop("mix")
+    fb, fs, fi, fw = res["mixed_full"].pop("mix")
+    res["mixed_full"]["spmv_phase"] = {"bytes": fb, "ms": fw, "phases": fi,
+                                       "achieved_gbs": fb / (fw * 1e-3) / 1e9 if fw else None,
+                                       "us_per_phase_with_sum": 1000.0 * fs / max(1, fi)}
     spmv_gbs = nbytes / (wms * 1e-3) / 1e9 if wms else None
     phase_gbs = nbytes / (sms * 1e-3) / 1e9 if sms else None
     oracle = None
@@ -453,8 +462,10 @@ def precision_tier(args, api, ctx):
     return {"workload": "block2m6_nh_prescribed_newmark" if nz == 64 else f"block128x64x{nz}_nh_prescribed_newmark",
             "n_tets": g.n_tets, "dofs": 3 * g.n_nodes - len(cd),
             "newton_iters": 1, "tol": 1e-10, "precond": "block_jacobi", "warmup": warm, "steps": steps,
-            "fp64": res["fp64"], "mixed": res["mixed"],
+            "fp64": res["fp64"], "mixed": res["mixed"], "mixed_full": res["mixed_full"],
             "speedup_mixed_vs_fp64": res["mixed"]["steps_per_s"] / res["fp64"]["steps_per_s"],
+            "speedup_mixed_full_vs_fp64": res["mixed_full"]["steps_per_s"] / res["fp64"]["steps_per_s"],
+            "rel_err_mixed_full_vs_fp64": _rel(out["mixed_full"], out["fp64"]),
             "rel_err_mixed_vs_fp64": _rel(out["mixed"], out["fp64"]),
             "oracle": oracle,
             "spmv_roofline": {"kernel": "pcg32_ring_kernel SpMV phase (sliced FP32 matrix streamed by "
@@ -465,8 +476,10 @@ def precision_tier(args, api, ctx):
                               "algorithmic_bytes": nbytes, "phase_ms": wms, "phases": nit,
                               "with_grid_sum": {"achieved": phase_gbs, "frac": phase_gbs / peak if phase_gbs else None,
                                                 "phase_ms": sms},
-                              "bytes_rule": "stored 3x3 blocks x 40 B (9 FP32 values + int32 column) + 24 B per "
-                                            "block row (own p read, q written)"}}
+                              "us_per_phase_with_sum": 1000.0 * sms / max(1, nit),
+                              "bytes_rule": "stored 3x3 blocks x 40 B (9 FP32 values + int32 column; the lower "
+                                            "triangle with the diagonal) + 24 B per block row (own p read, q "
+                                            "written); the transposed products go to L2 as reductions"}}
 
 
 def sweep_tier(args, api, ctx):
@@ -746,6 +759,26 @@ def batched_tier(args, api, ctx):
         lat.append(st[0].device_ms)
     ub = [s.displacements() for s in scenes]
     err = max(_rel(a, c) for a, c in zip(ub, u64))
+    # autotuner (tile shapes of the inner solve), then steps with the tuned
+    # shapes between two runs of steps with the defaults
+    tune = b.autotune(repeats=1)
+    tuned = {"choice": {k: tune[k] for k in ("piece_steps", "slice_cost")},
+             "solve_ms_default": tune.get("default_ms"), "solve_ms_tuned": tune.get("best_ms"),
+             "candidates": tune.get("candidates"), "key": tune["key"]}
+    def timed(n):
+        out = []
+        for _ in range(n):
+            st = b.step(1)
+            if any(x.status != 0 for x in st):
+                raise RuntimeError("batched tier: batch step failed")
+            out.append(st[0].device_ms)
+        return statistics.mean(out)
+    t_tuned = timed(steps)
+    b.set_tuning(20, 8.0)
+    t_default = timed(steps)
+    tuned.update({"ms_per_step_tuned": t_tuned, "ms_per_step_default_after": t_default,
+                  "ms_per_step_default_before": statistics.mean(lat),
+                  "gain": 0.5 * (t_default + statistics.mean(lat)) / t_tuned})
     n_tets = sum(s.n_tets for s in scenes)
     b.close()
     for s in scenes:
@@ -764,7 +797,7 @@ def batched_tier(args, api, ctx):
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
         cpu = batched_cpu_baseline(len(all_insts), n_tets)
-    return {"workload": "batch512_uneven_newmark", "cpu_baseline": cpu, "ranks": world,
+    return {"workload": "batch512_uneven_newmark", "cpu_baseline": cpu, "ranks": world, "autotune": tuned,
             "sharding": "scenes by tet count (greedy, no exchange)" if world > 1 else None,
             "speedup_batched_vs_cpu": (1000.0 / bms) / cpu["value"] if cpu and cpu.get("value") else None, "instances": len(scenes), "n_tets_total": n_tets,
             "newton_iters": 1, "tol": 1e-8, "precond": "block_jacobi", "warmup": warm, "steps": steps,
@@ -875,6 +908,7 @@ def serving_tier(args, api, ctx):
         bad = [r for r in done if r.status != 0]
         return {"offered_per_s": rate, "window_s": window, "offered": len(arr), "completed": len(done),
                 "failed": len(bad), "backlog_at_end": backlog, "steps_per_s": len(done) / wall,
+                "ok_steps_per_s": (len(done) - len(bad)) / wall,
                 "p50_ms": lat[len(lat) // 2] if lat else None,
                 "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None,
                 "mean_batch": stats["steps"] / max(1, stats["ticks"]), "warmed_scenes": warmed, "warm_s": warm_s,
@@ -887,21 +921,31 @@ def serving_tier(args, api, ctx):
     window = args.serving_seconds
     sat_b = run(True, args.serving_rate, window, 9)
     sat_p = run(False, args.serving_rate, window, 9)
-    sustain = max(10.0, 0.5 * sat_b["steps_per_s"])
-    lat_b = run(True, sustain, max(5.0, 0.6 * window), 10)
+    # rate sweep below the batched capacity: the highest rate whose queue
+    # stays flat (backlog at the end within 2% of the offered requests) is
+    # the sustainable one, and its p50 / p99 are service latencies
+    sweep = []
+    for frac in (0.15, 0.3, 0.6):
+        rate = max(5.0, frac * sat_b["ok_steps_per_s"])
+        r = run(True, rate, max(5.0, 0.5 * window), 10)
+        sweep.append({k: r[k] for k in ("offered_per_s", "ok_steps_per_s", "p50_ms", "p99_ms", "backlog_at_end",
+                                        "offered", "mean_batch", "admissions", "evictions")})
+    flat = [x for x in sweep if x["backlog_at_end"] <= 0.02 * max(1, x["offered"])]
+    sustain = max(flat, key=lambda x: x["offered_per_s"]) if flat else min(sweep, key=lambda x: x["offered_per_s"])
     cpu = serving_cpu_baseline(len(pool)) if not args.no_cpu_baseline else None
     return {"workload": "serving_pool_poisson", "pool_scenes": len(pool), "pool_tets": n_tets,
             "scaled": f"pool {len(pool)} of the configuration's 4096 scenes and {window:.0f} s windows of its 60 s: "
                       f"the full pool needs {4096 * mesh_s / max(1, len(pool)):.0f} s of host mesh generation and "
                       f"400 GB of resident data, beyond one bench run's few minutes",
             "budget_bytes": budget, "tol": 1e-6, "mesh_s": mesh_s, "cpu_baseline": cpu,
-            "saturation_steps_per_s": sat_b["steps_per_s"], "plain_saturation_steps_per_s": sat_p["steps_per_s"],
-            "throughput_ratio_batched_vs_plain": sat_b["steps_per_s"] / max(1e-9, sat_p["steps_per_s"]),
-            "sustainable": {"offered_per_s": sustain, "p50_ms": lat_b["p50_ms"], "p99_ms": lat_b["p99_ms"],
-                            "steps_per_s": lat_b["steps_per_s"], "backlog_at_end": lat_b["backlog_at_end"]},
-            "note": "latency = completion - arrival on the server clock; at the saturating rate the queue grows "
+            "saturation_steps_per_s": sat_b["ok_steps_per_s"], "plain_saturation_steps_per_s": sat_p["ok_steps_per_s"],
+            "throughput_ratio_batched_vs_plain": sat_b["ok_steps_per_s"] / max(1e-9, sat_p["ok_steps_per_s"]),
+            "sustainable": {**sustain, "queue_flat": bool(flat)},
+            "rate_sweep": sweep,
+            "note": "throughput counts successful steps (a diverged scene's requests fail and are not counted); "
+                    "latency = completion - arrival on the server clock; at the saturating rate the queue grows "
                     "(p50/p99 there are queueing, not service); requests past the window are not waited for",
-            "batched_mixed": sat_b, "plain_fp64": sat_p, "batched_at_sustainable_rate": lat_b}
+            "batched_mixed": sat_b, "plain_fp64": sat_p}
 
 
 def tiers_summary(line):
@@ -911,7 +955,7 @@ def tiers_summary(line):
             if not isinstance(d, dict) or k not in d:
                 return None
             d = d[k]
-        return round(d, 4) if isinstance(d, float) else d
+        return float(f"{d:.4g}") if isinstance(d, float) else d
     out = {"headline_steps_per_s": g(line, "value"), "e2e_steps_per_s": g(line, "e2e", "value"),
            "cpu_ref_steps_per_s": g(line, "cpu_baseline", "value"),
            "headline_rel_err_vs_oracle": g(line, "parity", "headline_rel_err"),
@@ -919,6 +963,7 @@ def tiers_summary(line):
     if "precision_tier" in line:
         t = line["precision_tier"]
         out["precision"] = {"speedup_mixed_vs_fp64": g(t, "speedup_mixed_vs_fp64"),
+                            "speedup_full_layout": g(t, "speedup_mixed_full_vs_fp64"),
                             "mixed_steps_per_s": g(t, "mixed", "steps_per_s"),
                             "fp64_steps_per_s": g(t, "fp64", "steps_per_s"),
                             "inner_iters": g(t, "mixed", "pcg_iterations_per_step"),
@@ -930,6 +975,7 @@ def tiers_summary(line):
     if "batched_tier" in line:
         t = line["batched_tier"]
         out["batched"] = {"speedup_vs_fp64_alone": g(t, "speedup_batched_mixed_vs_fp64_alone"),
+                          "autotune_gain": g(t, "autotune", "gain"),
                           "batch_steps_per_s": g(t, "batched_mixed", "batch_steps_per_s"),
                           "rel_err_vs_fp64": g(t, "max_rel_err_vs_fp64"),
                           "cpu_batch_steps_per_s": g(t, "cpu_baseline", "value")}
@@ -938,6 +984,7 @@ def tiers_summary(line):
         out["serving"] = {"ratio_vs_plain": g(t, "throughput_ratio_batched_vs_plain"),
                           "saturation_steps_per_s": g(t, "saturation_steps_per_s"),
                           "sustainable_rate": g(t, "sustainable", "offered_per_s"),
+                          "queue_flat": g(t, "sustainable", "queue_flat"),
                           "p50_ms": g(t, "sustainable", "p50_ms"), "p99_ms": g(t, "sustainable", "p99_ms"),
                           "cpu_steps_per_s": g(t, "cpu_baseline", "value")}
     if "ic0_tier" in line:

@@ -360,6 +360,27 @@ od_status od_batch_create(od_ctx* ctx, int n_scenes, od_scene* const* scenes, od
  * device_ms is the time of the whole call */
 od_status od_batch_step(od_batch* batch, int n_steps, od_step_stats* stats);
 od_status od_batch_destroy(od_batch* batch);
+/* Tile shapes of a batch's inner FP32 solve (no reference counterpart):
+ * the ring kernel's piece size (matrix steps per bulk copy into shared
+ * memory: 12, 16 or 20; default 20) and the per-slice fixed cost, in steps,
+ * that weights the partition of the slices over the CTAs (default 8). */
+typedef struct od_mixed_tuning {
+  int piece_steps;
+  double slice_cost;
+} od_mixed_tuning;
+typedef struct od_tune_report {
+  int candidates;
+  od_mixed_tuning best;
+  double default_ms, best_ms;    /* solve time of the default and of the chosen shapes */
+  int default_iters, best_iters; /* their inner iterations (summed over scenes) */
+} od_tune_report;
+od_status od_batch_get_tuning(od_batch* batch, od_mixed_tuning* out);
+od_status od_batch_set_tuning(od_batch* batch, const od_mixed_tuning* tuning);
+/* Autotuner: after at least one od_batch_step, solves the batch's last
+ * Newton system again with every candidate shape (3 piece sizes x slice
+ * costs 2, 4, 8, 16), each timed with CUDA events (best of repeats), and
+ * keeps the fastest.  Scene state is not changed. */
+od_status od_batch_autotune(od_batch* batch, int repeats, od_tune_report* report);
 
 /* ---- serving: step requests over a pool of scenes.  No reference
  * counterpart (the reference steps one Simulator at a time,
@@ -373,9 +394,9 @@ od_status od_batch_destroy(od_batch* batch);
  * the device while the byte budget allows; a request for a scene that is not
  * resident evicts least-recently-used scenes the tick does not step (to a
  * host checkpoint, as od_scene_save) and admits the scene: with
- * admission_thread = 1 a host worker thread with its own context builds it
- * while ticks run and it joins a later tick; otherwise the tick builds it
- * before stepping.  The server belongs to the thread that created it (its
+ * admission_thread = k > 0, k host worker threads with contexts of their own
+ * build admitted scenes in parallel while ticks run, and each joins a later
+ * tick; with 0 the tick builds it before stepping.  The server belongs to the thread that created it (its
  * context's thread); the worker only builds scenes. */
 typedef struct od_server od_server;
 typedef struct od_server_config {
@@ -383,7 +404,7 @@ typedef struct od_server_config {
   long long reserve_bytes;  /* kept free when budget_bytes <= 0 */
   int max_batch;            /* scenes stepped per tick at most (0: no limit) */
   int batched;              /* 1: one batch step per tick; 0: scene by scene (plain path) */
-  int admission_thread;     /* 1: build admitted scenes on a host worker thread */
+  int admission_thread;     /* host worker threads that build admitted scenes (0: the tick builds them) */
 } od_server_config;
 typedef struct od_scene_spec {
   int n_nodes;

@@ -99,6 +99,15 @@ class od_scene_info(C.Structure):
                 ("num_colors", C.c_int), ("device_bytes", C.c_longlong)]
 
 
+class od_mixed_tuning(C.Structure):
+    _fields_ = [("piece_steps", C.c_int), ("slice_cost", C.c_double)]
+
+
+class od_tune_report(C.Structure):
+    _fields_ = [("candidates", C.c_int), ("best", od_mixed_tuning), ("default_ms", C.c_double),
+                ("best_ms", C.c_double), ("default_iters", C.c_int), ("best_iters", C.c_int)]
+
+
 class od_server_config(C.Structure):
     _fields_ = [("budget_bytes", C.c_longlong), ("reserve_bytes", C.c_longlong), ("max_batch", C.c_int),
                 ("batched", C.c_int), ("admission_thread", C.c_int)]
@@ -212,6 +221,9 @@ SIGNATURES = {
     "od_batch_create": (C.c_int, [_vp, C.c_int, C.POINTER(_vp), C.POINTER(_vp)]),
     "od_batch_step": (C.c_int, [_vp, C.c_int, C.POINTER(od_step_stats)]),
     "od_batch_destroy": (C.c_int, [_vp]),
+    "od_batch_get_tuning": (C.c_int, [_vp, C.POINTER(od_mixed_tuning)]),
+    "od_batch_set_tuning": (C.c_int, [_vp, C.POINTER(od_mixed_tuning)]),
+    "od_batch_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(od_tune_report)]),
     "od_bsr_pcg_noalloc": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, C.POINTER(od_solver_params), _vp,
                                      C.POINTER(od_solve_stats)]),
     "od_mesh_relabel": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip]),
@@ -730,6 +742,63 @@ class Batch:
         st = (od_step_stats * len(self.scenes))()
         _check(load_library().od_batch_step(self.h, n, st), "od_batch_step")
         return list(st)
+
+    def tuning(self) -> dict:
+        t = od_mixed_tuning()
+        _check(load_library().od_batch_get_tuning(self.h, C.byref(t)), "od_batch_get_tuning")
+        return {"piece_steps": t.piece_steps, "slice_cost": t.slice_cost}
+
+    def set_tuning(self, piece_steps: int, slice_cost: float):
+        t = od_mixed_tuning(int(piece_steps), float(slice_cost))
+        _check(load_library().od_batch_set_tuning(self.h, C.byref(t)), "od_batch_set_tuning")
+
+    def tuning_key(self) -> str:
+        """Device and mesh class of the batch: SM count, scene count and the
+        scenes' total block rows and stored blocks, each rounded to two
+        significant digits."""
+        import math
+
+        def r2(v):
+            if v <= 0:
+                return 0
+            e = int(math.floor(math.log10(v))) - 1
+            return int(round(v / 10 ** e) * 10 ** e)
+        try:
+            import torch
+            sms = torch.cuda.get_device_properties(self.ctx.device).multi_processor_count
+        except Exception:
+            sms = f"dev{self.ctx.device}"
+        nb = sum((sc.info.dofs + 2) // 3 for sc in self.scenes)
+        nnzb = sum(sc.info.num_full_blocks for sc in self.scenes)
+        return f"sm{sms}-scenes{r2(len(self.scenes))}-rows{r2(nb)}-blocks{r2(nnzb)}"
+
+    def autotune(self, repeats: int = 1, cache: str | None = None) -> dict:
+        """od_batch_autotune: picks the inner solve's tile shapes (ring-kernel
+        piece size, partition slice cost) by timing the batch's last Newton
+        system with every candidate; the batch must have been stepped once.
+        With a cache file (JSON; default $OD_GB300_TUNE_CACHE when set) a
+        choice made before for the same device and mesh class is reused."""
+        import json
+        cache = cache or os.environ.get("OD_GB300_TUNE_CACHE")
+        key = self.tuning_key()
+        table = {}
+        if cache and os.path.exists(cache):
+            with open(cache) as f:
+                table = json.load(f)
+        if key in table:
+            self.set_tuning(table[key]["piece_steps"], table[key]["slice_cost"])
+            return {"key": key, "cached": True, **table[key]}
+        rep = od_tune_report()
+        _check(load_library().od_batch_autotune(self.h, int(repeats), C.byref(rep)), "od_batch_autotune")
+        out = {"piece_steps": rep.best.piece_steps, "slice_cost": rep.best.slice_cost,
+               "candidates": rep.candidates, "default_ms": rep.default_ms, "best_ms": rep.best_ms,
+               "default_iters": rep.default_iters, "best_iters": rep.best_iters}
+        if cache:
+            table[key] = out
+            os.makedirs(os.path.dirname(os.path.abspath(cache)), exist_ok=True)
+            with open(cache, "w") as f:
+                json.dump(table, f, indent=1, sort_keys=True)
+        return {"key": key, "cached": False, **out}
 
     def close(self):
         if getattr(self, "h", None) and not _shutting_down:

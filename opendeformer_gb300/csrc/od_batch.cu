@@ -71,6 +71,7 @@ struct Batch {
   int newton = 1, precond = OD_PRECOND_BLOCK_JACOBI;
   std::vector<od_solver_params> prm;
   cudaEvent_t ev[2] = {nullptr, nullptr};
+  bool stepped = false;  // a Newton system of the last step is on the device
 };
 
 static void batch_free(Batch* b) {
@@ -242,6 +243,64 @@ static od_status batch_step(Batch* B, std::vector<od_step_stats>& acc) {
     acc[i].steps++;
     B->sc[i]->time += B->sc[i]->ip.dt;
   }
+  B->stepped = true;
+  return OD_OK;
+}
+
+// Autotuner of the inner solve's tile shapes: the last Newton system of the
+// batch (matrices and right-hand sides still on the device) is solved again
+// with every candidate -- ring-kernel piece size x partition slice cost --
+// from a zero correction, each timed with CUDA events on the context stream
+// (best of `repeats`); the scenes' state is not touched (the corrections
+// are scratch between steps) and the scenes' iteration history, which
+// weights the partition, is put back after every solve.  The fastest
+// candidate stays set.
+static od_status batch_autotune(Batch* B, int repeats, od_tune_report* rep) {
+  Ctx* ctx = B->ctx;
+  MixedSys* m = B->mix;
+  std::vector<double> hist;
+  for (Scene* s : B->sc) hist.push_back(s->mix_iters_last);
+  auto restore = [&] {
+    for (size_t i = 0; i < B->sc.size(); i++) B->sc[i]->mix_iters_last = hist[i];
+  };
+  const int pieces[3] = {12, 16, 20};
+  const double costs[4] = {2.0, 4.0, 8.0, 16.0};
+  od_tune_report r{};
+  r.best_ms = 1e300;
+  std::vector<od_solve_stats> ss;
+  for (int pi = 0; pi < 3; pi++)
+    for (int ci = 0; ci < 4; ci++) {
+      OD_TRY(mixed_retune(m, pieces[pi], costs[ci]));
+      float best = 1e30f;
+      int iters = 0;
+      for (int rr = 0; rr < std::max(1, repeats); rr++) {
+        OD_TRY(nm_op(B, NM_ZERO_DV));
+        OD_CUDA(cudaEventRecord(B->ev[0], ctx->stream));
+        OD_TRY(mixed_solve(ctx, m, B->precond, B->prm, ss));
+        OD_CUDA(cudaEventRecord(B->ev[1], ctx->stream));
+        OD_CUDA(cudaEventSynchronize(B->ev[1]));
+        restore();
+        float ms = 0.f;
+        OD_CUDA(cudaEventElapsedTime(&ms, B->ev[0], B->ev[1]));
+        best = std::min(best, ms);
+        iters = 0;
+        for (const od_solve_stats& x : ss) iters += x.iterations;
+      }
+      r.candidates++;
+      if (pieces[pi] == 20 && costs[ci] == 8.0) {
+        r.default_ms = best;
+        r.default_iters = iters;
+      }
+      if (best < r.best_ms) {
+        r.best_ms = best;
+        r.best_iters = iters;
+        r.best.piece_steps = pieces[pi];
+        r.best.slice_cost = costs[ci];
+      }
+    }
+  OD_TRY(nm_op(B, NM_ZERO_DV));
+  OD_TRY(mixed_retune(m, r.best.piece_steps, r.best.slice_cost));
+  if (rep) *rep = r;
   return OD_OK;
 }
 
@@ -306,6 +365,27 @@ extern "C" od_status od_batch_destroy(od_batch* batch) {
   batch_free(batch->b);
   delete batch;
   return OD_OK;
+}
+
+extern "C" od_status od_batch_get_tuning(od_batch* batch, od_mixed_tuning* out) {
+  OD_BATCH_ARG(batch && out, "od_batch_get_tuning: NULL argument");
+  out->piece_steps = batch->b->mix->piece_steps;
+  out->slice_cost = batch->b->mix->slice_cost;
+  return OD_OK;
+}
+
+extern "C" od_status od_batch_set_tuning(od_batch* batch, const od_mixed_tuning* t) {
+  OD_BATCH_ARG(batch && t, "od_batch_set_tuning: NULL argument");
+  OD_CUDA(cudaSetDevice(batch->b->ctx->device));
+  return mixed_retune(batch->b->mix, t->piece_steps, t->slice_cost);
+}
+
+extern "C" od_status od_batch_autotune(od_batch* batch, int repeats, od_tune_report* report) {
+  OD_BATCH_ARG(batch, "od_batch_autotune: batch is NULL");
+  OD_BATCH_ARG(batch->b->stepped, "od_batch_autotune: step the batch once first (it tunes on the last system)");
+  OD_BATCH_ARG(repeats >= 1 && repeats <= 16, "od_batch_autotune: repeats must be in 1..16");
+  OD_CUDA(cudaSetDevice(batch->b->ctx->device));
+  return batch_autotune(batch->b, repeats, report);
 }
 
 extern "C" od_status od_batch_step(od_batch* batch, int n_steps, od_step_stats* stats) {

@@ -56,6 +56,34 @@ __device__ __forceinline__ void st_relaxed_f64(double* p, double x) {
   asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(__double_as_longlong(x)) : "memory");
 }
 
+// Value-as-flag access of the triangular sweeps per value type: a value is
+// "not yet written" while it holds the all-ones pattern (a NaN no arithmetic
+// result has), read and written with relaxed gpu-scope accesses.
+template <class T>
+struct SweepFlag;
+template <>
+struct SweepFlag<double> {
+  using U = unsigned long long;
+  static constexpr U kPend = kPending;
+  __device__ static __forceinline__ U ld(const double* p) { return ld_relaxed_u64(p); }
+  __device__ static __forceinline__ void st(double* p, double x) { st_relaxed_f64(p, x); }
+  __device__ static __forceinline__ double val(U v) { return __longlong_as_double((long long)v); }
+};
+template <>
+struct SweepFlag<float> {
+  using U = unsigned;
+  static constexpr U kPend = 0xffffffffu;
+  __device__ static __forceinline__ U ld(const float* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+  }
+  __device__ static __forceinline__ void st(float* p, float x) {
+    asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(__float_as_uint(x)) : "memory");
+  }
+  __device__ static __forceinline__ float val(U v) { return __uint_as_float(v); }
+};
+
 __device__ __forceinline__ bool grid_barrier(GridBarrier* gb) {
   __shared__ int ok_s;
   __syncthreads();

@@ -324,13 +324,27 @@ void build_ic_levels(const std::vector<int>& rp, const std::vector<int>& ci, int
 // to an even step count (so every slice starts on a 16-byte boundary of the
 // value and column arrays, as bulk copies require).  Padding slots point at
 // the slot's own slice row and take the value zero.
-void build_sliced(const std::vector<int>& row_ptr, const std::vector<int>& col, int nb, HostSliced& out) {
+// lower = true keeps the blocks of the lower triangle only (block column <=
+// block row, the reference's symmetric storage): src of a diagonal block is
+// -(block + 2), its values go in halved (the SpMV applies every stored block
+// and its transpose), padding -1.
+void build_sliced(const std::vector<int>& row_ptr, const std::vector<int>& col, int nb, HostSliced& out,
+                  bool lower) {
   const int S = kSliceRows;
   const int ns = (nb + S - 1) / S;
   out.ns = ns;
+  out.lower = lower;
   std::vector<int> order(nb);
   for (int i = 0; i < nb; i++) order[i] = i;
-  auto len = [&](int r) { return row_ptr[r + 1] - row_ptr[r]; };
+  // a row's stored blocks: all, or those up to the diagonal (columns ascend)
+  std::vector<int> rlen(nb);
+  for (int r = 0; r < nb; r++) {
+    int m = 0;
+    for (int k = row_ptr[r]; k < row_ptr[r + 1]; k++)
+      if (!lower || col[k] <= r) m++;
+    rlen[r] = m;
+  }
+  auto len = [&](int r) { return rlen[r]; };
   for (int w0 = 0; w0 < nb; w0 += kSliceWindow) {
     const int w1 = std::min(nb, w0 + kSliceWindow);
     std::stable_sort(order.begin() + w0, order.begin() + w1, [&](int a, int b) { return len(a) > len(b); });
@@ -361,9 +375,12 @@ void build_sliced(const std::vector<int>& row_ptr, const std::vector<int>& col, 
       int m = 0;
       if (r >= 0) {
         m = len(r);
-        for (int j = 0; j < m; j++) {
-          out.col[(size_t)(k0 + j) * S + t] = inv[col[row_ptr[r] + j]];
-          out.src[(size_t)(k0 + j) * S + t] = row_ptr[r] + j;
+        int j = 0;
+        for (int k = row_ptr[r]; k < row_ptr[r + 1]; k++) {
+          if (lower && col[k] > r) continue;
+          out.col[(size_t)(k0 + j) * S + t] = inv[col[k]];
+          out.src[(size_t)(k0 + j) * S + t] = (lower && col[k] == r) ? -(k + 2) : k;
+          j++;
         }
       }
       for (int k = k0 + m; k < k1; k++) out.col[(size_t)k * S + t] = rs;

@@ -185,6 +185,7 @@ struct RingScene {
 // vectors are in slice order (element 30*slice + lane).
 struct SliceSys {
   int ns = 0;                      // slices
+  int lower = 0;                   // lower-triangle storage (symmetric SpMV with transposed products)
   long long steps = 0;
   std::vector<int> off_host;       // ns+1
   double bytes = 0.0;              // algorithmic bytes of one SpMV + p.q phase
@@ -193,7 +194,8 @@ struct SliceSys {
   int* col = nullptr;              // steps*kSliceRows
   int* src = nullptr;              // steps*kSliceRows: full-BSR block or -1
   float* val = nullptr;            // steps*90
-  float* v32 = nullptr;            // p (40/slice), d, r, z, q (30/slice), preconditioner (90/slice)
+  float* v32 = nullptr;            // u (40/slice), d, r, p, w (30/slice), preconditioner (90/slice), s (30/slice);
+                                   // lower storage: w as float4 rows (40/slice) after s
   double* r64 = nullptr;           // FP64 residual (n_pad)
   long long device_bytes = 0;
 };
@@ -218,6 +220,7 @@ struct MixDesc {
   float* sval;
   float* v32;
   double* r64;
+  int lower;                       // lower-triangle sliced matrix (symmetric SpMV)
 };
 
 // A mixed-precision solve over one or more scenes (block diagonal): the
@@ -260,7 +263,12 @@ struct MixedSys {
   unsigned long long* cta_ns = nullptr;       // G (device)
   unsigned long long* cta_ns_host = nullptr;  // G (pinned)
   int rebalances = 0;
+  // tile shapes (the batch autotuner's choice, else the defaults)
+  int piece_steps = 20;            // ring-kernel steps per bulk copy (12, 16 or 20)
+  double slice_cost = 8.0;         // a slice's fixed cost in steps, for the CTA partition
 };
+bool ring_piece_supported(int ps);
+od_status mixed_retune(MixedSys* m, int piece_steps, double slice_cost);
 
 struct Ctx {
   int device = 0;
@@ -417,9 +425,11 @@ void build_full_bsr(int dofs, int nbc, int nrem, const std::vector<int>& pcol,
                     const std::vector<int>& rows, const std::vector<int>& oris, HostBsr& out);
 struct HostSliced {
   int ns = 0;
+  bool lower = false;
   std::vector<int> perm, off, col, src;
 };
-void build_sliced(const std::vector<int>& row_ptr, const std::vector<int>& col, int nb, HostSliced& out);
+void build_sliced(const std::vector<int>& row_ptr, const std::vector<int>& col, int nb, HostSliced& out,
+                  bool lower);
 void build_ic_levels(const std::vector<int>& rp, const std::vector<int>& ci, int n,
                      std::vector<int>& rows_by_level, std::vector<int>& lvl_ptr, bool forward);
 // incomplete LDL^T (od_rif.cpp): scalar columns of the symmetric matrix in

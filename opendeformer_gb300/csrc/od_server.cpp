@@ -14,11 +14,12 @@
 // that meets a request of a scene that is not resident evicts the least
 // recently used resident scenes it does not step itself (each to a host
 // checkpoint, od_scene_save) until the newcomer's estimated bytes fit, and
-// hands the newcomer to the admission worker: a host thread with a context
-// (and stream) of its own that builds the scene -- mesh analysis, pattern,
-// element maps, device arrays, integrator, checkpoint restore -- while the
-// tick's device work runs.  Scenes the worker finished join the next tick.
-// With admission_thread = 0 the tick builds them itself before stepping.
+// hands the newcomer to the admission workers: host threads, each with a
+// context (and stream) of its own, that build scenes -- mesh analysis,
+// pattern, element maps, device arrays, integrator, checkpoint restore --
+// in parallel while the tick's device work runs.  Scenes the workers
+// finished join the next tick.  With admission_thread = 0 the tick builds
+// them itself before stepping.
 //
 // Threads: the caller's thread owns the server and its context; the worker
 // only creates scenes in its own context and passes them over a locked
@@ -80,9 +81,9 @@ struct od_server {
   long long next_ticket = 1, stamp = 0;
   clock_type::time_point t0;
   od_server_stats stats{};
-  // admission worker
-  od_ctx* wctx = nullptr;
-  std::thread worker;
+  // admission workers, each with a context of its own
+  std::vector<od_ctx*> wctx;
+  std::vector<std::thread> workers;
   std::mutex mu;
   std::condition_variable cv;
   std::deque<int> todo;           // slots to build (locked)
@@ -114,7 +115,7 @@ od_status build_scene(od_ctx* c, Slot& sl, od_scene** out) {
   return OD_OK;
 }
 
-void worker_main(od_server* sv) {
+void worker_main(od_server* sv, od_ctx* wctx) {
   for (;;) {
     int sid = -1;
     {
@@ -126,7 +127,7 @@ void worker_main(od_server* sv) {
     }
     const auto t = clock_type::now();
     Built b{sid, nullptr, OD_OK, std::string()};
-    b.st = build_scene(sv->wctx, sv->slots[sid], &b.scene);
+    b.st = build_scene(wctx, sv->slots[sid], &b.scene);
     if (b.st != OD_OK) b.err = od_last_error();
     const double dt = std::chrono::duration<double>(clock_type::now() - t).count();
     std::lock_guard<std::mutex> lk(sv->mu);
@@ -230,6 +231,8 @@ extern "C" {
 od_status od_server_create(od_ctx* ctx, const od_server_config* cfg, od_server** out) {
   OD_CHECK_ARG(ctx && cfg && out, "od_server_create: NULL argument");
   OD_CHECK_ARG(cfg->max_batch >= 0, "od_server_create: max_batch must be >= 0");
+  OD_CHECK_ARG(cfg->admission_thread >= 0 && cfg->admission_thread <= 64,
+               "od_server_create: admission threads must be in 0..64");
   od_server* sv = new (std::nothrow) od_server();
   if (!sv) return OD_ERR_OUT_OF_MEMORY;
   sv->ctx = ctx;
@@ -244,16 +247,22 @@ od_status od_server_create(od_ctx* ctx, const od_server_config* cfg, od_server**
     if (e != cudaSuccess) { delete sv; return cuda_fail(e, "cudaMemGetInfo"); }
     sv->budget = std::max(0LL, (long long)fr - std::max(0LL, cfg->reserve_bytes));
   }
-  if (cfg->admission_thread) {
-    od_status st = od_ctx_create(ctx->c.device, &sv->wctx);
-    if (st != OD_OK) { delete sv; return st; }
-    try {
-      sv->worker = std::thread(worker_main, sv);
-    } catch (...) {
-      od_ctx_destroy(sv->wctx);
-      delete sv;
-      set_error("od_server_create: cannot start the admission thread");
-      return OD_ERR_INTERNAL;
+  for (int k = 0; k < cfg->admission_thread; k++) {
+    od_ctx* w = nullptr;
+    od_status st = od_ctx_create(ctx->c.device, &w);
+    if (st == OD_OK) {
+      try {
+        sv->workers.emplace_back(worker_main, sv, w);
+        sv->wctx.push_back(w);
+      } catch (...) {
+        od_ctx_destroy(w);
+        st = OD_ERR_INTERNAL;
+        set_error("od_server_create: cannot start an admission thread");
+      }
+    }
+    if (st != OD_OK) {
+      od_server_destroy(sv);
+      return st;
     }
   }
   *out = sv;
@@ -262,17 +271,16 @@ od_status od_server_create(od_ctx* ctx, const od_server_config* cfg, od_server**
 
 od_status od_server_destroy(od_server* sv) {
   if (!sv) return OD_OK;
-  if (sv->worker.joinable()) {
-    {
-      std::lock_guard<std::mutex> lk(sv->mu);
-      sv->stop = true;
-    }
-    sv->cv.notify_all();
-    sv->worker.join();
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->stop = true;
   }
+  sv->cv.notify_all();
+  for (std::thread& t : sv->workers)
+    if (t.joinable()) t.join();
   for (Built& b : sv->done) od_scene_destroy(b.scene);
   for (Slot& s : sv->slots) od_scene_destroy(s.scene);
-  od_ctx_destroy(sv->wctx);
+  for (od_ctx* w : sv->wctx) od_ctx_destroy(w);
   delete sv;
   return OD_OK;
 }
@@ -398,7 +406,7 @@ od_status od_server_tick(od_server* sv, int capacity, od_step_result* results, i
     }
     sl.bytes = est;
     sv->used += est;
-    if (sv->worker.joinable()) {
+    if (!sv->workers.empty()) {
       sl.state = Slot::kBuilding;
       {
         std::lock_guard<std::mutex> lk(sv->mu);

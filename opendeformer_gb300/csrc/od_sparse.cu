@@ -729,7 +729,10 @@ __global__ void mix_fill_kernel(int n_sc, const int* __restrict__ prefix, const 
     const int st = st0 + q / 90, rem = q % 90;
     const int j = rem / 30, lane = rem - 30 * j;
     const int blk = D.ssrc[(size_t)st * kSliceRows + lane / 3];
-    D.sval[(size_t)st * 90 + rem] = blk >= 0 ? (float)A[(size_t)blk * 9 + 3 * (lane % 3) + j] : 0.f;
+    float v = 0.f;   // padding
+    if (blk >= 0) v = (float)A[(size_t)blk * 9 + 3 * (lane % 3) + j];
+    else if (blk <= -2) v = (float)(0.5 * A[(size_t)(-blk - 2) * 9 + 3 * (lane % 3) + j]);   // halved diagonal
+    D.sval[(size_t)st * 90 + rem] = v;
   }
 }
 
@@ -835,7 +838,7 @@ __global__ void mix_update_kernel(int n_sc, const int* __restrict__ prefix, cons
 // Every CTA owns a contiguous range of slices (of one or more scenes);
 // consumer warp w of the CTA takes slices first + w, first + w + kRingWarps,
 // ...  Producer lane w (of the CTA's last warp) streams warp w's slices, cut
-// into pieces of at most kRingSteps steps, from global memory into a private
+// into pieces of at most PS steps (a template parameter), from global memory into a private
 // two-stage ring in shared memory with cp.async.bulk (evict-first in L2, so
 // the vectors stay resident), signalling a "full" mbarrier per stage; the
 // consumer warp releases a stage through its "empty" mbarrier.  The matrix
@@ -848,9 +851,14 @@ __global__ void mix_update_kernel(int n_sc, const int* __restrict__ prefix, cons
 constexpr int kRingWarps = 12;                       // consumer warps per CTA
 constexpr int kRingThreads = 32 * (kRingWarps + 1);  // + the producer warp
 constexpr int kRingConsumers = 32 * kRingWarps;
-constexpr int kRingSteps = 20;                       // steps per piece (even)
-constexpr int kRingStageBytes = kRingSteps * 400;    // 90 floats + 10 ints per step
-constexpr int kRingSmem = kRingWarps * 2 * kRingStageBytes + kRingWarps * 2 * 2 * 8;
+// Steps per piece (even; a tile shape the batch autotuner picks): each
+// stage holds a piece's values (90 floats per step) then its columns (10
+// ints per step); two stages per consumer warp plus the mbarriers.
+constexpr int kRingStepsDefault = 20;
+__host__ __device__ constexpr int ring_stage_bytes(int ps) { return ps * 400; }
+__host__ __device__ constexpr int ring_smem_bytes(int ps) {
+  return kRingWarps * 2 * ring_stage_bytes(ps) + kRingWarps * 2 * 2 * 8;
+}
 constexpr unsigned long long kMbarSpinLimit = 1ull << 24;
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -886,6 +894,12 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
       "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(policy)
       : "memory");
 }
+// w[0..2] += (a, b, c) as one vector reduction in L2 (w[3] stays zero)
+__device__ __forceinline__ void red_add_v4(float4* w, float a, float b, float c) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(w), "f"(a), "f"(b), "f"(c), "f"(0.f)
+               : "memory");
+}
+
 template <int NT>
 __device__ __forceinline__ void named_sync() {
   asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory");
@@ -1011,13 +1025,14 @@ __device__ __forceinline__ bool grid_barrier_named(GridBarrier* gb) {
 // slice element 30*slice + l, i.e. component l%3 of slice row l/3 (lanes
 // 30, 31 shadow lane 29 and store nothing).  Dot products accumulate in
 // compensated FP32 per lane and are summed in FP64.
+template <int PS>
 __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
     int n_sc, const int* __restrict__ cta_first, const int* __restrict__ cta_sc_lo, const int* __restrict__ sc_cta,
     const int* __restrict__ sc_slice, const MixDesc* __restrict__ desc, RingScene* __restrict__ ring, int pkind,
     double* __restrict__ part, GridBarrier* gb, unsigned long long* __restrict__ prof,
     unsigned long long* __restrict__ cta_ns) {
   extern __shared__ __align__(128) unsigned char ring_smem[];
-  unsigned long long* full = reinterpret_cast<unsigned long long*>(ring_smem + kRingWarps * 2 * kRingStageBytes);
+  unsigned long long* full = reinterpret_cast<unsigned long long*>(ring_smem + kRingWarps * 2 * ring_stage_bytes(PS));
   unsigned long long* empty = full + 2 * kRingWarps;
   __shared__ RingShared sh;
   const int G = gridDim.x;
@@ -1098,8 +1113,8 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
         const MixDesc& P = sh.lp[ls];
         const int lsl = sl - P.slice0;
         const int k1 = P.soff[lsl + 1];
-        for (int k = P.soff[lsl]; k < k1; k += kRingSteps) {
-          const int n = min(kRingSteps, k1 - k);
+        for (int k = P.soff[lsl]; k < k1; k += PS) {
+          const int n = min(PS, k1 - k);
           const int j = pc & 1;
           const unsigned par = ((pc >> 1) & 1) ^ 1;
           bool got = false;
@@ -1109,10 +1124,10 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
           }
           if (!got) { ok = false; break; }
           if (copy) {
-            unsigned char* st = ring_smem + (size_t)(2 * pw + j) * kRingStageBytes;
+            unsigned char* st = ring_smem + (size_t)(2 * pw + j) * ring_stage_bytes(PS);
             mbar_expect_tx(full + 2 * pw + j, (unsigned)n * 400u);
             bulk_g2s(st, P.sval + (size_t)k * 90, (unsigned)n * 360u, full + 2 * pw + j, policy);
-            bulk_g2s(st + kRingSteps * 360, P.scol + (size_t)k * kSliceRows, (unsigned)n * 40u, full + 2 * pw + j,
+            bulk_g2s(st + PS * 360, P.scol + (size_t)k * kSliceRows, (unsigned)n * 40u, full + 2 * pw + j,
                      policy);
           } else {
             mbar_arrive(full + 2 * pw + j);
@@ -1165,6 +1180,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
   struct Vecs {
     float4* u4;
     float *uf, *d, *r, *p, *w, *pinv, *s;
+    float4* w4;   // lower storage: w = A u as float4 rows, accumulated by reductions
     int s0;
   };
   auto vecs = [&](int ls) {
@@ -1179,6 +1195,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
     v.w = v.p + 30 * ns;
     v.pinv = v.w + 30 * ns;
     v.s = v.pinv + 90 * ns;
+    v.w4 = reinterpret_cast<float4*>(v.s + 30 * ns);
     v.s0 = P.slice0;
     return v;
   };
@@ -1213,6 +1230,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
         V.p[i] = 0.f;
         V.s[i] = 0.f;
         V.uf[4 * (size_t)rs + rsub] = ul;
+        if (sh.lp[ls].lower) reinterpret_cast<float*>(V.w4)[4 * (size_t)rs + rsub] = 0.f;
         comp_add_prod(cru, rl, ul);
         comp_add_prod(crr, rl, rl);
       }
@@ -1242,6 +1260,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
       for (int ls = 0; ls < L && alive; ls++) {
         if (!(k == 0 ? sh.act_in[ls] : sh.act[kp ^ 1][ls])) continue;  // no pieces this iteration
         const bool on = sh.act[kp][ls] != 0;
+        const bool lower = sh.lp[ls].lower != 0;   // scene-uniform
         const Vecs V = vecs(ls);
         const int* __restrict__ soff = sh.lp[ls].soff;
         Comp cwu{0.f, 0.f};
@@ -1249,8 +1268,10 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
           const int lsl = sl - V.s0;
           const int k1 = soff[lsl + 1];
           float y0 = 0.f, y1 = 0.f, y2 = 0.f;  // partial rows 0, 1, 2 of block row t
-          for (int kk = soff[lsl]; kk < k1; kk += kRingSteps) {
-            const int n = min(kRingSteps, k1 - kk);
+          // lower storage: u of block row t, for the transposed products
+          const float4 uo = (lower && on) ? V.u4[(size_t)lsl * kSliceRows + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+          for (int kk = soff[lsl]; kk < k1; kk += PS) {
+            const int n = min(PS, k1 - kk);
             const int j = pc & 1;
             if (!__all_sync(0xffffffffu, mbar_wait(full + 2 * w + j, (pc >> 1) & 1))) {
               atomicExch(&gb->timeout, 1);
@@ -1258,12 +1279,12 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
               break;
             }
             if (on) {
-              const unsigned char* stg = ring_smem + (size_t)(2 * w + j) * kRingStageBytes;
+              const unsigned char* stg = ring_smem + (size_t)(2 * w + j) * ring_stage_bytes(PS);
               const float* sv = reinterpret_cast<const float*>(stg);
-              const int* scol = reinterpret_cast<const int*>(stg + kRingSteps * 360);
+              const int* scol = reinterpret_cast<const int*>(stg + PS * 360);
               // lane (t, rsub) takes steps rsub, rsub + 3, ... of the piece
               // for all three rows of block row t: every gather is issued first
-              constexpr int kPer = (kRingSteps + 2) / 3;
+              constexpr int kPer = (PS + 2) / 3;
               float4 x[kPer];
 #pragma unroll
               for (int u = 0; u < kPer; u++) {
@@ -1284,6 +1305,13 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
                   y2 = fmaf(a[2], x[u].x, y2);
                   y2 = fmaf(a[32], x[u].y, y2);
                   y2 = fmaf(a[62], x[u].z, y2);
+                  if (lower && act_l) {
+                    // the block's transpose: B^T u_t into the column's row of w
+                    const float t0 = fmaf(a[0], uo.x, fmaf(a[1], uo.y, a[2] * uo.z));
+                    const float t1 = fmaf(a[30], uo.x, fmaf(a[31], uo.y, a[32] * uo.z));
+                    const float t2 = fmaf(a[60], uo.x, fmaf(a[61], uo.y, a[62] * uo.z));
+                    red_add_v4(V.w4 + scol[st * kSliceRows + t], t0, t1, t2);
+                  }
                 }
               }
             }
@@ -1301,7 +1329,17 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
             const float na = rsub == 0 ? a0 : (rsub == 1 ? a1 : a2);
             const float nb = rsub == 0 ? b0 : (rsub == 1 ? b1 : b2);
             const float y = (own + na) + nb;
-            if (act_l) {
+            if (lower) {
+              // w of the own row takes the gathered half by one reduction;
+              // (w, u) = 2 sum_rows u . (gathered half) (the scattered half
+              // carries the same products transposed)
+              const float yb = __shfl_sync(0xffffffffu, y, lbase + 1);
+              const float yc = __shfl_sync(0xffffffffu, y, lbase + 2);
+              if (act_l) {
+                comp_add_prod(cwu, 2.f * V.uf[4 * (size_t)(lsl * kSliceRows + t) + rsub], y);
+                if (rsub == 0) red_add_v4(V.w4 + (size_t)lsl * kSliceRows + t, y, yb, yc);
+              }
+            } else if (act_l) {
               V.w[(size_t)30 * lsl + lane] = y;
               comp_add_prod(cwu, V.uf[4 * (size_t)(lsl * kSliceRows + t) + rsub], y);
             }
@@ -1362,6 +1400,8 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
       constexpr int kUB = 4;
       const int hi = sh.lfirst[ls + 1];
       const Vecs V = vecs(ls);
+      const bool lower = sh.lp[ls].lower != 0;
+      float* w4f = reinterpret_cast<float*>(V.w4);
       const float alpha = (float)sh.alpha[ls], beta = (float)sh.beta[ls];
       Comp cru{0.f, 0.f}, crr{0.f, 0.f};
       for (int sl0 = first_slice(ls); sl0 < hi; sl0 += kUB * kRingWarps) {
@@ -1376,7 +1416,8 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
             pv[u] = V.p[i];
             sv[u] = V.s[i];
             uv[u] = V.uf[4 * (size_t)(lsl * kSliceRows + t) + rsub];
-            wv[u] = V.w[i];
+            // lower storage: w was summed by reductions in L2 (read there)
+            wv[u] = lower ? __ldcg(w4f + 4 * (size_t)(lsl * kSliceRows + t) + rsub) : V.w[i];
             rv[u] = V.r[i];
             if (pkind == OD_PRECOND_BLOCK_JACOBI) {
               const float* m = V.pinv + (size_t)90 * lsl + ln;
@@ -1409,6 +1450,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
               V.d[i] = fmaf(alpha, pn, dv[u]);
               V.r[i] = rl;
               V.uf[4 * (size_t)(lsl * kSliceRows + t) + rsub] = ul;
+              if (lower) w4f[4 * (size_t)(lsl * kSliceRows + t) + rsub] = 0.f;   // for the next SpMV phase
               comp_add_prod(cru, rl, ul);
               comp_add_prod(crr, rl, rl);
             }
@@ -2166,14 +2208,30 @@ static od_status pcg_finish(Scene* s, const double* d_b, double* d_x, double shi
 
 // ---- mixed-precision systems: build, partition, solve
 
+// the ring kernel of a piece size (12, 16 or 20 steps)
+static const void* ring_kernel(int ps) {
+  switch (ps) {
+    case 12: return (const void*)pcg32_ring_kernel<12>;
+    case 16: return (const void*)pcg32_ring_kernel<16>;
+    default: return (const void*)pcg32_ring_kernel<20>;
+  }
+}
+
+bool ring_piece_supported(int ps) { return ps == 12 || ps == 16 || ps == 20; }
+
+// co-resident CTAs of the ring kernel: one per SM for every piece size
 static int ring_kernel_ctas(const Ctx* ctx) {
-  if (cudaFuncSetAttribute(pcg32_ring_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kRingSmem) != cudaSuccess)
-    return 0;
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pcg32_ring_kernel, kRingThreads, kRingSmem) !=
-      cudaSuccess)
-    return 0;
-  return std::min(per_sm, 1) * ctx->num_sms;
+  int per_sm = 1;
+  for (int ps : {12, 16, 20}) {
+    int p = 0;
+    if (cudaFuncSetAttribute(ring_kernel(ps), cudaFuncAttributeMaxDynamicSharedMemorySize, ring_smem_bytes(ps)) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, ring_kernel(ps), kRingThreads, ring_smem_bytes(ps)) !=
+            cudaSuccess)
+      return 0;
+    per_sm = std::min(per_sm, p);
+  }
+  return per_sm * ctx->num_sms;
 }
 
 void slice_free(SliceSys* sl) {
@@ -2198,11 +2256,20 @@ od_status slice_build(Scene* s) {
   if (P.slice) return OD_OK;
   SliceSys* sl = new SliceSys();
   HostSliced hs;
-  build_sliced(s->hbsr_rp, s->hbsr_col, s->bsr.nb, hs);
+  // the symmetric (lower-triangle) operator halves the matrix stream of
+  // every inner iteration; OD_GB300_MIXED_SPMV=full keeps both triangles
+  // (deterministic: no atomic accumulation)
+  const char* menv = std::getenv("OD_GB300_MIXED_SPMV");
+  const bool lower = !(menv && std::strcmp(menv, "full") == 0);
+  build_sliced(s->hbsr_rp, s->hbsr_col, s->bsr.nb, hs, lower);
+  sl->lower = lower ? 1 : 0;
   sl->ns = hs.ns;
   sl->steps = hs.off[hs.ns];
   sl->off_host = hs.off;
-  sl->bytes = 40.0 * s->bsr.nnzb + 24.0 * s->bsr.nb;
+  long long stored = 0;
+  for (int r = 0; r < s->bsr.nb; r++)
+    for (int k = s->hbsr_rp[r]; k < s->hbsr_rp[r + 1]; k++) stored += (!lower || s->hbsr_col[k] <= r) ? 1 : 0;
+  sl->bytes = 40.0 * (double)stored + 24.0 * s->bsr.nb;
   auto fail = [&](od_status st) { slice_free(sl); return st; };
   od_status st;
   if ((st = dev_upload(&sl->perm, hs.perm.data(), hs.perm.size(), sl->device_bytes)) != OD_OK) return fail(st);
@@ -2211,7 +2278,8 @@ od_status slice_build(Scene* s) {
   if ((st = dev_upload(&sl->src, hs.src.data(), hs.src.size(), sl->device_bytes)) != OD_OK) return fail(st);
   const size_t ns = (size_t)std::max(1, sl->ns);
   const size_t nval = (size_t)std::max<long long>(1, sl->steps) * 90;
-  const size_t nvec = (40 + 4 * 30 + 90 + 30) * ns;   // u (float4 rows), d, r, p, w, preconditioner, s
+  // u (float4 rows), d, r, p, w, preconditioner, s; lower storage adds w as float4 rows
+  const size_t nvec = (40 + 4 * 30 + 90 + 30 + (lower ? 40 : 0)) * ns;
   cudaError_t e = cudaMalloc(&sl->val, sizeof(float) * nval);
   if (e == cudaSuccess) e = cudaMalloc(&sl->v32, sizeof(float) * nvec);
   if (e == cudaSuccess) e = cudaMemset(sl->v32, 0, sizeof(float) * nvec);
@@ -2254,8 +2322,7 @@ constexpr double kSliceCost = 8.0;
 static od_status mixed_partition(MixedSys* m, int G) {
   const int ns = m->ns;
   if ((int)m->slice_w.size() != ns) {
-    double c_slice = kSliceCost;
-    if (const char* e = std::getenv("OD_GB300_SLICE_COST")) c_slice = std::atof(e);
+    const double c_slice = m->slice_cost;
     m->slice_w.resize(ns);
     for (int k = 0; k < ns; k++) m->slice_w[k] = (double)(m->off_host[k + 1] - m->off_host[k]) + c_slice;
   }
@@ -2326,8 +2393,7 @@ static void mixed_work_weights(MixedSys* m) {
   if (known.empty()) return;
   std::nth_element(known.begin(), known.begin() + known.size() / 2, known.end());
   const double med = std::max(1.0, known[known.size() / 2]);
-  double c_slice = kSliceCost;
-  if (const char* e = std::getenv("OD_GB300_SLICE_COST")) c_slice = std::atof(e);
+  const double c_slice = m->slice_cost;
   m->slice_w.resize(m->ns);
   for (int s = 0; s < m->n_sc; s++) {
     const double it = m->scenes[s]->mix_iters_last > 0.0 ? m->scenes[s]->mix_iters_last : med;
@@ -2344,6 +2410,19 @@ static od_status mixed_partition_work(MixedSys* m, int G) {
   if (mixed_partition(m, G) == OD_OK) return OD_OK;
   m->slice_w.clear();
   return mixed_partition(m, G);
+}
+
+// new tile shapes for a built system: piece size of the ring kernel and the
+// per-slice cost of the partition (the slices are re-partitioned)
+od_status mixed_retune(MixedSys* m, int piece_steps, double slice_cost) {
+  if (!ring_piece_supported(piece_steps) || !(slice_cost >= 0.0)) {
+    set_error("mixed tuning: piece steps must be 12, 16 or 20 and the slice cost >= 0");
+    return OD_ERR_INVALID_ARG;
+  }
+  m->piece_steps = piece_steps;
+  m->slice_cost = slice_cost;
+  m->slice_w.clear();
+  return m->n_sc > 1 ? mixed_partition_work(m, m->cta_grid) : mixed_partition(m, m->cta_grid);
 }
 
 // After a solve of a one-scene system: scale the weights of each CTA's
@@ -2393,6 +2472,9 @@ od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::ve
     return OD_ERR_UNSUPPORTED;
   }
   MixedSys* m = new MixedSys();
+  if (const char* e = std::getenv("OD_GB300_SLICE_COST")) m->slice_cost = std::atof(e);
+  if (const char* e = std::getenv("OD_GB300_RING_PIECE"))
+    if (ring_piece_supported(std::atoi(e))) m->piece_steps = std::atoi(e);
   const int n = (int)scenes.size();
   m->n_sc = n;
   m->scenes = scenes;
@@ -2426,6 +2508,7 @@ od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::ve
     d.sval = sl->val;
     d.v32 = sl->v32;
     d.r64 = sl->r64;
+    d.lower = sl->lower;
     m->desc_host.push_back(d);
     m->sc_slice.push_back(d.slice0 + sl->ns);
     m->sc_nb.push_back(s->bsr.nb);
@@ -2544,8 +2627,8 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
                     (void*)&m->part,   (void*)&gbp,          (void*)&profp,       (void*)&m->cta_ns};
     if (prof) OD_CUDA(cudaEventRecord(ctx->ev_pool[0], strm));
     ctx->launches++;
-    OD_CUDA(cudaLaunchCooperativeKernel((void*)pcg32_ring_kernel, dim3(m->cta_grid), dim3(kRingThreads), args,
-                                        kRingSmem, strm));
+    OD_CUDA(cudaLaunchCooperativeKernel(ring_kernel(m->piece_steps), dim3(m->cta_grid), dim3(kRingThreads), args,
+                                        ring_smem_bytes(m->piece_steps), strm));
     if (prof) OD_CUDA(cudaEventRecord(ctx->ev_pool[1], strm));
     if (m->upd_dir.tiles > 0) {
       ctx->launches++;

@@ -77,16 +77,18 @@ constexpr unsigned kSweepSpinLimit = 1u << 21;
 // bounded wait until v (first read of *p) is written; after a timeout
 // anywhere (err set) no thread waits any more, so the launch ends promptly
 // and the host reports it
-__device__ __forceinline__ double finish_wait(unsigned long long v, const double* p, int* err) {
-  for (unsigned k = 1; v == kPending; k++) {
+template <class T>
+__device__ __forceinline__ T finish_wait(typename SweepFlag<T>::U v, const T* p, int* err) {
+  using F = SweepFlag<T>;
+  for (unsigned k = 1; v == F::kPend; k++) {
     if (k >= kSweepSpinLimit) {
       atomicOr(err, 1);
-      return 0.0;
+      return T(0);
     }
-    if ((k & 1023u) == 0 && *(volatile int*)err) return 0.0;
-    v = ld_relaxed_u64(p);
+    if ((k & 1023u) == 0 && *(volatile int*)err) return T(0);
+    v = F::ld(p);
   }
-  return __longlong_as_double((long long)v);
+  return F::val(v);
 }
 
 constexpr int kSweepBatch = 4;   // entries per lane with their value loads in flight together
@@ -97,24 +99,26 @@ constexpr unsigned kSweepPollBurst = 1024;   // polls of one value between check
 // outside the triple (forward: index < i0; backward: index >= i0 + m);
 // the entries inside the triple go to the warp's slots in[] (L_10, L_20,
 // L_21).  Each lane loads kSweepBatch entries, then their values together.
-template <bool FWD>
+template <bool FWD, class T>
 __device__ __forceinline__ void triple_sums(int rb0, int rb1, int rb2, int rb3, int i0, int m,
-                                            const int* __restrict__ idx, const double* __restrict__ val,
-                                            const double* vec, double* in, int* err, int lane, double& a0,
-                                            double& a1, double& a2) {
+                                            const int* __restrict__ idx, const T* __restrict__ val,
+                                            const T* vec, T* in, int* err, int lane, T& a0,
+                                            T& a1, T& a2) {
+  using F = SweepFlag<T>;
+  using U = typename F::U;
   for (int q0 = rb0; q0 < rb3; q0 += 32 * kSweepBatch) {
     int ix[kSweepBatch], kr[kSweepBatch];
-    double lv[kSweepBatch];
-    unsigned long long v[kSweepBatch];
+    T lv[kSweepBatch];
+    U v[kSweepBatch];
 #pragma unroll
     for (int u = 0; u < kSweepBatch; u++) {
       const int q = q0 + u * 32 + lane;
       ix[u] = -1;
       kr[u] = 0;
-      lv[u] = 0.0;
+      lv[u] = T(0);
       if (q < rb3) {
         const int c = idx[q];
-        const double l = val[q];
+        const T l = val[q];
         const int k = q < rb1 ? 0 : (q < rb2 ? 1 : 2);
         if (FWD ? c < i0 : c >= i0 + m) {
           ix[u] = c;
@@ -126,7 +130,7 @@ __device__ __forceinline__ void triple_sums(int rb0, int rb1, int rb2, int rb3, 
       }
     }
 #pragma unroll
-    for (int u = 0; u < kSweepBatch; u++) v[u] = ix[u] >= 0 ? ld_relaxed_u64(vec + ix[u]) : 0ull;
+    for (int u = 0; u < kSweepBatch; u++) v[u] = ix[u] >= 0 ? F::ld(vec + ix[u]) : U(0);
     // warp-cooperative wait: one lane polls the first value still pending
     // in the warp, then every lane re-reads its pending values once; the
     // values of one level land together, so one or two rounds usually do,
@@ -136,17 +140,17 @@ __device__ __forceinline__ void triple_sums(int rb0, int rb1, int rb2, int rb3, 
       int pu = -1;
 #pragma unroll
       for (int u = kSweepBatch - 1; u >= 0; u--)
-        if (ix[u] >= 0 && v[u] == kPending) pu = u;
+        if (ix[u] >= 0 && v[u] == F::kPend) pu = u;
       const unsigned ball = __ballot_sync(0xffffffffu, pu >= 0);
       if (!ball) break;
       int stop = 0;
       if (lane == __ffs(ball) - 1) {
-        const double* p = vec;
+        const T* p = vec;
 #pragma unroll
         for (int u = 0; u < kSweepBatch; u++)
           if (u == pu) p += ix[u];
         unsigned k = 0;
-        while (ld_relaxed_u64(p) == kPending && ++k < kSweepPollBurst) {
+        while (F::ld(p) == F::kPend && ++k < kSweepPollBurst) {
         }
         stop = round >= kSweepSpinLimit / kSweepPollBurst || *(volatile int*)err;
         if (round >= kSweepSpinLimit / kSweepPollBurst) atomicOr(err, 1);
@@ -154,17 +158,17 @@ __device__ __forceinline__ void triple_sums(int rb0, int rb1, int rb2, int rb3, 
       if (__any_sync(0xffffffffu, stop)) {
 #pragma unroll
         for (int u = 0; u < kSweepBatch; u++)
-          if (v[u] == kPending) v[u] = 0ull;
+          if (v[u] == F::kPend) v[u] = U(0);
         break;
       }
 #pragma unroll
       for (int u = 0; u < kSweepBatch; u++)
-        if (ix[u] >= 0 && v[u] == kPending) v[u] = ld_relaxed_u64(vec + ix[u]);
+        if (ix[u] >= 0 && v[u] == F::kPend) v[u] = F::ld(vec + ix[u]);
     }
 #pragma unroll
     for (int u = 0; u < kSweepBatch; u++) {
       if (ix[u] < 0) continue;
-      const double p = lv[u] * __longlong_as_double((long long)v[u]);
+      const T p = lv[u] * F::val(v[u]);
       if (kr[u] == 0) a0 += p;
       else if (kr[u] == 1) a1 += p;
       else a2 += p;
@@ -177,20 +181,21 @@ __device__ __forceinline__ void triple_sums(int rb0, int rb1, int rb2, int rb3, 
 // a warp sums the products of all three rows with values outside the
 // triple (three interleaved butterflies), then lane 0 resolves the chain
 // inside the triple in registers and publishes the three values.
-template <int IC>
+template <int IC, class T>
 __global__ void __launch_bounds__(kSweepThreads, 2) sweep_apply_kernel(
     int n, int n_pad, int ng, const int* __restrict__ frp, const int* __restrict__ fci,
-    const double* __restrict__ fval, const int* __restrict__ bcp, const int* __restrict__ bri,
-    const double* __restrict__ bval, const int* __restrict__ ord_f, const int* __restrict__ ord_b,
-    const double* __restrict__ dinv, const double* __restrict__ r, double* y, double* z, int* __restrict__ err,
-    const SolveScalars* sc, const int* __restrict__ perm, double* __restrict__ zout) {
-  __shared__ double inner_s[kSweepThreads / 32][3];
+    const T* __restrict__ fval, const int* __restrict__ bcp, const int* __restrict__ bri,
+    const T* __restrict__ bval, const int* __restrict__ ord_f, const int* __restrict__ ord_b,
+    const T* __restrict__ dinv, const T* __restrict__ r, T* y, T* z, int* __restrict__ err,
+    const SolveScalars* sc, const int* __restrict__ perm, T* __restrict__ zout) {
+  using F = SweepFlag<T>;
+  __shared__ T inner_s[kSweepThreads / 32][3];
   if (sc && *(volatile const int*)&sc->done) return;
   const int lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
   const int W = gridDim.x * wpb;
   const int w = blockIdx.x * wpb + (threadIdx.x >> 5);
-  double* in = inner_s[threadIdx.x >> 5];
+  T* in = inner_s[threadIdx.x >> 5];
   // padding rows carry the identity
   for (int i = n + blockIdx.x * blockDim.x + threadIdx.x; i < n_pad; i += gridDim.x * blockDim.x) {
     if (perm) zout[perm[i]] = r[perm[i]];
@@ -202,17 +207,17 @@ __global__ void __launch_bounds__(kSweepThreads, 2) sweep_apply_kernel(
     const int g = ord_f[t];
     const int i0 = 3 * g, m = min(3, n - i0);
     const int rb0 = frp[i0], rb1 = frp[i0 + 1], rb2 = frp[i0 + min(2, m)], rb3 = frp[i0 + m];
-    double rv[3] = {0.0, 0.0, 0.0}, dv[3] = {0.0, 0.0, 0.0};
+    T rv[3] = {T(0), T(0), T(0)}, dv[3] = {T(0), T(0), T(0)};
     if (lane == 0)
       for (int k = 0; k < m; k++) {
         rv[k] = r[perm ? perm[i0 + k] : i0 + k];
-        dv[k] = IC ? dinv[i0 + k] : 1.0;
+        dv[k] = IC ? dinv[i0 + k] : T(1);
       }
     __syncwarp();
-    if (lane < 3) in[lane] = 0.0;
+    if (lane < 3) in[lane] = T(0);
     __syncwarp();
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-    triple_sums<true>(rb0, rb1, rb2, rb3, i0, m, fci, fval, y, in, err, lane, a0, a1, a2);
+    T a0 = T(0), a1 = T(0), a2 = T(0);
+    triple_sums<true, T>(rb0, rb1, rb2, rb3, i0, m, fci, fval, y, in, err, lane, a0, a1, a2);
     for (int o = 16; o; o >>= 1) {
       a0 += __shfl_xor_sync(0xffffffffu, a0, o);
       a1 += __shfl_xor_sync(0xffffffffu, a1, o);
@@ -220,15 +225,15 @@ __global__ void __launch_bounds__(kSweepThreads, 2) sweep_apply_kernel(
     }
     __syncwarp();
     if (lane == 0) {
-      const double y0 = IC ? (rv[0] - a0) * dv[0] : rv[0] - a0;
-      st_relaxed_f64(y + i0, y0);
+      const T y0 = IC ? (rv[0] - a0) * dv[0] : rv[0] - a0;
+      F::st(y + i0, y0);
       if (m > 1) {
-        const double s1 = rv[1] - a1 - in[0] * y0;
-        const double y1 = IC ? s1 * dv[1] : s1;
-        st_relaxed_f64(y + i0 + 1, y1);
+        const T s1 = rv[1] - a1 - in[0] * y0;
+        const T y1 = IC ? s1 * dv[1] : s1;
+        F::st(y + i0 + 1, y1);
         if (m > 2) {
-          const double s2 = rv[2] - a2 - in[1] * y0 - in[2] * y1;
-          st_relaxed_f64(y + i0 + 2, IC ? s2 * dv[2] : s2);
+          const T s2 = rv[2] - a2 - in[1] * y0 - in[2] * y1;
+          F::st(y + i0 + 2, IC ? s2 * dv[2] : s2);
         }
       }
     }
@@ -239,20 +244,20 @@ __global__ void __launch_bounds__(kSweepThreads, 2) sweep_apply_kernel(
     const int g = ord_b[t];
     const int i0 = 3 * g, m = min(3, n - i0);
     const int cb0 = bcp[i0], cb1 = bcp[i0 + 1], cb2 = bcp[i0 + min(2, m)], cb3 = bcp[i0 + m];
-    double yv[3] = {0.0, 0.0, 0.0}, dv[3] = {0.0, 0.0, 0.0};
+    T yv[3] = {T(0), T(0), T(0)}, dv[3] = {T(0), T(0), T(0)};
     if (lane == 0) {
-      unsigned long long v[3] = {0ull, 0ull, 0ull};
+      typename F::U v[3] = {0, 0, 0};
       for (int k = 0; k < m; k++) {
-        v[k] = ld_relaxed_u64(y + i0 + k);
+        v[k] = F::ld(y + i0 + k);
         dv[k] = dinv[i0 + k];
       }
-      for (int k = 0; k < m; k++) yv[k] = finish_wait(v[k], y + i0 + k, err);
+      for (int k = 0; k < m; k++) yv[k] = finish_wait<T>(v[k], y + i0 + k, err);
     }
     __syncwarp();
-    if (lane < 3) in[lane] = 0.0;
+    if (lane < 3) in[lane] = T(0);
     __syncwarp();
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-    triple_sums<false>(cb0, cb1, cb2, cb3, i0, m, bri, bval, z, in, err, lane, a0, a1, a2);
+    T a0 = T(0), a1 = T(0), a2 = T(0);
+    triple_sums<false, T>(cb0, cb1, cb2, cb3, i0, m, bri, bval, z, in, err, lane, a0, a1, a2);
     for (int o = 16; o; o >>= 1) {
       a0 += __shfl_xor_sync(0xffffffffu, a0, o);
       a1 += __shfl_xor_sync(0xffffffffu, a1, o);
@@ -260,19 +265,19 @@ __global__ void __launch_bounds__(kSweepThreads, 2) sweep_apply_kernel(
     }
     __syncwarp();
     if (lane == 0) {
-      double z2 = 0.0, z1 = 0.0;
+      T z2 = T(0), z1 = T(0);
       if (m > 2) {
         z2 = IC ? (yv[2] - a2) * dv[2] : yv[2] * dv[2] - a2;
-        st_relaxed_f64(z + i0 + 2, z2);
+        F::st(z + i0 + 2, z2);
       }
       if (m > 1) {
-        const double e1 = a1 + z2 * in[2];
+        const T e1 = a1 + z2 * in[2];
         z1 = IC ? (yv[1] - e1) * dv[1] : yv[1] * dv[1] - e1;
-        st_relaxed_f64(z + i0 + 1, z1);
+        F::st(z + i0 + 1, z1);
       }
-      const double e0 = a0 + z1 * in[0] + z2 * in[1];
-      const double z0 = IC ? (yv[0] - e0) * dv[0] : yv[0] * dv[0] - e0;
-      st_relaxed_f64(z + i0, z0);
+      const T e0 = a0 + z1 * in[0] + z2 * in[1];
+      const T z0 = IC ? (yv[0] - e0) * dv[0] : yv[0] * dv[0] - e0;
+      F::st(z + i0, z0);
       if (perm) {  // the caller's order
         zout[perm[i0]] = z0;
         if (m > 1) zout[perm[i0 + 1]] = z1;
@@ -374,8 +379,8 @@ void sweep_group_levels(int n, const std::vector<int>& frp, const std::vector<in
 od_status sweep_grid(Scene* s, int n, int* grid) {
   int dev_coop = 0, per0 = 0, per1 = 0;
   OD_CUDA(cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, s->ctx->device));
-  OD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, sweep_apply_kernel<0>, kSweepThreads, 0));
-  OD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, sweep_apply_kernel<1>, kSweepThreads, 0));
+  OD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, sweep_apply_kernel<0, double>, kSweepThreads, 0));
+  OD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, sweep_apply_kernel<1, double>, kSweepThreads, 0));
   const int per_sm = std::min(per0, per1);
   if (!dev_coop || per_sm < 1) {
     set_error("the triangular-sweep apply needs cooperative launch");
@@ -611,7 +616,7 @@ od_status sweep_launch(Scene* s, const SweepView& v, const double* r, double* z,
     OD_CUDA(cudaMemsetAsync(zflag, 0xff, sizeof(double) * (size_t)n, strm));
   }
   OD_KL(s);
-  void* fn = v.ic ? (void*)sweep_apply_kernel<1> : (void*)sweep_apply_kernel<0>;
+  void* fn = v.ic ? (void*)sweep_apply_kernel<1, double> : (void*)sweep_apply_kernel<0, double>;
   OD_CUDA(cudaLaunchCooperativeKernel(fn, dim3(v.grid), dim3(kSweepThreads), args, 0, strm));
   if (prof) {
     OD_CUDA(cudaEventRecord(ctx->ev_pool[ctx->ev_pool.size() - 1], strm));

@@ -58,12 +58,17 @@ class Server:
     (default: the device's free memory at creation less reserve_bytes).
     batched=False steps each tick's requests one scene at a time instead (the
     plain path, for comparison; the scenes' precision is their spec's).
-    admission_thread=False builds admitted scenes inside the tick."""
+    admission_thread: host threads that build admitted scenes while ticks
+    run (True: half the host's cores, at most 8); False or 0 builds them
+    inside the tick."""
 
     def __init__(self, ctx: api.Context, budget_bytes: int | None = None, reserve_bytes: int = 4 << 30,
-                 max_batch: int | None = None, batched: bool = True, admission_thread: bool = True):
+                 max_batch: int | None = None, batched: bool = True, admission_thread: int | bool = True):
         self.ctx = ctx
         self.batched = batched
+        if admission_thread is True:   # default: several builders in parallel
+            import os
+            admission_thread = max(1, min(8, (os.cpu_count() or 2) // 2))
         cfg = api.od_server_config(int(budget_bytes or 0), int(reserve_bytes), int(max_batch or 0), int(batched),
                                    int(admission_thread))
         self._L = api.load_library()

@@ -137,3 +137,39 @@ def test_colour_scatter_assembly_matches_the_gather(monkeypatch):
         out[mode] = res
     for a, b in zip(out["scatter"], out["gather"]):
         assert rel_err(a, b) <= 1e-8
+
+
+def test_autotune_keeps_state_and_results(tmp_path):
+    """The autotuner re-solves the last Newton system with every candidate
+    tile shape: the scenes' state is unchanged by it, the fastest shape stays
+    set (or comes back from the cache file), and the tuned batch steps every
+    scene as the untuned one does (1e-7, both solves reach 1e-10)."""
+    tuned = [make_scene(k) for k in range(len(SPECS))]
+    plain = [make_scene(k) for k in range(len(SPECS))]
+    bt, bp = api.Batch(ctx(), tuned), api.Batch(ctx(), plain)
+    with pytest.raises(api.ODError):
+        bt.autotune()                       # nothing to tune on before a step
+    bt.step(3)
+    bp.step(3)
+    before = [(s.displacements(), *s.state()) for s in tuned]
+    cache = str(tmp_path / "tune.json")
+    rep = bt.autotune(repeats=1, cache=cache)
+    assert not rep["cached"] and rep["candidates"] == 12
+    assert rep["piece_steps"] in (12, 16, 20) and rep["slice_cost"] in (2.0, 4.0, 8.0, 16.0)
+    assert rep["best_ms"] <= rep["default_ms"]
+    assert bt.tuning() == {"piece_steps": rep["piece_steps"], "slice_cost": rep["slice_cost"]}
+    for s, b in zip(tuned, before):
+        assert all(np.array_equal(x, y) for x, y in zip((s.displacements(), *s.state()), b))
+    bt.step(4)
+    bp.step(4)
+    for k in range(len(SPECS)):
+        assert rel_err(tuned[k].displacements(), plain[k].displacements()) <= 1e-7, k
+    # a second batch of the same scenes finds the choice in the cache
+    bt.close()
+    again = api.Batch(ctx(), tuned)
+    again.step(1)
+    rep2 = again.autotune(cache=cache)
+    assert rep2["cached"] and rep2["key"] == rep["key"]
+    assert again.tuning() == {"piece_steps": rep["piece_steps"], "slice_cost": rep["slice_cost"]}
+    with pytest.raises(api.ODError):
+        again.set_tuning(14, 8.0)

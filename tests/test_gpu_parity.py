@@ -222,6 +222,24 @@ def test_persistent_and_multikernel_pcg_agree(golden, precond, monkeypatch):
 def test_mixed_precision_solve_reaches_fp64_tolerance(golden, precond):
     """FP32 inner PCG + FP64 refinement reaches the same true-residual
     tolerance as the FP64 solve and the same solution."""
+    _mixed_vs_fp64(golden, precond)
+
+
+@pytest.mark.parametrize("layout", ["lower", "full"])
+@pytest.mark.parametrize("precond", ["none", "block_jacobi"])
+def test_mixed_precision_matrix_layouts(golden, precond, layout, monkeypatch):
+    """The inner FP32 SpMV streams the lower triangle (each stored block
+    applied with its transpose, the transposed products summed by reductions)
+    by default, and both triangles with OD_GB300_MIXED_SPMV=full: the two
+    operators are the same matrix, and both solves reach the FP64 solution."""
+    if layout == "full":
+        monkeypatch.setenv("OD_GB300_MIXED_SPMV", "full")
+    else:
+        monkeypatch.delenv("OD_GB300_MIXED_SPMV", raising=False)
+    _mixed_vs_fp64(golden, precond)
+
+
+def _mixed_vs_fp64(golden, precond):
     p = golden("pattern_full")
     e = golden("elements_stvk_full")
     A = e["values"] * (1.0 / 3600.0) + e["mass"]
