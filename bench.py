@@ -395,14 +395,16 @@ def precision_tier(args, api, ctx):
     warm, steps = 2, args.tier_steps
     # mixed: the inner SpMV streams the lower triangle (transposed products by
     # reductions); mixed_full: both triangles (OD_GB300_MIXED_SPMV=full)
-    for prec in ("fp64", "mixed", "mixed_full"):
+    # mixed_ic0: the IC(0) preconditioner (FP64 factor, FP32 sweeps) in the
+    # mixed solve
+    for prec in ("fp64", "mixed", "mixed_full", "mixed_ic0"):
         if prec == "mixed_full":
             os.environ["OD_GB300_MIXED_SPMV"] = "full"
+        pc = api.IC0Preconditioner() if prec == "mixed_ic0" else api.BlockJacobiPreconditioner()
         s = api.Scene(ctx, g.X, g.tets, g.facets, cd, mat)
         s.set_displacements(u0)
         s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, 0.01, 0.001, 1 / 120,
-                                                 api.CGSolver(1e-10, 20000, api.BlockJacobiPreconditioner(),
-                                                              precision=prec.split("_")[0]), 1))
+                                                 api.CGSolver(1e-10, 20000, pc, precision=prec.split("_")[0]), 1))
         for w in range(warm):
             s.step(1)
             if w == 0:
@@ -430,6 +432,7 @@ def precision_tier(args, api, ctx):
     peak, peak_kind = peaks()
     nbytes, sms, nit, wms = res["mixed"].pop("mix")
     res["fp64"].pop("mix")
+    res["mixed_ic0"].pop("mix")
     fb, fs, fi, fw = res["mixed_full"].pop("mix")
     res["mixed_full"]["spmv_phase"] = {"bytes": fb, "ms": fw, "phases": fi,
                                        "achieved_gbs": fb / (fw * 1e-3) / 1e9 if fw else None,
@@ -463,6 +466,9 @@ def precision_tier(args, api, ctx):
             "n_tets": g.n_tets, "dofs": 3 * g.n_nodes - len(cd),
             "newton_iters": 1, "tol": 1e-10, "precond": "block_jacobi", "warmup": warm, "steps": steps,
             "fp64": res["fp64"], "mixed": res["mixed"], "mixed_full": res["mixed_full"],
+            "mixed_ic0": {**res["mixed_ic0"], "rel_err_vs_fp64": _rel(out["mixed_ic0"], out["fp64"]),
+                          "speedup_vs_fp64": res["mixed_ic0"]["steps_per_s"] / res["fp64"]["steps_per_s"],
+                          "precond": "IC(0): FP64 factor (colour order), FP32 sweeps and SpMV, multi-kernel inner PCG"},
             "speedup_mixed_vs_fp64": res["mixed"]["steps_per_s"] / res["fp64"]["steps_per_s"],
             "speedup_mixed_full_vs_fp64": res["mixed_full"]["steps_per_s"] / res["fp64"]["steps_per_s"],
             "rel_err_mixed_full_vs_fp64": _rel(out["mixed_full"], out["fp64"]),

@@ -123,6 +123,7 @@ struct Pcg {
   // solve (both built on first use)
   SliceSys* slice = nullptr;
   MixedSys* mix = nullptr;
+  struct MixIc0* mic = nullptr;  // mixed precision with IC(0) (FP32 factor copy and inner vectors)
   // incomplete LDL^T / threshold incomplete Cholesky (factor on the host,
   // triangular sweeps on the device)
   SweepSys* sweep = nullptr;
@@ -552,6 +553,17 @@ void sweep_group_levels(int n, const std::vector<int>& frp, const std::vector<in
                         const std::vector<int>& bri, std::vector<int>& ord_f, std::vector<int>& ord_b, int* depth_f,
                         int* depth_b);
 od_status sweep_launch(Scene* s, const SweepView& v, const double* r, double* z, const SolveScalars* sc);
+od_status sweep_launch_f32(Scene* s, const SweepView& v, const float* fval, const float* bval, const float* diag,
+                           const float* r, float* y, float* z, float* zperm, const SolveScalars* sc);
+// IC(0): the shifted FP64 factor of the scene's A64 (od_sparse.cu) and the
+// check of its sweeps' bounded waits
+od_status ic0_factor(Scene* s);
+od_status ic0_check(Scene* s);
+// mixed-precision solve with the IC(0) preconditioner (od_mixed_ic0.cu)
+struct MixIc0;
+void mixed_ic0_free(MixIc0* m);
+od_status mixed_ic0_solve(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm,
+                          od_solve_stats* st);
 
 // PCG on A64; b and x are device vectors of length n_pad
 od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm, od_solve_stats* st);

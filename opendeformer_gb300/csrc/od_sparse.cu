@@ -2012,10 +2012,10 @@ static od_status ic0_build(Scene* s) {
   return OD_OK;
 }
 
-static od_status ic0_check(Scene* s);
+od_status ic0_check(Scene* s);
 
 // shifted IC(0) factorisation of the current A64 with the Manteuffel retry
-static od_status ic0_factor(Scene* s) {
+od_status ic0_factor(Scene* s) {
   Pcg& P = s->pcg;
   od_status st = ic0_build(s);
   if (st != OD_OK) return st;
@@ -2098,7 +2098,7 @@ static od_status ic0_apply(Scene* s, const double* r, double* z, const SolveScal
   return sweep_launch(s, v, r, z, sc);
 }
 
-static od_status ic0_check(Scene* s) {
+od_status ic0_check(Scene* s) {
   Pcg& P = s->pcg;
   if (!P.ic_err) return OD_OK;
   cudaStream_t strm = s->ctx->stream;
@@ -2158,6 +2158,7 @@ void pcg_free(Scene* s) {
   cudaFree(P.sc);
   cudaFree(P.gbar);
   mixed_free(P.mix);
+  mixed_ic0_free(P.mic);
   slice_free(P.slice);
   sweep_free(P.sweep);
   if (P.sc_host) cudaFreeHost(P.sc_host);
@@ -2704,6 +2705,7 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
 static od_status pcg_solve_mixed(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm,
                                  od_solve_stats* st) {
   Pcg& P = s->pcg;
+  if (prm->precond == OD_PRECOND_IC0) return mixed_ic0_solve(s, d_b, d_x, prm, st);
   if (!P.mix) OD_TRY(mixed_build(s->ctx, {s}, {d_b}, {d_x}, &P.mix));
   MixedSys* m = P.mix;
   if (m->desc_host[0].b != d_b || m->desc_host[0].x != d_x) {

@@ -586,6 +586,38 @@ od_status selftest_value_wait_timeout(Ctx* c, int* timed_out) {
   return OD_OK;
 }
 
+// The IC sweeps on FP32 copies of the factor (the mixed-precision IC(0)
+// inner solve): same index arrays and dependency lists as v, FP32 values and
+// vectors, FP32 arithmetic.
+od_status sweep_launch_f32(Scene* s, const SweepView& v, const float* fval, const float* bval, const float* diag,
+                           const float* r, float* y, float* z, float* zperm, const SolveScalars* sc) {
+  Ctx* ctx = s->ctx;
+  cudaStream_t strm = ctx->stream;
+  int n = v.n, n_pad = v.n_pad, ng = (v.n + 2) / 3;
+  const int* frp = v.frp;
+  const int* fci = v.fci;
+  const int* bcp = v.bcp;
+  const int* bri = v.bri;
+  const int* of = v.ord_f;
+  const int* ob = v.ord_b;
+  int* err = v.err;
+  const int* perm = v.perm;
+  float* zflag = perm ? zperm : z;
+  float* zout = z;
+  void* args[] = {(void*)&n,    (void*)&n_pad, (void*)&ng,   (void*)&frp, (void*)&fci, (void*)&fval,
+                  (void*)&bcp,  (void*)&bri,   (void*)&bval, (void*)&of,  (void*)&ob,  (void*)&diag,
+                  (void*)&r,    (void*)&y,     (void*)&zflag, (void*)&err, (void*)&sc, (void*)&perm,
+                  (void*)&zout};
+  if (n > 0) {
+    OD_CUDA(cudaMemsetAsync(y, 0xff, sizeof(float) * (size_t)n, strm));
+    OD_CUDA(cudaMemsetAsync(zflag, 0xff, sizeof(float) * (size_t)n, strm));
+  }
+  OD_KL(s);
+  OD_CUDA(cudaLaunchCooperativeKernel((void*)sweep_apply_kernel<1, float>, dim3(v.grid), dim3(kSweepThreads), args, 0,
+                                      strm));
+  return OD_OK;
+}
+
 od_status sweep_launch(Scene* s, const SweepView& v, const double* r, double* z, const SolveScalars* sc) {
   Ctx* ctx = s->ctx;
   cudaStream_t strm = ctx->stream;

@@ -218,7 +218,7 @@ def test_persistent_and_multikernel_pcg_agree(golden, precond, monkeypatch):
     assert rel_err(x1, x0) <= 1e-8
 
 
-@pytest.mark.parametrize("precond", ["none", "jacobi", "block_jacobi"])
+@pytest.mark.parametrize("precond", ["none", "jacobi", "block_jacobi", "ic0"])
 def test_mixed_precision_solve_reaches_fp64_tolerance(golden, precond):
     """FP32 inner PCG + FP64 refinement reaches the same true-residual
     tolerance as the FP64 solve and the same solution."""
@@ -251,8 +251,11 @@ def _mixed_vs_fp64(golden, precond):
     assert rel_err(xm, x64) <= 1e-8
 
 
-@pytest.mark.parametrize("kind", ["neohookean", "stvk"])
-def test_mixed_precision_newmark_within_1e6_of_fp64(kind):
+@pytest.mark.parametrize("kind,precond", [("neohookean", "block_jacobi"), ("stvk", "block_jacobi"),
+                                           ("neohookean", "ic0")])
+def test_mixed_precision_newmark_within_1e6_of_fp64(kind, precond):
+    """20 Newmark steps (3 Newton iterations each) with the mixed solver stay
+    within 1e-6 of the FP64 solver; IC(0) mixed = FP64 factor, FP32 sweeps."""
     g = meshgen.tet_grid(12, 4, 4, h=0.05, jitter=0.15, seed=2)
     cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
     mat = material(kind, 1000.0, 98640.0, 0.4506, 0.1)
@@ -260,7 +263,7 @@ def test_mixed_precision_newmark_within_1e6_of_fp64(kind):
     for prec in ("fp64", "mixed"):
         s = api.Scene(ctx(), g.X, g.tets, g.facets, cd, mat)
         s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, 0.01, 0.001, 1 / 120,
-                                                 api.CGSolver(1e-10, 3000, api.BlockJacobiPreconditioner(),
+                                                 api.CGSolver(1e-10, 3000, api.Preconditioner(precond),
                                                               precision=prec), 3))
         s.set_loads(tractions=[([0.0, -500.0, 0.0], g.face_facets(0, 1))])
         s.set_traction_schedule(2.0)
