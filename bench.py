@@ -397,7 +397,8 @@ def precision_tier(args, api, ctx):
     # reductions); mixed_full: both triangles (OD_GB300_MIXED_SPMV=full)
     # mixed_ic0: the IC(0) preconditioner (FP64 factor, FP32 sweeps) in the
     # mixed solve
-    for prec in ("fp64", "mixed", "mixed_full", "mixed_ic0"):
+    variants = [v for v in args.precision_variants.split(",") if v]
+    for prec in variants:
         if prec == "mixed_full":
             os.environ["OD_GB300_MIXED_SPMV"] = "full"
         pc = api.IC0Preconditioner() if prec == "mixed_ic0" else api.BlockJacobiPreconditioner()
@@ -430,13 +431,17 @@ def precision_tier(args, api, ctx):
         s.close()
         del s
     peak, peak_kind = peaks()
+    if not {"fp64", "mixed"} <= set(res):
+        return {"workload": f"block128x64x{nz}_nh_prescribed_newmark", "variants": res}
     nbytes, sms, nit, wms = res["mixed"].pop("mix")
     res["fp64"].pop("mix")
-    res["mixed_ic0"].pop("mix")
-    fb, fs, fi, fw = res["mixed_full"].pop("mix")
-    res["mixed_full"]["spmv_phase"] = {"bytes": fb, "ms": fw, "phases": fi,
-                                       "achieved_gbs": fb / (fw * 1e-3) / 1e9 if fw else None,
-                                       "us_per_phase_with_sum": 1000.0 * fs / max(1, fi)}
+    if "mixed_ic0" in res:
+        res["mixed_ic0"].pop("mix")
+    if "mixed_full" in res:
+        fb, fs, fi, fw = res["mixed_full"].pop("mix")
+        res["mixed_full"]["spmv_phase"] = {"bytes": fb, "ms": fw, "phases": fi,
+                                           "achieved_gbs": fb / (fw * 1e-3) / 1e9 if fw else None,
+                                           "us_per_phase_with_sum": 1000.0 * fs / max(1, fi)}
     spmv_gbs = nbytes / (wms * 1e-3) / 1e9 if wms else None
     phase_gbs = nbytes / (sms * 1e-3) / 1e9 if sms else None
     oracle = None
@@ -465,13 +470,15 @@ def precision_tier(args, api, ctx):
     return {"workload": "block2m6_nh_prescribed_newmark" if nz == 64 else f"block128x64x{nz}_nh_prescribed_newmark",
             "n_tets": g.n_tets, "dofs": 3 * g.n_nodes - len(cd),
             "newton_iters": 1, "tol": 1e-10, "precond": "block_jacobi", "warmup": warm, "steps": steps,
-            "fp64": res["fp64"], "mixed": res["mixed"], "mixed_full": res["mixed_full"],
+            "fp64": res["fp64"], "mixed": res["mixed"], "mixed_full": res.get("mixed_full"),
             "mixed_ic0": {**res["mixed_ic0"], "rel_err_vs_fp64": _rel(out["mixed_ic0"], out["fp64"]),
                           "speedup_vs_fp64": res["mixed_ic0"]["steps_per_s"] / res["fp64"]["steps_per_s"],
-                          "precond": "IC(0): FP64 factor (colour order), FP32 sweeps and SpMV, multi-kernel inner PCG"},
+                          "precond": "IC(0): FP64 factor (colour order), FP32 sweeps and SpMV, multi-kernel inner PCG"}
+            if "mixed_ic0" in res else None,
             "speedup_mixed_vs_fp64": res["mixed"]["steps_per_s"] / res["fp64"]["steps_per_s"],
-            "speedup_mixed_full_vs_fp64": res["mixed_full"]["steps_per_s"] / res["fp64"]["steps_per_s"],
-            "rel_err_mixed_full_vs_fp64": _rel(out["mixed_full"], out["fp64"]),
+            "speedup_mixed_full_vs_fp64": res["mixed_full"]["steps_per_s"] / res["fp64"]["steps_per_s"]
+            if "mixed_full" in res else None,
+            "rel_err_mixed_full_vs_fp64": _rel(out["mixed_full"], out["fp64"]) if "mixed_full" in res else None,
             "rel_err_mixed_vs_fp64": _rel(out["mixed"], out["fp64"]),
             "oracle": oracle,
             "spmv_roofline": {"kernel": "pcg32_ring_kernel SpMV phase (sliced FP32 matrix streamed by "
@@ -1222,6 +1229,8 @@ def main():
     ap.add_argument("--only-tiers", default="", help="comma list of precision,batched,serving,sweep,ic0,relabel (default: all)")
     ap.add_argument("--precision-nz", type=int, default=64,
                     help="cube layers of the precision-tier block (64: 2,621,440 tets)")
+    ap.add_argument("--precision-variants", default="fp64,mixed,mixed_full,mixed_ic0",
+                    help="comma list of the precision tier's solvers (fp64, mixed, mixed_full, mixed_ic0)")
     ap.add_argument("--serving-pool", type=int, default=512)
     ap.add_argument("--serving-rate", type=float, default=2000.0)
     ap.add_argument("--serving-seconds", type=float, default=15.0)

@@ -523,8 +523,8 @@ static od_status check_solver(const od_solver_params* p) {
   OD_CHECK_ARG(p->tol >= 0.0 && p->max_iter >= 0, "solver tolerance / max_iter out of range");
   OD_CHECK_ARG(p->precond >= 0 && p->precond <= OD_PRECOND_IC, "unknown preconditioner");
   OD_CHECK_ARG(p->precision == OD_PRECISION_FP64 || p->precision == OD_PRECISION_MIXED, "unknown precision");
-  OD_CHECK_ARG(p->precision == OD_PRECISION_FP64 || p->precond < OD_PRECOND_IC0,
-               "mixed precision supports the none, Jacobi and block-Jacobi preconditioners");
+  OD_CHECK_ARG(p->precision == OD_PRECISION_FP64 || p->precond <= OD_PRECOND_IC0,
+               "mixed precision supports the none, Jacobi, block-Jacobi and IC(0) preconditioners");
   OD_CHECK_ARG(p->sainv_eps >= 0.0 && p->ldlt_eps >= 0.0 && std::isfinite(p->sainv_eps) &&
                    std::isfinite(p->ldlt_eps),
                "LDL^T drop bounds must be finite and >= 0");

@@ -333,6 +333,8 @@ extern "C" od_status od_batch_create(od_ctx* ctx, int n_scenes, od_scene* const*
     if (s->ctx != B->ctx) why = "a scene belongs to another context";
     else if (!s->has_integrator || s->ip.kind != OD_INTEGRATOR_NEWMARK) why = "every scene needs a Newmark integrator";
     else if (s->ip.solver.precision != OD_PRECISION_MIXED) why = "every scene needs the mixed-precision solver";
+    else if (s->ip.solver.precond >= OD_PRECOND_IC0)
+      why = "batched scenes use the none, Jacobi or block-Jacobi preconditioner (mixed IC(0) steps alone)";
     else if (s->has_damping) why = "scenes with external damping cannot be batched";
     else if (i > 0 && s->ip.newton_iters != B->sc[0]->ip.newton_iters) why = "scenes differ in Newton iterations";
     else if (i > 0 && s->ip.solver.precond != B->sc[0]->ip.solver.precond) why = "scenes differ in preconditioner";

@@ -2572,7 +2572,8 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
   const int n_sc = m->n_sc;
   st.assign(n_sc, od_solve_stats{});
   if (pk < 0 || pk >= OD_PRECOND_IC0) {
-    set_error("mixed precision supports the none, Jacobi and block-Jacobi preconditioners");
+    set_error("the multi-scene mixed solve supports the none, Jacobi and block-Jacobi preconditioners "
+              "(mixed IC(0) solves one scene at a time)");
     return OD_ERR_UNSUPPORTED;
   }
   if (m->fill_dir.tiles > 0) {

@@ -100,6 +100,8 @@ def test_batch_rejects_what_it_cannot_batch():
         api.Batch(ctx(), [make_scene(0, newton=1), make_scene(1, newton=2)])
     with pytest.raises(RuntimeError):
         api.Batch(ctx(), [make_scene(0), make_scene(1, precond="jacobi")])
+    with pytest.raises(RuntimeError):   # mixed IC(0) steps scene by scene
+        api.Batch(ctx(), [make_scene(0, precond="ic0"), make_scene(1, precond="ic0")])
     s = make_scene(0)
     with pytest.raises(RuntimeError):
         api.Batch(ctx(), [s, s])
