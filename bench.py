@@ -774,8 +774,9 @@ def batched_tier(args, api, ctx):
     err = max(_rel(a, c) for a, c in zip(ub, u64))
     # autotuner (tile shapes of the inner solve), then steps with the tuned
     # shapes between two runs of steps with the defaults
+    default_shape = b.tuning()
     tune = b.autotune(repeats=1)
-    tuned = {"choice": {k: tune[k] for k in ("piece_steps", "slice_cost")},
+    tuned = {"choice": {k: tune[k] for k in ("piece_steps", "consumer_warps", "slice_cost")},
              "solve_ms_default": tune.get("default_ms"), "solve_ms_tuned": tune.get("best_ms"),
              "candidates": tune.get("candidates"), "key": tune["key"]}
     def timed(n):
@@ -787,9 +788,9 @@ def batched_tier(args, api, ctx):
             out.append(st[0].device_ms)
         return statistics.mean(out)
     t_tuned = timed(steps)
-    b.set_tuning(20, 8.0)
+    b.set_tuning(default_shape["piece_steps"], default_shape["slice_cost"], default_shape["consumer_warps"])
     t_default = timed(steps)
-    tuned.update({"ms_per_step_tuned": t_tuned, "ms_per_step_default_after": t_default,
+    tuned.update({"default": default_shape, "ms_per_step_tuned": t_tuned, "ms_per_step_default_after": t_default,
                   "ms_per_step_default_before": statistics.mean(lat),
                   "gain": 0.5 * (t_default + statistics.mean(lat)) / t_tuned})
     n_tets = sum(s.n_tets for s in scenes)

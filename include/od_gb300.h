@@ -362,10 +362,14 @@ od_status od_batch_step(od_batch* batch, int n_steps, od_step_stats* stats);
 od_status od_batch_destroy(od_batch* batch);
 /* Tile shapes of a batch's inner FP32 solve (no reference counterpart):
  * the ring kernel's piece size (matrix steps per bulk copy into shared
- * memory: 12, 16 or 20; default 20) and the per-slice fixed cost, in steps,
- * that weights the partition of the slices over the CTAs (default 8). */
+ * memory: 12, 16 or 20), its consumer warps per CTA (12, or 15 with pieces of
+ * 12 or 16 steps) -- by default 12 and 15 for the lower-triangle matrix, 20
+ * and 12 for both triangles -- and the per-slice fixed cost, in steps, that
+ * weights the partition of the slices over the CTAs (default 8).  The
+ * report's default_ms is the solve with the shape set before tuning. */
 typedef struct od_mixed_tuning {
   int piece_steps;
+  int consumer_warps;
   double slice_cost;
 } od_mixed_tuning;
 typedef struct od_tune_report {
@@ -377,9 +381,9 @@ typedef struct od_tune_report {
 od_status od_batch_get_tuning(od_batch* batch, od_mixed_tuning* out);
 od_status od_batch_set_tuning(od_batch* batch, const od_mixed_tuning* tuning);
 /* Autotuner: after at least one od_batch_step, solves the batch's last
- * Newton system again with every candidate shape (3 piece sizes x slice
- * costs 2, 4, 8, 16), each timed with CUDA events (best of repeats), and
- * keeps the fastest.  Scene state is not changed. */
+ * Newton system again with every candidate shape (5 piece-size / consumer-
+ * warp pairs x slice costs 2, 4, 8, 16), each timed with CUDA events (best of
+ * repeats), and keeps the fastest.  Scene state is not changed. */
 od_status od_batch_autotune(od_batch* batch, int repeats, od_tune_report* report);
 
 /* ---- serving: step requests over a pool of scenes.  No reference

@@ -100,7 +100,7 @@ class od_scene_info(C.Structure):
 
 
 class od_mixed_tuning(C.Structure):
-    _fields_ = [("piece_steps", C.c_int), ("slice_cost", C.c_double)]
+    _fields_ = [("piece_steps", C.c_int), ("consumer_warps", C.c_int), ("slice_cost", C.c_double)]
 
 
 class od_tune_report(C.Structure):
@@ -746,10 +746,10 @@ class Batch:
     def tuning(self) -> dict:
         t = od_mixed_tuning()
         _check(load_library().od_batch_get_tuning(self.h, C.byref(t)), "od_batch_get_tuning")
-        return {"piece_steps": t.piece_steps, "slice_cost": t.slice_cost}
+        return {"piece_steps": t.piece_steps, "consumer_warps": t.consumer_warps, "slice_cost": t.slice_cost}
 
-    def set_tuning(self, piece_steps: int, slice_cost: float):
-        t = od_mixed_tuning(int(piece_steps), float(slice_cost))
+    def set_tuning(self, piece_steps: int, slice_cost: float, consumer_warps: int = 12):
+        t = od_mixed_tuning(int(piece_steps), int(consumer_warps), float(slice_cost))
         _check(load_library().od_batch_set_tuning(self.h, C.byref(t)), "od_batch_set_tuning")
 
     def tuning_key(self) -> str:
@@ -774,7 +774,7 @@ class Batch:
 
     def autotune(self, repeats: int = 1, cache: str | None = None) -> dict:
         """od_batch_autotune: picks the inner solve's tile shapes (ring-kernel
-        piece size, partition slice cost) by timing the batch's last Newton
+        piece size and consumer warps, partition slice cost) by timing the batch's last Newton
         system with every candidate; the batch must have been stepped once.
         With a cache file (JSON; default $OD_GB300_TUNE_CACHE when set) a
         choice made before for the same device and mesh class is reused."""
@@ -786,11 +786,12 @@ class Batch:
             with open(cache) as f:
                 table = json.load(f)
         if key in table:
-            self.set_tuning(table[key]["piece_steps"], table[key]["slice_cost"])
+            self.set_tuning(table[key]["piece_steps"], table[key]["slice_cost"], table[key]["consumer_warps"])
             return {"key": key, "cached": True, **table[key]}
         rep = od_tune_report()
         _check(load_library().od_batch_autotune(self.h, int(repeats), C.byref(rep)), "od_batch_autotune")
-        out = {"piece_steps": rep.best.piece_steps, "slice_cost": rep.best.slice_cost,
+        out = {"piece_steps": rep.best.piece_steps, "consumer_warps": rep.best.consumer_warps,
+               "slice_cost": rep.best.slice_cost,
                "candidates": rep.candidates, "default_ms": rep.default_ms, "best_ms": rep.best_ms,
                "default_iters": rep.default_iters, "best_iters": rep.best_iters}
         if cache:

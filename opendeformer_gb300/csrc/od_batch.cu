@@ -249,7 +249,8 @@ static od_status batch_step(Batch* B, std::vector<od_step_stats>& acc) {
 
 // Autotuner of the inner solve's tile shapes: the last Newton system of the
 // batch (matrices and right-hand sides still on the device) is solved again
-// with every candidate -- ring-kernel piece size x partition slice cost --
+// with every candidate -- ring-kernel piece size and consumer warps x
+// partition slice cost --
 // from a zero correction, each timed with CUDA events on the context stream
 // (best of `repeats`); the scenes' state is not touched (the corrections
 // are scratch between steps) and the scenes' iteration history, which
@@ -263,14 +264,16 @@ static od_status batch_autotune(Batch* B, int repeats, od_tune_report* rep) {
   auto restore = [&] {
     for (size_t i = 0; i < B->sc.size(); i++) B->sc[i]->mix_iters_last = hist[i];
   };
-  const int pieces[3] = {12, 16, 20};
+  const int shapes[5][2] = {{12, 12}, {16, 12}, {20, 12}, {12, 15}, {16, 15}};   // piece steps, consumer warps
   const double costs[4] = {2.0, 4.0, 8.0, 16.0};
+  const int def_ps = m->piece_steps, def_nw = m->ring_warps;   // the shape set before tuning
+  const double def_cost = m->slice_cost;
   od_tune_report r{};
   r.best_ms = 1e300;
   std::vector<od_solve_stats> ss;
-  for (int pi = 0; pi < 3; pi++)
+  for (int pi = 0; pi < 5; pi++)
     for (int ci = 0; ci < 4; ci++) {
-      OD_TRY(mixed_retune(m, pieces[pi], costs[ci]));
+      OD_TRY(mixed_retune(m, shapes[pi][0], shapes[pi][1], costs[ci]));
       float best = 1e30f;
       int iters = 0;
       for (int rr = 0; rr < std::max(1, repeats); rr++) {
@@ -287,19 +290,20 @@ static od_status batch_autotune(Batch* B, int repeats, od_tune_report* rep) {
         for (const od_solve_stats& x : ss) iters += x.iterations;
       }
       r.candidates++;
-      if (pieces[pi] == 20 && costs[ci] == 8.0) {
+      if (shapes[pi][0] == def_ps && shapes[pi][1] == def_nw && costs[ci] == def_cost) {
         r.default_ms = best;
         r.default_iters = iters;
       }
       if (best < r.best_ms) {
         r.best_ms = best;
         r.best_iters = iters;
-        r.best.piece_steps = pieces[pi];
+        r.best.piece_steps = shapes[pi][0];
+        r.best.consumer_warps = shapes[pi][1];
         r.best.slice_cost = costs[ci];
       }
     }
   OD_TRY(nm_op(B, NM_ZERO_DV));
-  OD_TRY(mixed_retune(m, r.best.piece_steps, r.best.slice_cost));
+  OD_TRY(mixed_retune(m, r.best.piece_steps, r.best.consumer_warps, r.best.slice_cost));
   if (rep) *rep = r;
   return OD_OK;
 }
@@ -372,6 +376,7 @@ extern "C" od_status od_batch_destroy(od_batch* batch) {
 extern "C" od_status od_batch_get_tuning(od_batch* batch, od_mixed_tuning* out) {
   OD_BATCH_ARG(batch && out, "od_batch_get_tuning: NULL argument");
   out->piece_steps = batch->b->mix->piece_steps;
+  out->consumer_warps = batch->b->mix->ring_warps;
   out->slice_cost = batch->b->mix->slice_cost;
   return OD_OK;
 }
@@ -379,7 +384,7 @@ extern "C" od_status od_batch_get_tuning(od_batch* batch, od_mixed_tuning* out) 
 extern "C" od_status od_batch_set_tuning(od_batch* batch, const od_mixed_tuning* t) {
   OD_BATCH_ARG(batch && t, "od_batch_set_tuning: NULL argument");
   OD_CUDA(cudaSetDevice(batch->b->ctx->device));
-  return mixed_retune(batch->b->mix, t->piece_steps, t->slice_cost);
+  return mixed_retune(batch->b->mix, t->piece_steps, t->consumer_warps, t->slice_cost);
 }
 
 extern "C" od_status od_batch_autotune(od_batch* batch, int repeats, od_tune_report* report) {

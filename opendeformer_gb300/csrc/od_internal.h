@@ -114,6 +114,8 @@ struct Pcg {
   int ic_colours = 0;           // colours (0: natural order)
   int* ic_pdof = nullptr;       // factor DOF -> the system's DOF (colour order only)
   double* ic_zp = nullptr;      // the backward sweep's values in factor order
+  std::vector<int> ic_cstart;   // first factor block of each colour (colour order)
+  bool ic_by_colour = false;    // sweeps one launch per colour (colours much larger than the sweep grid)
   // persistent (cooperative) solve
   void* gbar = nullptr;         // grid barrier state
   int* timeout_host = nullptr;  // pinned
@@ -265,11 +267,12 @@ struct MixedSys {
   unsigned long long* cta_ns_host = nullptr;  // G (pinned)
   int rebalances = 0;
   // tile shapes (the batch autotuner's choice, else the defaults)
-  int piece_steps = 20;            // ring-kernel steps per bulk copy (12, 16 or 20)
+  int piece_steps = 20;            // ring-kernel steps per bulk copy (12, 16 or 20; lower storage: 12)
+  int ring_warps = 12;             // consumer warps per CTA (12, or 15 with 12- or 16-step pieces; lower: 15)
   double slice_cost = 8.0;         // a slice's fixed cost in steps, for the CTA partition
 };
-bool ring_piece_supported(int ps);
-od_status mixed_retune(MixedSys* m, int piece_steps, double slice_cost);
+bool ring_shape_supported(int ps, int nw);
+od_status mixed_retune(MixedSys* m, int piece_steps, int ring_warps, double slice_cost);
 
 struct Ctx {
   int device = 0;
@@ -547,6 +550,9 @@ struct SweepView {
   // ready flags) and also write every value to the caller's z at perm[]
   const int* perm = nullptr;
   double* zperm = nullptr;
+  // colour order with colours far larger than the one-launch sweep's warps:
+  // first triple of each colour (the sweeps then go one launch per colour)
+  const std::vector<int>* colour_start = nullptr;
 };
 od_status sweep_grid(Scene* s, int n, int* grid);
 void sweep_group_levels(int n, const std::vector<int>& frp, const std::vector<int>& fci, const std::vector<int>& bcp,

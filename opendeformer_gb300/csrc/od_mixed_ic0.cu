@@ -297,6 +297,7 @@ od_status mixed_ic0_solve(Scene* s, const double* d_b, double* d_x, const od_sol
   v.ord_b = P.ic_gord_b;
   v.err = P.ic_err;
   v.perm = P.ic_pdof;
+  if (P.ic_by_colour) v.colour_start = &P.ic_cstart;
   const double inner_tol = prm->inner_tol > 0.0 ? prm->inner_tol : 1e-4;
   const int max_refine = prm->max_refine > 0 ? prm->max_refine : 20;
   double* part_a = m->part;           // p.q

@@ -836,7 +836,7 @@ __global__ void mix_update_kernel(int n_sc, const int* __restrict__ prefix, cons
 
 // ---- bulk-copy ring of the inner FP32 PCG
 // Every CTA owns a contiguous range of slices (of one or more scenes);
-// consumer warp w of the CTA takes slices first + w, first + w + kRingWarps,
+// consumer warp w of the CTA takes slices first + w, first + w + NW,
 // ...  Producer lane w (of the CTA's last warp) streams warp w's slices, cut
 // into pieces of at most PS steps (a template parameter), from global memory into a private
 // two-stage ring in shared memory with cp.async.bulk (evict-first in L2, so
@@ -848,16 +848,17 @@ __global__ void mix_update_kernel(int n_sc, const int* __restrict__ prefix, cons
 // (the stage is signalled without data): the producer reads the per-scene
 // activity the consumers publish, and may only see it late (it then copies
 // data the consumers skip), never early.
-constexpr int kRingWarps = 12;                       // consumer warps per CTA
-constexpr int kRingThreads = 32 * (kRingWarps + 1);  // + the producer warp
-constexpr int kRingConsumers = 32 * kRingWarps;
+// consumer warps per CTA: a template parameter (12 or 15; with the producer
+// warp and 128 registers a thread, 15 fill the register file)
+constexpr int kRingWarpsMax = 15;
+constexpr int kRingWarpsDefault = 12;
 // Steps per piece (even; a tile shape the batch autotuner picks): each
 // stage holds a piece's values (90 floats per step) then its columns (10
 // ints per step); two stages per consumer warp plus the mbarriers.
 constexpr int kRingStepsDefault = 20;
 __host__ __device__ constexpr int ring_stage_bytes(int ps) { return ps * 400; }
-__host__ __device__ constexpr int ring_smem_bytes(int ps) {
-  return kRingWarps * 2 * ring_stage_bytes(ps) + kRingWarps * 2 * 2 * 8;
+__host__ __device__ constexpr int ring_smem_bytes(int ps, int nw) {
+  return nw * 2 * ring_stage_bytes(ps) + nw * 2 * 2 * 8;
 }
 constexpr unsigned long long kMbarSpinLimit = 1ull << 24;
 
@@ -907,9 +908,9 @@ __device__ __forceinline__ void named_sync() {
 
 // Shared state of one CTA of the ring kernel for the scenes it spans.
 struct RingShared {
-  double ws[3][kMaxLocalScenes][kRingWarps];  // per-warp partials
+  double ws[3][kMaxLocalScenes][kRingWarpsMax];  // per-warp partials
   double res[3][kMaxLocalScenes];             // scene sums of the last reduction
-  double wg[kRingWarps];
+  double wg[kRingWarpsMax];
   double g;                                   // grid-wide sum of the last reduction
   double rz[kMaxLocalScenes], rr[kMaxLocalScenes], eps[kMaxLocalScenes];
   double alpha[kMaxLocalScenes], beta[kMaxLocalScenes];   // step lengths of the current iteration
@@ -938,7 +939,7 @@ __device__ __forceinline__ int local_scene(const RingShared& sh, int sl, int& ls
 // scenes over the scene's CTA range in a fixed order (bitwise the same in
 // every CTA; entries of CTAs without the scene stay zero); gval is summed
 // over all CTAs.  Consumers only.
-template <int NV>
+template <int NV, int NW>
 __device__ __forceinline__ bool ring_sums(RingShared& sh, int L, int sc_lo, int n_sc, double gval,
                                           double* __restrict__ part, double* __restrict__ part_g, GridBarrier* gb,
                                           unsigned long long* __restrict__ stamp = nullptr,
@@ -946,7 +947,7 @@ __device__ __forceinline__ bool ring_sums(RingShared& sh, int L, int sc_lo, int 
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int G = gridDim.x, b = blockIdx.x;
   if (lane == 0) sh.wg[w] = gval;
-  named_sync<kRingConsumers>();
+  named_sync<32 * NW>();
   if (work_ns && threadIdx.x == 0) {  // this CTA's share of the phase (its own slot)
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -962,13 +963,13 @@ __device__ __forceinline__ bool ring_sums(RingShared& sh, int L, int sc_lo, int 
 #pragma unroll
       for (int j = 0; j < NV; j++) {
         double t = 0.0;
-        for (int k = 0; k < kRingWarps; k++) t += sh.ws[j][lane][k];
+        for (int k = 0; k < NW; k++) t += sh.ws[j][lane][k];
         part[((size_t)j * n_sc + sc_lo + lane) * G + b] = t;
       }
     }
     if (lane == 0) {
       double t = 0.0;
-      for (int k = 0; k < kRingWarps; k++) t += sh.wg[k];
+      for (int k = 0; k < NW; k++) t += sh.wg[k];
       part_g[b] = t;
     }
     __threadfence();
@@ -1003,7 +1004,7 @@ __device__ __forceinline__ bool ring_sums(RingShared& sh, int L, int sc_lo, int 
       sh.ok = ok;
     }
   }
-  named_sync<kRingConsumers>();
+  named_sync<32 * NW>();
   return sh.ok != 0;
 }
 
@@ -1017,7 +1018,7 @@ __device__ __forceinline__ bool grid_barrier_named(GridBarrier* gb) {
 }
 
 // Inner FP32 PCG of every scene of a sliced system, one cooperative launch
-// of kRingThreads per CTA: scene s solves A32 d = rhs_scale * r64 from d = 0
+// of 32 (NW + 1) threads per CTA: scene s solves A32 d = rhs_scale * r64 from d = 0
 // until ||r_inner|| <= inner_tol ||r_0|| or max_iter, each scene with its own
 // step lengths; the loop runs while any scene is active.  Slices are
 // numbered through the scenes (scene s owns [slice0, slice0 + ns)); every
@@ -1025,15 +1026,15 @@ __device__ __forceinline__ bool grid_barrier_named(GridBarrier* gb) {
 // slice element 30*slice + l, i.e. component l%3 of slice row l/3 (lanes
 // 30, 31 shadow lane 29 and store nothing).  Dot products accumulate in
 // compensated FP32 per lane and are summed in FP64.
-template <int PS>
-__global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
+template <int PS, int NW>
+__global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
     int n_sc, const int* __restrict__ cta_first, const int* __restrict__ cta_sc_lo, const int* __restrict__ sc_cta,
     const int* __restrict__ sc_slice, const MixDesc* __restrict__ desc, RingScene* __restrict__ ring, int pkind,
     double* __restrict__ part, GridBarrier* gb, unsigned long long* __restrict__ prof,
     unsigned long long* __restrict__ cta_ns) {
   extern __shared__ __align__(128) unsigned char ring_smem[];
-  unsigned long long* full = reinterpret_cast<unsigned long long*>(ring_smem + kRingWarps * 2 * ring_stage_bytes(PS));
-  unsigned long long* empty = full + 2 * kRingWarps;
+  unsigned long long* full = reinterpret_cast<unsigned long long*>(ring_smem + NW * 2 * ring_stage_bytes(PS));
+  unsigned long long* empty = full + 2 * NW;
   __shared__ RingShared sh;
   const int G = gridDim.x;
   const int lane = threadIdx.x & 31;
@@ -1055,7 +1056,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
     sh.stop = 0;
     sh.pub = -1;
   }
-  if (threadIdx.x < 2 * kRingWarps) {
+  if (threadIdx.x < 2 * NW) {
     mbar_init(full + threadIdx.x, 1);
     mbar_init(empty + threadIdx.x, 1);
   }
@@ -1076,10 +1077,10 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   __syncthreads();
 
-  if (w == kRingWarps) {
+  if (w == NW) {
     // ---------------- producer: lane pw feeds consumer warp pw
     const int pw = lane;
-    if (pw >= kRingWarps || sfirst + pw >= send) return;
+    if (pw >= NW || sfirst + pw >= send) return;
     unsigned long long policy;
     asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(policy));
     unsigned pc = 0;  // pieces issued
@@ -1097,7 +1098,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
         if (sh.pub < kit - 1) break;
       }
       int ls = 0;
-      for (int sl = sfirst + pw; sl < send && ok; sl += kRingWarps) {
+      for (int sl = sfirst + pw; sl < send && ok; sl += NW) {
         local_scene(sh, sl, ls);
         // pieces of iteration kit exist for the scenes active in iteration
         // kit - 1 (published before the consumers start iteration kit - 1,
@@ -1162,10 +1163,10 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
   unsigned pc = 0;  // pieces consumed
   bool alive = true;
 
-  // a warp's slices of local scene ls: first_slice(ls), + kRingWarps, ... < lfirst[ls + 1]
+  // a warp's slices of local scene ls: first_slice(ls), + NW, ... < lfirst[ls + 1]
   auto first_slice = [&](int ls) {
     const int dlt = sh.lfirst[ls] - sfirst - w;
-    return dlt <= 0 ? sfirst + w : sfirst + w + ((dlt + kRingWarps - 1) / kRingWarps) * kRingWarps;
+    return dlt <= 0 ? sfirst + w : sfirst + w + ((dlt + NW - 1) / NW) * NW;
   };
   auto zero_ws = [&](int nv) {
     if (lane < L)
@@ -1209,7 +1210,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
     const int* __restrict__ perm = sh.lp[ls].sperm;
     const double* __restrict__ r64 = sh.lp[ls].r64;
     Comp cru{0.f, 0.f}, crr{0.f, 0.f};
-    for (int sl = first_slice(ls); sl < sh.lfirst[ls + 1]; sl += kRingWarps) {
+    for (int sl = first_slice(ls); sl < sh.lfirst[ls + 1]; sl += NW) {
       const int lsl = sl - V.s0;
       const int rs = lsl * kSliceRows + t;
       const int row = perm[rs];
@@ -1245,7 +1246,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
   __threadfence_block();
   if (threadIdx.x == 0) sh.pub = 0;   // act[0] (= the launch's activity) is final
   // u complete everywhere before the first gathers
-  if (!grid_barrier_named<kRingConsumers>(gb)) alive = false;
+  if (!grid_barrier_named<(32 * NW)>(gb)) alive = false;
 
   // profiling (prof != nullptr): CTA 0 times each SpMV + sum phase up to the
   // end of its grid-wide sum, i.e. including the slowest CTA
@@ -1264,7 +1265,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
         const Vecs V = vecs(ls);
         const int* __restrict__ soff = sh.lp[ls].soff;
         Comp cwu{0.f, 0.f};
-        for (int sl = first_slice(ls); sl < sh.lfirst[ls + 1] && alive; sl += kRingWarps) {
+        for (int sl = first_slice(ls); sl < sh.lfirst[ls + 1] && alive; sl += NW) {
           const int lsl = sl - V.s0;
           const int k1 = soff[lsl + 1];
           float y0 = 0.f, y1 = 0.f, y2 = 0.f;  // partial rows 0, 1, 2 of block row t
@@ -1351,7 +1352,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
       double na = 0.0;
       if (w == 0 && lane == 0)
         for (int ls = 0; ls < L; ls++) na += sh.act[kp][ls] ? 1.0 : 0.0;
-      if (!ring_sums<3>(sh, L, sc_lo, n_sc, na, part_3, part_g, gb, prof ? prof + 3 : nullptr, cta_ns))
+      if (!ring_sums<3, NW>(sh, L, sc_lo, n_sc, na, part_3, part_g, gb, prof ? prof + 3 : nullptr, cta_ns))
         alive = false;
     }
     if (!alive || sh.g == 0.0) break;
@@ -1389,7 +1390,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
       sh.act[kp ^ 1][ls] = na;
     }
     __threadfence_block();
-    named_sync<kRingConsumers>();
+    named_sync<(32 * NW)>();
     if (threadIdx.x == 0) sh.pub = k + 1;
     // ---- p = u + beta p, s = w + beta s, d += alpha p, r -= alpha s,
     // u = M^-1 r, (r, u), (r, r): kUB slices per batch, all loads of a batch
@@ -1404,11 +1405,11 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
       float* w4f = reinterpret_cast<float*>(V.w4);
       const float alpha = (float)sh.alpha[ls], beta = (float)sh.beta[ls];
       Comp cru{0.f, 0.f}, crr{0.f, 0.f};
-      for (int sl0 = first_slice(ls); sl0 < hi; sl0 += kUB * kRingWarps) {
+      for (int sl0 = first_slice(ls); sl0 < hi; sl0 += kUB * NW) {
         float dv[kUB], pv[kUB], sv[kUB], uv[kUB], wv[kUB], rv[kUB], m0[kUB], m1[kUB], m2[kUB];
 #pragma unroll
         for (int u = 0; u < kUB; u++) {
-          const int sl = sl0 + u * kRingWarps;
+          const int sl = sl0 + u * NW;
           if (sl < hi) {
             const int lsl = sl - V.s0;
             const size_t i = (size_t)30 * lsl + ln;
@@ -1431,7 +1432,7 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
         }
 #pragma unroll
         for (int u = 0; u < kUB; u++) {
-          const int sl = sl0 + u * kRingWarps;
+          const int sl = sl0 + u * NW;
           if (sl < hi) {  // warp-uniform
             const int lsl = sl - V.s0;
             const size_t i = (size_t)30 * lsl + ln;
@@ -1462,9 +1463,9 @@ __global__ void __launch_bounds__(kRingThreads, 1) pcg32_ring_kernel(
     }
     // u complete everywhere before the next gathers (also keeps this
     // iteration's sums from being overwritten before every CTA read them)
-    if (!grid_barrier_named<kRingConsumers>(gb)) { alive = false; break; }
+    if (!grid_barrier_named<(32 * NW)>(gb)) { alive = false; break; }
   }
-  named_sync<kRingConsumers>();
+  named_sync<(32 * NW)>();
   if (threadIdx.x == 0) sh.stop = 1;
   if (alive && w == 0 && lane < L) {
     const int s = sc_lo + lane;
@@ -1807,7 +1808,8 @@ od_status launch_spmv_full(Scene* s, const double* x, double* y) {
 // block), blocks visited in index order, each taking the lowest colour no
 // coloured neighbour has; order[] lists the blocks by colour, then index.
 // Returns the number of colours.  The oracle's IC(0) orders the same way.
-static int ic0_colour_order(int nb, const std::vector<int>& rp, const std::vector<int>& col, std::vector<int>& order) {
+static int ic0_colour_order(int nb, const std::vector<int>& rp, const std::vector<int>& col, std::vector<int>& order,
+                            std::vector<int>& start_out) {
   std::vector<int> colour(nb, -1), mark;
   int nc = 0;
   for (int b = 0; b < nb; b++) {
@@ -1826,6 +1828,7 @@ static int ic0_colour_order(int nb, const std::vector<int>& rp, const std::vecto
   std::vector<int> start(nc + 1, 0);
   for (int b = 0; b < nb; b++) start[colour[b] + 1]++;
   for (int c = 0; c < nc; c++) start[c + 1] += start[c];
+  start_out.assign(start.begin(), start.end());
   order.assign(nb, 0);
   for (int b = 0; b < nb; b++) order[start[colour[b]]++] = b;
   return nc;
@@ -1849,7 +1852,7 @@ static od_status ic0_build(Scene* s) {
   std::vector<int> bperm(nb), binv(nb);
   const char* oenv = std::getenv("OD_GB300_IC0_ORDER");
   const bool natural = oenv && std::strcmp(oenv, "natural") == 0;
-  P.ic_colours = natural ? 0 : ic0_colour_order(nb, rp, col, bperm);
+  P.ic_colours = natural ? 0 : ic0_colour_order(nb, rp, col, bperm, P.ic_cstart);
   if (natural)
     for (int b = 0; b < nb; b++) bperm[b] = b;
   for (int b = 0; b < nb; b++) binv[bperm[b]] = b;
@@ -2008,6 +2011,15 @@ static od_status ic0_build(Scene* s) {
   OD_CUDA(cudaMemset(P.ic_err, 0, sizeof(int)));
   OD_CUDA(cudaMallocHost(&P.ic_err_host, sizeof(int)));
   OD_TRY(sweep_grid(s, n, &P.ic_grid));
+  // colours far larger than the one-launch sweep's warps (8 per CTA) go one
+  // launch per colour instead
+  P.ic_by_colour = false;
+  if (!natural && P.ic_cstart.size() > 1) {
+    int largest = 0;
+    for (size_t c = 0; c + 1 < P.ic_cstart.size(); c++) largest = std::max(largest, P.ic_cstart[c + 1] - P.ic_cstart[c]);
+    const char* lenv = std::getenv("OD_GB300_IC0_SWEEP");
+    P.ic_by_colour = lenv ? std::strcmp(lenv, "levels") == 0 : largest > 4 * 8 * std::max(1, P.ic_grid);
+  }
   s->device_bytes += sizeof(double) * ((long long)nnz + 2LL * (long long)nl + 2LL * n);
   return OD_OK;
 }
@@ -2095,6 +2107,7 @@ static od_status ic0_apply(Scene* s, const double* r, double* z, const SolveScal
   v.err = P.ic_err;
   v.perm = P.ic_pdof;
   v.zperm = P.ic_zp;
+  if (P.ic_by_colour) v.colour_start = &P.ic_cstart;
   return sweep_launch(s, v, r, z, sc);
 }
 
@@ -2209,26 +2222,34 @@ static od_status pcg_finish(Scene* s, const double* d_b, double* d_x, double shi
 
 // ---- mixed-precision systems: build, partition, solve
 
-// the ring kernel of a piece size (12, 16 or 20 steps)
-static const void* ring_kernel(int ps) {
+// the ring kernel of a tile shape: piece size (12, 16 or 20 steps) x
+// consumer warps (12, or 15 with pieces of 12 or 16 steps: 15 warps of
+// 20-step rings exceed the shared memory)
+static const void* ring_kernel(int ps, int nw) {
+  if (nw == 15) return ps == 12 ? (const void*)pcg32_ring_kernel<12, 15> : (const void*)pcg32_ring_kernel<16, 15>;
   switch (ps) {
-    case 12: return (const void*)pcg32_ring_kernel<12>;
-    case 16: return (const void*)pcg32_ring_kernel<16>;
-    default: return (const void*)pcg32_ring_kernel<20>;
+    case 12: return (const void*)pcg32_ring_kernel<12, 12>;
+    case 16: return (const void*)pcg32_ring_kernel<16, 12>;
+    default: return (const void*)pcg32_ring_kernel<20, 12>;
   }
 }
 
-bool ring_piece_supported(int ps) { return ps == 12 || ps == 16 || ps == 20; }
+bool ring_shape_supported(int ps, int nw) {
+  return (nw == 12 && (ps == 12 || ps == 16 || ps == 20)) || (nw == 15 && (ps == 12 || ps == 16));
+}
 
-// co-resident CTAs of the ring kernel: one per SM for every piece size
+static const int kRingShapes[5][2] = {{12, 12}, {16, 12}, {20, 12}, {12, 15}, {16, 15}};
+
+// co-resident CTAs of the ring kernel: one per SM for every tile shape
 static int ring_kernel_ctas(const Ctx* ctx) {
   int per_sm = 1;
-  for (int ps : {12, 16, 20}) {
+  for (const auto& sh : kRingShapes) {
+    const int ps = sh[0], nw = sh[1];
     int p = 0;
-    if (cudaFuncSetAttribute(ring_kernel(ps), cudaFuncAttributeMaxDynamicSharedMemorySize, ring_smem_bytes(ps)) !=
-            cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, ring_kernel(ps), kRingThreads, ring_smem_bytes(ps)) !=
-            cudaSuccess)
+    if (cudaFuncSetAttribute(ring_kernel(ps, nw), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             ring_smem_bytes(ps, nw)) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, ring_kernel(ps, nw), 32 * (nw + 1),
+                                                      ring_smem_bytes(ps, nw)) != cudaSuccess)
       return 0;
     per_sm = std::min(per_sm, p);
   }
@@ -2415,12 +2436,14 @@ static od_status mixed_partition_work(MixedSys* m, int G) {
 
 // new tile shapes for a built system: piece size of the ring kernel and the
 // per-slice cost of the partition (the slices are re-partitioned)
-od_status mixed_retune(MixedSys* m, int piece_steps, double slice_cost) {
-  if (!ring_piece_supported(piece_steps) || !(slice_cost >= 0.0)) {
-    set_error("mixed tuning: piece steps must be 12, 16 or 20 and the slice cost >= 0");
+od_status mixed_retune(MixedSys* m, int piece_steps, int ring_warps, double slice_cost) {
+  if (!ring_shape_supported(piece_steps, ring_warps) || !(slice_cost >= 0.0)) {
+    set_error("mixed tuning: piece steps 12, 16 or 20 with 12 consumer warps, or 12 or 16 with 15, and a slice "
+              "cost >= 0");
     return OD_ERR_INVALID_ARG;
   }
   m->piece_steps = piece_steps;
+  m->ring_warps = ring_warps;
   m->slice_cost = slice_cost;
   m->slice_w.clear();
   return m->n_sc > 1 ? mixed_partition_work(m, m->cta_grid) : mixed_partition(m, m->cta_grid);
@@ -2473,9 +2496,23 @@ od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::ve
     return OD_ERR_UNSUPPORTED;
   }
   MixedSys* m = new MixedSys();
+  // default tile shape by layout (measured on the 2.6M-tet block: lower
+  // storage 47.7 ms per step with 12-step pieces and 15 consumer warps
+  // against 51.5 with 20 and 12; both triangles best with 20 and 12)
+  if (!scenes.empty() && scenes[0]->pcg.slice && scenes[0]->pcg.slice->lower) {
+    m->piece_steps = 12;
+    m->ring_warps = 15;
+  }
   if (const char* e = std::getenv("OD_GB300_SLICE_COST")) m->slice_cost = std::atof(e);
-  if (const char* e = std::getenv("OD_GB300_RING_PIECE"))
-    if (ring_piece_supported(std::atoi(e))) m->piece_steps = std::atoi(e);
+  {
+    int ps = m->piece_steps, nw = m->ring_warps;
+    if (const char* e = std::getenv("OD_GB300_RING_PIECE")) ps = std::atoi(e);
+    if (const char* e = std::getenv("OD_GB300_RING_WARPS")) nw = std::atoi(e);
+    if (ring_shape_supported(ps, nw)) {
+      m->piece_steps = ps;
+      m->ring_warps = nw;
+    }
+  }
   const int n = (int)scenes.size();
   m->n_sc = n;
   m->scenes = scenes;
@@ -2629,8 +2666,9 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
                     (void*)&m->part,   (void*)&gbp,          (void*)&profp,       (void*)&m->cta_ns};
     if (prof) OD_CUDA(cudaEventRecord(ctx->ev_pool[0], strm));
     ctx->launches++;
-    OD_CUDA(cudaLaunchCooperativeKernel(ring_kernel(m->piece_steps), dim3(m->cta_grid), dim3(kRingThreads), args,
-                                        ring_smem_bytes(m->piece_steps), strm));
+    OD_CUDA(cudaLaunchCooperativeKernel(ring_kernel(m->piece_steps, m->ring_warps), dim3(m->cta_grid),
+                                        dim3(32 * (m->ring_warps + 1)), args,
+                                        ring_smem_bytes(m->piece_steps, m->ring_warps), strm));
     if (prof) OD_CUDA(cudaEventRecord(ctx->ev_pool[1], strm));
     if (m->upd_dir.tiles > 0) {
       ctx->launches++;

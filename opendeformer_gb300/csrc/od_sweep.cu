@@ -586,11 +586,79 @@ od_status selftest_value_wait_timeout(Ctx* c, int* timed_out) {
   return OD_OK;
 }
 
+// Level-synchronous IC sweeps for a factor in colour order (IC(0) of a
+// large mesh): colour c is the contiguous triple range [cs[c], cs[c+1]) and
+// reads only earlier colours (forward) or later ones (backward), so one
+// launch per colour and direction, one thread per triple, needs no waits.
+// This serves colours far larger than the one-launch sweep's warp count,
+// where that kernel would take many triples per warp one after another.
+template <class T>
+__global__ void ic_level_fwd_kernel(int g0, int g1, int n, const int* __restrict__ frp, const int* __restrict__ fci,
+                                    const T* __restrict__ fval, const T* __restrict__ dinv,
+                                    const int* __restrict__ perm, const T* __restrict__ r, T* __restrict__ y,
+                                    const SolveScalars* __restrict__ sc) {
+  if (sc && *(volatile const int*)&sc->done) return;
+  const int g = g0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= g1) return;
+  for (int k = 0; k < 3; k++) {
+    const int i = 3 * g + k;
+    if (i >= n) break;
+    T acc = r[perm ? perm[i] : i];
+    for (int q = frp[i]; q < frp[i + 1]; q++) acc -= fval[q] * y[fci[q]];   // earlier colours, then the triple
+    y[i] = acc * dinv[i];
+  }
+}
+
+template <class T>
+__global__ void ic_level_bwd_kernel(int g0, int g1, int n, const int* __restrict__ bcp, const int* __restrict__ bri,
+                                    const T* __restrict__ bval, const T* __restrict__ dinv,
+                                    const int* __restrict__ perm, const T* __restrict__ y, T* __restrict__ z,
+                                    T* __restrict__ zout, const SolveScalars* __restrict__ sc) {
+  if (sc && *(volatile const int*)&sc->done) return;
+  const int g = g0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= g1) return;
+  for (int k = 2; k >= 0; k--) {
+    const int i = 3 * g + k;
+    if (i >= n) continue;
+    T acc = y[i];
+    for (int q = bcp[i]; q < bcp[i + 1]; q++) acc -= bval[q] * z[bri[q]];   // the triple, then later colours
+    acc *= dinv[i];
+    z[i] = acc;
+    if (perm) zout[perm[i]] = acc;
+  }
+}
+
+template <class T>
+static od_status ic_levels_launch(Scene* s, const SweepView& v, const T* fval, const T* bval, const T* diag,
+                                  const T* r, T* y, T* z, T* zperm, const SolveScalars* sc) {
+  cudaStream_t strm = s->ctx->stream;
+  const std::vector<int>& cs = *v.colour_start;
+  T* zin = v.perm ? zperm : z;   // z in the factor's order
+  const int nc = (int)cs.size() - 1;
+  for (int c = 0; c < nc; c++) {
+    const int g0 = cs[c], g1 = cs[c + 1];
+    if (g1 <= g0) continue;
+    OD_KL(s);
+    ic_level_fwd_kernel<T><<<(g1 - g0 + 255) / 256, 256, 0, strm>>>(g0, g1, v.n, v.frp, v.fci, fval, diag, v.perm, r,
+                                                                     y, sc);
+  }
+  for (int c = nc - 1; c >= 0; c--) {
+    const int g0 = cs[c], g1 = cs[c + 1];
+    if (g1 <= g0) continue;
+    OD_KL(s);
+    ic_level_bwd_kernel<T><<<(g1 - g0 + 255) / 256, 256, 0, strm>>>(g0, g1, v.n, v.bcp, v.bri, bval, diag, v.perm, y,
+                                                                     zin, z, sc);
+  }
+  OD_CUDA(cudaGetLastError());
+  return OD_OK;
+}
+
 // The IC sweeps on FP32 copies of the factor (the mixed-precision IC(0)
 // inner solve): same index arrays and dependency lists as v, FP32 values and
 // vectors, FP32 arithmetic.
 od_status sweep_launch_f32(Scene* s, const SweepView& v, const float* fval, const float* bval, const float* diag,
                            const float* r, float* y, float* z, float* zperm, const SolveScalars* sc) {
+  if (v.colour_start) return ic_levels_launch<float>(s, v, fval, bval, diag, r, y, z, zperm, sc);
   Ctx* ctx = s->ctx;
   cudaStream_t strm = ctx->stream;
   int n = v.n, n_pad = v.n_pad, ng = (v.n + 2) / 3;
@@ -619,6 +687,30 @@ od_status sweep_launch_f32(Scene* s, const SweepView& v, const float* fval, cons
 }
 
 od_status sweep_launch(Scene* s, const SweepView& v, const double* r, double* z, const SolveScalars* sc) {
+  if (v.colour_start) {
+    const bool prof = s->ctx->profiling && s->ctx->ev_pool.size() >= 2;
+    if (prof) OD_CUDA(cudaEventRecord(s->ctx->ev_pool[s->ctx->ev_pool.size() - 2], s->ctx->stream));
+    OD_TRY(ic_levels_launch<double>(s, v, v.fval, v.bval, v.diag, r, v.y, z, v.zperm, sc));
+    if (prof) {
+      Ctx* ctx = s->ctx;
+      OD_CUDA(cudaEventRecord(ctx->ev_pool[ctx->ev_pool.size() - 1], ctx->stream));
+      OD_CUDA(cudaEventSynchronize(ctx->ev_pool[ctx->ev_pool.size() - 1]));
+      float ms = 0.f;
+      OD_CUDA(cudaEventElapsedTime(&ms, ctx->ev_pool[ctx->ev_pool.size() - 2], ctx->ev_pool[ctx->ev_pool.size() - 1]));
+      bool ran = true;
+      if (sc) {
+        SolveScalars h;
+        OD_CUDA(cudaMemcpy(&h, sc, sizeof(SolveScalars), cudaMemcpyDeviceToHost));
+        ran = !h.done;
+      }
+      if (ran) {
+        ctx->sweep_applies++;
+        ctx->sweep_apply_ms += ms;
+        ctx->sweep_apply_bytes += 2.0 * 12.0 * (double)v.nnz + 56.0 * v.n;
+      }
+    }
+    return OD_OK;
+  }
   Ctx* ctx = s->ctx;
   cudaStream_t strm = ctx->stream;
   int n = v.n, n_pad = v.n_pad, ng = (v.n + 2) / 3;

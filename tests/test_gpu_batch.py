@@ -156,10 +156,12 @@ def test_autotune_keeps_state_and_results(tmp_path):
     before = [(s.displacements(), *s.state()) for s in tuned]
     cache = str(tmp_path / "tune.json")
     rep = bt.autotune(repeats=1, cache=cache)
-    assert not rep["cached"] and rep["candidates"] == 12
-    assert rep["piece_steps"] in (12, 16, 20) and rep["slice_cost"] in (2.0, 4.0, 8.0, 16.0)
+    assert not rep["cached"] and rep["candidates"] == 20
+    assert (rep["piece_steps"], rep["consumer_warps"]) in ((12, 12), (16, 12), (20, 12), (12, 15), (16, 15))
+    assert rep["slice_cost"] in (2.0, 4.0, 8.0, 16.0)
     assert rep["best_ms"] <= rep["default_ms"]
-    assert bt.tuning() == {"piece_steps": rep["piece_steps"], "slice_cost": rep["slice_cost"]}
+    shape = {k: rep[k] for k in ("piece_steps", "consumer_warps", "slice_cost")}
+    assert bt.tuning() == shape
     for s, b in zip(tuned, before):
         assert all(np.array_equal(x, y) for x, y in zip((s.displacements(), *s.state()), b))
     bt.step(4)
@@ -172,6 +174,8 @@ def test_autotune_keeps_state_and_results(tmp_path):
     again.step(1)
     rep2 = again.autotune(cache=cache)
     assert rep2["cached"] and rep2["key"] == rep["key"]
-    assert again.tuning() == {"piece_steps": rep["piece_steps"], "slice_cost": rep["slice_cost"]}
+    assert again.tuning() == shape
     with pytest.raises(api.ODError):
         again.set_tuning(14, 8.0)
+    with pytest.raises(api.ODError):
+        again.set_tuning(20, 8.0, consumer_warps=15)   # 15 warps of 20-step rings exceed the shared memory

@@ -317,6 +317,25 @@ def test_ic0_factor_paths_agree(golden, monkeypatch):
     assert rel_err(x1, x0) <= 1e-10
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ic0_sweeps_by_colour_agree(golden, monkeypatch, precision):
+    """IC(0) sweeps one launch per colour (OD_GB300_IC0_SWEEP=levels; the
+    default when colours hold far more block rows than the one-launch
+    sweep has warps) and the one-launch sweep apply the same factor: PCG
+    iterations within 1, solutions within 1e-9 (FP64) or 1e-8 (mixed)."""
+    out = {}
+    for mode in ("one_launch", "levels"):
+        monkeypatch.setenv("OD_GB300_IC0_SWEEP", "levels" if mode == "levels" else "one")
+        s, p, e = gpu_scene(golden, "neohookean", "full")
+        A = e["values"] * (1.0 / 3600.0) + e["mass"]
+        out[mode] = s.pcg(A, e["cg_b"], solver=api.CGSolver(1e-11, 5000, api.Preconditioner("ic0"),
+                                                             precision=precision))
+    (x1, s1), (x0, s0) = out["levels"], out["one_launch"]
+    assert s1.status == 0 and s0.status == 0
+    assert abs(s1.iterations - s0.iterations) <= 1 + (2 if precision == "mixed" else 0)
+    assert rel_err(x1, x0) <= (1e-9 if precision == "fp64" else 1e-8)
+
+
 def test_degenerate_scenes_step():
     """Edge cases of the setup and assembly paths: a single tetrahedron, and
     a mesh with every DOF constrained (no free DOF, empty force lists); both
