@@ -454,7 +454,9 @@ od_status od_server_add_scene(od_server* server, const od_scene_spec* spec, int*
 od_status od_server_now(od_server* server, double* t);
 od_status od_server_submit(od_server* server, const od_step_request* req, long long* ticket);
 /* one tick; results receives at most capacity completed requests (capacity
- * also caps the scenes stepped) */
+ * also caps the scenes stepped).  When the tick's step fails as a call, the
+ * requests it had taken come back in results with that status and the
+ * call returns it. */
 od_status od_server_tick(od_server* server, int capacity, od_step_result* results, int* n_results);
 od_status od_server_pending(od_server* server, long long* pending);
 /* makes scenes resident (in order, on the caller's thread) while they fit without eviction */

@@ -444,18 +444,35 @@ od_status od_server_tick(od_server* sv, int capacity, od_step_result* results, i
   const auto tk2 = clock_type::now();
   sv->stats.s_loads += std::chrono::duration<double>(tk2 - tk1).count();
   std::vector<od_step_stats> st(scenes.size());
+  od_status fail = OD_OK;   // a step that failed as a call: its requests come back with that status
   if (sv->cfg.batched) {
     od_batch* b = nullptr;
-    OD_TRY(od_batch_create(sv->ctx, (int)scenes.size(), scenes.data(), &b));
-    const od_status rc = od_batch_step(b, 1, st.data());
-    od_batch_destroy(b);
-    if (rc != OD_OK) return rc;
-  } else {
-    for (size_t k = 0; k < scenes.size(); k++) {
-      const od_status rc = od_step(scenes[k], 1, &st[k]);
-      if (rc != OD_OK && rc != OD_ERR_NOT_CONVERGED && rc != OD_ERR_NAN) return rc;
-      if (rc != OD_OK && st[k].status == OD_OK) st[k].status = rc;
+    fail = od_batch_create(sv->ctx, (int)scenes.size(), scenes.data(), &b);
+    if (fail == OD_OK) {
+      fail = od_batch_step(b, 1, st.data());
+      od_batch_destroy(b);
     }
+  } else {
+    for (size_t k = 0; k < scenes.size() && fail == OD_OK; k++) {
+      const od_status rc = od_step(scenes[k], 1, &st[k]);
+      if (rc != OD_OK && rc != OD_ERR_NOT_CONVERGED && rc != OD_ERR_NAN) fail = rc;
+      else if (rc != OD_OK && st[k].status == OD_OK) st[k].status = rc;
+    }
+  }
+  if (fail != OD_OK) {
+    const std::string why = od_last_error();
+    for (size_t k = 0; k < reqs.size(); k++) {
+      od_step_result& r = results[k];
+      r.ticket = reqs[k].ticket;
+      r.scene = reqs[k].r.scene;
+      r.status = fail;
+      r.pcg_iterations = 0;
+      r.arrival = reqs[k].r.arrival;
+      r.done = now_s(sv);
+    }
+    *n_results = (int)reqs.size();
+    set_error("od_server_tick: " + why);
+    return fail;
   }
   const auto tk3 = clock_type::now();
   sv->stats.s_step += std::chrono::duration<double>(tk3 - tk2).count();

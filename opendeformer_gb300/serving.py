@@ -140,11 +140,13 @@ class Server:
     # -- one tick
     def tick(self) -> list[StepRequest]:
         """Steps every resident scene with a pending request (the oldest
-        request of each); returns the completed requests."""
+        request of each); returns the completed requests.  When the step
+        fails as a call, its requests (with that status) are in self.failed
+        and ODError is raised."""
         if len(self._res) < self._n_scenes:
             self._res = (api.od_step_result * max(1, self._n_scenes))()
         n = C.c_int(0)
-        api._check(self._L.od_server_tick(self.h, len(self._res), self._res, C.byref(n)), "od_server_tick")
+        rc = self._L.od_server_tick(self.h, len(self._res), self._res, C.byref(n))
         out = []
         for k in range(n.value):
             r = self._res[k]
@@ -153,6 +155,8 @@ class Server:
             req.status = r.status
             req.pcg_iterations = r.pcg_iterations
             out.append(req)
+        self.failed = out if rc != api.OD_OK else []   # a failed tick's requests, with its status
+        api._check(rc, "od_server_tick")
         return out
 
     @property
