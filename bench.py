@@ -355,10 +355,21 @@ def cpu_processes():
 
 def cpu_pool_map(fn, jobs):
     """Runs the oracle workers in spawned processes (never forked from a
-    process that holds a CUDA context)."""
+    process that holds a CUDA context): at most one process per host core,
+    each with single-threaded BLAS, the jobs spread over them in order."""
     import multiprocessing as mp
-    with mp.get_context("spawn").Pool(len(jobs)) as pool:
-        return pool.map(fn, jobs)
+    procs = max(1, min(len(jobs), cpu_processes()))
+    saved = {k: os.environ.get(k) for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS")}
+    os.environ.update({k: "1" for k in saved})   # inherited by the spawned workers
+    try:
+        with mp.get_context("spawn").Pool(procs) as pool:
+            return pool.map(fn, jobs, chunksize=max(1, len(jobs) // (4 * procs)))
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
 
 
 def host_cpu_model():
@@ -714,6 +725,97 @@ def relabel_tier(args, api, ctx):
     return out
 
 
+def modal_tier(args, api, ctx):
+    """Modal linear Newmark (intergrator/linearNewmark.cpp) on the headline
+    beam: Hooke stiffness with the beam material's E and nu, consistent
+    mass, 16 modes; Newmark beta 1/4, gamma 1/2, Rayleigh 0.01 / 0.001,
+    dt 1/120 s, the beam's 500 Pa traction held constant.  Setup on the GPU
+    (Hooke assembly, thick-restart Lanczos on K^-1 M with FP64 block-Jacobi
+    PCG applies) against the reference's setup algorithm on one host core
+    (ARPACK shift-invert at 0 with a SuperLU factorisation, through scipy's
+    eigsh, on the compiled reference's K and M).  Steps end to end as the
+    reference's loop runs them: runOneTimeStep and
+    updateMeshVerticesDisplacements (the full-order field to the host) per
+    step, against the restated steps with numpy on the host."""
+    wl = WORKLOADS["beam98k_nh_newmark"]
+    g = wl["mesh"]()
+    _, rho, E, nu, thr = wl["material"]
+    r = args.modal_modes
+    cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+    s = api.Scene(ctx, g.X, g.tets, g.facets, cd, api.Material("corotational", rho, E, nu, thr))
+    s.set_loads(tractions=[([0.0, -wl["traction"], 0.0], g.face_facets(0, 1))])
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    m = api.LinearNewmark(s, r, 0.25, 0.5, wl["alpha_m"], wl["beta_k"], wl["dt"], youngs=E, poisson=nu)
+    setup_s = time.perf_counter() - t0
+    info = m.info
+    lam, phi = m.modes()
+    m.setExternalVirtualWork()
+    u = np.zeros((g.n_nodes, 3))
+    L = api.load_library()
+    for _ in range(3):
+        m.runOneTimeStep()
+        L.od_modal_get_displacements(m.h, api._d(u))
+    n_steps = max(200, 40 * args.tier_steps)
+    t0 = time.perf_counter()
+    for _ in range(n_steps):
+        api._check(L.od_modal_step(m.h, 1), "od_modal_step")
+        api._check(L.od_modal_get_displacements(m.h, api._d(u)), "od_modal_get_displacements")
+    gpu_step_s = (time.perf_counter() - t0) / n_steps
+    out = {"workload": "beam98k_hooke_modal16", "n_modes": r, "dofs": s.dofs, "krylov": info.krylov,
+           "lanczos_applies": info.lanczos_steps, "restarts": info.restarts,
+           "pcg_iterations_per_apply": info.pcg_iterations / max(1, info.lanczos_steps),
+           "max_residual": info.max_residual, "gpu_setup_s": setup_s,
+           "lambda_first_last": [float(lam[0]), float(lam[-1])],
+           "gpu_steps_per_s_e2e": 1.0 / gpu_step_s,
+           "e2e_note": "per step: od_modal_step + od_modal_get_displacements (the 3 x 18,785 field, pageable "
+                       "host buffer)"}
+    fext = s.external_forces()
+    m.close()
+    if not args.no_cpu_baseline:
+        try:
+            from oracle import modal as MO
+            from oracle import reforacle as R
+            if not R.available():
+                raise RuntimeError("compiled reference not available")
+            rs = R.RefScene(g.X, g.tets, g.facets, cd, "corotational", rho, E, nu, thr)
+            K, M = MO.reference_matrices(rs, E, nu)
+            os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+            t0 = time.perf_counter()
+            lam_ref, phi_ref = MO.modes(K, M, r)
+            cpu_setup = time.perf_counter() - t0
+            o = MO.LinearNewmarkOracle(lam_ref, phi_ref, 0.25, 0.5, wl["alpha_m"], wl["beta_k"], wl["dt"])
+            o.set_external(fext)
+            nc = 50
+            t0 = time.perf_counter()
+            for _ in range(nc):
+                o.step(1)
+                MO.to_nodes(o.full_order(), g.n_nodes, cd)
+            cpu_step_s = (time.perf_counter() - t0) / nc
+            # parity: the same 50 + (3 + n_steps) steps on the GPU modes
+            m = api.LinearNewmark(s, r, 0.25, 0.5, wl["alpha_m"], wl["beta_k"], wl["dt"], youngs=E, poisson=nu)
+            m.setExternalVirtualWork()
+            m.runOneTimeStep(nc)
+            gpu_u = m.displacements()
+            m.close()
+            ref_u = MO.to_nodes(o.full_order(), g.n_nodes, cd)
+            out.update({
+                "cpu_baseline": {"value": 1.0 / cpu_setup, "unit": "setups/s", "cores": 1, "kind": "reference",
+                                 "sample": f"ARPACK shift-invert at 0 with SuperLU (scipy eigsh, the algorithm "
+                                           f"and libraries EigenSolver links) on the compiled reference's Hooke K "
+                                           f"and mass: {cpu_setup:.1f} s for {r} modes of {s.dofs} DOFs; steps: "
+                                           f"the restated LinearNewmark step + full-order field in numpy, "
+                                           f"{nc} steps"},
+                "cpu_setup_s": cpu_setup, "cpu_steps_per_s": 1.0 / cpu_step_s,
+                "speedup_setup": cpu_setup / setup_s, "speedup_steps_e2e": cpu_step_s / gpu_step_s,
+                "lambda_max_rel_err_vs_arpack": float(np.abs(lam / lam_ref - 1.0).max()),
+                "u_rel_err_vs_oracle_after_50_steps": float(np.abs(gpu_u - ref_u).max() / np.abs(ref_u).max())})
+        except Exception as exc:
+            out["cpu_baseline"] = {"value": None, "sample": f"failed: {exc}"}
+    s.close()
+    return out
+
+
 def batched_tier(args, api, ctx):
     """Batched uneven instances: 512 jittered grids (per-axis cube counts
     log-uniform in [4, 40], 6 tets per cube), corotational / Neo-Hookean
@@ -1008,6 +1110,13 @@ def tiers_summary(line):
     if "sweep_tier" in line:
         t = line["sweep_tier"]
         out["sweep"] = {k: g(t, k, "steps_per_s") for k in ("ic", "ldlt") if isinstance(t.get(k), dict)}
+    if "modal_tier" in line:
+        t = line["modal_tier"]
+        out["modal"] = {"gpu_setup_s": g(t, "gpu_setup_s"), "cpu_setup_s": g(t, "cpu_setup_s"),
+                        "speedup_setup": g(t, "speedup_setup"), "steps_per_s_e2e": g(t, "gpu_steps_per_s_e2e"),
+                        "speedup_steps_e2e": g(t, "speedup_steps_e2e"),
+                        "lambda_rel_err": g(t, "lambda_max_rel_err_vs_arpack"),
+                        "u_rel_err": g(t, "u_rel_err_vs_oracle_after_50_steps")}
     return out
 
 
@@ -1147,11 +1256,19 @@ def run_gpu(args, wl):
                 "pipe_active_pct_ncu": 43.8,
                 "pipe_source": "ncu --set full capture of this kernel on this workload "
                                "(sm__pipe_fp64_cycles_active, of peak, active cycles)"}
-    roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+    phases = None
+    if counters.pcg_phase_iterations:
+        names = ("spmv_pq", "pq_sum", "update_rz_rr", "rz_rr_sum", "direction", "barrier")
+        phases = {k: round(1000.0 * counters.pcg_phase_ms[j] / counters.pcg_phase_iterations, 3)
+                  for j, k in enumerate(names)}
+        phases["note"] = ("us per PCG iteration on the clock of CTA 0 (%globaltimer); a *_sum or barrier "
+                          "phase includes the wait for the slowest CTA")
+        roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": nbytes,
                 "avg_launch_ms": avg_ms, "launches": kl,
                 "share_of_step_time": kms / total_ms if total_ms else None, "fp64": fp64,
+                "pcg_phases_us_per_iteration": phases,
                 "note": "the binding roofline is fp64 (FP64 pipe and grid barriers): the 98k-tet system "
                         "(18.6 MB) stays L2-resident, so DRAM traffic (traffic) is far below the algorithmic "
                         "bytes"}
@@ -1184,7 +1301,7 @@ def run_gpu(args, wl):
         only = [t for t in args.only_tiers.split(",") if t]
         for name, fn in (("precision_tier", precision_tier), ("batched_tier", batched_tier),
                          ("serving_tier", serving_tier), ("sweep_tier", sweep_tier),
-                         ("ic0_tier", ic0_tier), ("relabel_tier", relabel_tier)):
+                         ("ic0_tier", ic0_tier), ("relabel_tier", relabel_tier), ("modal_tier", modal_tier)):
             if only and name.split("_")[0] not in only:
                 continue
             try:
@@ -1227,11 +1344,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tiers", action="store_true", help="skip the mixed-precision and batched workloads")
     ap.add_argument("--tier-steps", type=int, default=5)
-    ap.add_argument("--only-tiers", default="", help="comma list of precision,batched,serving,sweep,ic0,relabel (default: all)")
+    ap.add_argument("--only-tiers", default="", help="comma list of precision,batched,serving,sweep,ic0,relabel,modal (default: all)")
     ap.add_argument("--precision-nz", type=int, default=64,
                     help="cube layers of the precision-tier block (64: 2,621,440 tets)")
     ap.add_argument("--precision-variants", default="fp64,mixed,mixed_full,mixed_ic0",
                     help="comma list of the precision tier's solvers (fp64, mixed, mixed_full, mixed_ic0)")
+    ap.add_argument("--modal-modes", type=int, default=16)
     ap.add_argument("--serving-pool", type=int, default=512)
     ap.add_argument("--serving-rate", type=float, default=2000.0)
     ap.add_argument("--serving-seconds", type=float, default=15.0)

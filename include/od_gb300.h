@@ -164,6 +164,13 @@ typedef struct od_counters {
   double sweep_apply_bytes;   /* their algorithmic bytes: 2 x (nnz x 12 B) + 7 x 8 B per row */
   long long sweep_levels;     /* dependency levels of the last factor's two sweeps (the apply's
                                  critical path, in rows) */
+  /* persistent PCG iterations timed phase by phase while profiling (the clock of
+     CTA 0, whose share of the rows equals every CTA's): [0] SpMV and p.q, [1] the
+     grid-wide sum of p.q (the wait for the slowest CTA included), [2] x, r, z
+     updates with r.z and r.r, [3] their sum, [4] p = z + beta p, [5] the barrier
+     before the next SpMV */
+  double pcg_phase_ms[6];
+  long long pcg_phase_iterations;
 } od_counters;
 
 typedef struct od_scene_info {
@@ -503,6 +510,67 @@ od_status od_bsr_pcg_noalloc(int nb, const int* d_row_ptr, const int* d_col, con
  * (the reference labels the first only); nodes in no element go last.
  * Node arrays (positions, constraints, facets) are the caller's to permute. */
 od_status od_mesh_relabel(int n_nodes, int n_elems, int nodes_per_elem, int* elems, int* new_labels);
+
+/* ---- modal (reduced) linear Newmark: intergrator/linearNewmark.{h,cpp}.
+ * LinearNewmark::LinearNewmark (linearNewmark.cpp:8-50) assembles the linear
+ * (Hooke) stiffness K (material/hooke.cpp:18-60) and the consistent mass M of
+ * the scene's mesh and constraints, and keeps the n_modes eigenpairs
+ * K phi = lambda M phi of smallest lambda (EigenSolver::getEigenValVectors,
+ * core/eigensolver.cpp:8-13: ARPACK's shift-invert mode at 0).  Here the
+ * eigenpairs come from a thick-restart Lanczos iteration on K^-1 M in the M
+ * inner product, with every K^-1 applied by the FP64 block-Jacobi PCG on the
+ * device; modes are M-orthonormal and ordered by ascending lambda.  The scene
+ * supplies mesh, constraints, density and the loads of od_scene_set_loads;
+ * its own integrator and displacement are not used or changed. */
+typedef struct od_modal od_modal;
+typedef struct od_modal_params {
+  int n_modes;            /* LinearNewmark's DOFS: modes kept (1 <= n_modes < scene dofs) */
+  double beta, gamma;     /* Newmark parameters */
+  double alpha_m, beta_k; /* Rayleigh damping: massDamp, stiffDamp */
+  double dt;              /* time step */
+  double youngs, poisson; /* HookeMaterial(rho, YOUNGS, POSSION); rho is the scene's density */
+  double tol;             /* eigenpair residual ||K^-1 M phi - phi / lambda||_M relative to
+                             1 / lambda; 0: 1e-10 */
+  int krylov;             /* Lanczos basis size (> n_modes + 1); 0: max(2 n_modes + 10, n_modes + 20),
+                             at most the scene dofs */
+  double inner_tol;       /* PCG tolerance of each K^-1 apply; 0: 1e-12 */
+  int inner_max_iter;     /* 0: 100000 */
+  int max_restarts;       /* 0: 200 */
+} od_modal_params;
+
+typedef struct od_modal_info {
+  int n_modes;
+  int dofs;
+  int krylov;
+  int lanczos_steps;       /* K^-1 M applies */
+  int restarts;
+  long long pcg_iterations;  /* summed over the applies */
+  double max_residual;     /* largest relative eigenpair residual at exit */
+  double setup_ms;         /* wall time of od_modal_create */
+} od_modal_info;
+
+od_status od_modal_create(od_scene* scene, const od_modal_params* params, od_modal** out);
+od_status od_modal_destroy(od_modal* modal);
+/* setExternalVirtualWork (linearNewmark.cpp:52-55, forcer.cpp:80-96): the
+ * modal forces phi_i . f_ext of a compacted DOF vector (NULL: the scene's
+ * current loads); the modal accelerations are set to them */
+od_status od_modal_set_external_forces(od_modal* modal, const double* f_ext);
+/* runOneTimeStep (linearNewmark.cpp:57-79), steps times */
+od_status od_modal_step(od_modal* modal, int steps);
+/* updateMeshVerticesDisplacements / getMeshVerticesVelocities
+ * (linearNewmark.cpp:81-131): sum_i d_i phi_i on the free DOFs, as 3 values
+ * per node; constrained entries get the scene's displacement (zero unless
+ * set) and zero velocity */
+od_status od_modal_get_displacements(od_modal* modal, double* u);
+od_status od_modal_get_velocities(od_modal* modal, double* v);
+/* eigenvalues (n_modes, ascending) and, if basis != NULL, the modes as
+ * n_modes rows of the compacted DOFs */
+od_status od_modal_get_modes(od_modal* modal, double* lambda, double* basis);
+/* reduced state d, v, a (n_modes each; any may be NULL) */
+od_status od_modal_get_state(od_modal* modal, double* d, double* v, double* a);
+/* the assembled Hooke stiffness in the reference value layout (num_values) */
+od_status od_modal_get_stiffness(od_modal* modal, double* values);
+od_status od_modal_get_info(od_modal* modal, od_modal_info* info);
 
 /* Checkpoint / resume: mesh displacement + integrator vectors as a host blob.
  * Call with buf == NULL to query the size. */

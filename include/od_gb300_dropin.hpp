@@ -247,4 +247,67 @@ class GpuIntergrator : public ODER::Intergrator {
   mutable od_status last_status = OD_OK;
 };
 
+// LinearNewmark (intergrator/linearNewmark.h:13-41), the modal integrator.
+// Its constructor's mesh and indexer are the scene's mesh and constraints;
+// HookeMaterial keeps its moduli private, so youngs and poisson are passed
+// here (the density is the scene's).  The eigenpairs come from the device
+// Lanczos solve (od_modal_create) instead of ARPACK.
+class GpuLinearNewmark : public ODER::Intergrator {
+ public:
+  GpuLinearNewmark(od_scene* s, ODER::Scalar beta, ODER::Scalar gamma, int DOFS, ODER::Scalar massDamp,
+                   ODER::Scalar stiffDamp, ODER::Scalar ts, ODER::Scalar youngs, ODER::Scalar poisson)
+      : Intergrator(DOFS, massDamp, stiffDamp, ts), scene(s) {
+    od_scene_info info{};
+    last_status = od_scene_get_info(scene, &info);
+    totalDofs = info.dofs;
+    nodes = info.n_nodes;
+    if (last_status != OD_OK) return;
+    od_modal_params p{};
+    p.n_modes = DOFS;
+    p.beta = beta;
+    p.gamma = gamma;
+    p.alpha_m = massDamp;
+    p.beta_k = stiffDamp;
+    p.dt = ts;
+    p.youngs = youngs;
+    p.poisson = poisson;
+    last_status = od_modal_create(scene, &p, &modal);
+  }
+  ~GpuLinearNewmark() override { od_modal_destroy(modal); }
+  GpuLinearNewmark(const GpuLinearNewmark&) = delete;
+  GpuLinearNewmark& operator=(const GpuLinearNewmark&) = delete;
+  // the forcer's full-order virtual works (forcer.cpp:80-96), projected on
+  // the modes on the device (linearNewmark.cpp:52-55)
+  void setExternalVirtualWork(const ODER::Forcer& forcer) override {
+    std::vector<double> vws((size_t)totalDofs, 0.0);
+    forcer.getVirtualWorks(totalDofs, totalDofs, nullptr, vws.data());
+    last_status = od_modal_set_external_forces(modal, vws.data());
+  }
+  void runOneTimeStep() override { last_status = od_modal_step(modal, 1); }
+  // free DOFs only; constrained axes keep the mesh's value (linearNewmark.cpp:94-108)
+  void updateMeshVerticesDisplacements(const ODER::Reference<ODER::NodeIndexer>& indexer,
+                                       ODER::Reference<ODER::Mesh>& mesh) const override {
+    std::vector<double> u(3 * (size_t)nodes);
+    last_status = od_modal_get_displacements(modal, u.data());
+    if (last_status != OD_OK) return;
+    for (int i = 0; i < nodes; i++)
+      for (int ax = 0; ax < 3; ax++)
+        if (indexer->getGlobalIndex(i, ax) >= 0) mesh->getVertexDisplacement(i)[ax] = u[3 * (size_t)i + ax];
+  }
+  void getMeshVerticesVelocities(const ODER::Reference<ODER::NodeIndexer>& indexer,
+                                 const ODER::Reference<ODER::Mesh>& mesh, ODER::Vector3* velocities) const override {
+    (void)indexer;
+    (void)mesh;
+    std::vector<double> v(3 * (size_t)nodes);
+    last_status = od_modal_get_velocities(modal, v.data());
+    if (last_status != OD_OK) return;
+    for (int i = 0; i < nodes; i++)
+      velocities[i] = ODER::Vector3(v[3 * (size_t)i], v[3 * (size_t)i + 1], v[3 * (size_t)i + 2]);
+  }
+  od_scene* scene;
+  od_modal* modal = nullptr;
+  int totalDofs = 0, nodes = 0;
+  mutable od_status last_status = OD_OK;
+};
+
 }  // namespace od_dropin

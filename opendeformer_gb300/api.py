@@ -89,7 +89,8 @@ class od_counters(C.Structure):
                 ("mix_spmv_work_ms", C.c_double), ("mix_fallbacks", C.c_longlong),
                 ("sweep_factors", C.c_longlong), ("sweep_factor_ms", C.c_double), ("sweep_nnz", C.c_longlong),
                 ("sweep_applies", C.c_longlong), ("sweep_apply_ms", C.c_double), ("sweep_apply_bytes", C.c_double),
-                ("sweep_levels", C.c_longlong)]
+                ("sweep_levels", C.c_longlong), ("pcg_phase_ms", C.c_double * 6),
+                ("pcg_phase_iterations", C.c_longlong)]
 
 
 class od_scene_info(C.Structure):
@@ -138,6 +139,19 @@ class od_server_stats(C.Structure):
                 ("resident", C.c_longlong), ("resident_bytes", C.c_longlong), ("budget_bytes", C.c_longlong)]
 
 
+class od_modal_params(C.Structure):
+    _fields_ = [("n_modes", C.c_int), ("beta", C.c_double), ("gamma", C.c_double), ("alpha_m", C.c_double),
+                ("beta_k", C.c_double), ("dt", C.c_double), ("youngs", C.c_double), ("poisson", C.c_double),
+                ("tol", C.c_double), ("krylov", C.c_int), ("inner_tol", C.c_double), ("inner_max_iter", C.c_int),
+                ("max_restarts", C.c_int)]
+
+
+class od_modal_info(C.Structure):
+    _fields_ = [("n_modes", C.c_int), ("dofs", C.c_int), ("krylov", C.c_int), ("lanczos_steps", C.c_int),
+                ("restarts", C.c_int), ("pcg_iterations", C.c_longlong), ("max_residual", C.c_double),
+                ("setup_ms", C.c_double)]
+
+
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _vp = C.c_void_p
@@ -146,6 +160,7 @@ _lib = None
 # Live handles, released in a safe order (scenes before contexts) when the
 # interpreter exits, before the CUDA runtime itself is torn down.
 _live_batches: "weakref.WeakSet" = weakref.WeakSet()
+_live_modals: "weakref.WeakSet" = weakref.WeakSet()
 _live_scenes: "weakref.WeakSet" = weakref.WeakSet()
 _live_ctxs: "weakref.WeakSet" = weakref.WeakSet()
 _shutting_down = False
@@ -154,6 +169,11 @@ _shutting_down = False
 @atexit.register
 def _release_all():
     global _shutting_down
+    for md in list(_live_modals):
+        try:
+            md.close()
+        except Exception:
+            pass
     for bt in list(_live_batches):
         try:
             bt.close()
@@ -237,6 +257,16 @@ SIGNATURES = {
     "od_server_warm": (C.c_int, [_vp, C.c_int, _ip, C.POINTER(C.c_int)]),
     "od_server_get_scene": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
     "od_server_get_stats": (C.c_int, [_vp, C.POINTER(od_server_stats)]),
+    "od_modal_create": (C.c_int, [_vp, C.POINTER(od_modal_params), C.POINTER(_vp)]),
+    "od_modal_destroy": (C.c_int, [_vp]),
+    "od_modal_set_external_forces": (C.c_int, [_vp, _dp]),
+    "od_modal_step": (C.c_int, [_vp, C.c_int]),
+    "od_modal_get_displacements": (C.c_int, [_vp, _dp]),
+    "od_modal_get_velocities": (C.c_int, [_vp, _dp]),
+    "od_modal_get_modes": (C.c_int, [_vp, _dp, _dp]),
+    "od_modal_get_state": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "od_modal_get_stiffness": (C.c_int, [_vp, _dp]),
+    "od_modal_get_info": (C.c_int, [_vp, C.POINTER(od_modal_info)]),
     "od_scene_save": (C.c_int, [_vp, _vp, C.POINTER(C.c_size_t)]),
     "od_scene_load": (C.c_int, [_vp, _vp, C.c_size_t]),
 }
@@ -719,6 +749,86 @@ class Scene:
     def load(self, blob: bytes):
         buf = C.create_string_buffer(blob, len(blob))
         _check(load_library().od_scene_load(self.h, C.cast(buf, _vp), len(blob)), "load")
+
+
+class LinearNewmark:
+    """Modal (reduced) linear Newmark on a scene's mesh and constraints
+    (intergrator/linearNewmark.{h,cpp}; od_modal_*): the n_modes lowest
+    eigenpairs of the Hooke stiffness against the scene's consistent mass,
+    then the reference's per-mode Newmark update.  The scene's density is
+    the mass density; youngs and poisson are HookeMaterial's."""
+
+    def __init__(self, scene: "Scene", n_modes: int, beta=0.25, gamma=0.5, massDamp=0.0, stiffDamp=0.0,
+                 ts=1.0 / 60, youngs=None, poisson=None, tol=0.0, krylov=0, inner_tol=0.0,
+                 inner_max_iter=0, max_restarts=0):
+        L = load_library()
+        self.scene = scene
+        m = scene.material
+        p = od_modal_params(int(n_modes), float(beta), float(gamma), float(massDamp), float(stiffDamp), float(ts),
+                            float(m.youngs if youngs is None else youngs),
+                            float(m.poisson if poisson is None else poisson), float(tol), int(krylov),
+                            float(inner_tol), int(inner_max_iter), int(max_restarts))
+        h = _vp()
+        _check(L.od_modal_create(scene.h, C.byref(p), C.byref(h)), "od_modal_create")
+        self.h = h
+        self.n_modes = int(n_modes)
+        _live_modals.add(self)
+
+    def close(self):
+        if getattr(self, "h", None) and not _shutting_down:
+            load_library().od_modal_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setExternalVirtualWork(self, f_ext=None):
+        """Modal forces of a compacted DOF vector, or of the scene's loads (None)."""
+        f = None if f_ext is None else np.ascontiguousarray(f_ext, dtype=np.float64)
+        if f is not None and f.size != self.scene.dofs:
+            raise ValueError(f"f_ext must have {self.scene.dofs} entries")
+        _check(load_library().od_modal_set_external_forces(self.h, _d(f) if f is not None else None),
+               "od_modal_set_external_forces")
+
+    def runOneTimeStep(self, steps: int = 1):
+        _check(load_library().od_modal_step(self.h, int(steps)), "od_modal_step")
+
+    def displacements(self):
+        u = np.zeros((self.scene.n_nodes, 3))
+        _check(load_library().od_modal_get_displacements(self.h, _d(u)), "od_modal_get_displacements")
+        return u
+
+    def velocities(self):
+        v = np.zeros((self.scene.n_nodes, 3))
+        _check(load_library().od_modal_get_velocities(self.h, _d(v)), "od_modal_get_velocities")
+        return v
+
+    def modes(self, basis=True):
+        """(eigenvalues ascending, modes as rows of the compacted DOFs or None)."""
+        lam = np.zeros(self.n_modes)
+        ph = np.zeros((self.n_modes, self.scene.dofs)) if basis else None
+        _check(load_library().od_modal_get_modes(self.h, _d(lam), _d(ph) if basis else None), "od_modal_get_modes")
+        return lam, ph
+
+    def state(self):
+        d, v, a = (np.zeros(self.n_modes) for _ in range(3))
+        _check(load_library().od_modal_get_state(self.h, _d(d), _d(v), _d(a)), "od_modal_get_state")
+        return d, v, a
+
+    def stiffness(self):
+        """The assembled Hooke stiffness in the reference value layout."""
+        k = np.zeros(self.scene.n_values)
+        _check(load_library().od_modal_get_stiffness(self.h, _d(k)), "od_modal_get_stiffness")
+        return k
+
+    @property
+    def info(self):
+        i = od_modal_info()
+        _check(load_library().od_modal_get_info(self.h, C.byref(i)), "od_modal_get_info")
+        return i
 
 
 class Batch:

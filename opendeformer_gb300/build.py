@@ -20,7 +20,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]
 SOURCES = ["od_host.cpp", "od_rif.cpp", "od_ric.cpp", "od_relabel.cpp", "od_server.cpp", "od_elements.cu", "od_sparse.cu", "od_api.cu",
-           "od_batch.cu", "od_noalloc.cu", "od_sweep.cu", "od_collision.cu", "od_peaks.cu", "od_mixed_ic0.cu"]
+           "od_batch.cu", "od_noalloc.cu", "od_sweep.cu", "od_collision.cu", "od_peaks.cu", "od_mixed_ic0.cu",
+           "od_modal.cu"]
 # per-file flags: the collision geometry rounds every operation separately,
 # as the reference's compiled code does
 FILE_FLAGS = {"od_collision.cu": ["-fmad=false"]}

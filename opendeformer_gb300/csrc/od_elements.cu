@@ -935,6 +935,88 @@ od_status launch_precompute(Scene* s) {
   return OD_OK;
 }
 
+// ------------------------------------------------------------ linear (Hooke)
+// HookeMaterial::generateStiffnessMatrix (material/hooke.cpp:18-60): per
+// element and node pair a <= b the block of LinearIsotropicTetElement::
+// generateSubStiffnessMatrix (element/tetelement.cpp:98-116) with the Lame
+// coefficients D = (lambda + 2 mu, lambda, mu) (hooke.cpp:6-16), written into
+// the colour-ordered staging layout (78 values: the element's 12x12 upper
+// triangle by rows) that the assembly sums in element order.
+__global__ void hooke_stage_kernel(int ne, const int4* __restrict__ tets, const double* __restrict__ X, double D0,
+                                   double D1, double D2, double* __restrict__ k78) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  const int4 t = tets[e];
+  const V3t<double> p0 = ld3(X, t.x), p1 = ld3(X, t.y), p2 = ld3(X, t.z), p3 = ld3(X, t.w);
+  // shape-function gradients scaled by 6V, oriented as the precomputes
+  const V3t<double> da = v_sub(p0, p3), db = v_sub(p1, p3), dc = v_sub(p2, p3), ca = v_sub(p0, p2),
+                    cb = v_sub(p1, p2);
+  V3t<double> g[4];
+  if (v_dot(da, v_cross(db, dc)) > 0.0) {
+    g[0] = v_cross(db, dc); g[1] = v_cross(dc, da); g[2] = v_cross(da, db); g[3] = v_cross(cb, ca);
+  } else {
+    g[0] = v_cross(dc, db); g[1] = v_cross(da, dc); g[2] = v_cross(db, da); g[3] = v_cross(ca, cb);
+  }
+  const double f = 1.0 / (36.0 * tet_vol(p0, p1, p2, p3));
+  for (int a = 0; a < 4; a++) {
+    const double Ba[3] = {g[a].x, g[a].y, g[a].z};
+    for (int b = a; b < 4; b++) {
+      const double Bb[3] = {g[b].x, g[b].y, g[b].z};
+      // K_ab(i, j), row i of node a, column j of node b
+      double Kab[9];
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+          double v;
+          if (i == j) {
+            const int j1 = (i + 1) % 3, j2 = (i + 2) % 3;
+            const int lo = j1 < j2 ? j1 : j2, hi = j1 < j2 ? j2 : j1;
+            v = D0 * Ba[i] * Bb[i] + D2 * (Ba[lo] * Bb[lo] + Ba[hi] * Bb[hi]);
+          } else {
+            v = D1 * Ba[i] * Bb[j] + D2 * Ba[j] * Bb[i];
+          }
+          Kab[3 * i + j] = v * f;
+        }
+      for (int i = 0; i < 3; i++) {
+        const int p = 3 * a + i, dp = p * 12 - (p * (p - 1)) / 2;   // packed index of (p, p)
+        if (a == b) {
+          for (int j = i; j < 3; j++) k78[(size_t)(dp + j - i) * ne + e] = Kab[3 * i + j];
+        } else {
+          for (int j = 0; j < 3; j++) k78[(size_t)(dp + 3 * b + j - p) * ne + e] = Kab[3 * i + j];
+        }
+      }
+    }
+  }
+}
+
+od_status launch_hooke(Scene* s, double youngs, double poisson, double* Kh) {
+  const int T = 128;
+  cudaStream_t st = s->ctx->stream;
+  const double lambda = poisson * youngs / ((1.0 + poisson) * (1.0 - 2.0 * poisson));
+  const double mu = youngs / (2.0 * (1.0 + poisson));
+  OD_CUDA(cudaMemsetAsync(Kh, 0, sizeof(double) * std::max(1, s->nvals), st));
+  if (s->n_tets == 0) return OD_OK;
+  OD_KL(s);
+  hooke_stage_kernel<<<nblk(s->n_tets, T), T, 0, st>>>(s->n_tets, s->tets, s->X, lambda + 2.0 * mu, lambda, mu,
+                                                      s->stage_k);
+  if (s->gat_kptr) {
+    if (s->nvals > 0) {
+      OD_KL(s);
+      gather_kernel<<<nblk(s->nvals, 256), 256, 0, st>>>(s->nvals, s->gat_kptr, s->gat_ksrc, s->stage_k, Kh, 0,
+                                                         nullptr, nullptr, nullptr, nullptr, 0);
+    }
+  } else {
+    for (size_t c = 0; c + 1 < s->color_off.size(); c++) {
+      const int e0 = s->color_off[c], e1 = s->color_off[c + 1];
+      if (e1 <= e0) continue;
+      OD_KL(s);
+      scatter_kernel<<<nblk(78LL * (e1 - e0), 256), 256, 0, st>>>(e0, e1 - e0, s->n_tets, s->stage_k, nullptr,
+                                                                   s->emap, s->gdof, Kh, nullptr);
+    }
+  }
+  OD_CUDA(cudaGetLastError());
+  return OD_OK;
+}
+
 static int vol_slot(const Scene* s) {
   return s->mat.kind == OD_MATERIAL_COROTATIONAL || s->mat.kind == OD_MATERIAL_COROTATIONAL_PLASTIC ? 99 : 21;
 }

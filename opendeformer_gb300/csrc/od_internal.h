@@ -69,6 +69,8 @@ struct Pcg {
   double* partial = nullptr;    // 4 arrays of per-CTA partials
   SolveScalars* sc = nullptr;
   SolveScalars* sc_host = nullptr;  // pinned mirror
+  unsigned long long* prof = nullptr;       // persistent solve's phase times (profiling), kPcgProfSlots
+  unsigned long long* prof_host = nullptr;  // pinned mirror
   int grid = 0;
   // preconditioner
   double* pinv = nullptr;       // Jacobi: n_pad; block-Jacobi: 9*nb
@@ -131,6 +133,11 @@ struct Pcg {
   SweepSys* sweep = nullptr;
 };
 
+// phases of a persistent PCG iteration timed while profiling: SpMV + p.q,
+// its grid-wide sum, the update (x, r, z, r.z, r.r), its sum, p = z + beta p,
+// the closing barrier; one more slot counts the iterations
+constexpr int kPcgPhases = 6;
+constexpr int kPcgProfSlots = kPcgPhases + 1;
 constexpr int kSliceRows = 10;      // block rows per slice (3 lanes each, 30 of a warp's 32)
 constexpr int kSliceWindow = 320;   // rows sorted by length inside windows of this many rows
 constexpr int kMaxLocalScenes = 32; // scenes one CTA of the inner FP32 solve may span
@@ -293,6 +300,8 @@ struct Ctx {
   double mix_spmv_ms = 0.0;
   double mix_spmv_work_ms = 0.0;
   double mix_spmv_bytes = 0.0;
+  double pcg_phase_ms[kPcgPhases] = {};  // persistent PCG phases (CTA 0, profiling)
+  long long pcg_phase_iters = 0;
   int profiling = 0;
   std::vector<cudaEvent_t> ev_pool;   // event pairs for SpMV timing
 };
@@ -472,6 +481,7 @@ void ric_factor(const RicColumns& A, const double* values, double eps, double re
 od_status launch_precompute(Scene* s);
 od_status launch_mass(Scene* s);
 od_status launch_eval(Scene* s, bool zero_first);       // K, fint at current u
+od_status launch_hooke(Scene* s, double youngs, double poisson, double* Kh);  // linear K, reference layout
 od_status launch_element_values(Scene* s, double* d_k78, double* d_f12);
 od_status launch_loads(Scene* s, const double* body, int n_facets_total, double traction_scale);
 // multi-scene element evaluation: zero K (values) and f_int (padded DOFs),

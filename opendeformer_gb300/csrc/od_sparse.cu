@@ -523,7 +523,8 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
     int nb, const int* __restrict__ rp, const int* __restrict__ col, const TA* __restrict__ A,
     const double* __restrict__ b, double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
     double* __restrict__ p, double* __restrict__ q, int pkind, const double* __restrict__ pinv,
-    double* __restrict__ part, double tol, int max_iter, SolveScalars* sc, GridBarrier* gb) {
+    double* __restrict__ part, double tol, int max_iter, SolveScalars* sc, GridBarrier* gb,
+    unsigned long long* __restrict__ prof) {
   constexpr int NR = GPW > 0 ? GPW : 1;
   const int G = gridDim.x;
   double* part_1 = part;          // one-value reductions (p.q, residual)
@@ -587,7 +588,20 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
   int it = 0;
   int status = isfinite(rr) ? OD_OK : OD_ERR_NAN;
 
+  // profiling (prof != nullptr): CTA 0 stamps the phases of every iteration
+  // (its own work, then its wait in the grid-wide sum or barrier that ends
+  // the phase) into prof[0..5]; prof[6] counts the iterations
+  const bool timer = prof && blockIdx.x == 0 && threadIdx.x == 0;
+  unsigned long long t_prev = 0;
+  auto stamp = [&](int slot) {
+    if (!timer) return;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (slot >= 0) prof[slot] += t - t_prev;
+    t_prev = t;
+  };
   while (status == OD_OK && it < max_iter && rr > eps) {
+    stamp(-1);
     // ---- q = A p; p.q
     double pq = 0.0;
     {
@@ -602,8 +616,10 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
         }
       }
     }
+    stamp(0);
     double v1[1] = {pq};
     if (!grid_sums<1>(v1, part_1, gb)) return;
+    stamp(1);
     const double alpha = rz / v1[0];
     // ---- x += alpha p; r -= alpha q; z = M^-1 r; r.z, r.r
     double rzn = 0.0, rrn = 0.0;
@@ -632,8 +648,10 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
         }
       }
     }
+    stamp(2);
     double v2[2] = {rzn, rrn};
     if (!grid_sums<2>(v2, part_2, gb)) return;
+    stamp(3);
     const double rz_new = v2[0];
     rr = v2[1];
     const double beta = rz_new / rz;
@@ -651,7 +669,10 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
         }
       }
     }
+    stamp(4);
     if (!grid_barrier(gb)) return;
+    stamp(5);
+    if (timer) prof[6] += 1;
   }
   // ---- write back x, then the true residual ||b - A x||^2
   if (GPW > 0) {
@@ -2143,6 +2164,12 @@ od_status pcg_alloc(Scene* s) {
   OD_CUDA(cudaMalloc(&P.gbar, sizeof(GridBarrier)));
   OD_CUDA(cudaMemset(P.gbar, 0, sizeof(GridBarrier)));
   OD_CUDA(cudaMallocHost(&P.timeout_host, sizeof(int)));
+  // the device counters only grow; the host keeps the last copy read (second
+  // half of prof_host) and takes differences
+  OD_CUDA(cudaMalloc(&P.prof, kPcgProfSlots * sizeof(unsigned long long)));
+  OD_CUDA(cudaMemset(P.prof, 0, kPcgProfSlots * sizeof(unsigned long long)));
+  OD_CUDA(cudaMallocHost(&P.prof_host, 2 * kPcgProfSlots * sizeof(unsigned long long)));
+  std::memset(P.prof_host, 0, 2 * kPcgProfSlots * sizeof(unsigned long long));
   // co-resident CTAs for the cooperative solve: one 768-thread CTA per SM
   // (fewest arrivals per grid barrier; the round-robin group mapping keeps
   // every SM's FP64 pipe equally loaded)
@@ -2176,6 +2203,8 @@ void pcg_free(Scene* s) {
   sweep_free(P.sweep);
   if (P.sc_host) cudaFreeHost(P.sc_host);
   if (P.timeout_host) cudaFreeHost(P.timeout_host);
+  cudaFree(P.prof);
+  if (P.prof_host) cudaFreeHost(P.prof_host);
   P = Pcg();
 }
 
@@ -2194,6 +2223,9 @@ static od_status pcg_finish(Scene* s, const double* d_b, double* d_x, double shi
     OD_CUDA(cudaGetLastError());
   }
   OD_CUDA(cudaMemcpyAsync(P.sc_host, P.sc, sizeof(SolveScalars), cudaMemcpyDeviceToHost, strm));
+  if (timed_persistent)
+    OD_CUDA(cudaMemcpyAsync(P.prof_host, P.prof, kPcgProfSlots * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                            strm));
   int timeout = 0;
   if (P.gbar) OD_CUDA(cudaMemcpyAsync(P.timeout_host, &((GridBarrier*)P.gbar)->timeout, sizeof(int),
                                       cudaMemcpyDeviceToHost, strm));
@@ -2206,6 +2238,10 @@ static od_status pcg_finish(Scene* s, const double* d_b, double* d_x, double shi
     s->ctx->pcg_kernel_ms += ms;
     s->ctx->pcg_kernel_launches++;
     s->ctx->pcg_kernel_iters += h.iter;
+    unsigned long long* last = P.prof_host + kPcgProfSlots;
+    for (int k = 0; k < kPcgPhases; k++) s->ctx->pcg_phase_ms[k] += 1e-6 * (double)(P.prof_host[k] - last[k]);
+    s->ctx->pcg_phase_iters += (long long)(P.prof_host[kPcgPhases] - last[kPcgPhases]);
+    for (int k = 0; k < kPcgProfSlots; k++) last[k] = P.prof_host[k];
   }
   od_status status = (od_status)h.status;
   if (timeout) { status = OD_ERR_DEVICE_TIMEOUT; set_error("PCG grid barrier timed out"); }
@@ -2820,12 +2856,14 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
     int pkv = pk;
     void* args[] = {(void*)&nb, (void*)&rpp, (void*)&colp, (void*)&Ap, (void*)&d_b, (void*)&xp, (void*)&P.r,
                     (void*)&P.z, (void*)&P.p, (void*)&P.q, (void*)&pkv, (void*)&P.pinv, (void*)&P.partial,
-                    (void*)&tol, (void*)&maxit, (void*)&P.sc, (void*)&gbp};
+                    (void*)&tol, (void*)&maxit, (void*)&P.sc, (void*)&gbp, nullptr};
     void* fn = need <= 1 ? (void*)pcg_persistent_kernel<double, 1>
              : need <= 2 ? (void*)pcg_persistent_kernel<double, 2>
              : need <= 4 ? (void*)pcg_persistent_kernel<double, 4>
                          : (void*)pcg_persistent_kernel<double, 0>;
     const bool prof = s->ctx->profiling && s->ctx->ev_pool.size() >= 2;
+    unsigned long long* profp = prof ? P.prof : nullptr;
+    args[17] = (void*)&profp;
     if (prof) OD_CUDA(cudaEventRecord(s->ctx->ev_pool[0], strm));
     OD_KL(s);
     OD_CUDA(cudaLaunchCooperativeKernel(fn, dim3(G2), dim3(kPThreads), args, 0, strm));

@@ -70,7 +70,8 @@ FILES = {
                  "corotationalHyperelastic.cpp", "invertibleHyperelastic.h",
                  "invertibleHyperelastic.cpp", "invertibleNeoHookean.h",
                  "invertibleNeoHookean.cpp", "invertibleStVK.h",
-                 "invertibleStVK.cpp", "corotationalPlastic.h", "corotationalPlastic.cpp"],
+                 "invertibleStVK.cpp", "corotationalPlastic.h", "corotationalPlastic.cpp",
+                 "hooke.h", "hooke.cpp"],
     "solver": ["cgSolver.h", "cgSolver.cpp", "jacobiPreconditioner.h",
                "jacobiPreconditioner.cpp", "inCholeskyPreconditioner.h",
                "inCholeskyPreconditioner.cpp", "inLDLTPreconditioner.h",

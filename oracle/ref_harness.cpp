@@ -54,6 +54,7 @@
 #include "invertibleNeoHookean.h"
 #include "invertibleStVK.h"
 #include "corotationalPlastic.h"
+#include "hooke.h"
 #include "preconditioner.h"
 #include "linearSolver.h"
 #include "cgSolver.h"
@@ -317,6 +318,31 @@ void odref_plastic_state(void* p, double* out) {
   // (nonlinearImplicitBackwardEuler.h:72); the other paths use the scene's
   const double* pre = (const double*)(s->be ? s->be->materialCache.getMemoryBlock() : s->cache.getMemoryBlock());
   memcpy(out, pre + (size_t)s->n_tets * (90 + 9 + 12), sizeof(double) * 9 * (size_t)s->n_tets);
+}
+
+// The modal path's matrices (LinearNewmark::LinearNewmark,
+// linearNewmark.cpp:33-38): which == 0 the Hooke stiffness
+// (HookeMaterial::generateStiffnessMatrix, hooke.cpp:18-60), which == 1 the
+// consistent mass (MechMaterial::generateMassMatrix into the scalar
+// assembler), both the lower triangle by columns from the reference's
+// assembler; returns the entry count (NULL arrays: count only).
+int odref_linear_csc(void* p, int which, double youngs, double poisson, int* pcol, int* rows, double* values) {
+  RefScene* s = (RefScene*)p;
+  SparseMatrixAssembler a(s->dofs);
+  HookeMaterial h(s->material->getDensity(), youngs, poisson);
+  if (which == 0) h.generateStiffnessMatrix(s->mesh, s->indexer, a);
+  else h.generateMassMatrix(s->mesh, s->indexer, a);
+  int nnz = 0;
+  for (int c = 0; c < s->dofs; c++) {
+    if (pcol) pcol[c] = nnz;
+    for (const auto& e : a.rowEntries[c]) {
+      if (rows) rows[nnz] = e.first;
+      if (values) values[nnz] = e.second;
+      nnz++;
+    }
+  }
+  if (pcol) pcol[s->dofs] = nnz;
+  return nnz;
 }
 
 void odref_mass(void* p, double* values) {

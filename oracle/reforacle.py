@@ -76,6 +76,8 @@ def lib():
         L.odref_relabel.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip]
         L.odref_plane_damping.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_double, C.c_int, _ip, _dp]
         L.odref_be_plane_damping.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double, C.c_int, _ip]
+        L.odref_linear_csc.restype = C.c_int
+        L.odref_linear_csc.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, _ip, _ip, _dp]
         _lib = L
     return _lib
 
@@ -171,6 +173,18 @@ class RefScene:
         v = np.zeros(self.n_values)
         lib().odref_mass(self.h, _d(v))
         return v
+
+    def linear_csc(self, which, youngs, poisson):
+        """The modal path's Hooke stiffness (which="K") or consistent mass
+        (which="M") from the reference's scalar assembler: (pcol, rows,
+        values) of the lower triangle by columns."""
+        w = {"K": 0, "M": 1}[which]
+        nnz = lib().odref_linear_csc(self.h, w, youngs, poisson, None, None, None)
+        pcol = np.zeros(self.dofs + 1, np.int32)
+        rows = np.zeros(nnz, np.int32)
+        vals = np.zeros(nnz)
+        lib().odref_linear_csc(self.h, w, youngs, poisson, _i(pcol), _i(rows), _d(vals))
+        return pcol, rows, vals
 
     def spmdv(self, values, x, y=None):
         values = np.ascontiguousarray(values, dtype=np.float64)

@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <array>
 #include <atomic>
+#include <chrono>
 #include <climits>
 #include <cstdint>
 #include <functional>
@@ -133,19 +134,82 @@ double rel_diff(const std::vector<double>& a, const std::vector<double>& b) {
   return den > 0.0 ? sqrt(num / den) : sqrt(num);
 }
 
+// wall-clock time spent in one seam (a material or solver call) over a loop
+struct SeamClock {
+  double ms = 0.0;
+  int calls = 0;
+  double per_call() const { return calls ? ms / calls : 0.0; }
+};
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// forwards every call to the material it wraps and times
+// generateMatrixAndVirtualWorks, the seam a drop-in material replaces
+class TimedMaterial : public FullOrderNonlinearMaterial<Mat> {
+ public:
+  TimedMaterial(const Reference<FullOrderNonlinearMaterial<Mat>>& m, Scalar rho, SeamClock* c)
+      : FullOrderNonlinearMaterial(rho, MarterialType(Marterial_Isotropic | Marterial_Invertible)), inner(m),
+        clock(c) {}
+  FullOrderNonlinearMaterialCache getPrecomputes(const Reference<Mesh>& mesh) const override {
+    return inner->getPrecomputes(mesh);
+  }
+  void generateMatrixAndVirtualWorks(const Reference<Mesh>& mesh, const Reference<NodeIndexer>& indexer,
+                                     const FullOrderNonlinearMaterialCache& cache,
+                                     const SparseSymMatrixIndicesPerElementCache& matrixIndices, Mat& matrix,
+                                     Scalar* vws) const override {
+    const double t0 = now_ms();
+    inner->generateMatrixAndVirtualWorks(mesh, indexer, cache, matrixIndices, matrix, vws);
+    clock->ms += now_ms() - t0;
+    clock->calls++;
+  }
+  Reference<FullOrderNonlinearMaterial<Mat>> inner;
+  SeamClock* clock;
+};
+
+// forwards to the solver it wraps and times solveLinearSystem
+class TimedSolver : public LinearSolver<Mat> {
+ public:
+  TimedSolver(const Reference<LinearSolver<Mat>>& s, SeamClock* c) : inner(s), clock(c) {}
+  void resetLinearSystem(const Mat* m) override {
+    mat = m;
+    inner->resetLinearSystem(m);
+  }
+  void solveLinearSystem(const Scalar* rhs, Scalar* result) override {
+    const double t0 = now_ms();
+    inner->solveLinearSystem(rhs, result);
+    clock->ms += now_ms() - t0;
+    clock->calls++;
+  }
+  Reference<LinearSolver<Mat>> inner;
+  SeamClock* clock;
+};
+
+// times of one loop: the whole steps, and the material and solver seams
+struct LoopTimes {
+  SeamClock step, material, solver;
+};
+
 // the reference's backward Euler with the given material and solver
 std::vector<double> run_reference_loop(const Input& in, RefSetup& s,
                                        const Reference<FullOrderNonlinearMaterial<Mat>>& material,
-                                       const Reference<LinearSolver<Mat>>& solver) {
-  NonlinearImplicitBackwardEuler<Mat> be(s.dofs, in.p.alpha_m, in.p.beta_k, in.p.dt, s.mesh, s.indexer, material,
-                                         solver);
+                                       const Reference<LinearSolver<Mat>>& solver, LoopTimes* times = nullptr) {
+  LoopTimes scratch;
+  LoopTimes& t = times ? *times : scratch;
+  Reference<FullOrderNonlinearMaterial<Mat>> tm(new TimedMaterial(material, in.p.rho, &t.material));
+  Reference<LinearSolver<Mat>> ts(new TimedSolver(solver, &t.solver));
+  NonlinearImplicitBackwardEuler<Mat> be(s.dofs, in.p.alpha_m, in.p.beta_k, in.p.dt, s.mesh, s.indexer, tm, ts);
   Forcer f;
   Scalar g[3] = {in.p.g[0], in.p.g[1], in.p.g[2]};
   f.addBodyForce(s.mesh, g, s.indexer);
   be.setExternalVirtualWork(f);
   for (int k = 0; k < in.p.steps; k++) {
+    const double t0 = now_ms();
     be.runOneTimeStep();
     be.updateMeshVerticesDisplacements(s.indexer, s.mesh);
+    t.step.ms += now_ms() - t0;
+    t.step.calls++;
   }
   return displacements(s, in.p.n_nodes);
 }
@@ -201,11 +265,13 @@ od_scene* new_scene(od_ctx* ctx, const Input& in) {
 
 int main(int argc, char** argv) {
   if (argc < 3) {
-    fprintf(stderr, "usage: dropin_check <dir> <tolerance>\n");
+    fprintf(stderr, "usage: dropin_check <dir> <tolerance> [seams]\n");
     return 2;
   }
   const std::string dir = argv[1];
   const double tol_ok = atof(argv[2]);
+  // "seams": only A-D, whose times are the cost of each seam at this size
+  const bool seams_only = argc > 3 && std::string(argv[3]) == "seams";
   Input in;
   {
     FILE* f = fopen((dir + "/params.txt").c_str(), "r");
@@ -240,8 +306,9 @@ int main(int argc, char** argv) {
   };
 
   // A: the reference as shipped
+  LoopTimes ta, tb, tc, td;
   RefSetup sa = make_setup(in);
-  const std::vector<double> ua = run_reference_loop(in, sa, reference_material(in), jacobi_cg());
+  const std::vector<double> ua = run_reference_loop(in, sa, reference_material(in), jacobi_cg(), &ta);
 
   // B: GpuMaterial inside the reference integrator
   od_scene* sb_scene = new_scene(ctx, in);
@@ -250,14 +317,14 @@ int main(int argc, char** argv) {
   // below keep them alive until their statuses are read
   auto* gm = new od_dropin::GpuMaterial(sb_scene, in.p.rho, MarterialType(Marterial_Isotropic | Marterial_Invertible));
   Reference<FullOrderNonlinearMaterial<Mat>> gm_ref(gm);
-  const std::vector<double> ub = run_reference_loop(in, sb, gm_ref, jacobi_cg());
+  const std::vector<double> ub = run_reference_loop(in, sb, gm_ref, jacobi_cg(), &tb);
 
   // C: GpuCGSolver inside the reference integrator
   od_scene* sc_scene = new_scene(ctx, in);
   RefSetup sc = make_setup(in);
   auto* gcg = new od_dropin::GpuCGSolver(sc_scene, in.p.tol, in.p.max_iter, OD_PRECOND_JACOBI);
   Reference<LinearSolver<Mat>> gcg_ref(gcg);
-  const std::vector<double> uc = run_reference_loop(in, sc, reference_material(in), gcg_ref);
+  const std::vector<double> uc = run_reference_loop(in, sc, reference_material(in), gcg_ref, &tc);
 
   // D: GpuIntergrator in place of the integrator
   od_scene* sd_scene = new_scene(ctx, in);
@@ -281,11 +348,29 @@ int main(int argc, char** argv) {
     gi.setExternalVirtualWork(f);
     check(gi.last_status, "setExternalVirtualWork");
     for (int k = 0; k < in.p.steps; k++) {
+      const double t0 = now_ms();
       gi.runOneTimeStep();
       check(gi.last_status, "runOneTimeStep");
       gi.updateMeshVerticesDisplacements(sd.indexer, sd.mesh);
+      td.step.ms += now_ms() - t0;
+      td.step.calls++;
     }
     ud = displacements(sd, in.p.n_nodes);
+  }
+  // per step: the whole step, the material call and the solver call (ms)
+  printf("seams_ms reference step %.3f material %.3f solver %.3f | GpuMaterial step %.3f material %.3f | "
+         "GpuCGSolver step %.3f solver %.3f (%d iterations) | GpuIntergrator step %.3f\n",
+         ta.step.per_call(), ta.material.per_call(), ta.solver.per_call(), tb.step.per_call(),
+         tb.material.per_call(), tc.step.per_call(), tc.solver.per_call(),
+         tc.solver.calls ? gcg->stats.iterations : 0, td.step.per_call());
+  if (seams_only) {
+    check(gm->last_status, "GpuMaterial");
+    check(gcg->last_status, "GpuCGSolver");
+    const double eb = rel_diff(ub, ua), ec = rel_diff(uc, ua), ed = rel_diff(ud, ua);
+    printf("material %.3e solver %.3e integrator %.3e\n", eb, ec, ed);
+    for (od_scene* s : {sb_scene, sc_scene, sd_scene}) od_scene_destroy(s);
+    od_ctx_destroy(ctx);
+    return !bad && eb <= tol_ok && ec <= tol_ok && ed <= tol_ok ? 0 : 1;
   }
 
   // E, F: threshold incomplete Cholesky, the reference's and the drop-in

@@ -35,8 +35,15 @@ the GPU path against them.  Cases:
   horizontal one with whole elements below it), with a repeated element,
   and backward-Euler steps with the forcer re-applied every step.
 
-``--only NAME`` writes one group (plastic, ldlt, ic or damping; the full
-run writes all).
+* ``modal_<case>``: the modal linear Newmark path: Hooke stiffness and
+  consistent mass (scalar CSC from the reference's assembler), the lowest
+  eigenpairs (ARPACK shift-invert at 0 through scipy's eigsh: the
+  reference's ARPACK++/SuperLU binaries cannot run here), modal forces of a
+  gravity load and the reduced state and displacements after restated
+  LinearNewmark steps (oracle/modal.py).
+
+``--only NAME`` writes one group (plastic, ldlt, ic, damping or modal; the
+full run writes all).
 """
 from __future__ import annotations
 
@@ -215,6 +222,45 @@ def damping_case():
          be_params=np.array([1.0 / 60.0, 0.01, 0.001, 1e-10]), **out)
 
 
+MODAL = (1000.0, 1e5, 0.4)                       # rho, E, nu of the Hooke material
+MODAL_STEP = (0.25, 0.5, 0.01, 0.001, 1.0 / 60.0)  # beta, gamma, massDamp, stiffDamp, dt
+MODAL_STEPS = 25
+
+
+def modal_cases():
+    """LinearNewmark: K (Hooke) and M from the reference's scalar assembler,
+    the lowest eigenpairs by ARPACK in the reference's shift-invert mode
+    (scipy's eigsh, the reference links ARPACK++/ARPACK/SuperLU binaries that
+    cannot run here), modal forces of a gravity load through the reference's
+    Forcer, and the restated per-mode Newmark steps (oracle/modal.py)."""
+    from oracle import modal as MO
+    rho, E, nu = MODAL
+    beta, gamma, am, bk, dt = MODAL_STEP
+    small = small_mesh()
+    grid = meshgen.tet_grid(8, 3, 3, h=0.05, jitter=0.1, seed=5, tets_per_cube=6)
+    cases = {"full": (small, meshgen.constrained_dofs_for_nodes(small.face_nodes(0, 0)), 6),
+             "partial": (small, partial_constraints(small), 6),
+             "grid": (grid, meshgen.constrained_dofs_for_nodes(grid.face_nodes(0, 0)), 12)}
+    for cname, (g, cd, r) in cases.items():
+        s = R.RefScene(g.X, g.tets, g.facets, cd, "corotational", rho, E, nu, 0.1)
+        kp, kr, kv = s.linear_csc("K", E, nu)
+        mp, mr, mv = s.linear_csc("M", E, nu)
+        K = MO.sym_from_lower_csc(kp, kr, kv, s.dofs)
+        M = MO.sym_from_lower_csc(mp, mr, mv, s.dofs)
+        lam, phi = MO.modes(K, M, r)
+        fext = s.loads(body=[0.0, 0.0, -9800.0])
+        o = MO.LinearNewmarkOracle(lam, phi, beta, gamma, am, bk, dt)
+        o.set_external(fext)
+        f_modal = o.f.copy()
+        o.step(MODAL_STEPS)
+        u = MO.to_nodes(o.full_order(), g.n_nodes, cd)
+        vel = MO.to_nodes(o.full_order(o.v), g.n_nodes, cd)
+        save(f"modal_{cname}", X=g.X, tets=g.tets, facets=g.facets, cdofs=cd, material=np.array(MODAL),
+             step_params=np.array(MODAL_STEP), steps=MODAL_STEPS, n_modes=r, K_pcol=kp, K_rows=kr, K_vals=kv,
+             M_pcol=mp, M_rows=mr, M_vals=mv, lam=lam, phi=phi, fext=fext, f_modal=f_modal, d=o.d, v=o.v,
+             a=o.a, u=u, vel=vel)
+
+
 def main():
     only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
     if only == "ic":
@@ -233,8 +279,12 @@ def main():
         ldlt_cases()
         print("golden fixtures ldlt_* written to", OUT)
         return
+    if only == "modal":
+        modal_cases()
+        print("golden fixtures modal_* written to", OUT)
+        return
     if only is not None:
-        raise SystemExit(f"--only {only}: single groups are 'plastic', 'ldlt', 'ic' and 'damping'")
+        raise SystemExit(f"--only {only}: single groups are 'plastic', 'ldlt', 'ic', 'damping' and 'modal'")
     g = small_mesh()
     cases = {"full": meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0)),
              "partial": partial_constraints(g)}
@@ -313,6 +363,7 @@ def main():
     ldlt_cases()
     ic_cases()
     damping_case()
+    modal_cases()
     print("golden fixtures written to", OUT)
 
 

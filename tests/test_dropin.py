@@ -1,6 +1,7 @@
 """The C++ drop-in classes (include/od_gb300_dropin.hpp) compile against the
 reference's own interfaces: every override matches a virtual of the
-reference's Material / LinearSolver / Preconditioner / Intergrator seams,
+reference's Material / LinearSolver / Preconditioner / Intergrator seams
+(the modal LinearNewmark's included),
 and the private-member accessors resolve.  Compiled against the patched
 copy of the reference headers that oracle/build_ref.py makes (skipped where
 that copy is absent); nothing runs, so no GPU is needed.
@@ -42,6 +43,12 @@ void use(od_scene* s, const od_integrator_params& p, ODER::BlockedSymSpMatrix& A
   in->updateMeshVerticesDisplacements(ix, mesh);
   in->getMeshVerticesVelocities(ix, mesh, vel);
   in->clearExternalDampingForceMatrix();
+  od_dropin::GpuLinearNewmark lm(s, 0.25, 0.5, 8, 0.01, 0.001, 1.0 / 60, 1e5, 0.4);
+  ODER::Intergrator* modal = &lm;
+  modal->setExternalVirtualWork(f);
+  modal->runOneTimeStep();
+  modal->updateMeshVerticesDisplacements(ix, mesh);
+  modal->getMeshVerticesVelocities(ix, mesh, vel);
 }
 """
 
