@@ -1261,8 +1261,13 @@ def run_gpu(args, wl):
         names = ("spmv_pq", "pq_sum", "update_rz_rr", "rz_rr_sum", "direction", "barrier")
         phases = {k: round(1000.0 * counters.pcg_phase_ms[j] / counters.pcg_phase_iterations, 3)
                   for j, k in enumerate(names)}
+        for j, k in enumerate(("spmv_pq", "update_rz_rr", "direction")):
+            phases[f"{k}_cta_max"] = round(1000.0 * counters.pcg_work_max_ms[j] / counters.pcg_phase_iterations, 3)
+            phases[f"{k}_cta_mean"] = round(1000.0 * counters.pcg_work_mean_ms[j] / counters.pcg_phase_iterations,
+                                            3)
         phases["note"] = ("us per PCG iteration on the clock of CTA 0 (%globaltimer); a *_sum or barrier "
-                          "phase includes the wait for the slowest CTA")
+                          "phase includes the wait for the slowest CTA; *_cta_max / *_cta_mean: every CTA's "
+                          "own work in the phase (its warps, no waits), slowest CTA per solve and mean")
         roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": nbytes,

@@ -171,6 +171,10 @@ typedef struct od_counters {
      before the next SpMV */
   double pcg_phase_ms[6];
   long long pcg_phase_iterations;
+  /* the same solves, each CTA's own SpMV, update and direction work (its warps'
+     time, without the waits): per solve the slowest CTA's and the mean over CTAs */
+  double pcg_work_max_ms[3];
+  double pcg_work_mean_ms[3];
 } od_counters;
 
 typedef struct od_scene_info {

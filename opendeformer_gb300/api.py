@@ -90,7 +90,8 @@ class od_counters(C.Structure):
                 ("sweep_factors", C.c_longlong), ("sweep_factor_ms", C.c_double), ("sweep_nnz", C.c_longlong),
                 ("sweep_applies", C.c_longlong), ("sweep_apply_ms", C.c_double), ("sweep_apply_bytes", C.c_double),
                 ("sweep_levels", C.c_longlong), ("pcg_phase_ms", C.c_double * 6),
-                ("pcg_phase_iterations", C.c_longlong)]
+                ("pcg_phase_iterations", C.c_longlong), ("pcg_work_max_ms", C.c_double * 3),
+                ("pcg_work_mean_ms", C.c_double * 3)]
 
 
 class od_scene_info(C.Structure):

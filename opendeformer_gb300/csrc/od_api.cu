@@ -199,6 +199,10 @@ od_status od_ctx_get_counters(od_ctx* ctx, od_counters* out) {
   out->mix_spmv_work_ms = ctx->c.mix_spmv_work_ms;
   for (int k = 0; k < od::kPcgPhases; k++) out->pcg_phase_ms[k] = ctx->c.pcg_phase_ms[k];
   out->pcg_phase_iterations = ctx->c.pcg_phase_iters;
+  for (int k = 0; k < 3; k++) {
+    out->pcg_work_max_ms[k] = ctx->c.pcg_work_max_ms[k];
+    out->pcg_work_mean_ms[k] = ctx->c.pcg_work_mean_ms[k];
+  }
   out->mix_fallbacks = ctx->c.mix_fallbacks;
   out->mix_spmv_bytes = ctx->c.mix_spmv_bytes;
   out->sweep_factors = ctx->c.sweep_factors;
@@ -220,6 +224,7 @@ od_status od_ctx_reset_counters(od_ctx* ctx) {
   ctx->c.mix_spmv_ms = ctx->c.mix_spmv_bytes = ctx->c.mix_spmv_work_ms = 0.0;
   for (double& v : ctx->c.pcg_phase_ms) v = 0.0;
   ctx->c.pcg_phase_iters = 0;
+  for (int k = 0; k < 3; k++) ctx->c.pcg_work_max_ms[k] = ctx->c.pcg_work_mean_ms[k] = 0.0;
   ctx->c.sweep_factors = ctx->c.sweep_nnz = ctx->c.sweep_applies = ctx->c.sweep_levels = 0;
   ctx->c.sweep_factor_ms = ctx->c.sweep_apply_ms = ctx->c.sweep_apply_bytes = 0.0;
   return OD_OK;

@@ -69,7 +69,8 @@ struct Pcg {
   double* partial = nullptr;    // 4 arrays of per-CTA partials
   SolveScalars* sc = nullptr;
   SolveScalars* sc_host = nullptr;  // pinned mirror
-  unsigned long long* prof = nullptr;       // persistent solve's phase times (profiling), kPcgProfSlots
+  unsigned long long* prof = nullptr;       // persistent solve's phase times (profiling), prof_slots
+  int prof_slots = 0;                       // kPcgProfSlots + 3 per CTA of the cooperative grid
   unsigned long long* prof_host = nullptr;  // pinned mirror
   int grid = 0;
   // preconditioner
@@ -301,6 +302,8 @@ struct Ctx {
   double mix_spmv_work_ms = 0.0;
   double mix_spmv_bytes = 0.0;
   double pcg_phase_ms[kPcgPhases] = {};  // persistent PCG phases (CTA 0, profiling)
+  double pcg_work_max_ms[3] = {};       // per solve: slowest CTA's own SpMV / update / direction work
+  double pcg_work_mean_ms[3] = {};      // per solve: mean over the CTAs
   long long pcg_phase_iters = 0;
   int profiling = 0;
   std::vector<cudaEvent_t> ev_pool;   // event pairs for SpMV timing

@@ -467,7 +467,9 @@ __device__ __forceinline__ double warp_sum(double v) {
 // partials in a fixed order and broadcasts through shared memory.  Every
 // CTA obtains bitwise the same sums.  Returns false after a barrier timeout.
 template <int NV>
-__device__ __forceinline__ bool grid_sums(double (&v)[NV], double* __restrict__ part, GridBarrier* gb) {
+__device__ __forceinline__ bool grid_sums(double (&v)[NV], double* __restrict__ part, GridBarrier* gb,
+                                          unsigned long long* __restrict__ work = nullptr,
+                                          unsigned long long t0 = 0) {
   __shared__ double ws[NV][32];
   __shared__ double res[NV];
   __shared__ int ok_s;
@@ -479,6 +481,11 @@ __device__ __forceinline__ bool grid_sums(double (&v)[NV], double* __restrict__ 
     if (lane == 0) ws[j][w] = t;
   }
   __syncthreads();
+  if (work && threadIdx.x == 0) {  // profiling: this CTA's own share of the phase
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    work[blockIdx.x] += t - t0;
+  }
   if (w == 0) {
 #pragma unroll
     for (int j = 0; j < NV; j++) {
@@ -590,9 +597,12 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
 
   // profiling (prof != nullptr): CTA 0 stamps the phases of every iteration
   // (its own work, then its wait in the grid-wide sum or barrier that ends
-  // the phase) into prof[0..5]; prof[6] counts the iterations
+  // the phase) into prof[0..5]; prof[6] counts the iterations; every CTA b
+  // adds the time its own warps took for the SpMV, update and direction
+  // phases to prof[7 + k G + b], k = 0, 1, 2
   const bool timer = prof && blockIdx.x == 0 && threadIdx.x == 0;
-  unsigned long long t_prev = 0;
+  unsigned long long* cta_work = prof ? prof + kPcgProfSlots : nullptr;
+  unsigned long long t_prev = 0, t_phase = 0;
   auto stamp = [&](int slot) {
     if (!timer) return;
     unsigned long long t;
@@ -600,8 +610,12 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
     if (slot >= 0) prof[slot] += t - t_prev;
     t_prev = t;
   };
+  auto phase_start = [&]() {
+    if (prof && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_phase));
+  };
   while (status == OD_OK && it < max_iter && rr > eps) {
     stamp(-1);
+    phase_start();
     // ---- q = A p; p.q
     double pq = 0.0;
     {
@@ -618,9 +632,10 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
     }
     stamp(0);
     double v1[1] = {pq};
-    if (!grid_sums<1>(v1, part_1, gb)) return;
+    if (!grid_sums<1>(v1, part_1, gb, cta_work, t_phase)) return;
     stamp(1);
     const double alpha = rz / v1[0];
+    phase_start();
     // ---- x += alpha p; r -= alpha q; z = M^-1 r; r.z, r.r
     double rzn = 0.0, rrn = 0.0;
     {
@@ -650,7 +665,7 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
     }
     stamp(2);
     double v2[2] = {rzn, rrn};
-    if (!grid_sums<2>(v2, part_2, gb)) return;
+    if (!grid_sums<2>(v2, part_2, gb, cta_work ? cta_work + G : nullptr, t_phase)) return;
     stamp(3);
     const double rz_new = v2[0];
     rr = v2[1];
@@ -658,6 +673,7 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
     rz = rz_new;
     it++;
     if (!isfinite(rr) || !isfinite(beta)) status = OD_ERR_NAN;
+    phase_start();
     // ---- p = z + beta p
     {
       OD_GROUP_LOOP(k, g) {
@@ -670,6 +686,14 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
       }
     }
     stamp(4);
+    if (cta_work) {  // profiling: this CTA's own share of the direction phase
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        cta_work[2 * G + blockIdx.x] += t - t_phase;
+      }
+    }
     if (!grid_barrier(gb)) return;
     stamp(5);
     if (timer) prof[6] += 1;
@@ -2166,10 +2190,11 @@ od_status pcg_alloc(Scene* s) {
   OD_CUDA(cudaMallocHost(&P.timeout_host, sizeof(int)));
   // the device counters only grow; the host keeps the last copy read (second
   // half of prof_host) and takes differences
-  OD_CUDA(cudaMalloc(&P.prof, kPcgProfSlots * sizeof(unsigned long long)));
-  OD_CUDA(cudaMemset(P.prof, 0, kPcgProfSlots * sizeof(unsigned long long)));
-  OD_CUDA(cudaMallocHost(&P.prof_host, 2 * kPcgProfSlots * sizeof(unsigned long long)));
-  std::memset(P.prof_host, 0, 2 * kPcgProfSlots * sizeof(unsigned long long));
+  P.prof_slots = kPcgProfSlots + 3 * P.grid;
+  OD_CUDA(cudaMalloc(&P.prof, P.prof_slots * sizeof(unsigned long long)));
+  OD_CUDA(cudaMemset(P.prof, 0, P.prof_slots * sizeof(unsigned long long)));
+  OD_CUDA(cudaMallocHost(&P.prof_host, 2 * P.prof_slots * sizeof(unsigned long long)));
+  std::memset(P.prof_host, 0, 2 * P.prof_slots * sizeof(unsigned long long));
   // co-resident CTAs for the cooperative solve: one 768-thread CTA per SM
   // (fewest arrivals per grid barrier; the round-robin group mapping keeps
   // every SM's FP64 pipe equally loaded)
@@ -2224,7 +2249,7 @@ static od_status pcg_finish(Scene* s, const double* d_b, double* d_x, double shi
   }
   OD_CUDA(cudaMemcpyAsync(P.sc_host, P.sc, sizeof(SolveScalars), cudaMemcpyDeviceToHost, strm));
   if (timed_persistent)
-    OD_CUDA(cudaMemcpyAsync(P.prof_host, P.prof, kPcgProfSlots * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+    OD_CUDA(cudaMemcpyAsync(P.prof_host, P.prof, P.prof_slots * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                             strm));
   int timeout = 0;
   if (P.gbar) OD_CUDA(cudaMemcpyAsync(P.timeout_host, &((GridBarrier*)P.gbar)->timeout, sizeof(int),
@@ -2238,10 +2263,23 @@ static od_status pcg_finish(Scene* s, const double* d_b, double* d_x, double shi
     s->ctx->pcg_kernel_ms += ms;
     s->ctx->pcg_kernel_launches++;
     s->ctx->pcg_kernel_iters += h.iter;
-    unsigned long long* last = P.prof_host + kPcgProfSlots;
+    unsigned long long* last = P.prof_host + P.prof_slots;
     for (int k = 0; k < kPcgPhases; k++) s->ctx->pcg_phase_ms[k] += 1e-6 * (double)(P.prof_host[k] - last[k]);
     s->ctx->pcg_phase_iters += (long long)(P.prof_host[kPcgPhases] - last[kPcgPhases]);
-    for (int k = 0; k < kPcgProfSlots; k++) last[k] = P.prof_host[k];
+    // per-CTA own work of this solve: the slowest CTA and the mean
+    const int G2 = P.coop_grid;
+    for (int k = 0; k < 3 && G2 > 0; k++) {
+      double mx = 0.0, sum = 0.0;
+      for (int b = 0; b < G2; b++) {
+        const size_t i = kPcgProfSlots + (size_t)k * G2 + b;
+        const double d = 1e-6 * (double)(P.prof_host[i] - last[i]);
+        mx = std::max(mx, d);
+        sum += d;
+      }
+      s->ctx->pcg_work_max_ms[k] += mx;
+      s->ctx->pcg_work_mean_ms[k] += sum / G2;
+    }
+    for (int k = 0; k < P.prof_slots; k++) last[k] = P.prof_host[k];
   }
   od_status status = (od_status)h.status;
   if (timeout) { status = OD_ERR_DEVICE_TIMEOUT; set_error("PCG grid barrier timed out"); }
