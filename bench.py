@@ -1179,6 +1179,13 @@ def run_gpu(args, wl):
     wall = time.perf_counter() - t0
     ctx.set_profiling(False)
     counters = ctx.counters()
+    # one more step, untimed, with the one-launch PCG's per-iteration phase
+    # timers on (they add clock reads and a CTA barrier to every iteration)
+    ctx.reset_counters()
+    ctx.set_profiling(2)
+    scene.step(1)
+    ctx.set_profiling(False)
+    phase_counters = ctx.counters()
     torch.cuda.synchronize()
     barrier()
     clocks = sampler.stop()
@@ -1257,17 +1264,19 @@ def run_gpu(args, wl):
                 "pipe_source": "ncu --set full capture of this kernel on this workload "
                                "(sm__pipe_fp64_cycles_active, of peak, active cycles)"}
     phases = None
-    if counters.pcg_phase_iterations:
+    pc = phase_counters
+    if pc.pcg_phase_iterations:
         names = ("spmv_pq", "pq_sum", "update_rz_rr", "rz_rr_sum", "direction", "barrier")
-        phases = {k: round(1000.0 * counters.pcg_phase_ms[j] / counters.pcg_phase_iterations, 3)
-                  for j, k in enumerate(names)}
+        phases = {k: round(1000.0 * pc.pcg_phase_ms[j] / pc.pcg_phase_iterations, 3) for j, k in enumerate(names)}
         for j, k in enumerate(("spmv_pq", "update_rz_rr", "direction")):
-            phases[f"{k}_cta_max"] = round(1000.0 * counters.pcg_work_max_ms[j] / counters.pcg_phase_iterations, 3)
-            phases[f"{k}_cta_mean"] = round(1000.0 * counters.pcg_work_mean_ms[j] / counters.pcg_phase_iterations,
-                                            3)
-        phases["note"] = ("us per PCG iteration on the clock of CTA 0 (%globaltimer); a *_sum or barrier "
-                          "phase includes the wait for the slowest CTA; *_cta_max / *_cta_mean: every CTA's "
-                          "own work in the phase (its warps, no waits), slowest CTA per solve and mean")
+            phases[f"{k}_cta_max"] = round(1000.0 * pc.pcg_work_max_ms[j] / pc.pcg_phase_iterations, 3)
+            phases[f"{k}_cta_mean"] = round(1000.0 * pc.pcg_work_mean_ms[j] / pc.pcg_phase_iterations, 3)
+        phases["iterations"] = pc.pcg_phase_iterations
+        phases["us_per_iteration_timed_steps"] = round(1000.0 * counters.pcg_ms / max(1, counters.pcg_iterations), 3)
+        phases["note"] = ("one extra step after the timed ones with the phase timers on: us per PCG iteration "
+                          "on the clock of CTA 0 (%globaltimer); a *_sum or barrier phase includes the wait for "
+                          "the slowest CTA; *_cta_max / *_cta_mean: every CTA's own work in the phase (its warps, "
+                          "no waits), slowest CTA per solve and mean; the timers themselves add about 2 us")
         roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": nbytes,

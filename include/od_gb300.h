@@ -187,6 +187,8 @@ typedef struct od_scene_info {
   int num_full_blocks;       /* device full-BSR block count (both triangles) */
   int num_colors;            /* element colours used by the atomic-free scatter */
   long long device_bytes;    /* device memory held by the scene */
+  int pcg_smem_bytes;        /* shared memory per CTA of the one-launch PCG when it keeps the
+                                matrix rows on chip (0: it reads them from L2 / HBM) */
 } od_scene_info;
 
 typedef struct od_ctx od_ctx;
@@ -215,8 +217,11 @@ od_status od_selftest_bounded_waits(od_ctx* ctx, int* barrier_timed_out, int* va
  * FP32; *fma_per_s receives multiply-adds per second (2 operations each),
  * *ms the launch time.  The roofline of the FP64 kernels. */
 od_status od_measure_fma_rate(od_ctx* ctx, int fp64, int iters, double* fma_per_s, double* ms);
-/* Counters (no reference counterpart).  With profiling on, every PCG SpMV
- * launch is bracketed by CUDA events on the context stream. */
+/* Counters (no reference counterpart).  enable = 1: every PCG launch is
+ * bracketed by CUDA events on the context stream (and the mixed solve's
+ * kernel records its phase times); 2: also the one-launch FP64 PCG's
+ * per-iteration phase timers (pcg_phase_ms, pcg_work_*), which add clock
+ * reads and a CTA barrier to every iteration; 0: off. */
 od_status od_ctx_set_profiling(od_ctx* ctx, int enable);
 od_status od_ctx_get_counters(od_ctx* ctx, od_counters* out);
 od_status od_ctx_reset_counters(od_ctx* ctx);

@@ -98,7 +98,7 @@ class od_scene_info(C.Structure):
     _fields_ = [("n_nodes", C.c_int), ("n_tets", C.c_int), ("n_facets", C.c_int), ("dofs", C.c_int),
                 ("num_block_columns", C.c_int), ("num_remained_columns", C.c_int),
                 ("num_row_indices", C.c_int), ("num_values", C.c_int), ("num_full_blocks", C.c_int),
-                ("num_colors", C.c_int), ("device_bytes", C.c_longlong)]
+                ("num_colors", C.c_int), ("device_bytes", C.c_longlong), ("pcg_smem_bytes", C.c_int)]
 
 
 class od_mixed_tuning(C.Structure):
@@ -454,8 +454,10 @@ class Context:
     def synchronize(self):
         _check(load_library().od_ctx_synchronize(self.h), "od_ctx_synchronize")
 
-    def set_profiling(self, enable: bool):
-        _check(load_library().od_ctx_set_profiling(self.h, 1 if enable else 0), "od_ctx_set_profiling")
+    def set_profiling(self, enable):
+        """False / 0 off; True / 1 CUDA events around PCG launches; 2 also the
+        one-launch PCG's per-iteration phase timers (they slow each iteration)."""
+        _check(load_library().od_ctx_set_profiling(self.h, int(enable)), "od_ctx_set_profiling")
 
     def selftest_bounded_waits(self):
         """od_selftest_bounded_waits: runs the grid-barrier and triangular-sweep

@@ -181,7 +181,7 @@ od_status od_ctx_set_profiling(od_ctx* ctx, int enable) {
     ctx->c.ev_pool.resize(2 * 64);
     for (auto& e : ctx->c.ev_pool) OD_CUDA(cudaEventCreate(&e));
   }
-  ctx->c.profiling = enable ? 1 : 0;
+  ctx->c.profiling = enable <= 0 ? 0 : (enable >= 2 ? 2 : 1);
   return OD_OK;
 }
 
@@ -433,6 +433,7 @@ od_status od_scene_get_info(od_scene* scene, od_scene_info* info) {
   info->num_full_blocks = s->bsr.nnzb;
   info->num_colors = (int)s->color_off.size() - 1;
   info->device_bytes = s->device_bytes;
+  info->pcg_smem_bytes = s->pcg.smem_bytes;
   return OD_OK;
 }
 

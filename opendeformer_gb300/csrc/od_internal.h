@@ -123,6 +123,7 @@ struct Pcg {
   void* gbar = nullptr;         // grid barrier state
   int* timeout_host = nullptr;  // pinned
   int coop_grid = 0;            // co-resident CTAs, 0 if cooperative launch is unavailable
+  int smem_bytes = 0;           // dynamic shared memory of the staged persistent solve (0: not used)
   int disable_persistent = 0;
   // mixed precision: the scene's sliced FP32 operator and its one-scene
   // solve (both built on first use)

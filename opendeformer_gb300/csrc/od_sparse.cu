@@ -462,24 +462,45 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // Grid-wide sums of NV per-thread values with one grid barrier and two
-// CTA barriers: warps reduce by shuffles, warp 0 forms the CTA partials,
-// lane 0 of warp 0 takes part in the grid barrier, then warp 0 sums all CTA
-// partials in a fixed order and broadcasts through shared memory.  Every
-// CTA obtains bitwise the same sums.  Returns false after a barrier timeout.
-template <int NV>
+// CTA barriers.  FP64 arithmetic is scarce on this part (about 1.7 lane
+// operations per SM per cycle), so the CTA's threads do none of the
+// reduction: they store their values to shared memory, warp 0 sums each
+// value's kPThreads entries (four fixed accumulator chains per lane, then
+// the lanes by shuffles), lane 0 of warp 0 takes part in the grid barrier,
+// then warp 0 sums all CTA partials in a fixed order.  Lane 0 then calls
+// fin(sums, extra) once for the CTA (the scalars every thread needs, e.g. a
+// step length, computed once instead of by every thread) and everything is
+// broadcast through shared memory.  Every CTA obtains bitwise the same sums.
+// Returns false after a barrier timeout.
+struct NoFinish {
+  __device__ void operator()(const double*, double*) const {}
+};
+constexpr int kSumsMax = 3;   // values per reduction
+// one shared block for every instantiation of grid_sums in a kernel (a
+// static __shared__ array inside the template would exist once per
+// instantiation)
+struct SumsShared {
+  double vals[kSumsMax][kPThreads];
+  double res[kSumsMax + 2];
+  int ok;
+};
+__device__ __forceinline__ SumsShared& sums_shared() {
+  __shared__ SumsShared sh;
+  return sh;
+}
+template <int NV, int NX = 0, class F = NoFinish>
 __device__ __forceinline__ bool grid_sums(double (&v)[NV], double* __restrict__ part, GridBarrier* gb,
                                           unsigned long long* __restrict__ work = nullptr,
-                                          unsigned long long t0 = 0) {
-  __shared__ double ws[NV][32];
-  __shared__ double res[NV];
-  __shared__ int ok_s;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+                                          unsigned long long t0 = 0, double* xout = nullptr, F fin = F()) {
+  static_assert(NV <= kSumsMax, "grid_sums: too many values");
+  SumsShared& sh = sums_shared();
+  auto& vals = sh.vals;
+  double* res = sh.res;
+  int& ok_s = sh.ok;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int G = gridDim.x;
 #pragma unroll
-  for (int j = 0; j < NV; j++) {
-    double t = warp_sum(v[j]);
-    if (lane == 0) ws[j][w] = t;
-  }
+  for (int j = 0; j < NV; j++) vals[j][threadIdx.x] = v[j];
   __syncthreads();
   if (work && threadIdx.x == 0) {  // profiling: this CTA's own share of the phase
     unsigned long long t;
@@ -489,7 +510,14 @@ __device__ __forceinline__ bool grid_sums(double (&v)[NV], double* __restrict__ 
   if (w == 0) {
 #pragma unroll
     for (int j = 0; j < NV; j++) {
-      double t = warp_sum(lane < nw ? ws[j][lane] : 0.0);
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+      for (int i = lane; i < (int)blockDim.x; i += 128) {
+        a0 += vals[j][i];
+        if (i + 32 < (int)blockDim.x) a1 += vals[j][i + 32];
+        if (i + 64 < (int)blockDim.x) a2 += vals[j][i + 64];
+        if (i + 96 < (int)blockDim.x) a3 += vals[j][i + 96];
+      }
+      const double t = warp_sum((a0 + a1) + (a2 + a3));
       if (lane == 0) part[(size_t)j * G + blockIdx.x] = t;
     }
     int ok = 1;
@@ -502,11 +530,18 @@ __device__ __forceinline__ bool grid_sums(double (&v)[NV], double* __restrict__ 
       acc = warp_sum(acc);
       if (lane == 0) res[j] = acc;
     }
-    if (lane == 0) ok_s = ok;
+    if (lane == 0) {
+      ok_s = ok;
+      if constexpr (NX > 0) fin(res, res + NV);
+    }
   }
   __syncthreads();
 #pragma unroll
   for (int j = 0; j < NV; j++) v[j] = res[j];
+  if constexpr (NX > 0) {
+#pragma unroll
+    for (int j = 0; j < NX; j++) xout[j] = res[NV + j];
+  }
   return ok_s != 0;
 }
 
@@ -525,7 +560,17 @@ __device__ __forceinline__ bool grid_sums(double (&v)[NV], double* __restrict__ 
   _Pragma("unroll") for (int k = 0; k < (GPW > 0 ? NR : 1); k++)              \
     for (int g = g0 + k * gstride; g < ngroups; g += (GPW > 0 ? ngroups : gstride))
 
-template <class TA, int GPW>
+// With SMEM (at most two groups per warp) every CTA first copies the
+// matrix blocks of its rows (9 values each, then their block columns) and
+// its rows of the Jacobi / block-Jacobi inverse into shared memory, one
+// segment per (warp, group), and every later product and preconditioner
+// apply reads them there: only the gathered vector entries go to L2.  The
+// products take the same operations in the same order as bsr_subrow.
+constexpr int kSmemGroupsMax = 2;                             // groups per warp of the SMEM variant
+constexpr int kSmemSegs = (kPThreads / 32) * kSmemGroupsMax;  // (warp, group) segments per CTA
+constexpr int kSmemPinv = 9 * kRowsPerWarp;                   // inverse values per segment
+
+template <class TA, int GPW, bool SMEM>
 __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
     int nb, const int* __restrict__ rp, const int* __restrict__ col, const TA* __restrict__ A,
     const double* __restrict__ b, double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
@@ -533,6 +578,7 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
     double* __restrict__ part, double tol, int max_iter, SolveScalars* sc, GridBarrier* gb,
     unsigned long long* __restrict__ prof) {
   constexpr int NR = GPW > 0 ? GPW : 1;
+  static_assert(!SMEM || (GPW >= 1 && GPW <= kSmemGroupsMax), "the SMEM variant keeps 1 or 2 groups per warp");
   const int G = gridDim.x;
   double* part_1 = part;          // one-value reductions (p.q, residual)
   double* part_2 = part + G;      // two/three-value reductions (G entries per value)
@@ -547,17 +593,101 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
 
   double xr[NR], rv[NR], zv[NR], pv[NR], qv[NR];
 
+  // ---- SMEM: stage this CTA's matrix rows and inverse rows
+  extern __shared__ __align__(16) unsigned char pcg_dsm[];
+  __shared__ int seg_off[SMEM ? kSmemSegs + 1 : 1];
+  double* sA = nullptr;   // 9 values per block of the CTA's segments
+  int* sC = nullptr;      // their block columns
+  double* sP = nullptr;   // kSmemPinv inverse values per segment
+  int lb[NR], le[NR];     // this lane's row: its blocks in the CTA's segments
+  if constexpr (SMEM) {
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < NR; k++) {
+        const int g = g0 + k * gstride;
+        int cnt = 0;
+        if (g < ngroups) {
+          const int r0 = g * kRowsPerWarp, r1 = min(nb, r0 + kRowsPerWarp);
+          cnt = rp[r1] - rp[r0];
+        }
+        seg_off[w * NR + k] = cnt;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int acc = 0;
+      for (int i = 0; i < wpc * NR; i++) {
+        const int c = seg_off[i];
+        seg_off[i] = acc;
+        acc += c;
+      }
+      seg_off[wpc * NR] = acc;
+    }
+    __syncthreads();
+    sP = reinterpret_cast<double*>(pcg_dsm);
+    sA = sP + (size_t)wpc * NR * kSmemPinv;
+    sC = reinterpret_cast<int*>(sA + 9 * (size_t)seg_off[wpc * NR]);
+#pragma unroll
+    for (int k = 0; k < NR; k++) {
+      const int g = g0 + k * gstride;
+      lb[k] = le[k] = 0;
+      if (g >= ngroups) continue;
+      const int r0 = g * kRowsPerWarp, r1 = min(nb, r0 + kRowsPerWarp);
+      const int base = rp[r0], off = seg_off[w * NR + k], cnt = rp[r1] - base;
+      for (int i = lane; i < 9 * cnt; i += 32) sA[9 * (size_t)off + i] = (double)A[9 * (size_t)base + i];
+      for (int i = lane; i < cnt; i += 32) sC[off + i] = col[base + i];
+      double* dst = sP + (size_t)(w * NR + k) * kSmemPinv;
+      if (pkind == OD_PRECOND_BLOCK_JACOBI)
+        for (int i = lane; i < 9 * (r1 - r0); i += 32) dst[i] = pinv[9 * (size_t)r0 + i];
+      else if (pkind == OD_PRECOND_JACOBI)
+        for (int i = lane; i < 3 * (r1 - r0); i += 32) dst[i] = pinv[3 * (size_t)r0 + i];
+      const int row = r0 + lane / 3;
+      if (lane < 30 && row < nb) {
+        lb[k] = off + rp[row] - base;
+        le[k] = off + rp[row + 1] - base;
+      }
+    }
+    __syncthreads();
+  }
+  // row product of this lane's row (group slot k) with v
+  auto row_product = [&](int k, int row, const double* __restrict__ v) -> double {
+    if constexpr (SMEM) {
+      double y = 0.0;
+      for (int j = lb[k]; j < le[k]; j++) {
+        const double* a = sA + (size_t)j * 9 + 3 * rsub;
+        const int c = 3 * sC[j];
+        y = fma(a[0], v[c], y);
+        y = fma(a[1], v[c + 1], y);
+        y = fma(a[2], v[c + 2], y);
+      }
+      return y;
+    } else {
+      (void)k;
+      return bsr_subrow<TA, double>(row, rsub, rp, col, A, v);
+    }
+  };
+
   // z = M^-1 r inside the warp (block-Jacobi through shuffles of the 3 lanes
   // of a block row; every lane takes part in the shuffles)
-  auto apply_precond = [&](int row, bool valid, double rl) {
+  auto apply_precond = [&](int k, int row, bool valid, double rl) {
     double r0 = __shfl_sync(0xffffffffu, rl, lbase < 32 ? lbase : 0);
     double r1 = __shfl_sync(0xffffffffu, rl, lbase + 1 < 32 ? lbase + 1 : 0);
     double r2 = __shfl_sync(0xffffffffu, rl, lbase + 2 < 32 ? lbase + 2 : 0);
     if (!valid) return 0.0;
-    if (pkind == OD_PRECOND_JACOBI) return pinv[3 * row + rsub] * rl;
-    if (pkind == OD_PRECOND_BLOCK_JACOBI) {
-      const double* m = pinv + 9 * (size_t)row + 3 * rsub;
-      return m[0] * r0 + m[1] * r1 + m[2] * r2;
+    if constexpr (SMEM) {
+      const double* seg = sP + (size_t)(w * NR + k) * kSmemPinv;
+      if (pkind == OD_PRECOND_JACOBI) return seg[lane] * rl;
+      if (pkind == OD_PRECOND_BLOCK_JACOBI) {
+        const double* m = seg + 3 * lane;
+        return m[0] * r0 + m[1] * r1 + m[2] * r2;
+      }
+    } else {
+      (void)k;
+      if (pkind == OD_PRECOND_JACOBI) return pinv[3 * row + rsub] * rl;
+      if (pkind == OD_PRECOND_BLOCK_JACOBI) {
+        const double* m = pinv + 9 * (size_t)row + 3 * rsub;
+        return m[0] * r0 + m[1] * r1 + m[2] * r2;
+      }
     }
     return rl;
   };
@@ -573,9 +703,9 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
       if (valid) {
         bv = b[i];
         xl = x[i];
-        rl = bv - bsr_subrow<TA, double>(row, rsub, rp, col, A, x);
+        rl = bv - row_product(k, row, x);
       }
-      const double zl = apply_precond(row, valid, rl);
+      const double zl = apply_precond(k, row, valid, rl);
       if (valid) {
         rz = fma(rl, zl, rz);
         bb = fma(bv, bv, bb);
@@ -623,7 +753,7 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
         const int row = g * kRowsPerWarp + lane / 3;
         if (lane < 30 && row < nb) {
           const int i = 3 * row + rsub;
-          const double y = bsr_subrow<TA, double>(row, rsub, rp, col, A, p);
+          const double y = row_product(k, row, p);
           const double pl = GPW > 0 ? pv[k] : p[i];
           if (GPW > 0) qv[k] = y; else q[i] = y;
           pq = fma(pl, y, pq);
@@ -631,10 +761,13 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
       }
     }
     stamp(0);
-    double v1[1] = {pq};
-    if (!grid_sums<1>(v1, part_1, gb, cta_work, t_phase)) return;
+    double v1[1] = {pq}, ax[1];
+    // alpha = r.z / p.q, formed once per CTA
+    if (!grid_sums<1, 1>(v1, part_1, gb, cta_work, t_phase, ax,
+                         [rz](const double* sums, double* x) { x[0] = rz / sums[0]; }))
+      return;
     stamp(1);
-    const double alpha = rz / v1[0];
+    const double alpha = ax[0];
     phase_start();
     // ---- x += alpha p; r -= alpha q; z = M^-1 r; r.z, r.r
     double rzn = 0.0, rrn = 0.0;
@@ -655,7 +788,7 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
             r[i] = rl;
           }
         }
-        const double zl = apply_precond(row, valid, rl);
+        const double zl = apply_precond(k, row, valid, rl);
         if (valid) {
           if (GPW > 0) zv[k] = zl; else z[i] = zl;
           rzn = fma(rl, zl, rzn);
@@ -664,12 +797,15 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
       }
     }
     stamp(2);
-    double v2[2] = {rzn, rrn};
-    if (!grid_sums<2>(v2, part_2, gb, cta_work ? cta_work + G : nullptr, t_phase)) return;
+    double v2[2] = {rzn, rrn}, bx[1];
+    // beta = r.z (new) / r.z (old), formed once per CTA
+    if (!grid_sums<2, 1>(v2, part_2, gb, cta_work ? cta_work + G : nullptr, t_phase, bx,
+                         [rz](const double* sums, double* x) { x[0] = sums[0] / rz; }))
+      return;
     stamp(3);
     const double rz_new = v2[0];
     rr = v2[1];
-    const double beta = rz_new / rz;
+    const double beta = bx[0];
     rz = rz_new;
     it++;
     if (!isfinite(rr) || !isfinite(beta)) status = OD_ERR_NAN;
@@ -708,10 +844,9 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
   if (!grid_barrier(gb)) return;
   double d2 = 0.0;
   OD_GROUP_LOOP(k, g) {
-    (void)k;
     const int row = g * kRowsPerWarp + lane / 3;
     if (lane < 30 && row < nb) {
-      const double dv = b[3 * row + rsub] - bsr_subrow<TA, double>(row, rsub, rp, col, A, x);
+      const double dv = b[3 * row + rsub] - row_product(k, row, x);
       d2 = fma(dv, dv, d2);
     }
   }
@@ -752,6 +887,23 @@ __device__ __forceinline__ void comp_add_prod(Comp& a, float x, float y) {
   a.c += t + e;
 }
 __device__ __forceinline__ double comp_value(const Comp& a) { return (double)a.s + (double)a.c; }
+// Sum of the 32 lanes' compensated partials in compensated FP32 (TwoSum of
+// the leading parts, the errors and trailing parts added), so only lane 0
+// converts to FP64: the FP64 pipe is far slower than the FP32 one here.
+// The sum's relative error stays near 2^-44 for these few levels.
+__device__ __forceinline__ double comp_warp_sum(Comp a) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float bs = __shfl_down_sync(0xffffffffu, a.s, o);
+    const float bc = __shfl_down_sync(0xffffffffu, a.c, o);
+    const float s = a.s + bs;
+    const float z = s - a.s;
+    const float t = (a.s - (s - z)) + (bs - z);
+    a.s = s;
+    a.c = (a.c + bc) + t;
+  }
+  return comp_value(a);  // lane 0
+}
 
 // ---- sliced FP32 systems of one or more scenes (layout: SliceSys)
 // Per-scene arrays are reached through MixDesc; every kernel below is one
@@ -1219,7 +1371,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
     __syncwarp();
   };
   auto flush = [&](int j, int ls, const Comp& c) {
-    const double tv = warp_sum(comp_value(c));
+    const double tv = comp_warp_sum(c);
     if (lane == 0) sh.ws[j][ls][w] = tv;
   };
   // the scene's vectors, indexed by the scene-local slice
@@ -2200,10 +2352,48 @@ od_status pcg_alloc(Scene* s) {
   // every SM's FP64 pipe equally loaded)
   int coop = 0, bps = 0;
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, s->ctx->device);
-  if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pcg_persistent_kernel<double, 4>, kPThreads, 0) ==
+  if (coop && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, pcg_persistent_kernel<double, 4, false>, kPThreads, 0) ==
                   cudaSuccess && bps > 0) {
     P.coop_grid = std::min(bps, 1) * std::max(1, s->ctx->num_sms);
     P.grid = std::max(P.grid, P.coop_grid);
+  }
+  // shared memory of the staged variant: the largest CTA share of matrix
+  // blocks (72 B values + 4 B column each) plus the inverse rows of every
+  // (warp, group) segment; 0 when it does not fit one CTA's shared memory or
+  // a warp would own more than two groups (OD_GB300_PCG_SMEM=0 disables it)
+  P.smem_bytes = 0;
+  const char* smem_env = std::getenv("OD_GB300_PCG_SMEM");
+  const int nb = s->bsr.nb;
+  if (P.coop_grid > 0 && nb > 0 && !(smem_env && smem_env[0] == '0') && (int)s->hbsr_rp.size() == nb + 1) {
+    const int G = P.coop_grid, wpc = kPThreads / 32;
+    const int ngroups = (nb + kRowsPerWarp - 1) / kRowsPerWarp;
+    const int need = (ngroups + G * wpc - 1) / (G * wpc);
+    if (need <= kSmemGroupsMax) {
+      std::vector<long long> cta((size_t)G, 0);
+      for (int g = 0; g < ngroups; g++) {
+        const int r0 = g * kRowsPerWarp, r1 = std::min(nb, r0 + kRowsPerWarp);
+        cta[(size_t)(g % G)] += s->hbsr_rp[r1] - s->hbsr_rp[r0];
+      }
+      const long long mx = *std::max_element(cta.begin(), cta.end());
+      const long long bytes = 8LL * wpc * need * kSmemPinv + 76LL * mx;
+      int dev_max = 0;
+      cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->ctx->device);
+      const void* fn = need <= 1 ? (const void*)pcg_persistent_kernel<double, 1, true>
+                                 : (const void*)pcg_persistent_kernel<double, 2, true>;
+      // the attribute is per function, shared by every scene: set it to the
+      // most the device allows, never to one scene's size
+      cudaFuncAttributes fa{};
+      const long long cap = (long long)dev_max - 1024;
+      if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess && bytes + (long long)fa.sharedSizeBytes <= cap &&
+          cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(cap - (long long)fa.sharedSizeBytes)) == cudaSuccess) {
+        int bps2 = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps2, fn, kPThreads, (size_t)bytes) == cudaSuccess &&
+            bps2 >= 1)
+          P.smem_bytes = (int)bytes;
+      }
+      cudaGetLastError();   // a refused attribute is not an error of the scene
+    }
   }
   OD_CUDA(cudaFree(P.partial));
   OD_CUDA(cudaMalloc(&P.partial, sizeof(double) * 4 * (size_t)P.grid));
@@ -2235,7 +2425,7 @@ void pcg_free(Scene* s) {
 
 // true residual ||b - A x|| / ||b|| on the device, then the statistics
 static od_status pcg_finish(Scene* s, const double* d_b, double* d_x, double shift, od_solve_stats* st,
-                            bool persistent, bool timed_persistent) {
+                            bool persistent, bool timed_persistent, bool phases = false) {
   Pcg& P = s->pcg;
   cudaStream_t strm = s->ctx->stream;
   const int nb = s->bsr.nb, n = P.n_pad;
@@ -2248,7 +2438,7 @@ static od_status pcg_finish(Scene* s, const double* d_b, double* d_x, double shi
     OD_CUDA(cudaGetLastError());
   }
   OD_CUDA(cudaMemcpyAsync(P.sc_host, P.sc, sizeof(SolveScalars), cudaMemcpyDeviceToHost, strm));
-  if (timed_persistent)
+  if (phases)
     OD_CUDA(cudaMemcpyAsync(P.prof_host, P.prof, P.prof_slots * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                             strm));
   int timeout = 0;
@@ -2263,6 +2453,8 @@ static od_status pcg_finish(Scene* s, const double* d_b, double* d_x, double shi
     s->ctx->pcg_kernel_ms += ms;
     s->ctx->pcg_kernel_launches++;
     s->ctx->pcg_kernel_iters += h.iter;
+  }
+  if (phases) {
     unsigned long long* last = P.prof_host + P.prof_slots;
     for (int k = 0; k < kPcgPhases; k++) s->ctx->pcg_phase_ms[k] += 1e-6 * (double)(P.prof_host[k] - last[k]);
     s->ctx->pcg_phase_iters += (long long)(P.prof_host[kPcgPhases] - last[kPcgPhases]);
@@ -2430,13 +2622,21 @@ static od_status mixed_partition(MixedSys* m, int G) {
   std::vector<int> first(G + 1, ns), sc_lo(G, 0);
   std::vector<int> sc_cta(2 * std::max(1, m->n_sc), -1);
   for (int s = 0; s < m->n_sc; s++) sc_cta[2 * s + 1] = -2;  // empty range for scenes without slices
+  // Each CTA takes slices up to an equal share of the remaining weight; it
+  // takes more when the scenes left after it would not fit the remaining
+  // CTAs at kMaxLocalScenes each (many small scenes), and it never spans more
+  // than kMaxLocalScenes scenes.
   int sl = 0;
   for (int b = 0; b < G; b++) {
     first[b] = sl;
     sc_lo[b] = sl < ns ? sc_of[sl] : 0;
-    const double target = cum[ns] * (b + 1) / G;
-    while (sl < ns && (cum[sl] < target || b == G - 1)) {
+    const double target = cum[sl] + (cum[ns] - cum[sl]) / (G - b);
+    const long long room_after = (long long)kMaxLocalScenes * (G - b - 1);
+    while (sl < ns) {
       if (sc_of[sl] - sc_lo[b] >= kMaxLocalScenes) break;
+      const bool share = cum[sl] < target || b == G - 1;
+      const bool crowded = (long long)(m->n_sc - sc_of[sl]) > room_after;
+      if (!share && !crowded) break;
       sl++;
     }
   }
@@ -2895,18 +3095,24 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
     void* args[] = {(void*)&nb, (void*)&rpp, (void*)&colp, (void*)&Ap, (void*)&d_b, (void*)&xp, (void*)&P.r,
                     (void*)&P.z, (void*)&P.p, (void*)&P.q, (void*)&pkv, (void*)&P.pinv, (void*)&P.partial,
                     (void*)&tol, (void*)&maxit, (void*)&P.sc, (void*)&gbp, nullptr};
-    void* fn = need <= 1 ? (void*)pcg_persistent_kernel<double, 1>
-             : need <= 2 ? (void*)pcg_persistent_kernel<double, 2>
-             : need <= 4 ? (void*)pcg_persistent_kernel<double, 4>
-                         : (void*)pcg_persistent_kernel<double, 0>;
+    // the shared-memory variant when every CTA's rows fit (P.smem_bytes)
+    const bool smem = P.smem_bytes > 0 && need <= kSmemGroupsMax;
+    void* fn = smem ? (need <= 1 ? (void*)pcg_persistent_kernel<double, 1, true>
+                                 : (void*)pcg_persistent_kernel<double, 2, true>)
+             : need <= 1 ? (void*)pcg_persistent_kernel<double, 1, false>
+             : need <= 2 ? (void*)pcg_persistent_kernel<double, 2, false>
+             : need <= 4 ? (void*)pcg_persistent_kernel<double, 4, false>
+                         : (void*)pcg_persistent_kernel<double, 0, false>;
+    const size_t dyn = smem ? (size_t)P.smem_bytes : 0;
     const bool prof = s->ctx->profiling && s->ctx->ev_pool.size() >= 2;
-    unsigned long long* profp = prof ? P.prof : nullptr;
+    const bool phases = prof && s->ctx->profiling >= 2;
+    unsigned long long* profp = phases ? P.prof : nullptr;
     args[17] = (void*)&profp;
     if (prof) OD_CUDA(cudaEventRecord(s->ctx->ev_pool[0], strm));
     OD_KL(s);
-    OD_CUDA(cudaLaunchCooperativeKernel(fn, dim3(G2), dim3(kPThreads), args, 0, strm));
+    OD_CUDA(cudaLaunchCooperativeKernel(fn, dim3(G2), dim3(kPThreads), args, dyn, strm));
     if (prof) OD_CUDA(cudaEventRecord(s->ctx->ev_pool[1], strm));
-    return pcg_finish(s, d_b, d_x, shift, st, true, prof);
+    return pcg_finish(s, d_b, d_x, shift, st, true, prof, phases);
   }
   OD_KL(s);
   pcg_init_kernel<double><<<g_rows, kThreads, 0, strm>>>(nb, s->bsr.row_ptr, s->bsr.col, s->A64, d_b, d_x, P.r, P.z,

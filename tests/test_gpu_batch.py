@@ -179,3 +179,39 @@ def test_autotune_keeps_state_and_results(tmp_path):
         again.set_tuning(14, 8.0)
     with pytest.raises(api.ODError):
         again.set_tuning(20, 8.0, consumer_warps=15)   # 15 warps of 20-step rings exceed the shared memory
+
+
+def test_batch_of_many_small_scenes_after_large_ones():
+    """A batch whose first scenes hold most of the work and whose tail is
+    thousands of one-cube scenes: the partition of the inner solve gives no
+    CTA more than its scene capacity (32) and still covers every scene, and
+    each tiny scene moves as it does alone."""
+    big = [make_scene(1, newton=1) for _ in range(6)]
+    tiny = []
+    for k in range(2400):
+        g = meshgen.tet_grid(1, 1, 1, h=0.05, jitter=0.0, seed=k, tets_per_cube=6)
+        cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+        s = api.Scene(ctx(), g.X, g.tets, g.facets, cd, api.CorotationalHyperelasticMaterial(1000.0, 1e5, 0.4, 0.1))
+        s.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, 0.01, 0.001, 1 / 60,
+                                                 api.CGSolver(1e-10, 5000, api.BlockJacobiPreconditioner(),
+                                                              precision="mixed"), 1))
+        s.set_loads(body=(0.0, 0.0, -9800.0 * (1 + k % 7)))
+        tiny.append(s)
+    b = api.Batch(ctx(), big + tiny)
+    stats = b.step(2)
+    assert all(st.status == 0 for st in stats)
+    probe = tiny[-1]
+    g = meshgen.tet_grid(1, 1, 1, h=0.05, jitter=0.0, seed=2399, tets_per_cube=6)
+    cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
+    alone = api.Scene(ctx(), g.X, g.tets, g.facets, cd, api.CorotationalHyperelasticMaterial(1000.0, 1e5, 0.4, 0.1))
+    alone.setup_integrator(api.NewmarkIntegrator(0.25, 0.5, 0.01, 0.001, 1 / 60,
+                                                 api.CGSolver(1e-10, 5000, api.BlockJacobiPreconditioner(),
+                                                              precision="mixed"), 1))
+    alone.set_loads(body=(0.0, 0.0, -9800.0 * (1 + 2399 % 7)))
+    assert alone.step(2).status == 0
+    ua = alone.displacements()
+    assert np.abs(ua).max() > 0
+    assert rel_err(probe.displacements(), ua) <= 1e-7
+    b.close()
+    for s in big + tiny + [alone]:
+        s.close()
