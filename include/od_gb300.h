@@ -175,6 +175,8 @@ typedef struct od_counters {
      time, without the waits): per solve the slowest CTA's and the mean over CTAs */
   double pcg_work_max_ms[3];
   double pcg_work_mean_ms[3];
+  double mix_fallback_ms;     /* host wall time of the FP64 solves that finished stalled mixed
+                                 solves (counted whether profiling is on or not) */
 } od_counters;
 
 typedef struct od_scene_info {
@@ -204,8 +206,10 @@ od_status od_ctx_create(int device, od_ctx** out);
 od_status od_ctx_destroy(od_ctx* ctx);
 od_status od_ctx_synchronize(od_ctx* ctx);
 /* Failure detection, tested without a GPU fault: runs the bounded device
- * waits against conditions that never clear -- a grid barrier one CTA never
- * reaches, a triangular-sweep wait on a value nobody writes -- and reports
+ * waits against conditions that never clear -- the two grid barriers (the
+ * generation barrier and the one-launch PCG's counting barrier) with a CTA
+ * that never reaches them, a triangular-sweep wait on a value nobody
+ * writes -- and reports
  * whether each ran out and raised its timeout flag (the flag the calls
  * above turn into OD_ERR_DEVICE_TIMEOUT).  Takes a few seconds; the context
  * stays usable. */
@@ -461,6 +465,7 @@ typedef struct od_server_stats {
   double s_step;            /* batch / scene steps */
   double s_worker;          /* worker thread: building scenes (overlaps the ticks) */
   long long resident, resident_bytes, budget_bytes;
+  double s_build;           /* of s_step: building and freeing the tick's batch */
 } od_server_stats;
 od_status od_server_create(od_ctx* ctx, const od_server_config* cfg, od_server** out);
 od_status od_server_destroy(od_server* server);

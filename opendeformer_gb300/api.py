@@ -91,7 +91,7 @@ class od_counters(C.Structure):
                 ("sweep_applies", C.c_longlong), ("sweep_apply_ms", C.c_double), ("sweep_apply_bytes", C.c_double),
                 ("sweep_levels", C.c_longlong), ("pcg_phase_ms", C.c_double * 6),
                 ("pcg_phase_iterations", C.c_longlong), ("pcg_work_max_ms", C.c_double * 3),
-                ("pcg_work_mean_ms", C.c_double * 3)]
+                ("pcg_work_mean_ms", C.c_double * 3), ("mix_fallback_ms", C.c_double)]
 
 
 class od_scene_info(C.Structure):
@@ -137,7 +137,8 @@ class od_server_stats(C.Structure):
     _fields_ = [("ticks", C.c_longlong), ("steps", C.c_longlong), ("admissions", C.c_longlong),
                 ("restores", C.c_longlong), ("evictions", C.c_longlong), ("deferred", C.c_longlong),
                 ("s_admit", C.c_double), ("s_loads", C.c_double), ("s_step", C.c_double), ("s_worker", C.c_double),
-                ("resident", C.c_longlong), ("resident_bytes", C.c_longlong), ("budget_bytes", C.c_longlong)]
+                ("resident", C.c_longlong), ("resident_bytes", C.c_longlong), ("budget_bytes", C.c_longlong),
+                ("s_build", C.c_double)]
 
 
 class od_modal_params(C.Structure):

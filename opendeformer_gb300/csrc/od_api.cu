@@ -199,6 +199,7 @@ od_status od_ctx_get_counters(od_ctx* ctx, od_counters* out) {
   out->mix_spmv_work_ms = ctx->c.mix_spmv_work_ms;
   for (int k = 0; k < od::kPcgPhases; k++) out->pcg_phase_ms[k] = ctx->c.pcg_phase_ms[k];
   out->pcg_phase_iterations = ctx->c.pcg_phase_iters;
+  out->mix_fallback_ms = ctx->c.mix_fallback_ms;
   for (int k = 0; k < 3; k++) {
     out->pcg_work_max_ms[k] = ctx->c.pcg_work_max_ms[k];
     out->pcg_work_mean_ms[k] = ctx->c.pcg_work_mean_ms[k];
@@ -221,6 +222,7 @@ od_status od_ctx_reset_counters(od_ctx* ctx) {
   ctx->c.pcg_kernel_launches = ctx->c.pcg_kernel_iters = 0;
   ctx->c.spmv_ms = ctx->c.pcg_kernel_ms = 0.0;
   ctx->c.mix_iters = ctx->c.mix_fallbacks = 0;
+  ctx->c.mix_fallback_ms = 0.0;
   ctx->c.mix_spmv_ms = ctx->c.mix_spmv_bytes = ctx->c.mix_spmv_work_ms = 0.0;
   for (double& v : ctx->c.pcg_phase_ms) v = 0.0;
   ctx->c.pcg_phase_iters = 0;

@@ -39,6 +39,27 @@ __device__ __forceinline__ int barrier_arrive_wait(GridBarrier* gb) {
   return ok && !*(volatile int*)&gb->timeout;
 }
 
+// Counting barrier for kernels whose CTAs pass the same sequence of
+// barriers: arrival is a release reduction that does not wait for its
+// result, and the CTA then polls the counter (zeroed before the launch)
+// until all gridDim.x arrivals of its epoch-th barrier are in -- one L2
+// round trip fewer than the generation barrier above.  The caller keeps
+// epoch (its count of barriers passed, from 1).  Bounded like the other.
+__device__ __forceinline__ int barrier_arrive_wait_count(GridBarrier* gb, unsigned epoch) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&gb->arrive) : "memory");
+  const unsigned target = epoch * gridDim.x;
+  unsigned long long spins = 0;
+  unsigned cur;
+  int ok = 1;
+  do {
+    asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(cur) : "l"(&gb->arrive) : "memory");
+    if ((int)(cur - target) >= 0) break;
+    if (++spins > kSpinLimit) { atomicExch(&gb->timeout, 1); ok = 0; break; }
+    if (*(volatile int*)&gb->timeout) { ok = 0; break; }
+  } while (true);
+  return ok && !*(volatile int*)&gb->timeout;
+}
+
 // Values that double as their own ready flags: filled with an all-ones NaN
 // (a pattern no arithmetic result has) before a launch and published once.
 // Nothing else is read through such a value, so relaxed GPU-scope 64-bit

@@ -124,6 +124,8 @@ struct Pcg {
   int* timeout_host = nullptr;  // pinned
   int coop_grid = 0;            // co-resident CTAs, 0 if cooperative launch is unavailable
   int smem_bytes = 0;           // dynamic shared memory of the staged persistent solve (0: not used)
+  int recur = -1;               // one-launch PCG form: 1 recurrence (q = A z + beta q; two grid syncs),
+                                // 0 the reference's (q = A p; three), -1 chosen by the tolerance
   int disable_persistent = 0;
   // mixed precision: the scene's sliced FP32 operator and its one-scene
   // solve (both built on first use)
@@ -297,6 +299,7 @@ struct Ctx {
   double pcg_kernel_ms = 0.0;
   long long mix_iters = 0;            // inner FP32 loop iterations (profiling)
   long long mix_fallbacks = 0;        // mixed solves finished by the FP64 solver
+  double mix_fallback_ms = 0.0;       // their host wall time
   long long sweep_factors = 0, sweep_nnz = 0, sweep_applies = 0, sweep_levels = 0;
   double sweep_factor_ms = 0.0, sweep_apply_ms = 0.0, sweep_apply_bytes = 0.0;
   double mix_spmv_ms = 0.0;

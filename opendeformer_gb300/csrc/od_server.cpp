@@ -447,11 +447,16 @@ od_status od_server_tick(od_server* sv, int capacity, od_step_result* results, i
   od_status fail = OD_OK;   // a step that failed as a call: its requests come back with that status
   if (sv->cfg.batched) {
     od_batch* b = nullptr;
+    const auto tb0 = clock_type::now();
     fail = od_batch_create(sv->ctx, (int)scenes.size(), scenes.data(), &b);
+    const auto tb1 = clock_type::now();
     if (fail == OD_OK) {
       fail = od_batch_step(b, 1, st.data());
+      const auto tb2 = clock_type::now();
       od_batch_destroy(b);
+      sv->stats.s_build += std::chrono::duration<double>(clock_type::now() - tb2).count();
     }
+    sv->stats.s_build += std::chrono::duration<double>(tb1 - tb0).count();
   } else {
     for (size_t k = 0; k < scenes.size() && fail == OD_OK; k++) {
       const od_status rc = od_step(scenes[k], 1, &st[k]);

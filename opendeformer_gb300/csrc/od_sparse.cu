@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstdio>
+#include <chrono>
 #include <cstring>
 
 #include "od_internal.h"
@@ -483,10 +484,19 @@ struct SumsShared {
   double vals[kSumsMax][kPThreads];
   double res[kSumsMax + 2];
   int ok;
+  unsigned epoch;   // barriers this CTA has passed (thread 0 only)
 };
 __device__ __forceinline__ SumsShared& sums_shared() {
   __shared__ SumsShared sh;
   return sh;
+}
+// the plain barrier of the kernels that use grid_sums (same counter)
+__device__ __forceinline__ bool grid_barrier_count(GridBarrier* gb) {
+  SumsShared& sh = sums_shared();
+  __syncthreads();
+  if (threadIdx.x == 0) sh.ok = barrier_arrive_wait_count(gb, ++sh.epoch);
+  __syncthreads();
+  return sh.ok != 0;
 }
 template <int NV, int NX = 0, class F = NoFinish>
 __device__ __forceinline__ bool grid_sums(double (&v)[NV], double* __restrict__ part, GridBarrier* gb,
@@ -521,7 +531,8 @@ __device__ __forceinline__ bool grid_sums(double (&v)[NV], double* __restrict__ 
       if (lane == 0) part[(size_t)j * G + blockIdx.x] = t;
     }
     int ok = 1;
-    if (lane == 0) ok = barrier_arrive_wait(gb);
+    if (lane == 0) ok = barrier_arrive_wait_count(gb, ++sh.epoch);
+    __syncwarp();   // orders lane 0's acquire before the other lanes' partial reads
     ok = __shfl_sync(0xffffffffu, ok, 0);
 #pragma unroll
     for (int j = 0; j < NV; j++) {
@@ -576,9 +587,10 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
     const double* __restrict__ b, double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
     double* __restrict__ p, double* __restrict__ q, int pkind, const double* __restrict__ pinv,
     double* __restrict__ part, double tol, int max_iter, SolveScalars* sc, GridBarrier* gb,
-    unsigned long long* __restrict__ prof) {
+    unsigned long long* __restrict__ prof, int recur) {
   constexpr int NR = GPW > 0 ? GPW : 1;
   static_assert(!SMEM || (GPW >= 1 && GPW <= kSmemGroupsMax), "the SMEM variant keeps 1 or 2 groups per warp");
+  if (threadIdx.x == 0) sums_shared().epoch = 0;   // the counting barrier's epochs (thread 0 only)
   const int G = gridDim.x;
   double* part_1 = part;          // one-value reductions (p.q, residual)
   double* part_2 = part + G;      // two/three-value reductions (G entries per value)
@@ -710,9 +722,10 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
         rz = fma(rl, zl, rz);
         bb = fma(bv, bv, bb);
         rr = fma(rl, rl, rr);
-        if (GPW > 0) { xr[k] = xl; rv[k] = rl; zv[k] = zl; pv[k] = zl; }
-        else { r[i] = rl; z[i] = zl; }
-        p[i] = zl;
+        if (GPW > 0) { xr[k] = xl; rv[k] = rl; zv[k] = zl; pv[k] = recur ? 0.0 : zl; qv[k] = 0.0; }
+        else { r[i] = rl; z[i] = zl; if (recur) q[i] = 0.0; }
+        p[i] = recur ? 0.0 : zl;
+        if (recur) z[i] = zl;   // the gathered vector of the recurrence form
       }
     }
   }
@@ -743,20 +756,37 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
   auto phase_start = [&]() {
     if (prof && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_phase));
   };
+  // recurrence form (recur != 0): the product is A z, then q = A z + beta q
+  // and p = z + beta p in place (A p = A z + beta A p_prev), so the
+  // direction pass and its barrier go; beta_r is the last iteration's beta
+  double beta_r = 0.0;
   while (status == OD_OK && it < max_iter && rr > eps) {
     stamp(-1);
     phase_start();
-    // ---- q = A p; p.q
+    // ---- q = A p (or A z + beta q); p.q
     double pq = 0.0;
     {
       OD_GROUP_LOOP(k, g) {
         const int row = g * kRowsPerWarp + lane / 3;
         if (lane < 30 && row < nb) {
           const int i = 3 * row + rsub;
-          const double y = row_product(k, row, p);
-          const double pl = GPW > 0 ? pv[k] : p[i];
-          if (GPW > 0) qv[k] = y; else q[i] = y;
-          pq = fma(pl, y, pq);
+          if (!recur) {
+            const double y = row_product(k, row, p);
+            const double pl = GPW > 0 ? pv[k] : p[i];
+            if (GPW > 0) qv[k] = y; else q[i] = y;
+            pq = fma(pl, y, pq);
+          } else {
+            const double y = row_product(k, row, z);
+            double pl, ql;
+            if (GPW > 0) {
+              ql = qv[k] = fma(beta_r, qv[k], y);
+              pl = pv[k] = fma(beta_r, pv[k], zv[k]);
+            } else {
+              ql = q[i] = fma(beta_r, q[i], y);
+              pl = p[i] = fma(beta_r, p[i], z[i]);
+            }
+            pq = fma(pl, ql, pq);
+          }
         }
       }
     }
@@ -791,6 +821,7 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
         const double zl = apply_precond(k, row, valid, rl);
         if (valid) {
           if (GPW > 0) zv[k] = zl; else z[i] = zl;
+          if (GPW > 0 && recur) z[i] = zl;   // gathered by the next product
           rzn = fma(rl, zl, rzn);
           rrn = fma(rl, rl, rrn);
         }
@@ -809,6 +840,11 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
     rz = rz_new;
     it++;
     if (!isfinite(rr) || !isfinite(beta)) status = OD_ERR_NAN;
+    if (recur) {
+      beta_r = beta;
+      if (timer) prof[6] += 1;
+      continue;
+    }
     phase_start();
     // ---- p = z + beta p
     {
@@ -830,7 +866,7 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
         cta_work[2 * G + blockIdx.x] += t - t_phase;
       }
     }
-    if (!grid_barrier(gb)) return;
+    if (!grid_barrier_count(gb)) return;
     stamp(5);
     if (timer) prof[6] += 1;
   }
@@ -841,7 +877,7 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
       if (lane < 30 && row < nb) x[3 * row + rsub] = xr[k];
     }
   }
-  if (!grid_barrier(gb)) return;
+  if (!grid_barrier_count(gb)) return;
   double d2 = 0.0;
   OD_GROUP_LOOP(k, g) {
     const int row = g * kRowsPerWarp + lane / 3;
@@ -1123,6 +1159,7 @@ struct RingShared {
   volatile int pub;                           // last iteration whose activity is published
   volatile int stop;
   int ok;
+  unsigned epoch;                             // counting-barrier epochs passed (thread 0 only)
 };
 
 // local scene of slice sl for a warp walking its slices in increasing order
@@ -1172,7 +1209,8 @@ __device__ __forceinline__ bool ring_sums(RingShared& sh, int L, int sc_lo, int 
     __threadfence();
     __syncwarp();
     int ok = 1;
-    if (lane == 0) ok = barrier_arrive_wait(gb);
+    if (lane == 0) ok = barrier_arrive_wait_count(gb, ++sh.epoch);
+    __syncwarp();   // orders lane 0's acquire before the other lanes' partial reads
     ok = __shfl_sync(0xffffffffu, ok, 0);
     if (stamp) {  // profiling: the last CTA's end of the phase
       unsigned long long tmax = 0;
@@ -1205,11 +1243,13 @@ __device__ __forceinline__ bool ring_sums(RingShared& sh, int L, int sc_lo, int 
   return sh.ok != 0;
 }
 
+// the ring kernel's plain barrier (consumer threads; the counting barrier
+// that ring_sums also uses, epochs in sh)
 template <int NT>
-__device__ __forceinline__ bool grid_barrier_named(GridBarrier* gb) {
+__device__ __forceinline__ bool grid_barrier_named(GridBarrier* gb, RingShared& sh) {
   __shared__ int okb_s;
   named_sync<NT>();
-  if (threadIdx.x == 0) okb_s = barrier_arrive_wait(gb);
+  if (threadIdx.x == 0) okb_s = barrier_arrive_wait_count(gb, ++sh.epoch);
   named_sync<NT>();
   return okb_s != 0;
 }
@@ -1252,6 +1292,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
   if (threadIdx.x == 0) {
     sh.stop = 0;
     sh.pub = -1;
+    sh.epoch = 0;
   }
   if (threadIdx.x < 2 * NW) {
     mbar_init(full + threadIdx.x, 1);
@@ -1443,7 +1484,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
   __threadfence_block();
   if (threadIdx.x == 0) sh.pub = 0;   // act[0] (= the launch's activity) is final
   // u complete everywhere before the first gathers
-  if (!grid_barrier_named<(32 * NW)>(gb)) alive = false;
+  if (!grid_barrier_named<(32 * NW)>(gb, sh)) alive = false;
 
   // profiling (prof != nullptr): CTA 0 times each SpMV + sum phase up to the
   // end of its grid-wide sum, i.e. including the slowest CTA
@@ -1660,7 +1701,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
     }
     // u complete everywhere before the next gathers (also keeps this
     // iteration's sums from being overwritten before every CTA read them)
-    if (!grid_barrier_named<(32 * NW)>(gb)) { alive = false; break; }
+    if (!grid_barrier_named<(32 * NW)>(gb, sh)) { alive = false; break; }
   }
   named_sync<(32 * NW)>();
   if (threadIdx.x == 0) sh.stop = 1;
@@ -2362,6 +2403,10 @@ od_status pcg_alloc(Scene* s) {
   // (warp, group) segment; 0 when it does not fit one CTA's shared memory or
   // a warp would own more than two groups (OD_GB300_PCG_SMEM=0 disables it)
   P.smem_bytes = 0;
+  // the one-launch PCG's form: -1 by tolerance (below), OD_GB300_PCG_FORM=recur
+  // or =standard forces one
+  P.recur = -1;
+  if (const char* f = std::getenv("OD_GB300_PCG_FORM")) P.recur = std::strcmp(f, "recur") == 0 ? 1 : 0;
   const char* smem_env = std::getenv("OD_GB300_PCG_SMEM");
   const int nb = s->bsr.nb;
   if (P.coop_grid > 0 && nb > 0 && !(smem_env && smem_env[0] == '0') && (int)s->hbsr_rp.size() == nb + 1) {
@@ -2993,7 +3038,10 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
       const MixDesc& D = m->desc_host[s];
       od_solve_stats s64{};
       if (!std::isfinite(rr[s])) OD_CUDA(cudaMemsetAsync(D.x, 0, sizeof(double) * 3 * (size_t)D.nb, strm));
+      const auto tf0 = std::chrono::steady_clock::now();
       const od_status rc64 = pcg_solve(m->scenes[s], D.b, D.x, &p64, &s64);
+      ctx->mix_fallback_ms +=
+          std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tf0).count();
       ctx->mix_fallbacks++;
       if (rc64 == OD_OK) {
         total[s] += s64.iterations;
@@ -3094,7 +3142,7 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
     int pkv = pk;
     void* args[] = {(void*)&nb, (void*)&rpp, (void*)&colp, (void*)&Ap, (void*)&d_b, (void*)&xp, (void*)&P.r,
                     (void*)&P.z, (void*)&P.p, (void*)&P.q, (void*)&pkv, (void*)&P.pinv, (void*)&P.partial,
-                    (void*)&tol, (void*)&maxit, (void*)&P.sc, (void*)&gbp, nullptr};
+                    (void*)&tol, (void*)&maxit, (void*)&P.sc, (void*)&gbp, nullptr, (void*)&P.recur};
     // the shared-memory variant when every CTA's rows fit (P.smem_bytes)
     const bool smem = P.smem_bytes > 0 && need <= kSmemGroupsMax;
     void* fn = smem ? (need <= 1 ? (void*)pcg_persistent_kernel<double, 1, true>
@@ -3104,6 +3152,13 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
              : need <= 4 ? (void*)pcg_persistent_kernel<double, 4, false>
                          : (void*)pcg_persistent_kernel<double, 0, false>;
     const size_t dyn = smem ? (size_t)P.smem_bytes : 0;
+    // the recurrence form (q = A z + beta q: two grid syncs per iteration
+    // instead of three) for tolerances down to 1e-10, where it takes the same
+    // iterations to the same true residual on the Newmark systems; tighter
+    // solves keep cgSolver.cpp's q = A p, so no recurrence drift can hold the
+    // residual above a very small target
+    int recur = P.recur >= 0 ? P.recur : (prm->tol >= 1e-10 ? 1 : 0);
+    args[18] = (void*)&recur;
     const bool prof = s->ctx->profiling && s->ctx->ev_pool.size() >= 2;
     const bool phases = prof && s->ctx->profiling >= 2;
     unsigned long long* profp = phases ? P.prof : nullptr;
@@ -3181,8 +3236,11 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
 // in which CTA 0 never arrives, so the other's wait runs out (kSpinLimit
 // polls) and it leaves with the barrier's timeout flag set -- the path every
 // persistent kernel takes when a CTA stops answering.
-__global__ void selftest_barrier_kernel(GridBarrier* gb, int* failed) {
+__global__ void selftest_barrier_kernel(GridBarrier* gb, GridBarrier* gb_count, int* failed) {
   if (blockIdx.x == 0) return;
+  // the counting barrier of the one-launch PCG, then the generation barrier
+  if (threadIdx.x == 0 && !barrier_arrive_wait_count(gb_count, 1)) atomicAdd(failed + 1, 1);
+  __syncthreads();
   if (!grid_barrier(gb) && threadIdx.x == 0) atomicAdd(failed, 1);
 }
 
@@ -3192,21 +3250,22 @@ od_status selftest_barrier_timeout(Ctx* c, int* timed_out) {
   OD_CUDA(cudaDeviceGetAttribute(&dev_coop, cudaDevAttrCooperativeLaunch, c->device));
   if (!dev_coop) return OD_OK;
   DeviceTemps tmp;
-  GridBarrier* gb = nullptr;
+  GridBarrier* gb = nullptr;    // [0] generation barrier, [1] counting barrier
   int* failed = nullptr;
-  OD_CUDA(tmp.alloc(&gb, sizeof(GridBarrier)));
-  OD_CUDA(tmp.alloc(&failed, sizeof(int)));
-  OD_CUDA(cudaMemsetAsync(gb, 0, sizeof(GridBarrier), c->stream));
-  OD_CUDA(cudaMemsetAsync(failed, 0, sizeof(int), c->stream));
-  void* args[] = {(void*)&gb, (void*)&failed};
+  OD_CUDA(tmp.alloc(&gb, 2 * sizeof(GridBarrier)));
+  OD_CUDA(tmp.alloc(&failed, 2 * sizeof(int)));
+  OD_CUDA(cudaMemsetAsync(gb, 0, 2 * sizeof(GridBarrier), c->stream));
+  OD_CUDA(cudaMemsetAsync(failed, 0, 2 * sizeof(int), c->stream));
+  GridBarrier* gb_count = gb + 1;
+  void* args[] = {(void*)&gb, (void*)&gb_count, (void*)&failed};
   cudaError_t e = cudaLaunchCooperativeKernel((void*)selftest_barrier_kernel, dim3(2), dim3(32), args, 0, c->stream);
-  GridBarrier h{};
-  int hf = 0;
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, gb, sizeof(GridBarrier), cudaMemcpyDeviceToHost, c->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&hf, failed, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  GridBarrier h[2]{};
+  int hf[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, gb, 2 * sizeof(GridBarrier), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hf, failed, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "barrier self-test");
-  *timed_out = h.timeout == 1 && hf == 1;
+  *timed_out = h[0].timeout == 1 && hf[0] == 1 && h[1].timeout == 1 && hf[1] == 1;
   return OD_OK;
 }
 
