@@ -480,7 +480,10 @@ od_status od_scene_evaluate(od_scene* scene, double* values, double* f_int) {
   OD_CHECK_ARG(scene, "od_scene_evaluate: scene is NULL");
   Scene* s = &scene->s;
   OD_CUDA(cudaSetDevice(s->ctx->device));
-  OD_TRY(launch_eval(s, true));
+  // OD_GB300_ELEMENT_DF=1: the mixed-precision path's double-float stiffness
+  // contraction (to compare it with the FP64 one)
+  const char* dfe = std::getenv("OD_GB300_ELEMENT_DF");
+  OD_TRY(launch_eval(s, true, dfe && dfe[0] == '1'));
   if (values) OD_CUDA(cudaMemcpyAsync(values, s->K, sizeof(double) * s->nvals, cudaMemcpyDeviceToHost, s->ctx->stream));
   if (f_int) OD_CUDA(cudaMemcpyAsync(f_int, s->fint, sizeof(double) * s->dofs, cudaMemcpyDeviceToHost, s->ctx->stream));
   OD_TRY(sync_stream(s));
@@ -707,7 +710,7 @@ static od_status be_step(Scene* s, od_step_stats* acc) {
   const int n = s->dofs, T = 256;
   cudaStream_t st = s->ctx->stream;
   const double h = p.dt;
-  OD_TRY(launch_eval(s, true));
+  OD_TRY(launch_eval(s, true, p.solver.precision == OD_PRECISION_MIXED));
   // A0 v with A0 = (h + beta_K) K + alpha_M M + D
   OD_TRY(launch_spmv_lower(s, s->K, h + p.beta_k, s->v, s->M, p.alpha_m, s->v, s->Dm, 1.0, s->v, s->tmp, false));
   OD_KL(s);
@@ -743,7 +746,7 @@ static od_status nm_step(Scene* s, od_step_stats* acc) {
     OD_KL(s);
     nm_stage_kernel<<<nblk(n, T), T, 0, st>>>(n, s->free_pos, bh2, gh, p.alpha_m, s->dp, s->vp, s->a, s->u, s->tmp,
                                               s->tmp2);
-    OD_TRY(launch_eval(s, true));
+    OD_TRY(launch_eval(s, true, p.solver.precision == OD_PRECISION_MIXED));
     // y = M (alpha_M v_k + a_k) + beta_K K v_k (+ D v_k)
     OD_TRY(launch_spmv_lower(s, s->M, 1.0, s->tmp, s->K, p.beta_k, s->tmp2, s->Dm, 1.0, s->tmp2, s->rhs, false));
     OD_KL(s);

@@ -287,6 +287,72 @@ __device__ __forceinline__ void corot_elem(int e, int ne, const int4* __restrict
   }
 }
 
+// ------------------------------------------------- double-float arithmetic
+// A value as hi + lo of two floats (about 46 significant bits), for the
+// mixed-precision path's element stiffness contraction: on this part the
+// FP64 units run at 1/70 of the FP32 rate and also execute every FP32 <->
+// FP64 conversion, so operands are split and results rebuilt with integer
+// bit operations, and the products and sums run on the FP32 units
+// (error-free TwoProduct by FMA and TwoSum, Dekker / Knuth).
+struct DFv {
+  float hi, lo;
+};
+
+// x = hi + lo + d with |d| <= 2^-47 |x|: hi is x with its significand cut to
+// 24 bits, lo the next 24 bits of the remainder.  Magnitudes below the
+// normal float range give 0; infinities and NaNs pass through hi.
+__device__ __forceinline__ DFv df_split(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7FF);
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  const int ef = e - 1023 + 127;
+  DFv r{0.f, 0.f};
+  if (ef >= 255) {
+    r.hi = __uint_as_float(sign | (e == 2047 && m ? 0x7FC00000u : 0x7F800000u));
+    return r;
+  }
+  if (ef <= 0) return r;
+  r.hi = __uint_as_float(sign | ((unsigned)ef << 23) | (unsigned)(m >> 29));
+  const unsigned rem = (unsigned)(m & 0x1FFFFFFFull);   // the remainder, in units of 2^(e-1075)
+  if (rem == 0) return r;
+  const int top = 31 - __clz((int)rem);                  // its leading bit, 0..28
+  const unsigned frac = (top >= 23 ? (rem >> (top - 23)) : (rem << (23 - top))) & 0x7FFFFFu;
+  const int elo = e - 1075 + top + 127;
+  if (elo > 0) r.lo = __uint_as_float(sign | ((unsigned)elo << 23) | frac);
+  return r;
+}
+
+// exact float -> double by bit operations (zero and subnormal floats give 0)
+__device__ __forceinline__ double df_widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned ef = (u >> 23) & 0xFFu;
+  if (ef == 0) return __longlong_as_double((long long)sign);
+  const unsigned long long e = ef == 255 ? 0x7FFull : (unsigned long long)(ef - 127 + 1023);
+  return __longlong_as_double((long long)(sign | (e << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
+
+__device__ __forceinline__ double df_value(DFv a) { return df_widen(a.hi) + df_widen(a.lo); }
+
+__device__ __forceinline__ DFv df_mul(DFv a, DFv b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);   // a.hi b.hi = p + e exactly
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const float s = p + e;
+  return DFv{s, e - (s - p)};
+}
+
+__device__ __forceinline__ DFv df_add(DFv a, DFv b) {
+  const float s = a.hi + b.hi;
+  const float v = s - a.hi;
+  const float t = (a.hi - (s - v)) + (b.hi - v);   // a.hi + b.hi = s + t exactly
+  const float lo = (t + a.lo) + b.lo;
+  const float r = s + lo;
+  return DFv{r, lo - (r - s)};
+}
+
 // ------------------------------------------- invertible hyperelastic element
 // Invertible SVD of F, energy derivatives in the invariants I1 = sum s^2,
 // I2 = sum s^4, I3 = prod s^2 (invertibleHyperelastic.h:22-30): Neo-Hookean
@@ -297,7 +363,7 @@ __device__ __forceinline__ void corot_elem(int e, int ne, const int4* __restrict
 // K_ab = U [sum_kl dP_ikjl (V^T dN_a)_k (V^T dN_b)_l] U^T / (36 V)
 // (tetelement.cpp:282-342); f_a = P dN_a / 6, f_3 = -(f_0 + f_1 + f_2)
 // (tetelement.cpp:344-355).
-template <int MODE>
+template <int MODE, bool DF = false>
 __device__ __forceinline__ void invhyper_elem(int e, int ne, int stvk, const int4* __restrict__ tets,
                                               const double* __restrict__ X, const double* __restrict__ u,
                                               const double* __restrict__ pre, double thr, double lambda, double mu,
@@ -401,6 +467,73 @@ __device__ __forceinline__ void invhyper_elem(int e, int ne, int stvk, const int
       out78[(size_t)k * ne + e] = val;
     }
   };
+  if constexpr (DF) {
+    // the contraction U [sum_kl dP_ikjl an_a,k an_b,l] U^T / (36 V) in
+    // double-float, the same terms in the same order as below
+    // Tm symmetric (6 values), Al and Be symmetric with zero diagonals (3 each)
+    DFv dan[4][3], dU[9], dT6[6], dA3[3], dB3[3];
+#pragma unroll
+    for (int nn = 0; nn < 4; nn++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) dan[nn][i] = df_split(an[nn][i]);
+#pragma unroll
+    for (int i = 0; i < 9; i++) dU[i] = df_split(U[i]);
+#pragma unroll
+    for (int i = 0; i < 6; i++) dT6[i] = df_split(T[i]);
+    dA3[0] = df_split(a01); dA3[1] = df_split(a02); dA3[2] = df_split(a12);
+    dB3[0] = df_split(b01); dB3[1] = df_split(b02); dB3[2] = df_split(b12);
+    auto sym6 = [](int i, int j) { return i <= j ? i * 3 - (i * (i - 1)) / 2 + (j - i) : j * 3 - (j * (j - 1)) / 2 + (i - j); };
+    auto off3 = [](int i, int j) { return i + j - 1; };   // (0,1) -> 0, (0,2) -> 1, (1,2) -> 2
+    const DFv dfac = df_split(fac);
+#pragma unroll 1
+    for (int a = 0; a < 4; a++) {
+#pragma unroll 1
+      for (int b = a; b < 4; b++) {
+        DFv sm[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++) {
+            DFv en{0.f, 0.f};
+            if (i == j) {
+#pragma unroll
+              for (int k = 0; k < 3; k++)
+                en = df_add(en, df_mul(df_mul(k == i ? dT6[sym6(i, i)] : dA3[off3(i, k)], dan[a][k]), dan[b][k]));
+            } else if (i < j) {
+              en = df_add(en, df_mul(df_mul(dT6[sym6(i, j)], dan[a][i]), dan[b][j]));
+              en = df_add(en, df_mul(df_mul(dB3[off3(i, j)], dan[a][j]), dan[b][i]));
+            } else {
+              en = df_add(en, df_mul(df_mul(dB3[off3(i, j)], dan[a][j]), dan[b][i]));
+              en = df_add(en, df_mul(df_mul(dT6[sym6(i, j)], dan[a][i]), dan[b][j]));
+            }
+            sm[i * 3 + j] = en;
+          }
+        DFv tmp[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++)
+            tmp[i * 3 + j] = df_add(df_add(df_mul(dU[i * 3], sm[j]), df_mul(dU[i * 3 + 1], sm[3 + j])),
+                                    df_mul(dU[i * 3 + 2], sm[6 + j]));
+        auto outv = [&](int i, int j) {
+          const DFv o = df_add(df_add(df_mul(tmp[i * 3], dU[j * 3]), df_mul(tmp[i * 3 + 1], dU[j * 3 + 1])),
+                               df_mul(tmp[i * 3 + 2], dU[j * 3 + 2]));
+          return df_value(df_mul(o, dfac));
+        };
+        if (a == b) {
+#pragma unroll
+          for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3 - i; j++) put(c_diag12[a * 3 + i] + j, outv(i, i + j));
+        } else {
+#pragma unroll
+          for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) put(c_diag12[a * 3 + i] + (b - a) * 3 - i + j, outv(i, j));
+        }
+      }
+    }
+  } else {
 #pragma unroll 1
   for (int a = 0; a < 4; a++) {
 #pragma unroll 1
@@ -442,6 +575,7 @@ __device__ __forceinline__ void invhyper_elem(int e, int ne, int stvk, const int
       }
     }
   }
+  }
   double f[12];
   const double sixth = 1.0 / 6.0;
 #pragma unroll
@@ -479,7 +613,7 @@ __global__ void __launch_bounds__(128) corot_kernel(int e0, int e1, int ne, cons
   if (e < e1) corot_elem<MODE>(e, ne, tets, X, u, pre, thr, emap, gdof, K, fint, out78, out12, perm);
 }
 
-template <int MODE>
+template <int MODE, bool DF = false>
 __global__ void __launch_bounds__(128) invhyper_kernel(int e0, int e1, int ne, int stvk, const int4* __restrict__ tets,
                                                        const double* __restrict__ X, const double* __restrict__ u,
                                                        const double* __restrict__ pre, double thr, double lambda,
@@ -489,7 +623,7 @@ __global__ void __launch_bounds__(128) invhyper_kernel(int e0, int e1, int ne, i
                                                        double* __restrict__ out12, const int* __restrict__ perm) {
   const int e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (e < e1)
-    invhyper_elem<MODE>(e, ne, stvk, tets, X, u, pre, thr, lambda, mu, emap, gdof, K, fint, out78, out12, perm);
+    invhyper_elem<MODE, DF>(e, ne, stvk, tets, X, u, pre, thr, lambda, mu, emap, gdof, K, fint, out78, out12, perm);
 }
 
 // ---- several scenes per launch: tile j of scene s (directory prefix) is
@@ -511,8 +645,9 @@ __global__ void __launch_bounds__(128) invhyper_batch_kernel(int n_sc, const int
   const SceneDev& D = sd[s];
   const int e = (blockIdx.x - prefix[s]) * 128 + threadIdx.x;
   if (e >= D.n_tets) return;
-  invhyper_elem<2>(e, D.n_tets, D.kind == OD_MATERIAL_STVK, D.tets, D.X, D.u, D.pre, D.thr, D.lambda, D.mu, D.emap,
-                   D.gdof, nullptr, nullptr, D.stage_k, D.stage_f, nullptr);
+  // batched scenes all run the mixed-precision solver: double-float contraction
+  invhyper_elem<2, true>(e, D.n_tets, D.kind == OD_MATERIAL_STVK, D.tets, D.X, D.u, D.pre, D.thr, D.lambda, D.mu,
+                         D.emap, D.gdof, nullptr, nullptr, D.stage_k, D.stage_f, nullptr);
 }
 
 // Corotational plastic element (corotationalPlastic.cpp:53-183,
@@ -1039,7 +1174,7 @@ od_status launch_mass(Scene* s) {
   return OD_OK;
 }
 
-od_status launch_eval(Scene* s, bool zero_first) {
+od_status launch_eval(Scene* s, bool zero_first, bool df) {
   const int T = 128;
   cudaStream_t st = s->ctx->stream;
   if (zero_first && (!s->gat_kptr || s->n_tets == 0)) {
@@ -1058,6 +1193,12 @@ od_status launch_eval(Scene* s, bool zero_first) {
     corot_kernel<2><<<nblk(s->n_tets, T), T, 0, st>>>(0, s->n_tets, s->n_tets, s->tets, s->X, s->u, s->pre,
                                                        s->mat.threshold, s->emap, s->gdof, nullptr, nullptr, s->stage_k,
                                                        s->stage_f, nullptr);
+  else if (df)
+    invhyper_kernel<2, true><<<nblk(s->n_tets, T), T, 0, st>>>(0, s->n_tets, s->n_tets,
+                                                                s->mat.kind == OD_MATERIAL_STVK, s->tets, s->X, s->u,
+                                                                s->pre, s->mat.threshold, s->lambda, s->mu, s->emap,
+                                                                s->gdof, nullptr, nullptr, s->stage_k, s->stage_f,
+                                                                nullptr);
   else
     invhyper_kernel<2><<<nblk(s->n_tets, T), T, 0, st>>>(0, s->n_tets, s->n_tets, s->mat.kind == OD_MATERIAL_STVK,
                                                           s->tets, s->X, s->u, s->pre, s->mat.threshold, s->lambda,

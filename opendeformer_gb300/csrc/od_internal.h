@@ -487,7 +487,9 @@ void ric_factor(const RicColumns& A, const double* values, double eps, double re
 // ---- kernels (od_elements.cu) ----
 od_status launch_precompute(Scene* s);
 od_status launch_mass(Scene* s);
-od_status launch_eval(Scene* s, bool zero_first);       // K, fint at current u
+// K, fint at current u; df: the mixed-precision path's double-float stiffness
+// contraction (invertible materials; the others are unchanged)
+od_status launch_eval(Scene* s, bool zero_first, bool df = false);
 od_status launch_hooke(Scene* s, double youngs, double poisson, double* Kh);  // linear K, reference layout
 od_status launch_element_values(Scene* s, double* d_k78, double* d_f12);
 od_status launch_loads(Scene* s, const double* body, int n_facets_total, double traction_scale);
