@@ -412,8 +412,14 @@ __device__ __forceinline__ void invhyper_elem(int e, int ne, int stvk, const int
   double a02 = 2.0 * g0 + 4.0 * (s02 + s22) * g1;
   double a12 = 2.0 * g0 + 4.0 * (s12 + s22) * g1;
   const double a00 = 2.0 * g0 + 8.0 * s02 * g1, a11 = 2.0 * g0 + 8.0 * s12 * g1, a22 = 2.0 * g0 + 8.0 * s22 * g1;
-  const double d00 = I3 * g2 / s02, d01 = I3 * g2 / sc01, d02 = I3 * g2 / sc02;
-  const double d11 = I3 * g2 / s12, d12 = I3 * g2 / sc12, d22 = I3 * g2 / s22;
+  // d_ij = I3 g2 / (s_i s_j); the mixed path forms them as products
+  // (I3 / (s_i s_j) is the product of the other factors: FP64 divisions are
+  // long instruction sequences on this part).  The forces keep the exact
+  // expressions.
+  const double d00 = DF ? g2 * (s12 * s22) : I3 * g2 / s02, d01 = DF ? g2 * (sc01 * s22) : I3 * g2 / sc01,
+               d02 = DF ? g2 * (sc02 * s12) : I3 * g2 / sc02;
+  const double d11 = DF ? g2 * (s02 * s22) : I3 * g2 / s12, d12 = DF ? g2 * (sc12 * s02) : I3 * g2 / sc12,
+               d22 = DF ? g2 * (s02 * s12) : I3 * g2 / s22;
   const double b00 = 4.0 * s02 * g1 - 2.0 * d00, b11 = 4.0 * s12 * g1 - 2.0 * d11, b22 = 4.0 * s22 * g1 - 2.0 * d22;
   double b01 = 4.0 * sc01 * g1 - 2.0 * d01, b02 = 4.0 * sc02 * g1 - 2.0 * d02, b12 = 4.0 * sc12 * g1 - 2.0 * d12;
   // Hessian in the invariants is diag-like: only H00 (StVK) or H22 (NH) set
@@ -422,7 +428,7 @@ __device__ __forceinline__ void invhyper_elem(int e, int ne, int stvk, const int
   for (int i = 0; i < 3; i++) {
     w[i][0] = 2.0 * sig[i];
     w[i][1] = 4.0 * sig[i] * (i == 0 ? s02 : (i == 1 ? s12 : s22));
-    w[i][2] = 2.0 * I3 / sig[i];
+    w[i][2] = DF ? 2.0 * sig[i] * (i == 0 ? s12 * s22 : (i == 1 ? s02 * s22 : s02 * s12)) : 2.0 * I3 / sig[i];
   }
   // w_i . (H w_j) with H = diag(h0, 0, h5) in the invariants (the only
   // non-zero Hessian entries of both energies)
