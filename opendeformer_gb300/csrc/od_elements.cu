@@ -163,130 +163,6 @@ __global__ void loads_kernel(int n, int dofs, const int* __restrict__ free_pos, 
   fext[i] = acc;
 }
 
-// -------------------------------------------------- corotational element
-// F = [x1-x0, x2-x0, x3-x0] Dm^-1; R = polar(F), or the proper QR factor when
-// the deformed volume is below threshold * rest volume
-// (tetelement.cpp:546-573); K_ab = R K0_ab R^T packed into 78 values and
-// f_a = sum_b (R K0_ab R^T x_b - R K0_ab X_b) (tetelement.cpp:583-651).
-// MODE 0 scatters into K / fint through the element map (one colour per
-// launch); MODE 1 stores per-element values in original element order;
-// MODE 2 stores them in the colour-ordered staging arrays (all elements in
-// one launch, scattered afterwards colour by colour).
-template <int MODE>
-__device__ __forceinline__ void corot_elem(int e, int ne, const int4* __restrict__ tets,
-                                           const double* __restrict__ X, const double* __restrict__ u,
-                                           const double* __restrict__ pre, double thr,
-                                           const int* __restrict__ emap, const int* __restrict__ gdof,
-                                           double* __restrict__ K, double* __restrict__ fint,
-                                           double* __restrict__ out78, double* __restrict__ out12,
-                                           const int* __restrict__ perm) {
-  int4 t = tets[e];
-  const int nd[4] = {t.x, t.y, t.z, t.w};
-  V3t<double> o[4], c[4];
-#pragma unroll
-  for (int i = 0; i < 4; i++) {
-    o[i] = ld3(X, nd[i]);
-    V3t<double> du = ld3(u, nd[i]);
-    c[i] = {o[i].x + du.x, o[i].y + du.y, o[i].z + du.z};
-  }
-  double Di[9], F[9];
-#pragma unroll
-  for (int i = 0; i < 9; i++) { Di[i] = pre[(size_t)(90 + i) * ne + e]; F[i] = 0.0; }
-#pragma unroll
-  for (int i = 1; i < 4; i++) {
-    double ax[3] = {c[i].x - c[0].x, c[i].y - c[0].y, c[i].z - c[0].z};
-#pragma unroll
-    for (int j = 0; j < 3; j++)
-#pragma unroll
-      for (int k = 0; k < 3; k++) F[j * 3 + k] += ax[j] * Di[(i - 1) * 3 + k];
-  }
-  const double v0 = pre[(size_t)99 * ne + e];
-  const double v1 = tet_vol(c[0], c[1], c[2], c[3]);
-  double R[9];
-  if (v1 >= thr * v0) polar3<double>(F, R);
-  else qr3<double>(F, R);
-
-  double f[12];
-#pragma unroll
-  for (int i = 0; i < 12; i++) f[i] = 0.0;
-  const size_t obase = MODE == 1 ? (size_t)perm[e] * 78 : 0;
-  auto put = [&](int k, double val) {
-    if (MODE == 0) {
-      int idx = emap[(size_t)k * ne + e];
-      if (idx >= 0) K[idx] += val;
-    } else if (MODE == 1) {
-      out78[obase + k] = val;
-    } else {
-      out78[(size_t)k * ne + e] = val;
-    }
-  };
-  int blk = 0;
-#pragma unroll 1
-  for (int a = 0; a < 4; a++) {
-    double K0[9], QK[9], QKQT[9];
-#pragma unroll
-    for (int i = 0; i < 9; i++) K0[i] = pre[(size_t)(9 * blk + i) * ne + e];
-    blk++;
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++) QK[i * 3 + j] = R[i * 3] * K0[j] + R[i * 3 + 1] * K0[3 + j] + R[i * 3 + 2] * K0[6 + j];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++) QKQT[i * 3 + j] = QK[i * 3] * R[j * 3] + QK[i * 3 + 1] * R[j * 3 + 1] + QK[i * 3 + 2] * R[j * 3 + 2];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3 - i; j++) put(c_diag12[a * 3 + i] + j, QKQT[i * 3 + i + j]);
-    const double ca[3] = {c[a].x, c[a].y, c[a].z}, oa[3] = {o[a].x, o[a].y, o[a].z};
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++) f[a * 3 + i] += QKQT[i * 3 + j] * ca[j] - QK[i * 3 + j] * oa[j];
-#pragma unroll 1
-    for (int b = a + 1; b < 4; b++) {
-      double QKT[9];
-#pragma unroll
-      for (int i = 0; i < 9; i++) K0[i] = pre[(size_t)(9 * blk + i) * ne + e];
-      blk++;
-#pragma unroll
-      for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-          QK[i * 3 + j] = R[i * 3] * K0[j] + R[i * 3 + 1] * K0[3 + j] + R[i * 3 + 2] * K0[6 + j];
-          QKT[i * 3 + j] = R[i * 3] * K0[j * 3] + R[i * 3 + 1] * K0[j * 3 + 1] + R[i * 3 + 2] * K0[j * 3 + 2];
-        }
-#pragma unroll
-      for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) QKQT[i * 3 + j] = QK[i * 3] * R[j * 3] + QK[i * 3 + 1] * R[j * 3 + 1] + QK[i * 3 + 2] * R[j * 3 + 2];
-      const double cb[3] = {c[b].x, c[b].y, c[b].z}, ob[3] = {o[b].x, o[b].y, o[b].z};
-#pragma unroll
-      for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int j = 0; j < 3; j++) {
-          put(c_diag12[a * 3 + i] + (b - a) * 3 - i + j, QKQT[i * 3 + j]);
-          f[a * 3 + i] += QKQT[i * 3 + j] * cb[j] - QK[i * 3 + j] * ob[j];
-          f[b * 3 + i] += QKQT[j * 3 + i] * ca[j] - QKT[i * 3 + j] * oa[j];
-        }
-    }
-  }
-  if (MODE == 0) {
-#pragma unroll
-    for (int k = 0; k < 12; k++) {
-      int g = gdof[(size_t)k * ne + e];
-      if (g >= 0) fint[g] += f[k];
-    }
-  } else if (MODE == 1) {
-#pragma unroll
-    for (int k = 0; k < 12; k++) out12[(size_t)perm[e] * 12 + k] = f[k];
-  } else {
-#pragma unroll
-    for (int k = 0; k < 12; k++) out12[(size_t)k * ne + e] = f[k];
-  }
-}
-
 // ------------------------------------------------- double-float arithmetic
 // A value as hi + lo of two floats (about 46 significant bits), for the
 // mixed-precision path's element stiffness contraction: on this part the
@@ -351,6 +227,191 @@ __device__ __forceinline__ DFv df_add(DFv a, DFv b) {
   const float lo = (t + a.lo) + b.lo;
   const float r = s + lo;
   return DFv{r, lo - (r - s)};
+}
+
+// -------------------------------------------------- corotational element
+// F = [x1-x0, x2-x0, x3-x0] Dm^-1; R = polar(F), or the proper QR factor when
+// the deformed volume is below threshold * rest volume
+// (tetelement.cpp:546-573); K_ab = R K0_ab R^T packed into 78 values and
+// f_a = sum_b (R K0_ab R^T x_b - R K0_ab X_b) (tetelement.cpp:583-651).
+// MODE 0 scatters into K / fint through the element map (one colour per
+// launch); MODE 1 stores per-element values in original element order;
+// MODE 2 stores them in the colour-ordered staging arrays (all elements in
+// one launch, scattered afterwards colour by colour).
+template <int MODE, bool DF = false>
+__device__ __forceinline__ void corot_elem(int e, int ne, const int4* __restrict__ tets,
+                                           const double* __restrict__ X, const double* __restrict__ u,
+                                           const double* __restrict__ pre, double thr,
+                                           const int* __restrict__ emap, const int* __restrict__ gdof,
+                                           double* __restrict__ K, double* __restrict__ fint,
+                                           double* __restrict__ out78, double* __restrict__ out12,
+                                           const int* __restrict__ perm) {
+  int4 t = tets[e];
+  const int nd[4] = {t.x, t.y, t.z, t.w};
+  V3t<double> o[4], c[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    o[i] = ld3(X, nd[i]);
+    V3t<double> du = ld3(u, nd[i]);
+    c[i] = {o[i].x + du.x, o[i].y + du.y, o[i].z + du.z};
+  }
+  double Di[9], F[9];
+#pragma unroll
+  for (int i = 0; i < 9; i++) { Di[i] = pre[(size_t)(90 + i) * ne + e]; F[i] = 0.0; }
+#pragma unroll
+  for (int i = 1; i < 4; i++) {
+    double ax[3] = {c[i].x - c[0].x, c[i].y - c[0].y, c[i].z - c[0].z};
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) F[j * 3 + k] += ax[j] * Di[(i - 1) * 3 + k];
+  }
+  const double v0 = pre[(size_t)99 * ne + e];
+  const double v1 = tet_vol(c[0], c[1], c[2], c[3]);
+  double R[9];
+  if (v1 >= thr * v0) polar3<double>(F, R);
+  else qr3<double>(F, R);
+
+  double f[12];
+#pragma unroll
+  for (int i = 0; i < 12; i++) f[i] = 0.0;
+  const size_t obase = MODE == 1 ? (size_t)perm[e] * 78 : 0;
+  auto put = [&](int k, double val) {
+    if (MODE == 0) {
+      int idx = emap[(size_t)k * ne + e];
+      if (idx >= 0) K[idx] += val;
+    } else if (MODE == 1) {
+      out78[obase + k] = val;
+    } else {
+      out78[(size_t)k * ne + e] = val;
+    }
+  };
+  if constexpr (DF) {
+    // The mixed-precision path: forces f_a = R sum_b K0_ab (R^T c_b - o_b) in
+    // FP64 (the same sum regrouped, the cancellation of R^T c_b against o_b
+    // taken first) and the stiffness R K0_ab R^T in double-float.
+    double y[4][3], g[4][3];
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      const double cb[3] = {c[b].x, c[b].y, c[b].z}, ob[3] = {o[b].x, o[b].y, o[b].z};
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        y[b][i] = (R[i] * cb[0] + R[3 + i] * cb[1] + R[6 + i] * cb[2]) - ob[i];
+        g[b][i] = 0.0;
+      }
+    }
+    DFv dR[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) dR[i] = df_split(R[i]);
+    int blk = 0;
+#pragma unroll 1
+    for (int a = 0; a < 4; a++) {
+#pragma unroll 1
+      for (int b = a; b < 4; b++) {
+        double K0[9];
+#pragma unroll
+        for (int i = 0; i < 9; i++) K0[i] = pre[(size_t)(9 * blk + i) * ne + e];
+        blk++;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+          g[a][i] += K0[i * 3] * y[b][0] + K0[i * 3 + 1] * y[b][1] + K0[i * 3 + 2] * y[b][2];
+          if (b != a) g[b][i] += K0[i] * y[a][0] + K0[3 + i] * y[a][1] + K0[6 + i] * y[a][2];
+        }
+        DFv dQK[9];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+          for (int j = 0; j < 3; j++)
+            dQK[i * 3 + j] = df_add(df_add(df_mul(dR[i * 3], df_split(K0[j])), df_mul(dR[i * 3 + 1], df_split(K0[3 + j]))),
+                                    df_mul(dR[i * 3 + 2], df_split(K0[6 + j])));
+        auto qkqt = [&](int i, int j) {
+          return df_value(df_add(df_add(df_mul(dQK[i * 3], dR[j * 3]), df_mul(dQK[i * 3 + 1], dR[j * 3 + 1])),
+                                 df_mul(dQK[i * 3 + 2], dR[j * 3 + 2])));
+        };
+        if (a == b) {
+#pragma unroll
+          for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3 - i; j++) put(c_diag12[a * 3 + i] + j, qkqt(i, i + j));
+        } else {
+#pragma unroll
+          for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) put(c_diag12[a * 3 + i] + (b - a) * 3 - i + j, qkqt(i, j));
+        }
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) f[a * 3 + i] = R[i * 3] * g[a][0] + R[i * 3 + 1] * g[a][1] + R[i * 3 + 2] * g[a][2];
+  } else {
+  int blk = 0;
+#pragma unroll 1
+  for (int a = 0; a < 4; a++) {
+    double K0[9], QK[9], QKQT[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) K0[i] = pre[(size_t)(9 * blk + i) * ne + e];
+    blk++;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) QK[i * 3 + j] = R[i * 3] * K0[j] + R[i * 3 + 1] * K0[3 + j] + R[i * 3 + 2] * K0[6 + j];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) QKQT[i * 3 + j] = QK[i * 3] * R[j * 3] + QK[i * 3 + 1] * R[j * 3 + 1] + QK[i * 3 + 2] * R[j * 3 + 2];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3 - i; j++) put(c_diag12[a * 3 + i] + j, QKQT[i * 3 + i + j]);
+    const double ca[3] = {c[a].x, c[a].y, c[a].z}, oa[3] = {o[a].x, o[a].y, o[a].z};
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) f[a * 3 + i] += QKQT[i * 3 + j] * ca[j] - QK[i * 3 + j] * oa[j];
+#pragma unroll 1
+    for (int b = a + 1; b < 4; b++) {
+      double QKT[9];
+#pragma unroll
+      for (int i = 0; i < 9; i++) K0[i] = pre[(size_t)(9 * blk + i) * ne + e];
+      blk++;
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          QK[i * 3 + j] = R[i * 3] * K0[j] + R[i * 3 + 1] * K0[3 + j] + R[i * 3 + 2] * K0[6 + j];
+          QKT[i * 3 + j] = R[i * 3] * K0[j * 3] + R[i * 3 + 1] * K0[j * 3 + 1] + R[i * 3 + 2] * K0[j * 3 + 2];
+        }
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) QKQT[i * 3 + j] = QK[i * 3] * R[j * 3] + QK[i * 3 + 1] * R[j * 3 + 1] + QK[i * 3 + 2] * R[j * 3 + 2];
+      const double cb[3] = {c[b].x, c[b].y, c[b].z}, ob[3] = {o[b].x, o[b].y, o[b].z};
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+          put(c_diag12[a * 3 + i] + (b - a) * 3 - i + j, QKQT[i * 3 + j]);
+          f[a * 3 + i] += QKQT[i * 3 + j] * cb[j] - QK[i * 3 + j] * ob[j];
+          f[b * 3 + i] += QKQT[j * 3 + i] * ca[j] - QKT[i * 3 + j] * oa[j];
+        }
+    }
+  }
+  }
+  if (MODE == 0) {
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+      int g = gdof[(size_t)k * ne + e];
+      if (g >= 0) fint[g] += f[k];
+    }
+  } else if (MODE == 1) {
+#pragma unroll
+    for (int k = 0; k < 12; k++) out12[(size_t)perm[e] * 12 + k] = f[k];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 12; k++) out12[(size_t)k * ne + e] = f[k];
+  }
 }
 
 // ------------------------------------------- invertible hyperelastic element
@@ -607,7 +668,7 @@ __device__ __forceinline__ void invhyper_elem(int e, int ne, int stvk, const int
   }
 }
 
-template <int MODE>
+template <int MODE, bool DF = false>
 __global__ void __launch_bounds__(128) corot_kernel(int e0, int e1, int ne, const int4* __restrict__ tets,
                                                     const double* __restrict__ X, const double* __restrict__ u,
                                                     const double* __restrict__ pre, double thr,
@@ -616,7 +677,7 @@ __global__ void __launch_bounds__(128) corot_kernel(int e0, int e1, int ne, cons
                                                     double* __restrict__ out78, double* __restrict__ out12,
                                                     const int* __restrict__ perm) {
   const int e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < e1) corot_elem<MODE>(e, ne, tets, X, u, pre, thr, emap, gdof, K, fint, out78, out12, perm);
+  if (e < e1) corot_elem<MODE, DF>(e, ne, tets, X, u, pre, thr, emap, gdof, K, fint, out78, out12, perm);
 }
 
 template <int MODE, bool DF = false>
@@ -641,8 +702,9 @@ __global__ void __launch_bounds__(128) corot_batch_kernel(int n_sc, const int* _
   const SceneDev& D = sd[s];
   const int e = (blockIdx.x - prefix[s]) * 128 + threadIdx.x;
   if (e >= D.n_tets) return;
-  corot_elem<2>(e, D.n_tets, D.tets, D.X, D.u, D.pre, D.thr, D.emap, D.gdof, nullptr, nullptr, D.stage_k, D.stage_f,
-                nullptr);
+  // batched scenes all run the mixed-precision solver: double-float stiffness
+  corot_elem<2, true>(e, D.n_tets, D.tets, D.X, D.u, D.pre, D.thr, D.emap, D.gdof, nullptr, nullptr, D.stage_k,
+                      D.stage_f, nullptr);
 }
 
 __global__ void __launch_bounds__(128) invhyper_batch_kernel(int n_sc, const int* __restrict__ prefix,
@@ -1195,6 +1257,10 @@ od_status launch_eval(Scene* s, bool zero_first, bool df) {
                                                          s->lambda, s->mu, s->mat.yield_criterion,
                                                          s->mat.creep_ratio, s->mat.max_plastic_strain, s->plastic,
                                                          s->stage_k, s->stage_f, nullptr);
+  else if (s->mat.kind == OD_MATERIAL_COROTATIONAL && df)
+    corot_kernel<2, true><<<nblk(s->n_tets, T), T, 0, st>>>(0, s->n_tets, s->n_tets, s->tets, s->X, s->u, s->pre,
+                                                             s->mat.threshold, s->emap, s->gdof, nullptr, nullptr,
+                                                             s->stage_k, s->stage_f, nullptr);
   else if (s->mat.kind == OD_MATERIAL_COROTATIONAL)
     corot_kernel<2><<<nblk(s->n_tets, T), T, 0, st>>>(0, s->n_tets, s->n_tets, s->tets, s->X, s->u, s->pre,
                                                        s->mat.threshold, s->emap, s->gdof, nullptr, nullptr, s->stage_k,
@@ -1253,6 +1319,31 @@ od_status launch_element_values(Scene* s, double* d_k78, double* d_f12) {
                                                           s->perm);
   OD_CUDA(cudaGetLastError());
   return OD_OK;
+}
+
+// every (facet, traction) pair of the scene gets the same traction vector
+__global__ void fill_traction_kernel(int n, double tx, double ty, double tz, double* __restrict__ tvec) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) {
+    tvec[3 * k] = tx;
+    tvec[3 * k + 1] = ty;
+    tvec[3 * k + 2] = tz;
+  }
+}
+
+// New load values on the facet list of the scene's last od_scene_set_loads
+// (one traction group): the traction vector is written on the device and
+// the external forces re-evaluated, no copy and no synchronisation.
+od_status scene_set_uniform_loads(Scene* s, const double* body, const double* traction) {
+  if (traction && s->n_trac > 0) {
+    OD_KL(s);
+    fill_traction_kernel<<<nblk(s->n_trac, 128), 128, 0, s->ctx->stream>>>(s->n_trac, traction[0], traction[1],
+                                                                            traction[2], s->trac_vec);
+  }
+  s->has_body = body != nullptr;
+  if (body)
+    for (int i = 0; i < 3; i++) s->load_body[i] = body[i];
+  return launch_loads(s, body, traction ? s->n_trac : 0, 1.0);
 }
 
 // body part then traction colours; s->trac_* hold the colour-ordered facets

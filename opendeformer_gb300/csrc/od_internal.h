@@ -491,6 +491,8 @@ od_status launch_mass(Scene* s);
 // contraction (invertible materials; the others are unchanged)
 od_status launch_eval(Scene* s, bool zero_first, bool df = false);
 od_status launch_hooke(Scene* s, double youngs, double poisson, double* Kh);  // linear K, reference layout
+// new body force / uniform traction on the facets of the last od_scene_set_loads
+od_status scene_set_uniform_loads(Scene* s, const double* body, const double* traction);
 od_status launch_element_values(Scene* s, double* d_k78, double* d_f12);
 od_status launch_loads(Scene* s, const double* body, int n_facets_total, double traction_scale);
 // multi-scene element evaluation: zero K (values) and f_int (padded DOFs),

@@ -61,6 +61,10 @@ struct Slot {
   std::vector<unsigned char> blob;  // checkpoint while evicted (written by the caller's thread,
   bool has_blob = false;            //  read by the worker only while the slot is building)
   std::deque<Request> queue;
+  // the resident scene's load layout: set once per residency by a full
+  // od_scene_set_loads; later requests only change the values
+  bool loads_ready = false;
+  bool trac_on = false;
 };
 
 struct Built {
@@ -143,6 +147,7 @@ void adopt(od_server* sv, Slot& sl, od_scene* sc) {
   sc->s.ctx = &sv->ctx->c;
   sl.scene = sc;
   sl.state = Slot::kResident;
+  sl.loads_ready = false;
   sl.has_blob = false;
   sl.blob.clear();
   sl.blob.shrink_to_fit();
@@ -220,8 +225,13 @@ od_status apply_request(Slot& sl, const od_step_request& r) {
   OD_TRY(od_integrator_update(sl.scene, &p));
   const int nlf = (int)sl.load_facets.size();
   const bool trac = nlf > 0 && (r.traction[0] != 0.0 || r.traction[1] != 0.0 || r.traction[2] != 0.0);
-  return od_scene_set_loads(sl.scene, r.body, trac ? 1 : 0, trac ? r.traction : nullptr, trac ? &nlf : nullptr,
-                            trac ? sl.load_facets.data() : nullptr);
+  if (sl.loads_ready && sl.trac_on == trac)   // same facets: new values on the device only
+    return scene_set_uniform_loads(&sl.scene->s, r.body, trac ? r.traction : nullptr);
+  OD_TRY(od_scene_set_loads(sl.scene, r.body, trac ? 1 : 0, trac ? r.traction : nullptr, trac ? &nlf : nullptr,
+                            trac ? sl.load_facets.data() : nullptr));
+  sl.loads_ready = true;
+  sl.trac_on = trac;
+  return OD_OK;
 }
 
 }  // namespace
