@@ -1022,18 +1022,23 @@ def serving_tier(args, api, ctx):
         sv.close()
         lat = sorted(1000.0 * (r.done - r.arrival) for r in done)
         bad = [r for r in done if r.status != 0]
+        its = sorted(r.pcg_iterations for r in done if r.status == 0)
         return {"offered_per_s": rate, "window_s": window, "offered": len(arr), "completed": len(done),
                 "failed": len(bad), "backlog_at_end": backlog, "steps_per_s": len(done) / wall,
                 "ok_steps_per_s": (len(done) - len(bad)) / wall,
                 "p50_ms": lat[len(lat) // 2] if lat else None,
                 "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None,
                 "mean_batch": stats["steps"] / max(1, stats["ticks"]), "warmed_scenes": warmed, "warm_s": warm_s,
+                "pcg_iterations": {"mean": float(np.mean(its)) if its else None,
+                                   "p50": its[len(its) // 2] if its else None,
+                                   "p99": its[min(len(its) - 1, int(0.99 * len(its)))] if its else None,
+                                   "max": its[-1] if its else None},
                 "fp64_fallbacks": ctx.counters().mix_fallbacks,
                 "fp64_fallback_s": ctx.counters().mix_fallback_ms / 1000.0,
                 "failed_detail": [{"scene": r.scene, "status": r.status, "iterations": r.pcg_iterations,
                                    "E": pool[r.scene]["E"], "kind": pool[r.scene]["kind"]} for r in bad][:4],
                 **{k: stats[k] for k in ("ticks", "admissions", "restores", "evictions", "deferred", "s_admit",
-                                         "s_loads", "s_step", "s_build", "s_worker")}}
+                                         "s_loads", "s_step", "s_build", "s_device", "s_worker")}}
 
     window = args.serving_seconds
     sat_b = run(True, args.serving_rate, window, 9)

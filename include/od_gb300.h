@@ -466,6 +466,7 @@ typedef struct od_server_stats {
   double s_worker;          /* worker thread: building scenes (overlaps the ticks) */
   long long resident, resident_bytes, budget_bytes;
   double s_build;           /* of s_step: building and freeing the tick's batch */
+  double s_device;          /* device time of the steps (CUDA events around each batch or scene step) */
 } od_server_stats;
 od_status od_server_create(od_ctx* ctx, const od_server_config* cfg, od_server** out);
 od_status od_server_destroy(od_server* server);

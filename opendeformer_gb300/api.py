@@ -138,7 +138,7 @@ class od_server_stats(C.Structure):
                 ("restores", C.c_longlong), ("evictions", C.c_longlong), ("deferred", C.c_longlong),
                 ("s_admit", C.c_double), ("s_loads", C.c_double), ("s_step", C.c_double), ("s_worker", C.c_double),
                 ("resident", C.c_longlong), ("resident_bytes", C.c_longlong), ("budget_bytes", C.c_longlong),
-                ("s_build", C.c_double)]
+                ("s_build", C.c_double), ("s_device", C.c_double)]
 
 
 class od_modal_params(C.Structure):

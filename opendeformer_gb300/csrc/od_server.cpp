@@ -491,6 +491,11 @@ od_status od_server_tick(od_server* sv, int capacity, od_step_result* results, i
   }
   const auto tk3 = clock_type::now();
   sv->stats.s_step += std::chrono::duration<double>(tk3 - tk2).count();
+  if (sv->cfg.batched) {
+    if (!st.empty()) sv->stats.s_device += 1e-3 * st[0].device_ms;   // one event pair around the batch step
+  } else {
+    for (const od_step_stats& x : st) sv->stats.s_device += 1e-3 * x.device_ms;
+  }
   const double t_done = now_s(sv);
   for (size_t k = 0; k < reqs.size(); k++) {
     od_step_result& r = results[k];
