@@ -1282,11 +1282,15 @@ def run_gpu(args, wl):
             phases[f"{k}_cta_mean"] = round(1000.0 * pc.pcg_work_mean_ms[j] / pc.pcg_phase_iterations, 3)
         phases["iterations"] = pc.pcg_phase_iterations
         phases["us_per_iteration_timed_steps"] = round(1000.0 * counters.pcg_ms / max(1, counters.pcg_iterations), 3)
+        phases["note_pipelined"] = ("the pipelined form (one sync per iteration, the default for this tolerance "
+                                    "and size) fills spmv_pq (the product and the recurrences), update_rz_rr (the "
+                                    "dot partials and M^-1 w) and rz_rr_sum (its one grid-wide sum); the other "
+                                    "phases and the per-CTA figures stay 0")
         phases["note"] = ("one extra step after the timed ones with the phase timers on: us per PCG iteration "
                           "on the clock of CTA 0 (%globaltimer); a *_sum or barrier phase includes the wait for "
                           "the slowest CTA; *_cta_max / *_cta_mean: every CTA's own work in the phase (its warps, "
                           "no waits), slowest CTA per solve and mean; the timers themselves add about 2 us")
-        roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+    roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                 "peak_source": peak_kind, "algorithmic_bytes_per_launch": nbytes,
                 "avg_launch_ms": avg_ms, "launches": kl,

@@ -704,8 +704,124 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
     return rl;
   };
 
+  double rz = 0.0, bb = 0.0, rr = 0.0, eps = 0.0;
+  int it = 0, status = OD_OK;
+  if (GPW > 0 && recur == 2) {
+    // ---- pipelined PCG (Ghysels and Vanroose, 2014): u = M^-1 r, w = A u
+    // and m = M^-1 w are carried by recurrences, so an iteration's three dot
+    // products (r.u, w.u, r.r) and the completion of m, which the product
+    // gathers, share one grid-wide sync.  m alternates between two arrays
+    // and the sums' partials between two halves by iteration parity: a CTA
+    // can only write an array again after the next sync, which every CTA
+    // reaches after its last read.  Same iterates as the reference's PCG in
+    // exact arithmetic; the stop test is the reference's, on r.r.
+    double uv[NR], wv[NR], sv[NR], zr[NR], mv[NR];
+    double* const mbuf[2] = {z, q};
+    double* const pbuf[2] = {part, part + 3 * (size_t)G};
+    double bbl = 0.0;
+    OD_GROUP_LOOP(k, g) {
+      const int row = g * kRowsPerWarp + lane / 3;
+      const bool valid = lane < 30 && row < nb;
+      const int i = 3 * row + rsub;
+      double bv = 0.0, rl = 0.0;
+      if (valid) {
+        bv = b[i];
+        xr[k] = x[i];
+        rl = bv - row_product(k, row, x);
+      }
+      const double ul = apply_precond(k, row, valid, rl);
+      if (valid) {
+        rv[k] = rl;
+        uv[k] = ul;
+        pv[k] = qv[k] = sv[k] = zr[k] = 0.0;
+        p[i] = ul;   // gathered by w = A u
+        bbl = fma(bv, bv, bbl);
+      }
+    }
+    {
+      double v1[1] = {bbl};
+      if (!grid_sums<1>(v1, part + 6 * (size_t)G, gb)) return;
+      bb = v1[0];
+    }
+    OD_GROUP_LOOP(k, g) {
+      const int row = g * kRowsPerWarp + lane / 3;
+      if (lane < 30 && row < nb) wv[k] = row_product(k, row, p);
+    }
+    eps = bb * tol * tol;
+    double gam_prev = 1.0, alpha_prev = 1.0;
+    // profiling: CTA 0's clock into the slots of the standard form: the
+    // product and recurrences -> [0], the dots and m -> [2], the sum -> [3]
+    const bool ptimer = prof && blockIdx.x == 0 && threadIdx.x == 0;
+    unsigned long long pt = 0;
+    auto pstamp = [&](int slot) {
+      if (!ptimer) return;
+      unsigned long long t;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+      if (slot >= 0) prof[slot] += t - pt;
+      pt = t;
+    };
+    for (;;) {
+      const int par = it & 1;
+      pstamp(-1);
+      double ga = 0.0, de = 0.0, rrl = 0.0;
+      OD_GROUP_LOOP(k, g) {
+        const int row = g * kRowsPerWarp + lane / 3;
+        const bool valid = lane < 30 && row < nb;
+        const int i = 3 * row + rsub;
+        const double ml = apply_precond(k, row, valid, valid ? wv[k] : 0.0);
+        if (valid) {
+          mv[k] = ml;
+          mbuf[par][i] = ml;
+          ga = fma(rv[k], uv[k], ga);
+          de = fma(wv[k], uv[k], de);
+          rrl = fma(rv[k], rv[k], rrl);
+        }
+      }
+      pstamp(2);
+      double v3[3] = {ga, de, rrl}, ab[2];
+      const bool first = it == 0;
+      // beta = gamma / gamma_prev, alpha = gamma / (delta - beta gamma / alpha_prev), once per CTA
+      if (!grid_sums<3, 2>(v3, pbuf[par], gb, nullptr, 0, ab, [=](const double* sm, double* xo) {
+            const double be = first ? 0.0 : sm[0] / gam_prev;
+            xo[0] = first ? sm[0] / sm[1] : sm[0] / (sm[1] - be * sm[0] / alpha_prev);
+            xo[1] = be;
+          }))
+        return;
+      pstamp(3);
+      rz = v3[0];
+      rr = v3[2];
+      if (!isfinite(rr)) {
+        status = OD_ERR_NAN;
+        break;
+      }
+      if (!(rr > eps) || it >= max_iter) break;
+      const double alpha = ab[0], beta = ab[1];
+      if (!isfinite(alpha) || !isfinite(beta)) {
+        status = OD_ERR_NAN;
+        break;
+      }
+      gam_prev = v3[0];
+      alpha_prev = alpha;
+      OD_GROUP_LOOP(k, g) {
+        const int row = g * kRowsPerWarp + lane / 3;
+        if (lane < 30 && row < nb) {
+          const double nl = row_product(k, row, mbuf[par]);
+          zr[k] = fma(beta, zr[k], nl);
+          qv[k] = fma(beta, qv[k], mv[k]);
+          sv[k] = fma(beta, sv[k], wv[k]);
+          pv[k] = fma(beta, pv[k], uv[k]);
+          xr[k] = fma(alpha, pv[k], xr[k]);
+          rv[k] = fma(-alpha, sv[k], rv[k]);
+          uv[k] = fma(-alpha, qv[k], uv[k]);
+          wv[k] = fma(-alpha, zr[k], wv[k]);
+        }
+      }
+      pstamp(0);
+      if (ptimer) prof[6] += 1;
+      it++;
+    }
+  } else {
   // ---- init: r = b - A x; z = M^-1 r; p = z (cgSolver.cpp:20-30)
-  double rz = 0.0, bb = 0.0, rr = 0.0;
   {
     OD_GROUP_LOOP(k, g) {
       const int row = g * kRowsPerWarp + lane / 3;
@@ -734,9 +850,8 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
     if (!grid_sums<3>(v3, part_2, gb)) return;
     rz = v3[0]; bb = v3[1]; rr = v3[2];
   }
-  const double eps = bb * tol * tol;
-  int it = 0;
-  int status = isfinite(rr) ? OD_OK : OD_ERR_NAN;
+  eps = bb * tol * tol;
+  status = isfinite(rr) ? OD_OK : OD_ERR_NAN;
 
   // profiling (prof != nullptr): CTA 0 stamps the phases of every iteration
   // (its own work, then its wait in the grid-wide sum or barrier that ends
@@ -870,6 +985,7 @@ __global__ void __launch_bounds__(kPThreads, 1) pcg_persistent_kernel(
     stamp(5);
     if (timer) prof[6] += 1;
   }
+  }   // the reference's form and the recurrence form
   // ---- write back x, then the true residual ||b - A x||^2
   if (GPW > 0) {
     OD_GROUP_LOOP(k, g) {
@@ -2403,10 +2519,11 @@ od_status pcg_alloc(Scene* s) {
   // (warp, group) segment; 0 when it does not fit one CTA's shared memory or
   // a warp would own more than two groups (OD_GB300_PCG_SMEM=0 disables it)
   P.smem_bytes = 0;
-  // the one-launch PCG's form: -1 by tolerance (below), OD_GB300_PCG_FORM=recur
-  // or =standard forces one
+  // the one-launch PCG's form: -1 by size and tolerance (at the launch);
+  // OD_GB300_PCG_FORM=standard, =recur or =pipelined forces one
   P.recur = -1;
-  if (const char* f = std::getenv("OD_GB300_PCG_FORM")) P.recur = std::strcmp(f, "recur") == 0 ? 1 : 0;
+  if (const char* f = std::getenv("OD_GB300_PCG_FORM"))
+    P.recur = std::strcmp(f, "pipelined") == 0 ? 2 : (std::strcmp(f, "recur") == 0 ? 1 : 0);
   const char* smem_env = std::getenv("OD_GB300_PCG_SMEM");
   const int nb = s->bsr.nb;
   if (P.coop_grid > 0 && nb > 0 && !(smem_env && smem_env[0] == '0') && (int)s->hbsr_rp.size() == nb + 1) {
@@ -3152,12 +3269,14 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
              : need <= 4 ? (void*)pcg_persistent_kernel<double, 4, false>
                          : (void*)pcg_persistent_kernel<double, 0, false>;
     const size_t dyn = smem ? (size_t)P.smem_bytes : 0;
-    // the recurrence form (q = A z + beta q: two grid syncs per iteration
-    // instead of three) for tolerances down to 1e-10, where it takes the same
-    // iterations to the same true residual on the Newmark systems; tighter
-    // solves keep cgSolver.cpp's q = A p, so no recurrence drift can hold the
+    // The form: pipelined (one grid sync per iteration; its vectors live in
+    // registers, so at most two groups per warp) for tolerances down to 1e-9;
+    // the recurrence form (q = A z + beta q: two syncs) down to 1e-10; below,
+    // cgSolver.cpp's q = A p (three), so no recurrence drift can hold the
     // residual above a very small target
-    int recur = P.recur >= 0 ? P.recur : (prm->tol >= 1e-10 ? 1 : 0);
+    int recur = P.recur >= 0 ? P.recur
+                             : (need <= 2 && prm->tol >= 1e-9 ? 2 : (prm->tol >= 1e-10 ? 1 : 0));
+    if (recur == 2 && need > 2) recur = 1;
     args[18] = (void*)&recur;
     const bool prof = s->ctx->profiling && s->ctx->ev_pool.size() >= 2;
     const bool phases = prof && s->ctx->profiling >= 2;
