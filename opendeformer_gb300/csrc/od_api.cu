@@ -754,6 +754,7 @@ static od_status nm_step(Scene* s, od_step_stats* acc) {
     // A = (1 + gamma h alpha_M) M + (gamma h beta_K + beta h^2) K + gamma h D
     OD_TRY(launch_expand(s, s->K, gh * p.beta_k + bh2, s->M, 1.0 + gh * p.alpha_m, s->Dm, gh));
     OD_CUDA(cudaMemsetAsync(s->dv, 0, sizeof(double) * (size_t)s->pcg.n_pad, st));
+    s->pcg.x_zero = true;
     od_solve_stats ss{};
     OD_TRY(pcg_solve(s, s->rhs, s->dv, &p.solver, &ss));
     OD_KL(s);

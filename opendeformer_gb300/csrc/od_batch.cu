@@ -228,7 +228,7 @@ static od_status batch_step(Batch* B, std::vector<od_step_stats>& acc) {
     OD_TRY(nm_op(B, NM_RESIDUAL));
     OD_TRY(launch_expand_batch(ctx, n, B->sd, B->expand));
     OD_TRY(nm_op(B, NM_ZERO_DV));
-    OD_TRY(mixed_solve(ctx, B->mix, B->precond, B->prm, ss));
+    OD_TRY(mixed_solve(ctx, B->mix, B->precond, B->prm, ss, true));
     OD_TRY(nm_op(B, NM_ADD));
     for (size_t i = 0; i < B->sc.size(); i++) {
       od_step_stats& a = acc[i];
@@ -279,7 +279,7 @@ static od_status batch_autotune(Batch* B, int repeats, od_tune_report* rep) {
       for (int rr = 0; rr < std::max(1, repeats); rr++) {
         OD_TRY(nm_op(B, NM_ZERO_DV));
         OD_CUDA(cudaEventRecord(B->ev[0], ctx->stream));
-        OD_TRY(mixed_solve(ctx, m, B->precond, B->prm, ss));
+        OD_TRY(mixed_solve(ctx, m, B->precond, B->prm, ss, true));
         OD_CUDA(cudaEventRecord(B->ev[1], ctx->stream));
         OD_CUDA(cudaEventSynchronize(B->ev[1]));
         restore();

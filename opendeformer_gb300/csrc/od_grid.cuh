@@ -45,19 +45,24 @@ __device__ __forceinline__ int barrier_arrive_wait(GridBarrier* gb) {
 // until all gridDim.x arrivals of its epoch-th barrier are in -- one L2
 // round trip fewer than the generation barrier above.  The caller keeps
 // epoch (its count of barriers passed, from 1).  Bounded like the other.
+// Only the counter is read on the way out: the timeout flag (a peer that
+// gave up) is read every 32 polls, so a CTA that passes a barrier after a
+// peer timed out leaves at its next barrier, which that peer never reaches.
 __device__ __forceinline__ int barrier_arrive_wait_count(GridBarrier* gb, unsigned epoch) {
   asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&gb->arrive) : "memory");
   const unsigned target = epoch * gridDim.x;
-  unsigned long long spins = 0;
-  unsigned cur;
-  int ok = 1;
-  do {
+  for (unsigned long long spins = 1;; spins++) {
+    unsigned cur;
     asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(cur) : "l"(&gb->arrive) : "memory");
-    if ((int)(cur - target) >= 0) break;
-    if (++spins > kSpinLimit) { atomicExch(&gb->timeout, 1); ok = 0; break; }
-    if (*(volatile int*)&gb->timeout) { ok = 0; break; }
-  } while (true);
-  return ok && !*(volatile int*)&gb->timeout;
+    if ((int)(cur - target) >= 0) return 1;
+    if ((spins & 31) == 0) {
+      if (*(volatile int*)&gb->timeout) return 0;
+      if (spins > kSpinLimit) {
+        atomicExch(&gb->timeout, 1);
+        return 0;
+      }
+    }
+  }
 }
 
 // Values that double as their own ready flags: filled with an all-ones NaN

@@ -60,6 +60,7 @@ struct Scene;
 struct Pcg {
   int n_pad = 0;
   int precision = OD_PRECISION_FP64;
+  bool x_zero = false;   // the next solve starts from x = 0 (set by the caller that zeroed x; cleared by the solve)
   double* x = nullptr;
   double* r = nullptr;
   double* z = nullptr;
@@ -605,9 +606,10 @@ od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::ve
                       const std::vector<double*>& x, MixedSys** out);
 void mixed_free(MixedSys* m);
 // solves every scene's A64 x = b with FP64 refinement around the FP32 inner
-// PCG (same preconditioner kind for all); per-scene parameters and results
+// PCG (same preconditioner kind for all); per-scene parameters and results.
+// x_zero: every scene's x is 0 on entry (the first residual is b itself)
 od_status mixed_solve(Ctx* ctx, MixedSys* m, int precond, const std::vector<od_solver_params>& prm,
-                      std::vector<od_solve_stats>& st);
+                      std::vector<od_solve_stats>& st, bool x_zero = false);
 
 }  // namespace od
 

@@ -79,6 +79,42 @@ __global__ void expand_kernel(long long total, const int* __restrict__ kind, con
   A[idx] = (TA)val;
 }
 
+// Row r of block row (blocks [kb, ke)) of c1 V1 x1 + c2 V2 x2 + c3 V3 x3
+// with V* read from the lower layout.  The next block's descriptors are
+// loaded with the current block's values (one memory round trip per block
+// instead of two); the multiply-adds run in block, column, source order.
+template <int NSRC>
+__device__ __forceinline__ double lower_row(int kb, int ke, int r, const int* __restrict__ col,
+                                            const int* __restrict__ kind, const int* __restrict__ off,
+                                            const int* __restrict__ gen, const double* __restrict__ v1, double c1,
+                                            const double* __restrict__ x1, const double* __restrict__ v2, double c2,
+                                            const double* __restrict__ x2, const double* __restrict__ v3, double c3,
+                                            const double* __restrict__ x3) {
+  double acc = 0.0;
+  if (kb >= ke) return acc;
+  int cbn = 3 * col[kb], kdn = kind[kb], ofn = off[kb];
+  for (int k = kb; k < ke; k++) {
+    const int cb = cbn, kd = kdn, of = ofn;
+    if (k + 1 < ke) {
+      cbn = 3 * col[k + 1];
+      kdn = kind[k + 1];
+      ofn = off[k + 1];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const int src = lower_src(kd, of, r, c, gen);
+      if (src >= 0) {
+        acc = fma(c1 * v1[src], x1[cb + c], acc);
+        if (NSRC >= 2) acc = fma(c2 * v2[src], x2[cb + c], acc);
+        if (NSRC >= 3) acc = fma(c3 * v3[src], x3[cb + c], acc);
+      } else if (src == -2) {
+        acc = fma(c1, x1[cb + c], acc);
+      }
+    }
+  }
+  return acc;
+}
+
 // y (+)= c1 V1 x1 + c2 V2 x2 + c3 V3 x3 with V* read from the lower layout
 // through the full-BSR descriptors (SpMDV semantics, numerMethod.h:134-262).
 // Three lanes per block row as in the full-BSR product; absent sources
@@ -95,21 +131,7 @@ __global__ void spmv_lower_kernel(int nb, const int* __restrict__ rp, const int*
   const int row = (blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5)) * 10 + lane / 3;
   const int r = lane % 3;
   if (row >= nb) return;
-  double acc = 0.0;
-  for (int k = rp[row]; k < rp[row + 1]; k++) {
-    const int cb = 3 * col[k], kd = kind[k], of = off[k];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const int src = lower_src(kd, of, r, c, gen);
-      if (src >= 0) {
-        acc = fma(c1 * v1[src], x1[cb + c], acc);
-        if (NSRC >= 2) acc = fma(c2 * v2[src], x2[cb + c], acc);
-        if (NSRC >= 3) acc = fma(c3 * v3[src], x3[cb + c], acc);
-      } else if (src == -2) {
-        acc = fma(c1, x1[cb + c], acc);
-      }
-    }
-  }
+  const double acc = lower_row<NSRC>(rp[row], rp[row + 1], r, col, kind, off, gen, v1, c1, x1, v2, c2, x2, v3, c3, x3);
   if (accumulate) y[3 * row + r] += acc;
   else y[3 * row + r] = acc;
 }
@@ -139,22 +161,9 @@ __global__ void spmv_lower_batch_kernel(int n_sc, const int* __restrict__ prefix
   const int row = (blockIdx.x - prefix[s]) * kBatchRows + (threadIdx.x >> 5) * 10 + lane / 3;
   const int r = lane % 3;
   if (row >= D.nb) return;
-  const double c2 = D.beta_k;
-  double acc = 0.0;
-  for (int k = D.row_ptr[row]; k < D.row_ptr[row + 1]; k++) {
-    const int cb = 3 * D.col[k], kd = D.desc_kind[k], of = D.desc_off[k];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const int src = lower_src(kd, of, r, c, D.gen);
-      if (src >= 0) {
-        acc = fma(D.M[src], D.tmp[cb + c], acc);
-        acc = fma(c2 * D.K[src], D.tmp2[cb + c], acc);
-      } else if (src == -2) {
-        acc = fma(1.0, D.tmp[cb + c], acc);
-      }
-    }
-  }
-  D.rhs[3 * row + r] = acc;
+  // the scene's M tmp + beta_K K tmp2 (c1 = 1: 1.0 * M[src] is M[src])
+  D.rhs[3 * row + r] = lower_row<2>(D.row_ptr[row], D.row_ptr[row + 1], r, D.col, D.desc_kind, D.desc_off, D.gen,
+                                    D.M, 1.0, D.tmp, D.K, D.beta_k, D.tmp2, nullptr, 0.0, nullptr);
 }
 
 // Row-block products of the full BSR.  Three lanes per block row, lane r
@@ -170,9 +179,12 @@ __device__ __forceinline__ double bsr_subrow(int row, int r, const int* __restri
                                              const TA* __restrict__ A, const TX* __restrict__ x) {
   double y = 0.0;
   const int kb = rp[row], ke = rp[row + 1];
+  // the next block's column is loaded with the current block's x entries
+  int cn = kb < ke ? col[kb] : 0;
   for (int k = kb; k < ke; k++) {
     const TA* a = A + (size_t)k * 9 + 3 * r;
-    const int c = 3 * col[k];
+    const int c = 3 * cn;
+    if (k + 1 < ke) cn = col[k + 1];
     y = fma((double)a[0], (double)x[c], y);
     y = fma((double)a[1], (double)x[c + 1], y);
     y = fma((double)a[2], (double)x[c + 2], y);
@@ -498,6 +510,10 @@ __device__ __forceinline__ bool grid_barrier_count(GridBarrier* gb) {
   __syncthreads();
   return sh.ok != 0;
 }
+// loads per lane issued together when a grid sum reads the CTA partials
+// (5 x 32 covers one CTA per SM on 152 SMs in one pass)
+constexpr int kGridSumLoads = 5;
+
 template <int NV, int NX = 0, class F = NoFinish>
 __device__ __forceinline__ bool grid_sums(double (&v)[NV], double* __restrict__ part, GridBarrier* gb,
                                           unsigned long long* __restrict__ work = nullptr,
@@ -534,12 +550,29 @@ __device__ __forceinline__ bool grid_sums(double (&v)[NV], double* __restrict__ 
     if (lane == 0) ok = barrier_arrive_wait_count(gb, ++sh.epoch);
     __syncwarp();   // orders lane 0's acquire before the other lanes' partial reads
     ok = __shfl_sync(0xffffffffu, ok, 0);
+    // every lane's loads of a pass issued before any is used (one L2 round
+    // trip per pass); each lane adds its entries in increasing CTA order
+    double acc[NV];
+#pragma unroll
+    for (int j = 0; j < NV; j++) acc[j] = 0.0;
+    for (int c0 = 0; c0 < G; c0 += 32 * kGridSumLoads) {
+      double ld[NV][kGridSumLoads];
+#pragma unroll
+      for (int j = 0; j < NV; j++)
+#pragma unroll
+        for (int q = 0; q < kGridSumLoads; q++) {
+          const int c = c0 + lane + 32 * q;
+          ld[j][q] = c < G ? __ldcg(part + (size_t)j * G + c) : 0.0;
+        }
+#pragma unroll
+      for (int j = 0; j < NV; j++)
+#pragma unroll
+        for (int q = 0; q < kGridSumLoads; q++) acc[j] += ld[j][q];
+    }
 #pragma unroll
     for (int j = 0; j < NV; j++) {
-      double acc = 0.0;
-      for (int c = lane; c < G; c += 32) acc += __ldcg(part + (size_t)j * G + c);
-      acc = warp_sum(acc);
-      if (lane == 0) res[j] = acc;
+      const double t = warp_sum(acc[j]);
+      if (lane == 0) res[j] = t;
     }
     if (lane == 0) {
       ok_s = ok;
@@ -1126,8 +1159,10 @@ __global__ void mix_precond_kernel(int n_sc, const int* __restrict__ prefix, int
 
 // r64 = b - A64 x (FP64) over kResRows block rows of a scene (three lanes per
 // block row, ten block rows per warp) and the tile's partials of r.r, b.b
+// r64 = b - A64 x and the tile partials of r.r, b.b; x_zero: x is known to
+// be 0, so r64 = b without the product (b - A 0 is b bit for bit)
 __global__ void mix_residual_kernel(int n_sc, const int* __restrict__ prefix, const MixDesc* __restrict__ desc,
-                                    double* __restrict__ part) {
+                                    double* __restrict__ part, int x_zero) {
   const int s = dir_scene(prefix, n_sc, blockIdx.x);
   const MixDesc& D = desc[s];
   const int lane = threadIdx.x & 31;
@@ -1137,7 +1172,7 @@ __global__ void mix_residual_kernel(int n_sc, const int* __restrict__ prefix, co
   if (lane < 30 && row < D.nb) {
     const int i = 3 * row + rs;
     const double bv = D.b[i];
-    const double rv = bv - bsr_subrow<double, double>(row, rs, D.row_ptr, D.col, D.A64, D.x);
+    const double rv = x_zero ? bv : bv - bsr_subrow<double, double>(row, rs, D.row_ptr, D.col, D.A64, D.x);
     D.r64[i] = rv;
     rr = rv * rv;
     bb = bv * bv;
@@ -1328,25 +1363,63 @@ __device__ __forceinline__ bool ring_sums(RingShared& sh, int L, int sc_lo, int 
     if (lane == 0) ok = barrier_arrive_wait_count(gb, ++sh.epoch);
     __syncwarp();   // orders lane 0's acquire before the other lanes' partial reads
     ok = __shfl_sync(0xffffffffu, ok, 0);
+    // Every lane's loads of one pass are issued before any is used (one L2
+    // round trip per pass rather than one per load); each lane still adds
+    // its entries in increasing CTA order, so the sums do not depend on
+    // the pass structure.
     if (stamp) {  // profiling: the last CTA's end of the phase
       unsigned long long tmax = 0;
-      for (int c = lane; c < G; c += 32) tmax = max(tmax, __ldcg(stamp + c));
+      for (int c0 = 0; c0 < G; c0 += 32 * kGridSumLoads) {
+        unsigned long long v[kGridSumLoads];
+#pragma unroll
+        for (int q = 0; q < kGridSumLoads; q++) {
+          const int c = c0 + lane + 32 * q;
+          v[q] = c < G ? __ldcg(stamp + c) : 0ull;
+        }
+#pragma unroll
+        for (int q = 0; q < kGridSumLoads; q++) tmax = max(tmax, v[q]);
+      }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
       if (lane == 0) sh.tmax = tmax;
     }
     double accg = 0.0;
-    for (int c = lane; c < G; c += 32) accg += __ldcg(part_g + c);
+    for (int c0 = 0; c0 < G; c0 += 32 * kGridSumLoads) {
+      double v[kGridSumLoads];
+#pragma unroll
+      for (int q = 0; q < kGridSumLoads; q++) {
+        const int c = c0 + lane + 32 * q;
+        v[q] = c < G ? __ldcg(part_g + c) : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < kGridSumLoads; q++) accg += v[q];
+    }
     for (int ls = 0; ls < L; ls++) {
       const int s = sc_lo + ls;
       const int c0 = sh.c0[ls], c1 = sh.c1[ls];
+      double acc[NV];
+#pragma unroll
+      for (int j = 0; j < NV; j++) acc[j] = 0.0;
+      for (int cb = c0; cb <= c1; cb += 32 * kGridSumLoads) {
+        double v[NV][kGridSumLoads];
+#pragma unroll
+        for (int j = 0; j < NV; j++) {
+          const double* pp = part + ((size_t)j * n_sc + s) * G;
+#pragma unroll
+          for (int q = 0; q < kGridSumLoads; q++) {
+            const int c = cb + lane + 32 * q;
+            v[j][q] = c <= c1 ? __ldcg(pp + c) : 0.0;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < NV; j++)
+#pragma unroll
+          for (int q = 0; q < kGridSumLoads; q++) acc[j] += v[j][q];
+      }
 #pragma unroll
       for (int j = 0; j < NV; j++) {
-        const double* pp = part + ((size_t)j * n_sc + s) * G;
-        double acc = 0.0;
-        for (int c = c0 + lane; c <= c1; c += 32) acc += __ldcg(pp + c);
-        acc = warp_sum(acc);
-        if (lane == 0) sh.res[j][ls] = acc;
+        const double a = warp_sum(acc[j]);
+        if (lane == 0) sh.res[j][ls] = a;
       }
     }
     accg = warp_sum(accg);
@@ -1619,13 +1692,28 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
         const Vecs V = vecs(ls);
         const int* __restrict__ soff = sh.lp[ls].soff;
         Comp cwu{0.f, 0.f};
-        for (int sl = first_slice(ls); sl < sh.lfirst[ls + 1] && alive; sl += NW) {
+        // a slice's step range and the u of its own block row (the
+        // transposed products and (w, u)) are loaded while the warp's
+        // previous slice is processed: the loads cannot move across the
+        // mbarrier waits, so each would otherwise be a memory round trip
+        // of its own per slice
+        const int sl_end = sh.lfirst[ls + 1];
+        int ka = 0, kb = 0;
+        float4 un = make_float4(0.f, 0.f, 0.f, 0.f);
+        auto fetch = [&](int sl) {
+          const int l = sl - V.s0;
+          ka = soff[l];
+          kb = soff[l + 1];
+          if (on) un = V.u4[(size_t)l * kSliceRows + t];
+        };
+        if (first_slice(ls) < sl_end) fetch(first_slice(ls));
+        for (int sl = first_slice(ls); sl < sl_end && alive; sl += NW) {
           const int lsl = sl - V.s0;
-          const int k1 = soff[lsl + 1];
+          const int k0 = ka, k1 = kb;
+          const float4 uo = un;
+          if (sl + NW < sl_end) fetch(sl + NW);
           float y0 = 0.f, y1 = 0.f, y2 = 0.f;  // partial rows 0, 1, 2 of block row t
-          // lower storage: u of block row t, for the transposed products
-          const float4 uo = (lower && on) ? V.u4[(size_t)lsl * kSliceRows + t] : make_float4(0.f, 0.f, 0.f, 0.f);
-          for (int kk = soff[lsl]; kk < k1; kk += PS) {
+          for (int kk = k0; kk < k1; kk += PS) {
             const int n = min(PS, k1 - kk);
             const int j = pc & 1;
             if (!__all_sync(0xffffffffu, mbar_wait(full + 2 * w + j, (pc >> 1) & 1))) {
@@ -1684,6 +1772,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
             const float na = rsub == 0 ? a0 : (rsub == 1 ? a1 : a2);
             const float nb = rsub == 0 ? b0 : (rsub == 1 ? b1 : b2);
             const float y = (own + na) + nb;
+            const float uown = rsub == 0 ? uo.x : (rsub == 1 ? uo.y : uo.z);   // u of row rsub of block row t
             if (lower) {
               // w of the own row takes the gathered half by one reduction;
               // (w, u) = 2 sum_rows u . (gathered half) (the scattered half
@@ -1691,12 +1780,12 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
               const float yb = __shfl_sync(0xffffffffu, y, lbase + 1);
               const float yc = __shfl_sync(0xffffffffu, y, lbase + 2);
               if (act_l) {
-                comp_add_prod(cwu, 2.f * V.uf[4 * (size_t)(lsl * kSliceRows + t) + rsub], y);
+                comp_add_prod(cwu, 2.f * uown, y);
                 if (rsub == 0) red_add_v4(V.w4 + (size_t)lsl * kSliceRows + t, y, yb, yc);
               }
             } else if (act_l) {
               V.w[(size_t)30 * lsl + lane] = y;
-              comp_add_prod(cwu, V.uf[4 * (size_t)(lsl * kSliceRows + t) + rsub], y);
+              comp_add_prod(cwu, uown, y);
             }
           }
         }
@@ -1752,7 +1841,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
     zero_ws(3);
     for (int ls = 0; ls < L; ls++) {
       if (!sh.act[kp ^ 1][ls]) continue;  // warp-uniform; the partials stay zero
-      constexpr int kUB = 4;
+      constexpr int kUB = PS <= 12 ? 6 : 4;   // slices per batch (registers allow 6 at the smaller pieces)
       const int hi = sh.lfirst[ls + 1];
       const Vecs V = vecs(ls);
       const bool lower = sh.lp[ls].lower != 0;
@@ -3020,11 +3109,12 @@ od_status mixed_build(Ctx* ctx, const std::vector<Scene*>& scenes, const std::ve
 
 // FP64 residual of every scene and its norms; brings rrbb (and the ring
 // outputs) back to the host
-static od_status mixed_residual(Ctx* ctx, MixedSys* m, bool with_ring) {
+static od_status mixed_residual(Ctx* ctx, MixedSys* m, bool with_ring, bool x_zero = false) {
   cudaStream_t strm = ctx->stream;
   if (m->res_dir.tiles > 0) {
     ctx->launches += 2;
-    mix_residual_kernel<<<m->res_dir.tiles, kThreads, 0, strm>>>(m->n_sc, m->res_dir.prefix, m->desc, m->res_part);
+    mix_residual_kernel<<<m->res_dir.tiles, kThreads, 0, strm>>>(m->n_sc, m->res_dir.prefix, m->desc, m->res_part,
+                                                                  x_zero ? 1 : 0);
     mix_residual_finish<<<nblk(m->n_sc, kThreads / 32), kThreads, 0, strm>>>(m->n_sc, m->res_dir.prefix, m->res_part,
                                                                              m->rrbb);
     OD_CUDA(cudaGetLastError());
@@ -3040,7 +3130,7 @@ static od_status mixed_residual(Ctx* ctx, MixedSys* m, bool with_ring) {
 }
 
 od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver_params>& prm,
-                      std::vector<od_solve_stats>& st) {
+                      std::vector<od_solve_stats>& st, bool x_zero) {
   cudaStream_t strm = ctx->stream;
   const int n_sc = m->n_sc;
   st.assign(n_sc, od_solve_stats{});
@@ -3057,7 +3147,7 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
     ctx->launches++;
     mix_precond_kernel<<<m->pre_dir.tiles, kThreads, 0, strm>>>(n_sc, m->pre_dir.prefix, pk, m->desc);
   }
-  OD_TRY(mixed_residual(ctx, m, false));
+  OD_TRY(mixed_residual(ctx, m, false, x_zero));
   std::vector<double> eps(n_sc), rr(n_sc), bb(n_sc);
   std::vector<int> total(n_sc, 0), sweeps(n_sc, 0), need(n_sc, 0), status(n_sc, OD_OK);
   for (int s = 0; s < n_sc; s++) {
@@ -3181,7 +3271,7 @@ od_status mixed_solve(Ctx* ctx, MixedSys* m, int pk, const std::vector<od_solver
 
 // single-scene mixed solve: the scene's own one-scene system
 static od_status pcg_solve_mixed(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm,
-                                 od_solve_stats* st) {
+                                 od_solve_stats* st, bool x_zero) {
   Pcg& P = s->pcg;
   if (prm->precond == OD_PRECOND_IC0) return mixed_ic0_solve(s, d_b, d_x, prm, st);
   if (!P.mix) OD_TRY(mixed_build(s->ctx, {s}, {d_b}, {d_x}, &P.mix));
@@ -3192,7 +3282,7 @@ static od_status pcg_solve_mixed(Scene* s, const double* d_b, double* d_x, const
     OD_CUDA(cudaMemcpyAsync(m->desc, m->desc_host.data(), sizeof(MixDesc), cudaMemcpyHostToDevice, s->ctx->stream));
   }
   std::vector<od_solve_stats> out;
-  od_status rc = mixed_solve(s->ctx, m, prm->precond, {*prm}, out);
+  od_status rc = mixed_solve(s->ctx, m, prm->precond, {*prm}, out, x_zero);
   if (st) *st = out[0];
   return rc;
 }
@@ -3202,6 +3292,8 @@ static od_status pcg_solve_mixed(Scene* s, const double* d_b, double* d_x, const
 // solve (cgSolver.cpp:23).
 od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_params* prm, od_solve_stats* st) {
   Pcg& P = s->pcg;
+  const bool x_zero = P.x_zero;   // one solve only
+  P.x_zero = false;
   cudaStream_t strm = s->ctx->stream;
   const int nb = s->bsr.nb, n = P.n_pad;
   const int pk = prm->precond;
@@ -3210,7 +3302,7 @@ od_status pcg_solve(Scene* s, const double* d_b, double* d_x, const od_solver_pa
     if (st) *st = od_solve_stats{};
     return OD_OK;
   }
-  if (prm->precision == OD_PRECISION_MIXED) return pcg_solve_mixed(s, d_b, d_x, prm, st);
+  if (prm->precision == OD_PRECISION_MIXED) return pcg_solve_mixed(s, d_b, d_x, prm, st, x_zero);
   const int G = P.grid;
   const int g_rows = std::min(G, nblk(nb, kWarpRows));
   const int g_upd = std::min(G, nblk(n, kUpdThreads));
