@@ -1238,11 +1238,16 @@ constexpr int kRingWarpsMax = 15;
 constexpr int kRingWarpsDefault = 12;
 // Steps per piece (even; a tile shape the batch autotuner picks): each
 // stage holds a piece's values (90 floats per step) then its columns (10
-// ints per step); two stages per consumer warp plus the mbarriers.
+// ints per step); kRingStages stages per consumer warp plus their
+// mbarriers.
 constexpr int kRingStepsDefault = 20;
 __host__ __device__ constexpr int ring_stage_bytes(int ps) { return ps * 400; }
+// stages per consumer warp (a third, with pieces of 8 or 10 steps so that
+// it fits, let the producer's prefetch slow the update phase more than it
+// sped the product)
+constexpr int kRingStages = 2;
 __host__ __device__ constexpr int ring_smem_bytes(int ps, int nw) {
-  return nw * 2 * ring_stage_bytes(ps) + nw * 2 * 2 * 8;
+  return nw * kRingStages * ring_stage_bytes(ps) + nw * kRingStages * 2 * 8;
 }
 constexpr unsigned long long kMbarSpinLimit = 1ull << 24;
 
@@ -1344,21 +1349,26 @@ __device__ __forceinline__ bool ring_sums(RingShared& sh, int L, int sc_lo, int 
     stamp[b] = t;
   }
   if (w == 0) {
+    // the CTA's partials of its scenes (staged in res, whose last values
+    // were used before this phase), all stored by lane 0: its release
+    // reduction at the barrier then orders them without a separate fence
     if (lane < L) {
 #pragma unroll
       for (int j = 0; j < NV; j++) {
         double t = 0.0;
         for (int k = 0; k < NW; k++) t += sh.ws[j][lane][k];
-        part[((size_t)j * n_sc + sc_lo + lane) * G + b] = t;
+        sh.res[j][lane] = t;
       }
     }
+    __syncwarp();
     if (lane == 0) {
+      for (int ls = 0; ls < L; ls++)
+#pragma unroll
+        for (int j = 0; j < NV; j++) part[((size_t)j * n_sc + sc_lo + ls) * G + b] = sh.res[j][ls];
       double t = 0.0;
       for (int k = 0; k < NW; k++) t += sh.wg[k];
       part_g[b] = t;
     }
-    __threadfence();
-    __syncwarp();
     int ok = 1;
     if (lane == 0) ok = barrier_arrive_wait_count(gb, ++sh.epoch);
     __syncwarp();   // orders lane 0's acquire before the other lanes' partial reads
@@ -1458,9 +1468,10 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
     const int* __restrict__ sc_slice, const MixDesc* __restrict__ desc, RingScene* __restrict__ ring, int pkind,
     double* __restrict__ part, GridBarrier* gb, unsigned long long* __restrict__ prof,
     unsigned long long* __restrict__ cta_ns) {
+  constexpr int ST = kRingStages;
   extern __shared__ __align__(128) unsigned char ring_smem[];
-  unsigned long long* full = reinterpret_cast<unsigned long long*>(ring_smem + NW * 2 * ring_stage_bytes(PS));
-  unsigned long long* empty = full + 2 * NW;
+  unsigned long long* full = reinterpret_cast<unsigned long long*>(ring_smem + NW * ST * ring_stage_bytes(PS));
+  unsigned long long* empty = full + ST * NW;
   __shared__ RingShared sh;
   const int G = gridDim.x;
   const int lane = threadIdx.x & 31;
@@ -1483,7 +1494,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
     sh.pub = -1;
     sh.epoch = 0;
   }
-  if (threadIdx.x < 2 * NW) {
+  if (threadIdx.x < ST * NW) {
     mbar_init(full + threadIdx.x, 1);
     mbar_init(empty + threadIdx.x, 1);
   }
@@ -1543,22 +1554,22 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
         const int k1 = P.soff[lsl + 1];
         for (int k = P.soff[lsl]; k < k1; k += PS) {
           const int n = min(PS, k1 - k);
-          const int j = pc & 1;
-          const unsigned par = ((pc >> 1) & 1) ^ 1;
+          const int j = (int)(pc % ST);
+          const unsigned par = ((pc / ST) & 1) ^ 1;
           bool got = false;
           for (unsigned long long i = 0; i < kMbarSpinLimit; i++) {
-            if (mbar_try_wait(empty + 2 * pw + j, par)) { got = true; break; }
+            if (mbar_try_wait(empty + ST * pw + j, par)) { got = true; break; }
             if (sh.stop) break;
           }
           if (!got) { ok = false; break; }
           if (copy) {
-            unsigned char* st = ring_smem + (size_t)(2 * pw + j) * ring_stage_bytes(PS);
-            mbar_expect_tx(full + 2 * pw + j, (unsigned)n * 400u);
-            bulk_g2s(st, P.sval + (size_t)k * 90, (unsigned)n * 360u, full + 2 * pw + j, policy);
-            bulk_g2s(st + PS * 360, P.scol + (size_t)k * kSliceRows, (unsigned)n * 40u, full + 2 * pw + j,
+            unsigned char* st = ring_smem + (size_t)(ST * pw + j) * ring_stage_bytes(PS);
+            mbar_expect_tx(full + ST * pw + j, (unsigned)n * 400u);
+            bulk_g2s(st, P.sval + (size_t)k * 90, (unsigned)n * 360u, full + ST * pw + j, policy);
+            bulk_g2s(st + PS * 360, P.scol + (size_t)k * kSliceRows, (unsigned)n * 40u, full + ST * pw + j,
                      policy);
           } else {
-            mbar_arrive(full + 2 * pw + j);
+            mbar_arrive(full + ST * pw + j);
           }
           pc++;
         }
@@ -1566,9 +1577,9 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
       kit++;
     }
     // drain: the last arming of each stage must complete before the CTA exits
-    for (unsigned u = 0; u < 2 && u < pc; u++) {
+    for (unsigned u = 0; u < (unsigned)ST && u < pc; u++) {
       const unsigned last = pc - 1 - u;
-      mbar_wait(full + 2 * pw + (last & 1), (last >> 1) & 1);
+      mbar_wait(full + ST * pw + (last % ST), (last / ST) & 1);
     }
     return;
   }
@@ -1715,14 +1726,14 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
           float y0 = 0.f, y1 = 0.f, y2 = 0.f;  // partial rows 0, 1, 2 of block row t
           for (int kk = k0; kk < k1; kk += PS) {
             const int n = min(PS, k1 - kk);
-            const int j = pc & 1;
-            if (!__all_sync(0xffffffffu, mbar_wait(full + 2 * w + j, (pc >> 1) & 1))) {
+            const int j = (int)(pc % ST);
+            if (!__all_sync(0xffffffffu, mbar_wait(full + ST * w + j, (pc / ST) & 1))) {
               atomicExch(&gb->timeout, 1);
               alive = false;
               break;
             }
             if (on) {
-              const unsigned char* stg = ring_smem + (size_t)(2 * w + j) * ring_stage_bytes(PS);
+              const unsigned char* stg = ring_smem + (size_t)(ST * w + j) * ring_stage_bytes(PS);
               const float* sv = reinterpret_cast<const float*>(stg);
               const int* scol = reinterpret_cast<const int*>(stg + PS * 360);
               // lane (t, rsub) takes steps rsub, rsub + 3, ... of the piece
@@ -1759,7 +1770,7 @@ __global__ void __launch_bounds__(32 * (NW + 1), 1) pcg32_ring_kernel(
               }
             }
             __syncwarp();
-            if (lane == 0) mbar_arrive(empty + 2 * w + j);
+            if (lane == 0) mbar_arrive(empty + ST * w + j);
             pc++;
           }
           if (on) {
