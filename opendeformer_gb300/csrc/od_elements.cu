@@ -6,7 +6,8 @@
 //
 // One thread per element; element data is structure-of-arrays in colour
 // order (pre[k * ne + e], emap[k * ne + e]) so every per-element load and the
-// map loads are coalesced.
+// map loads are coalesced.  The staged outputs (the gathered assembly's
+// input) are element-major, grouped by local node block (c_kslot below).
 #include "od_internal.h"
 #include "od_math.cuh"
 
@@ -15,6 +16,21 @@ namespace od {
 // packed position of (i, i) in the 78-entry upper triangle of the 12x12
 // element matrix (tetelement.cpp:284)
 __constant__ int c_diag12[12] = {0, 12, 23, 33, 42, 50, 57, 63, 68, 72, 75, 77};
+
+// Staged element values (the assembly's input) are element-major: 78
+// stiffness values per element with the entries of each local node block
+// contiguous -- blocks (0,0), (0,1), (0,2), (0,3), (1,1), ..., (3,3), a
+// diagonal block's 6 upper entries, an off-diagonal block's 9 row-major --
+// so that the assembly threads of one matrix block read one contiguous run
+// of each contributing element; then 12 forces per element in local DOF
+// order.  c_kslot maps the packed entry k (row-major upper triangle, the
+// reference's order) to its slot.
+__constant__ int c_kslot[78] = {0,  1,  2,  6,  7,  8,  15, 16, 17, 24, 25, 26, 3,  4,  9,  10, 11, 18, 19, 20,
+                                27, 28, 29, 5,  12, 13, 14, 21, 22, 23, 30, 31, 32, 33, 34, 35, 39, 40, 41, 48,
+                                49, 50, 36, 37, 42, 43, 44, 51, 52, 53, 38, 45, 46, 47, 54, 55, 56, 57, 58, 59,
+                                63, 64, 65, 60, 61, 66, 67, 68, 62, 69, 70, 71, 72, 73, 74, 75, 76, 77};
+__device__ __forceinline__ size_t kst(int k, int e) { return (size_t)e * 78 + c_kslot[k]; }
+__device__ __forceinline__ size_t fst(int k, int e) { return (size_t)e * 12 + k; }
 
 __device__ __forceinline__ V3t<double> ld3(const double* p, int n) {
   return {p[3 * n], p[3 * n + 1], p[3 * n + 2]};
@@ -283,7 +299,7 @@ __device__ __forceinline__ void corot_elem(int e, int ne, const int4* __restrict
     } else if (MODE == 1) {
       out78[obase + k] = val;
     } else {
-      out78[(size_t)k * ne + e] = val;
+      out78[kst(k, e)] = val;
     }
   };
   if constexpr (DF) {
@@ -410,7 +426,7 @@ __device__ __forceinline__ void corot_elem(int e, int ne, const int4* __restrict
     for (int k = 0; k < 12; k++) out12[(size_t)perm[e] * 12 + k] = f[k];
   } else {
 #pragma unroll
-    for (int k = 0; k < 12; k++) out12[(size_t)k * ne + e] = f[k];
+    for (int k = 0; k < 12; k++) out12[fst(k, e)] = f[k];
   }
 }
 
@@ -531,7 +547,7 @@ __device__ __forceinline__ void invhyper_elem(int e, int ne, int stvk, const int
     } else if (MODE == 1) {
       out78[obase + k] = val;
     } else {
-      out78[(size_t)k * ne + e] = val;
+      out78[kst(k, e)] = val;
     }
   };
   if constexpr (DF) {
@@ -664,7 +680,7 @@ __device__ __forceinline__ void invhyper_elem(int e, int ne, int stvk, const int
     for (int k = 0; k < 12; k++) out12[(size_t)perm[e] * 12 + k] = f[k];
   } else {
 #pragma unroll
-    for (int k = 0; k < 12; k++) out12[(size_t)k * ne + e] = f[k];
+    for (int k = 0; k < 12; k++) out12[fst(k, e)] = f[k];
   }
 }
 
@@ -819,7 +835,7 @@ __device__ __forceinline__ void plastic_elem(int e, int ne, const int4* __restri
   }
   auto put = [&](int k, double val) {
     if (MODE == 1) out78[(size_t)perm[e] * 78 + k] = val;
-    else out78[(size_t)k * ne + e] = val;
+    else out78[kst(k, e)] = val;
   };
   int blk = 0;
 #pragma unroll 1
@@ -868,7 +884,7 @@ __device__ __forceinline__ void plastic_elem(int e, int ne, const int4* __restri
     for (int k = 0; k < 12; k++) out12[(size_t)perm[e] * 12 + k] = f[k];
   } else {
 #pragma unroll
-    for (int k = 0; k < 12; k++) out12[(size_t)k * ne + e] = f[k];
+    for (int k = 0; k < 12; k++) out12[fst(k, e)] = f[k];
   }
 }
 
@@ -909,10 +925,10 @@ __global__ void scatter_kernel(int e0, int cnt, int ne, const double* __restrict
   const int e = e0 + (int)(t - (long long)k * cnt);
   if (k < 78) {
     const int idx = emap[(size_t)k * ne + e];
-    if (idx >= 0) K[idx] += k78[(size_t)k * ne + e];
+    if (idx >= 0) K[idx] += k78[kst(k, e)];
   } else {
     const int g = gdof[(size_t)(k - 78) * ne + e];
-    if (g >= 0) fint[g] += f12[(size_t)(k - 78) * ne + e];
+    if (g >= 0) fint[g] += f12[fst(k - 78, e)];
   }
 }
 
@@ -966,10 +982,10 @@ __global__ void scatter_batch_kernel(int n_sc, const int* __restrict__ prefix, i
   const int e = e0 + (t - k * cnt);
   if (k < 78) {
     const int idx = D.emap[(size_t)k * ne + e];
-    if (idx >= 0) D.K[idx] += D.stage_k[(size_t)k * ne + e];
+    if (idx >= 0) D.K[idx] += D.stage_k[kst(k, e)];
   } else {
     const int g = D.gdof[(size_t)(k - 78) * ne + e];
-    if (g >= 0) D.fint[g] += D.stage_f[(size_t)(k - 78) * ne + e];
+    if (g >= 0) D.fint[g] += D.stage_f[fst(k - 78, e)];
   }
 }
 
@@ -1020,15 +1036,22 @@ __global__ void __launch_bounds__(kScanBlock) gl_add_kernel(int n, int* __restri
   if (i < n) data[i] += offs[blockIdx.x];
 }
 
+// map entry t = k * ne + e (e the element's staged position) -> its staged
+// source: e * kk + slot (c_kslot for the 78 stiffness values, k for forces)
 __global__ void gl_fill_kernel(long long n, const int* __restrict__ dest, int* __restrict__ cur,
-                               int* __restrict__ src) {
+                               int* __restrict__ src, int ne, int kk) {
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const int d = dest[t];
-    if (d >= 0) src[atomicAdd(&cur[d], 1)] = (int)t;
+    if (d >= 0) {
+      const int k = (int)(t / ne), e = (int)(t - (long long)k * ne);
+      src[atomicAdd(&cur[d], 1)] = e * kk + (kk == 78 ? c_kslot[k] : k);
+    }
   }
 }
 
-// source t = k * ne + e (e the staged position) sorts by perm[e] * kk + k
+// a list's sources (e * kk + slot) sort by perm[e] * kk + slot: an element
+// contributes at most once to a destination, so this is the reference's
+// order, by original element index
 __global__ void gl_sort_kernel(int nd, const int* __restrict__ ptr, int* __restrict__ src,
                                const int* __restrict__ perm, int ne, int kk) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1036,11 +1059,11 @@ __global__ void gl_sort_kernel(int nd, const int* __restrict__ ptr, int* __restr
   const int a = ptr[i], b = ptr[i + 1];
   for (int j = a + 1; j < b; j++) {
     const int v = src[j];
-    const long long key = (long long)perm[v % ne] * kk + v / ne;
+    const long long key = (long long)perm[v / kk] * kk + v % kk;
     int q = j - 1;
     while (q >= a) {
       const int w = src[q];
-      if ((long long)perm[w % ne] * kk + w / ne <= key) break;
+      if ((long long)perm[w / kk] * kk + w % kk <= key) break;
       src[q + 1] = w;
       q--;
     }
@@ -1086,7 +1109,7 @@ static od_status gather_list(Scene* s, const int* dest, int kk, int nd, int** pt
   OD_CUDA(cudaMalloc(&src, sizeof(int) * (size_t)std::max(1, total)));
   OD_CUDA(cudaMalloc(&cur, sizeof(int) * (size_t)std::max(1, nd)));
   if (nd > 0) OD_CUDA(cudaMemcpyAsync(cur, ptr, sizeof(int) * (size_t)nd, cudaMemcpyDeviceToDevice, st));
-  gl_fill_kernel<<<grid, 256, 0, st>>>(n, dest, cur, src);
+  gl_fill_kernel<<<grid, 256, 0, st>>>(n, dest, cur, src, ne, kk);
   if (nd > 0) gl_sort_kernel<<<(nd + 255) / 256, 256, 0, st>>>(nd, ptr, src, s->perm, ne, kk);
   OD_CUDA(cudaGetLastError());
   OD_TRY(sync_stream(s));   // hs is read by the copy above; the temporaries go next
@@ -1182,9 +1205,9 @@ __global__ void hooke_stage_kernel(int ne, const int4* __restrict__ tets, const 
       for (int i = 0; i < 3; i++) {
         const int p = 3 * a + i, dp = p * 12 - (p * (p - 1)) / 2;   // packed index of (p, p)
         if (a == b) {
-          for (int j = i; j < 3; j++) k78[(size_t)(dp + j - i) * ne + e] = Kab[3 * i + j];
+          for (int j = i; j < 3; j++) k78[kst(dp + j - i, e)] = Kab[3 * i + j];
         } else {
-          for (int j = 0; j < 3; j++) k78[(size_t)(dp + 3 * b + j - p) * ne + e] = Kab[3 * i + j];
+          for (int j = 0; j < 3; j++) k78[kst(dp + 3 * b + j - p, e)] = Kab[3 * i + j];
         }
       }
     }
