@@ -468,7 +468,7 @@ __device__ __forceinline__ void invhyper_elem(int e, int ne, int stvk, const int
       for (int k = 0; k < 3; k++) F[j * 3 + k] += ax[j] * pre[(size_t)(12 + (i - 1) * 3 + k) * ne + e];
   }
   double sig[3], U[9], VT[9];
-  invertible_svd<double>(F, thr, sig, U, VT);
+  invertible_svd<double, DF>(F, thr, sig, U, VT);
   const double s02 = sig[0] * sig[0], s12 = sig[1] * sig[1], s22 = sig[2] * sig[2];
   const double I1 = s02 + s12 + s22, I3 = s02 * s12 * s22;
   double g0, g1, g2, h0 = 0.0, h5 = 0.0;

@@ -54,7 +54,13 @@ template <class FT> __device__ __forceinline__ void mul3(const FT* a, const FT* 
 // Symmetric 3x3 eigen-decomposition, eigenvectors as rows
 // (eigenSym3x3, core/numerMethod.h:327-429): trigonometric root for the
 // first eigenvalue, then a 2x2 problem on its orthogonal complement.
-template <class FT>
+// REFINE (FT = double): the trigonometric root in FP32, then two Newton
+// steps on the deviator's characteristic polynomial l^3 - J2 l - J3 (the
+// chosen root is the one of largest magnitude, where the derivative
+// 3 l^2 - J2 is at least 2 J2, so the FP32 start's ~1e-7 error falls below
+// FP64 rounding); FP64 transcendental functions are long instruction
+// sequences on the FP64 pipe.
+template <class FT, bool REFINE = false>
 __device__ void eig_sym3(const FT* t, FT* vals, FT* vecs) {
   const FT pi = FT(3.141592653589793238462643383279502884);
   const FT s3 = FT(1.7320508075688772935274463415058723669428);
@@ -71,8 +77,19 @@ __device__ void eig_sym3(const FT* t, FT* vals, FT* vecs) {
     vecs[0] = vecs[4] = vecs[8] = FT(1);
     return;
   }
-  FT ang = acos(clampv(cs, FT(-1), FT(1))) / FT(3);
-  FT e0 = (FT(2) / s3) * sq * (ang < pi / FT(6) ? cos(ang) : cos(ang + (FT(2) / FT(3)) * pi));
+  FT e0;
+  if constexpr (REFINE) {
+    const float pif = 3.14159265358979f;
+    const float angf = acosf((float)clampv(cs, FT(-1), FT(1))) / 3.f;
+    const float cf = angf < pif / 6.f ? cosf(angf) : cosf(angf + (2.f / 3.f) * pif);
+    e0 = (FT(2) / s3) * sq * (FT)cf;
+    const FT rdp = FT(1) / (FT(3) * e0 * e0 - J2);
+    e0 -= ((e0 * e0 - J2) * e0 - J3) * rdp;
+    e0 -= ((e0 * e0 - J2) * e0 - J3) * rdp;
+  } else {
+    FT ang = acos(clampv(cs, FT(-1), FT(1))) / FT(3);
+    e0 = (FT(2) / s3) * sq * (ang < pi / FT(6) ? cos(ang) : cos(ang + (FT(2) / FT(3)) * pi));
+  }
   vals[0] = e0 + ave;
   V3t<FT> r0 = {d0 - e0, t[1], t[2]}, r1 = {t[1], d1 - e0, t[4]}, r2 = {t[2], t[4], d2 - e0};
   FT l0 = sqrt(v_len2(r0)), l1 = sqrt(v_len2(r1)), l2 = sqrt(v_len2(r2));
@@ -508,7 +525,7 @@ __device__ __forceinline__ void coord_system(V3t<FT> v0, V3t<FT>& v1, V3t<FT>& v
 // U from eig(F F^T) made a rotation; V^T = U^T F / sigma with rank-deficient
 // rows completed by cross products; the smallest sigma negated when det V < 0;
 // sigma clamped below by thr.  Outputs U (row-major), VT, sigma.
-template <class FT>
+template <class FT, bool REFINE = false>
 __device__ void invertible_svd(const FT* F, FT thr, FT* sig, FT* U, FT* VT) {
   FT tri[6], ev[3], UT[9];
   tri[0] = F[0] * F[0] + F[1] * F[1] + F[2] * F[2];
@@ -517,7 +534,7 @@ __device__ void invertible_svd(const FT* F, FT thr, FT* sig, FT* U, FT* VT) {
   tri[3] = F[3] * F[3] + F[4] * F[4] + F[5] * F[5];
   tri[4] = F[6] * F[3] + F[7] * F[4] + F[8] * F[5];
   tri[5] = F[6] * F[6] + F[7] * F[7] + F[8] * F[8];
-  eig_sym3(tri, ev, UT);
+  eig_sym3<FT, REFINE>(tri, ev, UT);
   if (det3(UT) < FT(0)) { UT[0] = -UT[0]; UT[1] = -UT[1]; UT[2] = -UT[2]; }
 #pragma unroll
   for (int i = 0; i < 3; i++) ev[i] = ev[i] > FT(0) ? sqrt(ev[i]) : FT(0);

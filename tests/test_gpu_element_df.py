@@ -1,11 +1,16 @@
-"""The mixed-precision path's double-float stiffness contraction (FP32
-pairs, operands split and results rebuilt with integer bit operations)
-against the exact FP64 one, on displaced meshes: every assembled stiffness
-value within 1e-12 of the largest (the FP32 rounding of a plain FP32
-contraction was 5.7e-8).  The invertible elements' internal forces stay FP64
-and equal bit for bit; the corotational element's are the reference's sum
-regrouped in FP64 (R sum_b K0_ab (R^T x_b - X_b)), within 1e-12 of the
-largest."""
+"""The mixed-precision path's element evaluation against the FP64 one, on
+displaced meshes up to inverted elements.  Stiffness: the double-float
+contraction (FP32 pairs, operands split and results rebuilt with integer
+bit operations; a plain FP32 contraction was 5.7e-8 of the largest value
+off).  Forces: the
+invertible elements' stay FP64, their SVD's first eigenvalue taken from
+FP32 trigonometry and refined by Newton steps; the corotational element's
+are the reference's sum regrouped in FP64 (R sum_b K0_ab (R^T x_b - X_b)).
+The corotational values within 1e-12 of the largest.  The invertible
+elements' values within 1e-10: the refined eigenvalue can differ from the
+FP64 trigonometric one by an ulp, and where two singular values nearly
+coincide the eigenvectors turn by about ulp / gap (up to 1.4e-11 of the
+largest stiffness value on these meshes; typical entries 1e-15)."""
 import os
 
 import numpy as np
@@ -30,7 +35,7 @@ def evaluate(s, df):
 
 
 @pytest.mark.parametrize("kind", ["neohookean", "stvk", "corotational"])
-@pytest.mark.parametrize("scale", [0.002, 0.02])
+@pytest.mark.parametrize("scale", [0.002, 0.02, 0.2])
 def test_double_float_contraction_matches_fp64(kind, scale):
     g = meshgen.tet_grid(10, 4, 4, h=0.05, jitter=0.15, seed=21)
     cd = meshgen.constrained_dofs_for_nodes(g.face_nodes(0, 0))
@@ -43,10 +48,8 @@ def test_double_float_contraction_matches_fp64(kind, scale):
     k64, f64 = evaluate(s, False)
     kdf, fdf = evaluate(s, True)
     s.close()
+    bound = 1e-12 if kind == "corotational" else 1e-10
     assert np.abs(k64).max() > 0
-    assert np.abs(kdf - k64).max() <= 1e-12 * np.abs(k64).max()
-    if kind == "corotational":
-        assert np.abs(f64).max() > 0
-        assert np.abs(fdf - f64).max() <= 1e-12 * np.abs(f64).max()
-    else:
-        assert np.array_equal(fdf, f64)
+    assert np.abs(kdf - k64).max() <= bound * np.abs(k64).max()
+    assert np.abs(f64).max() > 0
+    assert np.abs(fdf - f64).max() <= bound * np.abs(f64).max()
