@@ -160,8 +160,10 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def traffic_from_profiles(workload, kernel):
-    """Per-launch DRAM bytes of a kernel from the committed ncu summary."""
+def traffic_from_profiles(workload, kernel, field=None):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary, or
+    with field="fp64_pipe_pct" that capture's FP64 pipe activity (a
+    "fp64_pipe_pct=<value>" entry on the same line)."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     if not os.path.exists(path):
         return None
@@ -169,7 +171,12 @@ def traffic_from_profiles(workload, kernel):
         for line in f:
             parts = line.split()
             if len(parts) >= 3 and parts[0] == workload and parts[1] == kernel:
-                return float(parts[2])
+                if field is None:
+                    return float(parts[2])
+                for p in parts[3:]:
+                    if p.startswith(field + "="):
+                        return float(p.split("=", 1)[1])
+                return None
     return None
 
 
@@ -1269,7 +1276,7 @@ def run_gpu(args, wl):
                 "fma_per_launch": fmas,
                 "peak_fma_per_sm_per_cycle": fma64 / (torch.cuda.get_device_properties(local_rank).multi_processor_count * sm_mhz * 1e6),
                 "fp32_peak_gflops": 2.0 * fma32 / 1e9,
-                "pipe_active_pct_ncu": 43.8,
+                "pipe_active_pct_ncu": traffic_from_profiles(args.workload, tkey, "fp64_pipe_pct"),
                 "pipe_source": "ncu --set full capture of this kernel on this workload "
                                "(sm__pipe_fp64_cycles_active, of peak, active cycles)"}
     phases = None

@@ -475,8 +475,14 @@ __device__ __forceinline__ void invhyper_elem(int e, int ne, int stvk, const int
   if (!stvk) {
     g0 = 0.5 * mu;
     g1 = 0.0;
-    g2 = (-0.5 * mu + 0.25 * lambda * log(I3)) / I3;
-    h5 = (0.5 * mu + 0.25 * lambda * (1.0 - log(I3))) / (I3 * I3);
+    if constexpr (DF) {   // one reciprocal of I3 for both
+      const double lI3 = log(I3), rI3 = 1.0 / I3;
+      g2 = (-0.5 * mu + 0.25 * lambda * lI3) * rI3;
+      h5 = (0.5 * mu + 0.25 * lambda * (1.0 - lI3)) * (rI3 * rI3);
+    } else {
+      g2 = (-0.5 * mu + 0.25 * lambda * log(I3)) / I3;
+      h5 = (0.5 * mu + 0.25 * lambda * (1.0 - log(I3))) / (I3 * I3);
+    }
   } else {
     g0 = 0.25 * lambda * (I1 - 3.0) - 0.5 * mu;
     g1 = 0.25 * mu;
@@ -491,8 +497,8 @@ __device__ __forceinline__ void invhyper_elem(int e, int ne, int stvk, const int
   const double a00 = 2.0 * g0 + 8.0 * s02 * g1, a11 = 2.0 * g0 + 8.0 * s12 * g1, a22 = 2.0 * g0 + 8.0 * s22 * g1;
   // d_ij = I3 g2 / (s_i s_j); the mixed path forms them as products
   // (I3 / (s_i s_j) is the product of the other factors: FP64 divisions are
-  // long instruction sequences on this part).  The forces keep the exact
-  // expressions.
+  // long instruction sequences on this part), and so its forces' I3 / s_i;
+  // the FP64 path keeps the reference's expressions.
   const double d00 = DF ? g2 * (s12 * s22) : I3 * g2 / s02, d01 = DF ? g2 * (sc01 * s22) : I3 * g2 / sc01,
                d02 = DF ? g2 * (sc02 * s12) : I3 * g2 / sc02;
   const double d11 = DF ? g2 * (s02 * s22) : I3 * g2 / s12, d12 = DF ? g2 * (sc12 * s02) : I3 * g2 / sc12,
@@ -523,7 +529,14 @@ __device__ __forceinline__ void invhyper_elem(int e, int ne, int stvk, const int
   // P = U diag(de) V^T
   double de[3], P[9];
 #pragma unroll
-  for (int i = 0; i < 3; i++) de[i] = 2.0 * g0 * sig[i] + 4.0 * g1 * sig[i] * sig[i] * sig[i] + 2.0 * g2 * I3 / sig[i];
+  for (int i = 0; i < 3; i++) {
+    if constexpr (DF) {   // I3 / s_i as the product s_i s_j^2 s_k^2
+      const double i3s = sig[i] * (i == 0 ? s12 * s22 : (i == 1 ? s02 * s22 : s02 * s12));
+      de[i] = 2.0 * g0 * sig[i] + 4.0 * g1 * sig[i] * sig[i] * sig[i] + 2.0 * g2 * i3s;
+    } else {
+      de[i] = 2.0 * g0 * sig[i] + 4.0 * g1 * sig[i] * sig[i] * sig[i] + 2.0 * g2 * I3 / sig[i];
+    }
+  }
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll

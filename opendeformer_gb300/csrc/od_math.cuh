@@ -64,12 +64,14 @@ template <class FT, bool REFINE = false>
 __device__ void eig_sym3(const FT* t, FT* vals, FT* vecs) {
   const FT pi = FT(3.141592653589793238462643383279502884);
   const FT s3 = FT(1.7320508075688772935274463415058723669428);
-  const FT ave = (t[0] + t[3] + t[5]) / FT(3);
+  // REFINE: fewer FP64 divisions and square roots below (a product by a
+  // reciprocal, one root per normalised vector): the same values to an ulp
+  const FT ave = REFINE ? (t[0] + t[3] + t[5]) * FT(1.0 / 3.0) : (t[0] + t[3] + t[5]) / FT(3);
   const FT d0 = t[0] - ave, d1 = t[3] - ave, d2 = t[5] - ave;
   const FT J2 = (d0 * d0 + d1 * d1 + d2 * d2) * FT(0.5) + t[1] * t[1] + t[2] * t[2] + t[4] * t[4];
   const FT J3 = d0 * (d1 * d2 - t[4] * t[4]) + t[1] * (t[4] * t[2] - t[1] * d2) + t[2] * (t[1] * t[4] - d1 * t[2]);
   const FT sq = sqrt(J2);
-  const FT cs = (FT(3) * FT(0.5) * s3) * ((J3 / J2) / sq);
+  const FT cs = REFINE ? (FT(3) * FT(0.5) * s3) * (J3 / (J2 * sq)) : (FT(3) * FT(0.5) * s3) * ((J3 / J2) / sq);
   if (isnan(cs) || isinf(cs)) {
     vals[0] = vals[1] = vals[2] = ave;
 #pragma unroll
@@ -92,17 +94,25 @@ __device__ void eig_sym3(const FT* t, FT* vals, FT* vecs) {
   }
   vals[0] = e0 + ave;
   V3t<FT> r0 = {d0 - e0, t[1], t[2]}, r1 = {t[1], d1 - e0, t[4]}, r2 = {t[2], t[4], d2 - e0};
-  FT l0 = sqrt(v_len2(r0)), l1 = sqrt(v_len2(r1)), l2 = sqrt(v_len2(r2));
+  // REFINE: the same choices on squared lengths, one reciprocal root
+  auto unit = [&](V3t<FT> v, FT len2) { return REFINE ? v_scale(v, rsqrt(len2)) : v_div(v, sqrt(len2)); };
+  FT l0 = v_len2(r0), l1 = v_len2(r1), l2 = v_len2(r2);
+  if constexpr (!REFINE) {
+    l0 = sqrt(l0);
+    l1 = sqrt(l1);
+    l2 = sqrt(l2);
+  }
+  auto norm0 = [&](V3t<FT> v, FT l) { return REFINE ? v_scale(v, rsqrt(l)) : v_div(v, l); };
   V3t<FT> s0, t1, t2;
   if (l0 > l1) {
-    if (l0 > l2) { s0 = v_div(r0, l0); t1 = v_sub(r1, v_scale(s0, v_dot(s0, r1))); t2 = v_sub(r2, v_scale(s0, v_dot(s0, r2))); }
-    else { s0 = v_div(r2, l2); t1 = v_sub(r0, v_scale(s0, v_dot(s0, r0))); t2 = v_sub(r1, v_scale(s0, v_dot(s0, r1))); }
+    if (l0 > l2) { s0 = norm0(r0, l0); t1 = v_sub(r1, v_scale(s0, v_dot(s0, r1))); t2 = v_sub(r2, v_scale(s0, v_dot(s0, r2))); }
+    else { s0 = norm0(r2, l2); t1 = v_sub(r0, v_scale(s0, v_dot(s0, r0))); t2 = v_sub(r1, v_scale(s0, v_dot(s0, r1))); }
   } else {
-    if (l1 > l2) { s0 = v_div(r1, l1); t1 = v_sub(r0, v_scale(s0, v_dot(s0, r0))); t2 = v_sub(r2, v_scale(s0, v_dot(s0, r2))); }
-    else { s0 = v_div(r2, l2); t1 = v_sub(r0, v_scale(s0, v_dot(s0, r0))); t2 = v_sub(r1, v_scale(s0, v_dot(s0, r1))); }
+    if (l1 > l2) { s0 = norm0(r1, l1); t1 = v_sub(r0, v_scale(s0, v_dot(s0, r0))); t2 = v_sub(r2, v_scale(s0, v_dot(s0, r2))); }
+    else { s0 = norm0(r2, l2); t1 = v_sub(r0, v_scale(s0, v_dot(s0, r0))); t2 = v_sub(r1, v_scale(s0, v_dot(s0, r1))); }
   }
   FT t1l = v_len2(t1), t2l = v_len2(t2);
-  V3t<FT> s1 = t1l > t2l ? v_div(t1, sqrt(t1l)) : v_div(t2, sqrt(t2l));
+  V3t<FT> s1 = t1l > t2l ? unit(t1, t1l) : unit(t2, t2l);
   V3t<FT> ev0 = v_cross(s0, s1);
   vecs[0] = ev0.x; vecs[1] = ev0.y; vecs[2] = ev0.z;
   auto mulm = [&](V3t<FT> v) {
@@ -118,7 +128,7 @@ __device__ void eig_sym3(const FT* t, FT* vals, FT* vecs) {
   V3t<FT> u0 = v_cross(v_sub(m0, v_scale(s0, e1)), ev0);
   V3t<FT> u1 = v_cross(v_sub(m1, v_scale(s1, e1)), ev0);
   FT u0l = v_len2(u0), u1l = v_len2(u1);
-  V3t<FT> ev1 = (u0l != FT(0)) ? (u0l > u1l ? v_div(u0, sqrt(u0l)) : v_div(u1, sqrt(u1l))) : s0;
+  V3t<FT> ev1 = (u0l != FT(0)) ? (u0l > u1l ? unit(u0, u0l) : unit(u1, u1l)) : s0;
   vecs[3] = ev1.x; vecs[4] = ev1.y; vecs[5] = ev1.z;
   V3t<FT> ev2 = v_cross(ev0, ev1);
   vecs[6] = ev2.x; vecs[7] = ev2.y; vecs[8] = ev2.z;
@@ -536,8 +546,18 @@ __device__ void invertible_svd(const FT* F, FT thr, FT* sig, FT* U, FT* VT) {
   tri[5] = F[6] * F[6] + F[7] * F[7] + F[8] * F[8];
   eig_sym3<FT, REFINE>(tri, ev, UT);
   if (det3(UT) < FT(0)) { UT[0] = -UT[0]; UT[1] = -UT[1]; UT[2] = -UT[2]; }
+  // REFINE: sigma = x rsqrt(x), and rsqrt(x) is 1 / sigma for the row scaling
+  FT rs[3];
 #pragma unroll
-  for (int i = 0; i < 3; i++) ev[i] = ev[i] > FT(0) ? sqrt(ev[i]) : FT(0);
+  for (int i = 0; i < 3; i++) {
+    if constexpr (REFINE) {
+      rs[i] = ev[i] > FT(0) ? rsqrt(ev[i]) : FT(0);
+      ev[i] = ev[i] > FT(0) ? ev[i] * rs[i] : FT(0);
+    } else {
+      ev[i] = ev[i] > FT(0) ? sqrt(ev[i]) : FT(0);
+    }
+  }
+  auto inv = [&](int i) { return REFINE ? rs[i] : FT(1) / ev[i]; };
   mul3(UT, F, VT);
   const FT eps = FT(1e-8);
   const int cond = (ev[0] < eps) + ((ev[1] < eps) << 1) + ((ev[2] < eps) << 2);
@@ -546,7 +566,7 @@ __device__ void invertible_svd(const FT* F, FT thr, FT* sig, FT* U, FT* VT) {
   auto scalerow = [&](int r, FT f) { VT[3 * r] *= f; VT[3 * r + 1] *= f; VT[3 * r + 2] *= f; };
   switch (cond) {
     case 0: {
-      scalerow(0, FT(1) / ev[0]); scalerow(1, FT(1) / ev[1]); scalerow(2, FT(1) / ev[2]);
+      scalerow(0, inv(0)); scalerow(1, inv(1)); scalerow(2, inv(2));
       if (det3(VT) < FT(0)) {
         int sm = ev[0] < ev[1] ? (ev[0] < ev[2] ? 0 : 2) : (ev[1] < ev[2] ? 1 : 2);
         scalerow(sm, FT(-1));
@@ -554,12 +574,12 @@ __device__ void invertible_svd(const FT* F, FT thr, FT* sig, FT* U, FT* VT) {
       }
       break;
     }
-    case 1: scalerow(1, FT(1) / ev[1]); scalerow(2, FT(1) / ev[2]); setrow(0, v_cross(row(1), row(2))); break;
-    case 2: scalerow(0, FT(1) / ev[0]); scalerow(2, FT(1) / ev[2]); setrow(1, v_cross(row(2), row(0))); break;
-    case 3: { scalerow(2, FT(1) / ev[2]); V3t<FT> a, c; coord_system(row(2), a, c); setrow(0, a); setrow(1, c); break; }
-    case 4: scalerow(0, FT(1) / ev[0]); scalerow(1, FT(1) / ev[1]); setrow(2, v_cross(row(0), row(1))); break;
-    case 5: { scalerow(1, FT(1) / ev[1]); V3t<FT> a, c; coord_system(row(1), a, c); setrow(2, a); setrow(0, c); break; }
-    case 6: { scalerow(0, FT(1) / ev[0]); V3t<FT> a, c; coord_system(row(0), a, c); setrow(1, a); setrow(2, c); break; }
+    case 1: scalerow(1, inv(1)); scalerow(2, inv(2)); setrow(0, v_cross(row(1), row(2))); break;
+    case 2: scalerow(0, inv(0)); scalerow(2, inv(2)); setrow(1, v_cross(row(2), row(0))); break;
+    case 3: { scalerow(2, inv(2)); V3t<FT> a, c; coord_system(row(2), a, c); setrow(0, a); setrow(1, c); break; }
+    case 4: scalerow(0, inv(0)); scalerow(1, inv(1)); setrow(2, v_cross(row(0), row(1))); break;
+    case 5: { scalerow(1, inv(1)); V3t<FT> a, c; coord_system(row(1), a, c); setrow(2, a); setrow(0, c); break; }
+    case 6: { scalerow(0, inv(0)); V3t<FT> a, c; coord_system(row(0), a, c); setrow(1, a); setrow(2, c); break; }
     default:
 #pragma unroll
       for (int i = 0; i < 9; i++) VT[i] = FT(0);
