@@ -508,8 +508,8 @@ od_status od_server_get_stats(od_server* server, od_server_stats* out);
  * returned, when max_iter ran out).  The array is shared: calls that overlap
  * on the GPU race, so callers serialise them.  The first call on a device
  * looks up the array's device address and keeps it for the process (a
- * cudaDeviceReset after it is not supported); make that first call before
- * any stream capture.  stream is a cudaStream_t (NULL: the default stream). */
+ * cudaDeviceReset after it is not supported).  stream is a cudaStream_t
+ * (NULL: the default stream). */
 #define OD_NOALLOC_MAX_BLOCK_ROWS 32768
 od_status od_bsr_pcg_noalloc(int nb, const int* d_row_ptr, const int* d_col, const double* d_values,
                              const double* d_b, double* d_x, const od_solver_params* params,

@@ -19,10 +19,8 @@
 // Host code must not pass g_pcg_scratch itself to a kernel (in host code the
 // name is a host-side stand-in, not a device address).  The device address
 // is looked up with cudaGetSymbolAddress once per device, on the first call
-// made with that device current; that first call should therefore come
-// before any stream capture.  The address is kept for the life of the
-// process: a cudaDeviceReset of that device after the first call is not
-// supported.
+// made with that device current, and kept for the life of the process: a
+// cudaDeviceReset of that device after the first call is not supported.
 //
 // The matrix comes from the caller, so the first kernel checks it before
 // any other reads it: a row pointer that does not start at 0 or decreases,
