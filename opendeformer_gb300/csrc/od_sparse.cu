@@ -1407,6 +1407,10 @@ __device__ __forceinline__ bool ring_sums(RingShared& sh, int L, int sc_lo, int 
     for (int ls = 0; ls < L; ls++) {
       const int s = sc_lo + ls;
       const int c0 = sh.c0[ls], c1 = sh.c1[ls];
+      // a scene that lives in this CTA alone (every local scene but the
+      // first and the last can): its sums are the CTA's own partials, which
+      // res holds already -- the same values the loads below would add up
+      if (c0 == c1) continue;
       double acc[NV];
 #pragma unroll
       for (int j = 0; j < NV; j++) acc[j] = 0.0;
