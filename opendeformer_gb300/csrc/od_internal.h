@@ -358,8 +358,8 @@ struct Scene {
   double* fint = nullptr;
   double* fext = nullptr;
   double* work_vals = nullptr;     // host-supplied values (SpMDV / PCG drop-in)
-  double* stage_k = nullptr;       // SoA [78][n_tets] element stiffness (colour order)
-  double* stage_f = nullptr;       // SoA [12][n_tets] element forces
+  double* stage_k = nullptr;       // [n_tets][78] element stiffness, node blocks contiguous (c_kslot; colour order)
+  double* stage_f = nullptr;       // [n_tets][12] element forces
   FullBsr bsr;
   void* A = nullptr;               // full BSR values (double or float)
   double* A64 = nullptr;           // FP64 full values
